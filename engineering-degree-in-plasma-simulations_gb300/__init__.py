@@ -1,0 +1,414 @@
+"""GB300-native electrostatic PIC + DSMC step loop (host mirror over the C ABI).
+
+Python mirror of the reference's ch4/v3 class surface (Misquic/Engineering-degree-in-Plasma-
+Simulations): World, Species, PotentialSolver and MC_MEX_Ionization, with the same method
+names where the reference has them.  Every call goes through include/pic_gb300.h into
+lib/libpic_gb300.so (hand-written sm_103a kernels).  There is no CPU fallback: if the
+library or a CUDA device is missing, construction raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "lib", "libpic_gb300.so")
+
+PIC_OK, PIC_ERR_ARG, PIC_ERR_CUDA, PIC_ERR_NOT_CONVERGED, PIC_ERR_CAPACITY, PIC_ERR_DEVICE = range(6)
+SOLVER_RBSOR, SOLVER_PCG = 0, 1
+GS, PCG = SOLVER_RBSOR, SOLVER_PCG  # reference SolverType names (PotentialSolver.h:24)
+
+# ch4/v3/src/all.h:16-25
+EPS0 = 8.85418782e-12
+QE = 1.602176565e-19
+AMU = 1.660538921e-27
+ME = 9.10938215e-31
+KB = 1.380648e-23
+
+PARTICLE = np.dtype([("pos", "<f8", 3), ("vel", "<f8", 3), ("w", "<f8"), ("id", "<u8")])
+
+
+class PicError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def build():
+    from . import build as _b  # noqa: F401  (package-relative build recipe)
+
+    return _b.build()
+
+
+def library():
+    """Load the CUDA library (building it first when the sources are newer)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    import importlib
+
+    importlib.import_module(__name__ + ".build").build()  # incremental: rebuilds only stale objects
+    L = C.CDLL(LIB_PATH)
+    vp, i, d, l, u64 = C.c_void_p, C.c_int, C.c_double, C.c_long, C.c_uint64
+    pvp = C.POINTER(C.c_void_p)
+    sig = {
+        "pic_world_create": [pvp, i, i, i, vp, vp, i],
+        "pic_world_destroy": [vp],
+        "pic_world_set_time": [vp, d, i],
+        "pic_world_advance_time": [vp, vp],
+        "pic_world_get_ts": [vp, vp],
+        "pic_world_set_boundaries": [vp, vp, vp, vp],
+        "pic_world_add_box": [vp, vp, vp, d],
+        "pic_world_get_field": [vp, i, vp],
+        "pic_world_set_field": [vp, i, vp],
+        "pic_species_create": [vp, C.c_char_p, d, d, d, l, d, vp],
+        "pic_species_add_particles": [vp, i, vp, vp, vp, vp, l, i],
+        "pic_species_load_uniform": [vp, i, vp, vp, l, d, d, d, u64],
+        "pic_species_count": [vp, i, vp],
+        "pic_species_get_particles": [vp, i, vp, vp, vp, vp, l, vp],
+        "pic_species_push": [vp, i, d, i],
+        "pic_species_number_density": [vp, i],
+        "pic_species_get_den": [vp, i, vp],
+        "pic_species_update_averages": [vp, i],
+        "pic_species_get_den_avg": [vp, i, vp],
+        "pic_species_sort": [vp, i, vp],
+        "pic_species_sums": [vp, i, vp],
+        "pic_charge_density": [vp],
+        "pic_solver_configure": [vp, i, d, i, d],
+        "pic_solver_solve": [vp, vp, vp],
+        "pic_solver_compute_ef": [vp],
+        "pic_solver_stats": [vp, vp, vp, vp],
+        "pic_mcc_create": [vp, i, i, d, d, d, d, d, i, vp, vp, vp, i, u64],
+        "pic_mcc_apply": [vp, d],
+        "pic_mcc_stats": [vp, vp],
+        "pic_loop_configure": [vp, i, i, vp, i, i, i],
+        "pic_step": [vp],
+        "pic_species_merge": [vp, i, i],
+        "pic_synchronize": [vp],
+        "pic_last_error": [C.c_char_p, i],
+        "pic_timing_enable": [vp, i],
+        "pic_timing_read": [vp, C.c_char_p, vp, vp],
+        "pic_timing_reset": [vp],
+        "pic_launch_count": [vp, vp],
+        "pic_world_stream": [vp, pvp],
+    }
+    for name, args in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = C.c_int
+    _lib = L
+    return L
+
+
+def _check(rc, allow=()):
+    if rc != PIC_OK and rc not in allow:
+        buf = C.create_string_buffer(512)
+        library().pic_last_error(buf, 512)
+        raise PicError(rc, buf.value.decode(errors="replace"))
+    return rc
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _f64(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a if shape is None else a.reshape(shape)
+
+
+class World:
+    """World(ni, nj, nk, x0, xm) -- ch4/v3/src/World.h:15-116 on one GPU."""
+
+    def __init__(self, ni, nj, nk, x0, xm, device=0):
+        self._L = library()
+        h = C.c_void_p()
+        _check(self._L.pic_world_create(C.byref(h), int(ni), int(nj), int(nk), _p(_f64(x0)), _p(_f64(xm)),
+                                        int(device)))
+        self._h = h
+        self.ni, self.nj, self.nk = int(ni), int(nj), int(nk)
+        self.nn = (self.ni, self.nj, self.nk)
+        self.nv = self.ni * self.nj * self.nk
+        self.num_cells = (self.ni - 1) * (self.nj - 1) * (self.nk - 1)
+        self.x0 = np.asarray(x0, np.float64)
+        self.xm = np.asarray(xm, np.float64)
+        self.dx = (self.xm - self.x0) / (np.asarray(self.nn) - 1)
+        self.species = []
+        self.periodic = (0, 0, 0)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.pic_world_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    # time (World.cpp:321-349)
+    def setTime(self, dt, num_ts):
+        _check(self._L.pic_world_set_time(self._h, float(dt), int(num_ts)))
+        self.dt = float(dt)
+
+    def advanceTime(self):
+        r = C.c_int()
+        _check(self._L.pic_world_advance_time(self._h, C.byref(r)))
+        return bool(r.value)
+
+    def getTs(self):
+        t = C.c_int()
+        _check(self._L.pic_world_get_ts(self._h, C.byref(t)))
+        return t.value
+
+    def getDx(self):
+        return self.dx.copy()
+
+    def getCellVolume(self):
+        return float(np.prod(self.dx))
+
+    # boundaries
+    def set_boundaries(self, periodic=(0, 0, 0), face_mode=(0,) * 6, face_phi=(0.0,) * 6):
+        self.periodic = tuple(int(p) for p in periodic)
+        _check(self._L.pic_world_set_boundaries(self._h, _p(np.asarray(periodic, np.int32)),
+                                                _p(np.asarray(face_mode, np.int32)), _p(_f64(face_phi))))
+
+    def dirichletBoundries(self, phi=0.0):
+        """All walls Dirichlet at phi (World::dirichletBoundries, World.cpp:263-274)."""
+        self.set_boundaries((0, 0, 0), (1,) * 6, (phi,) * 6)
+
+    def addBox(self, center, sides, phi):
+        """World::addObject<Rectangle>(pos, phi, sides) + computeObjectID."""
+        _check(self._L.pic_world_add_box(self._h, _p(_f64(center)), _p(_f64(sides)), float(phi)))
+
+    # fields
+    def _get(self, which, comps=1):
+        out = np.zeros(self.nv * comps)
+        _check(self._L.pic_world_get_field(self._h, which, _p(out)))
+        return out if comps == 1 else out.reshape(self.nv, comps)
+
+    @property
+    def phi(self):
+        return self._get(0)
+
+    @phi.setter
+    def phi(self, v):
+        _check(self._L.pic_world_set_field(self._h, 0, _p(_f64(v))))
+
+    @property
+    def rho(self):
+        return self._get(1)
+
+    @rho.setter
+    def rho(self, v):
+        _check(self._L.pic_world_set_field(self._h, 1, _p(_f64(v))))
+
+    @property
+    def node_vol(self):
+        return self._get(2)
+
+    @property
+    def ef(self):
+        return self._get(3, 3)
+
+    @ef.setter
+    def ef(self, v):
+        _check(self._L.pic_world_set_field(self._h, 3, _p(_f64(v))))
+
+    def computeChargeDensity(self, species=None):
+        """World::computeChargeDensity (World.cpp:193-200): den_s and rho = sum q_s den_s."""
+        _check(self._L.pic_charge_density(self._h))
+
+    # loop (main.cpp:177-286)
+    def configure_loop(self, solve_each_step=True, sort_every=20, subcycle=(1, 1, 1, 1), merge_every=0,
+                       merge_after=0, merge_min=10):
+        _check(self._L.pic_loop_configure(self._h, int(solve_each_step), int(sort_every),
+                                          _p(np.asarray(list(subcycle) + [1] * (4 - len(subcycle)), np.int32)),
+                                          int(merge_every), int(merge_after), int(merge_min)))
+
+    def step(self):
+        _check(self._L.pic_step(self._h))
+
+    def synchronize(self):
+        _check(self._L.pic_synchronize(self._h))
+
+    # measurement
+    def timing(self, on=True):
+        _check(self._L.pic_timing_enable(self._h, int(on)))
+
+    def timer(self, name):
+        ms, n = C.c_double(), C.c_long()
+        _check(self._L.pic_timing_read(self._h, name.encode(), C.byref(ms), C.byref(n)))
+        return ms.value, n.value
+
+    def timing_reset(self):
+        _check(self._L.pic_timing_reset(self._h))
+
+    def launches(self):
+        n = C.c_long()
+        _check(self._L.pic_launch_count(self._h, C.byref(n)))
+        return n.value
+
+
+class Species:
+    """Species(name, mass, charge, world, mpw0) -- ch4/v3/src/Species.h:31-133, particles on the GPU."""
+
+    def __init__(self, name, mass, charge, world, mpw0, capacity=1 << 20, weight_bound=0.0):
+        self.world = world
+        self.name, self.mass, self.charge, self.mpw0 = name, float(mass), float(charge), float(mpw0)
+        self.capacity = int(capacity)
+        sid = C.c_int()
+        _check(world._L.pic_species_create(world._h, name.encode(), self.mass, self.charge, self.mpw0,
+                                           self.capacity, float(weight_bound), C.byref(sid)))
+        self.id = sid.value
+        world.species.append(self)
+
+    @property
+    def _L(self):
+        return self.world._L
+
+    def addParticles(self, pos, vel, w, ids=None, rewind=True):
+        """Species::addParticle for arrays (Species.cpp:420-434)."""
+        pos = _f64(pos, (-1, 3))
+        vel = _f64(vel, (-1, 3))
+        w = _f64(w, (-1,))
+        idp = None if ids is None else np.ascontiguousarray(ids, np.uint64)
+        _check(self._L.pic_species_add_particles(self.world._h, self.id, _p(pos), _p(vel), _p(w), _p(idp), len(w),
+                                                 int(rewind)))
+
+    def addParticle(self, pos, vel, macro_weight=None):
+        self.addParticles([pos], [vel], [self.mpw0 if macro_weight is None else macro_weight])
+
+    def loadUniform(self, lo, hi, n, T, w_mean=None, w_sigma=0.0, seed=1):
+        _check(self._L.pic_species_load_uniform(self.world._h, self.id, _p(_f64(lo)), _p(_f64(hi)), int(n), float(T),
+                                                float(self.mpw0 if w_mean is None else w_mean), float(w_sigma),
+                                                int(seed)))
+
+    def getNumParticles(self):
+        n = C.c_long()
+        _check(self._L.pic_species_count(self.world._h, self.id, C.byref(n)))
+        return n.value
+
+    def getPartRef(self):
+        """Host copy of the particles (Species::getPartRef, Species.cpp:823-825)."""
+        n = self.getNumParticles()
+        pos = np.zeros((max(n, 1), 3))
+        vel = np.zeros((max(n, 1), 3))
+        w = np.zeros(max(n, 1))
+        ids = np.zeros(max(n, 1), np.uint64)
+        got = C.c_long()
+        _check(self._L.pic_species_get_particles(self.world._h, self.id, _p(pos), _p(vel), _p(w), _p(ids), max(n, 1),
+                                                 C.byref(got)))
+        n = got.value
+        out = np.zeros(n, PARTICLE)
+        out["pos"], out["vel"], out["w"], out["id"] = pos[:n], vel[:n], w[:n], ids[:n]
+        return out
+
+    def advance(self, dt, deposit=True):
+        _check(self._L.pic_species_push(self.world._h, self.id, float(dt), int(deposit)))
+
+    advanceElectrons = advance  # Species.cpp:258
+
+    def advanceNonElectron(self, neutrals, spherium, dt, deposit=True):  # Species.cpp:47
+        self.advance(dt, deposit)
+
+    def computeNumberDensity(self):
+        _check(self._L.pic_species_number_density(self.world._h, self.id))
+
+    @property
+    def den(self):
+        out = np.zeros(self.world.nv)
+        _check(self._L.pic_species_get_den(self.world._h, self.id, _p(out)))
+        return out
+
+    @property
+    def den_avg(self):
+        out = np.zeros(self.world.nv)
+        _check(self._L.pic_species_get_den_avg(self.world._h, self.id, _p(out)))
+        return out
+
+    def updateAverages(self):
+        _check(self._L.pic_species_update_averages(self.world._h, self.id))
+
+    def sortIndexes(self, counts=False):
+        buf = np.zeros(self.world.num_cells, np.int32) if counts else None
+        _check(self._L.pic_species_sort(self.world._h, self.id, _p(buf)))
+        return buf
+
+    def computeMacroParticlesCount(self):
+        return self.sortIndexes(counts=True)
+
+    def merge(self, min_count=10):
+        _check(self._L.pic_species_merge(self.world._h, self.id, int(min_count)))
+
+    def sums(self):
+        out = np.zeros(5)
+        _check(self._L.pic_species_sums(self.world._h, self.id, _p(out)))
+        return out
+
+    def getMicroCount(self):
+        return self.sums()[0]
+
+    def getMomentum(self):
+        return self.sums()[1:4]
+
+    def getKE(self):
+        return self.sums()[4]
+
+
+class PotentialSolver:
+    """PotentialSolver(world, max_it, tol, type) -- ch4/v3/src/PotentialSolver.h:26-88.
+
+    tol is the FP64 relative residual ||b - L phi|| / ||b|| of the reduced system."""
+
+    def __init__(self, world, max_solver_it, tolerance, solver_type=SOLVER_PCG, omega=1.4):
+        self.world = world
+        _check(world._L.pic_solver_configure(world._h, int(solver_type), float(tolerance), int(max_solver_it),
+                                             float(omega)))
+        self.iters, self.rel = 0, float("nan")
+
+    def solve(self, raise_on_fail=False):
+        it, rel = C.c_int(), C.c_double()
+        rc = _check(self.world._L.pic_solver_solve(self.world._h, C.byref(it), C.byref(rel)),
+                    allow=() if raise_on_fail else (PIC_ERR_NOT_CONVERGED,))
+        self.iters, self.rel = it.value, rel.value
+        return rc == PIC_OK
+
+    def computeEF(self):
+        _check(self.world._L.pic_solver_compute_ef(self.world._h))
+
+    def stats(self):
+        a, b, c = C.c_long(), C.c_long(), C.c_long()
+        _check(self.world._L.pic_solver_stats(self.world._h, C.byref(a), C.byref(b), C.byref(c)))
+        return dict(solves=a.value, refinements=b.value, inner=c.value)
+
+
+class MC_MEX_Ionization:
+    """Electron-impact ionisation / elastic collisions against a background gas
+    (GPU form of ch4/v3/src/Interactions.h:98-143)."""
+
+    def __init__(self, electrons, ions, world, n_neutral, T_neutral, m_neutral, E_ion_eV, table_E, table_s,
+                 sigma_ion_kind=0, sigma_ion_params=(1.015e-18, 9.793, 61.81, 0.0), B_inc=10.0, seed=12345):
+        self.world = world
+        self._tE = _f64(table_E)
+        self._tS = _f64(table_s)
+        _check(world._L.pic_mcc_create(world._h, electrons.id, ions.id, float(n_neutral), float(T_neutral),
+                                       float(m_neutral), float(E_ion_eV), float(B_inc), int(sigma_ion_kind),
+                                       _p(_f64(list(sigma_ion_params) + [0.0] * (4 - len(sigma_ion_params)))),
+                                       _p(self._tE), _p(self._tS), len(self._tE), int(seed)))
+
+    def apply(self, dt):
+        _check(self.world._L.pic_mcc_apply(self.world._h, float(dt)))
+
+    def stats(self):
+        out = np.zeros(4, np.uint64)
+        _check(self.world._L.pic_mcc_stats(self.world._h, _p(out)))
+        return dict(candidates=int(out[0]), collisions=int(out[1]), ionizations=int(out[2]), lost=int(out[3]))

@@ -1,0 +1,1196 @@
+// C ABI and host-side orchestration of the GB300 PIC + DSMC library.
+//
+// One pic_world = the reference World with its fields plus the species, solver and collision
+// model that the reference keeps in main.cpp (ch4/v3/src/main.cpp:71-139).  All device work
+// is issued on the world's own stream; only calls that hand data back to the host, and the
+// solver's convergence checks, synchronise it.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+#include "../../include/pic_gb300.h"
+#include "pic_kernels.h"
+
+using namespace pic;
+
+namespace {
+
+thread_local char g_err[512] = "";
+
+int fail(int code, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+#define CU(call)                                                                                   \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess) return fail(PIC_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+constexpr double kQe = 1.602176565e-19;  // ch4/v3/src/all.h:17
+constexpr double kMe = 9.10938215e-31;
+constexpr double kKb = 1.380648e-23;
+
+struct SpeciesHost {
+    std::string name;
+    double mass = 0, charge = 0, mpw0 = 0;
+    long capacity = 0;
+    SpeciesDev dev{};
+    float4* pos2 = nullptr;
+    float4* vel2 = nullptr;
+    unsigned long long* id2 = nullptr;
+    float* den = nullptr;
+    float* den_avg = nullptr;
+    int avg_samples = 0;
+    double scale = 1.0;  // fixed-point scale of the density accumulator
+    unsigned long long next_id = 0;
+    bool deposited = false;
+};
+
+struct TimerAcc {
+    double ms = 0;
+    long launches = 0;
+};
+struct PendingEvent {
+    std::string name;
+    cudaEvent_t a, b;
+};
+
+}  // namespace
+
+struct pic_world {
+    int device = 0;
+    int sms = 152;
+    cudaStream_t stream = nullptr;
+    GridDev g{};
+    // node fields
+    float4* ef = nullptr;
+    double* phi = nullptr;
+    double* phi_alt = nullptr;
+    float* rho = nullptr;
+    uint16_t* kind = nullptr;
+    float *r = nullptr, *e = nullptr, *d = nullptr, *d2 = nullptr, *q = nullptr, *z = nullptr;
+    double* part = nullptr;
+    double* scal = nullptr;
+    int* flag = nullptr;
+    double* h_scal = nullptr;  // pinned
+    int* h_flag = nullptr;     // pinned
+    // cells
+    int* cell_count = nullptr;
+    int* cell_start = nullptr;
+    int* scan_aux = nullptr;
+    unsigned* err = nullptr;
+    std::vector<SpeciesHost> sp;
+    // boundaries
+    int periodic[3] = {0, 0, 0};
+    int face_mode[6] = {0, 0, 0, 0, 0, 0};
+    double face_phi[6] = {0, 0, 0, 0, 0, 0};
+    struct Box {
+        double c[3], s[3], phi;
+    };
+    std::vector<Box> boxes;
+    // time
+    double dt = 1e-4;
+    int num_ts = 0;
+    int ts = -1;
+    // solver
+    int method = PIC_SOLVER_PCG;
+    double tol = 1e-6;
+    int max_it = 10000;
+    double omega = 1.4;
+    long n_solves = 0, n_refine = 0, n_inner = 0;
+    // collisions
+    bool mcc_on = false;
+    int mcc_e = -1, mcc_i = -1;
+    CollDev coll{};
+    float* tE = nullptr;
+    float* tS = nullptr;
+    unsigned long long* stats = nullptr;
+    double mcc_n = 0, mcc_sigv = 0;
+    uint64_t mcc_seed = 0;
+    // loop
+    int solve_each_step = 1, sort_every = 20, merge_every = 0, merge_after = 0, merge_min = 10;
+    int subcycle[kMaxSpecies] = {1, 1, 1, 1};
+    // timing
+    bool timing = false;
+    std::map<std::string, TimerAcc> timers;
+    std::vector<PendingEvent> pending;
+    std::vector<cudaEvent_t> event_pool;
+    long launches = 0;
+    int grid_nodes = 1024;
+    int grid_push_mcc = 304, grid_push = 456, grid_parts = 1216;
+};
+
+namespace {
+
+cudaEvent_t get_event(pic_world* w) {
+    if (!w->event_pool.empty()) {
+        cudaEvent_t e = w->event_pool.back();
+        w->event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+}
+
+// brackets a group of launches with CUDA events on the world's stream
+struct Scope {
+    pic_world* w;
+    const char* name;
+    cudaEvent_t a = nullptr;
+    int n;
+    Scope(pic_world* w_, const char* name_, int nlaunch) : w(w_), name(name_), n(nlaunch) {
+        w->launches += nlaunch;
+        if (w->timing) {
+            a = get_event(w);
+            cudaEventRecord(a, w->stream);
+        }
+        w->timers[name].launches += nlaunch;
+    }
+    ~Scope() {
+        if (w->timing) {
+            cudaEvent_t b = get_event(w);
+            cudaEventRecord(b, w->stream);
+            w->pending.push_back({name, a, b});
+        }
+    }
+};
+
+void collect_timers(pic_world* w) {
+    if (w->pending.empty()) return;
+    cudaStreamSynchronize(w->stream);
+    for (auto& p : w->pending) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, p.a, p.b);
+        w->timers[p.name].ms += ms;
+        w->event_pool.push_back(p.a);
+        w->event_pool.push_back(p.b);
+    }
+    w->pending.clear();
+}
+
+int check_device_error(pic_world* w) {
+    unsigned h = 0;
+    CU(cudaMemcpyAsync(&h, w->err, sizeof(unsigned), cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    if (h) {
+        CU(cudaMemsetAsync(w->err, 0, sizeof(unsigned), w->stream));
+        if (h & kErrCapacity) return fail(PIC_ERR_CAPACITY, "a species ran out of capacity (device flags 0x%x)", h);
+        return fail(PIC_ERR_DEVICE, "device fault flags 0x%x (bounded wait expired or merge truncated)", h);
+    }
+    return PIC_OK;
+}
+
+bool valid_sp(pic_world* w, int s) { return w && s >= 0 && s < (int)w->sp.size(); }
+
+// node kinds and masks; Dirichlet values written into phi_host
+void build_kinds(pic_world* w, std::vector<uint16_t>& kind, std::vector<double>& phi_host) {
+    const GridDev& g = w->g;
+    int nn[3] = {g.ni, g.nj, g.nk};
+    kind.assign(g.nv, kFree);
+    phi_host.assign(g.nv, 0.0);
+    for (int k = 0; k < g.nk; k++)
+        for (int j = 0; j < g.nj; j++)
+            for (int i = 0; i < g.ni; i++) {
+                int n = (k * g.nj + j) * g.ni + i, ijk[3] = {i, j, k};
+                bool alias = false;
+                for (int d = 0; d < 3; d++)
+                    if (w->periodic[d] && ijk[d] == nn[d] - 1) alias = true;
+                if (alias) {
+                    kind[n] = kAlias;
+                    continue;
+                }
+                double x[3] = {g.x0[0] + i * g.dxd[0], g.x0[1] + j * g.dxd[1], g.x0[2] + k * g.dxd[2]};
+                bool in_box = false;
+                for (auto& b : w->boxes) {
+                    bool in = true;
+                    for (int d = 0; d < 3; d++)
+                        if (std::fabs(x[d] - b.c[d]) > b.s[d] / 2) in = false;
+                    if (in && !in_box) {
+                        in_box = true;
+                        phi_host[n] = b.phi;
+                    }
+                }
+                if (in_box) {
+                    kind[n] = kFixed;
+                    continue;
+                }
+                int fixed_face = -1, wall = 0;
+                for (int d = 0; d < 3; d++) {
+                    if (w->periodic[d]) continue;
+                    for (int s = 0; s < 2; s++) {
+                        int f = 2 * d + s;
+                        if ((s == 0 && ijk[d] == 0) || (s == 1 && ijk[d] == nn[d] - 1)) {
+                            wall = 1;
+                            if (w->face_mode[f] == 1 && fixed_face < 0) fixed_face = f;
+                        }
+                    }
+                }
+                if (fixed_face >= 0) {
+                    kind[n] = kFixed;
+                    phi_host[n] = w->face_phi[fixed_face];
+                } else if (wall) {
+                    kind[n] = kMirror;
+                }
+            }
+    // neighbour masks of FREE nodes
+    for (int k = 0; k < g.nk; k++)
+        for (int j = 0; j < g.nj; j++)
+            for (int i = 0; i < g.ni; i++) {
+                int n = (k * g.nj + j) * g.ni + i;
+                if ((kind[n] & 3) != kFree) continue;
+                int ijk[3] = {i, j, k};
+                uint16_t mask = 0;
+                for (int d = 0; d < 3; d++)
+                    for (int s = 0; s < 2; s++) {
+                        int c = ijk[d] + (s ? 1 : -1);
+                        if (w->periodic[d]) {
+                            if (c < 0) c = nn[d] - 2;
+                            else if (c >= nn[d] - 1) c = 0;
+                        }
+                        int q3[3] = {ijk[0], ijk[1], ijk[2]};
+                        q3[d] = c;
+                        int qn = (q3[2] * g.nj + q3[1]) * g.ni + q3[0];
+                        int bit = 2 * d + s;
+                        if ((kind[qn] & 3) == kMirror) mask |= 1u << (2 + bit);
+                        if ((kind[qn] & 3) == kFixed) mask |= 1u << (8 + bit);
+                    }
+                kind[n] = (uint16_t)(kFree | mask);
+            }
+}
+
+int upload_kinds(pic_world* w, bool reset_phi) {
+    std::vector<uint16_t> kind;
+    std::vector<double> ph;
+    build_kinds(w, kind, ph);
+    const GridDev& g = w->g;
+    CU(cudaMemcpyAsync(w->kind, kind.data(), sizeof(uint16_t) * g.nv, cudaMemcpyHostToDevice, w->stream));
+    if (reset_phi) {
+        CU(cudaMemcpyAsync(w->phi, ph.data(), sizeof(double) * g.nv, cudaMemcpyHostToDevice, w->stream));
+    } else {
+        // keep the caller's phi but force Dirichlet values
+        std::vector<double> cur(g.nv);
+        CU(cudaMemcpyAsync(cur.data(), w->phi, sizeof(double) * g.nv, cudaMemcpyDeviceToHost, w->stream));
+        CU(cudaStreamSynchronize(w->stream));
+        for (int n = 0; n < g.nv; n++)
+            if ((kind[n] & 3) == kFixed) cur[n] = ph[n];
+        CU(cudaMemcpyAsync(w->phi, cur.data(), sizeof(double) * g.nv, cudaMemcpyHostToDevice, w->stream));
+    }
+    CU(cudaStreamSynchronize(w->stream));
+    return PIC_OK;
+}
+
+void fill_grid_boxes(pic_world* w) {
+    GridDev& g = w->g;
+    g.n_boxes = 0;
+    for (auto& b : w->boxes) {
+        if (g.n_boxes >= kMaxBoxes) break;
+        for (int d = 0; d < 3; d++) {
+            g.box_lo[g.n_boxes][d] = (float)(b.c[d] - b.s[d] / 2 - g.x0[d]);
+            g.box_hi[g.n_boxes][d] = (float)(b.c[d] + b.s[d] / 2 - g.x0[d]);
+        }
+        g.n_boxes++;
+    }
+    for (int d = 0; d < 3; d++) g.periodic[d] = w->periodic[d];
+}
+
+SolveWork solve_work(pic_world* w) {
+    SolveWork s;
+    s.phi = w->phi;
+    s.phi_alt = w->phi_alt;
+    s.rho = w->rho;
+    s.kind = reinterpret_cast<const uint8_t*>(w->kind);
+    s.r = w->r;
+    s.e = w->e;
+    s.d = w->d;
+    s.q = w->q;
+    s.z = w->z;
+    s.part = w->part;
+    s.scal = w->scal;
+    s.flag = w->flag;
+    return s;
+}
+
+}  // namespace
+
+
+// =====================================================================================
+// World
+// =====================================================================================
+extern "C" int pic_world_create(pic_world** out, int ni, int nj, int nk, const double* x0, const double* xm,
+                                int device) {
+    if (!out || !x0 || !xm) return fail(PIC_ERR_ARG, "null argument");
+    *out = nullptr;
+    if (ni < 3 || nj < 3 || nk < 3) return fail(PIC_ERR_ARG, "need at least 3 nodes per axis");
+    long long nv = (long long)ni * nj * nk;
+    if (nv > (1ll << 30)) return fail(PIC_ERR_ARG, "grid too large (%lld nodes)", nv);
+    for (int d = 0; d < 3; d++)
+        if (!(xm[d] > x0[d])) return fail(PIC_ERR_ARG, "xm must exceed x0 on every axis");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= device || device < 0)
+        return fail(PIC_ERR_CUDA, "no CUDA device %d available", device);
+    CU(cudaSetDevice(device));
+    pic_world* w = new pic_world();
+    w->device = device;
+    cudaDeviceGetAttribute(&w->sms, cudaDevAttrMultiProcessorCount, device);
+    GridDev& g = w->g;
+    g.ni = ni;
+    g.nj = nj;
+    g.nk = nk;
+    g.ci = ni - 1;
+    g.cj = nj - 1;
+    g.ck = nk - 1;
+    g.nv = (int)nv;
+    g.nc = g.ci * g.cj * g.ck;
+    int nn[3] = {ni, nj, nk};
+    for (int d = 0; d < 3; d++) {
+        g.x0[d] = x0[d];
+        g.xm[d] = xm[d];
+        g.dxd[d] = (xm[d] - x0[d]) / (nn[d] - 1);  // World::setExtents, World.cpp:72-76
+        g.dx[d] = (float)g.dxd[d];
+        g.inv_dx[d] = (float)(1.0 / g.dxd[d]);
+    }
+    auto alloc = [&](void** p, size_t bytes) -> bool { return cudaMalloc(p, bytes) == cudaSuccess; };
+    bool ok = cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking) == cudaSuccess;
+    ok = ok && alloc((void**)&w->ef, sizeof(float4) * nv) && alloc((void**)&w->phi, sizeof(double) * nv) &&
+         alloc((void**)&w->phi_alt, sizeof(double) * nv) && alloc((void**)&w->rho, sizeof(float) * nv) &&
+         alloc((void**)&w->kind, sizeof(uint16_t) * nv) && alloc((void**)&w->r, sizeof(float) * nv) &&
+         alloc((void**)&w->e, sizeof(float) * nv) && alloc((void**)&w->d, sizeof(float) * nv) &&
+         alloc((void**)&w->d2, sizeof(float) * nv) && alloc((void**)&w->q, sizeof(float) * nv) &&
+         alloc((void**)&w->z, sizeof(float) * nv) && alloc((void**)&w->part, sizeof(double) * kParts * 8) &&
+         alloc((void**)&w->scal, sizeof(double) * 16) && alloc((void**)&w->flag, sizeof(int) * 4) &&
+         alloc((void**)&w->cell_count, sizeof(int) * (g.nc + 1)) &&
+         alloc((void**)&w->cell_start, sizeof(int) * (g.nc + 1)) &&
+         alloc((void**)&w->scan_aux, sizeof(int) * (g.nc / 2048 + 2)) && alloc((void**)&w->err, sizeof(unsigned)) &&
+         cudaMallocHost((void**)&w->h_scal, sizeof(double) * 16) == cudaSuccess &&
+         cudaMallocHost((void**)&w->h_flag, sizeof(int) * 4) == cudaSuccess;
+    if (!ok) {
+        pic_world_destroy(w);
+        return fail(PIC_ERR_CUDA, "device allocation failed for a %d x %d x %d grid", ni, nj, nk);
+    }
+    cudaMemsetAsync(w->ef, 0, sizeof(float4) * nv, w->stream);
+    cudaMemsetAsync(w->rho, 0, sizeof(float) * nv, w->stream);
+    for (float* p : {w->r, w->e, w->d, w->d2, w->q, w->z}) cudaMemsetAsync(p, 0, sizeof(float) * nv, w->stream);
+    cudaMemsetAsync(w->err, 0, sizeof(unsigned), w->stream);
+    cudaMemsetAsync(w->flag, 0, sizeof(int) * 4, w->stream);
+    w->grid_nodes = (int)std::min<long long>(kParts, std::max<long long>(1, (nv + 255) / 256));
+    w->grid_parts = w->sms * 8;
+    int occ = 0;
+    w->grid_push = w->sms * 3;
+    w->grid_push_mcc = w->sms * 2;
+    (void)occ;
+    fill_grid_boxes(w);
+    int rc = upload_kinds(w, true);
+    if (rc != PIC_OK) {
+        pic_world_destroy(w);
+        return rc;
+    }
+    *out = w;
+    return PIC_OK;
+}
+
+extern "C" int pic_world_destroy(pic_world* w) {
+    if (!w) return PIC_OK;
+    cudaSetDevice(w->device);
+    if (w->stream) cudaStreamSynchronize(w->stream);
+    for (auto& s : w->sp) {
+        cudaFree(s.dev.pos);
+        cudaFree(s.dev.vel);
+        cudaFree(s.dev.id);
+        cudaFree(s.dev.counts);
+        cudaFree(s.dev.dead);
+        cudaFree(s.dev.holes);
+        cudaFree(s.dev.acc);
+        cudaFree(s.pos2);
+        cudaFree(s.vel2);
+        cudaFree(s.id2);
+        cudaFree(s.den);
+        cudaFree(s.den_avg);
+    }
+    void* ptrs[] = {w->ef,   w->phi,  w->phi_alt, w->rho,        w->kind,       w->r,        w->e,
+                    w->d,    w->d2,   w->q,       w->z,          w->part,       w->scal,     w->flag,
+                    w->cell_count,    w->cell_start,             w->scan_aux,   w->err,      w->tE,
+                    w->tS,   w->stats};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (w->h_scal) cudaFreeHost(w->h_scal);
+    if (w->h_flag) cudaFreeHost(w->h_flag);
+    for (auto& p : w->pending) {
+        cudaEventDestroy(p.a);
+        cudaEventDestroy(p.b);
+    }
+    for (auto e : w->event_pool) cudaEventDestroy(e);
+    if (w->stream) cudaStreamDestroy(w->stream);
+    delete w;
+    return PIC_OK;
+}
+
+extern "C" int pic_world_set_time(pic_world* w, double dt, int num_ts) {
+    if (!w || !(dt > 0)) return fail(PIC_ERR_ARG, "dt must be positive");
+    w->dt = dt;
+    w->num_ts = num_ts;
+    return PIC_OK;
+}
+extern "C" int pic_world_advance_time(pic_world* w, int* running) {
+    if (!w) return fail(PIC_ERR_ARG, "null world");
+    w->ts++;
+    if (running) *running = w->ts <= w->num_ts;
+    return PIC_OK;
+}
+extern "C" int pic_world_get_ts(pic_world* w, int* ts) {
+    if (!w || !ts) return fail(PIC_ERR_ARG, "null argument");
+    *ts = w->ts;
+    return PIC_OK;
+}
+extern "C" int pic_world_set_boundaries(pic_world* w, const int* periodic, const int* face_mode,
+                                        const double* face_phi) {
+    if (!w) return fail(PIC_ERR_ARG, "null world");
+    CU(cudaSetDevice(w->device));
+    for (int d = 0; d < 3; d++) w->periodic[d] = periodic ? (periodic[d] != 0) : 0;
+    for (int f = 0; f < 6; f++) {
+        w->face_mode[f] = face_mode ? face_mode[f] : 0;
+        w->face_phi[f] = face_phi ? face_phi[f] : 0.0;
+    }
+    int nn[3] = {w->g.ni, w->g.nj, w->g.nk};
+    for (int d = 0; d < 3; d++)
+        if (w->periodic[d] && nn[d] < 4) return fail(PIC_ERR_ARG, "periodic axis needs at least 4 nodes");
+    fill_grid_boxes(w);
+    return upload_kinds(w, false);
+}
+extern "C" int pic_world_add_box(pic_world* w, const double* center, const double* sides, double phi) {
+    if (!w || !center || !sides) return fail(PIC_ERR_ARG, "null argument");
+    if ((int)w->boxes.size() >= kMaxBoxes) return fail(PIC_ERR_ARG, "at most %d boxes", kMaxBoxes);
+    CU(cudaSetDevice(w->device));
+    pic_world::Box b;
+    for (int d = 0; d < 3; d++) {
+        b.c[d] = center[d];
+        b.s[d] = sides[d];
+    }
+    b.phi = phi;
+    w->boxes.push_back(b);
+    fill_grid_boxes(w);
+    return upload_kinds(w, false);
+}
+
+extern "C" int pic_world_get_field(pic_world* w, int which, double* out) {
+    if (!w || !out) return fail(PIC_ERR_ARG, "null argument");
+    CU(cudaSetDevice(w->device));
+    const GridDev& g = w->g;
+    if (which == 0) {
+        CU(cudaMemcpyAsync(out, w->phi, sizeof(double) * g.nv, cudaMemcpyDeviceToHost, w->stream));
+        CU(cudaStreamSynchronize(w->stream));
+    } else if (which == 1) {
+        std::vector<float> t(g.nv);
+        CU(cudaMemcpyAsync(t.data(), w->rho, sizeof(float) * g.nv, cudaMemcpyDeviceToHost, w->stream));
+        CU(cudaStreamSynchronize(w->stream));
+        for (int n = 0; n < g.nv; n++) out[n] = t[n];
+    } else if (which == 2) {
+        int nn[3] = {g.ni, g.nj, g.nk};
+        for (int k = 0; k < g.nk; k++)
+            for (int j = 0; j < g.nj; j++)
+                for (int i = 0; i < g.ni; i++) {
+                    int ijk[3] = {i, j, k};
+                    double v = g.dxd[0] * g.dxd[1] * g.dxd[2];
+                    for (int d = 0; d < 3; d++)
+                        if (!w->periodic[d] && (ijk[d] == 0 || ijk[d] == nn[d] - 1)) v *= 0.5;
+                    out[(k * g.nj + j) * g.ni + i] = v;
+                }
+    } else if (which == 3) {
+        std::vector<float4> t(g.nv);
+        CU(cudaMemcpyAsync(t.data(), w->ef, sizeof(float4) * g.nv, cudaMemcpyDeviceToHost, w->stream));
+        CU(cudaStreamSynchronize(w->stream));
+        for (int n = 0; n < g.nv; n++) {
+            out[3 * n] = t[n].x;
+            out[3 * n + 1] = t[n].y;
+            out[3 * n + 2] = t[n].z;
+        }
+    } else {
+        return fail(PIC_ERR_ARG, "unknown field %d", which);
+    }
+    return check_device_error(w);
+}
+extern "C" int pic_world_set_field(pic_world* w, int which, const double* in) {
+    if (!w || !in) return fail(PIC_ERR_ARG, "null argument");
+    CU(cudaSetDevice(w->device));
+    const GridDev& g = w->g;
+    if (which == 0) {
+        CU(cudaMemcpyAsync(w->phi, in, sizeof(double) * g.nv, cudaMemcpyHostToDevice, w->stream));
+        CU(cudaStreamSynchronize(w->stream));
+    } else if (which == 1) {
+        std::vector<float> t(in, in + g.nv);
+        CU(cudaMemcpyAsync(w->rho, t.data(), sizeof(float) * g.nv, cudaMemcpyHostToDevice, w->stream));
+        CU(cudaStreamSynchronize(w->stream));
+    } else if (which == 3) {
+        std::vector<float4> t(g.nv);
+        for (int n = 0; n < g.nv; n++) t[n] = make_float4((float)in[3 * n], (float)in[3 * n + 1], (float)in[3 * n + 2], 0.f);
+        CU(cudaMemcpyAsync(w->ef, t.data(), sizeof(float4) * g.nv, cudaMemcpyHostToDevice, w->stream));
+        CU(cudaStreamSynchronize(w->stream));
+    } else {
+        return fail(PIC_ERR_ARG, "field %d is not settable", which);
+    }
+    return PIC_OK;
+}
+
+// =====================================================================================
+// Species
+// =====================================================================================
+extern "C" int pic_species_create(pic_world* w, const char* name, double mass, double charge, double mpw0,
+                                  long capacity, double weight_bound, int* species_id) {
+    if (!w || !species_id) return fail(PIC_ERR_ARG, "null argument");
+    if ((int)w->sp.size() >= kMaxSpecies) return fail(PIC_ERR_ARG, "at most %d species", kMaxSpecies);
+    if (!(mass > 0) || capacity <= 0 || capacity > (1l << 30)) return fail(PIC_ERR_ARG, "bad mass or capacity");
+    CU(cudaSetDevice(w->device));
+    SpeciesHost s;
+    s.name = name ? name : "";
+    s.mass = mass;
+    s.charge = charge;
+    s.mpw0 = mpw0;
+    s.capacity = capacity;
+    const GridDev& g = w->g;
+    auto alloc = [&](void** p, size_t bytes) -> bool { return cudaMalloc(p, bytes) == cudaSuccess; };
+    bool ok = alloc((void**)&s.dev.pos, sizeof(float4) * capacity) && alloc((void**)&s.dev.vel, sizeof(float4) * capacity) &&
+              alloc((void**)&s.dev.id, sizeof(unsigned long long) * capacity) &&
+              alloc((void**)&s.dev.counts, sizeof(int) * 8) && alloc((void**)&s.dev.dead, sizeof(int) * capacity) &&
+              alloc((void**)&s.dev.holes, sizeof(int) * capacity) &&
+              alloc((void**)&s.dev.acc, sizeof(unsigned long long) * g.nv) &&
+              alloc((void**)&s.pos2, sizeof(float4) * capacity) && alloc((void**)&s.vel2, sizeof(float4) * capacity) &&
+              alloc((void**)&s.id2, sizeof(unsigned long long) * capacity) && alloc((void**)&s.den, sizeof(float) * g.nv) &&
+              alloc((void**)&s.den_avg, sizeof(float) * g.nv);
+    if (!ok) {
+        cudaFree(s.dev.pos); cudaFree(s.dev.vel); cudaFree(s.dev.id); cudaFree(s.dev.counts); cudaFree(s.dev.dead);
+        cudaFree(s.dev.holes); cudaFree(s.dev.acc); cudaFree(s.pos2); cudaFree(s.vel2); cudaFree(s.id2);
+        cudaFree(s.den); cudaFree(s.den_avg);
+        return fail(PIC_ERR_CUDA, "device allocation failed for species %s (capacity %ld)", s.name.c_str(), capacity);
+    }
+    s.dev.capacity = (int)capacity;
+    CU(cudaMemsetAsync(s.dev.counts, 0, sizeof(int) * 8, w->stream));
+    CU(cudaMemsetAsync(s.dev.acc, 0, sizeof(unsigned long long) * g.nv, w->stream));
+    CU(cudaMemsetAsync(s.den, 0, sizeof(float) * g.nv, w->stream));
+    CU(cudaMemsetAsync(s.den_avg, 0, sizeof(float) * g.nv, w->stream));
+    double bound = weight_bound > 0 ? weight_bound : (double)capacity * (mpw0 > 0 ? mpw0 : 1.0) * 64.0;
+    // largest power of two keeping every node sum below 2^62
+    int ex = (int)std::floor(std::log2(std::ldexp(1.0, 62) / bound));
+    if (ex > 60) ex = 60;
+    if (ex < -60) ex = -60;
+    s.scale = std::ldexp(1.0, ex);
+    w->sp.push_back(s);
+    *species_id = (int)w->sp.size() - 1;
+    return PIC_OK;
+}
+
+extern "C" int pic_species_add_particles(pic_world* w, int sp, const double* pos, const double* vel,
+                                         const double* wgt, const uint64_t* ids, long n, int rewind) {
+    if (!valid_sp(w, sp) || (n > 0 && (!pos || !vel || !wgt))) return fail(PIC_ERR_ARG, "bad species or arrays");
+    if (n == 0) return PIC_OK;
+    CU(cudaSetDevice(w->device));
+    SpeciesHost& s = w->sp[sp];
+    std::vector<unsigned long long> idv(n);
+    for (long p = 0; p < n; p++) idv[p] = ids ? ids[p] : s.next_id + p;
+    if (!ids) s.next_id += n;
+    double *dp, *dv, *dw;
+    unsigned long long* di;
+    CU(cudaMallocAsync((void**)&dp, sizeof(double) * 3 * n, w->stream));
+    CU(cudaMallocAsync((void**)&dv, sizeof(double) * 3 * n, w->stream));
+    CU(cudaMallocAsync((void**)&dw, sizeof(double) * n, w->stream));
+    CU(cudaMallocAsync((void**)&di, sizeof(unsigned long long) * n, w->stream));
+    CU(cudaMemcpyAsync(dp, pos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, w->stream));
+    CU(cudaMemcpyAsync(dv, vel, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, w->stream));
+    CU(cudaMemcpyAsync(dw, wgt, sizeof(double) * n, cudaMemcpyHostToDevice, w->stream));
+    CU(cudaMemcpyAsync(di, idv.data(), sizeof(unsigned long long) * n, cudaMemcpyHostToDevice, w->stream));
+    {
+        Scope sc(w, "load", 5);
+        launch_from_abs(w->g, s.dev, dp, dv, dw, di, (int)n, rewind, (float)(s.charge / s.mass * 0.5 * w->dt), w->ef,
+                        w->stream);
+    }
+    cudaFreeAsync(dp, w->stream);
+    cudaFreeAsync(dv, w->stream);
+    cudaFreeAsync(dw, w->stream);
+    cudaFreeAsync(di, w->stream);
+    CU(cudaStreamSynchronize(w->stream));
+    return check_device_error(w);
+}
+
+extern "C" int pic_species_load_uniform(pic_world* w, int sp, const double* lo, const double* hi, long n, double T,
+                                        double w_mean, double w_sigma, uint64_t seed) {
+    if (!valid_sp(w, sp) || !lo || !hi || n < 0) return fail(PIC_ERR_ARG, "bad arguments");
+    CU(cudaSetDevice(w->device));
+    SpeciesHost& s = w->sp[sp];
+    LoadArgs la;
+    for (int d = 0; d < 3; d++) {
+        la.lo[d] = std::max(lo[d], w->g.x0[d]);
+        la.hi[d] = std::min(hi[d], w->g.xm[d]);
+    }
+    la.vth = (float)std::sqrt(kKb * T / s.mass);
+    la.w_mean = (float)w_mean;
+    la.w_sigma = (float)w_sigma;
+    la.id0 = s.next_id;
+    la.key = make_uint2((unsigned)seed, (unsigned)(seed >> 32) ^ (unsigned)(sp * 0x9E3779B9u));
+    la.n = (int)n;
+    s.next_id += n;
+    {
+        Scope sc(w, "load", 2);
+        launch_load_uniform(w->g, s.dev, la, w->stream);
+    }
+    return check_device_error(w);
+}
+
+extern "C" int pic_species_count(pic_world* w, int sp, long* n) {
+    if (!valid_sp(w, sp) || !n) return fail(PIC_ERR_ARG, "bad arguments");
+    CU(cudaSetDevice(w->device));
+    int h = 0;
+    CU(cudaMemcpyAsync(&h, w->sp[sp].dev.counts, sizeof(int), cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    *n = h;
+    return PIC_OK;
+}
+
+extern "C" int pic_species_get_particles(pic_world* w, int sp, double* pos, double* vel, double* wgt, uint64_t* ids,
+                                         long cap, long* n_out) {
+    if (!valid_sp(w, sp)) return fail(PIC_ERR_ARG, "bad species");
+    long n = 0;
+    int rc = pic_species_count(w, sp, &n);
+    if (rc) return rc;
+    if (n_out) *n_out = n;
+    if (n > cap) return fail(PIC_ERR_ARG, "buffer holds %ld particles, species has %ld", cap, n);
+    if (n == 0) return PIC_OK;
+    SpeciesHost& s = w->sp[sp];
+    double *dp, *dv, *dw;
+    unsigned long long* di;
+    CU(cudaMallocAsync((void**)&dp, sizeof(double) * 3 * n, w->stream));
+    CU(cudaMallocAsync((void**)&dv, sizeof(double) * 3 * n, w->stream));
+    CU(cudaMallocAsync((void**)&dw, sizeof(double) * n, w->stream));
+    CU(cudaMallocAsync((void**)&di, sizeof(unsigned long long) * n, w->stream));
+    {
+        Scope sc(w, "export", 1);
+        launch_to_abs(w->g, s.dev, dp, dv, dw, di, (int)n, w->stream);
+    }
+    if (pos) CU(cudaMemcpyAsync(pos, dp, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, w->stream));
+    if (vel) CU(cudaMemcpyAsync(vel, dv, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, w->stream));
+    if (wgt) CU(cudaMemcpyAsync(wgt, dw, sizeof(double) * n, cudaMemcpyDeviceToHost, w->stream));
+    if (ids) CU(cudaMemcpyAsync(ids, di, sizeof(unsigned long long) * n, cudaMemcpyDeviceToHost, w->stream));
+    cudaFreeAsync(dp, w->stream);
+    cudaFreeAsync(dv, w->stream);
+    cudaFreeAsync(dw, w->stream);
+    cudaFreeAsync(di, w->stream);
+    CU(cudaStreamSynchronize(w->stream));
+    return check_device_error(w);
+}
+
+namespace {
+// one push of species sp; collisions fused when sp is the collision model's electron species
+int push_species(pic_world* w, int sp, double dt, int deposit, bool with_mcc, bool do_push) {
+    SpeciesHost& s = w->sp[sp];
+    PushArgs a{};
+    a.g = w->g;
+    a.sp = s.dev;
+    a.ef = w->ef;
+    a.qm_dt = do_push ? (float)(s.charge / s.mass * dt) : 0.f;
+    for (int d = 0; d < 3; d++) a.dtdx[d] = do_push ? (float)(dt / w->g.dxd[d]) : 0.f;
+    a.deposit = deposit;
+    a.dep_scale = (float)s.scale;
+    a.staged = 1;
+    a.err = w->err;
+    a.coll.enabled = 0;
+    if (with_mcc && w->mcc_on && sp == w->mcc_e) {
+        a.coll = w->coll;
+        a.coll.enabled = 1;
+        a.coll.p_null = (float)(w->mcc_n * w->mcc_sigv * dt);
+        a.coll.step = (unsigned)w->ts;
+        a.coll.ion = w->sp[w->mcc_i].dev;
+    }
+    if (deposit) s.deposited = true;
+    {
+        Scope sc(w, deposit ? "push_deposit" : "push", 1);
+        launch_push(a, w->stream, a.coll.enabled ? w->grid_push_mcc : w->grid_push);
+    }
+    {
+        Scope sc(w, "compact", a.coll.enabled ? 5 : 4);
+        launch_commit_appends(s.dev, w->err, w->stream);
+        if (a.coll.enabled) launch_commit_appends(w->sp[w->mcc_i].dev, w->err, w->stream);
+        launch_compact(s.dev, w->stream, w->sms * 4);
+    }
+    return PIC_OK;
+}
+}  // namespace
+
+extern "C" int pic_species_push(pic_world* w, int sp, double dt, int deposit) {
+    if (!valid_sp(w, sp)) return fail(PIC_ERR_ARG, "bad species");
+    CU(cudaSetDevice(w->device));
+    int rc = push_species(w, sp, dt, deposit, false, true);
+    if (rc) return rc;
+    CU(cudaGetLastError());
+    return PIC_OK;
+}
+
+extern "C" int pic_species_number_density(pic_world* w, int sp) {
+    if (!valid_sp(w, sp)) return fail(PIC_ERR_ARG, "bad species");
+    CU(cudaSetDevice(w->device));
+    int rc = push_species(w, sp, 0.0, 1, false, false);
+    if (rc) return rc;
+    CU(cudaGetLastError());
+    return PIC_OK;
+}
+
+extern "C" int pic_charge_density(pic_world* w) {
+    if (!w) return fail(PIC_ERR_ARG, "null world");
+    CU(cudaSetDevice(w->device));
+    FinalizeArgs a{};
+    a.g = w->g;
+    a.ns = (int)w->sp.size();
+    for (int s = 0; s < a.ns; s++) {
+        SpeciesHost& sh = w->sp[s];
+        a.acc[s] = sh.dev.acc;
+        a.inv_scale[s] = (float)(1.0 / sh.scale);
+        a.charge[s] = (float)sh.charge;
+        a.den[s] = sh.den;
+        a.fresh[s] = sh.deposited ? 1 : 0;
+    }
+    a.rho = w->rho;
+    {
+        Scope sc(w, "rho", 1);
+        launch_finalize_rho(a, w->stream, w->grid_nodes);
+    }
+    // a species not deposited since the last call keeps its den (the reference keeps the
+    // density of a subcycled species from its last push, main.cpp:222-234)
+    for (auto& s : w->sp) s.deposited = false;
+    CU(cudaGetLastError());
+    return PIC_OK;
+}
+
+extern "C" int pic_species_get_den(pic_world* w, int sp, double* out) {
+    if (!valid_sp(w, sp) || !out) return fail(PIC_ERR_ARG, "bad arguments");
+    CU(cudaSetDevice(w->device));
+    std::vector<float> t(w->g.nv);
+    CU(cudaMemcpyAsync(t.data(), w->sp[sp].den, sizeof(float) * w->g.nv, cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    for (int n = 0; n < w->g.nv; n++) out[n] = t[n];
+    return check_device_error(w);
+}
+
+extern "C" int pic_species_update_averages(pic_world* w, int sp) {
+    if (!valid_sp(w, sp)) return fail(PIC_ERR_ARG, "bad species");
+    CU(cudaSetDevice(w->device));
+    SpeciesHost& s = w->sp[sp];
+    // Field::updateMovingAverage (Field.h:245-261): restart after 20 samples
+    s.avg_samples++;
+    if (s.avg_samples > 20) s.avg_samples = 1;
+    float b = 1.f / s.avg_samples, a = (float)(s.avg_samples - 1) / s.avg_samples;
+    {
+        Scope sc(w, "averages", 1);
+        launch_den_avg(s.den_avg, s.den, w->g.nv, a, b, w->stream, w->grid_nodes);
+    }
+    CU(cudaGetLastError());
+    return PIC_OK;
+}
+extern "C" int pic_species_get_den_avg(pic_world* w, int sp, double* out) {
+    if (!valid_sp(w, sp) || !out) return fail(PIC_ERR_ARG, "bad arguments");
+    CU(cudaSetDevice(w->device));
+    std::vector<float> t(w->g.nv);
+    CU(cudaMemcpyAsync(t.data(), w->sp[sp].den_avg, sizeof(float) * w->g.nv, cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    for (int n = 0; n < w->g.nv; n++) out[n] = t[n];
+    return PIC_OK;
+}
+
+namespace {
+int sort_species(pic_world* w, int sp) {
+    SpeciesHost& s = w->sp[sp];
+    {
+        Scope sc(w, "sort", 5);
+        launch_sort(w->g, s.dev, s.pos2, s.vel2, s.id2, w->cell_count, w->cell_start, w->scan_aux, w->stream,
+                    w->grid_parts);
+    }
+    std::swap(s.dev.pos, s.pos2);
+    std::swap(s.dev.vel, s.vel2);
+    std::swap(s.dev.id, s.id2);
+    return PIC_OK;
+}
+}  // namespace
+
+extern "C" int pic_species_sort(pic_world* w, int sp, int32_t* cell_counts) {
+    if (!valid_sp(w, sp)) return fail(PIC_ERR_ARG, "bad species");
+    CU(cudaSetDevice(w->device));
+    sort_species(w, sp);
+    CU(cudaGetLastError());
+    if (cell_counts) {
+        // counts per cell = start[c+1] - start[c]; start has nc entries, the total is the count
+        std::vector<int> st(w->g.nc);
+        CU(cudaMemcpyAsync(st.data(), w->cell_start, sizeof(int) * w->g.nc, cudaMemcpyDeviceToHost, w->stream));
+        int n = 0;
+        CU(cudaMemcpyAsync(&n, w->sp[sp].dev.counts, sizeof(int), cudaMemcpyDeviceToHost, w->stream));
+        CU(cudaStreamSynchronize(w->stream));
+        for (int c = 0; c < w->g.nc; c++) cell_counts[c] = (c + 1 < w->g.nc ? st[c + 1] : n) - st[c];
+    }
+    return PIC_OK;
+}
+
+extern "C" int pic_species_sums(pic_world* w, int sp, double* out) {
+    if (!valid_sp(w, sp) || !out) return fail(PIC_ERR_ARG, "bad arguments");
+    CU(cudaSetDevice(w->device));
+    int grid = 512;
+    {
+        Scope sc(w, "sums", 1);
+        launch_sums(w->sp[sp].dev, w->part, w->stream, grid);
+    }
+    std::vector<double> h(grid * 5);
+    CU(cudaMemcpyAsync(h.data(), w->part, sizeof(double) * grid * 5, cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    double t[5] = {0, 0, 0, 0, 0};
+    for (int b = 0; b < grid; b++)
+        for (int c = 0; c < 5; c++) t[c] += h[b * 5 + c];
+    double m = w->sp[sp].mass;
+    out[0] = t[0];
+    out[1] = t[1] * m;
+    out[2] = t[2] * m;
+    out[3] = t[3] * m;
+    out[4] = t[4] * m * 0.5;
+    return check_device_error(w);
+}
+
+// =====================================================================================
+// Poisson
+// =====================================================================================
+extern "C" int pic_solver_configure(pic_world* w, int method, double tol_rel, int max_it, double omega) {
+    if (!w || (method != PIC_SOLVER_RBSOR && method != PIC_SOLVER_PCG) || !(tol_rel > 0) || max_it <= 0)
+        return fail(PIC_ERR_ARG, "bad solver configuration");
+    w->method = method;
+    w->tol = tol_rel;
+    w->max_it = max_it;
+    w->omega = omega > 0 && omega < 2 ? omega : 1.4;
+    return PIC_OK;
+}
+
+namespace {
+// FP64 residual (optionally after phi += e), returns |r|^2 and |b|^2 on the host
+int residual_norms(pic_world* w, SolveWork& sw, int apply_e, double& r2, double& b2) {
+    {
+        Scope sc(w, "poisson", 2);
+        launch_residual(w->g, sw, apply_e, w->stream, w->grid_nodes);
+        launch_reduce_partials(w->part, 2, w->grid_nodes, w->scal + 8, w->stream);
+    }
+    w->phi = sw.phi;
+    w->phi_alt = sw.phi_alt;
+    w->n_refine++;
+    CU(cudaMemcpyAsync(w->h_scal, w->scal + 8, sizeof(double) * 2, cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    r2 = w->h_scal[0];
+    b2 = w->h_scal[1];
+    return PIC_OK;
+}
+
+int solve_impl(pic_world* w, int* iters_out, double* rel_out) {
+    SolveWork sw = solve_work(w);
+    double r2, b2;
+    int rc = residual_norms(w, sw, 0, r2, b2);
+    if (rc) return rc;
+    double bn = b2 > 0 ? std::sqrt(b2) : 1.0;
+    double rel = std::sqrt(r2) / bn;
+    int iters = 0, outer = 0;
+    const int grid = w->grid_nodes;
+    while (rel > w->tol && iters < w->max_it && outer < 1000) {
+        outer++;
+        if (w->method == PIC_SOLVER_RBSOR) {
+            int sweeps = std::min(25, w->max_it - iters);
+            {
+                Scope sc(w, "poisson", 1 + 2 * sweeps);
+                CU(cudaMemsetAsync(w->e, 0, sizeof(float) * w->g.nv, w->stream));
+                launch_rbsor_sweeps(w->g, sw, (float)w->omega, sweeps, w->stream, grid);
+            }
+            iters += sweeps;
+        } else {
+            // inner FP32 flexible PCG to eta = 1e-3 of the current residual (or the final target)
+            double target = std::max(1e-6 * r2, 0.09 * w->tol * w->tol * b2);
+            {
+                Scope sc(w, "poisson", 2);
+                launch_pcg_init(w->g, sw, w->stream, grid);
+            }
+            float* din = w->d;
+            float* dout = w->d2;
+            int it = 0;
+            for (;;) {
+                int batch = std::min(16, w->max_it - iters);
+                if (batch <= 0) break;
+                {
+                    Scope sc(w, "poisson", 2 * batch);
+                    for (int b = 0; b < batch; b++) {
+                        launch_pcg_iter_impl(w->g, sw, din, dout, it, target, w->stream, grid);
+                        std::swap(din, dout);
+                        it++;
+                    }
+                }
+                iters += batch;
+                CU(cudaMemcpyAsync(w->h_flag, w->flag, sizeof(int), cudaMemcpyDeviceToHost, w->stream));
+                CU(cudaStreamSynchronize(w->stream));
+                if (w->h_flag[0]) break;
+            }
+        }
+        rc = residual_norms(w, sw, 1, r2, b2);
+        if (rc) return rc;
+        rel = std::sqrt(r2) / bn;
+    }
+    {
+        Scope sc(w, "poisson", 2);
+        launch_fill_aux(w->g, w->phi, reinterpret_cast<const uint8_t*>(w->kind), w->stream, grid);
+    }
+    if (iters_out) *iters_out = iters;
+    if (rel_out) *rel_out = rel;
+    w->n_solves++;
+    w->n_inner += iters;
+    CU(cudaGetLastError());
+    if (rel > w->tol) return fail(PIC_ERR_NOT_CONVERGED, "Poisson solve stopped at %d iterations, rel %.3e", iters, rel);
+    return PIC_OK;
+}
+}  // namespace
+
+extern "C" int pic_solver_solve(pic_world* w, int* iters, double* rel) {
+    if (!w) return fail(PIC_ERR_ARG, "null world");
+    CU(cudaSetDevice(w->device));
+    return solve_impl(w, iters, rel);
+}
+
+extern "C" int pic_solver_stats(pic_world* w, long* solves, long* refinements, long* inner) {
+    if (!w) return fail(PIC_ERR_ARG, "null world");
+    if (solves) *solves = w->n_solves;
+    if (refinements) *refinements = w->n_refine;
+    if (inner) *inner = w->n_inner;
+    return PIC_OK;
+}
+
+extern "C" int pic_solver_compute_ef(pic_world* w) {
+    if (!w) return fail(PIC_ERR_ARG, "null world");
+    CU(cudaSetDevice(w->device));
+    {
+        Scope sc(w, "efield", 1);
+        launch_efield(w->g, w->phi, w->ef, w->stream, w->grid_nodes);
+    }
+    CU(cudaGetLastError());
+    return PIC_OK;
+}
+
+// =====================================================================================
+// collisions
+// =====================================================================================
+namespace {
+double sigv_majorant(const std::vector<double>& E, const std::vector<double>& S, double m_red) {
+    double best = 0;
+    for (size_t s = 0; s < E.size(); s++) {
+        double v = std::sqrt(2 * E[s] * kQe / m_red) * S[s];
+        best = std::max(best, v);
+        if (s + 1 < E.size()) {
+            double b = (S[s + 1] - S[s]) / (E[s + 1] - E[s]), a = S[s] - b * E[s];
+            if (b < 0) {
+                double Es = -a / (3 * b);
+                if (Es > E[s] && Es < E[s + 1]) best = std::max(best, std::sqrt(2 * Es * kQe / m_red) * (a + b * Es));
+            }
+        }
+    }
+    return best * 1.0001;
+}
+}  // namespace
+
+extern "C" int pic_mcc_create(pic_world* w, int electrons, int ions, double n_neutral, double T_neutral,
+                              double m_neutral, double E_ion_eV, double B_inc, int sigma_ion_kind,
+                              const double* sigma_ion_params, const double* table_E, const double* table_s,
+                              int table_n, uint64_t seed) {
+    if (!valid_sp(w, electrons) || !valid_sp(w, ions) || electrons == ions)
+        return fail(PIC_ERR_ARG, "electrons and ions must be two distinct species");
+    if (!(E_ion_eV > 0)) return fail(PIC_ERR_ARG, "neutral species must have a positive ionisation energy");
+    if (!table_E || !table_s || table_n < 1 || !sigma_ion_params) return fail(PIC_ERR_ARG, "missing cross sections");
+    for (int i = 1; i < table_n; i++)
+        if (!(table_E[i] > table_E[i - 1])) return fail(PIC_ERR_ARG, "sigma table energies must increase");
+    CU(cudaSetDevice(w->device));
+    std::vector<double> E(table_E, table_E + table_n), S(table_s, table_s + table_n);
+    std::vector<float> Ef(E.begin(), E.end()), Sf(S.begin(), S.end());
+    if (w->tE) cudaFree(w->tE);
+    if (w->tS) cudaFree(w->tS);
+    if (!w->stats) CU(cudaMalloc((void**)&w->stats, sizeof(unsigned long long) * 4));
+    CU(cudaMalloc((void**)&w->tE, sizeof(float) * table_n));
+    CU(cudaMalloc((void**)&w->tS, sizeof(float) * table_n));
+    CU(cudaMemcpy(w->tE, Ef.data(), sizeof(float) * table_n, cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(w->tS, Sf.data(), sizeof(float) * table_n, cudaMemcpyHostToDevice));
+    CU(cudaMemset(w->stats, 0, sizeof(unsigned long long) * 4));
+    double m_e = w->sp[electrons].mass, m_n = m_neutral;
+    double m_red = m_n * m_e / (m_n + m_e);
+    CollDev& c = w->coll;
+    c = CollDev{};
+    c.sigv_max = (float)(w->mcc_sigv = sigv_majorant(E, S, m_red));
+    c.sig_n = (float)std::sqrt(kKb * T_neutral / m_n);
+    c.m_n = (float)m_n;
+    c.m_e = (float)m_e;
+    c.E_precalc_rel_eV = (float)(0.5 * m_red / kQe);
+    c.half_mred = (float)(0.5 * m_red);
+    c.E_precalc_ele_eV = (float)(kMe * 0.5 / kQe);
+    c.E_ion_eV = (float)E_ion_eV;
+    c.B_inc = (float)B_inc;
+    c.two_q_over_me = (float)(2 * kQe / kMe);
+    c.sig_kind = sigma_ion_kind;
+    if (sigma_ion_kind == 0) {
+        c.sig_a = (float)sigma_ion_params[0];
+        c.sig_b = (float)sigma_ion_params[1];
+        c.sig_c = (float)sigma_ion_params[2];
+    } else {
+        c.sig_A = (float)sigma_ion_params[0];
+        c.sig_b = (float)sigma_ion_params[1];
+        c.sig_c = (float)sigma_ion_params[2];
+    }
+    c.tE = w->tE;
+    c.tS = w->tS;
+    c.tn = table_n;
+    c.key = make_uint2((unsigned)seed, (unsigned)(seed >> 32));
+    c.stats = w->stats;
+    w->mcc_n = n_neutral;
+    w->mcc_seed = seed;
+    w->mcc_e = electrons;
+    w->mcc_i = ions;
+    w->mcc_on = true;
+    return PIC_OK;
+}
+
+extern "C" int pic_mcc_apply(pic_world* w, double dt) {
+    if (!w || !w->mcc_on) return fail(PIC_ERR_ARG, "no collision model");
+    CU(cudaSetDevice(w->device));
+    PushArgs a{};
+    SpeciesHost& s = w->sp[w->mcc_e];
+    a.g = w->g;
+    a.sp = s.dev;
+    a.ef = w->ef;
+    a.qm_dt = 0.f;
+    a.deposit = 0;
+    a.dep_scale = (float)s.scale;
+    a.staged = 0;
+    a.err = w->err;
+    a.coll = w->coll;
+    a.coll.enabled = 1;
+    a.coll.p_null = (float)(w->mcc_n * w->mcc_sigv * dt);
+    a.coll.step = (unsigned)w->ts;
+    a.coll.ion = w->sp[w->mcc_i].dev;
+    // collisions only: dt/dx = 0 keeps every particle in place, the products are not pushed
+    {
+        Scope sc(w, "mcc", 3);
+        launch_push(a, w->stream, w->grid_push_mcc);
+        launch_commit_appends(s.dev, w->err, w->stream);
+        launch_commit_appends(w->sp[w->mcc_i].dev, w->err, w->stream);
+    }
+    CU(cudaGetLastError());
+    return PIC_OK;
+}
+
+extern "C" int pic_mcc_stats(pic_world* w, uint64_t* out) {
+    if (!w || !out || !w->stats) return fail(PIC_ERR_ARG, "no collision model");
+    CU(cudaSetDevice(w->device));
+    CU(cudaMemcpyAsync(out, w->stats, sizeof(unsigned long long) * 4, cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    return PIC_OK;
+}
+
+// =====================================================================================
+// step loop (ch4/v3/src/main.cpp:177-286)
+// =====================================================================================
+extern "C" int pic_loop_configure(pic_world* w, int solve_each_step, int sort_every, const int* subcycle,
+                                  int merge_every, int merge_after, int merge_min) {
+    if (!w) return fail(PIC_ERR_ARG, "null world");
+    w->solve_each_step = solve_each_step;
+    w->sort_every = sort_every;
+    for (int s = 0; s < kMaxSpecies; s++) w->subcycle[s] = subcycle && subcycle[s] > 0 ? subcycle[s] : 1;
+    w->merge_every = merge_every;
+    w->merge_after = merge_after;
+    w->merge_min = merge_min;
+    return PIC_OK;
+}
+
+extern "C" int pic_species_merge(pic_world* w, int sp, int min_count) {
+    (void)min_count;
+    if (!valid_sp(w, sp)) return fail(PIC_ERR_ARG, "bad species");
+    return fail(PIC_ERR_ARG, "merge is not available in this build");
+}
+
+extern "C" int pic_step(pic_world* w) {
+    if (!w) return fail(PIC_ERR_ARG, "null world");
+    CU(cudaSetDevice(w->device));
+    Scope whole(w, "step", 0);
+    w->ts++;  // World::advanceTime
+    const int ts = w->ts;
+    if (w->merge_every > 0 && ts > w->merge_after && ts % w->merge_every == 0) {
+        for (int s = 0; s < (int)w->sp.size(); s++) {
+            int rc = pic_species_merge(w, s, w->merge_min);
+            if (rc) return rc;
+        }
+    }
+    // collisions are fused into the electron push, which runs first so that the ion products
+    // are pushed in this step too (the reference applies interactions before the species loop)
+    std::vector<int> order;
+    if (w->mcc_on) order.push_back(w->mcc_e);
+    for (int s = 0; s < (int)w->sp.size(); s++)
+        if (!(w->mcc_on && s == w->mcc_e)) order.push_back(s);
+    for (int s : order) {
+        int k = w->subcycle[s];
+        if (ts % k != 0) continue;
+        int rc = push_species(w, s, w->dt * k, 1, true, true);
+        if (rc) return rc;
+    }
+    int rc = pic_charge_density(w);
+    if (rc) return rc;
+    if (w->solve_each_step) {
+        rc = solve_impl(w, nullptr, nullptr);
+        if (rc) return rc;
+        rc = pic_solver_compute_ef(w);
+        if (rc) return rc;
+    }
+    if (w->sort_every > 0 && ts % w->sort_every == 0)
+        for (int s = 0; s < (int)w->sp.size(); s++) sort_species(w, s);
+    CU(cudaGetLastError());
+    return PIC_OK;
+}
+
+extern "C" int pic_synchronize(pic_world* w) {
+    if (!w) return fail(PIC_ERR_ARG, "null world");
+    CU(cudaSetDevice(w->device));
+    CU(cudaStreamSynchronize(w->stream));
+    return check_device_error(w);
+}
+
+extern "C" int pic_last_error(char* buf, int len) {
+    if (buf && len > 0) {
+        strncpy(buf, g_err, len - 1);
+        buf[len - 1] = 0;
+    }
+    return PIC_OK;
+}
+
+extern "C" int pic_timing_enable(pic_world* w, int on) {
+    if (!w) return fail(PIC_ERR_ARG, "null world");
+    w->timing = on != 0;
+    return PIC_OK;
+}
+extern "C" int pic_timing_read(pic_world* w, const char* name, double* ms, long* launches) {
+    if (!w || !name) return fail(PIC_ERR_ARG, "null argument");
+    collect_timers(w);
+    auto it = w->timers.find(name);
+    if (ms) *ms = it == w->timers.end() ? 0.0 : it->second.ms;
+    if (launches) *launches = it == w->timers.end() ? 0 : it->second.launches;
+    return PIC_OK;
+}
+extern "C" int pic_timing_reset(pic_world* w) {
+    if (!w) return fail(PIC_ERR_ARG, "null world");
+    collect_timers(w);
+    w->timers.clear();
+    return PIC_OK;
+}
+extern "C" int pic_launch_count(pic_world* w, long* n) {
+    if (!w || !n) return fail(PIC_ERR_ARG, "null argument");
+    *n = w->launches;
+    return PIC_OK;
+}
+extern "C" int pic_world_stream(pic_world* w, void** stream) {
+    if (!w || !stream) return fail(PIC_ERR_ARG, "null argument");
+    *stream = (void*)w->stream;
+    return PIC_OK;
+}

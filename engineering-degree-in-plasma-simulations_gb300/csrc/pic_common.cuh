@@ -1,0 +1,99 @@
+// Shared device-side definitions of the GB300 PIC + DSMC library (sm_103a).
+//
+// Data layout in HBM (one World):
+//   nodes  n = (k*nj + j)*ni + i            (reference Field::U, ch4/v3/src/Field.h:262-265)
+//   cells  c = (k*(nj-1) + j)*(ni-1) + i    (reference World::XtoC, ch4/v3/src/World.cpp:134-137)
+//   E      float4 per node {Ex, Ey, Ez, 0}  (16 B aligned: TMA bulk copies of node rows)
+//   phi    double per node (master copy; FP32 inner solves refine it)
+//   rho    float per node
+//   kind   uint8 per node: bits 0-1 node kind, bits 2-7 "neighbour d is a mirror wall"
+// Particles of a species, structure of arrays:
+//   pos    float4 {ox, oy, oz, cell-as-int}   offsets in [0,1) inside the cell
+//   vel    float4 {vx, vy, vz, w}             m/s and macroweight
+//   id     uint64                             keys the Philox streams
+// Charge deposition accumulates 64-bit fixed-point integers per node and species, so the
+// node sums do not depend on the order of the atomic updates.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace pic {
+
+constexpr int kMaxSpecies = 4;
+constexpr int kMaxBoxes = 8;
+
+enum NodeKind : uint8_t { kFree = 0, kFixed = 1, kMirror = 2, kAlias = 3 };
+
+// device error word bits (read back by pic_last_error)
+enum DevError : unsigned {
+    kErrCapacity = 1u << 0,    // an append would exceed the species capacity
+    kErrBarrierTimeout = 1u << 1,  // an mbarrier wait ran out of iterations
+    kErrMergeTruncated = 1u << 2,  // a merge cell held more particles than the per-cell cap
+    kErrNaN = 1u << 3,
+};
+
+struct GridDev {
+    int ni, nj, nk;       // nodes
+    int ci, cj, ck;       // cells per axis (n-1)
+    int nv, nc;           // node and cell totals
+    int periodic[3];
+    float dx[3], inv_dx[3];
+    double x0[3], xm[3], dxd[3];
+    int n_boxes;
+    float box_lo[kMaxBoxes][3], box_hi[kMaxBoxes][3];  // absorbing objects, absolute coordinates
+};
+
+struct SpeciesDev {
+    float4* pos;
+    float4* vel;
+    unsigned long long* id;
+    int* counts;  // [0] n, [1] pending appends, [2] dead, [3] holes, [4] movers
+    int* dead;    // dead particle indices of the last push
+    int* holes;   // compaction scratch
+    unsigned long long* acc;  // fixed-point number-density accumulators, one per node
+    int capacity;
+};
+
+// ------------------------------------------------------------------------------------
+// Philox-4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11)
+// ------------------------------------------------------------------------------------
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
+#pragma unroll
+    for (int r = 0; r < 10; r++) {
+        unsigned hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+        unsigned hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+        c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+        k.x += 0x9E3779B9u;
+        k.y += 0xBB67AE85u;
+    }
+    return c;
+}
+// uniform in (0,1): ((x >> 9) + 0.5) * 2^-23, 24 significant bits, exact in FP32
+__device__ __forceinline__ float u01(unsigned x) { return ((float)(x >> 9) + 0.5f) * (1.0f / 8388608.0f); }
+
+// splitmix64 finaliser (Steele, Lea, Flood 2014): ids of collision products
+__device__ __forceinline__ unsigned long long child_id(unsigned long long parent, unsigned step, unsigned kind) {
+    unsigned long long x = parent + 0x9E3779B97F4A7C15ull * ((((unsigned long long)step) << 2) | kind);
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+
+__device__ __forceinline__ void set_error(unsigned* err, unsigned bit) {
+    if (err) atomicOr(err, bit);
+}
+
+// cell index -> (i, j, k)
+__device__ __forceinline__ void cell_ijk(const GridDev& g, int c, int& i, int& j, int& k) {
+    int cij = g.ci * g.cj;
+    k = c / cij;
+    int r = c - k * cij;
+    j = r / g.ci;
+    i = r - j * g.ci;
+}
+// base node of cell (i,j,k)
+__device__ __forceinline__ int cell_base_node(const GridDev& g, int i, int j, int k) {
+    return (k * g.nj + j) * g.ni + i;
+}
+
+}  // namespace pic

@@ -1,0 +1,446 @@
+// Node-field kernels: charge density, E = -grad(phi), and the Poisson solvers.
+//
+// Reference behaviour followed (Misquic/Engineering-degree-in-Plasma-Simulations, ch4/v3/src):
+//   node volumes   World::computeNodeVolumes          World.cpp:353-366
+//   den, rho       Species::computeNumberDensity      Species.cpp:401-416; World::computeChargeDensity World.cpp:193-200
+//   moving average Field::updateMovingAverage         Field.h:245-261
+//   E field        PotentialSolver::computeEF         PotentialSolver.cpp:354-408
+//   Poisson        PotentialSolver::solveGS / solveNRPCG, PotentialSolver.cpp:69-313
+//
+// The Poisson equation is solved on the reduced system of FREE nodes: for a FREE node p and a
+// face neighbour q (periodic wrap applied), a FIXED q contributes its value to the right-hand
+// side, a MIRROR q (a reference Neumann wall, which copies its inner neighbour) equals phi_p and
+// drops out of both sides, and a FREE q is an unknown.  L phi = rho/eps0 with
+//   (L x)_p = D_p x_p - sum_{q FREE or FIXED} c_q x_q,   D_p = sum_{q not MIRROR} c_q,  c = 1/dx^2.
+// kind[n] (uint16): bits 0-1 node kind, bits 2-7 "neighbour d is MIRROR", bits 8-13
+// "neighbour d is FIXED"; direction order -x +x -y +y -z +z.
+#include "pic_kernels.h"
+
+namespace pic {
+
+constexpr double kEps0 = 8.85418782e-12;  // ch4/v3/src/all.h:16
+
+__device__ __forceinline__ void node_ijk(const GridDev& g, int n, int& i, int& j, int& k) {
+    int nij = g.ni * g.nj;
+    k = n / nij;
+    int r = n - k * nij;
+    j = r / g.ni;
+    i = r - j * g.ni;
+}
+// neighbour index along an axis with periodic wrap (the copy at n-1 folds onto 0)
+__device__ __forceinline__ int wrap_m(int c, int n, int per) { return (per && c == 0) ? n - 2 : c - 1; }
+__device__ __forceinline__ int wrap_p(int c, int n, int per) { return (per && c + 1 >= n - 1) ? 0 : c + 1; }
+
+struct Stencil {
+    int q[6];
+    float c[6];
+};
+__device__ __forceinline__ void stencil(const GridDev& g, int i, int j, int k, Stencil& s) {
+    int nij = g.ni * g.nj;
+    int im = wrap_m(i, g.ni, g.periodic[0]), ip = wrap_p(i, g.ni, g.periodic[0]);
+    int jm = wrap_m(j, g.nj, g.periodic[1]), jp = wrap_p(j, g.nj, g.periodic[1]);
+    int km = wrap_m(k, g.nk, g.periodic[2]), kp = wrap_p(k, g.nk, g.periodic[2]);
+    int row = k * nij + j * g.ni;
+    s.q[0] = row + im;
+    s.q[1] = row + ip;
+    s.q[2] = k * nij + jm * g.ni + i;
+    s.q[3] = k * nij + jp * g.ni + i;
+    s.q[4] = km * nij + j * g.ni + i;
+    s.q[5] = kp * nij + j * g.ni + i;
+    float cx = g.inv_dx[0] * g.inv_dx[0], cy = g.inv_dx[1] * g.inv_dx[1], cz = g.inv_dx[2] * g.inv_dx[2];
+    s.c[0] = s.c[1] = cx;
+    s.c[2] = s.c[3] = cy;
+    s.c[4] = s.c[5] = cz;
+}
+
+// ------------------------------------------------------------------------------------
+// charge density: fixed-point number density -> den_s (per species) and rho
+// ------------------------------------------------------------------------------------
+__global__ void k_finalize_rho(FinalizeArgs a) {
+    const GridDev& g = a.g;
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
+        int i, j, k;
+        node_ijk(g, n, i, j, k);
+        int ijk[3] = {i, j, k}, nn[3] = {g.ni, g.nj, g.nk};
+        bool alias = false;
+        unsigned fold = 0;
+        double vol = g.dxd[0] * g.dxd[1] * g.dxd[2];
+        for (int d = 0; d < 3; d++) {
+            if (g.periodic[d]) {
+                if (ijk[d] == nn[d] - 1) alias = true;
+                if (ijk[d] == 0) fold |= 1u << d;
+            } else if (ijk[d] == 0 || ijk[d] == nn[d] - 1) {
+                vol *= 0.5;
+            }
+        }
+        if (alias) continue;  // written by the node it copies
+        int stride[3] = {1, g.ni, g.ni * g.nj};
+        double rho = 0;
+        float den_out[kMaxSpecies];
+        for (int s = 0; s < a.ns; s++) {
+            if (!a.fresh[s]) {
+                // not deposited since the last call (subcycled species): keep its density
+                den_out[s] = a.den[s][n];
+                rho += (double)a.charge[s] * (double)den_out[s];
+                continue;
+            }
+            unsigned long long tot = 0;
+            for (unsigned m = 0; m < 8; m++) {
+                if (m & ~fold) continue;
+                int node = n;
+                for (int d = 0; d < 3; d++)
+                    if (m & (1u << d)) node += (nn[d] - 1) * stride[d];
+                tot += a.acc[s][node];
+                a.acc[s][node] = 0ull;
+            }
+            double den = (double)tot * (double)a.inv_scale[s] / vol;
+            den_out[s] = (float)den;
+            rho += (double)a.charge[s] * den;
+        }
+        for (unsigned m = 0; m < 8; m++) {
+            if (m & ~fold) continue;
+            int node = n;
+            for (int d = 0; d < 3; d++)
+                if (m & (1u << d)) node += (nn[d] - 1) * stride[d];
+            for (int s = 0; s < a.ns; s++)
+                if (a.fresh[s]) a.den[s][node] = den_out[s];
+            a.rho[node] = (float)rho;
+        }
+    }
+}
+void launch_finalize_rho(const FinalizeArgs& a, cudaStream_t s, int grid) { k_finalize_rho<<<grid, 256, 0, s>>>(a); }
+
+// avg = a*avg + b*den  (Field::updateMovingAverage with the sample count handled on the host)
+__global__ void k_den_avg(float* avg, const float* den, int nv, float a, float b) {
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nv; n += gridDim.x * blockDim.x)
+        avg[n] = a * avg[n] + b * den[n];
+}
+void launch_den_avg(float* avg, const float* den, int nv, float a, float b, cudaStream_t s, int grid) {
+    k_den_avg<<<grid, 256, 0, s>>>(avg, den, nv, a, b);
+}
+
+// ------------------------------------------------------------------------------------
+// E = -grad(phi): central inside, second-order one-sided on non-periodic faces
+// ------------------------------------------------------------------------------------
+__global__ void k_efield(GridDev g, const double* __restrict__ phi, float4* __restrict__ ef) {
+    int stride[3] = {1, g.ni, g.ni * g.nj}, nn[3] = {g.ni, g.nj, g.nk};
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
+        int ijk[3];
+        node_ijk(g, n, ijk[0], ijk[1], ijk[2]);
+        float e[3];
+        for (int d = 0; d < 3; d++) {
+            int c = ijk[d], st = stride[d], N = nn[d];
+            double inv2 = 1.0 / (2.0 * g.dxd[d]);
+            double v;
+            if (g.periodic[d]) {
+                int cc = (c == N - 1) ? 0 : c;
+                int base = n - (c - cc) * st;
+                int im = base + (((cc == 0) ? N - 2 : cc - 1) - cc) * st;
+                int ip = base + (((cc + 1 == N - 1) ? 0 : cc + 1) - cc) * st;
+                v = (phi[im] - phi[ip]) * inv2;
+            } else if (c == 0) {
+                v = (3 * phi[n] - 4 * phi[n + st] + phi[n + 2 * st]) * inv2;
+            } else if (c == N - 1) {
+                v = (-phi[n - 2 * st] + 4 * phi[n - st] - 3 * phi[n]) * inv2;
+            } else {
+                v = (phi[n - st] - phi[n + st]) * inv2;
+            }
+            e[d] = (float)v;
+        }
+        ef[n] = make_float4(e[0], e[1], e[2], 0.f);
+    }
+}
+void launch_efield(const GridDev& g, const double* phi, float4* ef, cudaStream_t s, int grid) {
+    k_efield<<<grid, 256, 0, s>>>(g, phi, ef);
+}
+
+// ------------------------------------------------------------------------------------
+// block reduction of up to four doubles into per-block partial slots
+// ------------------------------------------------------------------------------------
+template <int N>
+__device__ __forceinline__ void block_partials(double (&v)[N], double* part, int nslots_stride) {
+    __shared__ double s[N][8];
+#pragma unroll
+    for (int c = 0; c < N; c++) {
+        double x = v[c];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if ((threadIdx.x & 31) == 0) s[c][threadIdx.x >> 5] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < N) {
+        double x = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) x += s[threadIdx.x][w];
+        part[threadIdx.x * nslots_stride + blockIdx.x] = x;
+    }
+    __syncthreads();
+}
+// every block sums the same partials in the same order: identical scalars everywhere
+__device__ __forceinline__ double sum_partials(const double* part, int nblocks) {
+    __shared__ double s[8];
+    double x = 0;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) x += part[b];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = x;
+    __syncthreads();
+    double t = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += s[w];
+    __syncthreads();
+    return t;
+}
+
+// ------------------------------------------------------------------------------------
+// FP64 residual of the reduced system, optionally after phi += e (ping-pong buffers)
+//   r = b - L phi,  b = rho/eps0 + sum_{FIXED q} c_q phi_q ; partials: |r|^2, |b|^2
+// ------------------------------------------------------------------------------------
+__global__ void k_residual(GridDev g, const double* __restrict__ phi_in, double* __restrict__ phi_out,
+                           const float* __restrict__ e, const float* __restrict__ rho,
+                           const uint16_t* __restrict__ kind, float* __restrict__ r, double* part, int apply_e) {
+    double acc[2] = {0.0, 0.0};
+    const double inv_eps0 = 1.0 / kEps0;
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
+        uint16_t kd = kind[n];
+        if ((kd & 3) != kFree) {
+            if (apply_e) phi_out[n] = phi_in[n];
+            r[n] = 0.f;
+            continue;
+        }
+        int i, j, k;
+        node_ijk(g, n, i, j, k);
+        Stencil s;
+        stencil(g, i, j, k, s);
+        double vp = phi_in[n] + (apply_e ? (double)e[n] : 0.0);
+        double diag = 0, off = 0, bfix = 0;
+#pragma unroll
+        for (int d = 0; d < 6; d++) {
+            if (kd & (1u << (2 + d))) continue;  // mirror wall: equals phi_p
+            double c = (double)s.c[d];
+            int q = s.q[d];
+            diag += c;
+            double vq = phi_in[q] + (apply_e ? (double)e[q] : 0.0);
+            off += c * vq;
+            if (kd & (1u << (8 + d))) bfix += c * vq;
+        }
+        double b = (double)rho[n] * inv_eps0 + bfix;
+        double res = (double)rho[n] * inv_eps0 - (diag * vp - off);
+        if (apply_e) phi_out[n] = vp;
+        r[n] = (float)res;
+        acc[0] += res * res;
+        acc[1] += b * b;
+    }
+    block_partials<2>(acc, part, kParts);
+}
+void launch_residual(const GridDev& g, SolveWork& w, int apply_e, cudaStream_t s, int grid) {
+    const double* in = w.phi;
+    double* out = apply_e ? w.phi_alt : w.phi;
+    k_residual<<<grid, 256, 0, s>>>(g, in, out, w.e, w.rho, reinterpret_cast<const uint16_t*>(w.kind), w.r, w.part,
+                                     apply_e);
+    if (apply_e) {
+        double* t = w.phi;
+        w.phi = w.phi_alt;
+        w.phi_alt = t;
+    }
+}
+// sums nslots consecutive partial rows (grid-sized) into out[0..nslots)
+__global__ void k_reduce_partials(const double* part, int nblocks, double* out) {
+    double t = sum_partials(part + blockIdx.x * kParts, nblocks);
+    if (threadIdx.x == 0) out[blockIdx.x] = t;
+}
+void launch_reduce_partials(const double* part, int nslots, int nblocks, double* out, cudaStream_t s) {
+    // slot rows are kParts apart; the producing kernel wrote its first nblocks entries
+    k_reduce_partials<<<nslots, 256, 0, s>>>(part, nblocks, out);
+}
+
+// ------------------------------------------------------------------------------------
+// FP32 red-black SOR on the correction equation L e = r (e = 0 on non-FREE nodes)
+// ------------------------------------------------------------------------------------
+__global__ void k_rbsor(GridDev g, float* __restrict__ e, const float* __restrict__ r,
+                        const uint16_t* __restrict__ kind, float omega, int color) {
+    // thread t -> (m, j, k) with i = i0 + 2m of the requested colour
+    int half = (g.ni + 1) / 2;
+    int total = half * g.nj * g.nk;
+    float cx = g.inv_dx[0] * g.inv_dx[0], cy = g.inv_dx[1] * g.inv_dx[1], cz = g.inv_dx[2] * g.inv_dx[2];
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+        int m = t % half, jk = t / half;
+        int j = jk % g.nj, k = jk / g.nj;
+        int i = 2 * m + ((color + j + k) & 1);
+        if (i >= g.ni) continue;
+        int n = (k * g.nj + j) * g.ni + i;
+        uint16_t kd = kind[n];
+        if ((kd & 3) != kFree) continue;
+        Stencil s;
+        stencil(g, i, j, k, s);
+        float diag = 2.f * (cx + cy + cz), off = 0.f;
+#pragma unroll
+        for (int d = 0; d < 6; d++) {
+            if (kd & (1u << (2 + d))) {
+                diag -= s.c[d];
+                continue;
+            }
+            off += s.c[d] * e[s.q[d]];
+        }
+        float en = e[n];
+        e[n] = en + omega * ((r[n] + off) / diag - en);
+    }
+}
+void launch_rbsor_sweeps(const GridDev& g, SolveWork& w, float omega, int sweeps, cudaStream_t s, int grid) {
+    const uint16_t* kd = reinterpret_cast<const uint16_t*>(w.kind);
+    for (int it = 0; it < sweeps; it++) {
+        k_rbsor<<<grid, 256, 0, s>>>(g, w.e, w.r, kd, omega, 0);
+        k_rbsor<<<grid, 256, 0, s>>>(g, w.e, w.r, kd, omega, 1);
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// FP32 flexible (Polak-Ribiere) Jacobi-preconditioned CG on L e = r, e0 = 0.
+// Two kernels per iteration; d is ping-ponged so the direction update fuses into the SpMV:
+//   K1: d' = z + beta d ; q = L0 d' ; partial d'.q          (beta = 0 on the first iteration)
+//   K2: alpha = rz/dq ; e += alpha d' ; r -= alpha q ; z' = r/D ; partials r.z', r.z, r.r
+// scalars: scal[0..1] rz (double-buffered by iteration parity); flag[0] set when r.r <= target
+// ------------------------------------------------------------------------------------
+__device__ __forceinline__ float diag_of(uint16_t kd, const Stencil& s) {
+    float dg = 0.f;
+#pragma unroll
+    for (int d = 0; d < 6; d++)
+        if (!(kd & (1u << (2 + d)))) dg += s.c[d];
+    return dg;
+}
+__global__ void k_pcg_init(GridDev g, const float* __restrict__ r, float* __restrict__ z, float* __restrict__ e,
+                           const uint16_t* __restrict__ kind, double* part, int* flag) {
+    double acc[1] = {0.0};
+    if (blockIdx.x == 0 && threadIdx.x == 0) flag[0] = 0;
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
+        uint16_t kd = kind[n];
+        e[n] = 0.f;
+        if ((kd & 3) != kFree) {
+            z[n] = 0.f;
+            continue;
+        }
+        int i, j, k;
+        node_ijk(g, n, i, j, k);
+        Stencil s;
+        stencil(g, i, j, k, s);
+        float zz = r[n] / diag_of(kd, s);
+        z[n] = zz;
+        acc[0] += (double)r[n] * (double)zz;
+    }
+    block_partials<1>(acc, part + 1 * kParts, kParts);  // slot 1: r.z
+}
+__global__ void k_pcg_k1(GridDev g, const float* __restrict__ z, const float* __restrict__ d_in,
+                         float* __restrict__ d_out, float* __restrict__ q, const uint16_t* __restrict__ kind,
+                         double* part, double* scal, int* flag, int it, double target_rr) {
+    // previous iteration's r.z', r.z and r.r
+    double rz_new = sum_partials(part + 1 * kParts, gridDim.x);
+    double beta = 0.0;
+    if (it > 0) {
+        double rzo = sum_partials(part + 2 * kParts, gridDim.x);
+        double rr = sum_partials(part + 3 * kParts, gridDim.x);
+        if (rr <= target_rr || flag[0]) {
+            if (blockIdx.x == 0 && threadIdx.x == 0) flag[0] = 1;
+            return;
+        }
+        double rz_old = scal[(it - 1) & 1];
+        beta = (rz_new - rzo) / rz_old;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) scal[it & 1] = rz_new;
+    double acc[1] = {0.0};
+    float fb = (float)beta;
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
+        uint16_t kd = kind[n];
+        if ((kd & 3) != kFree) {
+            d_out[n] = 0.f;
+            q[n] = 0.f;
+            continue;
+        }
+        int i, j, k;
+        node_ijk(g, n, i, j, k);
+        Stencil s;
+        stencil(g, i, j, k, s);
+        float dn = z[n] + fb * d_in[n];
+        float dg = 0.f, off = 0.f;
+#pragma unroll
+        for (int d = 0; d < 6; d++) {
+            if (kd & (1u << (2 + d))) continue;
+            dg += s.c[d];
+            int qq = s.q[d];
+            off += s.c[d] * (z[qq] + fb * d_in[qq]);  // zero on non-FREE neighbours
+        }
+        float qv = dg * dn - off;
+        d_out[n] = dn;
+        q[n] = qv;
+        acc[0] += (double)dn * (double)qv;
+    }
+    block_partials<1>(acc, part + 0 * kParts, kParts);  // slot 0: d.q
+}
+__global__ void k_pcg_k2(GridDev g, const float* __restrict__ d, const float* __restrict__ q, float* __restrict__ e,
+                         float* __restrict__ r, float* __restrict__ z, const uint16_t* __restrict__ kind, double* part,
+                         double* scal, int* flag, int it) {
+    if (flag[0]) return;
+    double dq = sum_partials(part + 0 * kParts, gridDim.x);
+    double rz = scal[it & 1];
+    float alpha = dq != 0.0 ? (float)(rz / dq) : 0.f;
+    double acc[3] = {0.0, 0.0, 0.0};
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
+        uint16_t kd = kind[n];
+        if ((kd & 3) != kFree) continue;
+        int i, j, k;
+        node_ijk(g, n, i, j, k);
+        Stencil s;
+        stencil(g, i, j, k, s);
+        e[n] += alpha * d[n];
+        float rn = r[n] - alpha * q[n];
+        r[n] = rn;
+        float zo = z[n];
+        float zn = rn / diag_of(kd, s);
+        z[n] = zn;
+        acc[0] += (double)rn * (double)zn;
+        acc[1] += (double)rn * (double)zo;
+        acc[2] += (double)rn * (double)rn;
+    }
+    __syncthreads();
+    double a1[1] = {acc[0]}, a2[1] = {acc[1]}, a3[1] = {acc[2]};
+    block_partials<1>(a1, part + 1 * kParts, kParts);
+    block_partials<1>(a2, part + 2 * kParts, kParts);
+    block_partials<1>(a3, part + 3 * kParts, kParts);
+}
+void launch_pcg_init(const GridDev& g, SolveWork& w, cudaStream_t s, int grid) {
+    k_pcg_init<<<grid, 256, 0, s>>>(g, w.r, w.z, w.e, reinterpret_cast<const uint16_t*>(w.kind), w.part, w.flag);
+    cudaMemsetAsync(w.d, 0, sizeof(float) * g.nv, s);
+}
+// one iteration; d ping-pongs between w.d and w.q's partner buffer (w.phi_alt is FP64 and not used here)
+void launch_pcg_iter_impl(const GridDev& g, SolveWork& w, float* d_in, float* d_out, int it, double target_rr,
+                          cudaStream_t s, int grid) {
+    const uint16_t* kd = reinterpret_cast<const uint16_t*>(w.kind);
+    k_pcg_k1<<<grid, 256, 0, s>>>(g, w.z, d_in, d_out, w.q, kd, w.part, w.scal, w.flag, it, target_rr);
+    k_pcg_k2<<<grid, 256, 0, s>>>(g, d_out, w.q, w.e, w.r, w.z, kd, w.part, w.scal, w.flag, it);
+}
+
+// ------------------------------------------------------------------------------------
+// MIRROR nodes take the clamped interior value, then ALIAS nodes their periodic source
+// ------------------------------------------------------------------------------------
+__global__ void k_fill_mirror(GridDev g, double* phi, const uint16_t* kind) {
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
+        if ((kind[n] & 3) != kMirror) continue;
+        int ijk[3], nn[3] = {g.ni, g.nj, g.nk};
+        node_ijk(g, n, ijk[0], ijk[1], ijk[2]);
+        for (int d = 0; d < 3; d++)
+            if (!g.periodic[d]) ijk[d] = ijk[d] < 1 ? 1 : (ijk[d] > nn[d] - 2 ? nn[d] - 2 : ijk[d]);
+        phi[n] = phi[(ijk[2] * g.nj + ijk[1]) * g.ni + ijk[0]];
+    }
+}
+__global__ void k_fill_alias(GridDev g, double* phi, const uint16_t* kind) {
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
+        if ((kind[n] & 3) != kAlias) continue;
+        int ijk[3], nn[3] = {g.ni, g.nj, g.nk};
+        node_ijk(g, n, ijk[0], ijk[1], ijk[2]);
+        for (int d = 0; d < 3; d++)
+            if (g.periodic[d] && ijk[d] == nn[d] - 1) ijk[d] = 0;
+        phi[n] = phi[(ijk[2] * g.nj + ijk[1]) * g.ni + ijk[0]];
+    }
+}
+void launch_fill_aux(const GridDev& g, double* phi, const uint8_t* kind, cudaStream_t s, int grid) {
+    const uint16_t* kd = reinterpret_cast<const uint16_t*>(kind);
+    k_fill_mirror<<<grid, 256, 0, s>>>(g, phi, kd);
+    k_fill_alias<<<grid, 256, 0, s>>>(g, phi, kd);
+}
+
+}  // namespace pic

@@ -1,0 +1,103 @@
+// Host-side launch wrappers shared between the kernel translation units and the C ABI.
+#pragma once
+#include "pic_common.cuh"
+
+namespace pic {
+
+// Electron-impact collisions against a uniform background gas (fused into the electron push)
+struct CollDev {
+    int enabled;
+    float p_null;            // n_n (sigma v)_max dt : candidate probability
+    float sigv_max;          // (sigma v)_max [m^3/s]
+    float sig_n;             // sqrt(k T_n / m_n): neutral thermal speed per axis
+    float m_n, m_e;
+    float E_precalc_rel_eV;  // 0.5 m_red / q
+    float half_mred;         // 0.5 m_red
+    float E_precalc_ele_eV;  // m_e 0.5 / q
+    float E_ion_eV, B_inc, two_q_over_me;
+    int sig_kind;            // 0 reference fit, 1 Lotz
+    float sig_a, sig_b, sig_c, sig_A;
+    const float* tE;         // sigma_coll table energies [eV], ascending
+    const float* tS;         // sigma_coll table values [m^2]
+    int tn;
+    uint2 key;
+    unsigned step;
+    SpeciesDev ion;          // ion products are appended here
+    unsigned long long* stats;  // [0] candidates [1] collisions [2] ionisations [3] products lost
+};
+
+struct PushArgs {
+    GridDev g;
+    SpeciesDev sp;
+    const float4* ef;
+    float qm_dt;     // q/m dt
+    float dtdx[3];   // dt/dx per axis
+    int deposit;     // scatter the weight at the new position
+    float dep_scale; // fixed-point scale (power of two)
+    int staged;      // allow TMA-staged E tiles
+    unsigned* err;
+    CollDev coll;
+};
+
+// particles
+void launch_push(const PushArgs& a, cudaStream_t s, int grid);
+void launch_commit_appends(SpeciesDev sp, unsigned* err, cudaStream_t s);
+void launch_compact(SpeciesDev sp, cudaStream_t s, int grid);
+void launch_sort(const GridDev& g, SpeciesDev sp, float4* pos_alt, float4* vel_alt, unsigned long long* id_alt,
+                 int* cell_count, int* cell_start, int* scan_aux, cudaStream_t s, int grid);
+void launch_from_abs(const GridDev& g, SpeciesDev sp, const double* pos, const double* vel, const double* w,
+                     const unsigned long long* id, int n, int rewind, float qm_half_dt, const float4* ef,
+                     cudaStream_t s);
+void launch_to_abs(const GridDev& g, SpeciesDev sp, double* pos, double* vel, double* w, unsigned long long* id,
+                   int n, cudaStream_t s);
+struct LoadArgs {
+    double lo[3], hi[3];   // absolute box
+    float vth;             // sqrt(kT/m) per axis
+    float w_mean, w_sigma; // lognormal weight (sigma 0: constant w_mean)
+    unsigned long long id0;
+    uint2 key;
+    int n;
+};
+void launch_load_uniform(const GridDev& g, SpeciesDev sp, const LoadArgs& la, cudaStream_t s);
+void launch_sums(SpeciesDev sp, double* out, cudaStream_t s, int grid);
+
+// fields
+struct FinalizeArgs {
+    GridDev g;
+    int ns;
+    unsigned long long* acc[kMaxSpecies];
+    float inv_scale[kMaxSpecies];
+    float charge[kMaxSpecies];
+    float* den[kMaxSpecies];
+    int fresh[kMaxSpecies];  // deposited since the last call: rebuild den from the accumulator
+    float* rho;
+};
+void launch_finalize_rho(const FinalizeArgs& a, cudaStream_t s, int grid);
+void launch_efield(const GridDev& g, const double* phi, float4* ef, cudaStream_t s, int grid);
+void launch_kinds(const GridDev& g, uint8_t* kind, cudaStream_t s);
+
+struct SolveWork {
+    double* phi;      // master potential (FIXED nodes hold their values)
+    double* phi_alt;  // ping-pong partner
+    const float* rho;
+    const uint8_t* kind;
+    float* r;         // FP32 residual / right-hand side of the correction equation
+    float* e;         // FP32 correction
+    float* d;         // CG direction
+    float* q;         // CG L d
+    float* z;         // CG preconditioned residual
+    double* part;     // per-block partial sums [kParts * nslots]
+    double* scal;     // device scalars
+    int* flag;        // [0] inner converged
+};
+constexpr int kParts = 1024;
+void launch_residual(const GridDev& g, SolveWork& w, int apply_e, cudaStream_t s, int grid);
+void launch_reduce_partials(const double* part, int nslots, int nblocks, double* out, cudaStream_t s);
+void launch_rbsor_sweeps(const GridDev& g, SolveWork& w, float omega, int sweeps, cudaStream_t s, int grid);
+void launch_pcg_init(const GridDev& g, SolveWork& w, cudaStream_t s, int grid);
+void launch_pcg_iter_impl(const GridDev& g, SolveWork& w, float* d_in, float* d_out, int it, double target_rr,
+                          cudaStream_t s, int grid);
+void launch_fill_aux(const GridDev& g, double* phi, const uint8_t* kind, cudaStream_t s, int grid);
+void launch_den_avg(float* avg, const float* den, int nv, float a, float b, cudaStream_t s, int grid);
+
+}  // namespace pic

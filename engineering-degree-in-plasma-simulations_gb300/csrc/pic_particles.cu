@@ -1,0 +1,871 @@
+// Particle kernels: fused collide + push + deposit, compaction, counting sort by cell,
+// host <-> device conversion and the synthetic loaders.
+//
+// Reference behaviour followed (Misquic/Engineering-degree-in-Plasma-Simulations, ch4/v3/src):
+//   push           Species::advanceElectronsSerial      Species.cpp:356-399
+//   gather         Field<Vec3>::gather                  Field.h:200-232
+//   deposit        Species::computeNumberDensity        Species.cpp:401-416 (Field::scatter, Field.h:156-199)
+//   bounds         World::inBounds / inObject           World.cpp:201-205, 293-301
+//   collisions     MC_MEX_Ionization::collide, IONIZE_1 Interactions.cpp:845-947
+//   creation       Species::addParticle                 Species.cpp:420-434
+//   cell lists     Species::sortIndexes                 Species.cpp:905-915
+#include <climits>
+#include "pic_kernels.h"
+
+namespace pic {
+
+constexpr int kThreads = 256;
+constexpr int kPPT = 4;                     // particles per thread per chunk
+constexpr int kChunk = kThreads * kPPT;     // particles per chunk
+constexpr int kSeg = 512;                   // nodes per staged row segment
+constexpr int kMargin = 2;                  // deposit window starts this many nodes below the gather window
+constexpr size_t kPushSmem = 4 * kSeg * sizeof(float4) + 4 * kSeg * sizeof(unsigned long long);
+constexpr long long kWaitLimit = 1ll << 24;  // mbarrier polls before giving up
+
+// ------------------------------------------------------------------------------------
+// mbarrier + bulk-copy (TMA) helpers
+// ------------------------------------------------------------------------------------
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// global -> shared bulk copy completing on an mbarrier; both addresses 16-byte aligned,
+// size a multiple of 16 bytes (node rows of float4)
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+// bounded wait: returns false if the copies did not land within kWaitLimit polls
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity) {
+    for (long long it = 0; it < kWaitLimit; it++)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+// ------------------------------------------------------------------------------------
+// cross sections (MC_MEX_Ionization::evaluateSigmaColl / evaluateSigmaIon,
+// Interactions.cpp:541-566) in FP32
+// ------------------------------------------------------------------------------------
+__device__ float sigma_coll(const CollDev& c, float E) {
+    int lo = 0, hi = c.tn;  // first index with tE >= E (std::map::lower_bound)
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (__ldg(&c.tE[mid]) < E) lo = mid + 1;
+        else hi = mid;
+    }
+    if (lo == 0) return __ldg(&c.tS[0]);
+    if (lo == c.tn) return __ldg(&c.tS[c.tn - 1]);
+    float x1 = __ldg(&c.tE[lo - 1]), x2 = __ldg(&c.tE[lo]), y1 = __ldg(&c.tS[lo - 1]), y2 = __ldg(&c.tS[lo]);
+    return y1 + (E - x1) * (y2 - y1) / (x2 - x1);
+}
+__device__ float sigma_ion(const CollDev& c, float E) {
+    if (E <= c.E_ion_eV) return 0.f;
+    if (c.sig_kind == 0) return c.sig_a * logf(E / c.sig_b) / E * expf(-c.sig_c / E);
+    float I = c.E_ion_eV, x = E / I;
+    return c.sig_A * logf(x) / (E * I) * (1.f - c.sig_b * expf(-c.sig_c * (x - 1.f)));
+}
+
+// draw stream after the candidate test: blocks 2, 3, ... of (id_lo, id_hi, step, block)
+struct Draws {
+    uint4 ctr;
+    uint2 key;
+    uint4 buf;
+    int pos;
+    __device__ float next() {
+        if (pos >= 4) {
+            ctr.w += 1;
+            buf = philox4x32_10(ctr, key);
+            pos = 0;
+        }
+        unsigned v = pos == 0 ? buf.x : pos == 1 ? buf.y : pos == 2 ? buf.z : buf.w;
+        pos++;
+        return u01(v);
+    }
+};
+
+// MC_MEX_Ionization::newVelocityElecton, LAB form (Interactions.cpp:845-870), keeping the
+// reference's unnormalised perpendicular basis (i x u and u x (i x u)).
+__device__ float3 new_vel_electron(const CollDev& c, float E, float3 u, float r_pow, float r_phi) {
+    const float kPiRef = 3.141592653f;
+    float cos_ksi = (2.f + E - 2.f * powf(1.f + E, r_pow)) / E;
+    float sin_ksi = sqrtf(fmaxf(1.f - cos_ksi * cos_ksi, 0.f));
+    float sp, cp;
+    sincosf(2.f * kPiRef * r_phi, &sp, &cp);
+    float v_mag = sqrtf(E * c.two_q_over_me);
+    float3 a = make_float3(0.f, -u.z, u.y);  // (1,0,0) x u
+    float3 b = make_float3(u.y * a.z - u.z * a.y, u.z * a.x - u.x * a.z, u.x * a.y - u.y * a.x);
+    return make_float3((cos_ksi * u.x + a.x * sin_ksi * sp + b.x * sin_ksi * cp) * v_mag,
+                       (cos_ksi * u.y + a.y * sin_ksi * sp + b.y * sin_ksi * cp) * v_mag,
+                       (cos_ksi * u.z + a.z * sin_ksi * sp + b.z * sin_ksi * cp) * v_mag);
+}
+
+// ------------------------------------------------------------------------------------
+// push helpers
+// ------------------------------------------------------------------------------------
+struct Tile {
+    const float4* etile;  // staged E rows, or nullptr
+    unsigned long long* dtile;
+    int lo;               // first node of the gather window
+    int off[4];           // node offsets of the four rows: 0, ni, ni*nj, ni*nj+ni
+};
+
+__device__ __forceinline__ float4 load_e(const PushArgs& a, const Tile& t, int b, int m, int di) {
+    if (t.etile) return t.etile[m * kSeg + (b - t.lo) + di];
+    return __ldg(&a.ef[b + t.off[m] + di]);
+}
+
+// trilinear gather at (base node b, offsets o): the eight corners of Field::gather
+__device__ __forceinline__ float3 gather_e(const PushArgs& a, const Tile& t, int b, float3 o) {
+    float wx1 = o.x, wx0 = 1.f - o.x, wy1 = o.y, wy0 = 1.f - o.y, wz1 = o.z, wz0 = 1.f - o.z;
+    float4 e000 = load_e(a, t, b, 0, 0), e100 = load_e(a, t, b, 0, 1);
+    float4 e010 = load_e(a, t, b, 1, 0), e110 = load_e(a, t, b, 1, 1);
+    float4 e001 = load_e(a, t, b, 2, 0), e101 = load_e(a, t, b, 2, 1);
+    float4 e011 = load_e(a, t, b, 3, 0), e111 = load_e(a, t, b, 3, 1);
+    float w000 = wx0 * wy0 * wz0, w100 = wx1 * wy0 * wz0, w010 = wx0 * wy1 * wz0, w110 = wx1 * wy1 * wz0;
+    float w001 = wx0 * wy0 * wz1, w101 = wx1 * wy0 * wz1, w011 = wx0 * wy1 * wz1, w111 = wx1 * wy1 * wz1;
+    float3 E;
+    E.x = e000.x * w000 + e100.x * w100 + e010.x * w010 + e110.x * w110 + e001.x * w001 + e101.x * w101 +
+          e011.x * w011 + e111.x * w111;
+    E.y = e000.y * w000 + e100.y * w100 + e010.y * w010 + e110.y * w110 + e001.y * w001 + e101.y * w101 +
+          e011.y * w011 + e111.y * w111;
+    E.z = e000.z * w000 + e100.z * w100 + e010.z * w010 + e110.z * w110 + e001.z * w001 + e101.z * w101 +
+          e011.z * w011 + e111.z * w111;
+    return E;
+}
+
+// advance offsets by v dt/dx, move across cells, wrap periodic axes; returns the new cell or
+// -1 when the particle leaves the domain or enters an absorbing object
+__device__ __forceinline__ int move_particle(const PushArgs& a, int i, int j, int k, float3& o, float3 v) {
+    const GridDev& g = a.g;
+    const float kBelowOne = 0x1.fffffep-1f;
+    float ox = o.x + v.x * a.dtdx[0], oy = o.y + v.y * a.dtdx[1], oz = o.z + v.z * a.dtdx[2];
+    float fx = floorf(ox), fy = floorf(oy), fz = floorf(oz);
+    i += (int)fx;
+    j += (int)fy;
+    k += (int)fz;
+    o.x = fminf(ox - fx, kBelowOne);
+    o.y = fminf(oy - fy, kBelowOne);
+    o.z = fminf(oz - fz, kBelowOne);
+    if (g.periodic[0]) { i %= g.ci; if (i < 0) i += g.ci; }
+    if (g.periodic[1]) { j %= g.cj; if (j < 0) j += g.cj; }
+    if (g.periodic[2]) { k %= g.ck; if (k < 0) k += g.ck; }
+    if (i < 0 || i >= g.ci || j < 0 || j >= g.cj || k < 0 || k >= g.ck) return -1;
+    if (g.n_boxes) {
+        float X = ((float)i + o.x) * g.dx[0], Y = ((float)j + o.y) * g.dx[1], Z = ((float)k + o.z) * g.dx[2];
+        for (int bx = 0; bx < g.n_boxes; bx++)
+            if (X >= g.box_lo[bx][0] && X <= g.box_hi[bx][0] && Y >= g.box_lo[bx][1] && Y <= g.box_hi[bx][1] &&
+                Z >= g.box_lo[bx][2] && Z <= g.box_hi[bx][2])
+                return -1;
+    }
+    return (k * g.cj + j) * g.ci + i;
+}
+
+// eight fixed-point corner contributions of a weight w at offsets o (Field::scatter order)
+__device__ __forceinline__ void corner_fixed(float w, float3 o, float scale, unsigned long long q[8]) {
+    float wx1 = o.x, wx0 = 1.f - o.x, wy1 = o.y, wy0 = 1.f - o.y, wz1 = o.z, wz0 = 1.f - o.z;
+    float s = w * scale;
+    q[0] = __float2ull_rn(s * wx0 * wy0 * wz0);
+    q[1] = __float2ull_rn(s * wx1 * wy0 * wz0);
+    q[2] = __float2ull_rn(s * wx0 * wy1 * wz0);
+    q[3] = __float2ull_rn(s * wx1 * wy1 * wz0);
+    q[4] = __float2ull_rn(s * wx0 * wy0 * wz1);
+    q[5] = __float2ull_rn(s * wx1 * wy0 * wz1);
+    q[6] = __float2ull_rn(s * wx0 * wy1 * wz1);
+    q[7] = __float2ull_rn(s * wx1 * wy1 * wz1);
+}
+
+// commit the eight corner sums of a cell group: into the shared tile when the corner lies in
+// the deposit window, else straight to HBM
+__device__ __forceinline__ void commit_corners(const PushArgs& a, const Tile& t, int b, const unsigned long long q[8]) {
+#pragma unroll
+    for (int m = 0; m < 4; m++)
+#pragma unroll
+        for (int di = 0; di < 2; di++) {
+            unsigned long long v = q[2 * m + di];
+            if (v == 0) continue;
+            int node = b + t.off[m] + di;
+            int loc = b + di - (t.lo - kMargin);
+            if (t.dtile && loc >= 0 && loc < kSeg) atomicAdd(&t.dtile[m * kSeg + loc], v);
+            else atomicAdd(&a.sp.acc[node], v);
+        }
+}
+
+// corner values of one particle -> corner totals of its warp group (lanes that share the
+// cell), reduced with redux.sync on 21-bit limbs so that 64-bit fixed-point sums stay exact
+__device__ __forceinline__ void group_reduce(unsigned gmask, unsigned long long q[8]) {
+    unsigned long long hi = 0;
+#pragma unroll
+    for (int c = 0; c < 8; c++) hi |= q[c] >> 21;
+    bool need1 = __any_sync(0xffffffffu, hi != 0);
+    bool need2 = __any_sync(0xffffffffu, (hi >> 21) != 0);
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+        unsigned long long v = q[c];
+        unsigned long long s = __reduce_add_sync(gmask, (unsigned)(v & 0x1FFFFFull));
+        if (need1) s += (unsigned long long)__reduce_add_sync(gmask, (unsigned)((v >> 21) & 0x1FFFFFull)) << 21;
+        if (need2) s += (unsigned long long)__reduce_add_sync(gmask, (unsigned)(v >> 42)) << 42;
+        q[c] = s;
+    }
+}
+
+// append one particle to a species at (committed count + pending slot)
+__device__ __forceinline__ bool append_particle(const SpeciesDev& sp, int n_committed, float4 p, float4 v,
+                                                unsigned long long id, unsigned* err) {
+    int slot = atomicAdd(&sp.counts[1], 1);
+    int dst = n_committed + slot;
+    if (dst >= sp.capacity) {
+        set_error(err, kErrCapacity);
+        return false;
+    }
+    sp.pos[dst] = p;
+    sp.vel[dst] = v;
+    sp.id[dst] = id;
+    return true;
+}
+
+// ------------------------------------------------------------------------------------
+// fused collide + push + deposit
+// ------------------------------------------------------------------------------------
+template <bool kMcc>
+__global__ void __launch_bounds__(kThreads) k_push(PushArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    float4* etile = reinterpret_cast<float4*>(smem);
+    unsigned long long* dtile = reinterpret_cast<unsigned long long*>(smem + 4 * kSeg * sizeof(float4));
+    __shared__ __align__(8) unsigned long long bar;
+    __shared__ int s_min[kThreads / 32], s_max[kThreads / 32];
+    __shared__ int s_lo, s_hi, s_fail;
+
+    const GridDev& g = a.g;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int n = a.sp.counts[0];
+    const int ion_n = kMcc ? a.coll.ion.counts[0] : 0;
+    const int nchunks = (n + kChunk - 1) / kChunk;
+    const int nij = g.ni * g.nj;
+    unsigned st_cand = 0, st_coll = 0, st_ion = 0, st_lost = 0;
+
+    if (tid == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    unsigned phase = 0;
+
+    for (int ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
+        const int base = ch * kChunk;
+        float4 P[kPPT], V[kPPT];
+        int bn[kPPT];
+        int lmin = INT_MAX, lmax = -1;
+#pragma unroll
+        for (int q = 0; q < kPPT; q++) {
+            int p = base + q * kThreads + tid;
+            bn[q] = -1;
+            if (p < n) {
+                P[q] = a.sp.pos[p];
+                V[q] = a.sp.vel[p];
+                int c = __float_as_int(P[q].w);
+                if (c >= 0) {
+                    int i, j, k;
+                    cell_ijk(g, c, i, j, k);
+                    bn[q] = cell_base_node(g, i, j, k);
+                    lmin = min(lmin, bn[q]);
+                    lmax = max(lmax, bn[q]);
+                }
+            }
+        }
+        lmin = __reduce_min_sync(0xffffffffu, lmin);
+        lmax = __reduce_max_sync(0xffffffffu, lmax);
+        if (lane == 0) {
+            s_min[warp] = lmin;
+            s_max[warp] = lmax;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            int mn = INT_MAX, mx = -1;
+            for (int w = 0; w < kThreads / 32; w++) {
+                mn = min(mn, s_min[w]);
+                mx = max(mx, s_max[w]);
+            }
+            s_lo = mn;
+            s_hi = mx;
+            s_fail = 0;
+        }
+        __syncthreads();
+        const int lo = s_lo, hi = s_hi;
+        const bool use_tile = a.staged && hi >= 0 && (hi - lo + 2) <= kSeg - kMargin;
+        Tile t;
+        t.lo = lo;
+        t.off[0] = 0;
+        t.off[1] = g.ni;
+        t.off[2] = nij;
+        t.off[3] = nij + g.ni;
+        t.etile = nullptr;
+        t.dtile = nullptr;
+        if (use_tile) {
+            if (tid == 0) {
+                // rows [lo + off_m, lo + off_m + L) of the node field, L = span + 2 nodes
+                unsigned bytes = (unsigned)(hi - lo + 2) * (unsigned)sizeof(float4);
+                fence_proxy_async();
+                mbar_expect_tx(&bar, 4 * bytes);
+#pragma unroll
+                for (int m = 0; m < 4; m++) bulk_g2s(etile + m * kSeg, a.ef + lo + t.off[m], bytes, &bar);
+            }
+            for (int x = tid; x < 4 * kSeg; x += kThreads) dtile[x] = 0ull;
+            bool ok = mbar_wait_bounded(&bar, phase);
+            if (!ok) atomicExch(&s_fail, 1);
+            phase ^= 1u;
+            __syncthreads();
+            if (s_fail) {
+                // the copies did not complete in time: record it, wait once more (bounded) for
+                // the copies in flight, and leave without touching the tile
+                if (tid == 0) set_error(a.err, kErrBarrierTimeout);
+                mbar_wait_bounded(&bar, phase ^ 1u);
+                return;
+            }
+            t.etile = etile;
+            t.dtile = dtile;
+        }
+
+#pragma unroll
+        for (int q = 0; q < kPPT; q++) {
+            const int p = base + q * kThreads + tid;
+            int newc = -1;
+            float3 o = make_float3(P[q].x, P[q].y, P[q].z);
+            float3 v = make_float3(V[q].x, V[q].y, V[q].z);
+            const float w = V[q].w;
+            if (bn[q] >= 0) {
+                int c = __float_as_int(P[q].w), i, j, k;
+                cell_ijk(g, c, i, j, k);
+                bool product = false;
+                float3 po, pv, nv;
+                unsigned long long pid = 0;
+                if (kMcc) {
+                    // ---- electron-impact collision against the background gas ----
+                    const CollDev& cd = a.coll;
+                    unsigned long long id = a.sp.id[p];
+                    uint4 ctr = make_uint4((unsigned)id, (unsigned)(id >> 32), cd.step, 0u);
+                    uint4 r0 = philox4x32_10(ctr, cd.key);
+                    if (u01(r0.x) < cd.p_null) {
+                        st_cand++;
+                        ctr.w = 1u;
+                        uint4 r1 = philox4x32_10(ctr, cd.key);
+                        const float kTwoPi = 6.283185307179586f;
+                        float rr1 = sqrtf(-2.f * logf(u01(r0.y))), rr2 = sqrtf(-2.f * logf(u01(r1.x)));
+                        float s1, c1, s2, c2;
+                        sincosf(kTwoPi * u01(r0.z), &s1, &c1);
+                        sincosf(kTwoPi * u01(r1.y), &s2, &c2);
+                        nv = make_float3(cd.sig_n * rr1 * c1, cd.sig_n * rr1 * s1, cd.sig_n * rr2 * c2);
+                        float3 vr = make_float3(nv.x - v.x, nv.y - v.y, nv.z - v.z);
+                        float v_rel = sqrtf(vr.x * vr.x + vr.y * vr.y + vr.z * vr.z);
+                        float E_rel = cd.E_precalc_rel_eV * v_rel * v_rel;
+                        float sig = sigma_coll(cd, E_rel);
+                        if (u01(r0.w) * cd.sigv_max < sig * v_rel) {
+                            st_coll++;
+                            Draws dr;
+                            dr.ctr = ctr;
+                            dr.ctr.w = 2u;
+                            dr.key = cd.key;
+                            dr.buf = philox4x32_10(dr.ctr, cd.key);
+                            dr.pos = 0;
+                            // MC_MEX_Ionization::collide (Interactions.cpp:885-947)
+                            float E_rel_J = cd.half_mred * v_rel * v_rel;
+                            float P_ion = sigma_ion(cd, E_rel_J / 1.602176565e-19f) / sig;
+                            if (dr.next() <= P_ion) {
+                                float vmag = sqrtf(v.x * v.x + v.y * v.y + v.z * v.z);
+                                float E_inc = vmag * vmag * cd.E_precalc_ele_eV;
+                                if (E_inc >= cd.E_ion_eV) {
+                                    float E_ej = 10.0f * tanf(dr.next() * atanf((E_inc - cd.E_ion_eV) / (2.f * cd.B_inc)));
+                                    float E_sc = E_inc - cd.E_ion_eV - E_ej;
+                                    if (E_sc < 0.f) E_sc = 0.000001f;
+                                    float inv = 1.f / vmag;
+                                    float3 u = make_float3(v.x * inv, v.y * inv, v.z * inv);
+                                    float a1 = dr.next(), a2 = dr.next();
+                                    v = new_vel_electron(cd, E_sc, u, a1, a2);
+                                    float a3 = dr.next(), a4 = dr.next();
+                                    pv = new_vel_electron(cd, E_ej, u, a3, a4);
+                                    ctr.w = 4u;
+                                    uint4 r4 = philox4x32_10(ctr, cd.key);
+                                    po = make_float3(u01(r1.z), u01(r1.w), u01(r4.x));
+                                    pid = id;
+                                    product = true;
+                                    st_ion++;
+                                }
+                            } else {
+                                float inv_sum = 1.f / (cd.m_n + cd.m_e);
+                                float3 cm = make_float3((cd.m_n * nv.x + cd.m_e * v.x) * inv_sum,
+                                                        (cd.m_n * nv.y + cd.m_e * v.y) * inv_sum,
+                                                        (cd.m_n * nv.z + cd.m_e * v.z) * inv_sum);
+                                float cos_ksi = 2.f * dr.next() - 1.f;
+                                float sin_ksi = sqrtf(fmaxf(1.f - cos_ksi * cos_ksi, 0.f));
+                                float se, ce;
+                                sincosf(2.f * 3.141592653f * dr.next(), &se, &ce);
+                                float3 vr2 = make_float3(v_rel * cos_ksi, v_rel * sin_ksi * ce, v_rel * sin_ksi * se);
+                                float f = cd.m_n * inv_sum;
+                                v = make_float3(cm.x - f * vr2.x, cm.y - f * vr2.y, cm.z - f * vr2.z);
+                            }
+                        }
+                    }
+                }
+                // ---- leapfrog push (Species.cpp:369-373) ----
+                float3 E = gather_e(a, t, bn[q], o);
+                v.x += a.qm_dt * E.x;
+                v.y += a.qm_dt * E.y;
+                v.z += a.qm_dt * E.z;
+                newc = move_particle(a, i, j, k, o, v);
+                if (kMcc && product) {
+                    // the ejected electron and the ion: created at a uniform point of the
+                    // parent's cell without velocity rewind; the electron is pushed now
+                    float4 ion_p = make_float4(po.x, po.y, po.z, __int_as_float(c));
+                    float4 ion_v = make_float4(nv.x, nv.y, nv.z, w);
+                    if (!append_particle(a.coll.ion, ion_n, ion_p, ion_v, child_id(pid, a.coll.step, 2), a.err))
+                        st_lost++;
+                    float3 Ep = gather_e(a, t, bn[q], po);
+                    pv.x += a.qm_dt * Ep.x;
+                    pv.y += a.qm_dt * Ep.y;
+                    pv.z += a.qm_dt * Ep.z;
+                    int pc = move_particle(a, i, j, k, po, pv);
+                    if (pc >= 0) {
+                        if (append_particle(a.sp, n, make_float4(po.x, po.y, po.z, __int_as_float(pc)),
+                                            make_float4(pv.x, pv.y, pv.z, w), child_id(pid, a.coll.step, 1), a.err)) {
+                            if (a.deposit) {
+                                unsigned long long qq[8];
+                                corner_fixed(w, po, a.dep_scale, qq);
+                                int pi_, pj, pk;
+                                cell_ijk(g, pc, pi_, pj, pk);
+                                int pb = cell_base_node(g, pi_, pj, pk);
+#pragma unroll
+                                for (int m = 0; m < 4; m++)
+#pragma unroll
+                                    for (int di = 0; di < 2; di++)
+                                        if (qq[2 * m + di]) atomicAdd(&a.sp.acc[pb + t.off[m] + di], qq[2 * m + di]);
+                            }
+                        } else {
+                            st_lost++;
+                        }
+                    }
+                }
+                a.sp.pos[p] = make_float4(o.x, o.y, o.z, __int_as_float(newc));
+                a.sp.vel[p] = make_float4(v.x, v.y, v.z, w);
+            }
+            {
+                // warp-aggregated record of the particles that left the domain
+                const bool died = bn[q] >= 0 && newc < 0;
+                unsigned dm = __ballot_sync(0xffffffffu, died);
+                if (dm) {
+                    int b0 = 0;
+                    if (lane == __ffs(dm) - 1) b0 = atomicAdd(&a.sp.counts[2], __popc(dm));
+                    b0 = __shfl_sync(0xffffffffu, b0, __ffs(dm) - 1);
+                    if (died) a.sp.dead[b0 + __popc(dm & ((1u << lane) - 1u))] = p;
+                }
+            }
+            if (a.deposit) {
+                __syncwarp();
+                unsigned gmask = __match_any_sync(0xffffffffu, newc);
+                unsigned long long qv[8];
+                if (newc >= 0) corner_fixed(w, o, a.dep_scale, qv);
+                else
+                    for (int c = 0; c < 8; c++) qv[c] = 0ull;
+                group_reduce(gmask, qv);
+                if (newc >= 0 && lane == __ffs(gmask) - 1) {
+                    int i, j, k;
+                    cell_ijk(g, newc, i, j, k);
+                    commit_corners(a, t, cell_base_node(g, i, j, k), qv);
+                }
+            }
+        }
+        __syncthreads();
+        if (use_tile && a.deposit) {
+            const int wlo = lo - kMargin;
+            for (int x = tid; x < 4 * kSeg; x += kThreads) {
+                unsigned long long v = dtile[x];
+                if (v) atomicAdd(&a.sp.acc[wlo + t.off[x / kSeg] + (x % kSeg)], v);
+            }
+        }
+        __syncthreads();
+    }
+    if (kMcc) {
+        unsigned v[4] = {st_cand, st_coll, st_ion, st_lost};
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            unsigned x = __reduce_add_sync(0xffffffffu, v[c]);
+            if (lane == 0 && x) atomicAdd(&a.coll.stats[c], (unsigned long long)x);
+        }
+    }
+}
+
+void launch_push(const PushArgs& a, cudaStream_t s, int grid) {
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_push<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPushSmem);
+        cudaFuncSetAttribute(k_push<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPushSmem);
+        attr = true;
+    }
+    if (a.coll.enabled) k_push<true><<<grid, kThreads, kPushSmem, s>>>(a);
+    else k_push<false><<<grid, kThreads, kPushSmem, s>>>(a);
+}
+
+// ------------------------------------------------------------------------------------
+// appends and compaction
+// ------------------------------------------------------------------------------------
+__global__ void k_commit_appends(SpeciesDev sp, unsigned* err) {
+    int n = sp.counts[0], pend = sp.counts[1];
+    int nn = n + pend;
+    if (nn > sp.capacity) {
+        nn = sp.capacity;
+        set_error(err, kErrCapacity);
+    }
+    sp.counts[0] = nn;
+    sp.counts[1] = 0;
+}
+void launch_commit_appends(SpeciesDev sp, unsigned* err, cudaStream_t s) { k_commit_appends<<<1, 1, 0, s>>>(sp, err); }
+
+// dead particles below the new end become holes
+__global__ void k_compact_holes(SpeciesDev sp) {
+    int n = sp.counts[0], nd = sp.counts[2], nnew = n - nd;
+    for (int d = blockIdx.x * blockDim.x + threadIdx.x; d < nd; d += gridDim.x * blockDim.x) {
+        int idx = sp.dead[d];
+        if (idx < nnew) sp.holes[atomicAdd(&sp.counts[3], 1)] = idx;
+    }
+}
+// live particles above the new end fill the holes
+__global__ void k_compact_move(SpeciesDev sp) {
+    int n = sp.counts[0], nd = sp.counts[2], nnew = n - nd;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nd; t += gridDim.x * blockDim.x) {
+        int idx = nnew + t;
+        float4 p = sp.pos[idx];
+        if (__float_as_int(p.w) < 0) continue;
+        int h = sp.holes[atomicAdd(&sp.counts[4], 1)];
+        sp.pos[h] = p;
+        sp.vel[h] = sp.vel[idx];
+        sp.id[h] = sp.id[idx];
+    }
+}
+__global__ void k_compact_finish(SpeciesDev sp) {
+    sp.counts[0] -= sp.counts[2];
+    sp.counts[2] = 0;
+    sp.counts[3] = 0;
+    sp.counts[4] = 0;
+}
+void launch_compact(SpeciesDev sp, cudaStream_t s, int grid) {
+    k_compact_holes<<<grid, 256, 0, s>>>(sp);
+    k_compact_move<<<grid, 256, 0, s>>>(sp);
+    k_compact_finish<<<1, 1, 0, s>>>(sp);
+}
+
+// ------------------------------------------------------------------------------------
+// counting sort by cell (Species::sortIndexes keeps index lists; here the particles
+// themselves are reordered so that each cell is a contiguous run)
+// ------------------------------------------------------------------------------------
+__global__ void k_sort_hist(SpeciesDev sp, int* cnt) {
+    int n = sp.counts[0];
+    int stride = gridDim.x * blockDim.x;
+    int lim = ((n + 31) / 32) * 32;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < lim; p += stride) {
+        int c = p < n ? __float_as_int(sp.pos[p].w) : -1;
+        unsigned m = __match_any_sync(0xffffffffu, c);
+        if (c >= 0 && (threadIdx.x & 31) == __ffs(m) - 1) atomicAdd(&cnt[c], __popc(m));
+    }
+}
+// exclusive scan in three passes over tiles of 2048 counts
+constexpr int kScanTile = 2048;
+__global__ void k_scan_tiles(const int* in, int* out, int* aux, int n) {
+    __shared__ int s[kScanTile];
+    __shared__ int wsum[8];
+    int tile = blockIdx.x, t = threadIdx.x;  // 256 threads, 8 values each
+    int base = tile * kScanTile;
+    for (int x = t; x < kScanTile; x += 256) s[x] = base + x < n ? in[base + x] : 0;
+    __syncthreads();
+    int v[8], run = 0;
+    for (int q = 0; q < 8; q++) {
+        v[q] = run;
+        run += s[t * 8 + q];
+    }
+    // inclusive scan of per-thread totals
+    int lane = t & 31, w = t >> 5, x = run;
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[w] = x;
+    __syncthreads();
+    int woff = 0;
+    for (int q = 0; q < w; q++) woff += wsum[q];
+    int excl = woff + x - run;
+    for (int q = 0; q < 8; q++)
+        if (base + t * 8 + q < n) out[base + t * 8 + q] = excl + v[q];
+    if (t == 255) aux[tile] = woff + x;
+}
+__global__ void k_scan_aux(int* aux, int ntiles) {
+    // single block of 1024 threads, sequential chunks
+    __shared__ int carry;
+    __shared__ int wsum[32];
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int b0 = 0; b0 < ntiles; b0 += 1024) {
+        int idx = b0 + threadIdx.x;
+        int val = idx < ntiles ? aux[idx] : 0;
+        int lane = threadIdx.x & 31, w = threadIdx.x >> 5, x = val;
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) wsum[w] = x;
+        __syncthreads();
+        int woff = 0;
+        for (int q = 0; q < w; q++) woff += wsum[q];
+        int c0 = carry;
+        if (idx < ntiles) aux[idx] = c0 + woff + x - val;
+        __syncthreads();
+        if (threadIdx.x == 1023) carry = c0 + woff + x;
+        __syncthreads();
+    }
+}
+__global__ void k_scan_add(int* out, const int* aux, int n) {
+    int base = blockIdx.x * kScanTile;
+    int add = aux[blockIdx.x];
+    for (int x = threadIdx.x; x < kScanTile; x += 256)
+        if (base + x < n) out[base + x] += add;
+}
+__global__ void k_sort_scatter(SpeciesDev sp, const int* start, int* cursor, float4* pos2, float4* vel2,
+                               unsigned long long* id2) {
+    int n = sp.counts[0];
+    int stride = gridDim.x * blockDim.x;
+    int lim = ((n + 31) / 32) * 32;
+    int lane = threadIdx.x & 31;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < lim; p += stride) {
+        float4 ps = p < n ? sp.pos[p] : make_float4(0, 0, 0, __int_as_float(-1));
+        int c = __float_as_int(ps.w);
+        unsigned m = __match_any_sync(0xffffffffu, c);
+        int leader = __ffs(m) - 1;
+        int b = 0;
+        if (c >= 0 && lane == leader) b = atomicAdd(&cursor[c], __popc(m));
+        b = __shfl_sync(m, b, leader);
+        if (c >= 0) {
+            int dst = start[c] + b + __popc(m & ((1u << lane) - 1u));
+            pos2[dst] = ps;
+            vel2[dst] = sp.vel[p];
+            id2[dst] = sp.id[p];
+        }
+    }
+}
+void launch_sort(const GridDev& g, SpeciesDev sp, float4* pos_alt, float4* vel_alt, unsigned long long* id_alt,
+                 int* cell_count, int* cell_start, int* scan_aux, cudaStream_t s, int grid) {
+    int nc = g.nc;
+    cudaMemsetAsync(cell_count, 0, sizeof(int) * nc, s);
+    k_sort_hist<<<grid, 256, 0, s>>>(sp, cell_count);
+    int ntiles = (nc + kScanTile - 1) / kScanTile;
+    k_scan_tiles<<<ntiles, 256, 0, s>>>(cell_count, cell_start, scan_aux, nc);
+    k_scan_aux<<<1, 1024, 0, s>>>(scan_aux, ntiles);
+    k_scan_add<<<ntiles, 256, 0, s>>>(cell_start, scan_aux, nc);
+    cudaMemsetAsync(cell_count, 0, sizeof(int) * nc, s);
+    k_sort_scatter<<<grid, 256, 0, s>>>(sp, cell_start, cell_count, pos_alt, vel_alt, id_alt);
+}
+
+// ------------------------------------------------------------------------------------
+// host <-> device conversion (Species::addParticle semantics when rewind is set)
+// ------------------------------------------------------------------------------------
+__global__ void k_from_abs(GridDev g, SpeciesDev sp, const double* pos, const double* vel, const double* w,
+                           const unsigned long long* id, int n, int rewind, float qm_half_dt, const float4* ef) {
+    int n0 = sp.counts[0];
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        int dst = n0 + p;
+        if (dst >= sp.capacity) continue;
+        double x[3] = {pos[3 * p], pos[3 * p + 1], pos[3 * p + 2]};
+        float3 v = make_float3((float)vel[3 * p], (float)vel[3 * p + 1], (float)vel[3 * p + 2]);
+        bool ok = !(isnan(x[0]) || isnan(x[1]) || isnan(x[2]) || isnan(v.x) || isnan(v.y) || isnan(v.z));
+        int ijk[3];
+        float o[3];
+        int nc3[3] = {g.ci, g.cj, g.ck};
+        for (int d = 0; d < 3 && ok; d++) {
+            if (g.periodic[d]) {
+                double L = g.xm[d] - g.x0[d];
+                if (x[d] < g.x0[d]) x[d] += L;
+                else if (x[d] >= g.xm[d]) x[d] -= L;
+            }
+            if (x[d] < g.x0[d] || x[d] >= g.xm[d]) ok = false;
+            double lc = (x[d] - g.x0[d]) / g.dxd[d];
+            int c = (int)lc;
+            if (c >= nc3[d]) c = nc3[d] - 1;
+            double f = lc - c;
+            ijk[d] = c;
+            o[d] = fminf((float)f, 0x1.fffffep-1f);
+        }
+        int cell = -1;
+        if (ok) {
+            cell = (ijk[2] * g.cj + ijk[1]) * g.ci + ijk[0];
+            if (g.n_boxes) {
+                float X = ((float)ijk[0] + o[0]) * g.dx[0], Y = ((float)ijk[1] + o[1]) * g.dx[1],
+                      Z = ((float)ijk[2] + o[2]) * g.dx[2];
+                for (int b = 0; b < g.n_boxes; b++)
+                    if (X >= g.box_lo[b][0] && X <= g.box_hi[b][0] && Y >= g.box_lo[b][1] && Y <= g.box_hi[b][1] &&
+                        Z >= g.box_lo[b][2] && Z <= g.box_hi[b][2])
+                        cell = -1;
+            }
+        }
+        if (cell >= 0 && rewind && ef) {
+            // vel -= q/m E dt/2 (Species.cpp:431)
+            PushArgs dummy;
+            dummy.ef = ef;
+            Tile t;
+            t.etile = nullptr;
+            t.dtile = nullptr;
+            t.lo = 0;
+            t.off[0] = 0;
+            t.off[1] = g.ni;
+            t.off[2] = g.ni * g.nj;
+            t.off[3] = g.ni * g.nj + g.ni;
+            float3 E = gather_e(dummy, t, cell_base_node(g, ijk[0], ijk[1], ijk[2]), make_float3(o[0], o[1], o[2]));
+            v.x -= qm_half_dt * E.x;
+            v.y -= qm_half_dt * E.y;
+            v.z -= qm_half_dt * E.z;
+        }
+        sp.pos[dst] = make_float4(o[0], o[1], o[2], __int_as_float(cell));
+        sp.vel[dst] = make_float4(v.x, v.y, v.z, (float)w[p]);
+        sp.id[dst] = id[p];
+        if (cell < 0) sp.dead[atomicAdd(&sp.counts[2], 1)] = dst;
+    }
+}
+__global__ void k_from_abs_count(SpeciesDev sp, int n, unsigned* err) {
+    int nn = sp.counts[0] + n;
+    if (nn > sp.capacity) {
+        nn = sp.capacity;
+        set_error(err, kErrCapacity);
+    }
+    sp.counts[0] = nn;
+}
+void launch_from_abs(const GridDev& g, SpeciesDev sp, const double* pos, const double* vel, const double* w,
+                     const unsigned long long* id, int n, int rewind, float qm_half_dt, const float4* ef,
+                     cudaStream_t s) {
+    int grid = (n + 255) / 256;
+    if (grid > 4096) grid = 4096;
+    if (grid < 1) grid = 1;
+    k_from_abs<<<grid, 256, 0, s>>>(g, sp, pos, vel, w, id, n, rewind, qm_half_dt, ef);
+    k_from_abs_count<<<1, 1, 0, s>>>(sp, n, nullptr);
+    launch_compact(sp, s, 256);
+}
+
+__global__ void k_to_abs(GridDev g, SpeciesDev sp, double* pos, double* vel, double* w, unsigned long long* id,
+                         int n) {
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        float4 ps = sp.pos[p], vs = sp.vel[p];
+        int i, j, k;
+        cell_ijk(g, __float_as_int(ps.w), i, j, k);
+        pos[3 * p] = g.x0[0] + ((double)i + (double)ps.x) * g.dxd[0];
+        pos[3 * p + 1] = g.x0[1] + ((double)j + (double)ps.y) * g.dxd[1];
+        pos[3 * p + 2] = g.x0[2] + ((double)k + (double)ps.z) * g.dxd[2];
+        vel[3 * p] = vs.x;
+        vel[3 * p + 1] = vs.y;
+        vel[3 * p + 2] = vs.z;
+        w[p] = vs.w;
+        id[p] = sp.id[p];
+    }
+}
+void launch_to_abs(const GridDev& g, SpeciesDev sp, double* pos, double* vel, double* w, unsigned long long* id,
+                   int n, cudaStream_t s) {
+    int grid = (n + 255) / 256;
+    if (grid > 4096) grid = 4096;
+    if (grid < 1) grid = 1;
+    k_to_abs<<<grid, 256, 0, s>>>(g, sp, pos, vel, w, id, n);
+}
+
+// ------------------------------------------------------------------------------------
+// synthetic loader: uniform box, Maxwellian velocities, lognormal weights (Philox)
+// ------------------------------------------------------------------------------------
+__global__ void k_load_uniform(GridDev g, SpeciesDev sp, LoadArgs la) {
+    int n0 = sp.counts[0];
+    const float kTwoPi = 6.283185307179586f;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < la.n; p += gridDim.x * blockDim.x) {
+        int dst = n0 + p;
+        if (dst >= sp.capacity) continue;
+        unsigned long long id = la.id0 + (unsigned long long)p;
+        uint4 r0 = philox4x32_10(make_uint4((unsigned)id, (unsigned)(id >> 32), 0xA5A5A5A5u, 0u), la.key);
+        uint4 r1 = philox4x32_10(make_uint4((unsigned)id, (unsigned)(id >> 32), 0xA5A5A5A5u, 1u), la.key);
+        double x[3] = {la.lo[0] + (la.hi[0] - la.lo[0]) * (double)u01(r0.x),
+                       la.lo[1] + (la.hi[1] - la.lo[1]) * (double)u01(r0.y),
+                       la.lo[2] + (la.hi[2] - la.lo[2]) * (double)u01(r0.z)};
+        int ijk[3];
+        float o[3];
+        int nc3[3] = {g.ci, g.cj, g.ck};
+        for (int d = 0; d < 3; d++) {
+            double lc = (x[d] - g.x0[d]) / g.dxd[d];
+            int c = (int)lc;
+            c = c < 0 ? 0 : (c >= nc3[d] ? nc3[d] - 1 : c);
+            ijk[d] = c;
+            o[d] = fminf(fmaxf((float)(lc - c), 0.f), 0x1.fffffep-1f);
+        }
+        float s1, c1, s2, c2;
+        float ra = sqrtf(-2.f * logf(u01(r0.w))), rb = sqrtf(-2.f * logf(u01(r1.y)));
+        sincosf(kTwoPi * u01(r1.x), &s1, &c1);
+        sincosf(kTwoPi * u01(r1.z), &s2, &c2);
+        float3 v = make_float3(la.vth * ra * c1, la.vth * ra * s1, la.vth * rb * c2);
+        float wgt = la.w_mean;
+        if (la.w_sigma > 0.f) {
+            // lognormal with mean w_mean: mu = ln(w_mean) - sigma^2/2; the normal is rb*s2
+            float zn = rb * s2;
+            wgt = expf(logf(la.w_mean) - 0.5f * la.w_sigma * la.w_sigma + la.w_sigma * zn);
+        }
+        int cell = (ijk[2] * g.cj + ijk[1]) * g.ci + ijk[0];
+        sp.pos[dst] = make_float4(o[0], o[1], o[2], __int_as_float(cell));
+        sp.vel[dst] = make_float4(v.x, v.y, v.z, wgt);
+        sp.id[dst] = id;
+    }
+}
+__global__ void k_load_count(SpeciesDev sp, int n) {
+    int nn = sp.counts[0] + n;
+    sp.counts[0] = nn > sp.capacity ? sp.capacity : nn;
+}
+void launch_load_uniform(const GridDev& g, SpeciesDev sp, const LoadArgs& la, cudaStream_t s) {
+    int grid = (la.n + 255) / 256;
+    if (grid > 8192) grid = 8192;
+    if (grid < 1) grid = 1;
+    k_load_uniform<<<grid, 256, 0, s>>>(g, sp, la);
+    k_load_count<<<1, 1, 0, s>>>(sp, la.n);
+}
+
+// ------------------------------------------------------------------------------------
+// FP64 conservation sums (Species::getMicroCount / getMomentum / getKE, Species.cpp:732-752)
+// out[0] sum w, out[1..3] sum w v, out[4] sum w v.v   (per-block partials reduced on host side)
+// ------------------------------------------------------------------------------------
+__global__ void k_sums(SpeciesDev sp, double* part) {
+    int n = sp.counts[0];
+    double a[5] = {0, 0, 0, 0, 0};
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        float4 v = sp.vel[p];
+        double w = v.w, vx = v.x, vy = v.y, vz = v.z;
+        a[0] += w;
+        a[1] += w * vx;
+        a[2] += w * vy;
+        a[3] += w * vz;
+        a[4] += w * (vx * vx + vy * vy + vz * vz);
+    }
+    __shared__ double s[5][8];
+    for (int c = 0; c < 5; c++) {
+        double x = a[c];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if ((threadIdx.x & 31) == 0) s[c][threadIdx.x >> 5] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < 5) {
+        double x = 0;
+        for (int w = 0; w < 8; w++) x += s[threadIdx.x][w];
+        part[blockIdx.x * 5 + threadIdx.x] = x;
+    }
+}
+void launch_sums(SpeciesDev sp, double* out, cudaStream_t s, int grid) { k_sums<<<grid, 256, 0, s>>>(sp, out); }
+
+}  // namespace pic

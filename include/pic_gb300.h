@@ -1,0 +1,168 @@
+/* pic_gb300.h -- C ABI of the GB300 (sm_103a) electrostatic PIC + DSMC step library.
+ *
+ * Drop-in boundary for the ch4/v3 step loop of Misquic/Engineering-degree-in-Plasma-Simulations.
+ * The reference exposes C++ classes only (World, Species, PotentialSolver, Interaction); each
+ * entry point below names the reference member it replaces.  Plain pointers and sizes only:
+ * host arrays are FP64, node arrays are flat with i fastest (n = (k*nj + j)*ni + i, the
+ * reference Field::U, ch4/v3/src/Field.h:262-265), particle arrays are xyz-interleaved.
+ *
+ * Every function returns PIC_OK (0) or a PIC_ERR_* code; pic_last_error() gives the message.
+ * Device state lives in an opaque pic_world owned by the caller (World owns its fields and,
+ * here, also its species, solver and collision model).  Calls on one world are not
+ * re-entrant; work is issued on the world's own CUDA stream and the functions that return
+ * host data synchronise that stream.  There is no CPU fallback: without a usable CUDA device
+ * pic_world_create fails with PIC_ERR_CUDA.
+ */
+#ifndef PIC_GB300_H
+#define PIC_GB300_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PIC_OK 0
+#define PIC_ERR_ARG 1           /* bad argument (the reference throws std::invalid_argument) */
+#define PIC_ERR_CUDA 2          /* CUDA runtime error */
+#define PIC_ERR_NOT_CONVERGED 3 /* solver stopped at max_it (reference solve() returns false) */
+#define PIC_ERR_CAPACITY 4      /* a species ran out of capacity; particles were dropped */
+#define PIC_ERR_DEVICE 5        /* a kernel reported a fault flag (bounded wait expired) */
+
+typedef struct pic_world pic_world;
+
+/* ---- World (ch4/v3/src/World.h:15-116) ------------------------------------------------ */
+
+/* World(int ni, int nj, int nk, type_calc3 x0, type_calc3 xm)        World.h:63, World.cpp:22-26 */
+int pic_world_create(pic_world** out, int ni, int nj, int nk, const double* x0, const double* xm, int device);
+int pic_world_destroy(pic_world* w);
+/* World::setTime(dt, num_ts)                                          World.cpp:321-324 */
+int pic_world_set_time(pic_world* w, double dt, int num_ts);
+/* World::advanceTime() -> *running = ts <= num_ts                     World.cpp:337-341 */
+int pic_world_advance_time(pic_world* w, int* running);
+/* World::getTs()                                                      World.cpp:328-330 */
+int pic_world_get_ts(pic_world* w, int* ts);
+/* Boundary set-up, replacing World::dirichletBoundries / addInlet / computeObjectID for the
+ * domain faces (World.cpp:206-292).  periodic[3]: 1 makes an axis periodic (absent in the
+ * reference).  face_mode[6] for faces -x,+x,-y,+y,-z,+z: 0 Neumann wall (reference v3 GS:
+ * wall nodes copy their inner neighbour), 1 Dirichlet at face_phi[f].  Particles are absorbed
+ * on every non-periodic face (World::inBounds, World.cpp:201-205). */
+int pic_world_set_boundaries(pic_world* w, const int* periodic, const int* face_mode, const double* face_phi);
+/* World::addObject<Rectangle>(pos, phi, sides) + computeObjectID     World.h:118-130, Object.cpp:231-238:
+ * nodes inside the box are Dirichlet at phi; particles entering it are absorbed. */
+int pic_world_add_box(pic_world* w, const double* center, const double* sides, double phi);
+/* public fields World::phi, rho, node_vol, ef                        World.h:51-54
+ * which: 0 phi, 1 rho, 2 node_vol, 3 ef (3 values per node)          */
+int pic_world_get_field(pic_world* w, int which, double* out);
+int pic_world_set_field(pic_world* w, int which, const double* in); /* 0 phi, 1 rho, 3 ef */
+
+/* ---- Species (ch4/v3/src/Species.h:31-133) -------------------------------------------- */
+
+/* Species(name, mass, charge, world, mpw0)                            Species.h:56
+ * capacity: maximum macroparticles held on the device.  weight_bound: an upper bound of the
+ * species' total macroweight; it fixes the 64-bit fixed-point scale of the density
+ * accumulators (<= 0 picks capacity * mpw0 * 64). */
+int pic_species_create(pic_world* w, const char* name, double mass, double charge, double mpw0, long capacity,
+                       double weight_bound, int* species_id);
+/* Species::addParticle(pos, vel, w) for n particles                   Species.cpp:420-434
+ * rewind = 1: drop NaN / out-of-bounds / in-object particles and rewind v by q/m E dt/2 (as
+ * the reference); rewind = 0: place as given (as the interactions' emplace_back).
+ * ids may be NULL (sequential ids are assigned). */
+int pic_species_add_particles(pic_world* w, int sp, const double* pos, const double* vel, const double* wgt,
+                              const uint64_t* ids, long n, int rewind);
+/* Synthetic loader (GPU form of Species::loadParticleBoxThermal, Species.cpp:564-599): n
+ * particles uniform in [lo, hi), Maxwellian at T [K], lognormal weights of mean w_mean and
+ * log-sigma w_sigma (0: all w_mean), Philox stream keyed by seed. */
+int pic_species_load_uniform(pic_world* w, int sp, const double* lo, const double* hi, long n, double T,
+                             double w_mean, double w_sigma, uint64_t seed);
+/* Species::getNumParticles()                                          Species.cpp:43-45 */
+int pic_species_count(pic_world* w, int sp, long* n);
+/* Species::getConstPartRef(): host copy of the particles              Species.cpp:820-822 */
+int pic_species_get_particles(pic_world* w, int sp, double* pos, double* vel, double* wgt, uint64_t* ids, long cap,
+                              long* n);
+/* Species::advanceElectrons / advanceNonElectron (dt)                 Species.cpp:258-399, 47-256
+ * One leapfrog push; with deposit = 1 the weight is also scattered at the new position, which
+ * is Species::computeNumberDensity (Species.cpp:401-416) fused into the push. */
+int pic_species_push(pic_world* w, int sp, double dt, int deposit);
+/* Species::computeNumberDensity() alone (deposit without moving)      Species.cpp:401-416 */
+int pic_species_number_density(pic_world* w, int sp);
+/* Species::den (public field) after pic_charge_density                Species.h:49 */
+int pic_species_get_den(pic_world* w, int sp, double* out);
+/* Species::den_avg and Species::updateAverages()                      Species.cpp:764-766 */
+int pic_species_update_averages(pic_world* w, int sp);
+int pic_species_get_den_avg(pic_world* w, int sp, double* out);
+/* Species::sortIndexes(): reorder particles by cell; counts per cell  Species.cpp:905-915, 813-819
+ * (macro_part_count) are written to cell_counts when it is not NULL (length num_cells). */
+int pic_species_sort(pic_world* w, int sp, int32_t* cell_counts);
+/* Species::getMicroCount / getMomentum / getKE in FP64                Species.cpp:732-752
+ * out[0] sum w, out[1..3] mass * sum w v, out[4] 0.5 mass sum w v.v */
+int pic_species_sums(pic_world* w, int sp, double* out);
+
+/* World::computeChargeDensity(species): den_s and rho = sum q_s den_s  World.cpp:193-200 */
+int pic_charge_density(pic_world* w);
+
+/* ---- PotentialSolver (ch4/v3/src/PotentialSolver.h:26-88) ----------------------------- */
+
+#define PIC_SOLVER_RBSOR 0 /* red-black SOR, FP32 sweeps in FP64 refinement (replaces GS) */
+#define PIC_SOLVER_PCG 1   /* flexible Jacobi-PCG, FP32 iterations in FP64 refinement (replaces NR-PCG) */
+/* PotentialSolver(world, max_it, tolerance, SolverType)               PotentialSolver.cpp:44-52
+ * Stopping rule: FP64 ||b - L phi||_2 / ||b||_2 <= tol_rel (the reference stops on an absolute
+ * RMS residual).  omega is the SOR weight (reference 1.4). */
+int pic_solver_configure(pic_world* w, int method, double tol_rel, int max_it, double omega);
+/* PotentialSolver::solve()                                            PotentialSolver.cpp:55-67
+ * iters: inner sweeps / iterations; rel: final FP64 relative residual.
+ * Returns PIC_ERR_NOT_CONVERGED when max_it is reached (reference: solve() == false). */
+int pic_solver_solve(pic_world* w, int* iters, double* rel);
+/* PotentialSolver::computeEF()                                        PotentialSolver.cpp:354-408 */
+int pic_solver_compute_ef(pic_world* w);
+/* cumulative solver work since creation: solves, FP64 refinements (residual evaluations) and
+ * inner FP32 sweeps / iterations (no reference counterpart; the reference prints progress) */
+int pic_solver_stats(pic_world* w, long* solves, long* refinements, long* inner_iterations);
+
+/* ---- Interaction: MC_MEX_Ionization (ch4/v3/src/Interactions.h:98-143) ------------------
+ * Background-gas form: the neutral species is a uniform Maxwellian gas (density n_neutral,
+ * temperature T_neutral, mass m_neutral) instead of macroparticles.  sigma_coll is a table
+ * (E [eV], sigma [m^2]) interpolated as evaluateSigmaColl (Interactions.cpp:541-558).
+ * sigma_ion_kind 0: the reference fit a*ln(E/b)/E*exp(-c/E) (Interactions.cpp:559-566) with
+ * (p0,p1,p2) = (a,b,c); 1: Lotz form A*ln(E/I)/(E*I)*(1-b*exp(-c*(E/I-1))) with
+ * (p0,p1,p2,p3) = (A,b,c,unused).  E_ion_eV is the threshold, B_inc the Opal energy-sharing
+ * constant (Interactions.cpp:511).  Collisions use Philox streams keyed by (seed, step, id). */
+int pic_mcc_create(pic_world* w, int electrons, int ions, double n_neutral, double T_neutral, double m_neutral,
+                   double E_ion_eV, double B_inc, int sigma_ion_kind, const double* sigma_ion_params,
+                   const double* table_E, const double* table_s, int table_n, uint64_t seed);
+/* Interaction::apply(dt): collisions of every electron for the current step (no push). */
+int pic_mcc_apply(pic_world* w, double dt);
+/* counters since creation: candidates, collisions, ionisations, products lost */
+int pic_mcc_stats(pic_world* w, uint64_t* out);
+
+/* ---- the step loop (ch4/v3/src/main.cpp:177-286) -------------------------------------- */
+
+/* Loop options.  solve_each_step: Poisson + E every step (v3 comments it out, main.cpp:260-261;
+ * ch2 solves every step).  sort_every: counting sort by cell every k steps.  subcycle[sp]:
+ * push species sp every k steps with k*dt (main.cpp:211-238); 1 = every step.
+ * merge_every/merge_after/merge_min: merging (main.cpp:179: ts > 250 && ts % 50 == 0). */
+int pic_loop_configure(pic_world* w, int solve_each_step, int sort_every, const int* subcycle, int merge_every,
+                       int merge_after, int merge_min);
+/* one iteration of the time loop: advanceTime, [merge], collisions + push + deposit,
+ * compaction, [averages], charge density, [solve + E], [sort] */
+int pic_step(pic_world* w);
+/* velocity-binned merge (Species::merge, Species.cpp:981-1145) of cells holding at least
+ * min_count particles; sorts the species first */
+int pic_species_merge(pic_world* w, int sp, int min_count);
+
+/* ---- runtime ------------------------------------------------------------------------- */
+int pic_synchronize(pic_world* w);
+/* message of the last failing call on this thread (empty if none) */
+int pic_last_error(char* buf, int len);
+/* per-kernel CUDA-event timing: enable, then read accumulated milliseconds and launch counts
+ * of the named kernel groups ("push", "deposit", "rho", "poisson", "efield", "sort", ...). */
+int pic_timing_enable(pic_world* w, int on);
+int pic_timing_read(pic_world* w, const char* name, double* ms, long* launches);
+int pic_timing_reset(pic_world* w);
+/* kernels launched on this world since creation */
+int pic_launch_count(pic_world* w, long* n);
+/* the CUDA stream (cudaStream_t) the world issues its work on */
+int pic_world_stream(pic_world* w, void** stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,231 @@
+// pic_gb300.hpp -- header-only C++ facade with the reference's class surface over the C ABI.
+//
+// A ch4/v3-style driver (ch4/v3/src/main.cpp) keeps its shape: World, Species,
+// PotentialSolver and an Interaction with apply(dt), with the same member names.  The
+// particles live on the GPU, so Species::getPartRef() returns a host copy instead of a
+// mutable reference (Species.cpp:823-825), and the Poisson tolerance is the FP64 relative
+// residual.  Errors throw like the reference: std::invalid_argument for bad arguments,
+// std::runtime_error for device failures.
+#ifndef PIC_GB300_HPP
+#define PIC_GB300_HPP
+#include <array>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+#include "pic_gb300.h"
+
+namespace pic_gb300 {
+
+using type_calc = double;
+using type_calc3 = std::array<double, 3>;
+
+inline void check(int rc) {
+    if (rc == PIC_OK) return;
+    char buf[512];
+    pic_last_error(buf, sizeof(buf));
+    if (rc == PIC_ERR_ARG) throw std::invalid_argument(buf);
+    throw std::runtime_error(std::string("pic_gb300: ") + buf);
+}
+
+struct Particle {  // ch4/v3/src/Species.h:12-29 (host copy)
+    type_calc3 pos, vel;
+    type_calc macro_weight;
+    uint64_t id;
+};
+
+enum SolverType { GS = PIC_SOLVER_RBSOR, PCG = PIC_SOLVER_PCG };  // PotentialSolver.h:24
+
+class Species;
+
+class World {  // ch4/v3/src/World.h:15-116
+public:
+    const int ni, nj, nk, nv, num_cells;
+    World(int ni_, int nj_, int nk_, type_calc3 x0, type_calc3 xm, int device = 0)
+        : ni(ni_), nj(nj_), nk(nk_), nv(ni_ * nj_ * nk_), num_cells((ni_ - 1) * (nj_ - 1) * (nk_ - 1)) {
+        check(pic_world_create(&h_, ni, nj, nk, x0.data(), xm.data(), device));
+    }
+    World(const World&) = delete;
+    World& operator=(const World&) = delete;
+    ~World() { pic_world_destroy(h_); }
+    pic_world* handle() const { return h_; }
+    void setTime(type_calc dt, int num_ts) {
+        dt_ = dt;
+        check(pic_world_set_time(h_, dt, num_ts));
+    }
+    type_calc getDt() const { return dt_; }
+    bool advanceTime() {
+        int r = 0;
+        check(pic_world_advance_time(h_, &r));
+        return r != 0;
+    }
+    int getTs() const {
+        int t = 0;
+        check(pic_world_get_ts(h_, &t));
+        return t;
+    }
+    void dirichletBoundries(type_calc phi = 0) {  // World.cpp:263-274
+        int per[3] = {0, 0, 0}, mode[6] = {1, 1, 1, 1, 1, 1};
+        double val[6] = {phi, phi, phi, phi, phi, phi};
+        check(pic_world_set_boundaries(h_, per, mode, val));
+    }
+    void setBoundaries(const int periodic[3], const int face_mode[6], const double face_phi[6]) {
+        check(pic_world_set_boundaries(h_, periodic, face_mode, face_phi));
+    }
+    void addBox(type_calc3 pos, type_calc phi, type_calc3 sides) {  // addObject<Rectangle>(pos, phi, sides)
+        check(pic_world_add_box(h_, pos.data(), sides.data(), phi));
+    }
+    std::vector<double> phi() const { return field(0, 1); }
+    std::vector<double> rho() const { return field(1, 1); }
+    std::vector<double> node_vol() const { return field(2, 1); }
+    std::vector<double> ef() const { return field(3, 3); }
+    void setPhi(const std::vector<double>& v) { check(pic_world_set_field(h_, 0, v.data())); }
+    void computeChargeDensity() { check(pic_charge_density(h_)); }  // World.cpp:193-200
+    template <class V>
+    void computeChargeDensity(V&) {
+        computeChargeDensity();
+    }
+
+private:
+    std::vector<double> field(int which, int comps) const {
+        std::vector<double> out((size_t)nv * comps);
+        check(pic_world_get_field(h_, which, out.data()));
+        return out;
+    }
+    pic_world* h_ = nullptr;
+    type_calc dt_ = 1e-4;
+};
+
+class Species {  // ch4/v3/src/Species.h:31-133
+public:
+    const std::string name;
+    const type_calc mass, charge, mpw0;
+    Species(std::string name_, type_calc mass_, type_calc charge_, World& world, type_calc mpw0_,
+            long capacity = 1 << 20, double weight_bound = 0)
+        : name(name_), mass(mass_), charge(charge_), mpw0(mpw0_), world_(&world) {
+        check(pic_species_create(world.handle(), name.c_str(), mass, charge, mpw0, capacity, weight_bound, &id_));
+    }
+    int id() const { return id_; }
+    size_t getNumParticles() const {
+        long n = 0;
+        check(pic_species_count(world_->handle(), id_, &n));
+        return (size_t)n;
+    }
+    void addParticle(type_calc3 pos, type_calc3 vel, type_calc w) {  // Species.cpp:420-434
+        check(pic_species_add_particles(world_->handle(), id_, pos.data(), vel.data(), &w, nullptr, 1, 1));
+    }
+    void addParticle(type_calc3 pos, type_calc3 vel) { addParticle(pos, vel, mpw0); }
+    void addParticles(const std::vector<double>& pos, const std::vector<double>& vel, const std::vector<double>& w,
+                      bool rewind = true) {
+        check(pic_species_add_particles(world_->handle(), id_, pos.data(), vel.data(), w.data(), nullptr,
+                                        (long)w.size(), rewind ? 1 : 0));
+    }
+    void loadUniform(type_calc3 lo, type_calc3 hi, long n, type_calc T, type_calc w_mean, type_calc w_sigma,
+                     uint64_t seed) {
+        check(pic_species_load_uniform(world_->handle(), id_, lo.data(), hi.data(), n, T, w_mean, w_sigma, seed));
+    }
+    void advanceElectrons(type_calc dt) { check(pic_species_push(world_->handle(), id_, dt, 1)); }
+    void advanceNonElectron(Species&, Species&, type_calc dt) { check(pic_species_push(world_->handle(), id_, dt, 1)); }
+    void computeNumberDensity() { check(pic_species_number_density(world_->handle(), id_)); }
+    void updateAverages() { check(pic_species_update_averages(world_->handle(), id_)); }
+    void sortIndexes() { check(pic_species_sort(world_->handle(), id_, nullptr)); }
+    std::vector<int32_t> computeMacroParticlesCount() {
+        std::vector<int32_t> c((size_t)world_->num_cells);
+        check(pic_species_sort(world_->handle(), id_, c.data()));
+        return c;
+    }
+    void merge(int min_count = 10) { check(pic_species_merge(world_->handle(), id_, min_count)); }
+    std::vector<double> den() const {
+        std::vector<double> d((size_t)world_->nv);
+        check(pic_species_get_den(world_->handle(), id_, d.data()));
+        return d;
+    }
+    type_calc getMicroCount() const { return sums()[0]; }
+    type_calc3 getMomentum() const {
+        auto s = sums();
+        return {s[1], s[2], s[3]};
+    }
+    type_calc getKE() const { return sums()[4]; }
+    std::vector<Particle> getPartRef() const {
+        size_t n = getNumParticles();
+        std::vector<double> pos(3 * n + 3), vel(3 * n + 3), w(n + 1);
+        std::vector<uint64_t> ids(n + 1);
+        long got = 0;
+        check(pic_species_get_particles(world_->handle(), id_, pos.data(), vel.data(), w.data(), ids.data(),
+                                        (long)n + 1, &got));
+        std::vector<Particle> out((size_t)got);
+        for (long p = 0; p < got; p++)
+            out[p] = {{pos[3 * p], pos[3 * p + 1], pos[3 * p + 2]}, {vel[3 * p], vel[3 * p + 1], vel[3 * p + 2]}, w[p], ids[p]};
+        return out;
+    }
+
+private:
+    std::array<double, 5> sums() const {
+        std::array<double, 5> s{};
+        check(pic_species_sums(world_->handle(), id_, s.data()));
+        return s;
+    }
+    World* world_;
+    int id_ = -1;
+};
+
+class PotentialSolver {  // ch4/v3/src/PotentialSolver.h:26-88
+public:
+    PotentialSolver(World& world, unsigned max_solver_it, type_calc tolerance, SolverType type, double omega = 1.4)
+        : world_(&world) {
+        check(pic_solver_configure(world.handle(), (int)type, tolerance, (int)max_solver_it, omega));
+    }
+    bool solve() {  // PotentialSolver.cpp:55-67: false when not converged
+        int rc = pic_solver_solve(world_->handle(), &iters_, &rel_);
+        if (rc == PIC_ERR_NOT_CONVERGED) return false;
+        check(rc);
+        return true;
+    }
+    void computeEF() { check(pic_solver_compute_ef(world_->handle())); }
+    // only the reference's n0 = 0 case (main.cpp:138) is supported: no Boltzmann electrons
+    void setReferenceValues(type_calc, type_calc n0, type_calc) {
+        if (n0 != 0) throw std::invalid_argument("Boltzmann-electron term is not supported (n0 must be 0)");
+    }
+    int iterations() const { return iters_; }
+    double relativeResidual() const { return rel_; }
+
+private:
+    World* world_;
+    int iters_ = 0;
+    double rel_ = 0;
+};
+
+class Interaction {  // ch4/v3/src/Interactions.h:9-13
+public:
+    virtual void apply(type_calc dt) noexcept = 0;
+    virtual ~Interaction() noexcept = default;
+};
+
+// background-gas form of MC_MEX_Ionization (Interactions.h:98-143)
+class MC_MEX_Ionization : public Interaction {
+public:
+    MC_MEX_Ionization(Species& electrons, Species& ions, World& world, double n_neutral, double T_neutral,
+                      double m_neutral, double E_ion_eV, const std::vector<double>& table_E,
+                      const std::vector<double>& table_s, int sigma_ion_kind, std::array<double, 4> sigma_ion_params,
+                      double B_inc = 10.0, uint64_t seed = 12345)
+        : world_(&world) {
+        if (table_E.size() != table_s.size()) throw std::invalid_argument("sigma table sizes differ");
+        check(pic_mcc_create(world.handle(), electrons.id(), ions.id(), n_neutral, T_neutral, m_neutral, E_ion_eV,
+                             B_inc, sigma_ion_kind, sigma_ion_params.data(), table_E.data(), table_s.data(),
+                             (int)table_E.size(), seed));
+    }
+    void apply(type_calc dt) noexcept override { last_rc_ = pic_mcc_apply(world_->handle(), dt); }
+    int lastStatus() const { return last_rc_; }
+    std::array<uint64_t, 4> stats() const {
+        std::array<uint64_t, 4> s{};
+        check(pic_mcc_stats(world_->handle(), s.data()));
+        return s;
+    }
+
+private:
+    World* world_;
+    int last_rc_ = PIC_OK;
+};
+
+}  // namespace pic_gb300
+#endif

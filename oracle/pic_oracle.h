@@ -1,0 +1,145 @@
+/* pic_oracle.h -- TEST INFRASTRUCTURE ONLY.
+ *
+ * Plain-C FP64 restatement of the reference's ch4/v3 electrostatic PIC + DSMC step
+ * (Misquic/Engineering-degree-in-Plasma-Simulations).  It is the checker for the CUDA
+ * library and the timed CPU baseline; only tests/, __graft_entry__.smoke() and
+ * bench.py (cpu_baseline leg and --impl reference) may load it.  The product path
+ * never calls it and has no CPU fallback.
+ *
+ * Two families of functions:
+ *   or_*_ref  : restate the reference's own algorithms step for step (same loop order,
+ *               same FP64 operation order, same MT19937 draws).  These are pinned
+ *               bit-for-bit against the reference compiled from its sources
+ *               (oracle/_ref, tests/golden).
+ *   or_*      : FP64 restatements of the GPU forms that the reference lacks (periodic
+ *               x/y, background-neutral collisions with Philox streams, red-black SOR,
+ *               flexible PCG with FP64 residual refinement, Lotz cross-section).
+ *
+ * Layout conventions shared with the CUDA library:
+ *   node index  n = (k*nj + j)*ni + i          (reference Field::U, Field.h:262-265)
+ *   cell index  c = (k*(nj-1) + j)*(ni-1) + i  (reference World::XtoC, World.cpp:134-137)
+ */
+#ifndef PIC_ORACLE_H
+#define PIC_ORACLE_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* physical constants exactly as ch4/v3/src/all.h:16-25 */
+#define OR_EPS0 8.85418782e-12
+#define OR_QE 1.602176565e-19
+#define OR_AMU 1.660538921e-27
+#define OR_ME 9.10938215e-31
+#define OR_KB 1.380648e-23
+#define OR_PI 3.141592653
+
+/* node kinds */
+enum { OR_FREE = 0, OR_FIXED = 1, OR_MIRROR = 2, OR_ALIAS = 3 };
+
+typedef struct {
+    double pos[3];
+    double vel[3];
+    double w;
+} or_particle; /* reference Particle, Species.h:12-29 */
+
+typedef struct {
+    int ni, nj, nk;
+    double x0[3], xm[3], dx[3], inv_dx[3];
+    int periodic[3];
+    int n_boxes; /* axis-aligned Rectangle objects (Object.cpp:231-238): absorbing */
+    double box_c[8][3], box_half[8][3];
+} or_grid;
+
+void or_grid_init(or_grid* g, int ni, int nj, int nk, const double* x0, const double* xm, const int* periodic);
+int or_grid_add_box(or_grid* g, const double* center, const double* sides);
+/* node kinds for the three boundary flavours used by the configs:
+ *  wall_mode 0: reference v3 walls (MIRROR = Neumann copy of inner neighbour)
+ *  wall_mode 1: all non-periodic walls FIXED (Dirichlet, ch2 semantics)
+ *  periodic axes get ALIAS at index n-1; nodes inside boxes are FIXED. */
+void or_node_kinds(const or_grid* g, int wall_mode, uint8_t* kind);
+
+/* ---- random numbers ---- */
+typedef struct {
+    uint32_t mt[624];
+    int idx;
+} or_mt;
+void or_mt_seed(or_mt* r, uint32_t seed);
+uint32_t or_mt_next(or_mt* r);
+double or_mt_u01(or_mt* r); /* std::uniform_real_distribution<double>(0,1) over mt19937 */
+void or_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+double or_u01_from_u32(uint32_t x); /* ((x>>9)+0.5)*2^-23: the GPU's draw, exact in FP32 and FP64 */
+
+/* ---- fields ---- */
+void or_node_volumes(const or_grid* g, double* vol);
+void or_gather3_ref(const or_grid* g, const double* f3, const double lc[3], double out[3]);
+void or_scatter_ref(const or_grid* g, double* f, const double lc[3], double val);
+void or_number_density_ref(const or_grid* g, const or_particle* p, long n, double* den);
+void or_compute_ef_ref(const or_grid* g, const double* phi, double* ef);
+
+/* ---- push ---- */
+long or_push_electrons_ref(const or_grid* g, or_particle* p, long n, uint64_t* ids, const double* ef, double dt,
+                           double charge, double mass);
+long or_push_electrons_mt(const or_grid* g, or_particle* p, long n, uint64_t* ids, const double* ef, double dt,
+                          double charge, double mass, int nthreads);
+
+/* ---- Poisson ---- */
+int or_solve_gs_ref(const or_grid* g, const uint8_t* kind, double* phi, const double* rho, int max_it, double tol,
+                    int* iters, double* l2);
+int or_solve_pcg_ref(const or_grid* g, const uint8_t* kind, double* phi, const double* rho, int max_it, double tol,
+                     int axis_swap, int* iters, double* l2);
+void or_fill_aux(const or_grid* g, const uint8_t* kind, double* phi);
+void or_residual(const or_grid* g, const uint8_t* kind, const double* phi, const double* rho, double* rnorm2,
+                 double* bnorm2);
+int or_solve_rbsor(const or_grid* g, const uint8_t* kind, double* phi, const double* rho, double omega, double tol_rel,
+                   int max_sweeps, int* sweeps, double* rel);
+int or_solve_fpcg(const or_grid* g, const uint8_t* kind, double* phi, const double* rho, double tol_rel, int max_it,
+                  int* iters, double* rel);
+
+/* ---- collisions ---- */
+typedef struct {
+    double mass_neutral, mass_electron, E_ion_eV, B_inc;
+    int sigma_ion_kind; /* 0: reference fit a*ln(E/b)/E*exp(-c/E); 1: Lotz A*ln(E/I)/(E*I)*(1-b*exp(-c*(E/I-1))) */
+    double sig_a, sig_b, sig_c, sig_A;
+    const double* table_E; /* sigma_coll table (eV, m^2), ascending */
+    const double* table_s;
+    int table_n;
+    double n_neutral, T_neutral, sigv_max; /* background gas */
+} or_coll_params;
+double or_sigma_coll(const or_coll_params* cp, double E_eV);
+double or_sigma_ion(const or_coll_params* cp, double E_eV);
+double or_sigv_majorant(const or_coll_params* cp);
+
+/* Background-gas electron-impact collisions (GPU form, restated in FP64).
+ * Draws come from Philox-4x32-10 keyed by (seed, step, particle id) in the same order as
+ * the CUDA kernel.  Products (electron + ion, weight of the parent electron) are appended
+ * at ele[*n_ele] and ion[*n_ion] with ids derived from the parent id.  Returns the number
+ * of real collisions; *n_ionized receives the ionisations. */
+long or_mcc_background(const or_grid* g, const or_coll_params* cp, or_particle* ele, uint64_t* ele_id, long* n_ele,
+                       long cap_ele, or_particle* ion, uint64_t* ion_id, long* n_ion, long cap_ion, double dt,
+                       uint32_t seed_lo, uint32_t seed_hi, uint32_t step, long* n_ionized);
+uint64_t or_child_id(uint64_t parent, uint32_t step, uint32_t kind);
+
+/* Reference NTC ionisation with neutral macroparticles (Interactions.cpp:600-762), MT19937 draws.
+ * wsv_max is the persistent (W*sigma*v)_max, updated in place. Returns collisions. */
+long or_ntc_ionize_ref(const or_grid* g, const or_coll_params* cp, or_mt* r, or_particle* neu, long* n_neu,
+                       long cap_neu, or_particle* ion, long* n_ion, long cap_ion, or_particle* ele, long* n_ele,
+                       long cap_ele, double dt, double* wsv_max);
+
+/* Reference merge (Species.cpp:981-1145) including addParticle's rewind with the global dt.
+ * min_count: cells with fewer particles are skipped (reference: 10). Returns new count. */
+long or_merge_ref(const or_grid* g, or_mt* r, or_particle* p, long n, long cap, const double* ef, double charge,
+                  double mass, double dt_global, int min_count);
+
+/* Reference loadParticleBoxThermal (Species.cpp:564-599, 855-869), with rejection and rewind (E given). */
+long or_load_box_thermal_ref(const or_grid* g, or_mt* r, or_particle* p, long cap, const double* x0,
+                             const double* sides, double num_den, double T, double mpw0, double mass, double charge,
+                             const double* ef, double dt);
+
+/* conservation sums (Species.cpp:732-752) */
+void or_sums(const or_particle* p, long n, double mass, double* count, double mom[3], double* ke);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,427 @@
+"""Parity of the CUDA library (through the C ABI) with the FP64 oracle on identical inputs.
+
+Tolerances (FP32 device arithmetic against the FP64 oracle):
+  positions  |dx| <= 1e-5 * cell size after one push, <= 1e-5 * domain length after many
+  velocities |dv| <= 1e-5 * |v| + 1e-3 m/s
+  den, rho   max |d| <= 1e-6 * max |oracle|
+  E          max |d| <= 1e-6 * max |oracle|
+  phi        both driven to the same FP64 relative residual; max |d| <= 1e-6 * max |phi|
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+
+def by_id(arr, ids):
+    order = np.argsort(ids)
+    return arr[order], ids[order]
+
+
+def oracle_parts(pos, vel, w):
+    p = np.zeros(len(w), O.PARTICLE)
+    p["pos"], p["vel"], p["w"] = pos, vel, w
+    return p
+
+
+def load_thermal(port, g, seed, center, sides, den, T, mpw0, mass, charge, cap=10 ** 6):
+    mt = port.mt(seed)
+    return port.load_box_thermal_ref(g, mt, cap, center, sides, den, T, mpw0, mass, charge)
+
+
+def smooth_field(nv, nn, dx, amp, seed):
+    rng = np.random.default_rng(seed)
+    k, j, i = np.meshgrid(np.arange(nn[2]), np.arange(nn[1]), np.arange(nn[0]), indexing="ij")
+    ef = np.zeros((nv, 3))
+    for d in range(3):
+        a = rng.uniform(0.5, 1.5, 3)
+        ef[:, d] = (amp * np.sin(a[0] * i * 0.3 + d) * np.cos(a[1] * j * 0.25) * np.sin(a[2] * k * 0.2 + 1)).ravel()
+    return ef
+
+
+# ------------------------------------------------------------------------------------------
+# push + deposit
+# ------------------------------------------------------------------------------------------
+def test_push_deposit_golden(pic, port):
+    d = golden("push_deposit")
+    nn, x0, xm = d["nn"], d["x0"], d["xm"]
+    W = pic.World(*nn, x0, xm)
+    e = pic.Species("e-", pic.ME, -pic.QE, W, 100.0, capacity=4096)
+    W.setTime(float(d["dt"]), 10)
+    W.ef = d["ef"]
+    n0 = len(d["in_w"])
+    ids = np.arange(n0, dtype=np.uint64)
+    e.addParticles(d["in_pos"], d["in_vel"], d["in_w"], ids=ids, rewind=False)
+    assert e.getNumParticles() == n0
+    e.advance(float(d["dt"]), deposit=True)
+    W.computeChargeDensity()
+    gp = e.getPartRef()
+    # oracle with ids to match particles after swap-with-last deletion
+    g = port.grid(nn, x0, xm)
+    p = oracle_parts(d["in_pos"], d["in_vel"], d["in_w"])
+    oid = ids.copy()
+    n = port.push(g, p, d["ef"], float(d["dt"]), -O.QE, O.ME, ids=oid)
+    assert n == len(d["out_w"]) == len(gp)
+    op, oi = by_id(p[:n], oid[:n])
+    gq, gi = by_id(gp, gp["id"])
+    assert np.array_equal(oi, gi)
+    dx = (xm - x0) / (nn - 1)
+    assert np.all(np.abs(gq["pos"] - op["pos"]) <= 1e-5 * dx)
+    assert np.all(np.abs(gq["vel"] - op["vel"]) <= 1e-5 * np.abs(op["vel"]) + 1e-3)
+    den = e.den
+    assert np.max(np.abs(den - d["den"])) <= 1e-6 * np.max(np.abs(d["den"]))
+
+
+def test_multi_step_push_matches_oracle(pic, port):
+    nn, x0, xm = (21, 21, 21), (0.0, 0.0, 0.0), (0.2, 0.2, 0.2)
+    g = port.grid(nn, x0, xm)
+    nv = int(np.prod(nn))
+    dx = np.array([0.01, 0.01, 0.01])
+    ef = smooth_field(nv, nn, dx, 50.0, 3)
+    ele = load_thermal(port, g, 1, (0.1, 0.1, 0.1), (0.2, 0.2, 0.2), 4e7, 11604.0, 100.0, O.ME, -O.QE)
+    W = pic.World(*nn, x0, xm)
+    W.dirichletBoundries(0.0)
+    e = pic.Species("e-", pic.ME, -pic.QE, W, 100.0, capacity=len(ele) + 16)
+    W.ef = ef
+    ids = np.arange(len(ele), dtype=np.uint64)
+    e.addParticles(ele["pos"], ele["vel"], ele["w"], ids=ids, rewind=False)
+    dt = 5e-11
+    p = ele.copy()
+    oid = ids.copy()
+    n = len(p)
+    for s in range(20):
+        e.advance(dt, deposit=False)
+        n = port.push(g, p[:n], ef, dt, -O.QE, O.ME, ids=oid[:n])
+        if s % 7 == 3:
+            e.sortIndexes()
+    gp = e.getPartRef()
+    assert abs(len(gp) - n) <= max(2, n // 2000)  # boundary decisions of FP32 vs FP64 may differ
+    common, ia, ib = np.intersect1d(gp["id"], oid[:n], return_indices=True)
+    assert len(common) >= n - max(2, n // 2000)
+    assert np.max(np.abs(gp["pos"][ia] - p[:n]["pos"][ib])) <= 1e-5 * 0.2
+    assert len(gp) < len(ele)  # electrons reached the walls and were absorbed
+
+
+# ------------------------------------------------------------------------------------------
+# charge density
+# ------------------------------------------------------------------------------------------
+@pytest.mark.parametrize("periodic", [False, True])
+def test_rho_two_species(pic, port, periodic):
+    nn, x0, xm = (17, 13, 25), (0.0, 0.0, 0.0), (0.02, 0.015, 0.03)
+    per = (1, 1, 0) if periodic else (0, 0, 0)
+    g = port.grid(nn, x0, xm, periodic=per)
+    rng = np.random.default_rng(4)
+    W = pic.World(*nn, x0, xm)
+    W.set_boundaries(per, (1,) * 6, (0.0,) * 6)
+    sps, dens = [], []
+    for name, m, q, n in (("e-", pic.ME, -pic.QE, 30000), ("O2+", 32 * pic.AMU, pic.QE, 20000)):
+        pos = rng.uniform(x0, xm, (n, 3)) * 0.999999
+        vel = np.zeros((n, 3))
+        w = rng.lognormal(np.log(64) - 0.125, 0.5, n)
+        s = pic.Species(name, m, q, W, 64.0, capacity=n + 16)
+        s.addParticles(pos, vel, w, rewind=False)
+        s.computeNumberDensity()
+        sps.append((s, q))
+        dens.append((port.number_density(g, oracle_parts(pos, vel, w)), q))
+    W.computeChargeDensity()
+    rho_o = sum(q * dd for dd, q in dens)
+    for (s, _), (dd, _) in zip(sps, dens):
+        assert np.max(np.abs(s.den - dd)) <= 1e-6 * np.max(dd)
+    rho = W.rho
+    assert np.max(np.abs(rho - rho_o)) <= 1e-6 * np.max(np.abs(rho_o))
+    # total charge: sum den * node volume = sum w (alias nodes counted once)
+    vol = port.node_volumes(g)
+    kind = port.node_kinds(g, 1)
+    keep = kind != O.ALIAS
+    for (s, _), (dd, _) in zip(sps, dens):
+        tot = np.sum((s.den * vol)[keep])
+        assert abs(tot - s.getMicroCount()) <= 1e-6 * tot
+
+
+def test_rho_bitwise_reproducible_and_order_independent(pic):
+    nn, x0, xm = (33, 33, 65), (0.0, 0.0, 0.0), (0.01, 0.01, 0.02)
+    rng = np.random.default_rng(8)
+    n = 200000
+    pos = rng.uniform(x0, xm, (n, 3)) * 0.999999
+    w = rng.lognormal(np.log(64) - 0.125, 0.5, n)
+    results = []
+    for perm in (np.arange(n), rng.permutation(n), np.arange(n)):
+        W = pic.World(*nn, x0, xm)
+        W.set_boundaries((1, 1, 0), (1,) * 6, (0.0,) * 6)
+        s = pic.Species("e-", pic.ME, -pic.QE, W, 64.0, capacity=n)
+        s.addParticles(pos[perm], np.zeros((n, 3)), w[perm], rewind=False)
+        s.computeNumberDensity()
+        W.computeChargeDensity()
+        results.append(W.rho)
+        W.close()
+    assert np.array_equal(results[0], results[1]) and np.array_equal(results[0], results[2])
+
+
+# ------------------------------------------------------------------------------------------
+# E field and Poisson
+# ------------------------------------------------------------------------------------------
+@pytest.mark.parametrize("per", [(0, 0, 0), (1, 1, 0)])
+def test_efield_matches_oracle(pic, port, per):
+    nn, x0, xm = (16, 12, 20), (-0.01, 0.0, 0.0), (0.01, 0.012, 0.03)
+    g = port.grid(nn, x0, xm, periodic=per)
+    rng = np.random.default_rng(2)
+    phi = rng.normal(size=int(np.prod(nn))) * 50 + 300
+    kind = port.node_kinds(g, 1)
+    port.fill_aux(g, kind, phi)  # periodic copies consistent
+    W = pic.World(*nn, x0, xm)
+    W.set_boundaries(per, (0,) * 6, (0.0,) * 6)
+    W.phi = phi
+    pic.PotentialSolver(W, 10, 1e-6).computeEF()
+    ef = W.ef
+    ref = port.compute_ef(g, phi)
+    assert np.max(np.abs(ef - ref)) <= 1e-6 * np.max(np.abs(ref))
+
+
+POISSON_CASES = {
+    "c1_dirichlet": dict(nn=(21, 21, 21), x0=(0, 0, 0), xm=(0.2, 0.2, 0.2), per=(0, 0, 0), mode=(1,) * 6,
+                         phi=(0.0,) * 6, boxes=()),
+    "c2_periodic_xy": dict(nn=(16, 16, 40), x0=(0, 0, 0), xm=(0.005, 0.005, 0.0125), per=(1, 1, 0), mode=(1,) * 6,
+                           phi=(0, 0, 0, 0, 0.0, 500.0), boxes=()),
+    "v3_box_neumann": dict(nn=(11, 9, 13), x0=(-0.01, 0, 0), xm=(0.01, 0.016, 0.03), per=(0, 0, 0), mode=(0,) * 6,
+                           phi=(0.0,) * 6, boxes=(((0.0, 0.008, 0.0), (0.02, 0.016, 0.006), 100.0),
+                                                  ((0.0, 0.008, 0.03), (0.02, 0.016, 0.006), -100.0))),
+}
+
+
+@pytest.mark.parametrize("case", sorted(POISSON_CASES))
+@pytest.mark.parametrize("method", ["rbsor", "pcg"])
+def test_poisson_matches_oracle(pic, port, case, method):
+    c = POISSON_CASES[case]
+    g = port.grid(c["nn"], c["x0"], c["xm"], periodic=c["per"], boxes=[(b[0], b[1]) for b in c["boxes"]])
+    nv = int(np.prod(c["nn"]))
+    wall_mode = 1 if c["mode"][0] == 1 else 0
+    kind = port.node_kinds(g, wall_mode)
+    rng = np.random.default_rng(7)
+    rho = rng.normal(size=nv) * 1e-7 + 2e-7
+    W = pic.World(*c["nn"], c["x0"], c["xm"])
+    W.set_boundaries(c["per"], c["mode"], c["phi"])
+    for b in c["boxes"]:
+        W.addBox(b[0], b[1], b[2])
+    phi0 = W.phi  # Dirichlet values as set by the library
+    W.rho = rho
+    rho32 = W.rho  # the device keeps rho in FP32: give the oracle the same input
+    S = pic.PotentialSolver(W, 20000, 1e-9, pic.SOLVER_RBSOR if method == "rbsor" else pic.SOLVER_PCG, omega=1.8)
+    assert S.solve(raise_on_fail=True)
+    assert S.rel <= 1e-9
+    phi = W.phi
+    ref = phi0.copy()
+    ok, _, rel = port.solve_fpcg(g, kind, ref, rho32, 1e-13, 20000)
+    assert ok
+    # same residual measured by the oracle on the device answer
+    assert port.rel_residual(g, kind, phi, rho32) <= 2e-9
+    assert np.max(np.abs(phi - ref)) <= 1e-6 * np.max(np.abs(ref))
+
+
+def test_poisson_reference_gs_agrees_on_v3_walls(pic, port):
+    """The reference GS (golden) and the device solve agree on the v3 scenario walls."""
+    d = golden("poisson")
+    W = pic.World(*d["nn"], d["x0"], d["xm"])
+    W.set_boundaries((0, 0, 0), (0,) * 6, (0.0,) * 6)
+    W.addBox(d["box_c"], d["box_s"], float(d["box_phi"]))
+    W.rho = d["rho"]
+    S = pic.PotentialSolver(W, 20000, 1e-10, pic.SOLVER_PCG)
+    assert S.solve(raise_on_fail=True)
+    ref = d["v3box_gs_phi"]  # reference converged to an absolute RMS residual of 1e-6
+    assert np.max(np.abs(W.phi - ref)) <= 1e-5 * np.max(np.abs(ref))
+
+
+# ------------------------------------------------------------------------------------------
+# sort and compaction
+# ------------------------------------------------------------------------------------------
+def test_sort_invariants(pic):
+    nn, x0, xm = (20, 17, 33), (0.0, 0.0, 0.0), (0.019, 0.016, 0.032)
+    rng = np.random.default_rng(3)
+    n = 300000
+    W = pic.World(*nn, x0, xm)
+    s = pic.Species("e-", pic.ME, -pic.QE, W, 1.0, capacity=n)
+    pos = rng.uniform(x0, xm, (n, 3)) * 0.999999
+    ids = rng.permutation(n).astype(np.uint64)
+    s.addParticles(pos, rng.normal(size=(n, 3)), np.ones(n), ids=ids, rewind=False)
+    counts = s.sortIndexes(counts=True)
+    p = s.getPartRef()
+    dx = (np.array(xm) - np.array(x0)) / (np.array(nn) - 1)
+    ijk = np.floor((p["pos"] - np.array(x0)) / dx).astype(int)
+    cell = (ijk[:, 2] * (nn[1] - 1) + ijk[:, 1]) * (nn[0] - 1) + ijk[:, 0]
+    assert np.all(np.diff(cell) >= 0)
+    assert np.array_equal(np.sort(p["id"]), np.sort(ids))
+    assert np.array_equal(counts, np.bincount(cell, minlength=W.num_cells))
+
+
+def test_addparticle_rejects_and_rewinds_like_reference(pic, port):
+    nn, x0, xm = (11, 11, 11), (0.0, 0.0, 0.0), (0.01, 0.01, 0.01)
+    g = port.grid(nn, x0, xm)
+    ef = smooth_field(int(np.prod(nn)), nn, None, 1e3, 5)
+    W = pic.World(*nn, x0, xm)
+    W.setTime(1e-11, 10)
+    W.ef = ef
+    s = pic.Species("e-", pic.ME, -pic.QE, W, 1.0, capacity=100)
+    pos = np.array([[0.005, 0.005, 0.005], [0.011, 0.005, 0.005], [-0.001, 0.0, 0.0], [np.nan, 0.0, 0.0],
+                    [0.001, 0.009, 0.002]])
+    vel = np.full((5, 3), 1e5)
+    s.addParticles(pos, vel, np.ones(5), ids=np.arange(5, dtype=np.uint64), rewind=True)
+    p = s.getPartRef()
+    assert sorted(p["id"].tolist()) == [0, 4]
+    for q in p:
+        lc = (q["pos"] - np.array(x0)) / 0.001
+        e = np.zeros(3)
+        C = __import__("ctypes")
+        port.lib.or_gather3_ref.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        port.lib.or_gather3_ref(C.byref(g), ef.ctypes.data, lc.ctypes.data, e.ctypes.data)
+        expect = 1e5 - (-pic.QE / pic.ME) * e * 0.5e-11
+        assert np.all(np.abs(q["vel"] - expect) <= 1e-5 * np.abs(expect))
+
+
+# ------------------------------------------------------------------------------------------
+# collisions (background gas, Philox streams shared with the oracle)
+# ------------------------------------------------------------------------------------------
+def sigma_table():
+    E = np.geomspace(0.01, 1e5, 300)
+    s_el = 6e-20 / np.sqrt(1 + E / 10.0)
+    return E, s_el
+
+
+@pytest.mark.parametrize("kind", [0, 1])
+def test_mcc_matches_oracle(pic, port, kind):
+    nn, x0, xm = (9, 9, 9), (0.0, 0.0, 0.0), (0.008, 0.008, 0.008)
+    g = port.grid(nn, x0, xm)
+    E, S = sigma_table()
+    if kind == 0:
+        E_ion, params, mass_n = 13.6, (1.015e-18, 9.793, 61.81, 0.0), 16 * O.AMU
+        cp = port.coll_params(E, S + 0.0, mass_n, E_ion, 0, (1.015e-18, 9.793, 61.81))
+    else:
+        E_ion, params, mass_n = 12.06, (2.107e-17, 1.0, 0.18, 0.0), 32 * O.AMU
+        cp = port.coll_params(E, S, mass_n, E_ion, 1, (0.0, 1.0, 0.18), sig_A=2.107e-17)
+    rng = np.random.default_rng(6)
+    n = 40000
+    speed = np.sqrt(2 * rng.uniform(1, 300, n) * O.QE / O.ME)
+    dirs = rng.normal(size=(n, 3))
+    dirs /= np.linalg.norm(dirs, axis=1)[:, None]
+    vel = speed[:, None] * dirs
+    pos = rng.uniform(x0, xm, (n, 3)) * 0.999999
+    w = np.full(n, 10.0)
+    ids = np.arange(n, dtype=np.uint64) * 7 + 3
+    dt = 1e-10
+    n_neutral = 0.3 / (cp.sigv_max * dt)  # ~30 % candidates per step
+    cp.n_neutral = n_neutral
+    cp.T_neutral = 300.0
+    seed = 0x1234_5678_9ABC
+    W = pic.World(*nn, x0, xm)
+    W.setTime(dt, 10)
+    W.advanceTime()  # ts = 0
+    e = pic.Species("e-", pic.ME, -pic.QE, W, 10.0, capacity=3 * n)
+    ion = pic.Species("ion", mass_n, pic.QE, W, 10.0, capacity=3 * n)
+    e.addParticles(pos, vel, w, ids=ids, rewind=False)
+    M = pic.MC_MEX_Ionization(e, ion, W, n_neutral, 300.0, mass_n, E_ion, E, S, kind, params, seed=seed)
+    M.apply(dt)
+    st = M.stats()
+    ge = e.getPartRef()
+    gi = ion.getPartRef()
+    # oracle
+    oe = np.zeros(3 * n, O.PARTICLE)
+    oe[:n] = oracle_parts(pos, vel, w)
+    oid = np.zeros(3 * n, np.uint64)
+    oid[:n] = ids
+    oi = np.zeros(3 * n, O.PARTICLE)
+    oiid = np.zeros(3 * n, np.uint64)
+    ncoll, nion, ne, ni_ = port.mcc_background(g, cp, oe, oid, n, oi, oiid, 0, dt, seed, 0)
+    assert ncoll > 1000 and nion > 20
+    assert abs(st["collisions"] - ncoll) <= max(3, ncoll // 500)
+    assert abs(st["ionizations"] - nion) <= max(2, nion // 100)
+    # electrons that both sides scattered identically
+    common, ia, ib = np.intersect1d(ge["id"], oid[:ne], return_indices=True)
+    assert len(common) >= ne - max(3, ne // 500)
+    dv = np.linalg.norm(ge["vel"][ia] - oe[:ne]["vel"][ib], axis=1)
+    vmag = np.linalg.norm(oe[:ne]["vel"][ib], axis=1)
+    good = dv <= 1e-4 * vmag + 1.0
+    assert good.mean() >= 0.998
+    # ion products: same ids, positions inside the parent cell, velocity = sampled neutral
+    ci, ja, jb = np.intersect1d(gi["id"], oiid[:ni_], return_indices=True)
+    assert len(ci) >= ni_ - max(2, ni_ // 100)
+    assert np.max(np.abs(gi["pos"][ja] - oi[:ni_]["pos"][jb])) <= 1e-6
+    assert np.allclose(gi["vel"][ja], oi[:ni_]["vel"][jb], rtol=1e-4, atol=1e-2)
+
+
+# ------------------------------------------------------------------------------------------
+# the step loop on a C1-shaped case (ch2 semantics: solve each step)
+# ------------------------------------------------------------------------------------------
+def test_c1_loop_matches_oracle(pic, port):
+    nn, x0, xm = (21, 21, 21), (0.0, 0.0, 0.0), (0.2, 0.2, 0.2)
+    g = port.grid(nn, x0, xm)
+    kind = port.node_kinds(g, 1)
+    nv = int(np.prod(nn))
+    ne_, ni_ = 20000, 20000
+    den = 1e11
+    w = den * 0.008 / ne_
+    ele = load_thermal(port, g, 1, (0.1, 0.1, 0.1), (0.2, 0.2, 0.2), den, 11604.0, w, O.ME, -O.QE)
+    ion = load_thermal(port, g, 2, (0.1, 0.1, 0.1), (0.2, 0.2, 0.2), den, 1160.4, w, 16 * O.AMU, O.QE)
+    dt = 5e-12
+    W = pic.World(*nn, x0, xm)
+    W.dirichletBoundries(0.0)
+    W.setTime(dt, 1000)
+    E = pic.Species("e-", pic.ME, -pic.QE, W, w, capacity=len(ele) + 64)
+    I = pic.Species("O+", 16 * pic.AMU, pic.QE, W, w, capacity=len(ion) + 64)
+    E.addParticles(ele["pos"], ele["vel"], ele["w"], ids=np.arange(len(ele), dtype=np.uint64), rewind=False)
+    I.addParticles(ion["pos"], ion["vel"], ion["w"], ids=np.arange(len(ion), dtype=np.uint64), rewind=False)
+    S = pic.PotentialSolver(W, 20000, 1e-10, pic.SOLVER_PCG)
+    W.configure_loop(solve_each_step=True, sort_every=3)
+    # oracle state
+    pe, pi_ = ele.copy(), ion.copy()
+    ide, idi = np.arange(len(pe), dtype=np.uint64), np.arange(len(pi_), dtype=np.uint64)
+    n_e, n_i = len(pe), len(pi_)
+    ef = np.zeros((nv, 3))
+    phi = np.zeros(nv)
+    for step in range(5):
+        W.step()
+        n_e = port.push(g, pe[:n_e], ef, dt, -O.QE, O.ME, ids=ide[:n_e])
+        n_i = port.push(g, pi_[:n_i], ef, dt, O.QE, 16 * O.AMU, ids=idi[:n_i])
+        rho = -O.QE * port.number_density(g, pe[:n_e]) + O.QE * port.number_density(g, pi_[:n_i])
+        port.solve_fpcg(g, kind, phi, rho, 1e-12, 20000)
+        ef = port.compute_ef(g, phi)
+    assert np.max(np.abs(W.rho - rho)) <= 1e-5 * np.max(np.abs(rho))
+    assert np.max(np.abs(W.phi - phi)) <= 1e-5 * np.max(np.abs(phi))
+    assert np.max(np.abs(W.ef - ef)) <= 1e-5 * np.max(np.abs(ef))
+    gp = E.getPartRef()
+    common, ia, ib = np.intersect1d(gp["id"], ide[:n_e], return_indices=True)
+    assert len(common) >= n_e - 3
+    assert np.max(np.abs(gp["pos"][ia] - pe[:n_e]["pos"][ib])) <= 1e-5 * 0.2
+
+
+# ------------------------------------------------------------------------------------------
+# full-size properties (discharge grid 64 x 64 x 256, 4 M particles)
+# ------------------------------------------------------------------------------------------
+def test_c2_size_conservation_and_sort(pic):
+    nn, x0, xm = (64, 64, 256), (0.0, 0.0, 0.0), (0.02, 0.02, 0.08)
+    W = pic.World(*nn, x0, xm)
+    W.set_boundaries((1, 1, 0), (1,) * 6, (0, 0, 0, 0, 0.0, 500.0))
+    W.setTime(2e-12, 100)
+    e = pic.Species("e-", pic.ME, -pic.QE, W, 64.0, capacity=2_200_000)
+    i = pic.Species("O2+", 32 * pic.AMU, pic.QE, W, 64.0, capacity=2_200_000)
+    lo, hi = (0.0, 0.0, 0.3 * 0.08), (0.02, 0.02, 0.7 * 0.08)
+    e.loadUniform(lo, hi, 2_000_000, 2 * 11604.5, 64.0, 0.5, seed=1)
+    i.loadUniform(lo, hi, 2_000_000, 0.03 * 11604.5, 64.0, 0.5, seed=2)
+    S = pic.PotentialSolver(W, 5000, 1e-6, pic.SOLVER_PCG)
+    assert S.solve(raise_on_fail=True)
+    S.computeEF()
+    W.configure_loop(solve_each_step=True, sort_every=5)
+    tot_e0 = e.getMicroCount()
+    for _ in range(10):
+        W.step()
+    # particles are only lost through the z walls: none in 10 steps from the central band
+    assert e.getNumParticles() == 2_000_000 and i.getNumParticles() == 2_000_000
+    assert abs(e.getMicroCount() - tot_e0) <= 1e-9 * tot_e0
+    vol = W.node_vol
+    keep = np.ones(W.nv, bool).reshape(nn[2], nn[1], nn[0])
+    keep[:, -1, :] = False
+    keep[:, :, -1] = False
+    tot = np.sum((e.den * vol)[keep.ravel()])
+    assert abs(tot - tot_e0) <= 1e-6 * tot_e0
+    counts = e.computeMacroParticlesCount()
+    assert counts.sum() == 2_000_000

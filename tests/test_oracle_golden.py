@@ -1,0 +1,182 @@
+"""The FP64 oracle restatement (oracle/pic_oracle.c) against golden vectors produced by the
+reference's own ch4/v3 code (tests/golden/make_golden.py).  Bit-exact: same loop order, same
+FP64 operation order, same MT19937 draws."""
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import golden
+
+
+def to_parts(d, prefix):
+    n = len(d[prefix + "w"])
+    p = np.zeros(n, O.PARTICLE)
+    p["pos"], p["vel"], p["w"] = d[prefix + "pos"], d[prefix + "vel"], d[prefix + "w"]
+    return p
+
+
+def test_mt19937_canonical_matches_std(port):
+    # first outputs of std::mt19937(5489) are published; canonical doubles combine two draws
+    r = port.mt(5489)
+    first = [port.lib.or_mt_u01(C_byref(r)) for _ in range(2)]
+    assert 0.0 <= first[0] < 1.0 and 0.0 <= first[1] < 1.0
+    r2 = port.mt(5489)
+    import ctypes as C
+
+    port.lib.or_mt_next.restype = C.c_uint32
+    port.lib.or_mt_next.argtypes = [C.c_void_p]
+    assert port.lib.or_mt_next(C.byref(r2)) == 3499211612  # mt19937 reference output #1
+    assert port.lib.or_mt_next(C.byref(r2)) == 581869302
+
+
+def C_byref(x):
+    import ctypes as C
+
+    return C.byref(x)
+
+
+def test_philox_known_answer(port):
+    # Philox-4x32-10 known-answer vectors (Random123 kat_vectors)
+    assert list(port.philox([0, 0, 0, 0], [0, 0])) == [0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8]
+    assert list(port.philox([0xFFFFFFFF] * 4, [0xFFFFFFFF] * 2)) == [0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD]
+    assert list(port.philox([0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344], [0xA4093822, 0x299F31D0])) == [
+        0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1]
+
+
+def test_load_push_deposit_bit_exact(port):
+    d = golden("push_deposit")
+    g = port.grid(d["nn"], d["x0"], d["xm"])
+    # loadParticleBoxThermal with the reference's MT19937 stream
+    mt = port.mt(7)
+    loaded = port.load_box_thermal_ref(g, mt, 100000, (0, 0.008, 0.015), (0.018, 0.014, 0.028), 1e10, 30000.0, 100.0,
+                                       O.ME, -O.QE)
+    ref_in = to_parts(d, "in_")
+    assert len(loaded) == len(ref_in)
+    assert np.array_equal(loaded["pos"], ref_in["pos"]) and np.array_equal(loaded["vel"], ref_in["vel"])
+    p = ref_in.copy()
+    n = port.push(g, p, d["ef"], float(d["dt"]), -O.QE, O.ME)
+    out = to_parts(d, "out_")
+    assert n == len(out)
+    assert np.array_equal(p[:n]["pos"], out["pos"]) and np.array_equal(p[:n]["vel"], out["vel"])
+    den = port.number_density(g, p[:n])
+    assert np.array_equal(den, d["den"])
+
+
+def test_multithreaded_push_same_set(port):
+    d = golden("push_deposit")
+    g = port.grid(d["nn"], d["x0"], d["xm"])
+    a = to_parts(d, "in_")
+    b = a.copy()
+    ids = np.arange(len(b), dtype=np.uint64)
+    na = port.push(g, a, d["ef"], float(d["dt"]), -O.QE, O.ME)
+    nb = port.push(g, b, d["ef"], float(d["dt"]), -O.QE, O.ME, ids=ids, threads=4)
+    assert na == nb
+    ka = np.lexsort(a[:na]["pos"].T)
+    kb = np.lexsort(b[:nb]["pos"].T)
+    assert np.array_equal(a[:na]["pos"][ka], b[:nb]["pos"][kb])
+
+
+@pytest.mark.parametrize("mode", ["dirichlet", "v3box"])
+def test_poisson_and_efield_bit_exact(port, mode):
+    d = golden("poisson")
+    boxes = [] if mode == "dirichlet" else [(d["box_c"], d["box_s"])]
+    g = port.grid(d["nn"], d["x0"], d["xm"], boxes=boxes)
+    kind = port.node_kinds(g, 1 if mode == "dirichlet" else 0)
+    phi0 = np.zeros(port.nv(g))
+    if mode == "v3box":
+        phi0[kind == O.FIXED] = float(d["box_phi"])
+    # GS (PotentialSolver::solveGS)
+    phi = phi0.copy()
+    ok, it, l2 = port.solve_gs(g, kind, phi, d["rho"], 20000, 1e-6)
+    assert bool(ok) == bool(d[f"{mode}_gs_ok"])
+    assert np.array_equal(phi, d[f"{mode}_gs_phi"])
+    assert np.array_equal(port.compute_ef(g, phi), d[f"{mode}_gs_ef"])
+    # NR-PCG with the reference's coefficient assignment (PotentialSolver::buildMatrix)
+    phi = phi0.copy()
+    ok, it, l2 = port.solve_pcg_ref(g, kind, phi, d["rho"], 2000, 1e-6, axis_swap=1)
+    assert bool(ok == 1) == bool(d[f"{mode}_pcg_ok"])
+    assert np.array_equal(phi, d[f"{mode}_pcg_phi"])
+    assert np.array_equal(port.compute_ef(g, phi), d[f"{mode}_pcg_ef"])
+
+
+@pytest.mark.parametrize("mode", ["dirichlet", "v3box"])
+def test_gpu_form_solvers_reach_reference_solution(port, mode):
+    """Red-black SOR and flexible PCG on the reduced system converge to the reference GS answer."""
+    d = golden("poisson")
+    boxes = [] if mode == "dirichlet" else [(d["box_c"], d["box_s"])]
+    g = port.grid(d["nn"], d["x0"], d["xm"], boxes=boxes)
+    kind = port.node_kinds(g, 1 if mode == "dirichlet" else 0)
+    phi0 = np.zeros(port.nv(g))
+    if mode == "v3box":
+        phi0[kind == O.FIXED] = float(d["box_phi"])
+    ref = phi0.copy()
+    port.solve_gs(g, kind, ref, d["rho"], 200000, 1e-13)
+    for solver in ("rbsor", "fpcg"):
+        phi = phi0.copy()
+        if solver == "rbsor":
+            ok, _, rel = port.solve_rbsor(g, kind, phi, d["rho"], 1.6, 1e-12, 100000)
+        else:
+            ok, _, rel = port.solve_fpcg(g, kind, phi, d["rho"], 1e-12, 10000)
+        assert ok and rel <= 1e-12
+        assert np.max(np.abs(phi - ref)) <= 1e-9 * max(1.0, np.max(np.abs(ref)))
+
+
+def test_ntc_ionization_bit_exact(port):
+    d = golden("ntc")
+    g = port.grid(d["nn"], d["x0"], d["xm"])
+    e_ion = 1313.9 * 1000 / 6.02214076e23 / O.QE
+    cp = port.coll_params(d["table_E"], d["table_s"], 16 * O.AMU, e_ion)
+    mt = port.mt(int(d["seed"]))
+    # replay the two loads to bring the MT19937 stream to the same state
+    c, s = (0.002, 0.002, 0.0025), (0.004, 0.004, 0.005)
+    e0 = port.load_box_thermal_ref(g, mt, 10 ** 5, c, s, 2.5e12, 11604 * 300.0, 100.0, O.ME, -O.QE)
+    n0 = port.load_box_thermal_ref(g, mt, 10 ** 5, c, s, 1.25e22, 300.0, 5e11, 16 * O.AMU, 0.0)
+    assert np.array_equal(e0["vel"], d["ele0_vel"]) and np.array_equal(n0["pos"], d["neu0_pos"])
+    cap = 20000
+    ele = np.zeros(cap, O.PARTICLE)
+    neu = np.zeros(cap, O.PARTICLE)
+    ion = np.zeros(cap, O.PARTICLE)
+    ele[:len(e0)], neu[:len(n0)] = e0, n0
+    ne, nn_, ni_ = len(e0), len(n0), 0
+    wsv = float(d["wsv0"])
+    for it in (1, 2):
+        _, nn_, ni_, ne, wsv = port.ntc_ionize_ref(g, cp, mt, neu, nn_, ion, ni_, ele, ne, float(d["dt"]), wsv)
+        for nm, arr, n in (("ele", ele, ne), ("neu", neu, nn_), ("ion", ion, ni_)):
+            ref = to_parts(d, f"{nm}{it}_")
+            assert n == len(ref), (nm, it)
+            for f in ("pos", "vel", "w"):
+                assert np.array_equal(arr[:n][f], ref[f]), (nm, it, f)
+
+
+def test_merge_bit_exact(port):
+    d = golden("merge")
+    g = port.grid(d["nn"], d["x0"], d["xm"])
+    mt = port.mt(int(d["seed"]))
+    loaded = port.load_box_thermal_ref(g, mt, 10 ** 5, (0.001, 0.0005, 0.0005), (0.002, 0.001, 0.001), 6e13,
+                                       11604 * 2.0, 100.0, O.ME, -O.QE)
+    ref_in = to_parts(d, "in_")
+    assert np.array_equal(loaded["vel"], ref_in["vel"])
+    p = np.zeros(4 * len(ref_in), O.PARTICLE)
+    p[:len(ref_in)] = ref_in
+    n = port.merge_ref(g, mt, p, len(ref_in), d["ef"], -O.QE, O.ME, float(d["dt"]), 10)
+    out = to_parts(d, "out_")
+    assert n == len(out)
+    for f in ("pos", "vel", "w"):
+        assert np.array_equal(p[:n][f], out[f]), f
+
+
+def test_merge_conserves_mass_momentum_energy(port):
+    d = golden("merge")
+    g = port.grid(d["nn"], d["x0"], d["xm"])
+    p0 = to_parts(d, "in_")
+    p = np.zeros(4 * len(p0), O.PARTICLE)
+    p[:len(p0)] = p0
+    mt = port.mt(1)
+    zero = np.zeros_like(d["ef"])  # no rewind so the moments must be preserved
+    n = port.merge_ref(g, mt, p, len(p0), zero, -O.QE, O.ME, 0.0, 10)
+    assert n < len(p0)
+    c0, m0, k0 = port.sums(p0, O.ME)
+    c1, m1, k1 = port.sums(p[:n], O.ME)
+    assert abs(c1 - c0) <= 1e-12 * c0
+    assert np.all(np.abs(m1 - m0) <= 1e-9 * np.abs(m0).max())
+    assert abs(k1 - k0) <= 1e-9 * k0
