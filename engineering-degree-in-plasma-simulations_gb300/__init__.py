@@ -87,6 +87,7 @@ def library():
         "pic_loop_configure": [vp, i, i, vp, i, i, i],
         "pic_step": [vp],
         "pic_species_merge": [vp, i, i],
+        "pic_merge_stats": [vp, vp],
         "pic_synchronize": [vp],
         "pic_last_error": [C.c_char_p, i],
         "pic_timing_enable": [vp, i],
@@ -348,6 +349,11 @@ class Species:
 
     def merge(self, min_count=10):
         _check(self._L.pic_species_merge(self.world._h, self.id, int(min_count)))
+
+    def merge_stats(self):
+        out = np.zeros(4, np.uint64)
+        _check(self._L.pic_merge_stats(self.world._h, _p(out)))
+        return dict(bins=int(out[0]), removed=int(out[1]), dropped=int(out[2]))
 
     def sums(self):
         out = np.zeros(5)

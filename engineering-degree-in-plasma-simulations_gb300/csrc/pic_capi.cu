@@ -86,6 +86,8 @@ struct pic_world {
     int* cell_count = nullptr;
     int* cell_start = nullptr;
     int* scan_aux = nullptr;
+    int* merge_list = nullptr;  // candidate cells of a merge (num_cells + 1 ints)
+    unsigned long long* merge_stats = nullptr;
     unsigned* err = nullptr;
     std::vector<SpeciesHost> sp;
     // boundaries
@@ -383,10 +385,8 @@ extern "C" int pic_world_create(pic_world** out, int ni, int nj, int nk, const d
     cudaMemsetAsync(w->flag, 0, sizeof(int) * 4, w->stream);
     w->grid_nodes = (int)std::min<long long>(kParts, std::max<long long>(1, (nv + 255) / 256));
     w->grid_parts = w->sms * 8;
-    int occ = 0;
     w->grid_push = w->sms * 3;
     w->grid_push_mcc = w->sms * 2;
-    (void)occ;
     fill_grid_boxes(w);
     int rc = upload_kinds(w, true);
     if (rc != PIC_OK) {
@@ -418,7 +418,7 @@ extern "C" int pic_world_destroy(pic_world* w) {
     void* ptrs[] = {w->ef,   w->phi,  w->phi_alt, w->rho,        w->kind,       w->r,        w->e,
                     w->d,    w->d2,   w->q,       w->z,          w->part,       w->scal,     w->flag,
                     w->cell_count,    w->cell_start,             w->scan_aux,   w->err,      w->tE,
-                    w->tS,   w->stats};
+                    w->tS,   w->stats,  w->merge_list, w->merge_stats};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (w->h_scal) cudaFreeHost(w->h_scal);
@@ -1107,9 +1107,41 @@ extern "C" int pic_loop_configure(pic_world* w, int solve_each_step, int sort_ev
 }
 
 extern "C" int pic_species_merge(pic_world* w, int sp, int min_count) {
-    (void)min_count;
-    if (!valid_sp(w, sp)) return fail(PIC_ERR_ARG, "bad species");
-    return fail(PIC_ERR_ARG, "merge is not available in this build");
+    if (!valid_sp(w, sp) || min_count < 3) return fail(PIC_ERR_ARG, "bad species or min_count < 3");
+    CU(cudaSetDevice(w->device));
+    if (!w->merge_list) {
+        CU(cudaMalloc((void**)&w->merge_list, sizeof(int) * (w->g.nc + 1)));
+        CU(cudaMalloc((void**)&w->merge_stats, sizeof(unsigned long long) * 4));
+        CU(cudaMemsetAsync(w->merge_stats, 0, sizeof(unsigned long long) * 4, w->stream));
+    }
+    sort_species(w, sp);  // cells must be contiguous runs
+    SpeciesHost& s = w->sp[sp];
+    uint64_t seed = w->mcc_seed ^ 0x6D65726765ull;
+    {
+        Scope sc(w, "merge", 2);
+        launch_merge(w->g, s.dev, w->ef, w->cell_start, w->merge_list + 1, w->merge_list, min_count,
+                     (float)(s.charge / s.mass * 0.5 * w->dt), make_uint2((unsigned)seed, (unsigned)(seed >> 32)),
+                     (unsigned)w->ts, w->err, w->merge_stats, w->stream, w->sms * 8);
+    }
+    {
+        Scope sc(w, "compact", 4);
+        launch_commit_appends(s.dev, w->err, w->stream);
+        launch_compact(s.dev, w->stream, w->sms * 4);
+    }
+    CU(cudaGetLastError());
+    return PIC_OK;
+}
+
+extern "C" int pic_merge_stats(pic_world* w, uint64_t* out) {
+    if (!w || !out) return fail(PIC_ERR_ARG, "null argument");
+    CU(cudaSetDevice(w->device));
+    if (!w->merge_stats) {
+        out[0] = out[1] = out[2] = 0;
+        return PIC_OK;
+    }
+    CU(cudaMemcpyAsync(out, w->merge_stats, sizeof(unsigned long long) * 3, cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    return PIC_OK;
 }
 
 extern "C" int pic_step(pic_world* w) {

@@ -60,6 +60,9 @@ struct LoadArgs {
 };
 void launch_load_uniform(const GridDev& g, SpeciesDev sp, const LoadArgs& la, cudaStream_t s);
 void launch_sums(SpeciesDev sp, double* out, cudaStream_t s, int grid);
+void launch_merge(const GridDev& g, SpeciesDev sp, const float4* ef, const int* cell_start, int* list, int* nlist,
+                  int min_count, float qm_half_dt, uint2 key, unsigned step, unsigned* err,
+                  unsigned long long* stats, cudaStream_t s, int grid);
 
 // fields
 struct FinalizeArgs {

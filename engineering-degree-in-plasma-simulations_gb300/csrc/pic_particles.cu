@@ -868,4 +868,215 @@ __global__ void k_sums(SpeciesDev sp, double* part) {
 }
 void launch_sums(SpeciesDev sp, double* out, cudaStream_t s, int grid) { k_sums<<<grid, 256, 0, s>>>(sp, out); }
 
+// ------------------------------------------------------------------------------------
+// velocity-binned merge (Species::merge + sortVelocitiesInCell, Species.cpp:981-1145)
+// GPU form: per cell a CTA bins velocities on a 15^3 grid between the cell's min and max,
+// orders the cell by (bin, Philox hash of the id), and every bin with more than two particles
+// becomes two particles of half the bin weight at mean +- per-axis rms velocity, placed at the
+// two members with the smallest hashes (the reference picks two random members).  Sums are
+// FP64 in that order, so the result does not depend on the order of the particles in memory.
+// ------------------------------------------------------------------------------------
+constexpr int kMergeThreads = 128;
+constexpr int kMergeMax = 1024;  // particles of one cell handled per merge
+constexpr int kVelGrid = 15;     // Species.h:129
+
+__global__ void k_merge_candidates(SpeciesDev sp, const int* start, int nc, int min_count, int* list, int* nlist) {
+    int n = sp.counts[0];
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+        int cnt = (c + 1 < nc ? start[c + 1] : n) - start[c];
+        if (cnt >= min_count) list[atomicAdd(nlist, 1)] = c;
+    }
+}
+
+__device__ __forceinline__ int vel_bin(float v, float vmin, float dv) {
+    if (!(dv > 0.f)) return 0;
+    int b = (int)__fdiv_rn(__fsub_rn(v, vmin), dv);
+    return b < 0 ? 0 : (b > kVelGrid - 1 ? kVelGrid - 1 : b);
+}
+
+struct MergeArgs {
+    GridDev g;
+    SpeciesDev sp;
+    const float4* ef;
+    const int* start;
+    const int* list;
+    const int* nlist;
+    float qm_half_dt;  // rewind of addParticle (Species.cpp:431), global dt
+    uint2 key;
+    unsigned step;
+    unsigned* err;
+    unsigned long long* stats;  // [0] bins merged, [1] particles removed, [2] products dropped (NaN)
+};
+
+__global__ void __launch_bounds__(kMergeThreads) k_merge(MergeArgs a) {
+    __shared__ unsigned long long keys[kMergeMax];
+    __shared__ float4 vs[kMergeMax];
+    __shared__ float s_red[6][kMergeThreads / 32];
+    __shared__ float s_min[3], s_dv[3];
+    const int n = a.sp.counts[0];
+    const int nl = *a.nlist;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int li = blockIdx.x; li < nl; li += gridDim.x) {
+        const int c = a.list[li];
+        const int s0 = a.start[c];
+        int m = (c + 1 < a.g.nc ? a.start[c + 1] : n) - s0;
+        if (m > kMergeMax) {
+            if (tid == 0) set_error(a.err, kErrMergeTruncated);
+            m = kMergeMax;
+        }
+        float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (int q = tid; q < m; q += kMergeThreads) {
+            float4 v = a.sp.vel[s0 + q];
+            vs[q] = v;
+            mn[0] = fminf(mn[0], v.x); mn[1] = fminf(mn[1], v.y); mn[2] = fminf(mn[2], v.z);
+            mx[0] = fmaxf(mx[0], v.x); mx[1] = fmaxf(mx[1], v.y); mx[2] = fmaxf(mx[2], v.z);
+        }
+        for (int d = 0; d < 3; d++) {
+            for (int o = 16; o > 0; o >>= 1) {
+                mn[d] = fminf(mn[d], __shfl_xor_sync(0xffffffffu, mn[d], o));
+                mx[d] = fmaxf(mx[d], __shfl_xor_sync(0xffffffffu, mx[d], o));
+            }
+            if (lane == 0) {
+                s_red[d][warp] = mn[d];
+                s_red[3 + d][warp] = mx[d];
+            }
+        }
+        __syncthreads();
+        if (tid < 3) {
+            float lo = s_red[tid][0], hi = s_red[3 + tid][0];
+            for (int w = 1; w < kMergeThreads / 32; w++) {
+                lo = fminf(lo, s_red[tid][w]);
+                hi = fmaxf(hi, s_red[3 + tid][w]);
+            }
+            hi = hi > 0.f ? __fmul_rn(hi, 1.001f) : __fmul_rn(hi, 0.999f);  // Species.cpp:1007-1013
+            s_min[tid] = lo;
+            s_dv[tid] = __fdiv_rn(__fsub_rn(hi, lo), (float)kVelGrid);
+        }
+        __syncthreads();
+        // keys: bin (12 bits) | hash (42 bits) | local index (10 bits)
+        int P = 1;
+        while (P < m) P <<= 1;
+        for (int q = tid; q < P; q += kMergeThreads) {
+            if (q < m) {
+                float4 v = vs[q];
+                int b = (vel_bin(v.x, s_min[0], s_dv[0]) * kVelGrid + vel_bin(v.y, s_min[1], s_dv[1])) * kVelGrid +
+                        vel_bin(v.z, s_min[2], s_dv[2]);
+                unsigned long long id = a.sp.id[s0 + q];
+                uint4 h = philox4x32_10(make_uint4((unsigned)id, (unsigned)(id >> 32), a.step, 0x4D455247u), a.key);
+                unsigned long long hh = ((unsigned long long)h.y << 32 | h.x) & ((1ull << 42) - 1);
+                keys[q] = ((unsigned long long)b << 52) | (hh << 10) | (unsigned long long)q;
+            } else {
+                keys[q] = ~0ull;
+            }
+        }
+        __syncthreads();
+        // bitonic sort of P keys
+        for (int k = 2; k <= P; k <<= 1)
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                for (int q = tid; q < P; q += kMergeThreads) {
+                    int r = q ^ j;
+                    if (r > q) {
+                        unsigned long long x = keys[q], y = keys[r];
+                        bool up = (q & k) == 0;
+                        if ((x > y) == up) {
+                            keys[q] = y;
+                            keys[r] = x;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        // one thread per run of equal bins
+        for (int q = tid; q < m; q += kMergeThreads) {
+            unsigned bq = (unsigned)(keys[q] >> 52);
+            if (q > 0 && (unsigned)(keys[q - 1] >> 52) == bq) continue;
+            int e = q + 1;
+            while (e < m && (unsigned)(keys[e] >> 52) == bq) e++;
+            if (e - q <= 2) continue;  // Species.cpp:1058: merge bins with more than two particles
+            double W = 0, M[3] = {0, 0, 0}, E[3] = {0, 0, 0};
+            for (int r = q; r < e; r++) {
+                float4 v = vs[keys[r] & 1023];
+                double w = v.w, vx = v.x, vy = v.y, vz = v.z;
+                W += w;
+                M[0] += w * vx; M[1] += w * vy; M[2] += w * vz;
+                E[0] += w * (vx * vx); E[1] += w * (vy * vy); E[2] += w * (vz * vz);
+            }
+            double inv = 1.0 / W;
+            for (int d = 0; d < 3; d++) {
+                M[d] *= inv;
+                E[d] = E[d] * inv - M[d] * M[d];
+            }
+            for (int d = 0; d < 3; d++)  // Species.cpp:1074-1082
+                if (E[d] < 0) {
+                    if (E[d] < -10e-5) break;
+                    E[d] = 0;
+                }
+            double sq[3] = {sqrt(E[0]), sqrt(E[1]), sqrt(E[2])};
+            int la = (int)(keys[q] & 1023), lb = (int)(keys[q + 1] & 1023);
+            for (int r = q; r < e; r++) {
+                int p = s0 + (int)(keys[r] & 1023);
+                float4 ps = a.sp.pos[p];
+                a.sp.pos[p] = make_float4(ps.x, ps.y, ps.z, __int_as_float(-1));
+            }
+            int base = atomicAdd(&a.sp.counts[2], e - q);
+            for (int r = q; r < e; r++) a.sp.dead[base + (r - q)] = s0 + (int)(keys[r] & 1023);
+            atomicAdd(&a.stats[0], 1ull);
+            atomicAdd(&a.stats[1], (unsigned long long)(e - q));
+            int i, j, k;
+            cell_ijk(a.g, c, i, j, k);
+            int bnode = cell_base_node(a.g, i, j, k);
+            Tile t;
+            t.etile = nullptr;
+            t.dtile = nullptr;
+            t.lo = 0;
+            t.off[0] = 0;
+            t.off[1] = a.g.ni;
+            t.off[2] = a.g.ni * a.g.nj;
+            t.off[3] = a.g.ni * a.g.nj + a.g.ni;
+            PushArgs pa;
+            pa.ef = a.ef;
+            for (int side = 0; side < 2; side++) {
+                int l = side == 0 ? la : lb;
+                float4 ps = a.sp.pos[s0 + l];
+                float3 o = make_float3(ps.x, ps.y, ps.z);
+                double sgn = side == 0 ? 1.0 : -1.0;
+                float3 v = make_float3((float)(M[0] + sgn * sq[0]), (float)(M[1] + sgn * sq[1]),
+                                       (float)(M[2] + sgn * sq[2]));
+                if (isnan(v.x) || isnan(v.y) || isnan(v.z)) {  // addParticle drops NaN (Species.cpp:421-423)
+                    atomicAdd(&a.stats[2], 1ull);
+                    continue;
+                }
+                float3 Ev = gather_e(pa, t, bnode, o);
+                v.x -= a.qm_half_dt * Ev.x;
+                v.y -= a.qm_half_dt * Ev.y;
+                v.z -= a.qm_half_dt * Ev.z;
+                unsigned long long pid = child_id(a.sp.id[s0 + l], a.step, 3);
+                append_particle(a.sp, n, make_float4(o.x, o.y, o.z, __int_as_float(c)),
+                                make_float4(v.x, v.y, v.z, (float)(W * 0.5)), pid, a.err);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+void launch_merge(const GridDev& g, SpeciesDev sp, const float4* ef, const int* cell_start, int* list, int* nlist,
+                  int min_count, float qm_half_dt, uint2 key, unsigned step, unsigned* err,
+                  unsigned long long* stats, cudaStream_t s, int grid) {
+    cudaMemsetAsync(nlist, 0, sizeof(int), s);
+    k_merge_candidates<<<1024, 256, 0, s>>>(sp, cell_start, g.nc, min_count, list, nlist);
+    MergeArgs a;
+    a.g = g;
+    a.sp = sp;
+    a.ef = ef;
+    a.start = cell_start;
+    a.list = list;
+    a.nlist = nlist;
+    a.qm_half_dt = qm_half_dt;
+    a.key = key;
+    a.step = step;
+    a.err = err;
+    a.stats = stats;
+    k_merge<<<grid, kMergeThreads, 0, s>>>(a);
+}
+
 }  // namespace pic

@@ -147,6 +147,8 @@ int pic_step(pic_world* w);
 /* velocity-binned merge (Species::merge, Species.cpp:981-1145) of cells holding at least
  * min_count particles; sorts the species first */
 int pic_species_merge(pic_world* w, int sp, int min_count);
+/* merge counters since creation: bins merged, particles removed, products dropped (NaN) */
+int pic_merge_stats(pic_world* w, uint64_t* out);
 
 /* ---- runtime ------------------------------------------------------------------------- */
 int pic_synchronize(pic_world* w);

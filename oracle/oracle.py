@@ -103,6 +103,7 @@ class Port:
             "or_child_id": (C.c_uint64, [C.c_uint64, u32, u32]),
             "or_ntc_ionize_ref": (l, [vp, vp, vp, vp, vp, l, vp, vp, l, vp, vp, l, d, vp]),
             "or_merge_ref": (l, [vp, vp, vp, l, l, vp, d, d, d, i]),
+            "or_merge_gpuform": (l, [vp, vp, vp, vp, l, l, vp, d, d, d, i, u32, u32, u32]),
             "or_load_box_thermal_ref": (l, [vp, vp, vp, l, vp, vp, d, d, d, d, d, vp, d]),
             "or_sums": (None, [vp, l, d, vp, vp, vp]),
         }
@@ -237,6 +238,12 @@ class Port:
     def merge_ref(self, g, r, parts, n, ef, charge, mass, dt, min_count=10):
         return self.lib.or_merge_ref(C.byref(g), C.byref(r), _p(parts), n, len(parts),
                                      _p(np.ascontiguousarray(ef, np.float64)), charge, mass, dt, min_count)
+
+    def merge_gpuform(self, g, parts, ids, n, ef, charge, mass, dt, min_count, seed, step, cells=None):
+        cl = None if cells is None else np.ascontiguousarray(cells, np.int32)
+        return self.lib.or_merge_gpuform(C.byref(g), _p(parts), _p(ids), _p(cl), n, len(parts),
+                                         _p(None if ef is None else np.ascontiguousarray(ef, np.float64)), charge,
+                                         mass, dt, min_count, seed & 0xffffffff, (seed >> 32) & 0xffffffff, step)
 
     def load_box_thermal_ref(self, g, r, cap, x0, sides, num_den, T, mpw0, mass, charge, ef=None, dt=0.0):
         parts = np.zeros(cap, PARTICLE)

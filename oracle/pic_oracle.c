@@ -1329,6 +1329,114 @@ long or_merge_ref(const or_grid* g, or_mt* r, or_particle* p, long n, long cap, 
     return np;
 }
 
+static int vel_bin_f(float v, float vmin, float dv) {
+    if (!(dv > 0.f)) return 0;
+    int b = (int)((v - vmin) / dv);
+    return b < 0 ? 0 : (b > 14 ? 14 : b);
+}
+typedef struct {
+    uint64_t key;
+    long idx;
+} mkey;
+static int cmp_mkey(const void* a, const void* b) {
+    uint64_t x = ((const mkey*)a)->key, y = ((const mkey*)b)->key;
+    return (x > y) - (x < y);
+}
+long or_merge_gpuform(const or_grid* g, or_particle* p, uint64_t* ids, const int32_t* cells, long n, long cap,
+                      const double* ef, double charge, double mass, double dt_global, int min_count,
+                      uint32_t seed_lo, uint32_t seed_hi, uint32_t step) {
+    long nc = (long)(g->ni - 1) * (g->nj - 1) * (g->nk - 1);
+    ilist* cl = (ilist*)calloc(nc, sizeof(ilist));
+    for (long q = 0; q < n; q++) il_push(&cl[cells ? cells[q] : xtoc(g, p[q].pos)], q);
+    long np = n;
+    uint32_t key[2] = {seed_lo, seed_hi};
+    for (long c = 0; c < nc; c++) {
+        long m = cl[c].n;
+        if (m < min_count) continue;
+        if (m > 1024) m = 1024; /* the device handles 1024 particles per cell and flags the rest */
+        float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (long q = 0; q < m; q++)
+            for (int d = 0; d < 3; d++) {
+                float v = (float)p[cl[c].idx[q]].vel[d];
+                lo[d] = fminf(lo[d], v);
+                hi[d] = fmaxf(hi[d], v);
+            }
+        float dv[3];
+        for (int d = 0; d < 3; d++) {
+            hi[d] = hi[d] > 0.f ? hi[d] * 1.001f : hi[d] * 0.999f;
+            dv[d] = (hi[d] - lo[d]) / 15.0f;
+        }
+        mkey* keys = (mkey*)malloc(sizeof(mkey) * m);
+        for (long q = 0; q < m; q++) {
+            long pi = cl[c].idx[q];
+            int b = (vel_bin_f((float)p[pi].vel[0], lo[0], dv[0]) * 15 + vel_bin_f((float)p[pi].vel[1], lo[1], dv[1])) *
+                        15 + vel_bin_f((float)p[pi].vel[2], lo[2], dv[2]);
+            uint32_t ctr[4] = {(uint32_t)ids[pi], (uint32_t)(ids[pi] >> 32), step, 0x4D455247u}, out[4];
+            or_philox4x32_10(ctr, key, out);
+            uint64_t hh = (((uint64_t)out[1] << 32) | out[0]) & ((1ull << 42) - 1);
+            keys[q].key = ((uint64_t)b << 52) | (hh << 10) | (uint64_t)q;
+            keys[q].idx = pi;
+        }
+        qsort(keys, m, sizeof(mkey), cmp_mkey);
+        for (long q = 0; q < m;) {
+            long e = q + 1;
+            while (e < m && (keys[e].key >> 52) == (keys[q].key >> 52)) e++;
+            if (e - q > 2) {
+                double W = 0, M[3] = {0, 0, 0}, E[3] = {0, 0, 0};
+                for (long r = q; r < e; r++) {
+                    or_particle* pp = &p[keys[r].idx];
+                    double w = (float)pp->w;
+                    double v3[3] = {(float)pp->vel[0], (float)pp->vel[1], (float)pp->vel[2]};
+                    W += w;
+                    for (int d = 0; d < 3; d++) M[d] += w * v3[d];
+                    for (int d = 0; d < 3; d++) E[d] += w * (v3[d] * v3[d]);
+                }
+                double inv = 1.0 / W;
+                for (int d = 0; d < 3; d++) {
+                    M[d] *= inv;
+                    E[d] = E[d] * inv - M[d] * M[d];
+                }
+                for (int d = 0; d < 3; d++)
+                    if (E[d] < 0) {
+                        if (E[d] < -10e-5) break;
+                        E[d] = 0;
+                    }
+                double sq[3] = {sqrt(E[0]), sqrt(E[1]), sqrt(E[2])};
+                for (int side = 0; side < 2; side++) {
+                    long src = keys[q + side].idx;
+                    double sgn = side == 0 ? 1.0 : -1.0;
+                    double v[3] = {(float)(M[0] + sgn * sq[0]), (float)(M[1] + sgn * sq[1]), (float)(M[2] + sgn * sq[2])};
+                    if (isnan(v[0]) || isnan(v[1]) || isnan(v[2]) || np >= cap) continue;
+                    double lc[3], e3[3] = {0, 0, 0};
+                    xtol(g, p[src].pos, lc);
+                    if (ef) or_gather3_ref(g, ef, lc, e3);
+                    or_particle* o = &p[np];
+                    for (int d = 0; d < 3; d++) {
+                        o->pos[d] = p[src].pos[d];
+                        o->vel[d] = v[d] - charge / mass * 0.5 * dt_global * e3[d];
+                    }
+                    o->w = (float)(W * 0.5);
+                    ids[np] = or_child_id(ids[src], step, 3);
+                    np++;
+                }
+                for (long r = q; r < e; r++) p[keys[r].idx].w = 0;
+            }
+            q = e;
+        }
+        free(keys);
+    }
+    /* remove merged members keeping the order of the rest */
+    long k = 0;
+    for (long q = 0; q < np; q++)
+        if (p[q].w != 0) {
+            p[k] = p[q];
+            ids[k] = ids[q];
+            k++;
+        }
+    free_cells(cl, nc);
+    return k;
+}
+
 /* Species::sampleVth / sampleV3th (Species.cpp:855-869) */
 static double sample_vth(or_mt* r, double T, double mass) {
     double v_th = sqrt(2 * OR_KB * T / mass);

@@ -131,6 +131,16 @@ long or_ntc_ionize_ref(const or_grid* g, const or_coll_params* cp, or_mt* r, or_
 long or_merge_ref(const or_grid* g, or_mt* r, or_particle* p, long n, long cap, const double* ef, double charge,
                   double mass, double dt_global, int min_count);
 
+/* GPU form of the merge (restated from the CUDA kernel): per cell with >= min_count particles
+ * (cells[] given, or computed from positions when NULL), velocities binned on 15^3 in FP32
+ * exactly as the device does, members ordered by (bin, Philox hash of id); bins with more than
+ * two particles become two particles placed at the two smallest-hash members, ids from
+ * or_child_id(member id, step, 3).  Merged members get w = 0 and are removed at the end.
+ * Returns the new count. */
+long or_merge_gpuform(const or_grid* g, or_particle* p, uint64_t* ids, const int32_t* cells, long n, long cap,
+                      const double* ef, double charge, double mass, double dt_global, int min_count,
+                      uint32_t seed_lo, uint32_t seed_hi, uint32_t step);
+
 /* Reference loadParticleBoxThermal (Species.cpp:564-599, 855-869), with rejection and rewind (E given). */
 long or_load_box_thermal_ref(const or_grid* g, or_mt* r, or_particle* p, long cap, const double* x0,
                              const double* sides, double num_den, double T, double mpw0, double mass, double charge,

@@ -425,3 +425,65 @@ def test_c2_size_conservation_and_sort(pic):
     assert abs(tot - tot_e0) <= 1e-6 * tot_e0
     counts = e.computeMacroParticlesCount()
     assert counts.sum() == 2_000_000
+
+
+# ------------------------------------------------------------------------------------------
+# merge (velocity-binned, GPU form restated in the oracle)
+# ------------------------------------------------------------------------------------------
+def gpu_cells(pos, x0, dx, nn):
+    ijk = np.floor((pos - np.asarray(x0)) / np.asarray(dx)).astype(np.int64)
+    ijk = np.minimum(np.maximum(ijk, 0), np.asarray(nn) - 2)
+    return ((ijk[:, 2] * (nn[1] - 1) + ijk[:, 1]) * (nn[0] - 1) + ijk[:, 0]).astype(np.int32)
+
+
+def test_merge_matches_oracle_gpu_form(pic, port):
+    d = golden("merge")
+    nn, x0, xm = d["nn"], d["x0"], d["xm"]
+    dt = float(d["dt"])
+    W = pic.World(*nn, x0, xm)
+    W.setTime(dt, 10)
+    W.ef = d["ef"]
+    W.advanceTime()  # ts = 0
+    n = len(d["in_w"])
+    e = pic.Species("e-", pic.ME, -pic.QE, W, 100.0, capacity=4 * n)
+    ids = np.arange(n, dtype=np.uint64) * 3 + 1
+    e.addParticles(d["in_pos"], d["in_vel"], d["in_w"], ids=ids, rewind=False)
+    e.merge(min_count=10)
+    st = e.merge_stats()
+    gp = e.getPartRef()
+    g = port.grid(nn, x0, xm)
+    p = np.zeros(4 * n, O.PARTICLE)
+    p["pos"][:n] = d["in_pos"]
+    p["vel"][:n] = d["in_vel"].astype(np.float32).astype(np.float64)
+    p["w"][:n] = d["in_w"].astype(np.float32).astype(np.float64)
+    oid = np.zeros(4 * n, np.uint64)
+    oid[:n] = ids
+    dx = (np.asarray(xm) - np.asarray(x0)) / (np.asarray(nn) - 1)
+    cells = np.zeros(4 * n, np.int32)
+    cells[:n] = gpu_cells(d["in_pos"], x0, dx, nn)
+    n2 = port.merge_gpuform(g, p, oid, n, d["ef"], -O.QE, O.ME, dt, 10, 0x6D65726765, 0, cells=cells)
+    assert st["bins"] > 10 and st["removed"] > 3 * st["bins"] - 1
+    assert len(gp) == n2
+    assert np.array_equal(np.sort(gp["id"]), np.sort(oid[:n2]))
+    a, b = np.argsort(gp["id"]), np.argsort(oid[:n2])
+    assert np.max(np.abs(gp["vel"][a] - p[:n2]["vel"][b])) <= 1e-5 * np.max(np.abs(p[:n2]["vel"]))
+    assert np.allclose(gp["w"][a], p[:n2]["w"][b], rtol=1e-6)
+    assert np.max(np.abs(gp["pos"][a] - p[:n2]["pos"][b])) <= 1e-6 * np.max(dx)
+
+
+def test_merge_conserves_weight_momentum_energy(pic):
+    nn, x0, xm = (5, 5, 5), (0.0, 0.0, 0.0), (0.004, 0.004, 0.004)
+    rng = np.random.default_rng(12)
+    n = 40000
+    W = pic.World(*nn, x0, xm)
+    W.setTime(1e-12, 10)
+    e = pic.Species("e-", pic.ME, -pic.QE, W, 10.0, capacity=2 * n)
+    e.addParticles(rng.uniform(x0, xm, (n, 3)) * 0.999, rng.normal(size=(n, 3)) * 3e5, rng.lognormal(2, 0.5, n),
+                   rewind=False)
+    s0 = e.sums()
+    e.merge(min_count=65)
+    s1 = e.sums()
+    assert e.getNumParticles() < n
+    assert abs(s1[0] - s0[0]) <= 1e-6 * s0[0]
+    assert np.all(np.abs(s1[1:4] - s0[1:4]) <= 1e-5 * np.abs(s0[1:4]).max())
+    assert abs(s1[4] - s0[4]) <= 1e-5 * s0[4]
