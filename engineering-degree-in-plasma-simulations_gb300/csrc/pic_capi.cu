@@ -331,7 +331,10 @@ extern "C" int pic_world_create(pic_world** out, int ni, int nj, int nk, const d
                                 int device) {
     if (!out || !x0 || !xm) return fail(PIC_ERR_ARG, "null argument");
     *out = nullptr;
-    if (ni < 3 || nj < 3 || nk < 3) return fail(PIC_ERR_ARG, "need at least 3 nodes per axis");
+    if (ni < 2 || nj < 2 || nk < 2) return fail(PIC_ERR_ARG, "need at least 2 nodes per axis");
+    // particles store their cell packed as i | j << 10 | k << 20
+    if (ni - 1 > 1024 || nj - 1 > 1024 || nk - 1 > 2047)
+        return fail(PIC_ERR_ARG, "at most 1024 x 1024 x 2047 cells");
     long long nv = (long long)ni * nj * nk;
     if (nv > (1ll << 30)) return fail(PIC_ERR_ARG, "grid too large (%lld nodes)", nv);
     for (int d = 0; d < 3; d++)
@@ -352,6 +355,8 @@ extern "C" int pic_world_create(pic_world** out, int ni, int nj, int nk, const d
     g.ck = nk - 1;
     g.nv = (int)nv;
     g.nc = g.ci * g.cj * g.ck;
+    g.fd_ni = make_fastdiv((unsigned)ni);
+    g.fd_nj = make_fastdiv((unsigned)nj);
     int nn[3] = {ni, nj, nk};
     for (int d = 0; d < 3; d++) {
         g.x0[d] = x0[d];

@@ -32,7 +32,24 @@ enum DevError : unsigned {
     kErrNaN = 1u << 3,
 };
 
+// division by a runtime constant with a multiply-high (Granlund & Montgomery 1994), exact for
+// every 32-bit dividend; d >= 2
+struct FastDiv {
+    unsigned d, m, l;
+};
+__host__ __device__ inline FastDiv make_fastdiv(unsigned d) {
+    unsigned l = 0;
+    while ((1ull << l) < d) l++;
+    unsigned long long m = ((1ull << 32) * ((1ull << l) - d)) / d + 1;
+    return FastDiv{d, (unsigned)m, l};
+}
+__device__ __forceinline__ unsigned fdiv(unsigned n, const FastDiv& f) {
+    unsigned t = __umulhi(f.m, n);
+    return (t + ((n - t) >> 1)) >> (f.l - 1);
+}
+
 struct GridDev {
+    FastDiv fd_ni, fd_nj;  // node index decoding
     int ni, nj, nk;       // nodes
     int ci, cj, ck;       // cells per axis (n-1)
     int nv, nc;           // node and cell totals
@@ -83,8 +100,20 @@ __device__ __forceinline__ void set_error(unsigned* err, unsigned bit) {
     if (err) atomicOr(err, bit);
 }
 
-// cell index -> (i, j, k)
-__device__ __forceinline__ void cell_ijk(const GridDev& g, int c, int& i, int& j, int& k) {
+// A particle's cell is stored packed, i | j << 10 | k << 20 (i, j < 1024, k < 2048): decoding
+// needs no division, and the packed value orders cells exactly like the linear index
+// c = (k*(nj-1) + j)*(ni-1) + i of World::XtoC, which the sort and the cell lists use.
+__device__ __forceinline__ int pack_cell(int i, int j, int k) { return i | (j << 10) | (k << 20); }
+__device__ __forceinline__ void cell_ijk(const GridDev&, int c, int& i, int& j, int& k) {
+    i = c & 1023;
+    j = (c >> 10) & 1023;
+    k = c >> 20;
+}
+__device__ __forceinline__ int cell_linear(const GridDev& g, int c) {
+    return ((c >> 20) * g.cj + ((c >> 10) & 1023)) * g.ci + (c & 1023);
+}
+// linear cell index -> (i, j, k)
+__device__ __forceinline__ void linear_ijk(const GridDev& g, int c, int& i, int& j, int& k) {
     int cij = g.ci * g.cj;
     k = c / cij;
     int r = c - k * cij;

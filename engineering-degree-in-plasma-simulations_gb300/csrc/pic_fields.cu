@@ -21,11 +21,11 @@ namespace pic {
 constexpr double kEps0 = 8.85418782e-12;  // ch4/v3/src/all.h:16
 
 __device__ __forceinline__ void node_ijk(const GridDev& g, int n, int& i, int& j, int& k) {
-    int nij = g.ni * g.nj;
-    k = n / nij;
-    int r = n - k * nij;
-    j = r / g.ni;
-    i = r - j * g.ni;
+    unsigned t = fdiv((unsigned)n, g.fd_ni);
+    i = n - (int)t * g.ni;
+    unsigned kk = fdiv(t, g.fd_nj);
+    j = (int)t - (int)kk * g.nj;
+    k = (int)kk;
 }
 // neighbour index along an axis with periodic wrap (the copy at n-1 folds onto 0)
 __device__ __forceinline__ int wrap_m(int c, int n, int per) { return (per && c == 0) ? n - 2 : c - 1; }
@@ -58,23 +58,23 @@ __device__ __forceinline__ void stencil(const GridDev& g, int i, int j, int k, S
 // ------------------------------------------------------------------------------------
 __global__ void k_finalize_rho(FinalizeArgs a) {
     const GridDev& g = a.g;
+    const double inv_base = 1.0 / (g.dxd[0] * g.dxd[1] * g.dxd[2]);
+    const int nn[3] = {g.ni, g.nj, g.nk}, stride[3] = {1, g.ni, g.ni * g.nj};
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
-        int i, j, k;
-        node_ijk(g, n, i, j, k);
-        int ijk[3] = {i, j, k}, nn[3] = {g.ni, g.nj, g.nk};
+        int ijk[3];
+        node_ijk(g, n, ijk[0], ijk[1], ijk[2]);
         bool alias = false;
         unsigned fold = 0;
-        double vol = g.dxd[0] * g.dxd[1] * g.dxd[2];
+        double inv_vol = inv_base;  // boundary nodes have half volume per face: exact powers of two
         for (int d = 0; d < 3; d++) {
             if (g.periodic[d]) {
                 if (ijk[d] == nn[d] - 1) alias = true;
                 if (ijk[d] == 0) fold |= 1u << d;
             } else if (ijk[d] == 0 || ijk[d] == nn[d] - 1) {
-                vol *= 0.5;
+                inv_vol *= 2.0;
             }
         }
         if (alias) continue;  // written by the node it copies
-        int stride[3] = {1, g.ni, g.ni * g.nj};
         double rho = 0;
         float den_out[kMaxSpecies];
         for (int s = 0; s < a.ns; s++) {
@@ -84,27 +84,36 @@ __global__ void k_finalize_rho(FinalizeArgs a) {
                 rho += (double)a.charge[s] * (double)den_out[s];
                 continue;
             }
-            unsigned long long tot = 0;
-            for (unsigned m = 0; m < 8; m++) {
+            unsigned long long tot = a.acc[s][n];
+            a.acc[s][n] = 0ull;
+            if (fold) {
+                for (unsigned m = 1; m < 8; m++) {
+                    if (m & ~fold) continue;
+                    int node = n;
+                    for (int d = 0; d < 3; d++)
+                        if (m & (1u << d)) node += (nn[d] - 1) * stride[d];
+                    tot += a.acc[s][node];
+                    a.acc[s][node] = 0ull;
+                }
+            }
+            double den = (double)tot * ((double)a.inv_scale[s] * inv_vol);
+            den_out[s] = (float)den;
+            rho += (double)a.charge[s] * den;
+        }
+        const float rf = (float)rho;
+        for (int s = 0; s < a.ns; s++)
+            if (a.fresh[s]) a.den[s][n] = den_out[s];
+        a.rho[n] = rf;
+        if (fold) {
+            for (unsigned m = 1; m < 8; m++) {
                 if (m & ~fold) continue;
                 int node = n;
                 for (int d = 0; d < 3; d++)
                     if (m & (1u << d)) node += (nn[d] - 1) * stride[d];
-                tot += a.acc[s][node];
-                a.acc[s][node] = 0ull;
+                for (int s = 0; s < a.ns; s++)
+                    if (a.fresh[s]) a.den[s][node] = den_out[s];
+                a.rho[node] = rf;
             }
-            double den = (double)tot * (double)a.inv_scale[s] / vol;
-            den_out[s] = (float)den;
-            rho += (double)a.charge[s] * den;
-        }
-        for (unsigned m = 0; m < 8; m++) {
-            if (m & ~fold) continue;
-            int node = n;
-            for (int d = 0; d < 3; d++)
-                if (m & (1u << d)) node += (nn[d] - 1) * stride[d];
-            for (int s = 0; s < a.ns; s++)
-                if (a.fresh[s]) a.den[s][node] = den_out[s];
-            a.rho[node] = (float)rho;
         }
     }
 }
@@ -123,29 +132,32 @@ void launch_den_avg(float* avg, const float* den, int nv, float a, float b, cuda
 // E = -grad(phi): central inside, second-order one-sided on non-periodic faces
 // ------------------------------------------------------------------------------------
 __global__ void k_efield(GridDev g, const double* __restrict__ phi, float4* __restrict__ ef) {
-    int stride[3] = {1, g.ni, g.ni * g.nj}, nn[3] = {g.ni, g.nj, g.nk};
+    const int stride[3] = {1, g.ni, g.ni * g.nj}, nn[3] = {g.ni, g.nj, g.nk};
+    float inv2[3];
+    for (int d = 0; d < 3; d++) inv2[d] = (float)(1.0 / (2.0 * g.dxd[d]));
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
         int ijk[3];
         node_ijk(g, n, ijk[0], ijk[1], ijk[2]);
         float e[3];
         for (int d = 0; d < 3; d++) {
-            int c = ijk[d], st = stride[d], N = nn[d];
-            double inv2 = 1.0 / (2.0 * g.dxd[d]);
-            double v;
+            const int c = ijk[d], st = stride[d], N = nn[d];
+            double v;  // the difference of potentials is taken in FP64, the scaling in FP32
             if (g.periodic[d]) {
                 int cc = (c == N - 1) ? 0 : c;
                 int base = n - (c - cc) * st;
                 int im = base + (((cc == 0) ? N - 2 : cc - 1) - cc) * st;
                 int ip = base + (((cc + 1 == N - 1) ? 0 : cc + 1) - cc) * st;
-                v = (phi[im] - phi[ip]) * inv2;
+                v = phi[im] - phi[ip];
+            } else if (N == 2) {
+                v = c == 0 ? 2.0 * (phi[n] - phi[n + st]) : 2.0 * (phi[n - st] - phi[n]);  // first order
             } else if (c == 0) {
-                v = (3 * phi[n] - 4 * phi[n + st] + phi[n + 2 * st]) * inv2;
+                v = 3 * phi[n] - 4 * phi[n + st] + phi[n + 2 * st];
             } else if (c == N - 1) {
-                v = (-phi[n - 2 * st] + 4 * phi[n - st] - 3 * phi[n]) * inv2;
+                v = -phi[n - 2 * st] + 4 * phi[n - st] - 3 * phi[n];
             } else {
-                v = (phi[n - st] - phi[n + st]) * inv2;
+                v = phi[n - st] - phi[n + st];
             }
-            e[d] = (float)v;
+            e[d] = (float)v * inv2[d];
         }
         ef[n] = make_float4(e[0], e[1], e[2], 0.f);
     }
@@ -196,7 +208,7 @@ __global__ void k_residual(GridDev g, const double* __restrict__ phi_in, double*
                            const float* __restrict__ e, const float* __restrict__ rho,
                            const uint16_t* __restrict__ kind, float* __restrict__ r, double* part, int apply_e) {
     double acc[2] = {0.0, 0.0};
-    const double inv_eps0 = 1.0 / kEps0;
+    const float inv_eps0 = (float)(1.0 / kEps0);
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
         uint16_t kd = kind[n];
         if ((kd & 3) != kFree) {
@@ -208,24 +220,31 @@ __global__ void k_residual(GridDev g, const double* __restrict__ phi_in, double*
         node_ijk(g, n, i, j, k);
         Stencil s;
         stencil(g, i, j, k, s);
-        double vp = phi_in[n] + (apply_e ? (double)e[n] : 0.0);
-        double diag = 0, off = 0, bfix = 0;
+        const double pp = phi_in[n];
+        const float ep = apply_e ? e[n] : 0.f;
+        // L(phi + e)_p = sum over axes of c (2 v_p - v_minus - v_plus), a mirror neighbour taking
+        // the value of p.  The second differences of the potential are formed in FP64 (the two
+        // neighbour terms cancel to high relative precision), the rest in FP32.
+        float lphi = 0.f, bfix = 0.f;
 #pragma unroll
-        for (int d = 0; d < 6; d++) {
-            if (kd & (1u << (2 + d))) continue;  // mirror wall: equals phi_p
-            double c = (double)s.c[d];
-            int q = s.q[d];
-            diag += c;
-            double vq = phi_in[q] + (apply_e ? (double)e[q] : 0.0);
-            off += c * vq;
-            if (kd & (1u << (8 + d))) bfix += c * vq;
+        for (int ax = 0; ax < 3; ax++) {
+            const int dm = 2 * ax, dp = 2 * ax + 1;
+            const bool mm = kd & (1u << (2 + dm)), mp = kd & (1u << (2 + dp));
+            const double pm = mm ? pp : phi_in[s.q[dm]];
+            const double pq = mp ? pp : phi_in[s.q[dp]];
+            float d2 = (float)((pp - pm) + (pp - pq));
+            if (apply_e) d2 += (2.f * ep - (mm ? ep : e[s.q[dm]])) - (mp ? ep : e[s.q[dp]]);
+            lphi += s.c[dm] * d2;
+            if (kd & (1u << (8 + dm))) bfix += s.c[dm] * (float)pm;
+            if (kd & (1u << (8 + dp))) bfix += s.c[dp] * (float)pq;
         }
-        double b = (double)rho[n] * inv_eps0 + bfix;
-        double res = (double)rho[n] * inv_eps0 - (diag * vp - off);
-        if (apply_e) phi_out[n] = vp;
-        r[n] = (float)res;
-        acc[0] += res * res;
-        acc[1] += b * b;
+        const float src = rho[n] * inv_eps0;
+        const float res = src - lphi;
+        if (apply_e) phi_out[n] = pp + (double)ep;
+        r[n] = res;
+        const float b = src + bfix;
+        acc[0] += (double)res * (double)res;
+        acc[1] += (double)b * (double)b;
     }
     block_partials<2>(acc, part, kParts);
 }
@@ -307,6 +326,7 @@ __device__ __forceinline__ float diag_of(uint16_t kd, const Stencil& s) {
 __global__ void k_pcg_init(GridDev g, const float* __restrict__ r, float* __restrict__ z, float* __restrict__ e,
                            const uint16_t* __restrict__ kind, double* part, int* flag) {
     double acc[1] = {0.0};
+    float facc = 0.f;  // per-thread partial in FP32, block and grid sums in FP64
     if (blockIdx.x == 0 && threadIdx.x == 0) flag[0] = 0;
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
         uint16_t kd = kind[n];
@@ -321,8 +341,9 @@ __global__ void k_pcg_init(GridDev g, const float* __restrict__ r, float* __rest
         stencil(g, i, j, k, s);
         float zz = r[n] / diag_of(kd, s);
         z[n] = zz;
-        acc[0] += (double)r[n] * (double)zz;
+        facc += r[n] * zz;
     }
+    acc[0] = facc;
     block_partials<1>(acc, part + 1 * kParts, kParts);  // slot 1: r.z
 }
 __global__ void k_pcg_k1(GridDev g, const float* __restrict__ z, const float* __restrict__ d_in,
@@ -343,6 +364,7 @@ __global__ void k_pcg_k1(GridDev g, const float* __restrict__ z, const float* __
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) scal[it & 1] = rz_new;
     double acc[1] = {0.0};
+    float facc = 0.f;
     float fb = (float)beta;
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
         uint16_t kd = kind[n];
@@ -367,8 +389,9 @@ __global__ void k_pcg_k1(GridDev g, const float* __restrict__ z, const float* __
         float qv = dg * dn - off;
         d_out[n] = dn;
         q[n] = qv;
-        acc[0] += (double)dn * (double)qv;
+        facc += dn * qv;
     }
+    acc[0] = facc;
     block_partials<1>(acc, part + 0 * kParts, kParts);  // slot 0: d.q
 }
 __global__ void k_pcg_k2(GridDev g, const float* __restrict__ d, const float* __restrict__ q, float* __restrict__ e,
@@ -378,7 +401,7 @@ __global__ void k_pcg_k2(GridDev g, const float* __restrict__ d, const float* __
     double dq = sum_partials(part + 0 * kParts, gridDim.x);
     double rz = scal[it & 1];
     float alpha = dq != 0.0 ? (float)(rz / dq) : 0.f;
-    double acc[3] = {0.0, 0.0, 0.0};
+    float f0 = 0.f, f1 = 0.f, f2 = 0.f;
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
         uint16_t kd = kind[n];
         if ((kd & 3) != kFree) continue;
@@ -392,12 +415,12 @@ __global__ void k_pcg_k2(GridDev g, const float* __restrict__ d, const float* __
         float zo = z[n];
         float zn = rn / diag_of(kd, s);
         z[n] = zn;
-        acc[0] += (double)rn * (double)zn;
-        acc[1] += (double)rn * (double)zo;
-        acc[2] += (double)rn * (double)rn;
+        f0 += rn * zn;
+        f1 += rn * zo;
+        f2 += rn * rn;
     }
     __syncthreads();
-    double a1[1] = {acc[0]}, a2[1] = {acc[1]}, a3[1] = {acc[2]};
+    double a1[1] = {f0}, a2[1] = {f1}, a3[1] = {f2};
     block_partials<1>(a1, part + 1 * kParts, kParts);
     block_partials<1>(a2, part + 2 * kParts, kParts);
     block_partials<1>(a3, part + 3 * kParts, kParts);

@@ -19,6 +19,7 @@ constexpr int kPPT = 4;                     // particles per thread per chunk
 constexpr int kChunk = kThreads * kPPT;     // particles per chunk
 constexpr int kSeg = 512;                   // nodes per staged row segment
 constexpr int kMargin = 2;                  // deposit window starts this many nodes below the gather window
+// E rows (float4) + 64-bit fixed-point deposit tile, four rows of kSeg nodes each
 constexpr size_t kPushSmem = 4 * kSeg * sizeof(float4) + 4 * kSeg * sizeof(unsigned long long);
 constexpr long long kWaitLimit = 1ll << 24;  // mbarrier polls before giving up
 
@@ -119,26 +120,33 @@ __device__ float3 new_vel_electron(const CollDev& c, float E, float3 u, float r_
 // push helpers
 // ------------------------------------------------------------------------------------
 struct Tile {
-    const float4* etile;  // staged E rows, or nullptr
-    unsigned long long* dtile;
-    int lo;               // first node of the gather window
-    int off[4];           // node offsets of the four rows: 0, ni, ni*nj, ni*nj+ni
+    const float4* etile;       // staged E rows (row m at etile + m*kSeg), or nullptr
+    unsigned long long* dtile; // deposit tile (row m at dtile + m*kSeg), or nullptr
+    int lo;                    // first node of the gather window
+    int off[4];                // node offsets of the four rows: 0, ni, ni*nj, ni*nj+ni
 };
 
-__device__ __forceinline__ float4 load_e(const PushArgs& a, const Tile& t, int b, int m, int di) {
-    if (t.etile) return t.etile[m * kSeg + (b - t.lo) + di];
-    return __ldg(&a.ef[b + t.off[m] + di]);
-}
-
-// trilinear gather at (base node b, offsets o): the eight corners of Field::gather
+// E at the eight corners of the cell whose base node is b (Field::gather order)
 __device__ __forceinline__ float3 gather_e(const PushArgs& a, const Tile& t, int b, float3 o) {
+    const float4* e0;
+    int r1, r2, r3;
+    if (t.etile) {
+        e0 = t.etile + (b - t.lo);
+        r1 = kSeg;
+        r2 = 2 * kSeg;
+        r3 = 3 * kSeg;
+    } else {
+        e0 = a.ef + b;
+        r1 = t.off[1];
+        r2 = t.off[2];
+        r3 = t.off[3];
+    }
+    float4 e000 = e0[0], e100 = e0[1], e010 = e0[r1], e110 = e0[r1 + 1];
+    float4 e001 = e0[r2], e101 = e0[r2 + 1], e011 = e0[r3], e111 = e0[r3 + 1];
     float wx1 = o.x, wx0 = 1.f - o.x, wy1 = o.y, wy0 = 1.f - o.y, wz1 = o.z, wz0 = 1.f - o.z;
-    float4 e000 = load_e(a, t, b, 0, 0), e100 = load_e(a, t, b, 0, 1);
-    float4 e010 = load_e(a, t, b, 1, 0), e110 = load_e(a, t, b, 1, 1);
-    float4 e001 = load_e(a, t, b, 2, 0), e101 = load_e(a, t, b, 2, 1);
-    float4 e011 = load_e(a, t, b, 3, 0), e111 = load_e(a, t, b, 3, 1);
-    float w000 = wx0 * wy0 * wz0, w100 = wx1 * wy0 * wz0, w010 = wx0 * wy1 * wz0, w110 = wx1 * wy1 * wz0;
-    float w001 = wx0 * wy0 * wz1, w101 = wx1 * wy0 * wz1, w011 = wx0 * wy1 * wz1, w111 = wx1 * wy1 * wz1;
+    float a00 = wx0 * wy0, a10 = wx1 * wy0, a01 = wx0 * wy1, a11 = wx1 * wy1;
+    float w000 = a00 * wz0, w100 = a10 * wz0, w010 = a01 * wz0, w110 = a11 * wz0;
+    float w001 = a00 * wz1, w101 = a10 * wz1, w011 = a01 * wz1, w111 = a11 * wz1;
     float3 E;
     E.x = e000.x * w000 + e100.x * w100 + e010.x * w010 + e110.x * w110 + e001.x * w001 + e101.x * w101 +
           e011.x * w011 + e111.x * w111;
@@ -149,8 +157,8 @@ __device__ __forceinline__ float3 gather_e(const PushArgs& a, const Tile& t, int
     return E;
 }
 
-// advance offsets by v dt/dx, move across cells, wrap periodic axes; returns the new cell or
-// -1 when the particle leaves the domain or enters an absorbing object
+// advance offsets by v dt/dx, move across cells, wrap periodic axes; returns the new packed
+// cell or -1 when the particle leaves the domain or enters an absorbing object
 __device__ __forceinline__ int move_particle(const PushArgs& a, int i, int j, int k, float3& o, float3 v) {
     const GridDev& g = a.g;
     const float kBelowOne = 0x1.fffffep-1f;
@@ -162,10 +170,19 @@ __device__ __forceinline__ int move_particle(const PushArgs& a, int i, int j, in
     o.x = fminf(ox - fx, kBelowOne);
     o.y = fminf(oy - fy, kBelowOne);
     o.z = fminf(oz - fz, kBelowOne);
-    if (g.periodic[0]) { i %= g.ci; if (i < 0) i += g.ci; }
-    if (g.periodic[1]) { j %= g.cj; if (j < 0) j += g.cj; }
-    if (g.periodic[2]) { k %= g.ck; if (k < 0) k += g.ck; }
-    if (i < 0 || i >= g.ci || j < 0 || j >= g.cj || k < 0 || k >= g.ck) return -1;
+    if (g.periodic[0]) {
+        while (i < 0) i += g.ci;
+        while (i >= g.ci) i -= g.ci;
+    }
+    if (g.periodic[1]) {
+        while (j < 0) j += g.cj;
+        while (j >= g.cj) j -= g.cj;
+    }
+    if (g.periodic[2]) {
+        while (k < 0) k += g.ck;
+        while (k >= g.ck) k -= g.ck;
+    }
+    if ((unsigned)i >= (unsigned)g.ci || (unsigned)j >= (unsigned)g.cj || (unsigned)k >= (unsigned)g.ck) return -1;
     if (g.n_boxes) {
         float X = ((float)i + o.x) * g.dx[0], Y = ((float)j + o.y) * g.dx[1], Z = ((float)k + o.z) * g.dx[2];
         for (int bx = 0; bx < g.n_boxes; bx++)
@@ -173,54 +190,41 @@ __device__ __forceinline__ int move_particle(const PushArgs& a, int i, int j, in
                 Z >= g.box_lo[bx][2] && Z <= g.box_hi[bx][2])
                 return -1;
     }
-    return (k * g.cj + j) * g.ci + i;
+    return pack_cell(i, j, k);
 }
 
-// eight fixed-point corner contributions of a weight w at offsets o (Field::scatter order)
-__device__ __forceinline__ void corner_fixed(float w, float3 o, float scale, unsigned long long q[8]) {
+// the eight corner contributions of weight w at offsets o as 64-bit fixed point, added into the
+// shared tile when the cell's corners lie in the deposit window, else straight into HBM.
+// Integer sums do not depend on the order of the additions: rho is bit-reproducible.
+__device__ __forceinline__ void deposit_fixed(const PushArgs& a, const Tile& t, int b, float w, float3 o) {
     float wx1 = o.x, wx0 = 1.f - o.x, wy1 = o.y, wy0 = 1.f - o.y, wz1 = o.z, wz0 = 1.f - o.z;
-    float s = w * scale;
-    q[0] = __float2ull_rn(s * wx0 * wy0 * wz0);
-    q[1] = __float2ull_rn(s * wx1 * wy0 * wz0);
-    q[2] = __float2ull_rn(s * wx0 * wy1 * wz0);
-    q[3] = __float2ull_rn(s * wx1 * wy1 * wz0);
-    q[4] = __float2ull_rn(s * wx0 * wy0 * wz1);
-    q[5] = __float2ull_rn(s * wx1 * wy0 * wz1);
-    q[6] = __float2ull_rn(s * wx0 * wy1 * wz1);
-    q[7] = __float2ull_rn(s * wx1 * wy1 * wz1);
-}
-
-// commit the eight corner sums of a cell group: into the shared tile when the corner lies in
-// the deposit window, else straight to HBM
-__device__ __forceinline__ void commit_corners(const PushArgs& a, const Tile& t, int b, const unsigned long long q[8]) {
-#pragma unroll
-    for (int m = 0; m < 4; m++)
-#pragma unroll
-        for (int di = 0; di < 2; di++) {
-            unsigned long long v = q[2 * m + di];
-            if (v == 0) continue;
-            int node = b + t.off[m] + di;
-            int loc = b + di - (t.lo - kMargin);
-            if (t.dtile && loc >= 0 && loc < kSeg) atomicAdd(&t.dtile[m * kSeg + loc], v);
-            else atomicAdd(&a.sp.acc[node], v);
-        }
-}
-
-// corner values of one particle -> corner totals of its warp group (lanes that share the
-// cell), reduced with redux.sync on 21-bit limbs so that 64-bit fixed-point sums stay exact
-__device__ __forceinline__ void group_reduce(unsigned gmask, unsigned long long q[8]) {
-    unsigned long long hi = 0;
-#pragma unroll
-    for (int c = 0; c < 8; c++) hi |= q[c] >> 21;
-    bool need1 = __any_sync(0xffffffffu, hi != 0);
-    bool need2 = __any_sync(0xffffffffu, (hi >> 21) != 0);
-#pragma unroll
-    for (int c = 0; c < 8; c++) {
-        unsigned long long v = q[c];
-        unsigned long long s = __reduce_add_sync(gmask, (unsigned)(v & 0x1FFFFFull));
-        if (need1) s += (unsigned long long)__reduce_add_sync(gmask, (unsigned)((v >> 21) & 0x1FFFFFull)) << 21;
-        if (need2) s += (unsigned long long)__reduce_add_sync(gmask, (unsigned)(v >> 42)) << 42;
-        q[c] = s;
+    float s = w * a.dep_scale;
+    float s00 = s * wx0 * wy0, s10 = s * wx1 * wy0, s01 = s * wx0 * wy1, s11 = s * wx1 * wy1;
+    unsigned long long q000 = __float2ull_rn(s00 * wz0), q100 = __float2ull_rn(s10 * wz0);
+    unsigned long long q010 = __float2ull_rn(s01 * wz0), q110 = __float2ull_rn(s11 * wz0);
+    unsigned long long q001 = __float2ull_rn(s00 * wz1), q101 = __float2ull_rn(s10 * wz1);
+    unsigned long long q011 = __float2ull_rn(s01 * wz1), q111 = __float2ull_rn(s11 * wz1);
+    int loc = b - (t.lo - kMargin);
+    if (t.dtile && loc >= 0 && loc < kSeg - 1) {
+        unsigned long long* d = t.dtile + loc;
+        atomicAdd(d, q000);
+        atomicAdd(d + 1, q100);
+        atomicAdd(d + kSeg, q010);
+        atomicAdd(d + kSeg + 1, q110);
+        atomicAdd(d + 2 * kSeg, q001);
+        atomicAdd(d + 2 * kSeg + 1, q101);
+        atomicAdd(d + 3 * kSeg, q011);
+        atomicAdd(d + 3 * kSeg + 1, q111);
+    } else {
+        unsigned long long* d = a.sp.acc + b;
+        atomicAdd(d, q000);
+        atomicAdd(d + 1, q100);
+        atomicAdd(d + t.off[1], q010);
+        atomicAdd(d + t.off[1] + 1, q110);
+        atomicAdd(d + t.off[2], q001);
+        atomicAdd(d + t.off[2] + 1, q101);
+        atomicAdd(d + t.off[3], q011);
+        atomicAdd(d + t.off[3] + 1, q111);
     }
 }
 
@@ -239,11 +243,84 @@ __device__ __forceinline__ bool append_particle(const SpeciesDev& sp, int n_comm
     return true;
 }
 
+// Result of one accepted collision: the electron's new velocity, and for an ionisation the
+// ejected electron (velocity, offsets in the parent's cell) and the ion (neutral velocity).
+struct Collision {
+    int kind;  // 0 none, 1 elastic or failed ionisation, 2 ionisation
+    float3 v, pv, nv, po;
+};
+
+// MC_MEX_Ionization::collide with IONIZE_1 (Interactions.cpp:885-947), background-gas form.
+// Kept out of line: only the rare candidates (probability p_null) reach it.
+__device__ __noinline__ Collision collide_candidate(const CollDev& cd, unsigned long long id, float3 v, uint4 r0) {
+    Collision out;
+    out.kind = 0;
+    out.v = v;
+    uint4 ctr = make_uint4((unsigned)id, (unsigned)(id >> 32), cd.step, 1u);
+    uint4 r1 = philox4x32_10(ctr, cd.key);
+    const float kTwoPi = 6.283185307179586f;
+    float rr1 = sqrtf(-2.f * logf(u01(r0.y))), rr2 = sqrtf(-2.f * logf(u01(r1.x)));
+    float s1, c1, s2, c2;
+    sincosf(kTwoPi * u01(r0.z), &s1, &c1);
+    sincosf(kTwoPi * u01(r1.y), &s2, &c2);
+    float3 nv = make_float3(cd.sig_n * rr1 * c1, cd.sig_n * rr1 * s1, cd.sig_n * rr2 * c2);
+    float3 vr = make_float3(nv.x - v.x, nv.y - v.y, nv.z - v.z);
+    float v_rel = sqrtf(vr.x * vr.x + vr.y * vr.y + vr.z * vr.z);
+    float E_rel = cd.E_precalc_rel_eV * v_rel * v_rel;
+    float sig = sigma_coll(cd, E_rel);
+    if (!(u01(r0.w) * cd.sigv_max < sig * v_rel)) return out;
+    out.kind = 1;
+    out.nv = nv;
+    Draws dr;
+    dr.ctr = ctr;
+    dr.ctr.w = 2u;
+    dr.key = cd.key;
+    dr.buf = philox4x32_10(dr.ctr, cd.key);
+    dr.pos = 0;
+    float E_rel_J = cd.half_mred * v_rel * v_rel;
+    float P_ion = sigma_ion(cd, E_rel_J / 1.602176565e-19f) / sig;
+    if (dr.next() <= P_ion) {
+        float vmag = sqrtf(v.x * v.x + v.y * v.y + v.z * v.z);
+        float E_inc = vmag * vmag * cd.E_precalc_ele_eV;
+        if (E_inc < cd.E_ion_eV) return out;  // Interactions.cpp:901-905: no change
+        float E_ej = 10.0f * tanf(dr.next() * atanf((E_inc - cd.E_ion_eV) / (2.f * cd.B_inc)));
+        float E_sc = E_inc - cd.E_ion_eV - E_ej;
+        if (E_sc < 0.f) E_sc = 0.000001f;
+        float inv = 1.f / vmag;
+        float3 u = make_float3(v.x * inv, v.y * inv, v.z * inv);
+        float a1 = dr.next(), a2 = dr.next();
+        out.v = new_vel_electron(cd, E_sc, u, a1, a2);
+        float a3 = dr.next(), a4 = dr.next();
+        out.pv = new_vel_electron(cd, E_ej, u, a3, a4);
+        ctr.w = 4u;
+        uint4 r4 = philox4x32_10(ctr, cd.key);
+        out.po = make_float3(u01(r1.z), u01(r1.w), u01(r4.x));
+        out.kind = 2;
+    } else {
+        float inv_sum = 1.f / (cd.m_n + cd.m_e);
+        float3 cm = make_float3((cd.m_n * nv.x + cd.m_e * v.x) * inv_sum, (cd.m_n * nv.y + cd.m_e * v.y) * inv_sum,
+                                (cd.m_n * nv.z + cd.m_e * v.z) * inv_sum);
+        float cos_ksi = 2.f * dr.next() - 1.f;
+        float sin_ksi = sqrtf(fmaxf(1.f - cos_ksi * cos_ksi, 0.f));
+        float se, ce;
+        sincosf(2.f * 3.141592653f * dr.next(), &se, &ce);
+        float3 vr2 = make_float3(v_rel * cos_ksi, v_rel * sin_ksi * ce, v_rel * sin_ksi * se);
+        float f = cd.m_n * inv_sum;
+        out.v = make_float3(cm.x - f * vr2.x, cm.y - f * vr2.y, cm.z - f * vr2.z);
+    }
+    return out;
+}
+
 // ------------------------------------------------------------------------------------
 // fused collide + push + deposit
+//   A CTA takes chunks of 1024 particles (4 per thread).  For a cell-sorted chunk the four node
+//   rows its cells touch, [lo + off_m, lo + off_m + L), are bulk-copied (TMA) into shared
+//   memory; the gather reads them there, and the deposit accumulates into a shared 64-bit
+//   fixed-point tile that is committed to HBM with one atomic per touched node.  Unsorted
+//   chunks (span wider than a row segment) use global loads and atomics.
 // ------------------------------------------------------------------------------------
 template <bool kMcc>
-__global__ void __launch_bounds__(kThreads) k_push(PushArgs a) {
+__global__ void __launch_bounds__(kThreads, kMcc ? 2 : 3) k_push(PushArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     float4* etile = reinterpret_cast<float4*>(smem);
     unsigned long long* dtile = reinterpret_cast<unsigned long long*>(smem + 4 * kSeg * sizeof(float4));
@@ -265,6 +342,11 @@ __global__ void __launch_bounds__(kThreads) k_push(PushArgs a) {
     }
     __syncthreads();
     unsigned phase = 0;
+    Tile t;
+    t.off[0] = 0;
+    t.off[1] = g.ni;
+    t.off[2] = nij;
+    t.off[3] = nij + g.ni;
 
     for (int ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
         const int base = ch * kChunk;
@@ -280,9 +362,7 @@ __global__ void __launch_bounds__(kThreads) k_push(PushArgs a) {
                 V[q] = a.sp.vel[p];
                 int c = __float_as_int(P[q].w);
                 if (c >= 0) {
-                    int i, j, k;
-                    cell_ijk(g, c, i, j, k);
-                    bn[q] = cell_base_node(g, i, j, k);
+                    bn[q] = ((c >> 20) * g.nj + ((c >> 10) & 1023)) * g.ni + (c & 1023);
                     lmin = min(lmin, bn[q]);
                     lmax = max(lmax, bn[q]);
                 }
@@ -308,24 +388,19 @@ __global__ void __launch_bounds__(kThreads) k_push(PushArgs a) {
         __syncthreads();
         const int lo = s_lo, hi = s_hi;
         const bool use_tile = a.staged && hi >= 0 && (hi - lo + 2) <= kSeg - kMargin;
-        Tile t;
         t.lo = lo;
-        t.off[0] = 0;
-        t.off[1] = g.ni;
-        t.off[2] = nij;
-        t.off[3] = nij + g.ni;
         t.etile = nullptr;
         t.dtile = nullptr;
         if (use_tile) {
             if (tid == 0) {
-                // rows [lo + off_m, lo + off_m + L) of the node field, L = span + 2 nodes
                 unsigned bytes = (unsigned)(hi - lo + 2) * (unsigned)sizeof(float4);
                 fence_proxy_async();
                 mbar_expect_tx(&bar, 4 * bytes);
 #pragma unroll
                 for (int m = 0; m < 4; m++) bulk_g2s(etile + m * kSeg, a.ef + lo + t.off[m], bytes, &bar);
             }
-            for (int x = tid; x < 4 * kSeg; x += kThreads) dtile[x] = 0ull;
+            if (a.deposit)
+                for (int x = tid; x < 4 * kSeg; x += kThreads) dtile[x] = 0ull;
             bool ok = mbar_wait_bounded(&bar, phase);
             if (!ok) atomicExch(&s_fail, 1);
             phase ^= 1u;
@@ -338,154 +413,87 @@ __global__ void __launch_bounds__(kThreads) k_push(PushArgs a) {
                 return;
             }
             t.etile = etile;
-            t.dtile = dtile;
+            if (a.deposit) t.dtile = dtile;
         }
 
+        unsigned dead_mask[kPPT];
 #pragma unroll
         for (int q = 0; q < kPPT; q++) {
             const int p = base + q * kThreads + tid;
-            int newc = -1;
+            dead_mask[q] = 0;
+            if (bn[q] < 0) continue;
+            int c = __float_as_int(P[q].w);
+            int i = c & 1023, j = (c >> 10) & 1023, k = c >> 20;
             float3 o = make_float3(P[q].x, P[q].y, P[q].z);
             float3 v = make_float3(V[q].x, V[q].y, V[q].z);
             const float w = V[q].w;
-            if (bn[q] >= 0) {
-                int c = __float_as_int(P[q].w), i, j, k;
-                cell_ijk(g, c, i, j, k);
-                bool product = false;
-                float3 po, pv, nv;
-                unsigned long long pid = 0;
-                if (kMcc) {
-                    // ---- electron-impact collision against the background gas ----
-                    const CollDev& cd = a.coll;
-                    unsigned long long id = a.sp.id[p];
-                    uint4 ctr = make_uint4((unsigned)id, (unsigned)(id >> 32), cd.step, 0u);
-                    uint4 r0 = philox4x32_10(ctr, cd.key);
-                    if (u01(r0.x) < cd.p_null) {
-                        st_cand++;
-                        ctr.w = 1u;
-                        uint4 r1 = philox4x32_10(ctr, cd.key);
-                        const float kTwoPi = 6.283185307179586f;
-                        float rr1 = sqrtf(-2.f * logf(u01(r0.y))), rr2 = sqrtf(-2.f * logf(u01(r1.x)));
-                        float s1, c1, s2, c2;
-                        sincosf(kTwoPi * u01(r0.z), &s1, &c1);
-                        sincosf(kTwoPi * u01(r1.y), &s2, &c2);
-                        nv = make_float3(cd.sig_n * rr1 * c1, cd.sig_n * rr1 * s1, cd.sig_n * rr2 * c2);
-                        float3 vr = make_float3(nv.x - v.x, nv.y - v.y, nv.z - v.z);
-                        float v_rel = sqrtf(vr.x * vr.x + vr.y * vr.y + vr.z * vr.z);
-                        float E_rel = cd.E_precalc_rel_eV * v_rel * v_rel;
-                        float sig = sigma_coll(cd, E_rel);
-                        if (u01(r0.w) * cd.sigv_max < sig * v_rel) {
-                            st_coll++;
-                            Draws dr;
-                            dr.ctr = ctr;
-                            dr.ctr.w = 2u;
-                            dr.key = cd.key;
-                            dr.buf = philox4x32_10(dr.ctr, cd.key);
-                            dr.pos = 0;
-                            // MC_MEX_Ionization::collide (Interactions.cpp:885-947)
-                            float E_rel_J = cd.half_mred * v_rel * v_rel;
-                            float P_ion = sigma_ion(cd, E_rel_J / 1.602176565e-19f) / sig;
-                            if (dr.next() <= P_ion) {
-                                float vmag = sqrtf(v.x * v.x + v.y * v.y + v.z * v.z);
-                                float E_inc = vmag * vmag * cd.E_precalc_ele_eV;
-                                if (E_inc >= cd.E_ion_eV) {
-                                    float E_ej = 10.0f * tanf(dr.next() * atanf((E_inc - cd.E_ion_eV) / (2.f * cd.B_inc)));
-                                    float E_sc = E_inc - cd.E_ion_eV - E_ej;
-                                    if (E_sc < 0.f) E_sc = 0.000001f;
-                                    float inv = 1.f / vmag;
-                                    float3 u = make_float3(v.x * inv, v.y * inv, v.z * inv);
-                                    float a1 = dr.next(), a2 = dr.next();
-                                    v = new_vel_electron(cd, E_sc, u, a1, a2);
-                                    float a3 = dr.next(), a4 = dr.next();
-                                    pv = new_vel_electron(cd, E_ej, u, a3, a4);
-                                    ctr.w = 4u;
-                                    uint4 r4 = philox4x32_10(ctr, cd.key);
-                                    po = make_float3(u01(r1.z), u01(r1.w), u01(r4.x));
-                                    pid = id;
-                                    product = true;
-                                    st_ion++;
-                                }
-                            } else {
-                                float inv_sum = 1.f / (cd.m_n + cd.m_e);
-                                float3 cm = make_float3((cd.m_n * nv.x + cd.m_e * v.x) * inv_sum,
-                                                        (cd.m_n * nv.y + cd.m_e * v.y) * inv_sum,
-                                                        (cd.m_n * nv.z + cd.m_e * v.z) * inv_sum);
-                                float cos_ksi = 2.f * dr.next() - 1.f;
-                                float sin_ksi = sqrtf(fmaxf(1.f - cos_ksi * cos_ksi, 0.f));
-                                float se, ce;
-                                sincosf(2.f * 3.141592653f * dr.next(), &se, &ce);
-                                float3 vr2 = make_float3(v_rel * cos_ksi, v_rel * sin_ksi * ce, v_rel * sin_ksi * se);
-                                float f = cd.m_n * inv_sum;
-                                v = make_float3(cm.x - f * vr2.x, cm.y - f * vr2.y, cm.z - f * vr2.z);
-                            }
-                        }
+            Collision col;
+            col.kind = 0;
+            unsigned long long id = 0;
+            if (kMcc) {
+                const CollDev& cd = a.coll;
+                id = a.sp.id[p];
+                uint4 r0 = philox4x32_10(make_uint4((unsigned)id, (unsigned)(id >> 32), cd.step, 0u), cd.key);
+                if (u01(r0.x) < cd.p_null) {
+                    st_cand++;
+                    col = collide_candidate(cd, id, v, r0);
+                    if (col.kind) {
+                        st_coll++;
+                        v = col.v;
                     }
+                    if (col.kind == 2) st_ion++;
                 }
-                // ---- leapfrog push (Species.cpp:369-373) ----
-                float3 E = gather_e(a, t, bn[q], o);
-                v.x += a.qm_dt * E.x;
-                v.y += a.qm_dt * E.y;
-                v.z += a.qm_dt * E.z;
-                newc = move_particle(a, i, j, k, o, v);
-                if (kMcc && product) {
-                    // the ejected electron and the ion: created at a uniform point of the
-                    // parent's cell without velocity rewind; the electron is pushed now
-                    float4 ion_p = make_float4(po.x, po.y, po.z, __int_as_float(c));
-                    float4 ion_v = make_float4(nv.x, nv.y, nv.z, w);
-                    if (!append_particle(a.coll.ion, ion_n, ion_p, ion_v, child_id(pid, a.coll.step, 2), a.err))
+            }
+            // leapfrog push (Species.cpp:369-373)
+            float3 E = gather_e(a, t, bn[q], o);
+            v.x += a.qm_dt * E.x;
+            v.y += a.qm_dt * E.y;
+            v.z += a.qm_dt * E.z;
+            const int newc = move_particle(a, i, j, k, o, v);
+            if (kMcc && col.kind == 2) {
+                // the ejected electron and the ion are created at a uniform point of the parent's
+                // cell without velocity rewind; the electron is pushed and deposited now
+                if (!append_particle(a.coll.ion, ion_n, make_float4(col.po.x, col.po.y, col.po.z, __int_as_float(c)),
+                                     make_float4(col.nv.x, col.nv.y, col.nv.z, w), child_id(id, a.coll.step, 2), a.err))
+                    st_lost++;
+                float3 po = col.po, pv = col.pv;
+                float3 Ep = gather_e(a, t, bn[q], po);
+                pv.x += a.qm_dt * Ep.x;
+                pv.y += a.qm_dt * Ep.y;
+                pv.z += a.qm_dt * Ep.z;
+                int pc = move_particle(a, i, j, k, po, pv);
+                if (pc >= 0) {
+                    if (append_particle(a.sp, n, make_float4(po.x, po.y, po.z, __int_as_float(pc)),
+                                        make_float4(pv.x, pv.y, pv.z, w), child_id(id, a.coll.step, 1), a.err)) {
+                        if (a.deposit) {
+                            Tile tg = t;
+                            tg.dtile = nullptr;  // products go straight to HBM
+                            deposit_fixed(a, tg, ((pc >> 20) * g.nj + ((pc >> 10) & 1023)) * g.ni + (pc & 1023),
+                                          w, po);
+                        }
+                    } else {
                         st_lost++;
-                    float3 Ep = gather_e(a, t, bn[q], po);
-                    pv.x += a.qm_dt * Ep.x;
-                    pv.y += a.qm_dt * Ep.y;
-                    pv.z += a.qm_dt * Ep.z;
-                    int pc = move_particle(a, i, j, k, po, pv);
-                    if (pc >= 0) {
-                        if (append_particle(a.sp, n, make_float4(po.x, po.y, po.z, __int_as_float(pc)),
-                                            make_float4(pv.x, pv.y, pv.z, w), child_id(pid, a.coll.step, 1), a.err)) {
-                            if (a.deposit) {
-                                unsigned long long qq[8];
-                                corner_fixed(w, po, a.dep_scale, qq);
-                                int pi_, pj, pk;
-                                cell_ijk(g, pc, pi_, pj, pk);
-                                int pb = cell_base_node(g, pi_, pj, pk);
-#pragma unroll
-                                for (int m = 0; m < 4; m++)
-#pragma unroll
-                                    for (int di = 0; di < 2; di++)
-                                        if (qq[2 * m + di]) atomicAdd(&a.sp.acc[pb + t.off[m] + di], qq[2 * m + di]);
-                            }
-                        } else {
-                            st_lost++;
-                        }
                     }
                 }
-                a.sp.pos[p] = make_float4(o.x, o.y, o.z, __int_as_float(newc));
-                a.sp.vel[p] = make_float4(v.x, v.y, v.z, w);
             }
-            {
-                // warp-aggregated record of the particles that left the domain
-                const bool died = bn[q] >= 0 && newc < 0;
-                unsigned dm = __ballot_sync(0xffffffffu, died);
-                if (dm) {
-                    int b0 = 0;
-                    if (lane == __ffs(dm) - 1) b0 = atomicAdd(&a.sp.counts[2], __popc(dm));
-                    b0 = __shfl_sync(0xffffffffu, b0, __ffs(dm) - 1);
-                    if (died) a.sp.dead[b0 + __popc(dm & ((1u << lane) - 1u))] = p;
-                }
+            a.sp.pos[p] = make_float4(o.x, o.y, o.z, __int_as_float(newc));
+            a.sp.vel[p] = make_float4(v.x, v.y, v.z, w);
+            if (newc >= 0) {
+                if (a.deposit)
+                    deposit_fixed(a, t, ((newc >> 20) * g.nj + ((newc >> 10) & 1023)) * g.ni + (newc & 1023), w, o);
+            } else {
+                dead_mask[q] = 1;
             }
-            if (a.deposit) {
-                __syncwarp();
-                unsigned gmask = __match_any_sync(0xffffffffu, newc);
-                unsigned long long qv[8];
-                if (newc >= 0) corner_fixed(w, o, a.dep_scale, qv);
-                else
-                    for (int c = 0; c < 8; c++) qv[c] = 0ull;
-                group_reduce(gmask, qv);
-                if (newc >= 0 && lane == __ffs(gmask) - 1) {
-                    int i, j, k;
-                    cell_ijk(g, newc, i, j, k);
-                    commit_corners(a, t, cell_base_node(g, i, j, k), qv);
-                }
+        }
+        // warp-aggregated record of the particles that left the domain
+#pragma unroll
+        for (int q = 0; q < kPPT; q++) {
+            unsigned dm = __ballot_sync(0xffffffffu, dead_mask[q] != 0);
+            if (dm) {
+                int b0 = 0;
+                if (lane == __ffs(dm) - 1) b0 = atomicAdd(&a.sp.counts[2], __popc(dm));
+                b0 = __shfl_sync(0xffffffffu, b0, __ffs(dm) - 1);
+                if (dead_mask[q]) a.sp.dead[b0 + __popc(dm & ((1u << lane) - 1u))] = base + q * kThreads + tid;
             }
         }
         __syncthreads();
@@ -571,14 +579,14 @@ void launch_compact(SpeciesDev sp, cudaStream_t s, int grid) {
 // counting sort by cell (Species::sortIndexes keeps index lists; here the particles
 // themselves are reordered so that each cell is a contiguous run)
 // ------------------------------------------------------------------------------------
-__global__ void k_sort_hist(SpeciesDev sp, int* cnt) {
+__global__ void k_sort_hist(GridDev g, SpeciesDev sp, int* cnt) {
     int n = sp.counts[0];
     int stride = gridDim.x * blockDim.x;
     int lim = ((n + 31) / 32) * 32;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < lim; p += stride) {
         int c = p < n ? __float_as_int(sp.pos[p].w) : -1;
         unsigned m = __match_any_sync(0xffffffffu, c);
-        if (c >= 0 && (threadIdx.x & 31) == __ffs(m) - 1) atomicAdd(&cnt[c], __popc(m));
+        if (c >= 0 && (threadIdx.x & 31) == __ffs(m) - 1) atomicAdd(&cnt[cell_linear(g, c)], __popc(m));
     }
 }
 // exclusive scan in three passes over tiles of 2048 counts
@@ -641,8 +649,8 @@ __global__ void k_scan_add(int* out, const int* aux, int n) {
     for (int x = threadIdx.x; x < kScanTile; x += 256)
         if (base + x < n) out[base + x] += add;
 }
-__global__ void k_sort_scatter(SpeciesDev sp, const int* start, int* cursor, float4* pos2, float4* vel2,
-                               unsigned long long* id2) {
+__global__ void k_sort_scatter(GridDev g, SpeciesDev sp, const int* start, int* cursor, float4* pos2,
+                               float4* vel2, unsigned long long* id2) {
     int n = sp.counts[0];
     int stride = gridDim.x * blockDim.x;
     int lim = ((n + 31) / 32) * 32;
@@ -652,11 +660,12 @@ __global__ void k_sort_scatter(SpeciesDev sp, const int* start, int* cursor, flo
         int c = __float_as_int(ps.w);
         unsigned m = __match_any_sync(0xffffffffu, c);
         int leader = __ffs(m) - 1;
+        int lc = c >= 0 ? cell_linear(g, c) : 0;
         int b = 0;
-        if (c >= 0 && lane == leader) b = atomicAdd(&cursor[c], __popc(m));
+        if (c >= 0 && lane == leader) b = atomicAdd(&cursor[lc], __popc(m));
         b = __shfl_sync(m, b, leader);
         if (c >= 0) {
-            int dst = start[c] + b + __popc(m & ((1u << lane) - 1u));
+            int dst = start[lc] + b + __popc(m & ((1u << lane) - 1u));
             pos2[dst] = ps;
             vel2[dst] = sp.vel[p];
             id2[dst] = sp.id[p];
@@ -667,13 +676,13 @@ void launch_sort(const GridDev& g, SpeciesDev sp, float4* pos_alt, float4* vel_a
                  int* cell_count, int* cell_start, int* scan_aux, cudaStream_t s, int grid) {
     int nc = g.nc;
     cudaMemsetAsync(cell_count, 0, sizeof(int) * nc, s);
-    k_sort_hist<<<grid, 256, 0, s>>>(sp, cell_count);
+    k_sort_hist<<<grid, 256, 0, s>>>(g, sp, cell_count);
     int ntiles = (nc + kScanTile - 1) / kScanTile;
     k_scan_tiles<<<ntiles, 256, 0, s>>>(cell_count, cell_start, scan_aux, nc);
     k_scan_aux<<<1, 1024, 0, s>>>(scan_aux, ntiles);
     k_scan_add<<<ntiles, 256, 0, s>>>(cell_start, scan_aux, nc);
     cudaMemsetAsync(cell_count, 0, sizeof(int) * nc, s);
-    k_sort_scatter<<<grid, 256, 0, s>>>(sp, cell_start, cell_count, pos_alt, vel_alt, id_alt);
+    k_sort_scatter<<<grid, 256, 0, s>>>(g, sp, cell_start, cell_count, pos_alt, vel_alt, id_alt);
 }
 
 // ------------------------------------------------------------------------------------
@@ -707,7 +716,7 @@ __global__ void k_from_abs(GridDev g, SpeciesDev sp, const double* pos, const do
         }
         int cell = -1;
         if (ok) {
-            cell = (ijk[2] * g.cj + ijk[1]) * g.ci + ijk[0];
+            cell = pack_cell(ijk[0], ijk[1], ijk[2]);
             if (g.n_boxes) {
                 float X = ((float)ijk[0] + o[0]) * g.dx[0], Y = ((float)ijk[1] + o[1]) * g.dx[1],
                       Z = ((float)ijk[2] + o[2]) * g.dx[2];
@@ -819,7 +828,7 @@ __global__ void k_load_uniform(GridDev g, SpeciesDev sp, LoadArgs la) {
             float zn = rb * s2;
             wgt = expf(logf(la.w_mean) - 0.5f * la.w_sigma * la.w_sigma + la.w_sigma * zn);
         }
-        int cell = (ijk[2] * g.cj + ijk[1]) * g.ci + ijk[0];
+        int cell = pack_cell(ijk[0], ijk[1], ijk[2]);
         sp.pos[dst] = make_float4(o[0], o[1], o[2], __int_as_float(cell));
         sp.vel[dst] = make_float4(v.x, v.y, v.z, wgt);
         sp.id[dst] = id;
@@ -1023,8 +1032,9 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge(MergeArgs a) {
             atomicAdd(&a.stats[0], 1ull);
             atomicAdd(&a.stats[1], (unsigned long long)(e - q));
             int i, j, k;
-            cell_ijk(a.g, c, i, j, k);
+            linear_ijk(a.g, c, i, j, k);
             int bnode = cell_base_node(a.g, i, j, k);
+            const int cpk = pack_cell(i, j, k);
             Tile t;
             t.etile = nullptr;
             t.dtile = nullptr;
@@ -1051,7 +1061,7 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge(MergeArgs a) {
                 v.y -= a.qm_half_dt * Ev.y;
                 v.z -= a.qm_half_dt * Ev.z;
                 unsigned long long pid = child_id(a.sp.id[s0 + l], a.step, 3);
-                append_particle(a.sp, n, make_float4(o.x, o.y, o.z, __int_as_float(c)),
+                append_particle(a.sp, n, make_float4(o.x, o.y, o.z, __int_as_float(cpk)),
                                 make_float4(v.x, v.y, v.z, (float)(W * 0.5)), pid, a.err);
             }
         }

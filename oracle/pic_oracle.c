@@ -272,6 +272,9 @@ void or_compute_ef_ref(const or_grid* g, const double* phi, double* ef) {
                         long im = base + (long)((cc == 0 ? nn[d] - 2 : cc - 1) - cc) * st[d];
                         long ip = base + (long)((cc + 1 == nn[d] - 1 ? 0 : cc + 1) - cc) * st[d];
                         e = (phi[im] - phi[ip]) * inv2[d];
+                    } else if (nn[d] == 2) {
+                        /* one cell: first-order difference (the reference would read past the end) */
+                        e = c == 0 ? 2.0 * (phi[n] - phi[n + st[d]]) * inv2[d] : 2.0 * (phi[n - st[d]] - phi[n]) * inv2[d];
                     } else if (c == 0) {
                         e = (3 * phi[n] - 4 * phi[n + st[d]] + phi[n + 2 * st[d]]) * inv2[d];
                     } else if (c == nn[d] - 1) {
