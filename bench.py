@@ -360,6 +360,9 @@ def run_gpu(args, wl, rank, ws, local):
     W.close()
     # e2e: same loop through the C ABI from pinned host buffers (upload + per-step diagnostics)
     e2e = run_e2e(pic, wl, args, rank)
+    poisson = None
+    if rank == 0 and args.poisson > 0:
+        poisson = poisson_bench(pic, args.poisson)
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_reference(wl, inner / max(1, args.steps), sample=args.cpu_sample, steps=1)
@@ -384,10 +387,49 @@ def run_gpu(args, wl, rank, ws, local):
         "kernels": kernels,
         "cpu_baseline": cpu,
         "e2e": e2e,
+        "poisson_time_to_1e-6": poisson,
         "clocks": clocks,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def blob_rho(nn, seed):
+    """Seeded sum of 8-64 Gaussian blobs, amplitude +-1e-3 C/m^3, widths 2-20 cells (node field)."""
+    rng = np.random.default_rng(seed)
+    rho = np.zeros(nn[::-1])  # [k][j][i]
+    for _ in range(int(rng.integers(8, 65))):
+        c = rng.uniform(0, 1, 3) * (np.array(nn) - 1)
+        wdt = rng.uniform(2, 20)
+        amp = rng.uniform(-1e-3, 1e-3)
+        lo = np.maximum(0, np.floor(c - 3 * wdt)).astype(int)
+        hi = np.minimum(np.array(nn), np.ceil(c + 3 * wdt + 1)).astype(int)
+        ax = [np.arange(lo[d], hi[d]) for d in range(3)]
+        gx, gy, gz = [np.exp(-0.5 * ((a - c[d]) / wdt) ** 2) for d, a in enumerate(ax)]
+        rho[lo[2]:hi[2], lo[1]:hi[1], lo[0]:hi[0]] += amp * gz[:, None, None] * gy[None, :, None] * gx[None, None, :]
+    return rho.ravel()
+
+
+def poisson_bench(pic, n, seed=5):
+    """Time to a 1e-6 FP64 relative residual from the Dirichlet-only start, n^3 nodes over a
+    0.04 m cube, z faces at 0 V / 1000 V, periodic x, y; blob charge density."""
+    W = pic.World(n, n, n, (0.0, 0.0, 0.0), (0.04, 0.04, 0.04))
+    W.set_boundaries((1, 1, 0), (1,) * 6, (0, 0, 0, 0, 0.0, 1000.0))
+    W.rho = blob_rho((n, n, n), seed)
+    phi0 = W.phi
+    omega = 2.0 / (1.0 + np.sin(np.pi / (n - 1)))  # optimal SOR weight of the model problem
+    out = {"grid": [n, n, n], "tol": 1e-6}
+    for name, method, w in (("rbsor", pic.SOLVER_RBSOR, omega), ("pcg", pic.SOLVER_PCG, 1.4)):
+        W.phi = phi0
+        S = pic.PotentialSolver(W, 200000, 1e-6, method, omega=w)
+        W.synchronize()
+        t0 = time.perf_counter()
+        ok = S.solve()
+        W.synchronize()
+        out[name] = {"seconds": time.perf_counter() - t0, "iterations": S.iters, "rel": S.rel, "converged": ok}
+    out["rbsor"]["omega"] = omega
+    W.close()
+    return out
 
 
 def run_e2e(pic, wl, args, rank):
@@ -462,6 +504,7 @@ def main():
     ap.add_argument("--workload", default="large", choices=sorted(WORKLOADS))
     ap.add_argument("--cpu-sample", type=int, default=1_000_000)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--poisson", type=int, default=256, help="n of the n^3 Poisson time-to-1e-6 case (0: skip)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -193,6 +193,7 @@ int check_device_error(pic_world* w) {
 
 bool valid_sp(pic_world* w, int s) { return w && s >= 0 && s < (int)w->sp.size(); }
 
+
 // node kinds and masks; Dirichlet values written into phi_host
 void build_kinds(pic_world* w, std::vector<uint16_t>& kind, std::vector<double>& phi_host) {
     const GridDev& g = w->g;
@@ -905,7 +906,7 @@ int solve_impl(pic_world* w, int* iters_out, double* rel_out) {
         if (w->method == PIC_SOLVER_RBSOR) {
             int sweeps = std::min(25, w->max_it - iters);
             {
-                Scope sc(w, "poisson", 1 + 2 * sweeps);
+                Scope sc(w, "poisson", 3 * sweeps);
                 CU(cudaMemsetAsync(w->e, 0, sizeof(float) * w->g.nv, w->stream));
                 launch_rbsor_sweeps(w->g, sw, (float)w->omega, sweeps, w->stream, grid);
             }
@@ -940,6 +941,7 @@ int solve_impl(pic_world* w, int* iters_out, double* rel_out) {
         rc = residual_norms(w, sw, 1, r2, b2);
         if (rc) return rc;
         rel = std::sqrt(r2) / bn;
+        if (!(rel == rel)) break;  // NaN: diverged
     }
     {
         Scope sc(w, "poisson", 2);
@@ -950,7 +952,8 @@ int solve_impl(pic_world* w, int* iters_out, double* rel_out) {
     w->n_solves++;
     w->n_inner += iters;
     CU(cudaGetLastError());
-    if (rel > w->tol) return fail(PIC_ERR_NOT_CONVERGED, "Poisson solve stopped at %d iterations, rel %.3e", iters, rel);
+    if (!(rel <= w->tol))
+        return fail(PIC_ERR_NOT_CONVERGED, "Poisson solve stopped at %d iterations, rel %.3e", iters, rel);
     return PIC_OK;
 }
 }  // namespace

@@ -208,7 +208,6 @@ __global__ void k_residual(GridDev g, const double* __restrict__ phi_in, double*
                            const float* __restrict__ e, const float* __restrict__ rho,
                            const uint16_t* __restrict__ kind, float* __restrict__ r, double* part, int apply_e) {
     double acc[2] = {0.0, 0.0};
-    const float inv_eps0 = (float)(1.0 / kEps0);
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
         uint16_t kd = kind[n];
         if ((kd & 3) != kFree) {
@@ -223,28 +222,29 @@ __global__ void k_residual(GridDev g, const double* __restrict__ phi_in, double*
         const double pp = phi_in[n];
         const float ep = apply_e ? e[n] : 0.f;
         // L(phi + e)_p = sum over axes of c (2 v_p - v_minus - v_plus), a mirror neighbour taking
-        // the value of p.  The second differences of the potential are formed in FP64 (the two
-        // neighbour terms cancel to high relative precision), the rest in FP32.
-        float lphi = 0.f, bfix = 0.f;
+        // the value of p.  Second differences of the potential and the residual are FP64; the
+        // correction e enters through FP32 second differences.
+        double lphi = 0.0;
+        float bfix = 0.f;
 #pragma unroll
         for (int ax = 0; ax < 3; ax++) {
             const int dm = 2 * ax, dp = 2 * ax + 1;
             const bool mm = kd & (1u << (2 + dm)), mp = kd & (1u << (2 + dp));
             const double pm = mm ? pp : phi_in[s.q[dm]];
             const double pq = mp ? pp : phi_in[s.q[dp]];
-            float d2 = (float)((pp - pm) + (pp - pq));
-            if (apply_e) d2 += (2.f * ep - (mm ? ep : e[s.q[dm]])) - (mp ? ep : e[s.q[dp]]);
-            lphi += s.c[dm] * d2;
+            double d2 = (pp - pm) + (pp - pq);
+            if (apply_e) d2 += (double)((2.f * ep - (mm ? ep : e[s.q[dm]])) - (mp ? ep : e[s.q[dp]]));
+            lphi += (double)s.c[dm] * d2;
             if (kd & (1u << (8 + dm))) bfix += s.c[dm] * (float)pm;
             if (kd & (1u << (8 + dp))) bfix += s.c[dp] * (float)pq;
         }
-        const float src = rho[n] * inv_eps0;
-        const float res = src - lphi;
+        const double src = (double)rho[n] * (1.0 / kEps0);
+        const double res = src - lphi;
         if (apply_e) phi_out[n] = pp + (double)ep;
-        r[n] = res;
-        const float b = src + bfix;
-        acc[0] += (double)res * (double)res;
-        acc[1] += (double)b * (double)b;
+        r[n] = (float)res;
+        const double b = src + (double)bfix;
+        acc[0] += res * res;
+        acc[1] += b * b;
     }
     block_partials<2>(acc, part, kParts);
 }
@@ -272,40 +272,77 @@ void launch_reduce_partials(const double* part, int nslots, int nblocks, double*
 // ------------------------------------------------------------------------------------
 // FP32 red-black SOR on the correction equation L e = r (e = 0 on non-FREE nodes)
 // ------------------------------------------------------------------------------------
+// A periodic axis with an odd number of distinct nodes (n-1 odd) closes an odd cycle, so the
+// last distinct index n-2 ("seam") has a same-colour neighbour across the wrap.  Seam nodes are
+// left out of the red and black passes and relaxed (omega = 1) in a third pass.
+__device__ __forceinline__ bool on_seam(const GridDev& g, int i, int j, int k) {
+    return (g.periodic[0] && ((g.ni - 1) & 1) && i == g.ni - 2) ||
+           (g.periodic[1] && ((g.nj - 1) & 1) && j == g.nj - 2) ||
+           (g.periodic[2] && ((g.nk - 1) & 1) && k == g.nk - 2);
+}
+__device__ __forceinline__ void sor_update(const GridDev& g, float* __restrict__ e, const float* __restrict__ r,
+                                           const uint16_t* __restrict__ kind, float omega, int i, int j, int k) {
+    const int n = (k * g.nj + j) * g.ni + i;
+    const uint16_t kd = kind[n];
+    if ((kd & 3) != kFree) return;
+    Stencil s;
+    stencil(g, i, j, k, s);
+    float diag = 0.f, off = 0.f;
+#pragma unroll
+    for (int d = 0; d < 6; d++) {
+        if (kd & (1u << (2 + d))) continue;
+        diag += s.c[d];
+        off += s.c[d] * e[s.q[d]];  // zero on FIXED neighbours
+    }
+    const float en = e[n];
+    e[n] = en + omega * ((r[n] + off) / diag - en);
+}
 __global__ void k_rbsor(GridDev g, float* __restrict__ e, const float* __restrict__ r,
                         const uint16_t* __restrict__ kind, float omega, int color) {
-    // thread t -> (m, j, k) with i = i0 + 2m of the requested colour
-    int half = (g.ni + 1) / 2;
-    int total = half * g.nj * g.nk;
-    float cx = g.inv_dx[0] * g.inv_dx[0], cy = g.inv_dx[1] * g.inv_dx[1], cz = g.inv_dx[2] * g.inv_dx[2];
+    // thread t -> (m, j, k) with i = 2m + parity of the requested colour
+    const int half = (g.ni + 1) / 2;
+    const int total = half * g.nj * g.nk;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
         int m = t % half, jk = t / half;
         int j = jk % g.nj, k = jk / g.nj;
         int i = 2 * m + ((color + j + k) & 1);
-        if (i >= g.ni) continue;
-        int n = (k * g.nj + j) * g.ni + i;
-        uint16_t kd = kind[n];
-        if ((kd & 3) != kFree) continue;
-        Stencil s;
-        stencil(g, i, j, k, s);
-        float diag = 2.f * (cx + cy + cz), off = 0.f;
-#pragma unroll
-        for (int d = 0; d < 6; d++) {
-            if (kd & (1u << (2 + d))) {
-                diag -= s.c[d];
-                continue;
-            }
-            off += s.c[d] * e[s.q[d]];
+        if (i >= g.ni || on_seam(g, i, j, k)) continue;
+        sor_update(g, e, r, kind, omega, i, j, k);
+    }
+}
+__global__ void k_rbsor_seam(GridDev g, float* __restrict__ e, const float* __restrict__ r,
+                             const uint16_t* __restrict__ kind) {
+    const int nx = (g.periodic[0] && ((g.ni - 1) & 1)) ? g.nj * g.nk : 0;
+    const int ny = (g.periodic[1] && ((g.nj - 1) & 1)) ? g.ni * g.nk : 0;
+    const int nz = (g.periodic[2] && ((g.nk - 1) & 1)) ? g.ni * g.nj : 0;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nx + ny + nz; t += gridDim.x * blockDim.x) {
+        int i, j, k;
+        if (t < nx) {
+            i = g.ni - 2;
+            j = t % g.nj;
+            k = t / g.nj;
+        } else if (t < nx + ny) {
+            int u = t - nx;
+            j = g.nj - 2;
+            i = u % g.ni;
+            k = u / g.ni;
+        } else {
+            int u = t - nx - ny;
+            k = g.nk - 2;
+            i = u % g.ni;
+            j = u / g.ni;
         }
-        float en = e[n];
-        e[n] = en + omega * ((r[n] + off) / diag - en);
+        sor_update(g, e, r, kind, 1.0f, i, j, k);
     }
 }
 void launch_rbsor_sweeps(const GridDev& g, SolveWork& w, float omega, int sweeps, cudaStream_t s, int grid) {
     const uint16_t* kd = reinterpret_cast<const uint16_t*>(w.kind);
+    const bool seam = (g.periodic[0] && ((g.ni - 1) & 1)) || (g.periodic[1] && ((g.nj - 1) & 1)) ||
+                      (g.periodic[2] && ((g.nk - 1) & 1));
     for (int it = 0; it < sweeps; it++) {
         k_rbsor<<<grid, 256, 0, s>>>(g, w.e, w.r, kd, omega, 0);
         k_rbsor<<<grid, 256, 0, s>>>(g, w.e, w.r, kd, omega, 1);
+        if (seam) k_rbsor_seam<<<256, 256, 0, s>>>(g, w.e, w.r, kd);
     }
 }
 

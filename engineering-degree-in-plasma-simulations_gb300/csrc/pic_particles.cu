@@ -19,8 +19,9 @@ constexpr int kPPT = 4;                     // particles per thread per chunk
 constexpr int kChunk = kThreads * kPPT;     // particles per chunk
 constexpr int kSeg = 512;                   // nodes per staged row segment
 constexpr int kMargin = 2;                  // deposit window starts this many nodes below the gather window
-// E rows (float4) + 64-bit fixed-point deposit tile, four rows of kSeg nodes each
-constexpr size_t kPushSmem = 4 * kSeg * sizeof(float4) + 4 * kSeg * sizeof(unsigned long long);
+// E rows (float4) + fixed-point deposit tile: three 21-bit limb planes of 32-bit counters,
+// four rows of kSeg nodes each
+constexpr size_t kPushSmem = 4 * kSeg * sizeof(float4) + 3 * 4 * kSeg * sizeof(unsigned);
 constexpr long long kWaitLimit = 1ll << 24;  // mbarrier polls before giving up
 
 // ------------------------------------------------------------------------------------
@@ -120,8 +121,8 @@ __device__ float3 new_vel_electron(const CollDev& c, float E, float3 u, float r_
 // push helpers
 // ------------------------------------------------------------------------------------
 struct Tile {
-    const float4* etile;       // staged E rows (row m at etile + m*kSeg), or nullptr
-    unsigned long long* dtile; // deposit tile (row m at dtile + m*kSeg), or nullptr
+    const float4* etile;  // staged E rows (row m at etile + m*kSeg), or nullptr
+    unsigned* dtile;      // deposit tile: limb l of row m at dtile + (l*4 + m)*kSeg, or nullptr
     int lo;                    // first node of the gather window
     int off[4];                // node offsets of the four rows: 0, ni, ni*nj, ni*nj+ni
 };
@@ -193,38 +194,43 @@ __device__ __forceinline__ int move_particle(const PushArgs& a, int i, int j, in
     return pack_cell(i, j, k);
 }
 
-// the eight corner contributions of weight w at offsets o as 64-bit fixed point, added into the
-// shared tile when the cell's corners lie in the deposit window, else straight into HBM.
-// Integer sums do not depend on the order of the additions: rho is bit-reproducible.
-__device__ __forceinline__ void deposit_fixed(const PushArgs& a, const Tile& t, int b, float w, float3 o) {
+// the eight corner contributions of weight w at offsets o as 64-bit fixed point
+struct Corners {
+    unsigned long long q[8];  // order 000 100 010 110 001 101 011 111 (x fastest)
+};
+__device__ __forceinline__ void corner_values(float w, float3 o, float scale, Corners& c, bool add) {
     float wx1 = o.x, wx0 = 1.f - o.x, wy1 = o.y, wy0 = 1.f - o.y, wz1 = o.z, wz0 = 1.f - o.z;
-    float s = w * a.dep_scale;
+    float s = w * scale;
     float s00 = s * wx0 * wy0, s10 = s * wx1 * wy0, s01 = s * wx0 * wy1, s11 = s * wx1 * wy1;
-    unsigned long long q000 = __float2ull_rn(s00 * wz0), q100 = __float2ull_rn(s10 * wz0);
-    unsigned long long q010 = __float2ull_rn(s01 * wz0), q110 = __float2ull_rn(s11 * wz0);
-    unsigned long long q001 = __float2ull_rn(s00 * wz1), q101 = __float2ull_rn(s10 * wz1);
-    unsigned long long q011 = __float2ull_rn(s01 * wz1), q111 = __float2ull_rn(s11 * wz1);
+    unsigned long long v[8] = {__float2ull_rn(s00 * wz0), __float2ull_rn(s10 * wz0), __float2ull_rn(s01 * wz0),
+                               __float2ull_rn(s11 * wz0), __float2ull_rn(s00 * wz1), __float2ull_rn(s10 * wz1),
+                               __float2ull_rn(s01 * wz1), __float2ull_rn(s11 * wz1)};
+#pragma unroll
+    for (int c8 = 0; c8 < 8; c8++) c.q[c8] = add ? c.q[c8] + v[c8] : v[c8];
+}
+
+// commits the corner sums of one cell (base node b): into the shared tile as 21-bit limbs with
+// native 32-bit shared atomics when the cell lies in the deposit window, else one 64-bit atomic
+// per corner in HBM.  Integer sums do not depend on the order of the additions, so rho is
+// bit-reproducible.  A tile slot receives at most one chunk's particles (1024), so a limb plane
+// cannot overflow 32 bits.
+__device__ __forceinline__ void commit_corners(const PushArgs& a, const Tile& t, int b, const Corners& c) {
     int loc = b - (t.lo - kMargin);
     if (t.dtile && loc >= 0 && loc < kSeg - 1) {
-        unsigned long long* d = t.dtile + loc;
-        atomicAdd(d, q000);
-        atomicAdd(d + 1, q100);
-        atomicAdd(d + kSeg, q010);
-        atomicAdd(d + kSeg + 1, q110);
-        atomicAdd(d + 2 * kSeg, q001);
-        atomicAdd(d + 2 * kSeg + 1, q101);
-        atomicAdd(d + 3 * kSeg, q011);
-        atomicAdd(d + 3 * kSeg + 1, q111);
+#pragma unroll
+        for (int c8 = 0; c8 < 8; c8++) {
+            unsigned long long v = c.q[c8];
+            if (!v) continue;
+            int x = ((c8 >> 1) * kSeg) + loc + (c8 & 1);
+            atomicAdd(&t.dtile[x], (unsigned)(v & 0x1FFFFFull));
+            unsigned l1 = (unsigned)((v >> 21) & 0x1FFFFFull), l2 = (unsigned)(v >> 42);
+            if (l1) atomicAdd(&t.dtile[4 * kSeg + x], l1);
+            if (l2) atomicAdd(&t.dtile[8 * kSeg + x], l2);
+        }
     } else {
-        unsigned long long* d = a.sp.acc + b;
-        atomicAdd(d, q000);
-        atomicAdd(d + 1, q100);
-        atomicAdd(d + t.off[1], q010);
-        atomicAdd(d + t.off[1] + 1, q110);
-        atomicAdd(d + t.off[2], q001);
-        atomicAdd(d + t.off[2] + 1, q101);
-        atomicAdd(d + t.off[3], q011);
-        atomicAdd(d + t.off[3] + 1, q111);
+#pragma unroll
+        for (int c8 = 0; c8 < 8; c8++)
+            if (c.q[c8]) atomicAdd(&a.sp.acc[b + t.off[c8 >> 1] + (c8 & 1)], c.q[c8]);
     }
 }
 
@@ -323,7 +329,7 @@ template <bool kMcc>
 __global__ void __launch_bounds__(kThreads, kMcc ? 2 : 3) k_push(PushArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     float4* etile = reinterpret_cast<float4*>(smem);
-    unsigned long long* dtile = reinterpret_cast<unsigned long long*>(smem + 4 * kSeg * sizeof(float4));
+    unsigned* dtile = reinterpret_cast<unsigned*>(smem + 4 * kSeg * sizeof(float4));
     __shared__ __align__(8) unsigned long long bar;
     __shared__ int s_min[kThreads / 32], s_max[kThreads / 32];
     __shared__ int s_lo, s_hi, s_fail;
@@ -353,9 +359,11 @@ __global__ void __launch_bounds__(kThreads, kMcc ? 2 : 3) k_push(PushArgs a) {
         float4 P[kPPT], V[kPPT];
         int bn[kPPT];
         int lmin = INT_MAX, lmax = -1;
+        // each thread takes kPPT consecutive particles: in a cell-sorted chunk they mostly share a
+        // cell, so their deposits are summed in registers before touching shared memory
 #pragma unroll
         for (int q = 0; q < kPPT; q++) {
-            int p = base + q * kThreads + tid;
+            int p = base + tid * kPPT + q;
             bn[q] = -1;
             if (p < n) {
                 P[q] = a.sp.pos[p];
@@ -400,7 +408,7 @@ __global__ void __launch_bounds__(kThreads, kMcc ? 2 : 3) k_push(PushArgs a) {
                 for (int m = 0; m < 4; m++) bulk_g2s(etile + m * kSeg, a.ef + lo + t.off[m], bytes, &bar);
             }
             if (a.deposit)
-                for (int x = tid; x < 4 * kSeg; x += kThreads) dtile[x] = 0ull;
+                for (int x = tid; x < 12 * kSeg; x += kThreads) dtile[x] = 0u;
             bool ok = mbar_wait_bounded(&bar, phase);
             if (!ok) atomicExch(&s_fail, 1);
             phase ^= 1u;
@@ -417,9 +425,11 @@ __global__ void __launch_bounds__(kThreads, kMcc ? 2 : 3) k_push(PushArgs a) {
         }
 
         unsigned dead_mask[kPPT];
+        Corners run;        // deposit sums of the current cell run
+        int run_cell = -1;  // packed cell of the run, -1: none
 #pragma unroll
         for (int q = 0; q < kPPT; q++) {
-            const int p = base + q * kThreads + tid;
+            const int p = base + tid * kPPT + q;
             dead_mask[q] = 0;
             if (bn[q] < 0) continue;
             int c = __float_as_int(P[q].w);
@@ -468,8 +478,9 @@ __global__ void __launch_bounds__(kThreads, kMcc ? 2 : 3) k_push(PushArgs a) {
                         if (a.deposit) {
                             Tile tg = t;
                             tg.dtile = nullptr;  // products go straight to HBM
-                            deposit_fixed(a, tg, ((pc >> 20) * g.nj + ((pc >> 10) & 1023)) * g.ni + (pc & 1023),
-                                          w, po);
+                            Corners pcn;
+                            corner_values(w, po, a.dep_scale, pcn, false);
+                            commit_corners(a, tg, ((pc >> 20) * g.nj + ((pc >> 10) & 1023)) * g.ni + (pc & 1023), pcn);
                         }
                     } else {
                         st_lost++;
@@ -479,12 +490,20 @@ __global__ void __launch_bounds__(kThreads, kMcc ? 2 : 3) k_push(PushArgs a) {
             a.sp.pos[p] = make_float4(o.x, o.y, o.z, __int_as_float(newc));
             a.sp.vel[p] = make_float4(v.x, v.y, v.z, w);
             if (newc >= 0) {
-                if (a.deposit)
-                    deposit_fixed(a, t, ((newc >> 20) * g.nj + ((newc >> 10) & 1023)) * g.ni + (newc & 1023), w, o);
+                if (a.deposit) {
+                    if (newc != run_cell && run_cell >= 0)
+                        commit_corners(a, t, ((run_cell >> 20) * g.nj + ((run_cell >> 10) & 1023)) * g.ni +
+                                                 (run_cell & 1023), run);
+                    corner_values(w, o, a.dep_scale, run, newc == run_cell);
+                    run_cell = newc;
+                }
             } else {
                 dead_mask[q] = 1;
             }
         }
+        if (run_cell >= 0)
+            commit_corners(a, t, ((run_cell >> 20) * g.nj + ((run_cell >> 10) & 1023)) * g.ni + (run_cell & 1023),
+                           run);
         // warp-aggregated record of the particles that left the domain
 #pragma unroll
         for (int q = 0; q < kPPT; q++) {
@@ -493,14 +512,15 @@ __global__ void __launch_bounds__(kThreads, kMcc ? 2 : 3) k_push(PushArgs a) {
                 int b0 = 0;
                 if (lane == __ffs(dm) - 1) b0 = atomicAdd(&a.sp.counts[2], __popc(dm));
                 b0 = __shfl_sync(0xffffffffu, b0, __ffs(dm) - 1);
-                if (dead_mask[q]) a.sp.dead[b0 + __popc(dm & ((1u << lane) - 1u))] = base + q * kThreads + tid;
+                if (dead_mask[q]) a.sp.dead[b0 + __popc(dm & ((1u << lane) - 1u))] = base + tid * kPPT + q;
             }
         }
         __syncthreads();
         if (use_tile && a.deposit) {
             const int wlo = lo - kMargin;
             for (int x = tid; x < 4 * kSeg; x += kThreads) {
-                unsigned long long v = dtile[x];
+                unsigned long long v = (unsigned long long)dtile[x] + ((unsigned long long)dtile[4 * kSeg + x] << 21) +
+                                       ((unsigned long long)dtile[8 * kSeg + x] << 42);
                 if (v) atomicAdd(&a.sp.acc[wlo + t.off[x / kSeg] + (x % kSeg)], v);
             }
         }
