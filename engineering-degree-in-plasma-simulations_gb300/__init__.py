@@ -95,6 +95,7 @@ def library():
         "pic_timing_reset": [vp],
         "pic_launch_count": [vp, vp],
         "pic_world_stream": [vp, pvp],
+        "pic_number_density_noalloc": [i, i, i, vp, vp, vp, vp, vp, l, d, vp, vp],
     }
     for name, args in sig.items():
         f = getattr(L, name)

@@ -193,6 +193,14 @@ int check_device_error(pic_world* w) {
 
 bool valid_sp(pic_world* w, int s) { return w && s >= 0 && s < (int)w->sp.size(); }
 
+}  // namespace
+
+namespace pic {
+// records the message returned by pic_last_error for entry points in other translation units
+int set_last_error(int code, const char* msg) { return fail(code, "%s", msg); }
+}  // namespace pic
+
+namespace {
 
 // node kinds and masks; Dirichlet values written into phi_host
 void build_kinds(pic_world* w, std::vector<uint16_t>& kind, std::vector<double>& phi_host) {

@@ -4,6 +4,8 @@
 
 namespace pic {
 
+int set_last_error(int code, const char* msg);  // message for pic_last_error
+
 // Electron-impact collisions against a uniform background gas (fused into the electron push)
 struct CollDev {
     int enabled;

@@ -150,6 +150,23 @@ int pic_species_merge(pic_world* w, int sp, int min_count);
 /* merge counters since creation: bins merged, particles removed, products dropped (NaN) */
 int pic_merge_stats(pic_world* w, uint64_t* out);
 
+/* ---- number density without device allocation -------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device memory (code
+ * running under CUDA graph capture, plugins whose host owns all device memory, real-time
+ * loops that forbid allocation): the number density of one species from particle arrays the
+ * caller already holds on the current device, in the library's layout (pos4: float4 {ox, oy,
+ * oz, packed cell i | j<<10 | k<<20}; vel4: float4 {vx, vy, vz, w}), written to den_out (FP32,
+ * one value per node, node order as above).  Same CIC weights and 64-bit fixed-point sums as
+ * Species::computeNumberDensity (Species.cpp:401-416) with fixed-point scale `scale`.
+ * The working accumulator is a library-owned device array of 2^20 nodes (8 MiB per GPU, held
+ * until exit); larger grids are rejected with PIC_ERR_ARG.  No allocation is made.  The first
+ * call on a device looks up that array's address and should come before any stream capture.
+ * All calls share the array: calls that overlap on the GPU race.  Work is queued on `stream`
+ * (a cudaStream_t, NULL for the default stream) and not waited for. */
+int pic_number_density_noalloc(int ni, int nj, int nk, const double* x0, const double* xm, const int* periodic,
+                               const void* pos4, const void* vel4, long n, double scale, float* den_out,
+                               void* stream);
+
 /* ---- runtime ------------------------------------------------------------------------- */
 int pic_synchronize(pic_world* w);
 /* message of the last failing call on this thread (empty if none) */
