@@ -168,26 +168,35 @@ def barrier(ws):
         dist.barrier()
 
 
-def max_over_ranks(x, ws):
+def _reduce(x, ws, op):
+    """Reduction over replicas: tensors live on the GPU under NCCL, on the CPU under gloo."""
     if ws <= 1:
         return x
     import torch
     import torch.distributed as dist
 
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=op)
     return float(t.item())
+
+
+def max_over_ranks(x, ws):
+    import torch.distributed as dist
+
+    return _reduce(x, ws, dist.ReduceOp.MAX) if ws > 1 else x
 
 
 def sum_over_ranks(x, ws):
-    if ws <= 1:
-        return x
-    import torch
     import torch.distributed as dist
 
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.SUM)
-    return float(t.item())
+    return _reduce(x, ws, dist.ReduceOp.SUM) if ws > 1 else x
+
+
+def aggregate(parts_per_rank, seconds_per_rank, ws):
+    """Whole-job throughput of independent replicas: all ranks' particle-steps over the slowest
+    rank's time."""
+    return sum_over_ranks(parts_per_rank, ws) / max_over_ranks(seconds_per_rank, ws)
 
 
 # ------------------------------------------------------------------------------------------
@@ -322,10 +331,8 @@ def run_gpu(args, wl, rank, ws, local):
     for name in ("push_deposit", "compact", "rho", "poisson", "efield", "sort"):
         ms, nl = W.timer(name)
         groups[name] = dict(ms=ms, launches=nl)
-    device_s = step_ms / 1e3
-    device_s = max_over_ranks(device_s, ws)
     parts_per_step = 0.5 * (n0 + n1)
-    value = sum_over_ranks(parts_per_step * args.steps, ws) / device_s
+    value = aggregate(parts_per_step * args.steps, step_ms / 1e3, ws)
     # roofline of the dominant kernel group
     peak, peak_kind = measured_peak()
     nv = int(np.prod(wl["nn"]))

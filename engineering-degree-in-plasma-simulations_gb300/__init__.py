@@ -68,6 +68,7 @@ def library():
         "pic_species_add_particles": [vp, i, vp, vp, vp, vp, l, i],
         "pic_species_load_uniform": [vp, i, vp, vp, l, d, d, d, u64],
         "pic_species_count": [vp, i, vp],
+        "pic_species_load_box_thermal": [vp, i, vp, vp, d, d, u64],
         "pic_species_get_particles": [vp, i, vp, vp, vp, vp, l, vp],
         "pic_species_push": [vp, i, d, i],
         "pic_species_number_density": [vp, i],
@@ -77,6 +78,9 @@ def library():
         "pic_species_sort": [vp, i, vp],
         "pic_species_sums": [vp, i, vp],
         "pic_charge_density": [vp],
+        "pic_species_sample_moments": [vp, i],
+        "pic_species_clear_samples": [vp, i],
+        "pic_species_gas_properties": [vp, i, vp, vp],
         "pic_solver_configure": [vp, i, d, i, d],
         "pic_solver_solve": [vp, vp, vp],
         "pic_solver_compute_ef": [vp],
@@ -294,6 +298,11 @@ class Species:
                                                 float(self.mpw0 if w_mean is None else w_mean), float(w_sigma),
                                                 int(seed)))
 
+    def loadParticleBoxThermal(self, x0, sides, num_den, T, seed=1):
+        """Species::loadParticleBoxThermal (Species.cpp:564-599), Philox draws."""
+        _check(self._L.pic_species_load_box_thermal(self.world._h, self.id, _p(_f64(x0)), _p(_f64(sides)),
+                                                    float(num_den), float(T), int(seed)))
+
     def getNumParticles(self):
         n = C.c_long()
         _check(self._L.pic_species_count(self.world._h, self.id, C.byref(n)))
@@ -355,6 +364,19 @@ class Species:
         out = np.zeros(4, np.uint64)
         _check(self._L.pic_merge_stats(self.world._h, _p(out)))
         return dict(bins=int(out[0]), removed=int(out[1]), dropped=int(out[2]))
+
+    def sampleMoments(self):
+        _check(self._L.pic_species_sample_moments(self.world._h, self.id))
+
+    def clearSamples(self):
+        _check(self._L.pic_species_clear_samples(self.world._h, self.id))
+
+    def computeGasProperties(self):
+        """(vel [nv,3], T [nv]) as Species::computeGasProperties (Species.cpp:777-804)."""
+        vel = np.zeros((self.world.nv, 3))
+        T = np.zeros(self.world.nv)
+        _check(self._L.pic_species_gas_properties(self.world._h, self.id, _p(vel), _p(T)))
+        return vel, T
 
     def sums(self):
         out = np.zeros(5)

@@ -48,6 +48,7 @@ struct SpeciesHost {
     unsigned long long* id2 = nullptr;
     float* den = nullptr;
     float* den_avg = nullptr;
+    float* mom = nullptr;  // velocity moments, 7 node planes, allocated on first sampleMoments
     int avg_samples = 0;
     double scale = 1.0;  // fixed-point scale of the density accumulator
     unsigned long long next_id = 0;
@@ -428,6 +429,7 @@ extern "C" int pic_world_destroy(pic_world* w) {
         cudaFree(s.id2);
         cudaFree(s.den);
         cudaFree(s.den_avg);
+        if (s.mom) cudaFree(s.mom);
     }
     void* ptrs[] = {w->ef,   w->phi,  w->phi_alt, w->rho,        w->kind,       w->r,        w->e,
                     w->d,    w->d2,   w->q,       w->z,          w->part,       w->scal,     w->flag,
@@ -643,8 +645,37 @@ extern "C" int pic_species_load_uniform(pic_world* w, int sp, const double* lo, 
         la.hi[d] = std::min(hi[d], w->g.xm[d]);
     }
     la.vth = (float)std::sqrt(kKb * T / s.mass);
+    la.ref_thermal = 0;
     la.w_mean = (float)w_mean;
     la.w_sigma = (float)w_sigma;
+    la.id0 = s.next_id;
+    la.key = make_uint2((unsigned)seed, (unsigned)(seed >> 32) ^ (unsigned)(sp * 0x9E3779B9u));
+    la.n = (int)n;
+    s.next_id += n;
+    {
+        Scope sc(w, "load", 2);
+        launch_load_uniform(w->g, s.dev, la, w->stream);
+    }
+    return check_device_error(w);
+}
+
+extern "C" int pic_species_load_box_thermal(pic_world* w, int sp, const double* center, const double* sides,
+                                            double num_den, double T, uint64_t seed) {
+    if (!valid_sp(w, sp) || !center || !sides) return fail(PIC_ERR_ARG, "bad arguments");
+    CU(cudaSetDevice(w->device));
+    SpeciesHost& s = w->sp[sp];
+    double vol = sides[0] * sides[1] * sides[2];
+    long n = (long)(num_den * vol / s.mpw0);  // Species.cpp:565-567
+    if (n < 1) return fail(PIC_ERR_ARG, "number of macroparticles less than 1, change initial values");
+    LoadArgs la;
+    for (int d = 0; d < 3; d++) {
+        la.lo[d] = std::max(center[d] - sides[d] / 2, w->g.x0[d]);
+        la.hi[d] = std::min(center[d] + sides[d] / 2, w->g.xm[d]);
+    }
+    la.vth = (float)std::sqrt(2 * kKb * T / s.mass);
+    la.ref_thermal = 1;
+    la.w_mean = (float)s.mpw0;
+    la.w_sigma = 0.f;
     la.id0 = s.next_id;
     la.key = make_uint2((unsigned)seed, (unsigned)(seed >> 32) ^ (unsigned)(sp * 0x9E3779B9u));
     la.n = (int)n;
@@ -750,6 +781,63 @@ extern "C" int pic_species_number_density(pic_world* w, int sp) {
     int rc = push_species(w, sp, 0.0, 1, false, false);
     if (rc) return rc;
     CU(cudaGetLastError());
+    return PIC_OK;
+}
+
+extern "C" int pic_species_sample_moments(pic_world* w, int sp) {
+    if (!valid_sp(w, sp)) return fail(PIC_ERR_ARG, "bad species");
+    CU(cudaSetDevice(w->device));
+    SpeciesHost& s = w->sp[sp];
+    if (!s.mom) {
+        CU(cudaMalloc((void**)&s.mom, sizeof(float) * 7 * (size_t)w->g.nv));
+        CU(cudaMemsetAsync(s.mom, 0, sizeof(float) * 7 * (size_t)w->g.nv, w->stream));
+    }
+    {
+        Scope sc(w, "moments", 1);
+        launch_sample_moments(w->g, s.dev, s.mom, w->stream, w->grid_parts);
+    }
+    CU(cudaGetLastError());
+    return PIC_OK;
+}
+
+extern "C" int pic_species_clear_samples(pic_world* w, int sp) {
+    if (!valid_sp(w, sp)) return fail(PIC_ERR_ARG, "bad species");
+    CU(cudaSetDevice(w->device));
+    SpeciesHost& s = w->sp[sp];
+    if (s.mom) CU(cudaMemsetAsync(s.mom, 0, sizeof(float) * 7 * (size_t)w->g.nv, w->stream));
+    return PIC_OK;
+}
+
+// Species::computeGasProperties (Species.cpp:777-804): vel = nv/n, T = m/(2k) (var_u + var_v + var_w)
+extern "C" int pic_species_gas_properties(pic_world* w, int sp, double* vel, double* T) {
+    if (!valid_sp(w, sp)) return fail(PIC_ERR_ARG, "bad species");
+    CU(cudaSetDevice(w->device));
+    SpeciesHost& s = w->sp[sp];
+    const int nv = w->g.nv;
+    std::vector<float> m((size_t)7 * nv, 0.f);
+    if (s.mom) {
+        CU(cudaMemcpyAsync(m.data(), s.mom, sizeof(float) * 7 * (size_t)nv, cudaMemcpyDeviceToHost, w->stream));
+        CU(cudaStreamSynchronize(w->stream));
+    }
+    for (int n = 0; n < nv; n++) {
+        double cnt = m[n];
+        double u = cnt > 0 ? m[(size_t)nv + n] / cnt : 0, v = cnt > 0 ? m[(size_t)2 * nv + n] / cnt : 0,
+               ww = cnt > 0 ? m[(size_t)3 * nv + n] / cnt : 0;
+        if (vel) {
+            vel[3 * n] = u;
+            vel[3 * n + 1] = v;
+            vel[3 * n + 2] = ww;
+        }
+        if (T) {
+            if (cnt <= 0) {
+                T[n] = 0;
+                continue;
+            }
+            double uu = m[(size_t)4 * nv + n] / cnt - u * u, vv = m[(size_t)5 * nv + n] / cnt - v * v,
+                   wq = m[(size_t)6 * nv + n] / cnt - ww * ww;
+            T[n] = s.mass / (2 * kKb) * (uu + vv + wq);
+        }
+    }
     return PIC_OK;
 }
 

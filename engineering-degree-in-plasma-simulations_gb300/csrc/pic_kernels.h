@@ -54,7 +54,8 @@ void launch_to_abs(const GridDev& g, SpeciesDev sp, double* pos, double* vel, do
                    int n, cudaStream_t s);
 struct LoadArgs {
     double lo[3], hi[3];   // absolute box
-    float vth;             // sqrt(kT/m) per axis
+    float vth;             // sqrt(kT/m) per axis (Maxwellian) or sqrt(2kT/m) (reference sampleV3th)
+    int ref_thermal;       // 1: Species::sampleV3th speeds and directions (Species.cpp:855-869)
     float w_mean, w_sigma; // lognormal weight (sigma 0: constant w_mean)
     unsigned long long id0;
     uint2 key;
@@ -62,6 +63,7 @@ struct LoadArgs {
 };
 void launch_load_uniform(const GridDev& g, SpeciesDev sp, const LoadArgs& la, cudaStream_t s);
 void launch_sums(SpeciesDev sp, double* out, cudaStream_t s, int grid);
+void launch_sample_moments(const GridDev& g, SpeciesDev sp, float* mom, cudaStream_t s, int grid);
 void launch_merge(const GridDev& g, SpeciesDev sp, const float4* ef, const int* cell_start, int* list, int* nlist,
                   int min_count, float qm_half_dt, uint2 key, unsigned step, unsigned* err,
                   unsigned long long* stats, cudaStream_t s, int grid);

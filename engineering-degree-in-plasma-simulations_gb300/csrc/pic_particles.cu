@@ -842,6 +842,20 @@ __global__ void k_load_uniform(GridDev g, SpeciesDev sp, LoadArgs la) {
         sincosf(kTwoPi * u01(r1.x), &s1, &c1);
         sincosf(kTwoPi * u01(r1.z), &s2, &c2);
         float3 v = make_float3(la.vth * ra * c1, la.vth * ra * s1, la.vth * rb * c2);
+        if (la.ref_thermal) {
+            // Species::sampleVth: speed = |v_th (u1+u2+u3-1.5) per axis|; sampleV3th: isotropic
+            // direction from theta = 2 pi u, r = 2u - 1 (Species.cpp:855-869)
+            uint4 r2 = philox4x32_10(make_uint4((unsigned)id, (unsigned)(id >> 32), 0xA5A5A5A5u, 2u), la.key);
+            uint4 r3 = philox4x32_10(make_uint4((unsigned)id, (unsigned)(id >> 32), 0xA5A5A5A5u, 3u), la.key);
+            float v1 = la.vth * (u01(r1.x) + u01(r1.y) + u01(r1.z) - 1.5f);
+            float v2 = la.vth * (u01(r1.w) + u01(r2.x) + u01(r2.y) - 1.5f);
+            float v3 = la.vth * (u01(r2.z) + u01(r2.w) + u01(r3.x) - 1.5f);
+            float sp_ = sqrtf(v1 * v1 + v2 * v2 + v3 * v3);
+            float st, ct;
+            sincosf(2.f * 3.141592653f * u01(r3.y), &st, &ct);
+            float rr = -1.f + 2.f * u01(r3.z), aa = sqrtf(fmaxf(1.f - rr * rr, 0.f));
+            v = make_float3(sp_ * rr, sp_ * (ct * aa), sp_ * (st * aa));
+        }
         float wgt = la.w_mean;
         if (la.w_sigma > 0.f) {
             // lognormal with mean w_mean: mu = ln(w_mean) - sigma^2/2; the normal is rb*s2
@@ -1109,4 +1123,38 @@ void launch_merge(const GridDev& g, SpeciesDev sp, const float4* ef, const int* 
     k_merge<<<grid, kMergeThreads, 0, s>>>(a);
 }
 
+}  // namespace pic
+
+namespace pic {
+// ------------------------------------------------------------------------------------
+// velocity moments (Species::sampleMoments, Species.cpp:767-776): n, n v, n u^2, n v^2, n w^2
+// scattered with the CIC weights and accumulated across calls until cleared (the reference
+// never clears them inside the loop).  FP32 atomics: a diagnostic, not bit-reproducible.
+// mom layout: 7 planes of nv floats: n, nvx, nvy, nvz, nuu, nvv, nww
+// ------------------------------------------------------------------------------------
+__global__ void k_sample_moments(GridDev g, SpeciesDev sp, float* __restrict__ mom) {
+    const int n = sp.counts[0];
+    const int nij = g.ni * g.nj;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        float4 ps = sp.pos[p], vs = sp.vel[p];
+        int c = __float_as_int(ps.w);
+        if (c < 0) continue;
+        int i, j, k;
+        cell_ijk(g, c, i, j, k);
+        int b = cell_base_node(g, i, j, k);
+        float wx1 = ps.x, wx0 = 1.f - ps.x, wy1 = ps.y, wy0 = 1.f - ps.y, wz1 = ps.z, wz0 = 1.f - ps.z;
+        float wc[8] = {wx0 * wy0 * wz0, wx1 * wy0 * wz0, wx0 * wy1 * wz0, wx1 * wy1 * wz0,
+                       wx0 * wy0 * wz1, wx1 * wy0 * wz1, wx0 * wy1 * wz1, wx1 * wy1 * wz1};
+        int nd[8] = {b, b + 1, b + g.ni, b + g.ni + 1, b + nij, b + nij + 1, b + nij + g.ni, b + nij + g.ni + 1};
+        float val[7] = {vs.w, vs.w * vs.x, vs.w * vs.y, vs.w * vs.z, vs.w * vs.x * vs.x, vs.w * vs.y * vs.y,
+                        vs.w * vs.z * vs.z};
+#pragma unroll
+        for (int m = 0; m < 7; m++)
+#pragma unroll
+            for (int c8 = 0; c8 < 8; c8++) atomicAdd(&mom[(size_t)m * g.nv + nd[c8]], val[m] * wc[c8]);
+    }
+}
+void launch_sample_moments(const GridDev& g, SpeciesDev sp, float* mom, cudaStream_t s, int grid) {
+    k_sample_moments<<<grid, 256, 0, s>>>(g, sp, mom);
+}
 }  // namespace pic

@@ -73,6 +73,11 @@ int pic_species_add_particles(pic_world* w, int sp, const double* pos, const dou
  * log-sigma w_sigma (0: all w_mean), Philox stream keyed by seed. */
 int pic_species_load_uniform(pic_world* w, int sp, const double* lo, const double* hi, long n, double T,
                              double w_mean, double w_sigma, uint64_t seed);
+/* Species::loadParticleBoxThermal(x0, sides, num_den, T)             Species.cpp:564-599
+ * floor(num_den * volume / mpw0) particles of weight mpw0, uniform in the box, speeds and
+ * directions as sampleVth / sampleV3th (Species.cpp:855-869) with Philox draws. */
+int pic_species_load_box_thermal(pic_world* w, int sp, const double* center, const double* sides, double num_den,
+                                 double T, uint64_t seed);
 /* Species::getNumParticles()                                          Species.cpp:43-45 */
 int pic_species_count(pic_world* w, int sp, long* n);
 /* Species::getConstPartRef(): host copy of the particles              Species.cpp:820-822 */
@@ -95,6 +100,13 @@ int pic_species_sort(pic_world* w, int sp, int32_t* cell_counts);
 /* Species::getMicroCount / getMomentum / getKE in FP64                Species.cpp:732-752
  * out[0] sum w, out[1..3] mass * sum w v, out[4] 0.5 mass sum w v.v */
 int pic_species_sums(pic_world* w, int sp, double* out);
+
+/* Species::sampleMoments (Species.cpp:767-776): CIC scatter of n, n v, n u^2, n v^2, n w^2,
+ * accumulated across calls (FP32 atomics, a diagnostic); Species::clearSamples (805-812);
+ * Species::computeGasProperties (777-804): vel (3 per node) and T per node on the host. */
+int pic_species_sample_moments(pic_world* w, int sp);
+int pic_species_clear_samples(pic_world* w, int sp);
+int pic_species_gas_properties(pic_world* w, int sp, double* vel, double* T);
 
 /* World::computeChargeDensity(species): den_s and rho = sum q_s den_s  World.cpp:193-200 */
 int pic_charge_density(pic_world* w);

@@ -106,6 +106,8 @@ class Port:
             "or_merge_gpuform": (l, [vp, vp, vp, vp, l, l, vp, d, d, d, i, u32, u32, u32]),
             "or_load_box_thermal_ref": (l, [vp, vp, vp, l, vp, vp, d, d, d, d, d, vp, d]),
             "or_sums": (None, [vp, l, d, vp, vp, vp]),
+            "or_sample_moments_ref": (None, [vp, vp, l, vp]),
+            "or_gas_properties_ref": (None, [vp, vp, d, vp, vp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -252,6 +254,17 @@ class Port:
                                              _p(None if ef is None else np.ascontiguousarray(ef, np.float64)), dt)
         return parts[:n].copy()
 
+    def sample_moments(self, g, parts, mom=None):
+        mom = np.zeros(7 * self.nv(g)) if mom is None else mom
+        self.lib.or_sample_moments_ref(C.byref(g), _p(parts), len(parts), _p(mom))
+        return mom
+
+    def gas_properties(self, g, mom, mass):
+        vel = np.zeros((self.nv(g), 3))
+        T = np.zeros(self.nv(g))
+        self.lib.or_gas_properties_ref(C.byref(g), _p(mom), mass, _p(vel), _p(T))
+        return vel, T
+
     def sums(self, parts, mass):
         c, ke = C.c_double(), C.c_double()
         mom = np.zeros(3)
@@ -292,6 +305,8 @@ class Ref:
                 "ref_number_density": (None, [vp, i]),
                 "ref_charge_density": (None, [vp]),
                 "ref_merge": (None, [vp, i]),
+                "ref_sample_moments": (None, [vp, i]),
+                "ref_gas_properties": (None, [vp, i, vp, vp]),
                 "ref_get_field": (None, [vp, i, vp]),
                 "ref_set_field": (None, [vp, i, vp]),
                 "ref_get_den": (None, [vp, i, vp]),

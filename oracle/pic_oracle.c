@@ -1475,6 +1475,33 @@ long or_load_box_thermal_ref(const or_grid* g, or_mt* r, or_particle* p, long ca
     return n;
 }
 
+void or_sample_moments_ref(const or_grid* g, const or_particle* p, long n, double* mom) {
+    long nv = (long)g->ni * g->nj * g->nk;
+    for (long q = 0; q < n; q++) {
+        double lc[3];
+        xtol(g, p[q].pos, lc);
+        double w = p[q].w;
+        or_scatter_ref(g, mom, lc, w);
+        for (int d = 0; d < 3; d++) or_scatter_ref(g, mom + (1 + d) * nv, lc, w * p[q].vel[d]);
+        for (int d = 0; d < 3; d++) or_scatter_ref(g, mom + (4 + d) * nv, lc, w * p[q].vel[d] * p[q].vel[d]);
+    }
+}
+void or_gas_properties_ref(const or_grid* g, const double* mom, double mass, double* vel, double* T) {
+    long nv = (long)g->ni * g->nj * g->nk;
+    for (long n = 0; n < nv; n++) {
+        double cnt = mom[n];
+        for (int d = 0; d < 3; d++) vel[3 * n + d] = cnt != 0 ? mom[(1 + d) * nv + n] * (1.0 / cnt) : 0;
+        if (cnt <= 0) {
+            T[n] = 0;
+            continue;
+        }
+        double uu = mom[4 * nv + n] / cnt - vel[3 * n] * vel[3 * n];
+        double vv = mom[5 * nv + n] / cnt - vel[3 * n + 1] * vel[3 * n + 1];
+        double ww = mom[6 * nv + n] / cnt - vel[3 * n + 2] * vel[3 * n + 2];
+        T[n] = mass / (2 * OR_KB) * (uu + vv + ww);
+    }
+}
+
 void or_sums(const or_particle* p, long n, double mass, double* count, double mom[3], double* ke) {
     double c = 0, m[3] = {0, 0, 0}, k = 0;
     for (long q = 0; q < n; q++) {

@@ -146,6 +146,11 @@ long or_load_box_thermal_ref(const or_grid* g, or_mt* r, or_particle* p, long ca
                              const double* sides, double num_den, double T, double mpw0, double mass, double charge,
                              const double* ef, double dt);
 
+/* Species::sampleMoments (Species.cpp:767-776): accumulates into mom[7*nv] (planes n, nvx,
+ * nvy, nvz, nuu, nvv, nww); Species::computeGasProperties (777-804) -> vel[3*nv], T[nv] */
+void or_sample_moments_ref(const or_grid* g, const or_particle* p, long n, double* mom);
+void or_gas_properties_ref(const or_grid* g, const double* mom, double mass, double* vel, double* T);
+
 /* conservation sums (Species.cpp:732-752) */
 void or_sums(const or_particle* p, long n, double mass, double* count, double mom[3], double* ke);
 

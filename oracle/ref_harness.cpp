@@ -139,6 +139,19 @@ void ref_charge_density(void* h) {
     s->world->computeChargeDensity(s->species);
 }
 void ref_merge(void* h, int sp) { static_cast<RefSim*>(h)->species[sp].merge(); }
+// Species::sampleMoments + computeGasProperties; the public vel and T fields come back
+void ref_sample_moments(void* h, int sp) { static_cast<RefSim*>(h)->species[sp].sampleMoments(); }
+void ref_gas_properties(void* h, int sp, double* vel, double* T) {
+    Species& s = static_cast<RefSim*>(h)->species[sp];
+    s.computeGasProperties();
+    for (int k = 0; k < s.T.nk; k++)
+        for (int j = 0; j < s.T.nj; j++)
+            for (int i = 0; i < s.T.ni; i++) {
+                int n = s.T.U(i, j, k);
+                T[n] = s.T[i][j][k];
+                for (int d = 0; d < 3; d++) vel[3 * n + d] = s.vel[i][j][k][d];
+            }
+}
 
 static void get_scalar(const Field<type_calc>& f, double* out) {
     for (int k = 0; k < f.nk; k++)

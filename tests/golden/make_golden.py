@@ -44,10 +44,17 @@ def case_push_deposit():
     pushed = R.get_particles(e)
     R.L.ref_number_density(R.h, e)
     den = R.den(e)
+    # Species::sampleMoments twice (it accumulates) + computeGasProperties
+    R.L.ref_sample_moments(R.h, e)
+    R.L.ref_sample_moments(R.h, e)
+    gvel = np.zeros((R.nv, 3))
+    gT = np.zeros(R.nv)
+    R.L.ref_gas_properties(R.h, e, gvel.ctypes.data_as(C.c_void_p), gT.ctypes.data_as(C.c_void_p))
     out = dict(nn=np.array(nn), x0=np.array(x0), xm=np.array(xm), ef=ef, dt=np.array(1e-11))
     out.update({"in_" + k: v for k, v in parts_arrays(loaded).items()})
     out.update({"out_" + k: v for k, v in parts_arrays(pushed).items()})
     out["den"] = den
+    out["gas_vel"], out["gas_T"] = gvel, gT
     return out
 
 

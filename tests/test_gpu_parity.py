@@ -487,3 +487,43 @@ def test_merge_conserves_weight_momentum_energy(pic):
     assert abs(s1[0] - s0[0]) <= 1e-6 * s0[0]
     assert np.all(np.abs(s1[1:4] - s0[1:4]) <= 1e-5 * np.abs(s0[1:4]).max())
     assert abs(s1[4] - s0[4]) <= 1e-5 * s0[4]
+
+
+def test_moments_and_gas_properties(pic):
+    d = golden("push_deposit")
+    W = pic.World(*d["nn"], d["x0"], d["xm"])
+    e = pic.Species("e-", pic.ME, -pic.QE, W, 100.0, capacity=4096)
+    e.addParticles(d["out_pos"], d["out_vel"], d["out_w"], rewind=False)
+    e.sampleMoments()
+    e.sampleMoments()  # accumulates, as Species::sampleMoments does
+    vel, T = e.computeGasProperties()
+    # FP32 atomics against the FP64 reference; T is a difference of second moments
+    assert np.max(np.abs(vel - d["gas_vel"])) <= 1e-4 * np.max(np.abs(d["gas_vel"]))
+    big = d["gas_T"] > 1e-3 * d["gas_T"].max()
+    assert np.max(np.abs(T[big] - d["gas_T"][big]) / d["gas_T"][big]) <= 1e-3
+    e.clearSamples()
+    vel0, T0 = e.computeGasProperties()
+    assert not np.any(T0) and not np.any(vel0)
+
+
+def test_box_thermal_loader_matches_reference_distribution(pic, port):
+    """Species::loadParticleBoxThermal: count, weights and the speed distribution of
+    sampleV3th (sum of three uniforms per axis, isotropic direction) against the oracle's
+    MT19937 restatement of the reference loader."""
+    nn, x0, xm = (11, 11, 11), (0.0, 0.0, 0.0), (0.01, 0.01, 0.01)
+    W = pic.World(*nn, x0, xm)
+    e = pic.Species("e-", pic.ME, -pic.QE, W, 10.0, capacity=300000)
+    c, s, den, T = (0.005, 0.005, 0.005), (0.008, 0.006, 0.01), 4e11, 11604.0
+    e.loadParticleBoxThermal(c, s, den, T, seed=3)
+    p = e.getPartRef()
+    g = port.grid(nn, x0, xm)
+    ref = port.load_box_thermal_ref(g, port.mt(3), 300000, c, s, den, T, 10.0, O.ME, -O.QE)
+    assert len(p) == len(ref) == int(den * 0.008 * 0.006 * 0.01 / 10.0)
+    assert np.all(p["w"] == 10.0)
+    lo, hi = np.array(c) - np.array(s) / 2, np.array(c) + np.array(s) / 2
+    assert np.all(p["pos"] >= lo - 1e-12) and np.all(p["pos"] < hi + 1e-12)
+    sp_g = np.sort(np.linalg.norm(p["vel"], axis=1))
+    sp_r = np.sort(np.linalg.norm(ref["vel"], axis=1))
+    q = np.linspace(0.05, 0.95, 19)
+    assert np.allclose(np.quantile(sp_g, q), np.quantile(sp_r, q), rtol=0.01)
+    assert np.all(np.abs(p["vel"].mean(0)) <= 0.01 * sp_r.mean())

@@ -180,3 +180,13 @@ def test_merge_conserves_mass_momentum_energy(port):
     assert abs(c1 - c0) <= 1e-12 * c0
     assert np.all(np.abs(m1 - m0) <= 1e-9 * np.abs(m0).max())
     assert abs(k1 - k0) <= 1e-9 * k0
+
+
+def test_moments_and_gas_properties_bit_exact(port):
+    d = golden("push_deposit")
+    g = port.grid(d["nn"], d["x0"], d["xm"])
+    p = to_parts(d, "out_")
+    mom = port.sample_moments(g, p)
+    mom = port.sample_moments(g, p, mom)  # accumulated twice, as the golden run
+    vel, T = port.gas_properties(g, mom, O.ME)
+    assert np.array_equal(vel, d["gas_vel"]) and np.array_equal(T, d["gas_T"])
