@@ -597,6 +597,10 @@ extern "C" int pic_species_create(pic_world* w, const char* name, double mass, d
     if (ex > 60) ex = 60;
     if (ex < -60) ex = -60;
     s.scale = std::ldexp(1.0, ex);
+    // one scale for all species (the smallest), so rho can be summed exactly in integers;
+    // species are created before anything is deposited
+    for (auto& o : w->sp) s.scale = std::min(s.scale, o.scale);
+    for (auto& o : w->sp) o.scale = s.scale;
     w->sp.push_back(s);
     *species_id = (int)w->sp.size() - 1;
     return PIC_OK;
@@ -751,7 +755,10 @@ int push_species(pic_world* w, int sp, double dt, int deposit, bool with_mcc, bo
         a.coll.step = (unsigned)w->ts;
         a.coll.ion = w->sp[w->mcc_i].dev;
     }
-    if (deposit) s.deposited = true;
+    if (deposit) {
+        s.deposited = true;
+        CU(cudaMemsetAsync(s.dev.acc, 0, sizeof(unsigned long long) * w->g.nv, w->stream));
+    }
     {
         Scope sc(w, deposit ? "push_deposit" : "push", 1);
         launch_push(a, w->stream, a.coll.enabled ? w->grid_push_mcc : w->grid_push);
@@ -847,21 +854,25 @@ extern "C" int pic_charge_density(pic_world* w) {
     FinalizeArgs a{};
     a.g = w->g;
     a.ns = (int)w->sp.size();
+    a.int_path = a.ns > 0;
     for (int s = 0; s < a.ns; s++) {
         SpeciesHost& sh = w->sp[s];
         a.acc[s] = sh.dev.acc;
         a.inv_scale[s] = (float)(1.0 / sh.scale);
         a.charge[s] = (float)sh.charge;
         a.den[s] = sh.den;
-        a.fresh[s] = sh.deposited ? 1 : 0;
+        double zf = sh.charge / kQe;
+        a.z[s] = (int)std::lround(zf);
+        if (std::fabs(zf - a.z[s]) > 1e-9 || std::abs(a.z[s]) > 8 || sh.scale != w->sp[0].scale) a.int_path = 0;
     }
+    a.rho_scale = a.ns ? (float)(kQe / w->sp[0].scale) : 0.f;
     a.rho = w->rho;
     {
         Scope sc(w, "rho", 1);
         launch_finalize_rho(a, w->stream, w->grid_nodes);
     }
-    // a species not deposited since the last call keeps its den (the reference keeps the
-    // density of a subcycled species from its last push, main.cpp:222-234)
+    // the accumulators are cleared when a species deposits again, so a species that was not
+    // pushed this step keeps the density of its last push (main.cpp:222-234 subcycling)
     for (auto& s : w->sp) s.deposited = false;
     CU(cudaGetLastError());
     return PIC_OK;

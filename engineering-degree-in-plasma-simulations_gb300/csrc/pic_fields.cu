@@ -58,34 +58,30 @@ __device__ __forceinline__ void stencil(const GridDev& g, int i, int j, int k, S
 // ------------------------------------------------------------------------------------
 __global__ void k_finalize_rho(FinalizeArgs a) {
     const GridDev& g = a.g;
-    const double inv_base = 1.0 / (g.dxd[0] * g.dxd[1] * g.dxd[2]);
+    const float inv_base = (float)(1.0 / (g.dxd[0] * g.dxd[1] * g.dxd[2]));
     const int nn[3] = {g.ni, g.nj, g.nk}, stride[3] = {1, g.ni, g.ni * g.nj};
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
         int ijk[3];
         node_ijk(g, n, ijk[0], ijk[1], ijk[2]);
         bool alias = false;
         unsigned fold = 0;
-        double inv_vol = inv_base;  // boundary nodes have half volume per face: exact powers of two
+        float inv_vol = inv_base;  // boundary nodes have half volume per face: exact powers of two
         for (int d = 0; d < 3; d++) {
             if (g.periodic[d]) {
                 if (ijk[d] == nn[d] - 1) alias = true;
                 if (ijk[d] == 0) fold |= 1u << d;
             } else if (ijk[d] == 0 || ijk[d] == nn[d] - 1) {
-                inv_vol *= 2.0;
+                inv_vol *= 2.f;
             }
         }
         if (alias) continue;  // written by the node it copies
-        double rho = 0;
         float den_out[kMaxSpecies];
-        for (int s = 0; s < a.ns; s++) {
-            if (!a.fresh[s]) {
-                // not deposited since the last call (subcycled species): keep its density
-                den_out[s] = a.den[s][n];
-                rho += (double)a.charge[s] * (double)den_out[s];
-                continue;
-            }
+        long long rho_fixed = 0;
+        float rho_f = 0.f;
+#pragma unroll
+        for (int s = 0; s < kMaxSpecies; s++) {
+            if (s >= a.ns) break;
             unsigned long long tot = a.acc[s][n];
-            a.acc[s][n] = 0ull;
             if (fold) {
                 for (unsigned m = 1; m < 8; m++) {
                     if (m & ~fold) continue;
@@ -93,16 +89,18 @@ __global__ void k_finalize_rho(FinalizeArgs a) {
                     for (int d = 0; d < 3; d++)
                         if (m & (1u << d)) node += (nn[d] - 1) * stride[d];
                     tot += a.acc[s][node];
-                    a.acc[s][node] = 0ull;
                 }
             }
-            double den = (double)tot * ((double)a.inv_scale[s] * inv_vol);
-            den_out[s] = (float)den;
-            rho += (double)a.charge[s] * den;
+            den_out[s] = __ull2float_rn(tot) * (a.inv_scale[s] * inv_vol);
+            if (a.int_path) rho_fixed += (long long)a.z[s] * (long long)tot;
+            else rho_f += a.charge[s] * den_out[s];
         }
-        const float rf = (float)rho;
-        for (int s = 0; s < a.ns; s++)
-            if (a.fresh[s]) a.den[s][n] = den_out[s];
+        const float rf = a.int_path ? __ll2float_rn(rho_fixed) * (a.rho_scale * inv_vol) : rho_f;
+#pragma unroll
+        for (int s = 0; s < kMaxSpecies; s++) {
+            if (s >= a.ns) break;
+            a.den[s][n] = den_out[s];
+        }
         a.rho[n] = rf;
         if (fold) {
             for (unsigned m = 1; m < 8; m++) {
@@ -110,8 +108,11 @@ __global__ void k_finalize_rho(FinalizeArgs a) {
                 int node = n;
                 for (int d = 0; d < 3; d++)
                     if (m & (1u << d)) node += (nn[d] - 1) * stride[d];
-                for (int s = 0; s < a.ns; s++)
-                    if (a.fresh[s]) a.den[s][node] = den_out[s];
+#pragma unroll
+                for (int s = 0; s < kMaxSpecies; s++) {
+                    if (s >= a.ns) break;
+                    a.den[s][node] = den_out[s];
+                }
                 a.rho[node] = rf;
             }
         }
@@ -207,7 +208,12 @@ __device__ __forceinline__ double sum_partials(const double* part, int nblocks) 
 __global__ void k_residual(GridDev g, const double* __restrict__ phi_in, double* __restrict__ phi_out,
                            const float* __restrict__ e, const float* __restrict__ rho,
                            const uint16_t* __restrict__ kind, float* __restrict__ r, double* part, int apply_e) {
-    double acc[2] = {0.0, 0.0};
+    // L(phi)_p = sum_axes c ((phi_p - phi_minus) + (phi_p - phi_plus)), a mirror neighbour
+    // taking phi_p: differences of neighbouring potentials in FP64, so the residual keeps FP64
+    // accuracy (12 FP64 operations per node)
+    const double cd[3] = {1.0 / (g.dxd[0] * g.dxd[0]), 1.0 / (g.dxd[1] * g.dxd[1]), 1.0 / (g.dxd[2] * g.dxd[2])};
+    const float inv_eps0 = (float)(1.0 / kEps0);
+    float acc_r = 0.f, acc_b = 0.f;  // per-thread sums in FP32, block and grid sums in FP64
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
         uint16_t kd = kind[n];
         if ((kd & 3) != kFree) {
@@ -220,32 +226,32 @@ __global__ void k_residual(GridDev g, const double* __restrict__ phi_in, double*
         Stencil s;
         stencil(g, i, j, k, s);
         const double pp = phi_in[n];
+        double nb[3];
+        float bfix = 0.f, le = 0.f;
         const float ep = apply_e ? e[n] : 0.f;
-        // L(phi + e)_p = sum over axes of c (2 v_p - v_minus - v_plus), a mirror neighbour taking
-        // the value of p.  Second differences of the potential and the residual are FP64; the
-        // correction e enters through FP32 second differences.
-        double lphi = 0.0;
-        float bfix = 0.f;
 #pragma unroll
         for (int ax = 0; ax < 3; ax++) {
             const int dm = 2 * ax, dp = 2 * ax + 1;
             const bool mm = kd & (1u << (2 + dm)), mp = kd & (1u << (2 + dp));
             const double pm = mm ? pp : phi_in[s.q[dm]];
             const double pq = mp ? pp : phi_in[s.q[dp]];
-            double d2 = (pp - pm) + (pp - pq);
-            if (apply_e) d2 += (double)((2.f * ep - (mm ? ep : e[s.q[dm]])) - (mp ? ep : e[s.q[dp]]));
-            lphi += (double)s.c[dm] * d2;
+            nb[ax] = (pp - pm) + (pp - pq);
+            if (apply_e) le += s.c[dm] * ((2.f * ep - (mm ? ep : e[s.q[dm]])) - (mp ? ep : e[s.q[dp]]));
             if (kd & (1u << (8 + dm))) bfix += s.c[dm] * (float)pm;
             if (kd & (1u << (8 + dp))) bfix += s.c[dp] * (float)pq;
         }
-        const double src = (double)rho[n] * (1.0 / kEps0);
-        const double res = src - lphi;
+        double lphi = fma(cd[2], nb[2], fma(cd[1], nb[1], cd[0] * nb[0]));
+        if (apply_e) lphi += (double)le;
+        const float src = rho[n] * inv_eps0;
+        const double res = (double)src - lphi;
         if (apply_e) phi_out[n] = pp + (double)ep;
-        r[n] = (float)res;
-        const double b = src + (double)bfix;
-        acc[0] += res * res;
-        acc[1] += b * b;
+        const float rf = (float)res;
+        r[n] = rf;
+        const float b = src + bfix;
+        acc_r += rf * rf;
+        acc_b += b * b;
     }
+    double acc[2] = {acc_r, acc_b};
     block_partials<2>(acc, part, kParts);
 }
 void launch_residual(const GridDev& g, SolveWork& w, int apply_e, cudaStream_t s, int grid) {

@@ -72,11 +72,15 @@ void launch_merge(const GridDev& g, SpeciesDev sp, const float4* ef, const int* 
 struct FinalizeArgs {
     GridDev g;
     int ns;
-    unsigned long long* acc[kMaxSpecies];
+    const unsigned long long* acc[kMaxSpecies];
     float inv_scale[kMaxSpecies];
     float charge[kMaxSpecies];
     float* den[kMaxSpecies];
-    int fresh[kMaxSpecies];  // deposited since the last call: rebuild den from the accumulator
+    // integer path: every species shares one fixed-point scale and carries an integer number of
+    // elementary charges, so rho = q_e * sum_s z_s acc_s is formed exactly in 64-bit integers
+    int int_path;
+    int z[kMaxSpecies];
+    float rho_scale;  // q_e / scale
     float* rho;
 };
 void launch_finalize_rho(const FinalizeArgs& a, cudaStream_t s, int grid);

@@ -123,15 +123,16 @@ __device__ float3 new_vel_electron(const CollDev& c, float E, float3 u, float r_
 struct Tile {
     const float4* etile;  // staged E rows (row m at etile + m*kSeg), or nullptr
     unsigned* dtile;      // deposit tile: limb l of row m at dtile + (l*4 + m)*kSeg, or nullptr
-    int lo;                    // first node of the gather window
-    int off[4];                // node offsets of the four rows: 0, ni, ni*nj, ni*nj+ni
+    int lo;               // first base node of the staged window
+    int span;             // base nodes lo .. lo + span are staged
+    int off[4];           // node offsets of the four rows: 0, ni, ni*nj, ni*nj+ni
 };
 
 // E at the eight corners of the cell whose base node is b (Field::gather order)
 __device__ __forceinline__ float3 gather_e(const PushArgs& a, const Tile& t, int b, float3 o) {
     const float4* e0;
     int r1, r2, r3;
-    if (t.etile) {
+    if (t.etile && (unsigned)(b - t.lo) <= (unsigned)t.span) {
         e0 = t.etile + (b - t.lo);
         r1 = kSeg;
         r2 = 2 * kSeg;
@@ -332,7 +333,7 @@ __global__ void __launch_bounds__(kThreads, kMcc ? 2 : 3) k_push(PushArgs a) {
     unsigned* dtile = reinterpret_cast<unsigned*>(smem + 4 * kSeg * sizeof(float4));
     __shared__ __align__(8) unsigned long long bar;
     __shared__ int s_min[kThreads / 32], s_max[kThreads / 32];
-    __shared__ int s_lo, s_hi, s_fail;
+    __shared__ int s_lo, s_hi, s_fail, s_first, s_last;
 
     const GridDev& g = a.g;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -376,6 +377,17 @@ __global__ void __launch_bounds__(kThreads, kMcc ? 2 : 3) k_push(PushArgs a) {
                 }
             }
         }
+        // the window follows the chunk's first and last particle (the sorted order); particles
+        // that have since moved to another row of cells fall outside it and use global memory
+        {
+            const int plast = min(base + kChunk, n) - 1 - base;
+            if (tid == 0) s_first = bn[0];
+            if (tid == plast / kPPT) {
+#pragma unroll
+                for (int q = 0; q < kPPT; q++)
+                    if (q == plast % kPPT) s_last = bn[q];
+            }
+        }
         lmin = __reduce_min_sync(0xffffffffu, lmin);
         lmax = __reduce_max_sync(0xffffffffu, lmax);
         if (lane == 0) {
@@ -389,6 +401,11 @@ __global__ void __launch_bounds__(kThreads, kMcc ? 2 : 3) k_push(PushArgs a) {
                 mn = min(mn, s_min[w]);
                 mx = max(mx, s_max[w]);
             }
+            if (mx >= 0 && mx - mn + 2 > kSeg - kMargin && s_first >= 0 && s_last >= s_first &&
+                s_last - s_first + 2 <= kSeg - kMargin) {
+                mn = s_first;  // outliers present: keep the bulk of the chunk
+                mx = s_last;
+            }
             s_lo = mn;
             s_hi = mx;
             s_fail = 0;
@@ -397,6 +414,7 @@ __global__ void __launch_bounds__(kThreads, kMcc ? 2 : 3) k_push(PushArgs a) {
         const int lo = s_lo, hi = s_hi;
         const bool use_tile = a.staged && hi >= 0 && (hi - lo + 2) <= kSeg - kMargin;
         t.lo = lo;
+        t.span = hi - lo;
         t.etile = nullptr;
         t.dtile = nullptr;
         if (use_tile) {
@@ -754,6 +772,7 @@ __global__ void k_from_abs(GridDev g, SpeciesDev sp, const double* pos, const do
             t.etile = nullptr;
             t.dtile = nullptr;
             t.lo = 0;
+            t.span = -1;
             t.off[0] = 0;
             t.off[1] = g.ni;
             t.off[2] = g.ni * g.nj;
@@ -1073,6 +1092,7 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge(MergeArgs a) {
             t.etile = nullptr;
             t.dtile = nullptr;
             t.lo = 0;
+            t.span = -1;
             t.off[0] = 0;
             t.off[1] = a.g.ni;
             t.off[2] = a.g.ni * a.g.nj;
