@@ -55,7 +55,13 @@ WORKLOADS = {
     # 64 x 64 x 256 nodes over 0.02 x 0.02 x 0.08 m, 500 V, O2 1e21 m^-3, 2 M + 2 M, mean weight 64
     "discharge": dict(nn=(64, 64, 256), L=(0.02, 0.02, 0.08), V=500.0, n_gas=1e21, n_each=2_000_000,
                       w_mean=64.0, dt=2e-12, name="electrode discharge 64x64x256, 2M e- + 2M O2+"),
+    # the large discharge at one eighth of the nodes and particles: particle arrays (0.5 GB per
+    # species) still exceed L2, small enough for a full profiler capture
+    "mid": dict(nn=(128, 128, 256), L=(0.04, 0.04, 0.08), V=1000.0, n_gas=2e21, n_each=12_500_000,
+                w_mean=40.96, dt=1e-12, name="mid discharge 128x128x256, 12.5M e- + 12.5M O2+"),
 }
+MERGE_EVERY = 20  # merge pass cadence in the timed loop (the reference merges every 50 steps)
+MERGE_MIN = 64    # a cell is merged when it holds more than this many particles of a species
 
 
 def setup_world(pic, wl, seed=1):
@@ -75,7 +81,8 @@ def setup_world(pic, wl, seed=1):
     M = pic.MC_MEX_Ionization(e, i, W, wl["n_gas"], 300.0, 32 * AMU, LOTZ["I"], E, S, sigma_ion_kind=1,
                               sigma_ion_params=(LOTZ["A"], LOTZ["b"], LOTZ["c"], 0.0), seed=seed)
     S_ = pic.PotentialSolver(W, 20000, 1e-6, pic.SOLVER_PCG)
-    W.configure_loop(solve_each_step=True, sort_every=20)
+    W.configure_loop(solve_each_step=True, sort_every=20, merge_every=MERGE_EVERY, merge_after=0,
+                     merge_min=MERGE_MIN)
     return W, e, i, M, S_
 
 
@@ -301,6 +308,8 @@ def run_reference(args, wl, rank, ws):
 # GPU arm
 # ------------------------------------------------------------------------------------------
 def run_gpu(args, wl, rank, ws, local):
+    import torch
+
     pic = importlib.import_module(PKG)
     W, e, i, M, S = setup_world(pic, wl, seed=1 + rank)
     assert S.solve(raise_on_fail=True)  # initial vacuum + space-charge field (main.cpp:172-173)
@@ -317,11 +326,14 @@ def run_gpu(args, wl, rank, ws, local):
     barrier(ws)
     W.synchronize()
     with ClockSampler(local) as clk:
+        # the timed steps are the profiler range (cudaProfilerStart/Stop; no effect without a profiler)
+        torch.cuda.profiler.start()
         t0 = time.perf_counter()
         for _ in range(args.steps):
             W.step()
         W.synchronize()
         wall = time.perf_counter() - t0
+        torch.cuda.profiler.stop()
     n1 = e.getNumParticles() + i.getNumParticles()
     launches = W.launches() - launches0
     step_ms, _ = W.timer("step")
@@ -386,7 +398,8 @@ def run_gpu(args, wl, rank, ws, local):
                    "ionizations_per_step": coll["ionizations"] / args.steps,
                    "poisson_inner_per_step": inner / args.steps, "sort_every": 20,
                    "l2": "inputs larger than L2 (particles %.1f GB)" % (parts_per_step * 36 / 1e9),
-                   "merging": "off", "parallelism": "replicas" if ws > 1 else "1 GPU"},
+                   "merging": "every %d steps, cells above %d particles" % (MERGE_EVERY, MERGE_MIN),
+                   "parallelism": "replicas" if ws > 1 else "1 GPU"},
         "wall_s": wall,
         "gpu_launches": launches,
         "roofline": roof,

@@ -212,7 +212,7 @@ __global__ void k_residual(GridDev g, const double* __restrict__ phi_in, double*
     // taking phi_p: differences of neighbouring potentials in FP64, so the residual keeps FP64
     // accuracy (12 FP64 operations per node)
     const double cd[3] = {1.0 / (g.dxd[0] * g.dxd[0]), 1.0 / (g.dxd[1] * g.dxd[1]), 1.0 / (g.dxd[2] * g.dxd[2])};
-    const float inv_eps0 = (float)(1.0 / kEps0);
+    const double inv_eps0 = 1.0 / kEps0;
     float acc_r = 0.f, acc_b = 0.f;  // per-thread sums in FP32, block and grid sums in FP64
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
         uint16_t kd = kind[n];
@@ -242,12 +242,13 @@ __global__ void k_residual(GridDev g, const double* __restrict__ phi_in, double*
         }
         double lphi = fma(cd[2], nb[2], fma(cd[1], nb[1], cd[0] * nb[0]));
         if (apply_e) lphi += (double)le;
-        const float src = rho[n] * inv_eps0;
-        const double res = (double)src - lphi;
+        // the source rho / eps0 in FP64: an FP32 product alone would floor the residual near 3e-8
+        const double src = (double)rho[n] * inv_eps0;
+        const double res = src - lphi;
         if (apply_e) phi_out[n] = pp + (double)ep;
         const float rf = (float)res;
         r[n] = rf;
-        const float b = src + bfix;
+        const float b = (float)src + bfix;
         acc_r += rf * rf;
         acc_b += b * b;
     }

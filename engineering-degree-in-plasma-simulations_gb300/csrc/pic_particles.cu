@@ -19,6 +19,7 @@ constexpr int kPPT = 4;                     // particles per thread per chunk
 constexpr int kChunk = kThreads * kPPT;     // particles per chunk
 constexpr int kSeg = 512;                   // nodes per staged row segment
 constexpr int kMargin = 2;                  // deposit window starts this many nodes below the gather window
+constexpr int kHalfWin = (kSeg - kMargin - 2) / 2;  // staged base nodes either side of the chunk's anchor
 // E rows (float4) + fixed-point deposit tile: three 21-bit limb planes of 32-bit counters,
 // four rows of kSeg nodes each
 constexpr size_t kPushSmem = 4 * kSeg * sizeof(float4) + 3 * 4 * kSeg * sizeof(unsigned);
@@ -333,7 +334,7 @@ __global__ void __launch_bounds__(kThreads, kMcc ? 2 : 3) k_push(PushArgs a) {
     unsigned* dtile = reinterpret_cast<unsigned*>(smem + 4 * kSeg * sizeof(float4));
     __shared__ __align__(8) unsigned long long bar;
     __shared__ int s_min[kThreads / 32], s_max[kThreads / 32];
-    __shared__ int s_lo, s_hi, s_fail, s_first, s_last;
+    __shared__ int s_lo, s_hi, s_fail, s_first;
 
     const GridDev& g = a.g;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -359,7 +360,6 @@ __global__ void __launch_bounds__(kThreads, kMcc ? 2 : 3) k_push(PushArgs a) {
         const int base = ch * kChunk;
         float4 P[kPPT], V[kPPT];
         int bn[kPPT];
-        int lmin = INT_MAX, lmax = -1;
         // each thread takes kPPT consecutive particles: in a cell-sorted chunk they mostly share a
         // cell, so their deposits are summed in registers before touching shared memory
 #pragma unroll
@@ -370,29 +370,37 @@ __global__ void __launch_bounds__(kThreads, kMcc ? 2 : 3) k_push(PushArgs a) {
                 P[q] = a.sp.pos[p];
                 V[q] = a.sp.vel[p];
                 int c = __float_as_int(P[q].w);
-                if (c >= 0) {
-                    bn[q] = ((c >> 20) * g.nj + ((c >> 10) & 1023)) * g.ni + (c & 1023);
+                if (c >= 0) bn[q] = ((c >> 20) * g.nj + ((c >> 10) & 1023)) * g.ni + (c & 1023);
+            }
+        }
+        // the window is centred on the base node of the chunk's middle particle (the sorted order
+        // puts the bulk of the chunk around it); particles more than kHalfWin nodes away (moved to
+        // another row of cells since the last sort, or an unsorted chunk) use global memory
+        {
+            const int mid = (min(base + kChunk, n) - base) >> 1;
+            if (tid == mid / kPPT) {
+#pragma unroll
+                for (int q = 0; q < kPPT; q++)
+                    if (q == mid % kPPT) s_first = bn[q];
+            }
+        }
+        __syncthreads();
+        {
+            const int anchor = s_first;
+            int lmin = INT_MAX, lmax = -1;
+#pragma unroll
+            for (int q = 0; q < kPPT; q++) {
+                if (bn[q] >= 0 && anchor >= 0 && abs(bn[q] - anchor) <= kHalfWin) {
                     lmin = min(lmin, bn[q]);
                     lmax = max(lmax, bn[q]);
                 }
             }
-        }
-        // the window follows the chunk's first and last particle (the sorted order); particles
-        // that have since moved to another row of cells fall outside it and use global memory
-        {
-            const int plast = min(base + kChunk, n) - 1 - base;
-            if (tid == 0) s_first = bn[0];
-            if (tid == plast / kPPT) {
-#pragma unroll
-                for (int q = 0; q < kPPT; q++)
-                    if (q == plast % kPPT) s_last = bn[q];
+            lmin = __reduce_min_sync(0xffffffffu, lmin);
+            lmax = __reduce_max_sync(0xffffffffu, lmax);
+            if (lane == 0) {
+                s_min[warp] = lmin;
+                s_max[warp] = lmax;
             }
-        }
-        lmin = __reduce_min_sync(0xffffffffu, lmin);
-        lmax = __reduce_max_sync(0xffffffffu, lmax);
-        if (lane == 0) {
-            s_min[warp] = lmin;
-            s_max[warp] = lmax;
         }
         __syncthreads();
         if (tid == 0) {
@@ -400,11 +408,6 @@ __global__ void __launch_bounds__(kThreads, kMcc ? 2 : 3) k_push(PushArgs a) {
             for (int w = 0; w < kThreads / 32; w++) {
                 mn = min(mn, s_min[w]);
                 mx = max(mx, s_max[w]);
-            }
-            if (mx >= 0 && mx - mn + 2 > kSeg - kMargin && s_first >= 0 && s_last >= s_first &&
-                s_last - s_first + 2 <= kSeg - kMargin) {
-                mn = s_first;  // outliers present: keep the bulk of the chunk
-                mx = s_last;
             }
             s_lo = mn;
             s_hi = mx;
