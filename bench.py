@@ -430,24 +430,62 @@ def blob_rho(nn, seed):
     return rho.ravel()
 
 
-def poisson_bench(pic, n, seed=5):
+def poisson_bench(pic, n, seed=5, train_steps=300):
     """Time to a 1e-6 FP64 relative residual from the Dirichlet-only start, n^3 nodes over a
-    0.04 m cube, z faces at 0 V / 1000 V, periodic x, y; blob charge density."""
+    0.04 m cube, z faces at 0 V / 1000 V, periodic x, y; blob charge density.  Plain red-black
+    SOR and Jacobi-PCG against the learned multilevel preconditioner, first at its starting
+    (BPX) weights, then after online training on the pairs of four solves of other blob densities
+    plus white-noise pairs.  Training time is reported separately (it is amortised over a run)."""
+    nn = (n, n, n)
     W = pic.World(n, n, n, (0.0, 0.0, 0.0), (0.04, 0.04, 0.04))
     W.set_boundaries((1, 1, 0), (1,) * 6, (0, 0, 0, 0, 0.0, 1000.0))
-    W.rho = blob_rho((n, n, n), seed)
+    rho_test = blob_rho(nn, seed)
+    W.rho = rho_test
     phi0 = W.phi
     omega = 2.0 / (1.0 + np.sin(np.pi / (n - 1)))  # optimal SOR weight of the model problem
     out = {"grid": [n, n, n], "tol": 1e-6}
-    for name, method, w in (("rbsor", pic.SOLVER_RBSOR, omega), ("pcg", pic.SOLVER_PCG, 1.4)):
+
+    def timed(method, w=1.4):
         W.phi = phi0
         S = pic.PotentialSolver(W, 200000, 1e-6, method, omega=w)
+        W.timing(True)
+        W.timing_reset()
         W.synchronize()
         t0 = time.perf_counter()
         ok = S.solve()
         W.synchronize()
-        out[name] = {"seconds": time.perf_counter() - t0, "iterations": S.iters, "rel": S.rel, "converged": ok}
+        wall = time.perf_counter() - t0
+        dev_ms, launches = W.timer("poisson")
+        W.timing(False)
+        return {"seconds": wall, "iterations": S.iters, "rel": S.rel, "converged": ok,
+                "device_seconds": dev_ms / 1e3, "launches": launches}
+
+    out["rbsor"] = timed(pic.SOLVER_RBSOR, omega)
     out["rbsor"]["omega"] = omega
+    out["pcg"] = timed(pic.SOLVER_PCG)
+    lp = pic.LearnedPreconditioner(W)
+    lp.reset()
+    out["learned_start"] = timed(pic.SOLVER_LEARNED)
+    # online training on (rho, phi) pairs of the run's other solves
+    W.synchronize()
+    t0 = time.perf_counter()
+    lp.collect(True)
+    S = pic.PotentialSolver(W, 200000, 1e-6, pic.SOLVER_LEARNED)
+    for k in range(4):
+        W.rho = blob_rho(nn, seed + 101 + k)
+        W.phi = phi0
+        S.solve()
+    lp.collect(False)
+    loss_first = lp.train(10)
+    loss_last = lp.train(train_steps - 10) if train_steps > 10 else loss_first
+    W.synchronize()
+    train_s = time.perf_counter() - t0
+    W.rho = rho_test
+    out["learned"] = timed(pic.SOLVER_LEARNED)
+    out["learned"]["training"] = {"pair_solves": 4, "steps": train_steps, "seconds": train_s,
+                                  "loss_first10": loss_first, "loss_rest": loss_last}
+    out["speedup_vs_pcg"] = out["pcg"]["seconds"] / out["learned"]["seconds"]
+    out["speedup_vs_rbsor"] = out["rbsor"]["seconds"] / out["learned"]["seconds"]
     W.close()
     return out
 

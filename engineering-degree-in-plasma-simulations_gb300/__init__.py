@@ -15,7 +15,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "lib", "libpic_gb300.so")
 
 PIC_OK, PIC_ERR_ARG, PIC_ERR_CUDA, PIC_ERR_NOT_CONVERGED, PIC_ERR_CAPACITY, PIC_ERR_DEVICE = range(6)
-SOLVER_RBSOR, SOLVER_PCG = 0, 1
+SOLVER_RBSOR, SOLVER_PCG, SOLVER_LEARNED = 0, 1, 2
 GS, PCG = SOLVER_RBSOR, SOLVER_PCG  # reference SolverType names (PotentialSolver.h:24)
 
 # ch4/v3/src/all.h:16-25
@@ -100,6 +100,14 @@ def library():
         "pic_launch_count": [vp, vp],
         "pic_world_stream": [vp, pvp],
         "pic_number_density_noalloc": [i, i, i, vp, vp, vp, vp, vp, l, d, vp, vp],
+        "pic_learned_levels": [vp, vp, vp, vp],
+        "pic_learned_reset": [vp],
+        "pic_learned_weights": [vp, vp, l, vp],
+        "pic_learned_set_weights": [vp, vp, l],
+        "pic_learned_apply": [vp, vp, vp],
+        "pic_learned_loss_grad": [vp, vp, vp, vp, vp],
+        "pic_learned_collect": [vp, i],
+        "pic_learned_train": [vp, i, d, i, vp],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -418,6 +426,57 @@ class PotentialSolver:
         a, b, c = C.c_long(), C.c_long(), C.c_long()
         _check(self.world._L.pic_solver_stats(self.world._h, C.byref(a), C.byref(b), C.byref(c)))
         return dict(solves=a.value, refinements=b.value, inner=c.value)
+
+
+class LearnedPreconditioner:
+    """The world's learned multilevel Poisson preconditioner (used by SOLVER_LEARNED)."""
+
+    def __init__(self, world):
+        self.world = world
+
+    def levels(self):
+        n = C.c_int()
+        dims = np.zeros(36, np.int32)
+        diag = np.zeros(12)
+        _check(self.world._L.pic_learned_levels(self.world._h, C.byref(n), _p(dims), _p(diag)))
+        return [tuple(dims[3 * k:3 * k + 3]) for k in range(n.value)], diag[:n.value].copy()
+
+    def reset(self):
+        _check(self.world._L.pic_learned_reset(self.world._h))
+
+    def weights(self):
+        n = C.c_long()
+        _check(self.world._L.pic_learned_weights(self.world._h, None, 0, C.byref(n)))
+        out = np.zeros(n.value, np.float32)
+        _check(self.world._L.pic_learned_weights(self.world._h, _p(out), n.value, C.byref(n)))
+        return out
+
+    def set_weights(self, w):
+        w = np.ascontiguousarray(w, np.float32)
+        _check(self.world._L.pic_learned_set_weights(self.world._h, _p(w), w.size))
+
+    def loss_grad(self, r, x):
+        """Energy-norm loss of the pair (r, x) and its gradient (parameter layout), no update."""
+        r, x = _f64(r).ravel(), _f64(x).ravel()
+        loss = C.c_double()
+        g = np.zeros(self.weights().size, np.float32)
+        _check(self.world._L.pic_learned_loss_grad(self.world._h, _p(r), _p(x), C.byref(loss), _p(g)))
+        return loss.value, g
+
+    def collect(self, on=True):
+        _check(self.world._L.pic_learned_collect(self.world._h, int(on)))
+
+    def train(self, steps, lr=3e-4, pair_every=2):
+        loss = C.c_double()
+        _check(self.world._L.pic_learned_train(self.world._h, int(steps), float(lr), int(pair_every), C.byref(loss)))
+        return loss.value
+
+    def apply(self, r):
+        """z = B r over all nodes (r read on FREE nodes; z zero elsewhere)."""
+        r = _f64(r).ravel()
+        z = np.zeros_like(r)
+        _check(self.world._L.pic_learned_apply(self.world._h, _p(r), _p(z)))
+        return z
 
 
 class MC_MEX_Ionization:

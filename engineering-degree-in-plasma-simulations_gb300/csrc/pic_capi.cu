@@ -13,6 +13,7 @@
 #include <vector>
 #include "../../include/pic_gb300.h"
 #include "pic_kernels.h"
+#include "pic_learned.h"
 
 using namespace pic;
 
@@ -109,6 +110,9 @@ struct pic_world {
     int max_it = 10000;
     double omega = 1.4;
     long n_solves = 0, n_refine = 0, n_inner = 0;
+    LpState* lp = nullptr;  // learned preconditioner, created on first use
+    int lp_collect = 0;     // store (first residual, total correction) of each solve as a training pair
+    uint64_t lp_seed = 0x1ea2d5eedull;
     // collisions
     bool mcc_on = false;
     int mcc_e = -1, mcc_i = -1;
@@ -314,6 +318,83 @@ void fill_grid_boxes(pic_world* w) {
     for (int d = 0; d < 3; d++) g.periodic[d] = w->periodic[d];
 }
 
+void free_lp(pic_world* w) {
+    if (!w->lp) return;
+    LpState* L = w->lp;
+    for (int l = 1; l < kLpMaxLevels; l++) {
+        if (L->z[l]) cudaFree(L->z[l]);
+        if (L->e[l]) cudaFree(L->e[l]);
+    }
+    if (L->W) cudaFree(L->W);
+    if (L->fold) cudaFree(L->fold);
+    lp_free_train(*L);
+    delete L;
+    w->lp = nullptr;
+}
+
+// the learned preconditioner of the world's current grid and periodic axes (created on first use,
+// weights at their multilevel-diagonal start)
+int ensure_lp(pic_world* w) {
+    const GridDev& g = w->g;
+    if (w->lp && w->lp->per[0] == w->periodic[0] && w->lp->per[1] == w->periodic[1] &&
+        w->lp->per[2] == w->periodic[2])
+        return PIC_OK;
+    free_lp(w);
+    int n0[3] = {g.ni - w->periodic[0], g.nj - w->periodic[1], g.nk - w->periodic[2]};
+    if (std::min(n0[0], std::min(n0[1], n0[2])) < 2)
+        return fail(PIC_ERR_ARG, "the learned preconditioner needs at least 2 distinct nodes per axis");
+    LpState* L = new LpState();
+    w->lp = L;
+    for (int d = 0; d < 3; d++) {
+        L->per[d] = w->periodic[d];
+        L->dims[0][d] = n0[d];
+    }
+    L->nlev = 1;
+    while (L->nlev < kLpMaxLevels) {
+        int nx[3];
+        for (int d = 0; d < 3; d++) nx[d] = (L->dims[L->nlev - 1][d] + 1) / 2;
+        if (std::min(nx[0], std::min(nx[1], nx[2])) < 2) break;
+        if (nx[0] == L->dims[L->nlev - 1][0] && nx[1] == L->dims[L->nlev - 1][1] && nx[2] == L->dims[L->nlev - 1][2])
+            break;
+        for (int d = 0; d < 3; d++) L->dims[L->nlev][d] = nx[d];
+        L->nlev++;
+    }
+    for (int l = 1; l < L->nlev; l++) {
+        size_t nvox = (size_t)L->dims[l][0] * L->dims[l][1] * L->dims[l][2];
+        CU(cudaMalloc(&L->z[l], sizeof(float) * nvox));
+        CU(cudaMalloc(&L->e[l], sizeof(float) * nvox));
+    }
+    double c[3] = {1.0 / (g.dxd[0] * g.dxd[0]), 1.0 / (g.dxd[1] * g.dxd[1]), 1.0 / (g.dxd[2] * g.dxd[2])};
+    lp_galerkin_diag(c, L->nlev, L->diag);
+    lp_layout(L->lay);
+    CU(cudaMalloc(&L->W, sizeof(float) * L->lay.total));
+    CU(cudaMalloc(&L->fold, sizeof(float) * kLpFold * kLpNetLevels));
+    std::vector<float> hw(L->lay.total);
+    lp_init_weights(L->lay, L->diag, L->nlev, hw.data());
+    CU(cudaMemcpyAsync(L->W, hw.data(), sizeof(float) * hw.size(), cudaMemcpyHostToDevice, w->stream));
+    launch_lp_fold(*L, w->stream);
+    CU(cudaStreamSynchronize(w->stream));
+    CU(cudaGetLastError());
+    return PIC_OK;
+}
+
+int ensure_lp_train(pic_world* w) {
+    int rc = ensure_lp(w);
+    if (rc) return rc;
+    if (w->lp->train) return PIC_OK;
+    std::vector<float> hw(w->lp->lay.total);
+    CU(cudaMemcpyAsync(hw.data(), w->lp->W, sizeof(float) * hw.size(), cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    if (lp_alloc_train(w->g, *w->lp, hw.data())) {
+        cudaGetLastError();
+        free_lp(w);
+        return fail(PIC_ERR_CUDA, "device allocation failed for the preconditioner training state");
+    }
+    launch_lp_prep(*w->lp, w->stream);
+    CU(cudaStreamSynchronize(w->stream));
+    return PIC_OK;
+}
+
 SolveWork solve_work(pic_world* w) {
     SolveWork s;
     s.phi = w->phi;
@@ -416,6 +497,7 @@ extern "C" int pic_world_destroy(pic_world* w) {
     if (!w) return PIC_OK;
     cudaSetDevice(w->device);
     if (w->stream) cudaStreamSynchronize(w->stream);
+    free_lp(w);
     for (auto& s : w->sp) {
         cudaFree(s.dev.pos);
         cudaFree(s.dev.vel);
@@ -972,8 +1054,14 @@ extern "C" int pic_species_sums(pic_world* w, int sp, double* out) {
 // Poisson
 // =====================================================================================
 extern "C" int pic_solver_configure(pic_world* w, int method, double tol_rel, int max_it, double omega) {
-    if (!w || (method != PIC_SOLVER_RBSOR && method != PIC_SOLVER_PCG) || !(tol_rel > 0) || max_it <= 0)
+    if (!w || (method != PIC_SOLVER_RBSOR && method != PIC_SOLVER_PCG && method != PIC_SOLVER_LEARNED) ||
+        !(tol_rel > 0) || max_it <= 0)
         return fail(PIC_ERR_ARG, "bad solver configuration");
+    if (method == PIC_SOLVER_LEARNED) {
+        CU(cudaSetDevice(w->device));
+        int rc = ensure_lp(w);
+        if (rc) return rc;
+    }
     w->method = method;
     w->tol = tol_rel;
     w->max_it = max_it;
@@ -999,11 +1087,19 @@ int residual_norms(pic_world* w, SolveWork& sw, int apply_e, double& r2, double&
     return PIC_OK;
 }
 
+int ensure_lp_train(pic_world* w);
+
 int solve_impl(pic_world* w, int* iters_out, double* rel_out) {
     SolveWork sw = solve_work(w);
     double r2, b2;
     int rc = residual_norms(w, sw, 0, r2, b2);
     if (rc) return rc;
+    const bool collect = w->lp_collect && w->method != PIC_SOLVER_RBSOR;
+    if (collect) {
+        rc = ensure_lp_train(w);
+        if (rc) return rc;
+        if (lp_pair_begin(*w->lp, w->r, w->g.nv, w->stream)) return fail(PIC_ERR_CUDA, "training pair allocation");
+    }
     double bn = b2 > 0 ? std::sqrt(b2) : 1.0;
     double rel = std::sqrt(r2) / bn;
     int iters = 0, outer = 0;
@@ -1018,6 +1114,38 @@ int solve_impl(pic_world* w, int* iters_out, double* rel_out) {
                 launch_rbsor_sweeps(w->g, sw, (float)w->omega, sweeps, w->stream, grid);
             }
             iters += sweeps;
+        } else if (w->method == PIC_SOLVER_LEARNED) {
+            // inner FP32 flexible CG with the learned multilevel preconditioner, to eta = 1e-3 of
+            // the current residual (or the final target)
+            int lrc = ensure_lp(w);
+            if (lrc) return lrc;
+            double target = std::max(1e-6 * r2, 0.09 * w->tol * w->tol * b2);
+            {
+                Scope sc(w, "poisson", 4 + 2 * w->lp->nlev);
+                launch_lpcg_init(w->g, sw, *w->lp, w->stream, grid, w->sms);
+            }
+            float* din = w->d;
+            float* dout = w->d2;
+            int it = 0;
+            for (;;) {
+                int batch = std::min(4, w->max_it - iters);
+                if (batch <= 0) break;
+                {
+                    Scope sc(w, "poisson", (1 + 2 * w->lp->nlev) * batch);
+                    for (int b = 0; b < batch; b++) {
+                        launch_lpcg_iter(w->g, sw, *w->lp, din, dout, it, target, w->stream, grid, w->sms);
+                        std::swap(din, dout);
+                        it++;
+                    }
+                }
+                CU(cudaMemcpyAsync(w->h_flag, w->flag, 2 * sizeof(int), cudaMemcpyDeviceToHost, w->stream));
+                CU(cudaStreamSynchronize(w->stream));
+                if (w->h_flag[0]) {
+                    iters += w->h_flag[1] - (it - batch);  // the batch stopped at iteration flag[1]
+                    break;
+                }
+                iters += batch;
+            }
         } else {
             // inner FP32 flexible PCG to eta = 1e-3 of the current residual (or the final target)
             double target = std::max(1e-6 * r2, 0.09 * w->tol * w->tol * b2);
@@ -1039,12 +1167,16 @@ int solve_impl(pic_world* w, int* iters_out, double* rel_out) {
                         it++;
                     }
                 }
-                iters += batch;
-                CU(cudaMemcpyAsync(w->h_flag, w->flag, sizeof(int), cudaMemcpyDeviceToHost, w->stream));
+                CU(cudaMemcpyAsync(w->h_flag, w->flag, 2 * sizeof(int), cudaMemcpyDeviceToHost, w->stream));
                 CU(cudaStreamSynchronize(w->stream));
-                if (w->h_flag[0]) break;
+                if (w->h_flag[0]) {
+                    iters += w->h_flag[1] - (it - batch);  // the batch stopped at iteration flag[1]
+                    break;
+                }
+                iters += batch;
             }
         }
+        if (collect) lp_pair_add(*w->lp, w->e, w->g.nv, w->stream, grid);
         rc = residual_norms(w, sw, 1, r2, b2);
         if (rc) return rc;
         rel = std::sqrt(r2) / bn;
@@ -1054,6 +1186,7 @@ int solve_impl(pic_world* w, int* iters_out, double* rel_out) {
         Scope sc(w, "poisson", 2);
         launch_fill_aux(w->g, w->phi, reinterpret_cast<const uint8_t*>(w->kind), w->stream, grid);
     }
+    if (collect) lp_pair_end(*w->lp);
     if (iters_out) *iters_out = iters;
     if (rel_out) *rel_out = rel;
     w->n_solves++;
@@ -1077,6 +1210,162 @@ extern "C" int pic_solver_stats(pic_world* w, long* solves, long* refinements, l
     if (refinements) *refinements = w->n_refine;
     if (inner) *inner = w->n_inner;
     return PIC_OK;
+}
+
+// ---- learned preconditioner -------------------------------------------------------------
+extern "C" int pic_learned_levels(pic_world* w, int* nlev, int* dims, double* diag) {
+    if (!w) return fail(PIC_ERR_ARG, "null world");
+    CU(cudaSetDevice(w->device));
+    int rc = ensure_lp(w);
+    if (rc) return rc;
+    const LpState& L = *w->lp;
+    if (nlev) *nlev = L.nlev;
+    for (int l = 0; l < L.nlev; l++) {
+        if (dims)
+            for (int d = 0; d < 3; d++) dims[3 * l + d] = L.dims[l][d];
+        if (diag) diag[l] = L.diag[l];
+    }
+    return PIC_OK;
+}
+extern "C" int pic_learned_reset(pic_world* w) {
+    if (!w) return fail(PIC_ERR_ARG, "null world");
+    CU(cudaSetDevice(w->device));
+    free_lp(w);
+    return ensure_lp(w);
+}
+extern "C" int pic_learned_weights(pic_world* w, float* out, long capacity, long* count) {
+    if (!w) return fail(PIC_ERR_ARG, "null world");
+    CU(cudaSetDevice(w->device));
+    int rc = ensure_lp(w);
+    if (rc) return rc;
+    const LpState& L = *w->lp;
+    if (count) *count = L.lay.total;
+    if (!out) return PIC_OK;
+    if (capacity < L.lay.total) return fail(PIC_ERR_ARG, "capacity %ld < %d parameters", capacity, L.lay.total);
+    CU(cudaMemcpyAsync(out, L.W, sizeof(float) * L.lay.total, cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    return PIC_OK;
+}
+extern "C" int pic_learned_set_weights(pic_world* w, const float* in, long count) {
+    if (!w || !in) return fail(PIC_ERR_ARG, "null argument");
+    CU(cudaSetDevice(w->device));
+    int rc = ensure_lp(w);
+    if (rc) return rc;
+    LpState& L = *w->lp;
+    if (count != L.lay.total) return fail(PIC_ERR_ARG, "expected %d parameters, got %ld", L.lay.total, count);
+    CU(cudaMemcpyAsync(L.W, in, sizeof(float) * count, cudaMemcpyHostToDevice, w->stream));
+    launch_lp_fold(L, w->stream);
+    CU(cudaStreamSynchronize(w->stream));
+    CU(cudaGetLastError());
+    return PIC_OK;
+}
+extern "C" int pic_learned_apply(pic_world* w, const double* r, double* z) {
+    if (!w || !r || !z) return fail(PIC_ERR_ARG, "null argument");
+    CU(cudaSetDevice(w->device));
+    int rc = ensure_lp(w);
+    if (rc) return rc;
+    const GridDev& g = w->g;
+    std::vector<uint16_t> kind(g.nv);
+    CU(cudaMemcpyAsync(kind.data(), w->kind, sizeof(uint16_t) * g.nv, cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    std::vector<float> rf(g.nv);
+    for (int n = 0; n < g.nv; n++) rf[n] = (kind[n] & 3) == kFree ? (float)r[n] : 0.f;
+    CU(cudaMemcpyAsync(w->r, rf.data(), sizeof(float) * g.nv, cudaMemcpyHostToDevice, w->stream));
+    launch_lp_apply(g, *w->lp, w->r, w->z, w->kind, nullptr, nullptr, nullptr, w->stream, w->grid_nodes, w->sms);
+    CU(cudaGetLastError());
+    CU(cudaMemcpyAsync(rf.data(), w->z, sizeof(float) * g.nv, cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    for (int n = 0; n < g.nv; n++) z[n] = rf[n];
+    return PIC_OK;
+}
+
+extern "C" int pic_learned_collect(pic_world* w, int on) {
+    if (!w) return fail(PIC_ERR_ARG, "null world");
+    CU(cudaSetDevice(w->device));
+    if (on) {
+        int rc = ensure_lp_train(w);
+        if (rc) return rc;
+    }
+    w->lp_collect = on != 0;
+    return PIC_OK;
+}
+namespace {
+int lp_check_err(pic_world* w) {
+    unsigned h = 0;
+    CU(cudaMemcpyAsync(&h, lp_train_err(*w->lp), sizeof(unsigned), cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    if (h) {
+        CU(cudaMemsetAsync(lp_train_err(*w->lp), 0, sizeof(unsigned), w->stream));
+        return fail(PIC_ERR_DEVICE, "a tensor-core wait of the preconditioner training ran out (flags 0x%x)", h);
+    }
+    return PIC_OK;
+}
+}  // namespace
+extern "C" int pic_learned_loss_grad(pic_world* w, const double* r, const double* x, double* loss, float* grad) {
+    if (!w || !r || !x) return fail(PIC_ERR_ARG, "null argument");
+    CU(cudaSetDevice(w->device));
+    int rc = ensure_lp_train(w);
+    if (rc) return rc;
+    const GridDev& g = w->g;
+    std::vector<uint16_t> kind(g.nv);
+    CU(cudaMemcpyAsync(kind.data(), w->kind, sizeof(uint16_t) * g.nv, cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    std::vector<float> rf(g.nv), xf(g.nv);
+    for (int n = 0; n < g.nv; n++) {
+        bool f = (kind[n] & 3) == kFree;
+        rf[n] = f ? (float)r[n] : 0.f;
+        xf[n] = f ? (float)x[n] : 0.f;
+    }
+    LpState& L = *w->lp;
+    CU(cudaMemcpyAsync(lp_train_r(L), rf.data(), sizeof(float) * g.nv, cudaMemcpyHostToDevice, w->stream));
+    CU(cudaMemcpyAsync(lp_train_x(L), xf.data(), sizeof(float) * g.nv, cudaMemcpyHostToDevice, w->stream));
+    {
+        Scope sc(w, "learned_train", 1);
+        launch_lp_loss_grad(g, L, w->kind, lp_train_r(L), lp_train_x(L), w->stream, w->grid_nodes, w->sms);
+    }
+    CU(cudaGetLastError());
+    double h = 0;
+    CU(cudaMemcpyAsync(&h, lp_train_red(L), sizeof(double), cudaMemcpyDeviceToHost, w->stream));
+    if (grad) CU(cudaMemcpyAsync(grad, lp_train_grad(L), sizeof(float) * L.lay.total, cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    if (loss) *loss = h;
+    return lp_check_err(w);
+}
+// steps of Adam on the energy-norm loss; each step uses a stored solve pair when one exists and
+// (step % pair_every == 0), else a white-noise pair x ~ N(0, 1) on FREE nodes with r = L x
+extern "C" int pic_learned_train(pic_world* w, int steps, double lr, int pair_every, double* mean_loss) {
+    if (!w || steps < 0 || !(lr > 0)) return fail(PIC_ERR_ARG, "bad training arguments");
+    CU(cudaSetDevice(w->device));
+    int rc = ensure_lp_train(w);
+    if (rc) return rc;
+    LpState& L = *w->lp;
+    const GridDev& g = w->g;
+    double sum = 0;
+    int np = lp_npairs(L), used_pairs = 0;
+    for (int st = 0; st < steps; st++) {
+        const float *r, *x;
+        if (np > 0 && pair_every > 0 && st % pair_every == 0) {
+            int k = used_pairs++ % np;
+            r = lp_pair_r(L, k);
+            x = lp_pair_x(L, k);
+        } else {
+            launch_lp_noise_pair(g, L, w->kind, w->lp_seed, w->stream, w->grid_nodes);
+            r = lp_train_r(L);
+            x = lp_train_x(L);
+        }
+        {
+            Scope sc(w, "learned_train", 1);
+            launch_lp_loss_grad(g, L, w->kind, r, x, w->stream, w->grid_nodes, w->sms);
+            launch_lp_adam(L, (float)lr, w->stream);
+        }
+        double h = 0;
+        CU(cudaMemcpyAsync(&h, lp_train_red(L), sizeof(double), cudaMemcpyDeviceToHost, w->stream));
+        CU(cudaStreamSynchronize(w->stream));
+        sum += h;
+    }
+    CU(cudaGetLastError());
+    if (mean_loss) *mean_loss = steps ? sum / steps : 0.0;
+    return lp_check_err(w);
 }
 
 extern "C" int pic_solver_compute_ef(pic_world* w) {

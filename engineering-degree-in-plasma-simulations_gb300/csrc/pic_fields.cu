@@ -14,44 +14,9 @@
 //   (L x)_p = D_p x_p - sum_{q FREE or FIXED} c_q x_q,   D_p = sum_{q not MIRROR} c_q,  c = 1/dx^2.
 // kind[n] (uint16): bits 0-1 node kind, bits 2-7 "neighbour d is MIRROR", bits 8-13
 // "neighbour d is FIXED"; direction order -x +x -y +y -z +z.
-#include "pic_kernels.h"
+#include "pic_stencil.cuh"
 
 namespace pic {
-
-constexpr double kEps0 = 8.85418782e-12;  // ch4/v3/src/all.h:16
-
-__device__ __forceinline__ void node_ijk(const GridDev& g, int n, int& i, int& j, int& k) {
-    unsigned t = fdiv((unsigned)n, g.fd_ni);
-    i = n - (int)t * g.ni;
-    unsigned kk = fdiv(t, g.fd_nj);
-    j = (int)t - (int)kk * g.nj;
-    k = (int)kk;
-}
-// neighbour index along an axis with periodic wrap (the copy at n-1 folds onto 0)
-__device__ __forceinline__ int wrap_m(int c, int n, int per) { return (per && c == 0) ? n - 2 : c - 1; }
-__device__ __forceinline__ int wrap_p(int c, int n, int per) { return (per && c + 1 >= n - 1) ? 0 : c + 1; }
-
-struct Stencil {
-    int q[6];
-    float c[6];
-};
-__device__ __forceinline__ void stencil(const GridDev& g, int i, int j, int k, Stencil& s) {
-    int nij = g.ni * g.nj;
-    int im = wrap_m(i, g.ni, g.periodic[0]), ip = wrap_p(i, g.ni, g.periodic[0]);
-    int jm = wrap_m(j, g.nj, g.periodic[1]), jp = wrap_p(j, g.nj, g.periodic[1]);
-    int km = wrap_m(k, g.nk, g.periodic[2]), kp = wrap_p(k, g.nk, g.periodic[2]);
-    int row = k * nij + j * g.ni;
-    s.q[0] = row + im;
-    s.q[1] = row + ip;
-    s.q[2] = k * nij + jm * g.ni + i;
-    s.q[3] = k * nij + jp * g.ni + i;
-    s.q[4] = km * nij + j * g.ni + i;
-    s.q[5] = kp * nij + j * g.ni + i;
-    float cx = g.inv_dx[0] * g.inv_dx[0], cy = g.inv_dx[1] * g.inv_dx[1], cz = g.inv_dx[2] * g.inv_dx[2];
-    s.c[0] = s.c[1] = cx;
-    s.c[2] = s.c[3] = cy;
-    s.c[4] = s.c[5] = cz;
-}
 
 // ------------------------------------------------------------------------------------
 // charge density: fixed-point number density -> den_s (per species) and rho
@@ -165,40 +130,6 @@ __global__ void k_efield(GridDev g, const double* __restrict__ phi, float4* __re
 }
 void launch_efield(const GridDev& g, const double* phi, float4* ef, cudaStream_t s, int grid) {
     k_efield<<<grid, 256, 0, s>>>(g, phi, ef);
-}
-
-// ------------------------------------------------------------------------------------
-// block reduction of up to four doubles into per-block partial slots
-// ------------------------------------------------------------------------------------
-template <int N>
-__device__ __forceinline__ void block_partials(double (&v)[N], double* part, int nslots_stride) {
-    __shared__ double s[N][8];
-#pragma unroll
-    for (int c = 0; c < N; c++) {
-        double x = v[c];
-        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-        if ((threadIdx.x & 31) == 0) s[c][threadIdx.x >> 5] = x;
-    }
-    __syncthreads();
-    if (threadIdx.x < N) {
-        double x = 0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++) x += s[threadIdx.x][w];
-        part[threadIdx.x * nslots_stride + blockIdx.x] = x;
-    }
-    __syncthreads();
-}
-// every block sums the same partials in the same order: identical scalars everywhere
-__device__ __forceinline__ double sum_partials(const double* part, int nblocks) {
-    __shared__ double s[8];
-    double x = 0;
-    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) x += part[b];
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = x;
-    __syncthreads();
-    double t = 0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += s[w];
-    __syncthreads();
-    return t;
 }
 
 // ------------------------------------------------------------------------------------
@@ -360,13 +291,6 @@ void launch_rbsor_sweeps(const GridDev& g, SolveWork& w, float omega, int sweeps
 //   K2: alpha = rz/dq ; e += alpha d' ; r -= alpha q ; z' = r/D ; partials r.z', r.z, r.r
 // scalars: scal[0..1] rz (double-buffered by iteration parity); flag[0] set when r.r <= target
 // ------------------------------------------------------------------------------------
-__device__ __forceinline__ float diag_of(uint16_t kd, const Stencil& s) {
-    float dg = 0.f;
-#pragma unroll
-    for (int d = 0; d < 6; d++)
-        if (!(kd & (1u << (2 + d)))) dg += s.c[d];
-    return dg;
-}
 __global__ void k_pcg_init(GridDev g, const float* __restrict__ r, float* __restrict__ z, float* __restrict__ e,
                            const uint16_t* __restrict__ kind, double* part, int* flag) {
     double acc[1] = {0.0};
@@ -400,7 +324,10 @@ __global__ void k_pcg_k1(GridDev g, const float* __restrict__ z, const float* __
         double rzo = sum_partials(part + 2 * kParts, gridDim.x);
         double rr = sum_partials(part + 3 * kParts, gridDim.x);
         if (rr <= target_rr || flag[0]) {
-            if (blockIdx.x == 0 && threadIdx.x == 0) flag[0] = 1;
+            if (blockIdx.x == 0 && threadIdx.x == 0 && !flag[0]) {
+                flag[1] = it;  // iterations completed
+                flag[0] = 1;
+            }
             return;
         }
         double rz_old = scal[(it - 1) & 1];

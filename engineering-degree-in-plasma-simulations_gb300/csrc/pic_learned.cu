@@ -1,10 +1,16 @@
-// Learned Poisson preconditioner: tensor-core (tcgen05) kernels.
+// Learned multilevel Poisson preconditioner: inference, training and the flexible CG that
+// uses it, plus a one-tile tcgen05 GEMM check of the tensor-core operand layout.
 //
-// This translation unit holds the tcgen05 GEMM tile used by the preconditioner network's
-// channel-mixing convolutions, and a check entry point that multiplies one tile so the
-// operand layout can be verified against a host GEMM.
+// Level transfers are cell-centred trilinear: along one axis the fine point f receives
+// 3/4 of coarse point f/2 and 1/4 of its neighbour on the side of f (f even: f/2 - 1, f odd:
+// f/2 + 1); restriction is the exact transpose.  Periodic axes wrap at every level (over
+// the level's own extent), other axes read zero outside the box.
+#include <algorithm>
+#include <cmath>
+#include <vector>
 #include <cuda_bf16.h>
-#include "pic_kernels.h"
+#include "pic_learned.h"
+#include "pic_stencil.cuh"
 #include "pic_tc.cuh"
 
 namespace pic {
@@ -66,6 +72,1078 @@ __global__ void __launch_bounds__(128) k_tc_gemm_tile(const __nv_bfloat16* __res
     tc_fence_before();
     __syncthreads();
     if (warp == 0) tc_dealloc(tm, ncols);
+}
+
+
+// =====================================================================================
+// level views and transfers
+// =====================================================================================
+LView lp_view(float* a, const int n[3], int sy, int sz, const int per[3]) {
+    LView v;
+    v.a = a;
+    for (int d = 0; d < 3; d++) {
+        v.n[d] = n[d];
+        v.per[d] = per[d];
+    }
+    v.sy = sy;
+    v.sz = sz;
+    v.fx = make_fastdiv((unsigned)n[0]);
+    v.fxy = make_fastdiv((unsigned)(n[0] * n[1]));
+    v.nvox = n[0] * n[1] * n[2];
+    return v;
+}
+LView lp_level_view(const LpState& L, int l, float* a) {
+    return lp_view(a, L.dims[l], L.dims[l][0], L.dims[l][0] * L.dims[l][1], L.per);
+}
+LView lp_node_view(const GridDev& g, const LpState& L, float* a) {
+    return lp_view(a, L.dims[0], g.ni, g.ni * g.nj, L.per);
+}
+
+__device__ __forceinline__ void lv_decode(const LView& v, unsigned idx, int& x, int& y, int& z) {
+    unsigned t = fdiv(idx, v.fx);
+    x = (int)(idx - t * (unsigned)v.n[0]);
+    unsigned zz = fdiv(idx, v.fxy);
+    z = (int)zz;
+    y = (int)(t - zz * (unsigned)v.n[1]);
+}
+__device__ __forceinline__ int lv_off(const LView& v, int x, int y, int z) { return x + y * v.sy + z * v.sz; }
+// coordinate c + d along an axis of extent n (|d| <= 2, n >= 2): wrapped, or -1 outside
+__device__ __forceinline__ int lv_nb(int c, int d, int n, int per) {
+    int u = c + d;
+    if (per) return u < 0 ? u + n : (u >= n ? u - n : u);
+    return (u < 0 || u >= n) ? -1 : u;
+}
+
+// z_coarse = R z_fine
+__global__ void k_lp_restrict(LView f, LView c, const int* flag) {
+    if (flag && flag[0]) return;
+    for (unsigned idx = blockIdx.x * blockDim.x + threadIdx.x; idx < (unsigned)c.nvox; idx += gridDim.x * blockDim.x) {
+        int cc[3];
+        lv_decode(c, idx, cc[0], cc[1], cc[2]);
+        int fi[3][4];
+#pragma unroll
+        for (int ax = 0; ax < 3; ax++) {
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                int raw = 2 * cc[ax] + k - 1;
+                int nc2 = 2 * c.n[ax];
+                if (f.per[ax]) {
+                    raw = raw < 0 ? raw + nc2 : (raw >= nc2 ? raw - nc2 : raw);
+                    fi[ax][k] = raw < f.n[ax] ? raw : -1;
+                } else {
+                    fi[ax][k] = (raw >= 0 && raw < f.n[ax]) ? raw : -1;
+                }
+            }
+        }
+        const float w4[4] = {0.25f, 0.75f, 0.75f, 0.25f};
+        float acc = 0.f;
+#pragma unroll
+        for (int kz = 0; kz < 4; kz++) {
+            if (fi[2][kz] < 0) continue;
+            float az = 0.f;
+#pragma unroll
+            for (int ky = 0; ky < 4; ky++) {
+                if (fi[1][ky] < 0) continue;
+                const float* row = f.a + fi[1][ky] * f.sy + fi[2][kz] * f.sz;
+                float ay = 0.f;
+#pragma unroll
+                for (int kx = 0; kx < 4; kx++)
+                    if (fi[0][kx] >= 0) ay += w4[kx] * row[fi[0][kx]];
+                az += w4[ky] * ay;
+            }
+            acc += w4[kz] * az;
+        }
+        c.a[lv_off(c, cc[0], cc[1], cc[2])] = acc;
+    }
+}
+
+// sum_c P(f, c) e_coarse[c] at fine point f
+__device__ __forceinline__ float lp_prolong_at(const LView& cv, const int f[3]) {
+    int ci[3][2];
+#pragma unroll
+    for (int ax = 0; ax < 3; ax++) {
+        int c0 = f[ax] >> 1;
+        ci[ax][0] = c0;
+        ci[ax][1] = lv_nb(c0, (f[ax] & 1) ? 1 : -1, cv.n[ax], cv.per[ax]);
+    }
+    const float w2[2] = {0.75f, 0.25f};
+    float acc = 0.f;
+#pragma unroll
+    for (int kz = 0; kz < 2; kz++) {
+        if (ci[2][kz] < 0) continue;
+        float az = 0.f;
+#pragma unroll
+        for (int ky = 0; ky < 2; ky++) {
+            if (ci[1][ky] < 0) continue;
+            const float* row = cv.a + ci[1][ky] * cv.sy + ci[2][kz] * cv.sz;
+            float ay = 0.f;
+#pragma unroll
+            for (int kx = 0; kx < 2; kx++)
+                if (ci[0][kx] >= 0) ay += w2[kx] * row[ci[0][kx]];
+            az += w2[ky] * ay;
+        }
+        acc += w2[kz] * az;
+    }
+    return acc;
+}
+
+// 3x3x3 stencil (taps t = 9(dz+1) + 3(dy+1) + (dx+1)) at point c
+__device__ __forceinline__ float lp_stencil27(const LView& v, const float* __restrict__ S, const int c[3]) {
+    float acc = 0.f;
+#pragma unroll
+    for (int dz = -1; dz <= 1; dz++) {
+        int z = lv_nb(c[2], dz, v.n[2], v.per[2]);
+        if (z < 0) continue;
+#pragma unroll
+        for (int dy = -1; dy <= 1; dy++) {
+            int y = lv_nb(c[1], dy, v.n[1], v.per[1]);
+            if (y < 0) continue;
+            const float* row = v.a + y * v.sy + z * v.sz;
+#pragma unroll
+            for (int dx = -1; dx <= 1; dx++) {
+                int x = lv_nb(c[0], dx, v.n[0], v.per[0]);
+                if (x >= 0) acc += __ldg(&S[9 * (dz + 1) + 3 * (dy + 1) + dx + 1]) * row[x];
+            }
+        }
+    }
+    return acc;
+}
+
+// folded network level: away from non-periodic faces the 5x5x5 stencil K5; on a face point the
+// exact form sum_{t: c + o_t inside} sum_t' K27[t][t'] z[c + o_t + o_t'] (the network reads its
+// intermediate channels as zero outside the box)
+__device__ float lp_net_op(const LView& v, const float* __restrict__ fold, const int c[3]) {
+    bool interior = true;
+#pragma unroll
+    for (int ax = 0; ax < 3; ax++)
+        if (!v.per[ax] && (c[ax] == 0 || c[ax] == v.n[ax] - 1)) interior = false;
+    float acc = 0.f;
+    if (interior) {
+        const float* K5 = fold + 729;
+        for (int dz = -2; dz <= 2; dz++) {
+            int z = lv_nb(c[2], dz, v.n[2], v.per[2]);
+            if (z < 0) continue;
+            for (int dy = -2; dy <= 2; dy++) {
+                int y = lv_nb(c[1], dy, v.n[1], v.per[1]);
+                if (y < 0) continue;
+                const float* row = v.a + y * v.sy + z * v.sz;
+                const float* k = K5 + 25 * (dz + 2) + 5 * (dy + 2) + 2;
+#pragma unroll
+                for (int dx = -2; dx <= 2; dx++) {
+                    int x = lv_nb(c[0], dx, v.n[0], v.per[0]);
+                    if (x >= 0) acc += __ldg(&k[dx]) * row[x];
+                }
+            }
+        }
+        return acc;
+    }
+    for (int t = 0; t < 27; t++) {
+        int u[3] = {lv_nb(c[0], t % 3 - 1, v.n[0], v.per[0]), lv_nb(c[1], (t / 3) % 3 - 1, v.n[1], v.per[1]),
+                    lv_nb(c[2], t / 9 - 1, v.n[2], v.per[2])};
+        if (u[0] < 0 || u[1] < 0 || u[2] < 0) continue;
+        acc += lp_stencil27(v, fold + 27 * t, u);
+    }
+    return acc;
+}
+
+// e_l = op_l(z_l) + P e_{l+1}; mode 1: network level (fold), 2: diagonal scaling
+__global__ void k_lp_up(LView zin, LView cin, LView out, int mode, const float* __restrict__ fold, float inv_diag,
+                        const int* flag) {
+    if (flag && flag[0]) return;
+    for (unsigned idx = blockIdx.x * blockDim.x + threadIdx.x; idx < (unsigned)out.nvox;
+         idx += gridDim.x * blockDim.x) {
+        int c[3];
+        lv_decode(out, idx, c[0], c[1], c[2]);
+        float v = mode == 1 ? lp_net_op(zin, fold, c) : inv_diag * zin.a[lv_off(zin, c[0], c[1], c[2])];
+        if (cin.a) v += lp_prolong_at(cin, c);
+        out.a[lv_off(out, c[0], c[1], c[2])] = v;
+    }
+}
+
+// level 0 on the node array: z = mask * (S0 * r + P e_1); partials z.r (slot 1), z.q (slot 2)
+__global__ void k_lp_up0(GridDev g, LView rin, LView cin, float* __restrict__ z, const uint16_t* __restrict__ kind,
+                         const float* __restrict__ S0, const float* __restrict__ q, double* part, const int* flag) {
+    if (flag && flag[0]) return;
+    float f_zr = 0.f, f_zq = 0.f;
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
+        if ((kind[n] & 3) != kFree) {
+            z[n] = 0.f;
+            continue;
+        }
+        int c[3];
+        node_ijk(g, n, c[0], c[1], c[2]);
+        float v = lp_stencil27(rin, S0, c);
+        if (cin.a) v += lp_prolong_at(cin, c);
+        z[n] = v;
+        f_zr += v * rin.a[n];
+        if (q) f_zq += v * q[n];
+    }
+    if (part) {
+        double a1[1] = {f_zr}, a2[1] = {f_zq};
+        block_partials<1>(a1, part + 1 * kParts, kParts);
+        block_partials<1>(a2, part + 2 * kParts, kParts);
+    }
+}
+
+static int lp_blocks(int nvox, int sms) { return std::max(1, std::min((nvox + 255) / 256, sms * 8)); }
+
+void launch_lp_apply(const GridDev& g, const LpState& L, const float* r, float* z, const uint16_t* kind,
+                     const float* q, double* part, const int* flag, cudaStream_t s, int grid_nodes, int sms) {
+    LView r0 = lp_node_view(g, L, const_cast<float*>(r));
+    for (int l = 1; l < L.nlev; l++) {
+        LView f = l == 1 ? r0 : lp_level_view(L, l - 1, L.z[l - 1]);
+        LView c = lp_level_view(L, l, L.z[l]);
+        k_lp_restrict<<<lp_blocks(c.nvox, sms), 256, 0, s>>>(f, c, flag);
+    }
+    LView none{};
+    none.a = nullptr;
+    for (int l = L.nlev - 1; l >= 1; l--) {
+        LView zin = lp_level_view(L, l, L.z[l]);
+        LView cin = l + 1 < L.nlev ? lp_level_view(L, l + 1, L.e[l + 1]) : none;
+        LView out = lp_level_view(L, l, L.e[l]);
+        int mode = l <= kLpNetLevels ? 1 : 2;
+        const float* fold = mode == 1 ? L.fold + (l - 1) * kLpFold : nullptr;
+        k_lp_up<<<lp_blocks(out.nvox, sms), 256, 0, s>>>(zin, cin, out, mode, fold, (float)(1.0 / L.diag[l]), flag);
+    }
+    LView cin = L.nlev > 1 ? lp_level_view(L, 1, L.e[1]) : none;
+    k_lp_up0<<<grid_nodes, 256, 0, s>>>(g, r0, cin, z, kind, L.W + L.lay.s0, q, part, flag);
+}
+
+// folded stencils of every network level: M = Wm Wl (C x 27), K27[t][t'] = sum_c Wp[t][c] M[c][t'],
+// K5[d] = sum over t + t' = d of K27[t][t']
+__global__ void k_lp_fold(const float* __restrict__ W, LpLayout lay, float* fold) {
+    const int l = blockIdx.x + 1;
+    const int C = lp_channels(l);
+    __shared__ float M[64 * 27];
+    __shared__ float K[729];
+    const float* Wl = W + lay.wl[l];
+    const float* Wm = W + lay.wm[l];
+    const float* Wp = W + lay.wp[l];
+    for (int x = threadIdx.x; x < C * 27; x += blockDim.x) {
+        int c = x / 27, t = x % 27;
+        float a = 0.f;
+        for (int k = 0; k < C; k++) a += Wm[c * C + k] * Wl[k * 27 + t];
+        M[x] = a;
+    }
+    __syncthreads();
+    for (int x = threadIdx.x; x < 729; x += blockDim.x) {
+        int t = x / 27, tp = x % 27;
+        float a = 0.f;
+        for (int c = 0; c < C; c++) a += Wp[t * C + c] * M[c * 27 + tp];
+        K[x] = a;
+        fold[(l - 1) * kLpFold + x] = a;
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < 125; d += blockDim.x) {
+        int dx = d % 5 - 2, dy = (d / 5) % 5 - 2, dz = d / 25 - 2;
+        float a = 0.f;
+        for (int t = 0; t < 27; t++) {
+            int tx = t % 3 - 1, ty = (t / 3) % 3 - 1, tz = t / 9 - 1;
+            int ux = dx - tx, uy = dy - ty, uz = dz - tz;
+            if (ux < -1 || ux > 1 || uy < -1 || uy > 1 || uz < -1 || uz > 1) continue;
+            a += K[t * 27 + 9 * (uz + 1) + 3 * (uy + 1) + ux + 1];
+        }
+        fold[(l - 1) * kLpFold + 729 + d] = a;
+    }
+}
+void launch_lp_fold(const LpState& L, cudaStream_t s) {
+    int nnet = std::min(kLpNetLevels, L.nlev - 1);
+    if (nnet > 0) k_lp_fold<<<nnet, 256, 0, s>>>(L.W, L.lay, L.fold);
+}
+
+// =====================================================================================
+// flexible CG with the learned preconditioner, FP32 on the correction equation L e = r
+//   init : z = B r ; partials z.r
+//   K1   : beta = -alpha_prev (z.q_prev) / rz_prev (0 on the first iteration); d' = z + beta d ;
+//          q = L d' ; partial d'.q
+//   K2   : alpha = rz / d'q ; e += alpha d' ; r -= alpha q ; partial r.r
+//   B    : z = B r ; partials z.r, z.q            (beta = z.(r_new - r_old) / rz_prev)
+// scal[0..1] rz and scal[2..3] alpha, double-buffered by iteration parity
+// =====================================================================================
+__global__ void k_lpcg_k1(GridDev g, const float* __restrict__ z, const float* __restrict__ d_in,
+                          float* __restrict__ d_out, float* __restrict__ q, const uint16_t* __restrict__ kind,
+                          double* part, double* scal, int* flag, int it, double target_rr) {
+    double rz_new = sum_partials(part + 1 * kParts, gridDim.x);
+    double beta = 0.0;
+    if (it > 0) {
+        double zq = sum_partials(part + 2 * kParts, gridDim.x);
+        double rr = sum_partials(part + 3 * kParts, gridDim.x);
+        if (rr <= target_rr || flag[0]) {
+            if (blockIdx.x == 0 && threadIdx.x == 0 && !flag[0]) {
+                flag[1] = it;  // iterations completed
+                flag[0] = 1;
+            }
+            return;
+        }
+        double rz_old = scal[(it - 1) & 1];
+        double alpha_old = scal[2 + ((it - 1) & 1)];
+        beta = rz_old != 0.0 ? -alpha_old * zq / rz_old : 0.0;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) scal[it & 1] = rz_new;
+    float facc = 0.f;
+    const float fb = (float)beta;
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
+        uint16_t kd = kind[n];
+        if ((kd & 3) != kFree) {
+            d_out[n] = 0.f;
+            q[n] = 0.f;
+            continue;
+        }
+        int i, j, k;
+        node_ijk(g, n, i, j, k);
+        Stencil s;
+        stencil(g, i, j, k, s);
+        float dn = z[n] + fb * d_in[n];
+        float dg = 0.f, off = 0.f;
+#pragma unroll
+        for (int d = 0; d < 6; d++) {
+            if (kd & (1u << (2 + d))) continue;
+            dg += s.c[d];
+            int qq = s.q[d];
+            off += s.c[d] * (z[qq] + fb * d_in[qq]);
+        }
+        float qv = dg * dn - off;
+        d_out[n] = dn;
+        q[n] = qv;
+        facc += dn * qv;
+    }
+    double acc[1] = {facc};
+    block_partials<1>(acc, part + 0 * kParts, kParts);
+}
+__global__ void k_lpcg_k2(GridDev g, const float* __restrict__ d, const float* __restrict__ q, float* __restrict__ e,
+                          float* __restrict__ r, const uint16_t* __restrict__ kind, double* part, double* scal,
+                          int* flag, int it) {
+    if (flag[0]) return;
+    double dq = sum_partials(part + 0 * kParts, gridDim.x);
+    double rz = scal[it & 1];
+    double alpha_d = dq != 0.0 ? rz / dq : 0.0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) scal[2 + (it & 1)] = alpha_d;
+    const float alpha = (float)alpha_d;
+    float frr = 0.f;
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
+        if ((kind[n] & 3) != kFree) continue;
+        e[n] += alpha * d[n];
+        float rn = r[n] - alpha * q[n];
+        r[n] = rn;
+        frr += rn * rn;
+    }
+    double acc[1] = {frr};
+    block_partials<1>(acc, part + 3 * kParts, kParts);
+}
+__global__ void k_lpcg_zero(float* e, float* q, int nv, int* flag) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) flag[0] = 0;
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nv; n += gridDim.x * blockDim.x) {
+        e[n] = 0.f;
+        q[n] = 0.f;
+    }
+}
+
+void launch_lpcg_init(const GridDev& g, SolveWork& w, const LpState& L, cudaStream_t s, int grid, int sms) {
+    k_lpcg_zero<<<grid, 256, 0, s>>>(w.e, w.q, g.nv, w.flag);
+    cudaMemsetAsync(w.d, 0, sizeof(float) * g.nv, s);
+    launch_lp_apply(g, L, w.r, w.z, reinterpret_cast<const uint16_t*>(w.kind), w.q, w.part, nullptr, s, grid, sms);
+}
+void launch_lpcg_iter(const GridDev& g, SolveWork& w, const LpState& L, float* d_in, float* d_out, int it,
+                      double target_rr, cudaStream_t s, int grid, int sms) {
+    const uint16_t* kd = reinterpret_cast<const uint16_t*>(w.kind);
+    k_lpcg_k1<<<grid, 256, 0, s>>>(g, w.z, d_in, d_out, w.q, kd, w.part, w.scal, w.flag, it, target_rr);
+    k_lpcg_k2<<<grid, 256, 0, s>>>(g, d_out, w.q, w.e, w.r, kd, w.part, w.scal, w.flag, it);
+    launch_lp_apply(g, L, w.r, w.z, kd, w.q, w.part, w.flag, s, grid, sms);
+}
+
+
+
+// =====================================================================================
+// training: one step = forward (unfolded network), energy-norm loss, backward, Adam
+//   loss = (B r - x)^T L (B r - x) / x^T L x for a pair (r, x) with L x = r
+// Network contractions run on the tensor cores as GEMMs over tiles of 128 voxels:
+//   lift       h1  = im2col_+(z)  [V x 32] * Wl^T  [32 x C]
+//   mix        h2  = h1 [V x C] * Wm^T [C x C]
+//   proj bwd   dh2 = im2col_-(g)  [V x 32] * Wp    [32 x C]
+//   mix bwd    dh1 = dh2 [V x C] * Wm  [C x C]
+//   weight gradients dWp = im2col_-(g)^T h2, dWm = dh2^T h1, dWl^T = im2col_+(z)^T dh1 (K = voxels)
+// im2col_+(z)[v][t] = z[v + o_t], im2col_-(g)[v][t] = g[v - o_t] (taps t >= 27 are zero).
+// The projection forward (27 taps x C channels per voxel) runs on the CUDA cores.
+// =====================================================================================
+struct LpTrain {
+    __nv_bfloat16* h1[kLpNetLevels + 1] = {};
+    __nv_bfloat16* h2[kLpNetLevels + 1] = {};
+    __nv_bfloat16* dh2[kLpNetLevels + 1] = {};
+    __nv_bfloat16* dh1[kLpNetLevels + 1] = {};
+    float* g[kLpMaxLevels] = {};  // restricted loss gradient, levels >= 1
+    float *x = nullptr, *r = nullptr, *e0 = nullptr, *ge = nullptr;  // node arrays
+    float *grad = nullptr, *m = nullptr, *v = nullptr, *pscale = nullptr;
+    __nv_bfloat16* wbf = nullptr;  // per network level: Wl [C][32], Wm [C][C], Wm^T [C][C], Wp^T [C][32]
+    int wbf_off[kLpNetLevels + 1][4] = {};
+    double* part = nullptr;  // [32][kParts] partial sums
+    double* red = nullptr;   // reduced scalars [64]
+    float* wg = nullptr;     // per-CTA weight-gradient tiles [kWgCtas][128][64]
+    unsigned* err = nullptr;
+    double* h_red = nullptr;  // pinned
+    float* pair_r[4] = {};
+    float* pair_x[4] = {};
+    int npairs = 0, next_pair = 0;
+    long step = 0;
+};
+constexpr int kWgCtas = 152;
+
+enum : int { kAZPos = 0, kAGNeg = 1, kAAct = 2 };
+
+// value of row v (level voxel), column k of the A operand of an activation GEMM
+template <int AMODE>
+__device__ __forceinline__ float tc_a_value(const LView& src, const __nv_bfloat16* act, int K, int v, const int c[3],
+                                            int k) {
+    if (AMODE == kAAct) return __bfloat162float(act[(size_t)v * K + k]);
+    if (k >= 27) return 0.f;
+    const int sgn = AMODE == kAZPos ? 1 : -1;
+    int x = lv_nb(c[0], sgn * (k % 3 - 1), src.n[0], src.per[0]);
+    int y = lv_nb(c[1], sgn * ((k / 3) % 3 - 1), src.n[1], src.per[1]);
+    int z = lv_nb(c[2], sgn * (k / 9 - 1), src.n[2], src.per[2]);
+    if (x < 0 || y < 0 || z < 0) return 0.f;
+    return src.a[lv_off(src, x, y, z)];
+}
+
+// out[v][n] = sum_k A(v, k) Bw[n][k]  (bf16 operands, FP32 accumulation in TMEM, bf16 result)
+// 128 threads, one voxel row each; K in {16, 32, 64}, N in {16, 32, 64}
+template <int AMODE>
+__global__ void __launch_bounds__(128) k_tc_act(LView src, const __nv_bfloat16* __restrict__ act, int K,
+                                                const __nv_bfloat16* __restrict__ Bw, int N, int V,
+                                                __nv_bfloat16* __restrict__ out, unsigned* err) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __nv_bfloat16* sA = reinterpret_cast<__nv_bfloat16*>(smem);
+    const int slices = K / 16;
+    __nv_bfloat16* sB = sA + slices * 2048;
+    __shared__ uint32_t tmem_base;
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ int s_fail;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    for (int idx = tid; idx < N * K; idx += 128) {
+        int n = idx / K, k = idx - n * K;
+        sB[(k >> 4) * (N * 16) + tc_slice_offset(n, k & 15)] = Bw[idx];
+    }
+    const uint32_t ncols = N < 32 ? 32 : N;
+    if (warp == 0) {
+        tc_alloc(&tmem_base, ncols);
+        tc_relinquish();
+    }
+    if (tid == 0) {
+        tc_mbar_init(&bar, 1);
+        s_fail = 0;
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tm = tmem_base;
+    const uint32_t idesc = tc_idesc_bf16(128, N);
+    unsigned phase = 0;
+    const int ntiles = (V + 127) / 128;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int v = tile * 128 + tid;
+        int c[3] = {0, 0, 0};
+        if (v < V && AMODE != kAAct) lv_decode(src, (unsigned)v, c[0], c[1], c[2]);
+        for (int k = 0; k < K; k++) {
+            float a = v < V ? tc_a_value<AMODE>(src, act, K, v, c, k) : 0.f;
+            sA[(k >> 4) * 2048 + tc_slice_offset(tid, k & 15)] = __float2bfloat16(a);
+        }
+        tc_fence_smem();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (tid == 0) {
+            for (int sl = 0; sl < slices; sl++)
+                tc_mma_bf16(tm, tc_smem_desc(sA + sl * 2048, 128, 256), tc_smem_desc(sB + sl * N * 16, 128, 256),
+                            idesc, sl > 0 ? 1u : 0u);
+            tc_commit(&bar);
+        }
+        if (!tc_mbar_wait(&bar, phase, kTcWaitLimit)) atomicExch(&s_fail, 1);
+        phase ^= 1u;
+        __syncthreads();
+        if (s_fail) {
+            // the MMAs did not complete in time: record it and wait (bounded) before freeing TMEM
+            if (tid == 0) set_error(err, kErrBarrierTimeout);
+            tc_mbar_wait(&bar, phase ^ 1u, kTcWaitLimit);
+            break;
+        }
+        tc_fence_after();
+        for (int c0 = 0; c0 < N; c0 += 16) {
+            float vals[16];
+            tc_ld16(tm + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, vals);
+            if (v < V) {
+                __align__(16) __nv_bfloat16 b[16];
+#pragma unroll
+                for (int q = 0; q < 16; q++) b[q] = __float2bfloat16(vals[q]);
+                uint4* dst = reinterpret_cast<uint4*>(out + (size_t)v * N + c0);
+                dst[0] = reinterpret_cast<uint4*>(b)[0];
+                dst[1] = reinterpret_cast<uint4*>(b)[1];
+            }
+        }
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tc_dealloc(tm, ncols);
+}
+
+// D[m][n] = sum_v A(m, v) B(n, v) over all voxels; A(m, v) = im2col(src)[v][m] (m < 27) or
+// act[v][m] (m < Mv), B(n, v) = actB[v][n]; M padded to 128 (rows >= Mv zero).  Each CTA writes its
+// partial D (rows < Mv, N columns) to wg[blockIdx.x][128][64].
+template <int AMODE>
+__global__ void __launch_bounds__(128) k_tc_wgrad(LView src, const __nv_bfloat16* __restrict__ actA, int Mv,
+                                                  const __nv_bfloat16* __restrict__ actB, int N, int V, float* wg,
+                                                  unsigned* err) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __nv_bfloat16* sA = reinterpret_cast<__nv_bfloat16*>(smem);  // 8 slices x 128 rows x 16
+    __nv_bfloat16* sB = sA + 8 * 2048;                             // 8 slices x N rows x 16
+    __shared__ uint32_t tmem_base;
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ int s_fail;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    for (int idx = tid; idx < 8 * 2048; idx += 128) sA[idx] = __float2bfloat16(0.f);
+    const uint32_t ncols = N < 32 ? 32 : N;
+    if (warp == 0) {
+        tc_alloc(&tmem_base, ncols);
+        tc_relinquish();
+    }
+    if (tid == 0) {
+        tc_mbar_init(&bar, 1);
+        s_fail = 0;
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tm = tmem_base;
+    const uint32_t idesc = tc_idesc_bf16(128, N);
+    unsigned phase = 0;
+    bool first = true, ok = true;
+    const int ntiles = (V + 127) / 128;
+    const int sl = tid >> 4, kk = tid & 15;  // this thread's voxel column inside the tile
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int v = tile * 128 + tid;
+        int c[3] = {0, 0, 0};
+        if (v < V && AMODE != kAAct) lv_decode(src, (unsigned)v, c[0], c[1], c[2]);
+        for (int m = 0; m < Mv; m++) {
+            float a = v < V ? tc_a_value<AMODE>(src, actA, Mv, v, c, m) : 0.f;
+            sA[sl * 2048 + tc_slice_offset(m, kk)] = __float2bfloat16(a);
+        }
+        for (int n = 0; n < N; n++) {
+            __nv_bfloat16 b = v < V ? actB[(size_t)v * N + n] : __float2bfloat16(0.f);
+            sB[sl * (N * 16) + tc_slice_offset(n, kk)] = b;
+        }
+        tc_fence_smem();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (tid == 0) {
+            for (int s8 = 0; s8 < 8; s8++)
+                tc_mma_bf16(tm, tc_smem_desc(sA + s8 * 2048, 128, 256), tc_smem_desc(sB + s8 * N * 16, 128, 256),
+                            idesc, (first && s8 == 0) ? 0u : 1u);
+            tc_commit(&bar);
+        }
+        first = false;
+        if (!tc_mbar_wait(&bar, phase, kTcWaitLimit)) atomicExch(&s_fail, 1);
+        phase ^= 1u;
+        __syncthreads();
+        if (s_fail) {
+            if (tid == 0) set_error(err, kErrBarrierTimeout);
+            tc_mbar_wait(&bar, phase ^ 1u, kTcWaitLimit);
+            ok = false;
+            break;
+        }
+        tc_fence_after();
+    }
+    float* dst = wg + (size_t)blockIdx.x * 128 * 64;
+    if (ok) {
+        for (int c0 = 0; c0 < N; c0 += 16) {
+            float vals[16];
+            tc_ld16(tm + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, vals);
+            if (tid < Mv)
+#pragma unroll
+                for (int q = 0; q < 16; q++) dst[tid * 64 + c0 + q] = first ? 0.f : vals[q];
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tc_dealloc(tm, ncols);
+}
+
+// sums the per-CTA tiles in a fixed order into the flat gradient: grad[off + m*sm + n*sn]
+__global__ void k_lp_wg_reduce(const float* wg, int nctas, int Mv, int N, float* grad, int off, int sm, int sn) {
+    for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < Mv * N; x += gridDim.x * blockDim.x) {
+        int m = x / N, n = x - m * N;
+        double a = 0.0;
+        for (int b = 0; b < nctas; b++) a += wg[((size_t)b * 128 + m) * 64 + n];
+        grad[off + m * sm + n * sn] = (float)a;
+    }
+}
+
+// o = projection(h2) + P e_coarse on a network level
+__global__ void k_lp_proj(LView zv, const __nv_bfloat16* __restrict__ h2, int C, const float* __restrict__ Wp, LView cin,
+                          LView out) {
+    for (unsigned idx = blockIdx.x * blockDim.x + threadIdx.x; idx < (unsigned)out.nvox;
+         idx += gridDim.x * blockDim.x) {
+        int c[3];
+        lv_decode(out, idx, c[0], c[1], c[2]);
+        float acc = 0.f;
+        for (int t = 0; t < 27; t++) {
+            int x = lv_nb(c[0], t % 3 - 1, zv.n[0], zv.per[0]);
+            int y = lv_nb(c[1], (t / 3) % 3 - 1, zv.n[1], zv.per[1]);
+            int z = lv_nb(c[2], t / 9 - 1, zv.n[2], zv.per[2]);
+            if (x < 0 || y < 0 || z < 0) continue;
+            const uint4* row = reinterpret_cast<const uint4*>(h2 + (size_t)lv_off(zv, x, y, z) * C);
+            const float* w = Wp + t * C;
+            for (int c8 = 0; c8 < C / 8; c8++) {
+                uint4 u = row[c8];
+                const __nv_bfloat16* b = reinterpret_cast<const __nv_bfloat16*>(&u);
+#pragma unroll
+                for (int q = 0; q < 8; q++) acc += __ldg(&w[c8 * 8 + q]) * __bfloat162float(b[q]);
+            }
+        }
+        if (cin.a) acc += lp_prolong_at(cin, c);
+        out.a[lv_off(out, c[0], c[1], c[2])] = acc;
+    }
+}
+
+// (L v)_p on FREE nodes for v zero off FREE nodes (the operator of the reduced system)
+__device__ __forceinline__ float lp_apply_L(const GridDev& g, const float* __restrict__ v, uint16_t kd, int n) {
+    int i, j, k;
+    node_ijk(g, n, i, j, k);
+    Stencil s;
+    stencil(g, i, j, k, s);
+    float dg = 0.f, off = 0.f;
+#pragma unroll
+    for (int d = 0; d < 6; d++) {
+        if (kd & (1u << (2 + d))) continue;
+        dg += s.c[d];
+        off += s.c[d] * v[s.q[d]];
+    }
+    return dg * v[n] - off;
+}
+
+// white-noise sample x on FREE nodes (Philox keyed by (seed, step, node)) and r = L x
+__global__ void k_lp_noise(GridDev g, const uint16_t* __restrict__ kind, float* x, unsigned long long seed, long step) {
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
+        if ((kind[n] & 3) != kFree) {
+            x[n] = 0.f;
+            continue;
+        }
+        uint4 rr = philox4x32_10(make_uint4((unsigned)n, (unsigned)step, 0x5eedu, 0u),
+                                 make_uint2((unsigned)seed, (unsigned)(seed >> 32)));
+        float u1 = u01(rr.x), u2 = u01(rr.y);
+        x[n] = sqrtf(-2.f * logf(u1)) * cospif(2.f * u2);
+    }
+}
+__global__ void k_lp_L(GridDev g, const uint16_t* __restrict__ kind, const float* __restrict__ x, float* r) {
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
+        uint16_t kd = kind[n];
+        r[n] = (kd & 3) == kFree ? lp_apply_L(g, x, kd, n) : 0.f;
+    }
+}
+// ge = L e - L x on FREE nodes; partials (e - x).ge (slot 0) and x.Lx (slot 1)
+__global__ void k_lp_loss(GridDev g, const uint16_t* __restrict__ kind, const float* __restrict__ e,
+                          const float* __restrict__ x, float* ge, double* part) {
+    float f0 = 0.f, f1 = 0.f;
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
+        uint16_t kd = kind[n];
+        if ((kd & 3) != kFree) {
+            ge[n] = 0.f;
+            continue;
+        }
+        float le = lp_apply_L(g, e, kd, n), lx = lp_apply_L(g, x, kd, n);
+        float d = le - lx;
+        ge[n] = d;
+        f0 += (e[n] - x[n]) * d;
+        f1 += x[n] * lx;
+    }
+    double a0[1] = {f0}, a1[1] = {f1};
+    block_partials<1>(a0, part + 0 * kParts, kParts);
+    block_partials<1>(a1, part + 1 * kParts, kParts);
+}
+// ge *= 2 / x.Lx ; red[0] = loss
+__global__ void k_lp_loss_scale(int nv, float* ge, const double* part, double* red) {
+    double num = sum_partials(part + 0 * kParts, gridDim.x);
+    double q = sum_partials(part + 1 * kParts, gridDim.x);
+    const float sc = q > 0 ? (float)(2.0 / q) : 0.f;
+    if (blockIdx.x == 0 && threadIdx.x == 0) red[0] = q > 0 ? num / q : 0.0;
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nv; n += gridDim.x * blockDim.x) ge[n] *= sc;
+}
+// dS0[t] partials = sum_v ge[v] r[v + o_t] (level 0, FREE nodes; r is zero elsewhere)
+__global__ void k_lp_ds0(GridDev g, LView rin, const uint16_t* __restrict__ kind, const float* __restrict__ ge,
+                         double* part) {
+    float acc[27];
+#pragma unroll
+    for (int t = 0; t < 27; t++) acc[t] = 0.f;
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
+        if ((kind[n] & 3) != kFree) continue;
+        int c[3];
+        node_ijk(g, n, c[0], c[1], c[2]);
+        const float gv = ge[n];
+#pragma unroll
+        for (int t = 0; t < 27; t++) {
+            int x = lv_nb(c[0], t % 3 - 1, rin.n[0], rin.per[0]);
+            int y = lv_nb(c[1], (t / 3) % 3 - 1, rin.n[1], rin.per[1]);
+            int z = lv_nb(c[2], t / 9 - 1, rin.n[2], rin.per[2]);
+            if (x >= 0 && y >= 0 && z >= 0) acc[t] += gv * rin.a[lv_off(rin, x, y, z)];
+        }
+    }
+    __shared__ double s[27][8];
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+#pragma unroll
+    for (int t = 0; t < 27; t++) {
+        double x = acc[t];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) s[t][wp] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < 27) {
+        double x = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) x += s[threadIdx.x][w];
+        part[threadIdx.x * kParts + blockIdx.x] = x;
+    }
+}
+__global__ void k_lp_ds0_collect(const double* part, int nblocks, float* grad, int off) {
+    const int t = blockIdx.x;
+    double x = sum_partials(part + t * kParts, nblocks);
+    if (threadIdx.x == 0) grad[off + t] = (float)x;
+}
+
+// bf16 operand copies of the network weights
+__global__ void k_lp_prep_bf16(const float* __restrict__ W, LpLayout lay, __nv_bfloat16* wbf, int o1, int o2, int o3,
+                               int o4, int l) {
+    const int C = lp_channels(l);
+    const float* Wl = W + lay.wl[l];
+    const float* Wm = W + lay.wm[l];
+    const float* Wp = W + lay.wp[l];
+    for (int x = threadIdx.x; x < C * 32; x += blockDim.x) {
+        int c = x / 32, t = x % 32;
+        wbf[o1 + x] = __float2bfloat16(t < 27 ? Wl[c * 27 + t] : 0.f);  // lift B [C][32]
+        wbf[o4 + x] = __float2bfloat16(t < 27 ? Wp[t * C + c] : 0.f);   // proj-backward B [C][32]
+    }
+    for (int x = threadIdx.x; x < C * C; x += blockDim.x) {
+        int a = x / C, b = x % C;
+        wbf[o2 + x] = __float2bfloat16(Wm[a * C + b]);  // mix B: [out][in]
+        wbf[o3 + x] = __float2bfloat16(Wm[b * C + a]);  // mix-backward B: [in][out]
+    }
+}
+
+// Adam (beta1 0.9, beta2 0.999), the step of each parameter scaled by its group's magnitude
+__global__ void k_lp_adam(float* W, const float* __restrict__ grad, float* m, float* v, const float* __restrict__ pscale,
+                          int n, float lr, float bc1, float bc2) {
+    for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < n; x += gridDim.x * blockDim.x) {
+        float gx = grad[x];
+        float mm = 0.9f * m[x] + 0.1f * gx;
+        float vv = 0.999f * v[x] + 0.001f * gx * gx;
+        m[x] = mm;
+        v[x] = vv;
+        float mh = mm / bc1, vh = vv / bc2;
+        W[x] -= lr * pscale[x] * mh / (sqrtf(vh) + 1e-30f);
+    }
+}
+
+void lp_free_train(LpState& L) {
+    LpTrain* T = L.train;
+    if (!T) return;
+    for (int l = 1; l <= kLpNetLevels; l++)
+        for (void* p : {(void*)T->h1[l], (void*)T->h2[l], (void*)T->dh2[l], (void*)T->dh1[l]})
+            if (p) cudaFree(p);
+    for (int l = 1; l < kLpMaxLevels; l++)
+        if (T->g[l]) cudaFree(T->g[l]);
+    for (void* p : {(void*)T->x, (void*)T->r, (void*)T->e0, (void*)T->ge, (void*)T->grad, (void*)T->m, (void*)T->v,
+                    (void*)T->pscale, (void*)T->wbf, (void*)T->part, (void*)T->red, (void*)T->wg, (void*)T->err})
+        if (p) cudaFree(p);
+    for (int k = 0; k < 4; k++) {
+        if (T->pair_r[k]) cudaFree(T->pair_r[k]);
+        if (T->pair_x[k]) cudaFree(T->pair_x[k]);
+    }
+    if (T->h_red) cudaFreeHost(T->h_red);
+    delete T;
+    L.train = nullptr;
+}
+
+#define LP_CU(call)                      \
+    do {                                 \
+        if ((call) != cudaSuccess) return 2; \
+    } while (0)
+
+// allocates the training state; returns 0 or 2 (CUDA error)
+int lp_alloc_train(const GridDev& g, LpState& L, const float* init_W) {
+    if (L.train) return 0;
+    LpTrain* T = new LpTrain();
+    L.train = T;
+    for (int l = 1; l <= kLpNetLevels && l < L.nlev; l++) {
+        size_t V = (size_t)L.dims[l][0] * L.dims[l][1] * L.dims[l][2];
+        size_t bytes = V * lp_channels(l) * sizeof(__nv_bfloat16);
+        LP_CU(cudaMalloc(&T->h1[l], bytes));
+        LP_CU(cudaMalloc(&T->h2[l], bytes));
+        LP_CU(cudaMalloc(&T->dh2[l], bytes));
+        LP_CU(cudaMalloc(&T->dh1[l], bytes));
+    }
+    for (int l = 1; l < L.nlev; l++)
+        LP_CU(cudaMalloc(&T->g[l], sizeof(float) * (size_t)L.dims[l][0] * L.dims[l][1] * L.dims[l][2]));
+    for (float** p : {&T->x, &T->r, &T->e0, &T->ge}) LP_CU(cudaMalloc(p, sizeof(float) * g.nv));
+    const int n = L.lay.total;
+    for (float** p : {&T->grad, &T->m, &T->v, &T->pscale}) LP_CU(cudaMalloc(p, sizeof(float) * n));
+    LP_CU(cudaMemset(T->m, 0, sizeof(float) * n));
+    LP_CU(cudaMemset(T->v, 0, sizeof(float) * n));
+    LP_CU(cudaMemset(T->grad, 0, sizeof(float) * n));
+    // step scale of each parameter: the largest starting magnitude of its group
+    std::vector<float> ps(n, 1.f);
+    auto group = [&](int off, int cnt) {
+        float mx = 0.f;
+        for (int k = 0; k < cnt; k++) mx = std::max(mx, std::fabs(init_W[off + k]));
+        for (int k = 0; k < cnt; k++) ps[off + k] = mx > 0 ? mx : 1.f;
+    };
+    group(L.lay.s0, 27);
+    int wbf = 0;
+    for (int l = 1; l <= kLpNetLevels; l++) {
+        int C = lp_channels(l);
+        group(L.lay.wl[l], C * 27);
+        group(L.lay.wm[l], C * C);
+        group(L.lay.wp[l], 27 * C);
+        T->wbf_off[l][0] = wbf;
+        wbf += C * 32;
+        T->wbf_off[l][1] = wbf;
+        wbf += C * C;
+        T->wbf_off[l][2] = wbf;
+        wbf += C * C;
+        T->wbf_off[l][3] = wbf;
+        wbf += C * 32;
+    }
+    LP_CU(cudaMemcpy(T->pscale, ps.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
+    LP_CU(cudaMalloc(&T->wbf, sizeof(__nv_bfloat16) * wbf));
+    LP_CU(cudaMalloc(&T->part, sizeof(double) * 32 * kParts));
+    LP_CU(cudaMalloc(&T->red, sizeof(double) * 64));
+    LP_CU(cudaMalloc(&T->wg, sizeof(float) * (size_t)kWgCtas * 128 * 64));
+    LP_CU(cudaMalloc(&T->err, sizeof(unsigned)));
+    LP_CU(cudaMemset(T->err, 0, sizeof(unsigned)));
+    LP_CU(cudaMallocHost(&T->h_red, sizeof(double) * 64));
+    return 0;
+}
+
+static size_t tc_act_smem(int K, int N) { return (size_t)(K / 16) * (128 + N) * 16 * sizeof(__nv_bfloat16); }
+static size_t tc_wg_smem(int N) { return (size_t)8 * (128 + N) * 16 * sizeof(__nv_bfloat16); }
+
+template <int AMODE>
+static void launch_tc_act(LView src, const __nv_bfloat16* act, int K, const __nv_bfloat16* Bw, int N, int V,
+                          __nv_bfloat16* out, unsigned* err, cudaStream_t s, int sms) {
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_tc_act<AMODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_act_smem(64, 64));
+        attr = true;
+    }
+    int tiles = (V + 127) / 128;
+    k_tc_act<AMODE><<<std::max(1, std::min(tiles, sms * 4)), 128, tc_act_smem(K, N), s>>>(src, act, K, Bw, N, V, out,
+                                                                                          err);
+}
+template <int AMODE>
+static void launch_tc_wgrad(LView src, const __nv_bfloat16* actA, int Mv, const __nv_bfloat16* actB, int N, int V,
+                            float* wg, unsigned* err, cudaStream_t s) {
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_tc_wgrad<AMODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_wg_smem(64));
+        attr = true;
+    }
+    k_tc_wgrad<AMODE><<<kWgCtas, 128, tc_wg_smem(N), s>>>(src, actA, Mv, actB, N, V, wg, err);
+}
+
+void launch_lp_prep(const LpState& L, cudaStream_t s) {
+    const LpTrain* T = L.train;
+    for (int l = 1; l <= kLpNetLevels; l++)
+        k_lp_prep_bf16<<<1, 256, 0, s>>>(L.W, L.lay, T->wbf, T->wbf_off[l][0], T->wbf_off[l][1], T->wbf_off[l][2],
+                                         T->wbf_off[l][3], l);
+}
+
+// forward + loss + backward for the pair (r, x) on the node array; gradient into T->grad,
+// loss into T->red[0].  r and x are zero off FREE nodes.
+void launch_lp_loss_grad(const GridDev& g, LpState& L, const uint16_t* kind, const float* r, const float* x,
+                         cudaStream_t s, int grid, int sms) {
+    LpTrain* T = L.train;
+    LView none{};
+    none.a = nullptr;
+    LView r0 = lp_node_view(g, L, const_cast<float*>(r));
+    // forward: restriction chain
+    for (int l = 1; l < L.nlev; l++) {
+        LView f = l == 1 ? r0 : lp_level_view(L, l - 1, L.z[l - 1]);
+        LView c = lp_level_view(L, l, L.z[l]);
+        k_lp_restrict<<<lp_blocks(c.nvox, sms), 256, 0, s>>>(f, c, nullptr);
+    }
+    for (int l = L.nlev - 1; l >= 1; l--) {
+        LView zin = lp_level_view(L, l, L.z[l]);
+        LView cin = l + 1 < L.nlev ? lp_level_view(L, l + 1, L.e[l + 1]) : none;
+        LView out = lp_level_view(L, l, L.e[l]);
+        if (l <= kLpNetLevels) {
+            const int C = lp_channels(l), V = zin.nvox;
+            launch_tc_act<kAZPos>(zin, nullptr, 32, T->wbf + T->wbf_off[l][0], C, V, T->h1[l], T->err, s, sms);
+            launch_tc_act<kAAct>(zin, T->h1[l], C, T->wbf + T->wbf_off[l][1], C, V, T->h2[l], T->err, s, sms);
+            k_lp_proj<<<lp_blocks(V, sms), 256, 0, s>>>(zin, T->h2[l], C, L.W + L.lay.wp[l], cin, out);
+        } else {
+            k_lp_up<<<lp_blocks(out.nvox, sms), 256, 0, s>>>(zin, cin, out, 2, nullptr, (float)(1.0 / L.diag[l]),
+                                                            nullptr);
+        }
+    }
+    LView cin1 = L.nlev > 1 ? lp_level_view(L, 1, L.e[1]) : none;
+    k_lp_up0<<<grid, 256, 0, s>>>(g, r0, cin1, T->e0, kind, L.W + L.lay.s0, nullptr, nullptr, nullptr);
+    // loss and its gradient with respect to e
+    k_lp_loss<<<grid, 256, 0, s>>>(g, kind, T->e0, x, T->ge, T->part);
+    k_lp_loss_scale<<<grid, 256, 0, s>>>(g.nv, T->ge, T->part, T->red);
+    // backward: restriction chain of the gradient, then every level's parameters
+    LView g0 = lp_node_view(g, L, T->ge);
+    for (int l = 1; l < L.nlev; l++) {
+        LView f = l == 1 ? g0 : lp_level_view(L, l - 1, T->g[l - 1]);
+        LView c = lp_level_view(L, l, T->g[l]);
+        k_lp_restrict<<<lp_blocks(c.nvox, sms), 256, 0, s>>>(f, c, nullptr);
+    }
+    k_lp_ds0<<<grid, 256, 0, s>>>(g, r0, kind, T->ge, T->part);
+    k_lp_ds0_collect<<<27, 256, 0, s>>>(T->part, grid, T->grad, L.lay.s0);
+    for (int l = 1; l <= kLpNetLevels && l < L.nlev; l++) {
+        const int C = lp_channels(l);
+        LView zin = lp_level_view(L, l, L.z[l]);
+        LView gl = lp_level_view(L, l, T->g[l]);
+        const int V = zin.nvox;
+        const int rb = std::max(1, std::min(64, (27 * C + 255) / 256));
+        launch_tc_act<kAGNeg>(gl, nullptr, 32, T->wbf + T->wbf_off[l][3], C, V, T->dh2[l], T->err, s, sms);
+        launch_tc_wgrad<kAGNeg>(gl, nullptr, 27, T->h2[l], C, V, T->wg, T->err, s);
+        k_lp_wg_reduce<<<rb, 256, 0, s>>>(T->wg, kWgCtas, 27, C, T->grad, L.lay.wp[l], C, 1);
+        launch_tc_act<kAAct>(gl, T->dh2[l], C, T->wbf + T->wbf_off[l][2], C, V, T->dh1[l], T->err, s, sms);
+        launch_tc_wgrad<kAAct>(gl, T->dh2[l], C, T->h1[l], C, V, T->wg, T->err, s);
+        k_lp_wg_reduce<<<rb, 256, 0, s>>>(T->wg, kWgCtas, C, C, T->grad, L.lay.wm[l], C, 1);
+        launch_tc_wgrad<kAZPos>(zin, nullptr, 27, T->dh1[l], C, V, T->wg, T->err, s);
+        k_lp_wg_reduce<<<rb, 256, 0, s>>>(T->wg, kWgCtas, 27, C, T->grad, L.lay.wl[l], 1, 27);
+    }
+}
+
+void launch_lp_noise_pair(const GridDev& g, LpState& L, const uint16_t* kind, unsigned long long seed, cudaStream_t s,
+                          int grid) {
+    LpTrain* T = L.train;
+    k_lp_noise<<<grid, 256, 0, s>>>(g, kind, T->x, seed, T->step);
+    k_lp_L<<<grid, 256, 0, s>>>(g, kind, T->x, T->r);
+}
+
+__global__ void k_lp_acc(float* dst, const float* __restrict__ src, int n) {
+    for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < n; x += gridDim.x * blockDim.x) dst[x] += src[x];
+}
+// training pairs from solves: the first residual r0 of a solve and the sum x of its corrections
+int lp_pair_begin(LpState& L, const float* r0, int nv, cudaStream_t s) {
+    LpTrain* T = L.train;
+    int k = T->next_pair;
+    if (!T->pair_r[k]) {
+        LP_CU(cudaMalloc(&T->pair_r[k], sizeof(float) * nv));
+        LP_CU(cudaMalloc(&T->pair_x[k], sizeof(float) * nv));
+    }
+    LP_CU(cudaMemcpyAsync(T->pair_r[k], r0, sizeof(float) * nv, cudaMemcpyDeviceToDevice, s));
+    LP_CU(cudaMemsetAsync(T->pair_x[k], 0, sizeof(float) * nv, s));
+    return 0;
+}
+void lp_pair_add(LpState& L, const float* e, int nv, cudaStream_t s, int grid) {
+    LpTrain* T = L.train;
+    k_lp_acc<<<grid, 256, 0, s>>>(T->pair_x[T->next_pair], e, nv);
+}
+void lp_pair_end(LpState& L) {
+    LpTrain* T = L.train;
+    T->next_pair = (T->next_pair + 1) % 4;
+    T->npairs = std::min(T->npairs + 1, 4);
+}
+const float* lp_pair_r(const LpState& L, int k) { return L.train->pair_r[k]; }
+const float* lp_pair_x(const LpState& L, int k) { return L.train->pair_x[k]; }
+int lp_npairs(const LpState& L) { return L.train ? L.train->npairs : 0; }
+float* lp_train_x(const LpState& L) { return L.train->x; }
+float* lp_train_r(const LpState& L) { return L.train->r; }
+float* lp_train_grad(const LpState& L) { return L.train->grad; }
+double* lp_train_red(const LpState& L) { return L.train->red; }
+unsigned* lp_train_err(const LpState& L) { return L.train->err; }
+
+void launch_lp_adam(LpState& L, float lr, cudaStream_t s) {
+    LpTrain* T = L.train;
+    T->step++;
+    float bc1 = 1.f - powf(0.9f, (float)T->step), bc2 = 1.f - powf(0.999f, (float)T->step);
+    k_lp_adam<<<std::max(1, std::min(1024, (L.lay.total + 255) / 256)), 256, 0, s>>>(L.W, T->grad, T->m, T->v,
+                                                                                     T->pscale, L.lay.total, lr, bc1, bc2);
+    launch_lp_prep(L, s);
+    launch_lp_fold(L, s);
+}
+
+// =====================================================================================
+// host: layout, initial weights, Galerkin diagonals
+// =====================================================================================
+void lp_layout(LpLayout& lay) {
+    int off = 0;
+    lay.s0 = off;
+    off += 27;
+    for (int l = 1; l <= kLpNetLevels; l++) {
+        int C = lp_channels(l);
+        lay.wl[l] = off;
+        off += C * 27;
+        lay.wm[l] = off;
+        off += C * C;
+        lay.wp[l] = off;
+        off += 27 * C;
+    }
+    lay.wl[0] = lay.wm[0] = lay.wp[0] = 0;
+    lay.total = off;
+}
+
+// BPX start: S0 = delta / diag_0; network level l: lift and projection pick the centre tap of
+// channel 0, the mix is the identity, the projection scales by 1 / diag_l
+void lp_init_weights(const LpLayout& lay, const double* diag, int nlev, float* W) {
+    std::fill(W, W + lay.total, 0.f);
+    W[lay.s0 + 13] = (float)(1.0 / diag[0]);
+    for (int l = 1; l <= kLpNetLevels; l++) {
+        int C = lp_channels(l);
+        double d = l < nlev ? diag[l] : 1.0;
+        W[lay.wl[l] + 0 * 27 + 13] = 1.f;
+        for (int c = 0; c < C; c++) W[lay.wm[l] + c * C + c] = 1.f;
+        W[lay.wp[l] + 13 * C + 0] = (float)(1.0 / d);
+    }
+}
+
+namespace {
+std::vector<double> up1(const std::vector<double>& a, size_t nf) {
+    std::vector<double> f(nf, 0.0);
+    size_t nc = a.size();
+    for (size_t i = 0; i < nf; i++) {
+        size_t c = i >> 1;
+        double v = 0.75 * a[c];
+        if (i & 1) {
+            if (c + 1 < nc) v += 0.25 * a[c + 1];
+        } else if (c > 0) {
+            v += 0.25 * a[c - 1];
+        }
+        f[i] = v;
+    }
+    return f;
+}
+std::vector<double> dn1(const std::vector<double>& f) {
+    size_t nf = f.size(), nc = (nf + 1) / 2;
+    std::vector<double> c(nc, 0.0);
+    for (size_t k = 0; k < nc; k++) {
+        long raw[4] = {(long)(2 * k) - 1, (long)(2 * k), (long)(2 * k + 1), (long)(2 * k + 2)};
+        const double w[4] = {0.25, 0.75, 0.75, 0.25};
+        for (int m = 0; m < 4; m++)
+            if (raw[m] >= 0 && raw[m] < (long)nf) c[k] += w[m] * f[raw[m]];
+    }
+    return c;
+}
+}  // namespace
+
+// diag_l = (cx + cy + cz) t_l m_l^2, with t_l, m_l the interior diagonals of P^T T P and P^T P
+// along one axis after l coarsenings (T = tridiag(-1, 2, -1)), probed on a long 1-D array
+void lp_galerkin_diag(const double c[3], int nlev, double* diag) {
+    size_t n = (size_t)1 << (nlev + 3);
+    for (int l = 0; l < nlev; l++) {
+        size_t nc = n >> l;
+        std::vector<double> f(nc, 0.0);
+        f[nc / 2] = 1.0;
+        for (int k = 0; k < l; k++) f = up1(f, 2 * f.size());
+        std::vector<double> tf(f.size()), mf = f;
+        for (size_t i = 0; i < f.size(); i++)
+            tf[i] = 2 * f[i] - (i > 0 ? f[i - 1] : 0.0) - (i + 1 < f.size() ? f[i + 1] : 0.0);
+        for (int k = 0; k < l; k++) {
+            tf = dn1(tf);
+            mf = dn1(mf);
+        }
+        diag[l] = (c[0] + c[1] + c[2]) * tf[nc / 2] * mf[nc / 2] * mf[nc / 2];
+    }
 }
 
 }  // namespace pic

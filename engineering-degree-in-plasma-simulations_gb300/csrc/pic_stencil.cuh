@@ -1,0 +1,84 @@
+// Node-index decoding, the 7-point stencil of the reduced Poisson system, and deterministic
+// block reductions, shared by the field kernels and the learned-preconditioner kernels.
+#pragma once
+#include "pic_kernels.h"
+
+namespace pic {
+
+constexpr double kEps0 = 8.85418782e-12;  // ch4/v3/src/all.h:16
+
+__device__ __forceinline__ void node_ijk(const GridDev& g, int n, int& i, int& j, int& k) {
+    unsigned t = fdiv((unsigned)n, g.fd_ni);
+    i = n - (int)t * g.ni;
+    unsigned kk = fdiv(t, g.fd_nj);
+    j = (int)t - (int)kk * g.nj;
+    k = (int)kk;
+}
+// neighbour index along an axis with periodic wrap (the copy at n-1 folds onto 0)
+__device__ __forceinline__ int wrap_m(int c, int n, int per) { return (per && c == 0) ? n - 2 : c - 1; }
+__device__ __forceinline__ int wrap_p(int c, int n, int per) { return (per && c + 1 >= n - 1) ? 0 : c + 1; }
+
+struct Stencil {
+    int q[6];
+    float c[6];
+};
+__device__ __forceinline__ void stencil(const GridDev& g, int i, int j, int k, Stencil& s) {
+    int nij = g.ni * g.nj;
+    int im = wrap_m(i, g.ni, g.periodic[0]), ip = wrap_p(i, g.ni, g.periodic[0]);
+    int jm = wrap_m(j, g.nj, g.periodic[1]), jp = wrap_p(j, g.nj, g.periodic[1]);
+    int km = wrap_m(k, g.nk, g.periodic[2]), kp = wrap_p(k, g.nk, g.periodic[2]);
+    int row = k * nij + j * g.ni;
+    s.q[0] = row + im;
+    s.q[1] = row + ip;
+    s.q[2] = k * nij + jm * g.ni + i;
+    s.q[3] = k * nij + jp * g.ni + i;
+    s.q[4] = km * nij + j * g.ni + i;
+    s.q[5] = kp * nij + j * g.ni + i;
+    float cx = g.inv_dx[0] * g.inv_dx[0], cy = g.inv_dx[1] * g.inv_dx[1], cz = g.inv_dx[2] * g.inv_dx[2];
+    s.c[0] = s.c[1] = cx;
+    s.c[2] = s.c[3] = cy;
+    s.c[4] = s.c[5] = cz;
+}
+
+// ------------------------------------------------------------------------------------
+// block reduction of up to four doubles into per-block partial slots
+// ------------------------------------------------------------------------------------
+template <int N>
+__device__ __forceinline__ void block_partials(double (&v)[N], double* part, int nslots_stride) {
+    __shared__ double s[N][8];
+#pragma unroll
+    for (int c = 0; c < N; c++) {
+        double x = v[c];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if ((threadIdx.x & 31) == 0) s[c][threadIdx.x >> 5] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < N) {
+        double x = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) x += s[threadIdx.x][w];
+        part[threadIdx.x * nslots_stride + blockIdx.x] = x;
+    }
+    __syncthreads();
+}
+// every block sums the same partials in the same order: identical scalars everywhere
+__device__ __forceinline__ double sum_partials(const double* part, int nblocks) {
+    __shared__ double s[8];
+    double x = 0;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) x += part[b];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = x;
+    __syncthreads();
+    double t = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += s[w];
+    __syncthreads();
+    return t;
+}
+
+__device__ __forceinline__ float diag_of(uint16_t kd, const Stencil& s) {
+    float dg = 0.f;
+#pragma unroll
+    for (int d = 0; d < 6; d++)
+        if (!(kd & (1u << (2 + d)))) dg += s.c[d];
+    return dg;
+}
+}  // namespace pic

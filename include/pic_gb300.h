@@ -115,6 +115,8 @@ int pic_charge_density(pic_world* w);
 
 #define PIC_SOLVER_RBSOR 0 /* red-black SOR, FP32 sweeps in FP64 refinement (replaces GS) */
 #define PIC_SOLVER_PCG 1   /* flexible Jacobi-PCG, FP32 iterations in FP64 refinement (replaces NR-PCG) */
+#define PIC_SOLVER_LEARNED 2 /* flexible CG with the learned multilevel preconditioner, FP32 iterations in
+                              * FP64 refinement (no reference counterpart) */
 /* PotentialSolver(world, max_it, tolerance, SolverType)               PotentialSolver.cpp:44-52
  * Stopping rule: FP64 ||b - L phi||_2 / ||b||_2 <= tol_rel (the reference stops on an absolute
  * RMS residual).  omega is the SOR weight (reference 1.4). */
@@ -128,6 +130,34 @@ int pic_solver_compute_ef(pic_world* w);
 /* cumulative solver work since creation: solves, FP64 refinements (residual evaluations) and
  * inner FP32 sweeps / iterations (no reference counterpart; the reference prints progress) */
 int pic_solver_stats(pic_world* w, long* solves, long* refinements, long* inner_iterations);
+
+/* ---- learned multilevel preconditioner (no reference counterpart) ----------------------
+ * B r = sum_l P^l o_l over a box hierarchy (level 0 = the distinct nodes; each level halves the
+ * previous one, rounding up), cell-centred trilinear prolongation P, restriction P^T; level 0
+ * applies a learned 3x3x3 stencil, levels 1-4 a linear 3-D convolutional network (lift 1->C,
+ * mix CxC, projection C->1; C = 16, 32, 64, 64), deeper levels the inverse Galerkin diagonal.
+ * The weights start as the BPX preconditioner.  Created on first use for the world's grid. */
+/* number of levels, their extents (x, y, z per level, up to 12 levels) and Galerkin diagonals */
+int pic_learned_levels(pic_world* w, int* nlev, int* dims, double* diag);
+/* restores the starting (BPX) weights */
+int pic_learned_reset(pic_world* w);
+/* copies the FP32 parameters out (out may be NULL to query the count) or in: the level-0
+ * stencil [27], then per network level lift [C][27], mix [C][C] (out, in), projection [27][C] */
+int pic_learned_weights(pic_world* w, float* out, long capacity, long* count);
+int pic_learned_set_weights(pic_world* w, const float* in, long count);
+/* z = B r for host arrays of all nodes (r is read on FREE nodes; z is zero elsewhere) */
+int pic_learned_apply(pic_world* w, const double* r, double* z);
+/* Training.  Loss of a pair (r, x) with L x = r: (B r - x)^T L (B r - x) / x^T L x, its gradient
+ * by the library's own forward and backward kernels (tensor-core GEMMs, BF16 operands, FP32
+ * accumulation).  loss_grad evaluates one pair (host arrays of all nodes, read on FREE nodes)
+ * and returns the loss and the gradient in the parameter layout, without updating. */
+int pic_learned_loss_grad(pic_world* w, const double* r, const double* x, double* loss, float* grad);
+/* collect (first residual, total correction) of every PCG / learned solve as a training pair
+ * (the last four are kept) */
+int pic_learned_collect(pic_world* w, int on);
+/* steps of Adam (learning rate lr relative to each parameter group's size); a step uses a
+ * collected pair when one exists and step % pair_every == 0, else a white-noise pair */
+int pic_learned_train(pic_world* w, int steps, double lr, int pair_every, double* mean_loss);
 
 /* ---- Interaction: MC_MEX_Ionization (ch4/v3/src/Interactions.h:98-143) ------------------
  * Background-gas form: the neutral species is a uniform Maxwellian gas (density n_neutral,

@@ -192,7 +192,7 @@ POISSON_CASES = {
 
 
 @pytest.mark.parametrize("case", sorted(POISSON_CASES))
-@pytest.mark.parametrize("method", ["rbsor", "pcg"])
+@pytest.mark.parametrize("method", ["rbsor", "pcg", "learned"])
 def test_poisson_matches_oracle(pic, port, case, method):
     c = POISSON_CASES[case]
     g = port.grid(c["nn"], c["x0"], c["xm"], periodic=c["per"], boxes=[(b[0], b[1]) for b in c["boxes"]])
@@ -208,7 +208,8 @@ def test_poisson_matches_oracle(pic, port, case, method):
     phi0 = W.phi  # Dirichlet values as set by the library
     W.rho = rho
     rho32 = W.rho  # the device keeps rho in FP32: give the oracle the same input
-    S = pic.PotentialSolver(W, 20000, 1e-9, pic.SOLVER_RBSOR if method == "rbsor" else pic.SOLVER_PCG, omega=1.8)
+    solver = {"rbsor": pic.SOLVER_RBSOR, "pcg": pic.SOLVER_PCG, "learned": pic.SOLVER_LEARNED}[method]
+    S = pic.PotentialSolver(W, 20000, 1e-9, solver, omega=1.8)
     assert S.solve(raise_on_fail=True)
     assert S.rel <= 1e-9
     phi = W.phi
@@ -522,8 +523,12 @@ def test_box_thermal_loader_matches_reference_distribution(pic, port):
     assert np.all(p["w"] == 10.0)
     lo, hi = np.array(c) - np.array(s) / 2, np.array(c) + np.array(s) / 2
     assert np.all(p["pos"] >= lo - 1e-12) and np.all(p["pos"] < hi + 1e-12)
-    sp_g = np.sort(np.linalg.norm(p["vel"], axis=1))
-    sp_r = np.sort(np.linalg.norm(ref["vel"], axis=1))
-    q = np.linspace(0.05, 0.95, 19)
-    assert np.allclose(np.quantile(sp_g, q), np.quantile(sp_r, q), rtol=0.01)
+    stats = pytest.importorskip("scipy.stats")
+    sp_g = np.linalg.norm(p["vel"], axis=1)
+    sp_r = np.linalg.norm(ref["vel"], axis=1)
+    # different random streams: two-sample Kolmogorov-Smirnov tests of the speed and of each
+    # velocity component (19 200 draws each; a correct sampler fails at p < 1e-4 once in 10^4)
+    assert stats.ks_2samp(sp_g, sp_r).pvalue > 1e-4
+    for ax in range(3):
+        assert stats.ks_2samp(p["vel"][:, ax], ref["vel"][:, ax]).pvalue > 1e-4
     assert np.all(np.abs(p["vel"].mean(0)) <= 0.01 * sp_r.mean())
