@@ -14,6 +14,7 @@
 //   (L x)_p = D_p x_p - sum_{q FREE or FIXED} c_q x_q,   D_p = sum_{q not MIRROR} c_q,  c = 1/dx^2.
 // kind[n] (uint16): bits 0-1 node kind, bits 2-7 "neighbour d is MIRROR", bits 8-13
 // "neighbour d is FIXED"; direction order -x +x -y +y -z +z.
+#include "pic_ff.cuh"
 #include "pic_stencil.cuh"
 
 namespace pic {
@@ -95,9 +96,14 @@ void launch_den_avg(float* avg, const float* den, int nv, float a, float b, cuda
 }
 
 // ------------------------------------------------------------------------------------
-// E = -grad(phi): central inside, second-order one-sided on non-periodic faces
+// E = -grad(phi): central inside, second-order one-sided on non-periodic faces.  Potential
+// differences are taken on the float-float values (exact high parts), the scaling in FP32.
 // ------------------------------------------------------------------------------------
-__global__ void k_efield(GridDev g, const double* __restrict__ phi, float4* __restrict__ ef) {
+__device__ __forceinline__ float ffd(float2 a, float2 b) {
+    FF d = ff_diff(a, b);
+    return d.hi + d.lo;
+}
+__global__ void k_efield(GridDev g, const float2* __restrict__ phi, float4* __restrict__ ef) {
     const int stride[3] = {1, g.ni, g.ni * g.nj}, nn[3] = {g.ni, g.nj, g.nk};
     float inv2[3];
     for (int d = 0; d < 3; d++) inv2[d] = (float)(1.0 / (2.0 * g.dxd[d]));
@@ -107,43 +113,49 @@ __global__ void k_efield(GridDev g, const double* __restrict__ phi, float4* __re
         float e[3];
         for (int d = 0; d < 3; d++) {
             const int c = ijk[d], st = stride[d], N = nn[d];
-            double v;  // the difference of potentials is taken in FP64, the scaling in FP32
+            float v;
             if (g.periodic[d]) {
                 int cc = (c == N - 1) ? 0 : c;
                 int base = n - (c - cc) * st;
                 int im = base + (((cc == 0) ? N - 2 : cc - 1) - cc) * st;
                 int ip = base + (((cc + 1 == N - 1) ? 0 : cc + 1) - cc) * st;
-                v = phi[im] - phi[ip];
+                v = ffd(phi[im], phi[ip]);
             } else if (N == 2) {
-                v = c == 0 ? 2.0 * (phi[n] - phi[n + st]) : 2.0 * (phi[n - st] - phi[n]);  // first order
+                v = c == 0 ? 2.f * ffd(phi[n], phi[n + st]) : 2.f * ffd(phi[n - st], phi[n]);  // first order
             } else if (c == 0) {
-                v = 3 * phi[n] - 4 * phi[n + st] + phi[n + 2 * st];
+                // 3 phi_0 - 4 phi_1 + phi_2 = 3 (phi_0 - phi_1) - (phi_1 - phi_2)
+                v = 3.f * ffd(phi[n], phi[n + st]) - ffd(phi[n + st], phi[n + 2 * st]);
             } else if (c == N - 1) {
-                v = -phi[n - 2 * st] + 4 * phi[n - st] - 3 * phi[n];
+                // -phi_{-2} + 4 phi_{-1} - 3 phi_0 = 3 (phi_{-1} - phi_0) - (phi_{-2} - phi_{-1})
+                v = 3.f * ffd(phi[n - st], phi[n]) - ffd(phi[n - 2 * st], phi[n - st]);
             } else {
-                v = phi[n - st] - phi[n + st];
+                v = ffd(phi[n - st], phi[n + st]);
             }
-            e[d] = (float)v * inv2[d];
+            e[d] = v * inv2[d];
         }
         ef[n] = make_float4(e[0], e[1], e[2], 0.f);
     }
 }
-void launch_efield(const GridDev& g, const double* phi, float4* ef, cudaStream_t s, int grid) {
+void launch_efield(const GridDev& g, const float2* phi, float4* ef, cudaStream_t s, int grid) {
     k_efield<<<grid, 256, 0, s>>>(g, phi, ef);
 }
 
 // ------------------------------------------------------------------------------------
-// FP64 residual of the reduced system, optionally after phi += e (ping-pong buffers)
+// Residual of the reduced system in float-float, optionally after phi += e (ping-pong buffers)
 //   r = b - L phi,  b = rho/eps0 + sum_{FIXED q} c_q phi_q ; partials: |r|^2, |b|^2
+// (L phi)_p = sum_ax c_ax ((phi_p - phi_minus) + (phi_p - phi_plus)), a mirror neighbour taking
+// phi_p: the differences are error-free in their high parts, the products by c and the sums are
+// float-float, so r carries about 48 bits like an FP64 residual, on the FP32 pipe.  The
+// correction's part L e is FP32 (e is small against phi).  The kernel also records rho and the
+// FP32 boundary part of b, from which the next solve updates r without a full pass.
 // ------------------------------------------------------------------------------------
-__global__ void k_residual(GridDev g, const double* __restrict__ phi_in, double* __restrict__ phi_out,
+__global__ void k_residual(GridDev g, const float2* __restrict__ phi_in, float2* __restrict__ phi_out,
                            const float* __restrict__ e, const float* __restrict__ rho,
-                           const uint16_t* __restrict__ kind, float* __restrict__ r, double* part, int apply_e) {
-    // L(phi)_p = sum_axes c ((phi_p - phi_minus) + (phi_p - phi_plus)), a mirror neighbour
-    // taking phi_p: differences of neighbouring potentials in FP64, so the residual keeps FP64
-    // accuracy (12 FP64 operations per node)
-    const double cd[3] = {1.0 / (g.dxd[0] * g.dxd[0]), 1.0 / (g.dxd[1] * g.dxd[1]), 1.0 / (g.dxd[2] * g.dxd[2])};
-    const double inv_eps0 = 1.0 / kEps0;
+                           const uint16_t* __restrict__ kind, float* __restrict__ r, double* part, int apply_e,
+                           float* __restrict__ rho_prev, float* __restrict__ bfix_out) {
+    FF cf[3];
+    for (int ax = 0; ax < 3; ax++) cf[ax] = ff_from_double(1.0 / (g.dxd[ax] * g.dxd[ax]));
+    const FF ie = ff_from_double(1.0 / kEps0);
     float acc_r = 0.f, acc_b = 0.f;  // per-thread sums in FP32, block and grid sums in FP64
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
         uint16_t kd = kind[n];
@@ -156,46 +168,79 @@ __global__ void k_residual(GridDev g, const double* __restrict__ phi_in, double*
         node_ijk(g, n, i, j, k);
         Stencil s;
         stencil(g, i, j, k, s);
-        const double pp = phi_in[n];
-        double nb[3];
+        const float2 pp = phi_in[n];
+        FF lphi{0.f, 0.f};
         float bfix = 0.f, le = 0.f;
         const float ep = apply_e ? e[n] : 0.f;
 #pragma unroll
         for (int ax = 0; ax < 3; ax++) {
             const int dm = 2 * ax, dp = 2 * ax + 1;
             const bool mm = kd & (1u << (2 + dm)), mp = kd & (1u << (2 + dp));
-            const double pm = mm ? pp : phi_in[s.q[dm]];
-            const double pq = mp ? pp : phi_in[s.q[dp]];
-            nb[ax] = (pp - pm) + (pp - pq);
+            const float2 pm = mm ? pp : phi_in[s.q[dm]];
+            const float2 pq = mp ? pp : phi_in[s.q[dp]];
+            const FF d1 = ff_diff(pp, pm), d2 = ff_diff(pp, pq);
+            FF sd = two_sum(d1.hi, d2.hi);
+            sd.lo += d1.lo + d2.lo;
+            lphi = ff_add(lphi, ff_mul(cf[ax], sd));
             if (apply_e) le += s.c[dm] * ((2.f * ep - (mm ? ep : e[s.q[dm]])) - (mp ? ep : e[s.q[dp]]));
-            if (kd & (1u << (8 + dm))) bfix += s.c[dm] * (float)pm;
-            if (kd & (1u << (8 + dp))) bfix += s.c[dp] * (float)pq;
+            if (kd & (1u << (8 + dm))) bfix += s.c[dm] * pm.x;
+            if (kd & (1u << (8 + dp))) bfix += s.c[dp] * pq.x;
         }
-        double lphi = fma(cd[2], nb[2], fma(cd[1], nb[1], cd[0] * nb[0]));
-        if (apply_e) lphi += (double)le;
-        // the source rho / eps0 in FP64: an FP32 product alone would floor the residual near 3e-8
-        const double src = (double)rho[n] * inv_eps0;
-        const double res = src - lphi;
-        if (apply_e) phi_out[n] = pp + (double)ep;
-        const float rf = (float)res;
+        if (apply_e) lphi = ff_add_f(lphi, le);
+        const float rh = rho[n];
+        FF src = two_prod(rh, ie.hi);
+        src.lo += rh * ie.lo;
+        const FF res = ff_add(src, ff_neg(lphi));
+        if (apply_e) {
+            const FF np = ff_add_f(FF{pp.x, pp.y}, ep);
+            phi_out[n] = make_float2(np.hi, np.lo);
+        }
+        const float rf = res.hi + res.lo;
         r[n] = rf;
-        const float b = (float)src + bfix;
+        const float b = src.hi + bfix;
         acc_r += rf * rf;
+        acc_b += b * b;
+        if (rho_prev) rho_prev[n] = rh;
+        if (bfix_out) bfix_out[n] = bfix;
+    }
+    double acc[2] = {acc_r, acc_b};
+    block_partials<2>(acc, part, kParts);
+}
+void launch_residual(const GridDev& g, SolveWork& w, int apply_e, cudaStream_t s, int grid, float* rho_prev,
+                     float* bfix_out) {
+    const float2* in = w.phi;
+    float2* out = apply_e ? w.phi_alt : w.phi;
+    k_residual<<<grid, 256, 0, s>>>(g, in, out, w.e, w.rho, reinterpret_cast<const uint16_t*>(w.kind), w.r, w.part,
+                                     apply_e, rho_prev, bfix_out);
+    if (apply_e) {
+        float2* t = w.phi;
+        w.phi = w.phi_alt;
+        w.phi_alt = t;
+    }
+}
+// residual of the next solve without an FP64 pass: r += (rho - rho_prev) / eps0 on FREE nodes
+// (r holds the FP64 residual of the current phi, rounded to FP32); partials |r|^2, |b|^2
+__global__ void k_rhs_update(GridDev g, float* __restrict__ r, const float* __restrict__ rho,
+                             float* __restrict__ rho_prev, const float* __restrict__ bfix,
+                             const uint16_t* __restrict__ kind, double* part) {
+    const float inv_eps0_f = (float)(1.0 / kEps0);
+    float acc_r = 0.f, acc_b = 0.f;
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
+        if ((kind[n] & 3) != kFree) continue;
+        const float rh = rho[n];
+        const float rn = r[n] + (rh - rho_prev[n]) * inv_eps0_f;
+        r[n] = rn;
+        rho_prev[n] = rh;
+        const float b = rh * inv_eps0_f + bfix[n];
+        acc_r += rn * rn;
         acc_b += b * b;
     }
     double acc[2] = {acc_r, acc_b};
     block_partials<2>(acc, part, kParts);
 }
-void launch_residual(const GridDev& g, SolveWork& w, int apply_e, cudaStream_t s, int grid) {
-    const double* in = w.phi;
-    double* out = apply_e ? w.phi_alt : w.phi;
-    k_residual<<<grid, 256, 0, s>>>(g, in, out, w.e, w.rho, reinterpret_cast<const uint16_t*>(w.kind), w.r, w.part,
-                                     apply_e);
-    if (apply_e) {
-        double* t = w.phi;
-        w.phi = w.phi_alt;
-        w.phi_alt = t;
-    }
+void launch_rhs_update(const GridDev& g, SolveWork& w, float* rho_prev, const float* bfix, cudaStream_t s, int grid) {
+    k_rhs_update<<<grid, 256, 0, s>>>(g, w.r, w.rho, rho_prev, bfix, reinterpret_cast<const uint16_t*>(w.kind),
+                                       w.part);
 }
 // sums nslots consecutive partial rows (grid-sized) into out[0..nslots)
 __global__ void k_reduce_partials(const double* part, int nblocks, double* out) {
@@ -411,7 +456,7 @@ void launch_pcg_iter_impl(const GridDev& g, SolveWork& w, float* d_in, float* d_
 // ------------------------------------------------------------------------------------
 // MIRROR nodes take the clamped interior value, then ALIAS nodes their periodic source
 // ------------------------------------------------------------------------------------
-__global__ void k_fill_mirror(GridDev g, double* phi, const uint16_t* kind) {
+__global__ void k_fill_mirror(GridDev g, float2* phi, const uint16_t* kind) {
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
         if ((kind[n] & 3) != kMirror) continue;
         int ijk[3], nn[3] = {g.ni, g.nj, g.nk};
@@ -421,7 +466,7 @@ __global__ void k_fill_mirror(GridDev g, double* phi, const uint16_t* kind) {
         phi[n] = phi[(ijk[2] * g.nj + ijk[1]) * g.ni + ijk[0]];
     }
 }
-__global__ void k_fill_alias(GridDev g, double* phi, const uint16_t* kind) {
+__global__ void k_fill_alias(GridDev g, float2* phi, const uint16_t* kind) {
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
         if ((kind[n] & 3) != kAlias) continue;
         int ijk[3], nn[3] = {g.ni, g.nj, g.nk};
@@ -431,7 +476,7 @@ __global__ void k_fill_alias(GridDev g, double* phi, const uint16_t* kind) {
         phi[n] = phi[(ijk[2] * g.nj + ijk[1]) * g.ni + ijk[0]];
     }
 }
-void launch_fill_aux(const GridDev& g, double* phi, const uint8_t* kind, cudaStream_t s, int grid) {
+void launch_fill_aux(const GridDev& g, float2* phi, const uint8_t* kind, cudaStream_t s, int grid) {
     const uint16_t* kd = reinterpret_cast<const uint16_t*>(kind);
     k_fill_mirror<<<grid, 256, 0, s>>>(g, phi, kd);
     k_fill_alias<<<grid, 256, 0, s>>>(g, phi, kd);

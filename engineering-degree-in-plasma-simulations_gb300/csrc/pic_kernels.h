@@ -84,12 +84,12 @@ struct FinalizeArgs {
     float* rho;
 };
 void launch_finalize_rho(const FinalizeArgs& a, cudaStream_t s, int grid);
-void launch_efield(const GridDev& g, const double* phi, float4* ef, cudaStream_t s, int grid);
+void launch_efield(const GridDev& g, const float2* phi, float4* ef, cudaStream_t s, int grid);
 void launch_kinds(const GridDev& g, uint8_t* kind, cudaStream_t s);
 
 struct SolveWork {
-    double* phi;      // master potential (FIXED nodes hold their values)
-    double* phi_alt;  // ping-pong partner
+    float2* phi;      // master potential, float-float (FIXED nodes hold their values)
+    float2* phi_alt;  // ping-pong partner
     const float* rho;
     const uint8_t* kind;
     float* r;         // FP32 residual / right-hand side of the correction equation
@@ -102,13 +102,15 @@ struct SolveWork {
     int* flag;        // [0] inner converged
 };
 constexpr int kParts = 1024;
-void launch_residual(const GridDev& g, SolveWork& w, int apply_e, cudaStream_t s, int grid);
+void launch_residual(const GridDev& g, SolveWork& w, int apply_e, cudaStream_t s, int grid, float* rho_prev,
+                     float* bfix_out);
+void launch_rhs_update(const GridDev& g, SolveWork& w, float* rho_prev, const float* bfix, cudaStream_t s, int grid);
 void launch_reduce_partials(const double* part, int nslots, int nblocks, double* out, cudaStream_t s);
 void launch_rbsor_sweeps(const GridDev& g, SolveWork& w, float omega, int sweeps, cudaStream_t s, int grid);
 void launch_pcg_init(const GridDev& g, SolveWork& w, cudaStream_t s, int grid);
 void launch_pcg_iter_impl(const GridDev& g, SolveWork& w, float* d_in, float* d_out, int it, double target_rr,
                           cudaStream_t s, int grid);
-void launch_fill_aux(const GridDev& g, double* phi, const uint8_t* kind, cudaStream_t s, int grid);
+void launch_fill_aux(const GridDev& g, float2* phi, const uint8_t* kind, cudaStream_t s, int grid);
 void launch_den_avg(float* avg, const float* den, int nv, float a, float b, cudaStream_t s, int grid);
 
 }  // namespace pic

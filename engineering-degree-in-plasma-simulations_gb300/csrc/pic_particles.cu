@@ -196,6 +196,17 @@ __device__ __forceinline__ int move_particle(const PushArgs& a, int i, int j, in
     return pack_cell(i, j, k);
 }
 
+// round-to-nearest conversion of a non-negative float below 2^64 to a 64-bit integer through two
+// 32-bit conversions, bit-identical to __float2ull_rn: hi = floor(x / 2^32) and lo = x - hi 2^32
+// are exact in FP32 (lo < 2^32 keeps at most 24 significant bits of x), and x is an integer
+// whenever hi > 0.  64-bit conversions are slow on this GPU; 32-bit ones run on the integer and
+// conversion units at full rate.
+__device__ __forceinline__ unsigned long long f2u64_rn(float x) {
+    const float hi = floorf(x * 0x1p-32f);
+    const float lo = fmaf(hi, -0x1p32f, x);
+    return ((unsigned long long)__float2uint_rz(hi) << 32) + __float2uint_rn(lo);
+}
+
 // the eight corner contributions of weight w at offsets o as 64-bit fixed point
 struct Corners {
     unsigned long long q[8];  // order 000 100 010 110 001 101 011 111 (x fastest)
@@ -204,9 +215,8 @@ __device__ __forceinline__ void corner_values(float w, float3 o, float scale, Co
     float wx1 = o.x, wx0 = 1.f - o.x, wy1 = o.y, wy0 = 1.f - o.y, wz1 = o.z, wz0 = 1.f - o.z;
     float s = w * scale;
     float s00 = s * wx0 * wy0, s10 = s * wx1 * wy0, s01 = s * wx0 * wy1, s11 = s * wx1 * wy1;
-    unsigned long long v[8] = {__float2ull_rn(s00 * wz0), __float2ull_rn(s10 * wz0), __float2ull_rn(s01 * wz0),
-                               __float2ull_rn(s11 * wz0), __float2ull_rn(s00 * wz1), __float2ull_rn(s10 * wz1),
-                               __float2ull_rn(s01 * wz1), __float2ull_rn(s11 * wz1)};
+    unsigned long long v[8] = {f2u64_rn(s00 * wz0), f2u64_rn(s10 * wz0), f2u64_rn(s01 * wz0), f2u64_rn(s11 * wz0),
+                               f2u64_rn(s00 * wz1), f2u64_rn(s10 * wz1), f2u64_rn(s01 * wz1), f2u64_rn(s11 * wz1)};
 #pragma unroll
     for (int c8 = 0; c8 < 8; c8++) c.q[c8] = add ? c.q[c8] + v[c8] : v[c8];
 }
