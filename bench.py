@@ -476,14 +476,15 @@ def poisson_bench(pic, n, seed=5, train_steps=300):
         W.phi = phi0
         S.solve()
     lp.collect(False)
-    loss_first = lp.train(10)
-    loss_last = lp.train(train_steps - 10) if train_steps > 10 else loss_first
+    rounds = []
+    for _ in range(max(1, train_steps // 100)):
+        loss, before, after, kept = lp.train(100)
+        rounds.append({"loss": loss, "val_iters_before": before, "val_iters_after": after, "kept": kept})
     W.synchronize()
     train_s = time.perf_counter() - t0
     W.rho = rho_test
     out["learned"] = timed(pic.SOLVER_LEARNED)
-    out["learned"]["training"] = {"pair_solves": 4, "steps": train_steps, "seconds": train_s,
-                                  "loss_first10": loss_first, "loss_rest": loss_last}
+    out["learned"]["training"] = {"pair_solves": 4, "steps": train_steps, "seconds": train_s, "rounds": rounds}
     out["speedup_vs_pcg"] = out["pcg"]["seconds"] / out["learned"]["seconds"]
     out["speedup_vs_rbsor"] = out["rbsor"]["seconds"] / out["learned"]["seconds"]
     W.close()

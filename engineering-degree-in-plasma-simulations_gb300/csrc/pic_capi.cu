@@ -118,6 +118,7 @@ struct pic_world {
     float* bfix = nullptr;  // FP32 boundary part of b per node
     bool rhs_valid = false;
     int lp_collect = 0;     // store (first residual, total correction) of each solve as a training pair
+    long lp_fallbacks = 0;  // learned solves handed to Jacobi-PCG
     uint64_t lp_seed = 0x1ea2d5eedull;
     // collisions
     bool mcc_on = false;
@@ -1122,12 +1123,65 @@ int residual_update(pic_world* w, SolveWork& sw, double& r2, double& b2) {
 
 int ensure_lp_train(pic_world* w);
 
+constexpr int kLearnedInnerCap = 400;  // iterations of one learned inner solve before falling back
+
+// FP32 flexible CG with the learned preconditioner on L e = r (w->r), e from zero, until
+// r.r <= target or cap iterations; *done = iterations, *conv = reached the target
+int learned_inner(pic_world* w, SolveWork& sw, double target, int cap, int* done, bool* conv) {
+    const int grid = w->grid_nodes;
+    {
+        Scope sc(w, "poisson", 4 + 2 * w->lp->nlev);
+        launch_lpcg_init(w->g, sw, *w->lp, w->stream, grid, w->sms);
+    }
+    float* din = w->d;
+    float* dout = w->d2;
+    int it = 0;
+    *done = 0;
+    *conv = false;
+    while (it < cap) {
+        int batch = std::min(4, cap - it);
+        {
+            Scope sc(w, "poisson", (1 + 2 * w->lp->nlev) * batch);
+            for (int b = 0; b < batch; b++) {
+                launch_lpcg_iter(w->g, sw, *w->lp, din, dout, it, target, w->stream, grid, w->sms);
+                std::swap(din, dout);
+                it++;
+            }
+        }
+        CU(cudaMemcpyAsync(w->h_flag, w->flag, 2 * sizeof(int), cudaMemcpyDeviceToHost, w->stream));
+        CU(cudaStreamSynchronize(w->stream));
+        if (w->h_flag[0]) {
+            *done = w->h_flag[1];  // the batch stopped at iteration flag[1]
+            *conv = true;
+            return PIC_OK;
+        }
+    }
+    *done = it;
+    return PIC_OK;
+}
+
+// iterations the learned preconditioner needs to reduce the residual r (FP32, node array) by
+// 1e-6 from a zero start (at most cap); the validation of a training round
+int learned_validation_iters(pic_world* w, const float* r, int cap, int* iters) {
+    w->rhs_valid = false;
+    CU(cudaMemcpyAsync(w->r, r, sizeof(float) * w->g.nv, cudaMemcpyDeviceToDevice, w->stream));
+    launch_lp_norm2(w->r, w->g.nv, w->part, w->scal + 12, w->stream, w->grid_nodes);
+    CU(cudaMemcpyAsync(w->h_scal, w->scal + 12, sizeof(double), cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    SolveWork sw = solve_work(w);
+    bool conv = false;
+    int rc = learned_inner(w, sw, 1e-12 * w->h_scal[0], cap, iters, &conv);
+    if (!conv) *iters = cap;
+    return rc;
+}
+
 int solve_impl(pic_world* w, int* iters_out, double* rel_out) {
     SolveWork sw = solve_work(w);
     double r2, b2;
     // an FP32 update of the last FP64 residual when phi is unchanged since; the answer is always
     // certified by an FP64 residual below
     bool estimated = w->rhs_valid;
+    bool use_pcg = false;  // set when the learned preconditioner stalls in this solve
     int rc = estimated ? residual_update(w, sw, r2, b2) : residual_norms(w, sw, 0, r2, b2);
     if (rc) return rc;
     const bool collect = w->lp_collect && w->method != PIC_SOLVER_RBSOR;
@@ -1153,6 +1207,10 @@ int solve_impl(pic_world* w, int* iters_out, double* rel_out) {
         if (!(iters < w->max_it && outer < 1000)) break;
         outer++;
         estimated = false;
+        if (w->method == PIC_SOLVER_LEARNED && !use_pcg) {
+            int lrc = ensure_lp(w);
+            if (lrc) return lrc;
+        }
         if (w->method == PIC_SOLVER_RBSOR) {
             int sweeps = std::min(25, w->max_it - iters);
             {
@@ -1161,37 +1219,19 @@ int solve_impl(pic_world* w, int* iters_out, double* rel_out) {
                 launch_rbsor_sweeps(w->g, sw, (float)w->omega, sweeps, w->stream, grid);
             }
             iters += sweeps;
-        } else if (w->method == PIC_SOLVER_LEARNED) {
+        } else if (w->method == PIC_SOLVER_LEARNED && !use_pcg) {
             // inner FP32 flexible CG with the learned multilevel preconditioner, to eta = 1e-3 of
-            // the current residual (or the final target)
-            int lrc = ensure_lp(w);
-            if (lrc) return lrc;
+            // the current residual (or the final target); a preconditioner that stalls hands the
+            // rest of this solve to Jacobi-PCG
             double target = std::max(1e-6 * r2, 0.09 * w->tol * w->tol * b2);
-            {
-                Scope sc(w, "poisson", 4 + 2 * w->lp->nlev);
-                launch_lpcg_init(w->g, sw, *w->lp, w->stream, grid, w->sms);
-            }
-            float* din = w->d;
-            float* dout = w->d2;
-            int it = 0;
-            for (;;) {
-                int batch = std::min(4, w->max_it - iters);
-                if (batch <= 0) break;
-                {
-                    Scope sc(w, "poisson", (1 + 2 * w->lp->nlev) * batch);
-                    for (int b = 0; b < batch; b++) {
-                        launch_lpcg_iter(w->g, sw, *w->lp, din, dout, it, target, w->stream, grid, w->sms);
-                        std::swap(din, dout);
-                        it++;
-                    }
-                }
-                CU(cudaMemcpyAsync(w->h_flag, w->flag, 2 * sizeof(int), cudaMemcpyDeviceToHost, w->stream));
-                CU(cudaStreamSynchronize(w->stream));
-                if (w->h_flag[0]) {
-                    iters += w->h_flag[1] - (it - batch);  // the batch stopped at iteration flag[1]
-                    break;
-                }
-                iters += batch;
+            int done = 0;
+            bool conv = false;
+            rc = learned_inner(w, sw, target, std::min(kLearnedInnerCap, w->max_it - iters), &done, &conv);
+            if (rc) return rc;
+            iters += done;
+            if (!conv) {
+                use_pcg = true;
+                w->lp_fallbacks++;
             }
         } else {
             // inner FP32 flexible PCG to eta = 1e-3 of the current residual (or the final target)
@@ -1380,16 +1420,32 @@ extern "C" int pic_learned_loss_grad(pic_world* w, const double* r, const double
     return lp_check_err(w);
 }
 // steps of Adam on the energy-norm loss; each step uses a stored solve pair when one exists and
-// (step % pair_every == 0), else a white-noise pair x ~ N(0, 1) on FREE nodes with r = L x
-extern "C" int pic_learned_train(pic_world* w, int steps, double lr, int pair_every, double* mean_loss) {
+// (step % pair_every == 0), else a white-noise pair x ~ N(0, 1) on FREE nodes with r = L x.
+// The round is judged by the solver: the iterations of a validation solve (the latest pair's
+// residual, or a white-noise residual) before and after; a round that needs more is rolled back.
+extern "C" int pic_learned_train(pic_world* w, int steps, double lr, int pair_every, double* mean_loss,
+                                 int* val_iters, int* accepted) {
     if (!w || steps < 0 || !(lr > 0)) return fail(PIC_ERR_ARG, "bad training arguments");
     CU(cudaSetDevice(w->device));
     int rc = ensure_lp_train(w);
     if (rc) return rc;
     LpState& L = *w->lp;
     const GridDev& g = w->g;
+    const int np = lp_npairs(L);
+    // validation right-hand side
+    if (np > 0) {
+        CU(cudaMemcpyAsync(lp_train_val(L), lp_pair_r(L, np - 1), sizeof(float) * g.nv, cudaMemcpyDeviceToDevice,
+                           w->stream));
+    } else {
+        launch_lp_noise_pair(g, L, w->kind, w->lp_seed ^ 0x9e3779b97f4a7c15ull, w->stream, w->grid_nodes);
+        CU(cudaMemcpyAsync(lp_train_val(L), lp_train_r(L), sizeof(float) * g.nv, cudaMemcpyDeviceToDevice, w->stream));
+    }
+    int before = 0, after = 0;
+    rc = learned_validation_iters(w, lp_train_val(L), kLearnedInnerCap, &before);
+    if (rc) return rc;
+    CU(cudaMemcpyAsync(lp_train_wprev(L), L.W, sizeof(float) * L.lay.total, cudaMemcpyDeviceToDevice, w->stream));
     double sum = 0;
-    int np = lp_npairs(L), used_pairs = 0;
+    int used_pairs = 0;
     for (int st = 0; st < steps; st++) {
         const float *r, *x;
         if (np > 0 && pair_every > 0 && st % pair_every == 0) {
@@ -1412,8 +1468,24 @@ extern "C" int pic_learned_train(pic_world* w, int steps, double lr, int pair_ev
         sum += h;
     }
     CU(cudaGetLastError());
+    rc = lp_check_err(w);
+    if (rc) return rc;
+    rc = learned_validation_iters(w, lp_train_val(L), kLearnedInnerCap, &after);
+    if (rc) return rc;
+    const bool keep = after <= before;
+    if (!keep) {
+        CU(cudaMemcpyAsync(L.W, lp_train_wprev(L), sizeof(float) * L.lay.total, cudaMemcpyDeviceToDevice, w->stream));
+        launch_lp_prep(L, w->stream);
+        launch_lp_fold(L, w->stream);
+        CU(cudaStreamSynchronize(w->stream));
+    }
     if (mean_loss) *mean_loss = steps ? sum / steps : 0.0;
-    return lp_check_err(w);
+    if (val_iters) {
+        val_iters[0] = before;
+        val_iters[1] = after;
+    }
+    if (accepted) *accepted = keep ? 1 : 0;
+    return PIC_OK;
 }
 
 extern "C" int pic_solver_compute_ef(pic_world* w) {

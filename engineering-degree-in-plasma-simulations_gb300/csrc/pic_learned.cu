@@ -438,6 +438,22 @@ __global__ void k_lpcg_zero(float* e, float* q, int nv, int* flag) {
     }
 }
 
+// |a|^2 over n values into out[0] (deterministic: block partials, then one fixed-order sum)
+__global__ void k_lp_sq(const float* __restrict__ a, int n, double* part) {
+    float f = 0.f;
+    for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < n; x += gridDim.x * blockDim.x) f += a[x] * a[x];
+    double acc[1] = {f};
+    block_partials<1>(acc, part, kParts);
+}
+__global__ void k_lp_sum1(const double* part, int nblocks, double* out) {
+    double t = sum_partials(part, nblocks);
+    if (threadIdx.x == 0) out[0] = t;
+}
+void launch_lp_norm2(const float* a, int n, double* part, double* out, cudaStream_t s, int grid) {
+    k_lp_sq<<<grid, 256, 0, s>>>(a, n, part);
+    k_lp_sum1<<<1, 256, 0, s>>>(part, grid, out);
+}
+
 void launch_lpcg_init(const GridDev& g, SolveWork& w, const LpState& L, cudaStream_t s, int grid, int sms) {
     k_lpcg_zero<<<grid, 256, 0, s>>>(w.e, w.q, g.nv, w.flag);
     cudaMemsetAsync(w.d, 0, sizeof(float) * g.nv, s);
@@ -473,6 +489,8 @@ struct LpTrain {
     float* g[kLpMaxLevels] = {};  // restricted loss gradient, levels >= 1
     float *x = nullptr, *r = nullptr, *e0 = nullptr, *ge = nullptr;  // node arrays
     float *grad = nullptr, *m = nullptr, *v = nullptr, *pscale = nullptr;
+    float* wprev = nullptr;  // weights before a training round (restored when validation rejects it)
+    float* val_r = nullptr;  // right-hand side of the validation solve
     __nv_bfloat16* wbf = nullptr;  // per network level: Wl [C][32], Wm [C][C], Wm^T [C][C], Wp^T [C][32]
     int wbf_off[kLpNetLevels + 1][4] = {};
     double* part = nullptr;  // [32][kParts] partial sums
@@ -850,7 +868,8 @@ void lp_free_train(LpState& L) {
     for (int l = 1; l < kLpMaxLevels; l++)
         if (T->g[l]) cudaFree(T->g[l]);
     for (void* p : {(void*)T->x, (void*)T->r, (void*)T->e0, (void*)T->ge, (void*)T->grad, (void*)T->m, (void*)T->v,
-                    (void*)T->pscale, (void*)T->wbf, (void*)T->part, (void*)T->red, (void*)T->wg, (void*)T->err})
+                    (void*)T->pscale, (void*)T->wbf, (void*)T->part, (void*)T->red, (void*)T->wg, (void*)T->err,
+                    (void*)T->wprev, (void*)T->val_r})
         if (p) cudaFree(p);
     for (int k = 0; k < 4; k++) {
         if (T->pair_r[k]) cudaFree(T->pair_r[k]);
@@ -881,9 +900,9 @@ int lp_alloc_train(const GridDev& g, LpState& L, const float* init_W) {
     }
     for (int l = 1; l < L.nlev; l++)
         LP_CU(cudaMalloc(&T->g[l], sizeof(float) * (size_t)L.dims[l][0] * L.dims[l][1] * L.dims[l][2]));
-    for (float** p : {&T->x, &T->r, &T->e0, &T->ge}) LP_CU(cudaMalloc(p, sizeof(float) * g.nv));
+    for (float** p : {&T->x, &T->r, &T->e0, &T->ge, &T->val_r}) LP_CU(cudaMalloc(p, sizeof(float) * g.nv));
     const int n = L.lay.total;
-    for (float** p : {&T->grad, &T->m, &T->v, &T->pscale}) LP_CU(cudaMalloc(p, sizeof(float) * n));
+    for (float** p : {&T->grad, &T->m, &T->v, &T->pscale, &T->wprev}) LP_CU(cudaMalloc(p, sizeof(float) * n));
     LP_CU(cudaMemset(T->m, 0, sizeof(float) * n));
     LP_CU(cudaMemset(T->v, 0, sizeof(float) * n));
     LP_CU(cudaMemset(T->grad, 0, sizeof(float) * n));
@@ -1048,6 +1067,8 @@ const float* lp_pair_r(const LpState& L, int k) { return L.train->pair_r[k]; }
 const float* lp_pair_x(const LpState& L, int k) { return L.train->pair_x[k]; }
 int lp_npairs(const LpState& L) { return L.train ? L.train->npairs : 0; }
 float* lp_train_x(const LpState& L) { return L.train->x; }
+float* lp_train_val(const LpState& L) { return L.train->val_r; }
+float* lp_train_wprev(const LpState& L) { return L.train->wprev; }
 float* lp_train_r(const LpState& L) { return L.train->r; }
 float* lp_train_grad(const LpState& L) { return L.train->grad; }
 double* lp_train_red(const LpState& L) { return L.train->red; }

@@ -78,6 +78,8 @@ const float* lp_pair_r(const LpState& L, int k);
 const float* lp_pair_x(const LpState& L, int k);
 int lp_npairs(const LpState& L);
 float* lp_train_x(const LpState& L);
+float* lp_train_val(const LpState& L);
+float* lp_train_wprev(const LpState& L);
 float* lp_train_r(const LpState& L);
 float* lp_train_grad(const LpState& L);
 double* lp_train_red(const LpState& L);
@@ -88,6 +90,7 @@ unsigned* lp_train_err(const LpState& L);
 void launch_lp_apply(const GridDev& g, const LpState& L, const float* r, float* z, const uint16_t* kind,
                      const float* q, double* part, const int* flag, cudaStream_t s, int grid_nodes, int sms);
 // flexible CG iteration with the learned preconditioner (see pic_learned.cu)
+void launch_lp_norm2(const float* a, int n, double* part, double* out, cudaStream_t s, int grid);
 void launch_lpcg_init(const GridDev& g, SolveWork& w, const LpState& L, cudaStream_t s, int grid, int sms);
 void launch_lpcg_iter(const GridDev& g, SolveWork& w, const LpState& L, float* d_in, float* d_out, int it,
                       double target_rr, cudaStream_t s, int grid, int sms);

@@ -156,8 +156,11 @@ int pic_learned_loss_grad(pic_world* w, const double* r, const double* x, double
  * (the last four are kept) */
 int pic_learned_collect(pic_world* w, int on);
 /* steps of Adam (learning rate lr relative to each parameter group's size); a step uses a
- * collected pair when one exists and step % pair_every == 0, else a white-noise pair */
-int pic_learned_train(pic_world* w, int steps, double lr, int pair_every, double* mean_loss);
+ * collected pair when one exists and step % pair_every == 0, else a white-noise pair.  The round
+ * is judged by the solver: val_iters[0..1] = iterations of a validation solve before and after;
+ * a round that needs more iterations is rolled back (*accepted = 0). */
+int pic_learned_train(pic_world* w, int steps, double lr, int pair_every, double* mean_loss, int* val_iters,
+                      int* accepted);
 
 /* ---- Interaction: MC_MEX_Ionization (ch4/v3/src/Interactions.h:98-143) ------------------
  * Background-gas form: the neutral species is a uniform Maxwellian gas (density n_neutral,

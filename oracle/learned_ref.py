@@ -193,28 +193,11 @@ def apply_L(e, mask, c, per):
     return mask * out
 
 
-def loss_and_grads(r, x, mask, W, c, per, diags, scale_free=True):
-    """Loss of one pair (r, x) with L x = r, and its gradients with respect to every weight.
-
-    scale_free: the squared sine of the energy-norm angle between e = B r and x,
-        1 - <e, x>_L^2 / (<e, e>_L <x, x>_L)   (CG does not see the scale of B);
-    otherwise the energy-norm error (e - x)^T L (e - x) / x^T L x."""
+def backward(r, mask, W, per, diags, ge):
+    """Gradients of sum(ge * B r) with respect to every weight (ge: the loss gradient at e = B r)."""
     shapes = level_shapes(r.shape)
-    e, (zs, caches) = apply(r, mask, W, per, diags, keep=True)
-    x = mask * x
-    lx = apply_L(x, mask, c, per)
-    le = apply_L(e, mask, c, per)
-    q = np.sum(x * lx)
-    if scale_free:
-        a = np.sum(e * lx)
-        p = np.sum(e * le)
-        loss = 1.0 - a * a / (p * q)
-        ge = (2.0 * a / (p * q)) * ((a / p) * le - lx)
-    else:
-        lerr = le - lx
-        loss = np.sum((e - x) * lerr) / q
-        ge = 2.0 * lerr / q
-    gs = [ge]
+    _, (zs, caches) = apply(r, mask, W, per, diags, keep=True)
+    gs = [mask * ge]
     for l in range(1, len(shapes)):
         gs.append(restrict(gs[-1], per))
     G = {"S0": np.array([np.sum(gs[0] * shift(zs[0], d, per)) for d in TAPS]), "net": []}
@@ -232,7 +215,30 @@ def loss_and_grads(r, x, mask, W, c, per, diags, scale_free=True):
         for t, d in enumerate(TAPS):
             dWl[:, t] = np.tensordot(dh1, shift(z, d, per), axes=([0, 1, 2], [0, 1, 2]))
         G["net"].append({"Wl": dWl, "Wm": dWm, "Wp": dWp})
-    return loss, G
+    return G
+
+
+def loss_and_grads(r, x, mask, W, c, per, diags, scale_free=True):
+    """Loss of one pair (r, x) with L x = r, and its gradients with respect to every weight.
+
+    scale_free: the squared sine of the energy-norm angle between e = B r and x,
+        1 - <e, x>_L^2 / (<e, e>_L <x, x>_L)   (CG does not see the scale of B);
+    otherwise the energy-norm error (e - x)^T L (e - x) / x^T L x."""
+    e = apply(r, mask, W, per, diags)
+    x = mask * x
+    lx = apply_L(x, mask, c, per)
+    le = apply_L(e, mask, c, per)
+    q = np.sum(x * lx)
+    if scale_free:
+        a = np.sum(e * lx)
+        p = np.sum(e * le)
+        loss = 1.0 - a * a / (p * q)
+        ge = (2.0 * a / (p * q)) * ((a / p) * le - lx)
+    else:
+        lerr = le - lx
+        loss = np.sum((e - x) * lerr) / q
+        ge = 2.0 * lerr / q
+    return loss, backward(r, mask, W, per, diags, ge)
 
 
 def fpcg(b, mask, c, per, precond, tol=1e-6, maxit=5000):

@@ -188,10 +188,11 @@ def test_loss_and_gradients_match_oracle(pic):
         assert err <= 0.05, (a, n, err)
 
 
-def test_training_lowers_the_loss_and_keeps_solves_exact(pic):
-    """Online training on the pairs of earlier solves and on white-noise pairs: the loss falls,
-    and the trained preconditioner still drives the solve to the same FP64 residual with far
-    fewer iterations than Jacobi-PCG."""
+def test_training_is_judged_by_the_solver_and_keeps_solves_exact(pic):
+    """Online training on the pairs of earlier solves and on white-noise pairs.  A round is kept
+    only if a validation solve needs no more iterations than before it (otherwise it is rolled
+    back), and the preconditioner still drives the solve to the same FP64 residual with far fewer
+    iterations than Jacobi-PCG."""
     n = 49
     W = pic.World(n, n, n, (0.0, 0.0, 0.0), (0.02, 0.02, 0.02))
     W.set_boundaries((1, 1, 0), (1,) * 6, (0, 0, 0, 0, 0.0, 50.0))
@@ -216,14 +217,20 @@ def test_training_lowers_the_loss_and_keeps_solves_exact(pic):
         W.rho = blobs()
         assert S.solve(raise_on_fail=True)
     lp.collect(False)
-    first = lp.train(20, lr=3e-4, pair_every=2)
-    lp.train(300, lr=3e-4, pair_every=2)
-    last = lp.train(20, lr=3e-4, pair_every=2)
-    assert last < first
+    rho_test = blobs()
     W.phi = phi0
-    W.rho = blobs()
+    W.rho = rho_test
+    assert S.solve(raise_on_fail=True)
+    iters_start = S.iters
+    for _ in range(3):
+        loss, before, after, kept = lp.train(100, lr=1e-4, pair_every=2)
+        assert np.isfinite(loss)
+        assert (after <= before) == kept
+    W.phi = phi0
+    W.rho = rho_test
     assert S.solve(raise_on_fail=True)
     learned_iters, phi_l = S.iters, W.phi
+    assert learned_iters <= iters_start + 3
     W.phi = phi0
     P = pic.PotentialSolver(W, 20000, 1e-8, pic.SOLVER_PCG)
     assert P.solve(raise_on_fail=True)
