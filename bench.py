@@ -564,11 +564,19 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=1_000_000)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--poisson", type=int, default=256, help="n of the n^3 Poisson time-to-1e-6 case (0: skip)")
+    ap.add_argument("--poisson-only", action="store_true",
+                    help="run only the Poisson time-to-1e-6 comparison (the second metric) and print it")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     wl = WORKLOADS[args.workload]
     rank, ws, local = dist_init()
+    if args.poisson_only:
+        if rank == 0 and args.impl != "reference":
+            pic = importlib.import_module(PKG)
+            print(json.dumps({"metric": "Poisson time-to-1e-6 FP64 residual", "unit": "s",
+                              "poisson_time_to_1e-6": poisson_bench(pic, args.poisson or 256)}), flush=True)
+        return
     if args.impl == "reference":
         run_reference(args, wl, rank, ws)
     else:
