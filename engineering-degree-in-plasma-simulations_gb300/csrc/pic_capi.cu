@@ -81,6 +81,9 @@ struct pic_world {
     uint16_t* kind = nullptr;
     float *r = nullptr, *e = nullptr, *d = nullptr, *d2 = nullptr, *q = nullptr, *z = nullptr;
     double* part = nullptr;
+    double* gpart = nullptr;     // block partials of the node-kernel reductions [8][gstride]
+    int gstride = 0;
+    unsigned* ticket = nullptr;  // last-block counter of those reductions
     double* scal = nullptr;
     int* flag = nullptr;
     double* h_scal = nullptr;  // pinned
@@ -417,6 +420,9 @@ SolveWork solve_work(pic_world* w) {
     s.part = w->part;
     s.scal = w->scal;
     s.flag = w->flag;
+    s.gpart = w->gpart;
+    s.gstride = w->gstride;
+    s.ticket = w->ticket;
     return s;
 }
 
@@ -473,6 +479,8 @@ extern "C" int pic_world_create(pic_world** out, int ni, int nj, int nk, const d
          alloc((void**)&w->d2, sizeof(float) * nv) && alloc((void**)&w->q, sizeof(float) * nv) &&
          alloc((void**)&w->z, sizeof(float) * nv) && alloc((void**)&w->part, sizeof(double) * kParts * 8) &&
          alloc((void**)&w->scal, sizeof(double) * 16) && alloc((void**)&w->flag, sizeof(int) * 4) &&
+         alloc((void**)&w->gpart, sizeof(double) * 8 * (size_t)std::max(kParts, node_blocks(nv))) &&
+         alloc((void**)&w->ticket, sizeof(unsigned) * 4) &&
          alloc((void**)&w->cell_count, sizeof(int) * (g.nc + 1)) &&
          alloc((void**)&w->cell_start, sizeof(int) * (g.nc + 1)) &&
          alloc((void**)&w->scan_aux, sizeof(int) * (g.nc / 2048 + 2)) && alloc((void**)&w->err, sizeof(unsigned)) &&
@@ -487,6 +495,8 @@ extern "C" int pic_world_create(pic_world** out, int ni, int nj, int nk, const d
     for (float* p : {w->r, w->e, w->d, w->d2, w->q, w->z}) cudaMemsetAsync(p, 0, sizeof(float) * nv, w->stream);
     cudaMemsetAsync(w->err, 0, sizeof(unsigned), w->stream);
     cudaMemsetAsync(w->flag, 0, sizeof(int) * 4, w->stream);
+    cudaMemsetAsync(w->ticket, 0, sizeof(unsigned) * 4, w->stream);
+    w->gstride = std::max(kParts, node_blocks(nv));
     w->grid_nodes = (int)std::min<long long>(kParts, std::max<long long>(1, (nv + 255) / 256));
     w->grid_parts = w->sms * 8;
     w->grid_push = w->sms * 3;
@@ -525,6 +535,7 @@ extern "C" int pic_world_destroy(pic_world* w) {
     }
     void* ptrs[] = {w->ef,   w->phi,  w->phi_alt, w->rho,        w->kind,       w->r,        w->e,
                     w->d,    w->d2,   w->q,       w->z,          w->part,       w->scal,     w->flag,
+                    w->gpart, w->ticket,
                     w->cell_count,    w->cell_start,             w->scan_aux,   w->err,      w->tE,
                     w->tS,   w->stats,  w->merge_list, w->merge_stats};
     for (void* p : ptrs)
@@ -1093,9 +1104,8 @@ int residual_norms(pic_world* w, SolveWork& sw, int apply_e, double& r2, double&
     }
     w->rhs_valid = false;
     {
-        Scope sc(w, "poisson", 2);
-        launch_residual(w->g, sw, apply_e, w->stream, w->grid_nodes, w->rho_prev, w->bfix);
-        launch_reduce_partials(w->part, 2, w->grid_nodes, w->scal + 8, w->stream);
+        Scope sc(w, "poisson", 1);
+        launch_residual(w->g, sw, apply_e, w->stream, w->rho_prev, w->bfix);
     }
     w->phi = sw.phi;
     w->phi_alt = sw.phi_alt;
@@ -1110,9 +1120,8 @@ int residual_norms(pic_world* w, SolveWork& sw, int apply_e, double& r2, double&
 // the residual of the current phi for the new rho from the last FP64 residual (FP32 update)
 int residual_update(pic_world* w, SolveWork& sw, double& r2, double& b2) {
     {
-        Scope sc(w, "poisson", 2);
-        launch_rhs_update(w->g, sw, w->rho_prev, w->bfix, w->stream, w->grid_nodes);
-        launch_reduce_partials(w->part, 2, w->grid_nodes, w->scal + 8, w->stream);
+        Scope sc(w, "poisson", 1);
+        launch_rhs_update(w->g, sw, w->rho_prev, w->bfix, w->stream);
     }
     CU(cudaMemcpyAsync(w->h_scal, w->scal + 8, sizeof(double) * 2, cudaMemcpyDeviceToHost, w->stream));
     CU(cudaStreamSynchronize(w->stream));
@@ -1128,10 +1137,9 @@ constexpr int kLearnedInnerCap = 400;  // iterations of one learned inner solve 
 // FP32 flexible CG with the learned preconditioner on L e = r (w->r), e from zero, until
 // r.r <= target or cap iterations; *done = iterations, *conv = reached the target
 int learned_inner(pic_world* w, SolveWork& sw, double target, int cap, int* done, bool* conv) {
-    const int grid = w->grid_nodes;
     {
         Scope sc(w, "poisson", 4 + 2 * w->lp->nlev);
-        launch_lpcg_init(w->g, sw, *w->lp, w->stream, grid, w->sms);
+        launch_lpcg_init(w->g, sw, *w->lp, w->stream, w->sms);
     }
     float* din = w->d;
     float* dout = w->d2;
@@ -1143,7 +1151,7 @@ int learned_inner(pic_world* w, SolveWork& sw, double target, int cap, int* done
         {
             Scope sc(w, "poisson", (1 + 2 * w->lp->nlev) * batch);
             for (int b = 0; b < batch; b++) {
-                launch_lpcg_iter(w->g, sw, *w->lp, din, dout, it, target, w->stream, grid, w->sms);
+                launch_lpcg_iter(w->g, sw, *w->lp, din, dout, it, target, w->stream, w->sms);
                 std::swap(din, dout);
                 it++;
             }
@@ -1216,7 +1224,7 @@ int solve_impl(pic_world* w, int* iters_out, double* rel_out) {
             {
                 Scope sc(w, "poisson", 3 * sweeps);
                 CU(cudaMemsetAsync(w->e, 0, sizeof(float) * w->g.nv, w->stream));
-                launch_rbsor_sweeps(w->g, sw, (float)w->omega, sweeps, w->stream, grid);
+                launch_rbsor_sweeps(w->g, sw, (float)w->omega, sweeps, w->stream);
             }
             iters += sweeps;
         } else if (w->method == PIC_SOLVER_LEARNED && !use_pcg) {
@@ -1237,8 +1245,8 @@ int solve_impl(pic_world* w, int* iters_out, double* rel_out) {
             // inner FP32 flexible PCG to eta = 1e-3 of the current residual (or the final target)
             double target = std::max(1e-6 * r2, 0.09 * w->tol * w->tol * b2);
             {
-                Scope sc(w, "poisson", 2);
-                launch_pcg_init(w->g, sw, w->stream, grid);
+                Scope sc(w, "poisson", 1);
+                launch_pcg_init(w->g, sw, w->stream);
             }
             float* din = w->d;
             float* dout = w->d2;
@@ -1249,7 +1257,7 @@ int solve_impl(pic_world* w, int* iters_out, double* rel_out) {
                 {
                     Scope sc(w, "poisson", 2 * batch);
                     for (int b = 0; b < batch; b++) {
-                        launch_pcg_iter_impl(w->g, sw, din, dout, it, target, w->stream, grid);
+                        launch_pcg_iter_impl(w->g, sw, din, dout, it, target, w->stream);
                         std::swap(din, dout);
                         it++;
                     }
@@ -1359,7 +1367,7 @@ extern "C" int pic_learned_apply(pic_world* w, const double* r, double* z) {
     for (int n = 0; n < g.nv; n++) rf[n] = (kind[n] & 3) == kFree ? (float)r[n] : 0.f;
     w->rhs_valid = false;
     CU(cudaMemcpyAsync(w->r, rf.data(), sizeof(float) * g.nv, cudaMemcpyHostToDevice, w->stream));
-    launch_lp_apply(g, *w->lp, w->r, w->z, w->kind, nullptr, nullptr, nullptr, w->stream, w->grid_nodes, w->sms);
+    launch_lp_apply(g, *w->lp, w->r, w->z, w->kind, nullptr, nullptr, nullptr, w->stream, w->sms);
     CU(cudaGetLastError());
     CU(cudaMemcpyAsync(rf.data(), w->z, sizeof(float) * g.nv, cudaMemcpyDeviceToHost, w->stream));
     CU(cudaStreamSynchronize(w->stream));

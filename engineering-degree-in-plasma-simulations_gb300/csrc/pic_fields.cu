@@ -149,16 +149,21 @@ void launch_efield(const GridDev& g, const float2* phi, float4* ef, cudaStream_t
 // correction's part L e is FP32 (e is small against phi).  The kernel also records rho and the
 // FP32 boundary part of b, from which the next solve updates r without a full pass.
 // ------------------------------------------------------------------------------------
-__global__ void k_residual(GridDev g, const float2* __restrict__ phi_in, float2* __restrict__ phi_out,
-                           const float* __restrict__ e, const float* __restrict__ rho,
-                           const uint16_t* __restrict__ kind, float* __restrict__ r, double* part, int apply_e,
-                           float* __restrict__ rho_prev, float* __restrict__ bfix_out) {
+__global__ void __launch_bounds__(kNodeThreads) k_residual(
+    GridDev g, const float2* __restrict__ phi_in, float2* __restrict__ phi_out, const float* __restrict__ e,
+    const float* __restrict__ rho, const uint16_t* __restrict__ kind, float* __restrict__ r, double* gpart,
+    int gstride, unsigned* ticket, double* out, int apply_e, float* __restrict__ rho_prev,
+    float* __restrict__ bfix_out) {
     FF cf[3];
     for (int ax = 0; ax < 3; ax++) cf[ax] = ff_from_double(1.0 / (g.dxd[ax] * g.dxd[ax]));
     const FF ie = ff_from_double(1.0 / kEps0);
     float acc_r = 0.f, acc_b = 0.f;  // per-thread sums in FP32, block and grid sums in FP64
-    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
-        uint16_t kd = kind[n];
+    const int base = blockIdx.x * kNodeTile + threadIdx.x;
+#pragma unroll
+    for (int q4 = 0; q4 < kNodeTile / kNodeThreads; q4++) {
+        const int n = base + q4 * kNodeThreads;
+        if (n >= g.nv) break;
+        const uint16_t kd = kind[n];
         if ((kd & 3) != kFree) {
             if (apply_e) phi_out[n] = phi_in[n];
             r[n] = 0.f;
@@ -203,29 +208,37 @@ __global__ void k_residual(GridDev g, const float2* __restrict__ phi_in, float2*
         if (rho_prev) rho_prev[n] = rh;
         if (bfix_out) bfix_out[n] = bfix;
     }
-    double acc[2] = {acc_r, acc_b};
-    block_partials<2>(acc, part, kParts);
+    const float v[2] = {acc_r, acc_b};
+    grid_sum<2>(v, gpart, gstride, ticket, out);
 }
-void launch_residual(const GridDev& g, SolveWork& w, int apply_e, cudaStream_t s, int grid, float* rho_prev,
-                     float* bfix_out) {
+void launch_residual(const GridDev& g, SolveWork& w, int apply_e, cudaStream_t s, float* rho_prev, float* bfix_out) {
     const float2* in = w.phi;
     float2* out = apply_e ? w.phi_alt : w.phi;
-    k_residual<<<grid, 256, 0, s>>>(g, in, out, w.e, w.rho, reinterpret_cast<const uint16_t*>(w.kind), w.r, w.part,
-                                     apply_e, rho_prev, bfix_out);
+    k_residual<<<node_blocks(g.nv), kNodeThreads, 0, s>>>(g, in, out, w.e, w.rho,
+                                                          reinterpret_cast<const uint16_t*>(w.kind), w.r, w.gpart,
+                                                          w.gstride, w.ticket, w.scal + kS_R2, apply_e, rho_prev,
+                                                          bfix_out);
     if (apply_e) {
         float2* t = w.phi;
         w.phi = w.phi_alt;
         w.phi_alt = t;
     }
 }
-// residual of the next solve without an FP64 pass: r += (rho - rho_prev) / eps0 on FREE nodes
-// (r holds the FP64 residual of the current phi, rounded to FP32); partials |r|^2, |b|^2
-__global__ void k_rhs_update(GridDev g, float* __restrict__ r, const float* __restrict__ rho,
-                             float* __restrict__ rho_prev, const float* __restrict__ bfix,
-                             const uint16_t* __restrict__ kind, double* part) {
+// residual of the next solve without a full pass: r += (rho - rho_prev) / eps0 on FREE nodes
+// (r holds the residual of the current phi, rounded to FP32); |r|^2, |b|^2 into out[0..1]
+__global__ void __launch_bounds__(kNodeThreads) k_rhs_update(GridDev g, float* __restrict__ r,
+                                                             const float* __restrict__ rho,
+                                                             float* __restrict__ rho_prev,
+                                                             const float* __restrict__ bfix,
+                                                             const uint16_t* __restrict__ kind, double* gpart,
+                                                             int gstride, unsigned* ticket, double* out) {
     const float inv_eps0_f = (float)(1.0 / kEps0);
     float acc_r = 0.f, acc_b = 0.f;
-    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
+    const int base = blockIdx.x * kNodeTile + threadIdx.x;
+#pragma unroll
+    for (int q4 = 0; q4 < kNodeTile / kNodeThreads; q4++) {
+        const int n = base + q4 * kNodeThreads;
+        if (n >= g.nv) break;
         if ((kind[n] & 3) != kFree) continue;
         const float rh = rho[n];
         const float rn = r[n] + (rh - rho_prev[n]) * inv_eps0_f;
@@ -235,12 +248,13 @@ __global__ void k_rhs_update(GridDev g, float* __restrict__ r, const float* __re
         acc_r += rn * rn;
         acc_b += b * b;
     }
-    double acc[2] = {acc_r, acc_b};
-    block_partials<2>(acc, part, kParts);
+    const float v[2] = {acc_r, acc_b};
+    grid_sum<2>(v, gpart, gstride, ticket, out);
 }
-void launch_rhs_update(const GridDev& g, SolveWork& w, float* rho_prev, const float* bfix, cudaStream_t s, int grid) {
-    k_rhs_update<<<grid, 256, 0, s>>>(g, w.r, w.rho, rho_prev, bfix, reinterpret_cast<const uint16_t*>(w.kind),
-                                       w.part);
+void launch_rhs_update(const GridDev& g, SolveWork& w, float* rho_prev, const float* bfix, cudaStream_t s) {
+    k_rhs_update<<<node_blocks(g.nv), kNodeThreads, 0, s>>>(g, w.r, w.rho, rho_prev, bfix,
+                                                            reinterpret_cast<const uint16_t*>(w.kind), w.gpart,
+                                                            w.gstride, w.ticket, w.scal + kS_R2);
 }
 // sums nslots consecutive partial rows (grid-sized) into out[0..nslots)
 __global__ void k_reduce_partials(const double* part, int nblocks, double* out) {
@@ -318,8 +332,9 @@ __global__ void k_rbsor_seam(GridDev g, float* __restrict__ e, const float* __re
         sor_update(g, e, r, kind, 1.0f, i, j, k);
     }
 }
-void launch_rbsor_sweeps(const GridDev& g, SolveWork& w, float omega, int sweeps, cudaStream_t s, int grid) {
+void launch_rbsor_sweeps(const GridDev& g, SolveWork& w, float omega, int sweeps, cudaStream_t s) {
     const uint16_t* kd = reinterpret_cast<const uint16_t*>(w.kind);
+    const int grid = ((g.ni + 1) / 2 * g.nj * g.nk + 255) / 256;  // one thread per node of a colour
     const bool seam = (g.periodic[0] && ((g.ni - 1) & 1)) || (g.periodic[1] && ((g.nj - 1) & 1)) ||
                       (g.periodic[2] && ((g.nk - 1) & 1));
     for (int it = 0; it < sweeps; it++) {
@@ -336,38 +351,44 @@ void launch_rbsor_sweeps(const GridDev& g, SolveWork& w, float omega, int sweeps
 //   K2: alpha = rz/dq ; e += alpha d' ; r -= alpha q ; z' = r/D ; partials r.z', r.z, r.r
 // scalars: scal[0..1] rz (double-buffered by iteration parity); flag[0] set when r.r <= target
 // ------------------------------------------------------------------------------------
-__global__ void k_pcg_init(GridDev g, const float* __restrict__ r, float* __restrict__ z, float* __restrict__ e,
-                           const uint16_t* __restrict__ kind, double* part, int* flag) {
-    double acc[1] = {0.0};
-    float facc = 0.f;  // per-thread partial in FP32, block and grid sums in FP64
+__global__ void __launch_bounds__(kNodeThreads) k_pcg_init(GridDev g, const float* __restrict__ r,
+                                                           float* __restrict__ z, float* __restrict__ e,
+                                                           float* __restrict__ d, const uint16_t* __restrict__ kind,
+                                                           double* gpart, int gstride, unsigned* ticket,
+                                                           double* scal, int* flag) {
     if (blockIdx.x == 0 && threadIdx.x == 0) flag[0] = 0;
-    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
-        uint16_t kd = kind[n];
+    const float c3[3] = {g.inv_dx[0] * g.inv_dx[0], g.inv_dx[1] * g.inv_dx[1], g.inv_dx[2] * g.inv_dx[2]};
+    float acc = 0.f;
+    const int base = blockIdx.x * kNodeTile + threadIdx.x;
+#pragma unroll
+    for (int q4 = 0; q4 < kNodeTile / kNodeThreads; q4++) {
+        const int n = base + q4 * kNodeThreads;
+        if (n >= g.nv) break;
+        const uint16_t kd = kind[n];
         e[n] = 0.f;
+        d[n] = 0.f;
         if ((kd & 3) != kFree) {
             z[n] = 0.f;
             continue;
         }
-        int i, j, k;
-        node_ijk(g, n, i, j, k);
-        Stencil s;
-        stencil(g, i, j, k, s);
-        float zz = r[n] / diag_of(kd, s);
+        const float rr = r[n];
+        const float zz = rr * inv_diag_of(kd, c3);
         z[n] = zz;
-        facc += r[n] * zz;
+        acc += rr * zz;
     }
-    acc[0] = facc;
-    block_partials<1>(acc, part + 1 * kParts, kParts);  // slot 1: r.z
+    const float v[1] = {acc};
+    grid_sum<1>(v, gpart, gstride, ticket, scal + kS_RZN);  // r.z
 }
-__global__ void k_pcg_k1(GridDev g, const float* __restrict__ z, const float* __restrict__ d_in,
-                         float* __restrict__ d_out, float* __restrict__ q, const uint16_t* __restrict__ kind,
-                         double* part, double* scal, int* flag, int it, double target_rr) {
-    // previous iteration's r.z', r.z and r.r
-    double rz_new = sum_partials(part + 1 * kParts, gridDim.x);
+__global__ void __launch_bounds__(kNodeThreads) k_pcg_k1(GridDev g, const float* __restrict__ z,
+                                                         const float* __restrict__ d_in, float* __restrict__ d_out,
+                                                         float* __restrict__ q, const uint16_t* __restrict__ kind,
+                                                         double* gpart, int gstride, unsigned* ticket, double* scal,
+                                                         int* flag, int it, double target_rr) {
+    // scalars of the previous iteration: r.z', r.z, r.r
+    const double rz_new = scal[kS_RZN];
     double beta = 0.0;
     if (it > 0) {
-        double rzo = sum_partials(part + 2 * kParts, gridDim.x);
-        double rr = sum_partials(part + 3 * kParts, gridDim.x);
+        const double rzo = scal[kS_RZO], rr = scal[kS_RR];
         if (rr <= target_rr || flag[0]) {
             if (blockIdx.x == 0 && threadIdx.x == 0 && !flag[0]) {
                 flag[1] = it;  // iterations completed
@@ -375,15 +396,17 @@ __global__ void k_pcg_k1(GridDev g, const float* __restrict__ z, const float* __
             }
             return;
         }
-        double rz_old = scal[(it - 1) & 1];
-        beta = (rz_new - rzo) / rz_old;
+        beta = (rz_new - rzo) / scal[kS_RZ + ((it - 1) & 1)];
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) scal[it & 1] = rz_new;
-    double acc[1] = {0.0};
+    if (blockIdx.x == 0 && threadIdx.x == 0) scal[kS_RZ + (it & 1)] = rz_new;
+    const float fb = (float)beta;
     float facc = 0.f;
-    float fb = (float)beta;
-    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
-        uint16_t kd = kind[n];
+    const int base = blockIdx.x * kNodeTile + threadIdx.x;
+#pragma unroll
+    for (int q4 = 0; q4 < kNodeTile / kNodeThreads; q4++) {
+        const int n = base + q4 * kNodeThreads;
+        if (n >= g.nv) break;
+        const uint16_t kd = kind[n];
         if ((kd & 3) != kFree) {
             d_out[n] = 0.f;
             q[n] = 0.f;
@@ -393,64 +416,69 @@ __global__ void k_pcg_k1(GridDev g, const float* __restrict__ z, const float* __
         node_ijk(g, n, i, j, k);
         Stencil s;
         stencil(g, i, j, k, s);
-        float dn = z[n] + fb * d_in[n];
+        const float dn = z[n] + fb * d_in[n];
         float dg = 0.f, off = 0.f;
 #pragma unroll
-        for (int d = 0; d < 6; d++) {
-            if (kd & (1u << (2 + d))) continue;
-            dg += s.c[d];
-            int qq = s.q[d];
-            off += s.c[d] * (z[qq] + fb * d_in[qq]);  // zero on non-FREE neighbours
+        for (int dd = 0; dd < 6; dd++) {
+            if (kd & (1u << (2 + dd))) continue;
+            dg += s.c[dd];
+            const int qq = s.q[dd];
+            off += s.c[dd] * (z[qq] + fb * d_in[qq]);  // zero on non-FREE neighbours
         }
-        float qv = dg * dn - off;
+        const float qv = dg * dn - off;
         d_out[n] = dn;
         q[n] = qv;
         facc += dn * qv;
     }
-    acc[0] = facc;
-    block_partials<1>(acc, part + 0 * kParts, kParts);  // slot 0: d.q
+    const float v[1] = {facc};
+    grid_sum<1>(v, gpart, gstride, ticket, scal + kS_DQ);
 }
-__global__ void k_pcg_k2(GridDev g, const float* __restrict__ d, const float* __restrict__ q, float* __restrict__ e,
-                         float* __restrict__ r, float* __restrict__ z, const uint16_t* __restrict__ kind, double* part,
-                         double* scal, int* flag, int it) {
+__global__ void __launch_bounds__(kNodeThreads) k_pcg_k2(GridDev g, const float* __restrict__ d,
+                                                         const float* __restrict__ q, float* __restrict__ e,
+                                                         float* __restrict__ r, float* __restrict__ z,
+                                                         const uint16_t* __restrict__ kind, double* gpart,
+                                                         int gstride, unsigned* ticket, double* scal, int* flag,
+                                                         int it) {
     if (flag[0]) return;
-    double dq = sum_partials(part + 0 * kParts, gridDim.x);
-    double rz = scal[it & 1];
-    float alpha = dq != 0.0 ? (float)(rz / dq) : 0.f;
+    const double dq = scal[kS_DQ];
+    const double rz = scal[kS_RZ + (it & 1)];
+    const float alpha = dq != 0.0 ? (float)(rz / dq) : 0.f;
+    const float c3[3] = {g.inv_dx[0] * g.inv_dx[0], g.inv_dx[1] * g.inv_dx[1], g.inv_dx[2] * g.inv_dx[2]};
     float f0 = 0.f, f1 = 0.f, f2 = 0.f;
-    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
-        uint16_t kd = kind[n];
+    const int base = blockIdx.x * kNodeTile + threadIdx.x;
+#pragma unroll
+    for (int q4 = 0; q4 < kNodeTile / kNodeThreads; q4++) {
+        const int n = base + q4 * kNodeThreads;
+        if (n >= g.nv) break;
+        const uint16_t kd = kind[n];
         if ((kd & 3) != kFree) continue;
-        int i, j, k;
-        node_ijk(g, n, i, j, k);
-        Stencil s;
-        stencil(g, i, j, k, s);
         e[n] += alpha * d[n];
-        float rn = r[n] - alpha * q[n];
+        const float rn = r[n] - alpha * q[n];
         r[n] = rn;
-        float zo = z[n];
-        float zn = rn / diag_of(kd, s);
+        const float zo = z[n];
+        const float zn = rn * inv_diag_of(kd, c3);
         z[n] = zn;
         f0 += rn * zn;
         f1 += rn * zo;
         f2 += rn * rn;
     }
-    __syncthreads();
-    double a1[1] = {f0}, a2[1] = {f1}, a3[1] = {f2};
-    block_partials<1>(a1, part + 1 * kParts, kParts);
-    block_partials<1>(a2, part + 2 * kParts, kParts);
-    block_partials<1>(a3, part + 3 * kParts, kParts);
+    const float v[3] = {f0, f1, f2};
+    grid_sum<3>(v, gpart, gstride, ticket, scal + kS_RZN);  // r.z', r.z, r.r
 }
-void launch_pcg_init(const GridDev& g, SolveWork& w, cudaStream_t s, int grid) {
-    k_pcg_init<<<grid, 256, 0, s>>>(g, w.r, w.z, w.e, reinterpret_cast<const uint16_t*>(w.kind), w.part, w.flag);
-    cudaMemsetAsync(w.d, 0, sizeof(float) * g.nv, s);
+void launch_pcg_init(const GridDev& g, SolveWork& w, cudaStream_t s) {
+    k_pcg_init<<<node_blocks(g.nv), kNodeThreads, 0, s>>>(g, w.r, w.z, w.e, w.d,
+                                                          reinterpret_cast<const uint16_t*>(w.kind), w.gpart,
+                                                          w.gstride, w.ticket, w.scal, w.flag);
 }
-// one iteration; d ping-pongs between w.d and w.q's partner buffer (w.phi_alt is FP64 and not used here)
+// one iteration; d ping-pongs between two buffers
 void launch_pcg_iter_impl(const GridDev& g, SolveWork& w, float* d_in, float* d_out, int it, double target_rr,
-                          cudaStream_t s, int grid) {
+                          cudaStream_t s) {
     const uint16_t* kd = reinterpret_cast<const uint16_t*>(w.kind);
-    k_pcg_k1<<<grid, 256, 0, s>>>(g, w.z, d_in, d_out, w.q, kd, w.part, w.scal, w.flag, it, target_rr);
-    k_pcg_k2<<<grid, 256, 0, s>>>(g, d_out, w.q, w.e, w.r, w.z, kd, w.part, w.scal, w.flag, it);
+    const int nb = node_blocks(g.nv);
+    k_pcg_k1<<<nb, kNodeThreads, 0, s>>>(g, w.z, d_in, d_out, w.q, kd, w.gpart, w.gstride, w.ticket, w.scal, w.flag,
+                                         it, target_rr);
+    k_pcg_k2<<<nb, kNodeThreads, 0, s>>>(g, d_out, w.q, w.e, w.r, w.z, kd, w.gpart, w.gstride, w.ticket, w.scal,
+                                         w.flag, it);
 }
 
 // ------------------------------------------------------------------------------------

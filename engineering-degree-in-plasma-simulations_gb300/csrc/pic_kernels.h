@@ -98,18 +98,38 @@ struct SolveWork {
     float* q;         // CG L d
     float* z;         // CG preconditioned residual
     double* part;     // per-block partial sums [kParts * nslots]
-    double* scal;     // device scalars
-    int* flag;        // [0] inner converged
+    double* scal;     // device scalars (slots below)
+    int* flag;        // [0] inner converged, [1] iterations completed
+    double* gpart;    // node-kernel block partials [8][gstride]
+    int gstride;
+    unsigned* ticket; // last-block counter of the node-kernel reductions
 };
 constexpr int kParts = 1024;
-void launch_residual(const GridDev& g, SolveWork& w, int apply_e, cudaStream_t s, int grid, float* rho_prev,
-                     float* bfix_out);
-void launch_rhs_update(const GridDev& g, SolveWork& w, float* rho_prev, const float* bfix, cudaStream_t s, int grid);
+// Node kernels take a tile of kNodeTile consecutive nodes per block, kNodeTile / blockDim.x per
+// thread, strided by blockDim.x so that every load is coalesced and a thread's loads are
+// independent of each other.
+constexpr int kNodeThreads = 256;
+constexpr int kNodeTile = 4 * kNodeThreads;
+inline int node_blocks(int nv) { return (nv + kNodeTile - 1) / kNodeTile; }
+// device scalar slots of the solvers
+enum : int {
+    kS_RZ = 0,      // [0..1] r.z of iterations it (double-buffered by parity)
+    kS_ALPHA = 2,   // [2..3] alpha (learned preconditioner CG)
+    kS_DQ = 4,      // d.q
+    kS_RZN = 5,     // new r.z (Jacobi) / z.r (learned)
+    kS_RZO = 6,     // r_new.z_old (Jacobi) / z.q (learned)
+    kS_RR = 7,      // r.r
+    kS_R2 = 8,      // residual |r|^2, |b|^2 at 8, 9
+    kS_VAL = 12,    // validation norm
+};
+// residual (optionally after phi += e); |r|^2 and |b|^2 into scal[kS_R2..]
+void launch_residual(const GridDev& g, SolveWork& w, int apply_e, cudaStream_t s, float* rho_prev, float* bfix_out);
+void launch_rhs_update(const GridDev& g, SolveWork& w, float* rho_prev, const float* bfix, cudaStream_t s);
 void launch_reduce_partials(const double* part, int nslots, int nblocks, double* out, cudaStream_t s);
-void launch_rbsor_sweeps(const GridDev& g, SolveWork& w, float omega, int sweeps, cudaStream_t s, int grid);
-void launch_pcg_init(const GridDev& g, SolveWork& w, cudaStream_t s, int grid);
+void launch_rbsor_sweeps(const GridDev& g, SolveWork& w, float omega, int sweeps, cudaStream_t s);
+void launch_pcg_init(const GridDev& g, SolveWork& w, cudaStream_t s);
 void launch_pcg_iter_impl(const GridDev& g, SolveWork& w, float* d_in, float* d_out, int it, double target_rr,
-                          cudaStream_t s, int grid);
+                          cudaStream_t s);
 void launch_fill_aux(const GridDev& g, float2* phi, const uint8_t* kind, cudaStream_t s, int grid);
 void launch_den_avg(float* avg, const float* den, int nv, float a, float b, cudaStream_t s, int grid);
 

@@ -260,12 +260,20 @@ __global__ void k_lp_up(LView zin, LView cin, LView out, int mode, const float* 
     }
 }
 
-// level 0 on the node array: z = mask * (S0 * r + P e_1); partials z.r (slot 1), z.q (slot 2)
-__global__ void k_lp_up0(GridDev g, LView rin, LView cin, float* __restrict__ z, const uint16_t* __restrict__ kind,
-                         const float* __restrict__ S0, const float* __restrict__ q, double* part, const int* flag) {
+// level 0 on the node array: z = mask * (S0 * r + P e_1); with out != nullptr also z.r -> out[0]
+// and z.q -> out[1] (deterministic grid sums)
+__global__ void __launch_bounds__(kNodeThreads) k_lp_up0(GridDev g, LView rin, LView cin, float* __restrict__ z,
+                                                         const uint16_t* __restrict__ kind,
+                                                         const float* __restrict__ S0, const float* __restrict__ q,
+                                                         double* gpart, int gstride, unsigned* ticket, double* out,
+                                                         const int* flag) {
     if (flag && flag[0]) return;
     float f_zr = 0.f, f_zq = 0.f;
-    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
+    const int base = blockIdx.x * kNodeTile + threadIdx.x;
+#pragma unroll
+    for (int q4 = 0; q4 < kNodeTile / kNodeThreads; q4++) {
+        const int n = base + q4 * kNodeThreads;
+        if (n >= g.nv) break;
         if ((kind[n] & 3) != kFree) {
             z[n] = 0.f;
             continue;
@@ -278,17 +286,20 @@ __global__ void k_lp_up0(GridDev g, LView rin, LView cin, float* __restrict__ z,
         f_zr += v * rin.a[n];
         if (q) f_zq += v * q[n];
     }
-    if (part) {
-        double a1[1] = {f_zr}, a2[1] = {f_zq};
-        block_partials<1>(a1, part + 1 * kParts, kParts);
-        block_partials<1>(a2, part + 2 * kParts, kParts);
+    if (out) {
+        const float vv[2] = {f_zr, f_zq};
+        grid_sum<2>(vv, gpart, gstride, ticket, out);
     }
 }
 
-static int lp_blocks(int nvox, int sms) { return std::max(1, std::min((nvox + 255) / 256, sms * 8)); }
+// one thread per voxel of a level
+static int lp_blocks(int nvox, int sms) {
+    (void)sms;
+    return std::max(1, (nvox + 255) / 256);
+}
 
 void launch_lp_apply(const GridDev& g, const LpState& L, const float* r, float* z, const uint16_t* kind,
-                     const float* q, double* part, const int* flag, cudaStream_t s, int grid_nodes, int sms) {
+                     const float* q, const SolveWork* red, const int* flag, cudaStream_t s, int sms) {
     LView r0 = lp_node_view(g, L, const_cast<float*>(r));
     for (int l = 1; l < L.nlev; l++) {
         LView f = l == 1 ? r0 : lp_level_view(L, l - 1, L.z[l - 1]);
@@ -306,7 +317,10 @@ void launch_lp_apply(const GridDev& g, const LpState& L, const float* r, float* 
         k_lp_up<<<lp_blocks(out.nvox, sms), 256, 0, s>>>(zin, cin, out, mode, fold, (float)(1.0 / L.diag[l]), flag);
     }
     LView cin = L.nlev > 1 ? lp_level_view(L, 1, L.e[1]) : none;
-    k_lp_up0<<<grid_nodes, 256, 0, s>>>(g, r0, cin, z, kind, L.W + L.lay.s0, q, part, flag);
+    k_lp_up0<<<node_blocks(g.nv), kNodeThreads, 0, s>>>(g, r0, cin, z, kind, L.W + L.lay.s0, q,
+                                                        red ? red->gpart : nullptr, red ? red->gstride : 0,
+                                                        red ? red->ticket : nullptr,
+                                                        red ? red->scal + kS_RZN : nullptr, flag);
 }
 
 // folded stencils of every network level: M = Wm Wl (C x 27), K27[t][t'] = sum_c Wp[t][c] M[c][t'],
@@ -360,14 +374,15 @@ void launch_lp_fold(const LpState& L, cudaStream_t s) {
 //   B    : z = B r ; partials z.r, z.q            (beta = z.(r_new - r_old) / rz_prev)
 // scal[0..1] rz and scal[2..3] alpha, double-buffered by iteration parity
 // =====================================================================================
-__global__ void k_lpcg_k1(GridDev g, const float* __restrict__ z, const float* __restrict__ d_in,
-                          float* __restrict__ d_out, float* __restrict__ q, const uint16_t* __restrict__ kind,
-                          double* part, double* scal, int* flag, int it, double target_rr) {
-    double rz_new = sum_partials(part + 1 * kParts, gridDim.x);
+__global__ void __launch_bounds__(kNodeThreads) k_lpcg_k1(GridDev g, const float* __restrict__ z,
+                                                          const float* __restrict__ d_in, float* __restrict__ d_out,
+                                                          float* __restrict__ q, const uint16_t* __restrict__ kind,
+                                                          double* gpart, int gstride, unsigned* ticket,
+                                                          double* scal, int* flag, int it, double target_rr) {
+    const double rz_new = scal[kS_RZN];
     double beta = 0.0;
     if (it > 0) {
-        double zq = sum_partials(part + 2 * kParts, gridDim.x);
-        double rr = sum_partials(part + 3 * kParts, gridDim.x);
+        const double zq = scal[kS_RZO], rr = scal[kS_RR];
         if (rr <= target_rr || flag[0]) {
             if (blockIdx.x == 0 && threadIdx.x == 0 && !flag[0]) {
                 flag[1] = it;  // iterations completed
@@ -375,15 +390,19 @@ __global__ void k_lpcg_k1(GridDev g, const float* __restrict__ z, const float* _
             }
             return;
         }
-        double rz_old = scal[(it - 1) & 1];
-        double alpha_old = scal[2 + ((it - 1) & 1)];
+        const double rz_old = scal[kS_RZ + ((it - 1) & 1)];
+        const double alpha_old = scal[kS_ALPHA + ((it - 1) & 1)];
         beta = rz_old != 0.0 ? -alpha_old * zq / rz_old : 0.0;
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) scal[it & 1] = rz_new;
+    if (blockIdx.x == 0 && threadIdx.x == 0) scal[kS_RZ + (it & 1)] = rz_new;
     float facc = 0.f;
     const float fb = (float)beta;
-    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
-        uint16_t kd = kind[n];
+    const int base = blockIdx.x * kNodeTile + threadIdx.x;
+#pragma unroll
+    for (int q4 = 0; q4 < kNodeTile / kNodeThreads; q4++) {
+        const int n = base + q4 * kNodeThreads;
+        if (n >= g.nv) break;
+        const uint16_t kd = kind[n];
         if ((kd & 3) != kFree) {
             d_out[n] = 0.f;
             q[n] = 0.f;
@@ -393,51 +412,57 @@ __global__ void k_lpcg_k1(GridDev g, const float* __restrict__ z, const float* _
         node_ijk(g, n, i, j, k);
         Stencil s;
         stencil(g, i, j, k, s);
-        float dn = z[n] + fb * d_in[n];
+        const float dn = z[n] + fb * d_in[n];
         float dg = 0.f, off = 0.f;
 #pragma unroll
         for (int d = 0; d < 6; d++) {
             if (kd & (1u << (2 + d))) continue;
             dg += s.c[d];
-            int qq = s.q[d];
+            const int qq = s.q[d];
             off += s.c[d] * (z[qq] + fb * d_in[qq]);
         }
-        float qv = dg * dn - off;
+        const float qv = dg * dn - off;
         d_out[n] = dn;
         q[n] = qv;
         facc += dn * qv;
     }
-    double acc[1] = {facc};
-    block_partials<1>(acc, part + 0 * kParts, kParts);
+    const float v[1] = {facc};
+    grid_sum<1>(v, gpart, gstride, ticket, scal + kS_DQ);
 }
-__global__ void k_lpcg_k2(GridDev g, const float* __restrict__ d, const float* __restrict__ q, float* __restrict__ e,
-                          float* __restrict__ r, const uint16_t* __restrict__ kind, double* part, double* scal,
-                          int* flag, int it) {
+__global__ void __launch_bounds__(kNodeThreads) k_lpcg_k2(GridDev g, const float* __restrict__ d,
+                                                          const float* __restrict__ q, float* __restrict__ e,
+                                                          float* __restrict__ r, const uint16_t* __restrict__ kind,
+                                                          double* gpart, int gstride, unsigned* ticket,
+                                                          double* scal, int* flag, int it) {
     if (flag[0]) return;
-    double dq = sum_partials(part + 0 * kParts, gridDim.x);
-    double rz = scal[it & 1];
-    double alpha_d = dq != 0.0 ? rz / dq : 0.0;
-    if (blockIdx.x == 0 && threadIdx.x == 0) scal[2 + (it & 1)] = alpha_d;
+    const double dq = scal[kS_DQ];
+    const double rz = scal[kS_RZ + (it & 1)];
+    const double alpha_d = dq != 0.0 ? rz / dq : 0.0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) scal[kS_ALPHA + (it & 1)] = alpha_d;
     const float alpha = (float)alpha_d;
     float frr = 0.f;
-    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
+    const int base = blockIdx.x * kNodeTile + threadIdx.x;
+#pragma unroll
+    for (int q4 = 0; q4 < kNodeTile / kNodeThreads; q4++) {
+        const int n = base + q4 * kNodeThreads;
+        if (n >= g.nv) break;
         if ((kind[n] & 3) != kFree) continue;
         e[n] += alpha * d[n];
-        float rn = r[n] - alpha * q[n];
+        const float rn = r[n] - alpha * q[n];
         r[n] = rn;
         frr += rn * rn;
     }
-    double acc[1] = {frr};
-    block_partials<1>(acc, part + 3 * kParts, kParts);
+    const float v[1] = {frr};
+    grid_sum<1>(v, gpart, gstride, ticket, scal + kS_RR);
 }
-__global__ void k_lpcg_zero(float* e, float* q, int nv, int* flag) {
+__global__ void k_lpcg_zero(float* e, float* q, float* d, int nv, int* flag) {
     if (blockIdx.x == 0 && threadIdx.x == 0) flag[0] = 0;
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nv; n += gridDim.x * blockDim.x) {
         e[n] = 0.f;
         q[n] = 0.f;
+        d[n] = 0.f;
     }
 }
-
 // |a|^2 over n values into out[0] (deterministic: block partials, then one fixed-order sum)
 __global__ void k_lp_sq(const float* __restrict__ a, int n, double* part) {
     float f = 0.f;
@@ -454,20 +479,20 @@ void launch_lp_norm2(const float* a, int n, double* part, double* out, cudaStrea
     k_lp_sum1<<<1, 256, 0, s>>>(part, grid, out);
 }
 
-void launch_lpcg_init(const GridDev& g, SolveWork& w, const LpState& L, cudaStream_t s, int grid, int sms) {
-    k_lpcg_zero<<<grid, 256, 0, s>>>(w.e, w.q, g.nv, w.flag);
-    cudaMemsetAsync(w.d, 0, sizeof(float) * g.nv, s);
-    launch_lp_apply(g, L, w.r, w.z, reinterpret_cast<const uint16_t*>(w.kind), w.q, w.part, nullptr, s, grid, sms);
+void launch_lpcg_init(const GridDev& g, SolveWork& w, const LpState& L, cudaStream_t s, int sms) {
+    k_lpcg_zero<<<(g.nv + 255) / 256, 256, 0, s>>>(w.e, w.q, w.d, g.nv, w.flag);
+    launch_lp_apply(g, L, w.r, w.z, reinterpret_cast<const uint16_t*>(w.kind), w.q, &w, nullptr, s, sms);
 }
 void launch_lpcg_iter(const GridDev& g, SolveWork& w, const LpState& L, float* d_in, float* d_out, int it,
-                      double target_rr, cudaStream_t s, int grid, int sms) {
+                      double target_rr, cudaStream_t s, int sms) {
     const uint16_t* kd = reinterpret_cast<const uint16_t*>(w.kind);
-    k_lpcg_k1<<<grid, 256, 0, s>>>(g, w.z, d_in, d_out, w.q, kd, w.part, w.scal, w.flag, it, target_rr);
-    k_lpcg_k2<<<grid, 256, 0, s>>>(g, d_out, w.q, w.e, w.r, kd, w.part, w.scal, w.flag, it);
-    launch_lp_apply(g, L, w.r, w.z, kd, w.q, w.part, w.flag, s, grid, sms);
+    const int nb = node_blocks(g.nv);
+    k_lpcg_k1<<<nb, kNodeThreads, 0, s>>>(g, w.z, d_in, d_out, w.q, kd, w.gpart, w.gstride, w.ticket, w.scal, w.flag,
+                                          it, target_rr);
+    k_lpcg_k2<<<nb, kNodeThreads, 0, s>>>(g, d_out, w.q, w.e, w.r, kd, w.gpart, w.gstride, w.ticket, w.scal, w.flag,
+                                          it);
+    launch_lp_apply(g, L, w.r, w.z, kd, w.q, &w, w.flag, s, sms);
 }
-
-
 
 // =====================================================================================
 // training: one step = forward (unfolded network), energy-norm loss, backward, Adam
@@ -1002,7 +1027,8 @@ void launch_lp_loss_grad(const GridDev& g, LpState& L, const uint16_t* kind, con
         }
     }
     LView cin1 = L.nlev > 1 ? lp_level_view(L, 1, L.e[1]) : none;
-    k_lp_up0<<<grid, 256, 0, s>>>(g, r0, cin1, T->e0, kind, L.W + L.lay.s0, nullptr, nullptr, nullptr);
+    k_lp_up0<<<node_blocks(g.nv), kNodeThreads, 0, s>>>(g, r0, cin1, T->e0, kind, L.W + L.lay.s0, nullptr, nullptr, 0,
+                                                        nullptr, nullptr, nullptr);
     // loss and its gradient with respect to e
     k_lp_loss<<<grid, 256, 0, s>>>(g, kind, T->e0, x, T->ge, T->part);
     k_lp_loss_scale<<<grid, 256, 0, s>>>(g.nv, T->ge, T->part, T->red);

@@ -84,15 +84,15 @@ float* lp_train_r(const LpState& L);
 float* lp_train_grad(const LpState& L);
 double* lp_train_red(const LpState& L);
 unsigned* lp_train_err(const LpState& L);
-// z = B r on the node array (r zero off FREE nodes); with part != nullptr the last kernel also
-// writes per-block partials of z.r (slot 1) and z.q (slot 2); every kernel returns early when
-// flag[0] is set (inner solve converged)
+// z = B r on the node array (r zero off FREE nodes); with red != nullptr the last kernel also
+// sums z.r and z.q into red->scal[kS_RZN], [kS_RZO]; every kernel returns early when flag[0] is
+// set (inner solve converged)
 void launch_lp_apply(const GridDev& g, const LpState& L, const float* r, float* z, const uint16_t* kind,
-                     const float* q, double* part, const int* flag, cudaStream_t s, int grid_nodes, int sms);
+                     const float* q, const SolveWork* red, const int* flag, cudaStream_t s, int sms);
 // flexible CG iteration with the learned preconditioner (see pic_learned.cu)
 void launch_lp_norm2(const float* a, int n, double* part, double* out, cudaStream_t s, int grid);
-void launch_lpcg_init(const GridDev& g, SolveWork& w, const LpState& L, cudaStream_t s, int grid, int sms);
+void launch_lpcg_init(const GridDev& g, SolveWork& w, const LpState& L, cudaStream_t s, int sms);
 void launch_lpcg_iter(const GridDev& g, SolveWork& w, const LpState& L, float* d_in, float* d_out, int it,
-                      double target_rr, cudaStream_t s, int grid, int sms);
+                      double target_rr, cudaStream_t s, int sms);
 
 }  // namespace pic

@@ -82,3 +82,61 @@ __device__ __forceinline__ float diag_of(uint16_t kd, const Stencil& s) {
     return dg;
 }
 }  // namespace pic
+
+namespace pic {
+
+// Deterministic grid-wide sums of N per-thread FP32 values: every block writes its FP64
+// partial sums to part[c * stride + block]; the last block to finish (an atomic ticket) adds the
+// partials in block order and writes out[c].  The order of the additions never depends on
+// timing, so the sums are bit-reproducible from run to run.
+template <int N>
+__device__ __forceinline__ void grid_sum(const float (&v)[N], double* part, int stride, unsigned* ticket,
+                                         double* out) {
+    __shared__ double s[N][32];
+    __shared__ unsigned s_last;
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int c = 0; c < N; c++) {
+        double x = v[c];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) s[c][wp] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < N) {
+        double x = 0;
+        for (int w = 0; w < nw; w++) x += s[threadIdx.x][w];
+        part[threadIdx.x * stride + blockIdx.x] = x;
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = (atomicAdd(ticket, 1u) == gridDim.x - 1) ? 1u : 0u;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+#pragma unroll
+    for (int c = 0; c < N; c++) {
+        double x = 0;
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) x += __ldcg(&part[c * stride + b]);
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        __syncthreads();
+        if (lane == 0) s[c][wp] = x;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t = 0;
+            for (int w = 0; w < nw; w++) t += s[c][w];
+            out[c] = t;
+        }
+    }
+    if (threadIdx.x == 0) *ticket = 0u;
+}
+
+// inverse diagonal of the reduced operator from the node's mirror mask
+__device__ __forceinline__ float inv_diag_of(uint16_t kd, const float c[3]) {
+    float dg = 0.f;
+#pragma unroll
+    for (int d = 0; d < 6; d++)
+        if (!(kd & (1u << (2 + d)))) dg += c[d >> 1];
+    return 1.f / dg;
+}
+
+}  // namespace pic
