@@ -17,12 +17,16 @@ namespace pic {
 constexpr int kThreads = 256;
 constexpr int kPPT = 4;                     // particles per thread per chunk
 constexpr int kChunk = kThreads * kPPT;     // particles per chunk
-constexpr int kSeg = 512;                   // nodes per staged row segment
+constexpr int kSeg = 256;                   // nodes per staged row segment
 constexpr int kMargin = 2;                  // deposit window starts this many nodes below the gather window
 constexpr int kHalfWin = (kSeg - kMargin - 2) / 2;  // staged base nodes either side of the chunk's anchor
-// E rows (float4) + fixed-point deposit tile: three 21-bit limb planes of 32-bit counters,
-// four rows of kSeg nodes each
-constexpr size_t kPushSmem = 4 * kSeg * sizeof(float4) + 3 * 4 * kSeg * sizeof(unsigned);
+// shared memory of the push: the next chunk's particles (pos, vel, and ids with collisions),
+// the E rows (float4) and the fixed-point deposit tile (three 21-bit limb planes of 32-bit
+// counters), four rows of kSeg nodes each
+__host__ __device__ constexpr size_t kPbufBytes(bool mcc) { return (size_t)kChunk * (2 * sizeof(float4) + (mcc ? 8 : 0)); }
+__host__ __device__ constexpr size_t kPushSmem(bool mcc) {
+    return kPbufBytes(mcc) + 4 * kSeg * sizeof(float4) + 3 * 4 * kSeg * sizeof(unsigned);
+}
 constexpr long long kWaitLimit = 1ll << 24;  // mbarrier polls before giving up
 
 // ------------------------------------------------------------------------------------
@@ -331,23 +335,38 @@ __device__ __noinline__ Collision collide_candidate(const CollDev& cd, unsigned 
 
 // ------------------------------------------------------------------------------------
 // fused collide + push + deposit
-//   A CTA takes chunks of 1024 particles (4 per thread).  For a cell-sorted chunk the four node
-//   rows its cells touch, [lo + off_m, lo + off_m + L), are bulk-copied (TMA) into shared
-//   memory; the gather reads them there, and the deposit accumulates into a shared 64-bit
-//   fixed-point tile that is committed to HBM with one atomic per touched node.  Unsorted
-//   chunks (span wider than a row segment) use global loads and atomics.
+//   A CTA takes chunks of 1024 particles (4 consecutive per thread), software-pipelined: the
+//   next chunk's particle arrays are bulk-copied (TMA) into shared memory while the current
+//   chunk is processed.  For each chunk the four node rows around the base node of its middle
+//   particle, [lo + off_m, lo + off_m + L), are bulk-copied into shared memory; the gather reads
+//   them there, and the deposit accumulates into a shared 64-bit fixed-point tile committed to
+//   HBM with one atomic per touched node.  Particles outside the window use HBM directly.
 // ------------------------------------------------------------------------------------
+// bulk copy of one full chunk's particle arrays into the staging buffer
+template <bool kMcc>
+__device__ __forceinline__ void issue_chunk(const SpeciesDev& sp, int base, float4* ppos, float4* pvel,
+                                            unsigned long long* pid, unsigned long long* bar) {
+    const unsigned b16 = kChunk * sizeof(float4);
+    fence_proxy_async();
+    mbar_expect_tx(bar, 2 * b16 + (kMcc ? kChunk * 8u : 0u));
+    bulk_g2s(ppos, sp.pos + base, b16, bar);
+    bulk_g2s(pvel, sp.vel + base, b16, bar);
+    if (kMcc) bulk_g2s(pid, sp.id + base, kChunk * 8u, bar);
+}
+
 template <bool kMcc>
 __global__ void __launch_bounds__(kThreads, kMcc ? 2 : 3) k_push(PushArgs a) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    float4* etile = reinterpret_cast<float4*>(smem);
-    unsigned* dtile = reinterpret_cast<unsigned*>(smem + 4 * kSeg * sizeof(float4));
-    __shared__ __align__(8) unsigned long long bar;
-    __shared__ int s_min[kThreads / 32], s_max[kThreads / 32];
-    __shared__ int s_lo, s_hi, s_fail, s_first;
+    extern __shared__ __align__(128) unsigned char smem[];
+    float4* ppos = reinterpret_cast<float4*>(smem);
+    float4* pvel = ppos + kChunk;
+    unsigned long long* pid = reinterpret_cast<unsigned long long*>(pvel + kChunk);
+    float4* etile = reinterpret_cast<float4*>(smem + kPbufBytes(kMcc));
+    unsigned* dtile = reinterpret_cast<unsigned*>(etile + 4 * kSeg);
+    __shared__ __align__(8) unsigned long long bar_p, bar_e;
+    __shared__ int s_fail;
 
     const GridDev& g = a.g;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int tid = threadIdx.x, lane = tid & 31;
     const int n = a.sp.counts[0];
     const int ion_n = kMcc ? a.coll.ion.counts[0] : 0;
     const int nchunks = (n + kChunk - 1) / kChunk;
@@ -355,100 +374,107 @@ __global__ void __launch_bounds__(kThreads, kMcc ? 2 : 3) k_push(PushArgs a) {
     unsigned st_cand = 0, st_coll = 0, st_ion = 0, st_lost = 0;
 
     if (tid == 0) {
-        mbar_init(&bar, 1);
+        mbar_init(&bar_p, 1);
+        mbar_init(&bar_e, 1);
         fence_mbar_init();
+        s_fail = 0;
     }
     __syncthreads();
-    unsigned phase = 0;
+    unsigned phase_p = 0, phase_e = 0;
     Tile t;
     t.off[0] = 0;
     t.off[1] = g.ni;
     t.off[2] = nij;
     t.off[3] = nij + g.ni;
+    // last base node whose eight corners exist: the window must not copy past the node array
+    const int max_base = g.nv - 2 - t.off[3];
 
-    for (int ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
+    int ch = blockIdx.x;
+    bool pending = false;  // a particle bulk copy into the staging buffer is in flight
+    if (ch < nchunks && (ch + 1) * kChunk <= n && tid == 0) issue_chunk<kMcc>(a.sp, ch * kChunk, ppos, pvel, pid, &bar_p);
+    pending = ch < nchunks && (ch + 1) * kChunk <= n;
+
+    for (; ch < nchunks; ch += gridDim.x) {
         const int base = ch * kChunk;
+        const int nin = min(kChunk, n - base);
+        // ---- this chunk's particles into registers (staged by TMA, or loaded here for the last,
+        // partial chunk)
+        if (pending) {
+            if (!mbar_wait_bounded(&bar_p, phase_p)) atomicExch(&s_fail, 1);
+            phase_p ^= 1u;
+            pending = false;
+            __syncthreads();
+            if (s_fail) {
+                if (tid == 0) set_error(a.err, kErrBarrierTimeout);
+                mbar_wait_bounded(&bar_p, phase_p ^ 1u);  // the copy in flight, bounded
+                return;
+            }
+        } else {
+            for (int x = tid; x < nin; x += kThreads) {
+                ppos[x] = a.sp.pos[base + x];
+                pvel[x] = a.sp.vel[base + x];
+                if (kMcc) pid[x] = a.sp.id[base + x];
+            }
+            __syncthreads();
+        }
         float4 P[kPPT], V[kPPT];
+        unsigned long long ID[kPPT];
         int bn[kPPT];
-        // each thread takes kPPT consecutive particles: in a cell-sorted chunk they mostly share a
-        // cell, so their deposits are summed in registers before touching shared memory
 #pragma unroll
         for (int q = 0; q < kPPT; q++) {
-            int p = base + tid * kPPT + q;
+            const int x = tid * kPPT + q;
             bn[q] = -1;
-            if (p < n) {
-                P[q] = a.sp.pos[p];
-                V[q] = a.sp.vel[p];
-                int c = __float_as_int(P[q].w);
+            if (x < nin) {
+                P[q] = ppos[x];
+                V[q] = pvel[x];
+                if (kMcc) ID[q] = pid[x];
+                const int c = __float_as_int(P[q].w);
                 if (c >= 0) bn[q] = ((c >> 20) * g.nj + ((c >> 10) & 1023)) * g.ni + (c & 1023);
             }
         }
-        // the window is centred on the base node of the chunk's middle particle (the sorted order
-        // puts the bulk of the chunk around it); particles more than kHalfWin nodes away (moved to
-        // another row of cells since the last sort, or an unsorted chunk) use global memory
+        // ---- window: +-kHalfWin base nodes around the base node of the chunk's middle particle
+        int lo = 0, hi = -1;
         {
-            const int mid = (min(base + kChunk, n) - base) >> 1;
-            if (tid == mid / kPPT) {
-#pragma unroll
-                for (int q = 0; q < kPPT; q++)
-                    if (q == mid % kPPT) s_first = bn[q];
+            const int c = __float_as_int(ppos[nin >> 1].w);
+            if (c >= 0) {
+                const int anchor = ((c >> 20) * g.nj + ((c >> 10) & 1023)) * g.ni + (c & 1023);
+                lo = max(0, anchor - kHalfWin);
+                hi = min(anchor + kHalfWin, max_base);
             }
         }
-        __syncthreads();
-        {
-            const int anchor = s_first;
-            int lmin = INT_MAX, lmax = -1;
-#pragma unroll
-            for (int q = 0; q < kPPT; q++) {
-                if (bn[q] >= 0 && anchor >= 0 && abs(bn[q] - anchor) <= kHalfWin) {
-                    lmin = min(lmin, bn[q]);
-                    lmax = max(lmax, bn[q]);
-                }
-            }
-            lmin = __reduce_min_sync(0xffffffffu, lmin);
-            lmax = __reduce_max_sync(0xffffffffu, lmax);
-            if (lane == 0) {
-                s_min[warp] = lmin;
-                s_max[warp] = lmax;
-            }
-        }
-        __syncthreads();
+        const bool use_tile = a.staged && hi >= lo;
+        __syncthreads();  // every thread has read the staging buffer
         if (tid == 0) {
-            int mn = INT_MAX, mx = -1;
-            for (int w = 0; w < kThreads / 32; w++) {
-                mn = min(mn, s_min[w]);
-                mx = max(mx, s_max[w]);
+            if (use_tile) {
+                const unsigned bytes = (unsigned)(hi - lo + 2) * (unsigned)sizeof(float4);
+                fence_proxy_async();
+                mbar_expect_tx(&bar_e, 4 * bytes);
+#pragma unroll
+                for (int m = 0; m < 4; m++) bulk_g2s(etile + m * kSeg, a.ef + lo + t.off[m], bytes, &bar_e);
             }
-            s_lo = mn;
-            s_hi = mx;
-            s_fail = 0;
+            const int nx = ch + gridDim.x;
+            if (nx < nchunks && (nx + 1) * kChunk <= n) issue_chunk<kMcc>(a.sp, nx * kChunk, ppos, pvel, pid, &bar_p);
         }
-        __syncthreads();
-        const int lo = s_lo, hi = s_hi;
-        const bool use_tile = a.staged && hi >= 0 && (hi - lo + 2) <= kSeg - kMargin;
+        {
+            const int nx = ch + gridDim.x;
+            pending = nx < nchunks && (nx + 1) * kChunk <= n;
+        }
         t.lo = lo;
         t.span = hi - lo;
         t.etile = nullptr;
         t.dtile = nullptr;
         if (use_tile) {
-            if (tid == 0) {
-                unsigned bytes = (unsigned)(hi - lo + 2) * (unsigned)sizeof(float4);
-                fence_proxy_async();
-                mbar_expect_tx(&bar, 4 * bytes);
-#pragma unroll
-                for (int m = 0; m < 4; m++) bulk_g2s(etile + m * kSeg, a.ef + lo + t.off[m], bytes, &bar);
-            }
             if (a.deposit)
                 for (int x = tid; x < 12 * kSeg; x += kThreads) dtile[x] = 0u;
-            bool ok = mbar_wait_bounded(&bar, phase);
-            if (!ok) atomicExch(&s_fail, 1);
-            phase ^= 1u;
+            if (!mbar_wait_bounded(&bar_e, phase_e)) atomicExch(&s_fail, 1);
+            phase_e ^= 1u;
             __syncthreads();
             if (s_fail) {
-                // the copies did not complete in time: record it, wait once more (bounded) for
-                // the copies in flight, and leave without touching the tile
+                // a copy did not complete in time: record it, wait once more (bounded) for the
+                // copies in flight, and leave without touching the tile
                 if (tid == 0) set_error(a.err, kErrBarrierTimeout);
-                mbar_wait_bounded(&bar, phase ^ 1u);
+                mbar_wait_bounded(&bar_e, phase_e ^ 1u);
+                if (pending) mbar_wait_bounded(&bar_p, phase_p);
                 return;
             }
             t.etile = etile;
@@ -473,7 +499,7 @@ __global__ void __launch_bounds__(kThreads, kMcc ? 2 : 3) k_push(PushArgs a) {
             unsigned long long id = 0;
             if (kMcc) {
                 const CollDev& cd = a.coll;
-                id = a.sp.id[p];
+                id = ID[q];
                 uint4 r0 = philox4x32_10(make_uint4((unsigned)id, (unsigned)(id >> 32), cd.step, 0u), cd.key);
                 if (u01(r0.x) < cd.p_null) {
                     st_cand++;
@@ -548,6 +574,8 @@ __global__ void __launch_bounds__(kThreads, kMcc ? 2 : 3) k_push(PushArgs a) {
         }
         __syncthreads();
         if (use_tile && a.deposit) {
+            // commit the tile: slot o of row m is node lo - kMargin + off_m + o (only slots that
+            // received a deposit are nonzero, and those are nodes of the grid)
             const int wlo = lo - kMargin;
             for (int x = tid; x < 4 * kSeg; x += kThreads) {
                 unsigned long long v = (unsigned long long)dtile[x] + ((unsigned long long)dtile[4 * kSeg + x] << 21) +
@@ -570,12 +598,12 @@ __global__ void __launch_bounds__(kThreads, kMcc ? 2 : 3) k_push(PushArgs a) {
 void launch_push(const PushArgs& a, cudaStream_t s, int grid) {
     static bool attr = false;
     if (!attr) {
-        cudaFuncSetAttribute(k_push<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPushSmem);
-        cudaFuncSetAttribute(k_push<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPushSmem);
+        cudaFuncSetAttribute(k_push<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPushSmem(true));
+        cudaFuncSetAttribute(k_push<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPushSmem(false));
         attr = true;
     }
-    if (a.coll.enabled) k_push<true><<<grid, kThreads, kPushSmem, s>>>(a);
-    else k_push<false><<<grid, kThreads, kPushSmem, s>>>(a);
+    if (a.coll.enabled) k_push<true><<<grid, kThreads, kPushSmem(true), s>>>(a);
+    else k_push<false><<<grid, kThreads, kPushSmem(false), s>>>(a);
 }
 
 // ------------------------------------------------------------------------------------
