@@ -120,6 +120,25 @@ __global__ void k_lp_restrict(LView f, LView c, const int* flag) {
     for (unsigned idx = blockIdx.x * blockDim.x + threadIdx.x; idx < (unsigned)c.nvox; idx += gridDim.x * blockDim.x) {
         int cc[3];
         lv_decode(c, idx, cc[0], cc[1], cc[2]);
+        const float w4[4] = {0.25f, 0.75f, 0.75f, 0.25f};
+        if (cc[0] >= 1 && 2 * cc[0] + 2 < f.n[0] && cc[1] >= 1 && 2 * cc[1] + 2 < f.n[1] && cc[2] >= 1 &&
+            2 * cc[2] + 2 < f.n[2]) {
+            // interior: the 4 x 4 x 4 fine points are inside the box, no wrap
+            const float* p0 = f.a + (2 * cc[0] - 1) + (2 * cc[1] - 1) * f.sy + (2 * cc[2] - 1) * f.sz;
+            float acc = 0.f;
+#pragma unroll
+            for (int kz = 0; kz < 4; kz++) {
+                float az = 0.f;
+#pragma unroll
+                for (int ky = 0; ky < 4; ky++) {
+                    const float* row = p0 + ky * f.sy + kz * f.sz;
+                    az += w4[ky] * (w4[0] * row[0] + w4[1] * row[1] + w4[2] * row[2] + w4[3] * row[3]);
+                }
+                acc += w4[kz] * az;
+            }
+            c.a[lv_off(c, cc[0], cc[1], cc[2])] = acc;
+            continue;
+        }
         int fi[3][4];
 #pragma unroll
         for (int ax = 0; ax < 3; ax++) {
@@ -135,7 +154,6 @@ __global__ void k_lp_restrict(LView f, LView c, const int* flag) {
                 }
             }
         }
-        const float w4[4] = {0.25f, 0.75f, 0.75f, 0.25f};
         float acc = 0.f;
 #pragma unroll
         for (int kz = 0; kz < 4; kz++) {
@@ -159,6 +177,22 @@ __global__ void k_lp_restrict(LView f, LView c, const int* flag) {
 
 // sum_c P(f, c) e_coarse[c] at fine point f
 __device__ __forceinline__ float lp_prolong_at(const LView& cv, const int f[3]) {
+    const float w2[2] = {0.75f, 0.25f};
+    {
+        // interior: both coarse neighbours of every axis inside the box, no wrap
+        const int c0x = f[0] >> 1, c0y = f[1] >> 1, c0z = f[2] >> 1;
+        const int sx = (f[0] & 1) ? 1 : -1, sy = (f[1] & 1) ? 1 : -1, sz = (f[2] & 1) ? 1 : -1;
+        if ((unsigned)(c0x + sx) < (unsigned)cv.n[0] && (unsigned)(c0y + sy) < (unsigned)cv.n[1] &&
+            (unsigned)(c0z + sz) < (unsigned)cv.n[2]) {
+            const float* p = cv.a + c0x + c0y * cv.sy + c0z * cv.sz;
+            const int oy = sy * cv.sy, oz = sz * cv.sz;
+            const float a0 = w2[0] * p[0] + w2[1] * p[sx];
+            const float a1 = w2[0] * p[oy] + w2[1] * p[oy + sx];
+            const float a2 = w2[0] * p[oz] + w2[1] * p[oz + sx];
+            const float a3 = w2[0] * p[oz + oy] + w2[1] * p[oz + oy + sx];
+            return w2[0] * (w2[0] * a0 + w2[1] * a1) + w2[1] * (w2[0] * a2 + w2[1] * a3);
+        }
+    }
     int ci[3][2];
 #pragma unroll
     for (int ax = 0; ax < 3; ax++) {
@@ -166,7 +200,6 @@ __device__ __forceinline__ float lp_prolong_at(const LView& cv, const int f[3]) 
         ci[ax][0] = c0;
         ci[ax][1] = lv_nb(c0, (f[ax] & 1) ? 1 : -1, cv.n[ax], cv.per[ax]);
     }
-    const float w2[2] = {0.75f, 0.25f};
     float acc = 0.f;
 #pragma unroll
     for (int kz = 0; kz < 2; kz++) {
@@ -189,6 +222,20 @@ __device__ __forceinline__ float lp_prolong_at(const LView& cv, const int f[3]) 
 
 // 3x3x3 stencil (taps t = 9(dz+1) + 3(dy+1) + (dx+1)) at point c
 __device__ __forceinline__ float lp_stencil27(const LView& v, const float* __restrict__ S, const int c[3]) {
+    if (c[0] >= 1 && c[0] + 1 < v.n[0] && c[1] >= 1 && c[1] + 1 < v.n[1] && c[2] >= 1 && c[2] + 1 < v.n[2]) {
+        // interior: constant offsets, no wrap
+        const float* p = v.a + (c[0] - 1) + (c[1] - 1) * v.sy + (c[2] - 1) * v.sz;
+        float acc = 0.f;
+#pragma unroll
+        for (int dz = 0; dz < 3; dz++)
+#pragma unroll
+            for (int dy = 0; dy < 3; dy++) {
+                const float* row = p + dy * v.sy + dz * v.sz;
+                const float* k = S + 9 * dz + 3 * dy;
+                acc += __ldg(&k[0]) * row[0] + __ldg(&k[1]) * row[1] + __ldg(&k[2]) * row[2];
+            }
+        return acc;
+    }
     float acc = 0.f;
 #pragma unroll
     for (int dz = -1; dz <= 1; dz++) {
@@ -218,6 +265,20 @@ __device__ float lp_net_op(const LView& v, const float* __restrict__ fold, const
     for (int ax = 0; ax < 3; ax++)
         if (!v.per[ax] && (c[ax] == 0 || c[ax] == v.n[ax] - 1)) interior = false;
     float acc = 0.f;
+    if (c[0] >= 2 && c[0] + 2 < v.n[0] && c[1] >= 2 && c[1] + 2 < v.n[1] && c[2] >= 2 && c[2] + 2 < v.n[2]) {
+        // all 125 taps inside the box: constant offsets
+        const float* p = v.a + (c[0] - 2) + (c[1] - 2) * v.sy + (c[2] - 2) * v.sz;
+        const float* K5 = fold + 729;
+        for (int dz = 0; dz < 5; dz++)
+#pragma unroll
+            for (int dy = 0; dy < 5; dy++) {
+                const float* row = p + dy * v.sy + dz * v.sz;
+                const float* k = K5 + 25 * dz + 5 * dy;
+#pragma unroll
+                for (int dx = 0; dx < 5; dx++) acc += __ldg(&k[dx]) * row[dx];
+            }
+        return acc;
+    }
     if (interior) {
         const float* K5 = fold + 729;
         for (int dz = -2; dz <= 2; dz++) {

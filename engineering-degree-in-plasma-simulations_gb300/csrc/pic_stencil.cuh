@@ -106,8 +106,8 @@ __device__ __forceinline__ void grid_sum(const float (&v)[N], double* part, int 
         double x = 0;
         for (int w = 0; w < nw; w++) x += s[threadIdx.x][w];
         part[threadIdx.x * stride + blockIdx.x] = x;
+        __threadfence();  // the writers publish their partials before the ticket is taken
     }
-    __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) s_last = (atomicAdd(ticket, 1u) == gridDim.x - 1) ? 1u : 0u;
     __syncthreads();
@@ -138,5 +138,14 @@ __device__ __forceinline__ float inv_diag_of(uint16_t kd, const float c[3]) {
         if (!(kd & (1u << (2 + d)))) dg += c[d >> 1];
     return 1.f / dg;
 }
+// the 64 inverse diagonals (one per mirror mask) in shared memory, filled by the block
+__device__ __forceinline__ void fill_inv_diag_table(float* tab, const GridDev& g) {
+    if (threadIdx.x < 64) {
+        const float c[3] = {g.inv_dx[0] * g.inv_dx[0], g.inv_dx[1] * g.inv_dx[1], g.inv_dx[2] * g.inv_dx[2]};
+        tab[threadIdx.x] = inv_diag_of((uint16_t)(threadIdx.x << 2), c);
+    }
+    __syncthreads();
+}
+__device__ __forceinline__ float inv_diag_lookup(const float* tab, uint16_t kd) { return tab[(kd >> 2) & 63]; }
 
 }  // namespace pic
