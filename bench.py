@@ -80,7 +80,7 @@ def setup_world(pic, wl, seed=1):
     E, S = sigma_tables()
     M = pic.MC_MEX_Ionization(e, i, W, wl["n_gas"], 300.0, 32 * AMU, LOTZ["I"], E, S, sigma_ion_kind=1,
                               sigma_ion_params=(LOTZ["A"], LOTZ["b"], LOTZ["c"], 0.0), seed=seed)
-    S_ = pic.PotentialSolver(W, 20000, 1e-6, pic.SOLVER_PCG)
+    S_ = pic.PotentialSolver(W, 20000, 1e-6, pic.SOLVER_LEARNED)
     W.configure_loop(solve_each_step=True, sort_every=20, merge_every=MERGE_EVERY, merge_after=0,
                      merge_min=MERGE_MIN)
     return W, e, i, M, S_
@@ -393,7 +393,8 @@ def run_gpu(args, wl, rank, ws, local):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
         "config": {"workload": wl["name"], "grid": list(wl["nn"]), "particles_per_step": parts_per_step,
-                   "poisson": "FP32 Jacobi-PCG in FP64 refinement to 1e-6 relative, warm-started",
+                   "poisson": "flexible CG with the learned multilevel preconditioner, FP32 iterations in "
+                                      "float-float refinement to 1e-6 relative, warm-started",
                    "collisions_per_step": coll["collisions"] / args.steps,
                    "ionizations_per_step": coll["ionizations"] / args.steps,
                    "poisson_inner_per_step": inner / args.steps, "sort_every": 20,
@@ -525,7 +526,7 @@ def run_e2e(pic, wl, args, rank):
     E, S = sigma_tables()
     pic.MC_MEX_Ionization(e, i, W, wl["n_gas"], 300.0, 32 * AMU, LOTZ["I"], E, S, sigma_ion_kind=1,
                           sigma_ion_params=(LOTZ["A"], LOTZ["b"], LOTZ["c"], 0.0), seed=1)
-    Sv = pic.PotentialSolver(W, 20000, 1e-6, pic.SOLVER_PCG)
+    Sv = pic.PotentialSolver(W, 20000, 1e-6, pic.SOLVER_LEARNED)
     W.configure_loop(solve_each_step=True, sort_every=20)
     import ctypes as C
 
@@ -537,6 +538,7 @@ def run_e2e(pic, wl, args, rank):
                                           C.c_void_p(w.data_ptr()), None, n, 1)
         if rc:
             raise RuntimeError("upload failed %d" % rc)
+        sp.sortIndexes()  # cell order, as after a sort step of the loop
     Sv.solve(raise_on_fail=True)
     Sv.computeEF()
     diag = np.zeros(5)

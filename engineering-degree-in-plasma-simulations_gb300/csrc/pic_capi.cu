@@ -746,6 +746,10 @@ extern "C" int pic_species_add_particles(pic_world* w, int sp, const double* pos
     return check_device_error(w);
 }
 
+namespace {
+int sort_species(pic_world* w, int sp);
+}  // namespace
+
 extern "C" int pic_species_load_uniform(pic_world* w, int sp, const double* lo, const double* hi, long n, double T,
                                         double w_mean, double w_sigma, uint64_t seed) {
     if (!valid_sp(w, sp) || !lo || !hi || n < 0) return fail(PIC_ERR_ARG, "bad arguments");
@@ -768,6 +772,7 @@ extern "C" int pic_species_load_uniform(pic_world* w, int sp, const double* lo, 
         Scope sc(w, "load", 2);
         launch_load_uniform(w->g, s.dev, la, w->stream);
     }
+    sort_species(w, sp);  // loaded particles leave in cell order, like after a sort step
     return check_device_error(w);
 }
 
@@ -796,6 +801,7 @@ extern "C" int pic_species_load_box_thermal(pic_world* w, int sp, const double* 
         Scope sc(w, "load", 2);
         launch_load_uniform(w->g, s.dev, la, w->stream);
     }
+    sort_species(w, sp);  // loaded particles leave in cell order, like after a sort step
     return check_device_error(w);
 }
 

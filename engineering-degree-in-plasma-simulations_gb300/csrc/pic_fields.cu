@@ -357,8 +357,7 @@ __global__ void __launch_bounds__(kNodeThreads) k_pcg_init(GridDev g, const floa
                                                            double* gpart, int gstride, unsigned* ticket,
                                                            double* scal, int* flag) {
     if (blockIdx.x == 0 && threadIdx.x == 0) flag[0] = 0;
-    __shared__ float idiag[64];
-    fill_inv_diag_table(idiag, g);
+    const float c3[3] = {g.inv_dx[0] * g.inv_dx[0], g.inv_dx[1] * g.inv_dx[1], g.inv_dx[2] * g.inv_dx[2]};
     float acc = 0.f;
     const int base = blockIdx.x * kNodeTile + threadIdx.x;
 #pragma unroll
@@ -373,7 +372,7 @@ __global__ void __launch_bounds__(kNodeThreads) k_pcg_init(GridDev g, const floa
             continue;
         }
         const float rr = r[n];
-        const float zz = rr * inv_diag_lookup(idiag, kd);
+        const float zz = rr * inv_diag_of(kd, c3);
         z[n] = zz;
         acc += rr * zz;
     }
@@ -444,8 +443,7 @@ __global__ void __launch_bounds__(kNodeThreads) k_pcg_k2(GridDev g, const float*
     const double dq = scal[kS_DQ];
     const double rz = scal[kS_RZ + (it & 1)];
     const float alpha = dq != 0.0 ? (float)(rz / dq) : 0.f;
-    __shared__ float idiag[64];
-    fill_inv_diag_table(idiag, g);
+    const float c3[3] = {g.inv_dx[0] * g.inv_dx[0], g.inv_dx[1] * g.inv_dx[1], g.inv_dx[2] * g.inv_dx[2]};
     float f0 = 0.f, f1 = 0.f, f2 = 0.f;
     const int base = blockIdx.x * kNodeTile + threadIdx.x;
 #pragma unroll
@@ -458,7 +456,7 @@ __global__ void __launch_bounds__(kNodeThreads) k_pcg_k2(GridDev g, const float*
         const float rn = r[n] - alpha * q[n];
         r[n] = rn;
         const float zo = z[n];
-        const float zn = rn * inv_diag_lookup(idiag, kd);
+        const float zn = rn * inv_diag_of(kd, c3);
         z[n] = zn;
         f0 += rn * zn;
         f1 += rn * zo;
