@@ -60,6 +60,14 @@ WORKLOADS = {
     "mid": dict(nn=(128, 128, 256), L=(0.04, 0.04, 0.08), V=1000.0, n_gas=2e21, n_each=12_500_000,
                 w_mean=40.96, dt=1e-12, name="mid discharge 128x128x256, 12.5M e- + 12.5M O2+"),
 }
+# BASELINE config 4: 64 independent discharges on 32 x 32 x 128 nodes (C2 physics), anodes spaced
+# uniformly over 200-800 V, background densities over 5e20-2e21 m^-3, particles per species per
+# instance log-uniform over 10k-2M; the instances are stacked along z in one world (instance slabs),
+# so every kernel launch advances all of them
+ENSEMBLE = dict(kind="ensemble", instances=64, nn=(32, 32, 128), L=(0.02, 0.02, 0.08), V=(200.0, 800.0),
+                n_gas=(5e20, 2e21), n_range=(10_000, 2_000_000), density=1e13, dt=2e-12,
+                name="ensemble of 64 discharges, 32x32x128 nodes each, stacked in one world")
+WORKLOADS["ensemble"] = ENSEMBLE
 MERGE_EVERY = 20  # merge pass cadence in the timed loop (the reference merges every 50 steps)
 MERGE_MIN = 64    # a cell is merged when it holds more than this many particles of a species
 
@@ -80,6 +88,41 @@ def setup_world(pic, wl, seed=1):
     E, S = sigma_tables()
     M = pic.MC_MEX_Ionization(e, i, W, wl["n_gas"], 300.0, 32 * AMU, LOTZ["I"], E, S, sigma_ion_kind=1,
                               sigma_ion_params=(LOTZ["A"], LOTZ["b"], LOTZ["c"], 0.0), seed=seed)
+    S_ = pic.PotentialSolver(W, 20000, 1e-6, pic.SOLVER_LEARNED)
+    W.configure_loop(solve_each_step=True, sort_every=20, merge_every=MERGE_EVERY, merge_after=0,
+                     merge_min=MERGE_MIN)
+    return W, e, i, M, S_
+
+
+def setup_ensemble(pic, wl, seed=1):
+    nI = wl["instances"]
+    ni, nj, nks = wl["nn"]
+    L = wl["L"]
+    dz = L[2] / (nks - 1)
+    nk = nI * nks
+    W = pic.World(ni, nj, nk, (0.0, 0.0, 0.0), (L[0], L[1], (nk - 1) * dz))
+    W.set_boundaries((1, 1, 0), (1,) * 6, (0.0,) * 6)
+    volts = np.linspace(wl["V"][0], wl["V"][1], nI)
+    W.set_slabs(np.zeros(nI), volts)
+    W.setTime(wl["dt"], 1 << 30)
+    rng = np.random.default_rng(seed)
+    counts = np.exp(rng.uniform(np.log(wl["n_range"][0]), np.log(wl["n_range"][1]), nI)).astype(np.int64)
+    band = L[0] * L[1] * 0.4 * L[2]
+    w_means = wl["density"] * band / counts
+    cap = int(counts.sum() * 1.25) + 4096
+    bound = float((counts * w_means).sum()) * 400.0
+    e = pic.Species("e-", ME, -QE, W, float(np.median(w_means)), capacity=cap, weight_bound=bound)
+    i = pic.Species("O2+", 32 * AMU, QE, W, float(np.median(w_means)), capacity=cap, weight_bound=bound)
+    for s_ in range(nI):
+        z0 = s_ * nks * dz
+        lo, hi = (0.0, 0.0, z0 + 0.3 * L[2]), (L[0], L[1], z0 + 0.7 * L[2])
+        e.loadUniform(lo, hi, int(counts[s_]), 2.0 * EV_K, w_means[s_], 0.5, seed=seed + 2 * s_)
+        i.loadUniform(lo, hi, int(counts[s_]), 0.03 * EV_K, w_means[s_], 0.5, seed=seed + 2 * s_ + 1)
+    E, S = sigma_tables()
+    dens = np.geomspace(wl["n_gas"][0], wl["n_gas"][1], nI)
+    M = pic.MC_MEX_Ionization(e, i, W, float(dens[0]), 300.0, 32 * AMU, LOTZ["I"], E, S, sigma_ion_kind=1,
+                              sigma_ion_params=(LOTZ["A"], LOTZ["b"], LOTZ["c"], 0.0), seed=seed)
+    M.set_slab_density(dens)
     S_ = pic.PotentialSolver(W, 20000, 1e-6, pic.SOLVER_LEARNED)
     W.configure_loop(solve_each_step=True, sort_every=20, merge_every=MERGE_EVERY, merge_after=0,
                      merge_min=MERGE_MIN)
@@ -311,7 +354,8 @@ def run_gpu(args, wl, rank, ws, local):
     import torch
 
     pic = importlib.import_module(PKG)
-    W, e, i, M, S = setup_world(pic, wl, seed=1 + rank)
+    ensemble = wl.get("kind") == "ensemble"
+    W, e, i, M, S = (setup_ensemble if ensemble else setup_world)(pic, wl, seed=1 + rank)
     assert S.solve(raise_on_fail=True)  # initial vacuum + space-charge field (main.cpp:172-173)
     S.computeEF()
     for _ in range(args.warmup):
@@ -347,7 +391,7 @@ def run_gpu(args, wl, rank, ws, local):
     value = aggregate(parts_per_step * args.steps, step_ms / 1e3, ws)
     # roofline of the dominant kernel group
     peak, peak_kind = measured_peak()
-    nv = int(np.prod(wl["nn"]))
+    nv = int(W.nv)
     inner = st1["inner"] - st0["inner"]
     refine = st1["refinements"] - st0["refinements"]
     n_e_avg = 0.5 * parts_per_step  # electrons ~ half
@@ -378,12 +422,12 @@ def run_gpu(args, wl, rank, ws, local):
     clocks = clk.summary()
     W.close()
     # e2e: same loop through the C ABI from pinned host buffers (upload + per-step diagnostics)
-    e2e = run_e2e(pic, wl, args, rank)
+    e2e = None if ensemble else run_e2e(pic, wl, args, rank)
     poisson = None
     if rank == 0 and args.poisson > 0:
         poisson = poisson_bench(pic, args.poisson)
     cpu = None
-    if rank == 0 and not args.no_cpu:
+    if rank == 0 and not args.no_cpu and not ensemble:
         cpu = cpu_reference(wl, inner / max(1, args.steps), sample=args.cpu_sample, steps=1)
         cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
     coll = {k: coll1[k] - coll0[k] for k in coll1}
@@ -392,7 +436,9 @@ def run_gpu(args, wl, rank, ws, local):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": wl["name"], "grid": list(wl["nn"]), "particles_per_step": parts_per_step,
+        "config": {"workload": wl["name"],
+                   "grid": list(wl["nn"]) + ([wl["instances"]] if ensemble else []),
+                   "particles_per_step": parts_per_step,
                    "poisson": "flexible CG with the learned multilevel preconditioner, FP32 iterations in "
                                       "float-float refinement to 1e-6 relative, warm-started",
                    "collisions_per_step": coll["collisions"] / args.steps,

@@ -101,6 +101,8 @@ def library():
         "pic_world_stream": [vp, pvp],
         "pic_number_density_noalloc": [i, i, i, vp, vp, vp, vp, vp, l, d, vp, vp],
         "pic_learned_levels": [vp, vp, vp, vp],
+        "pic_world_set_slabs": [vp, i, vp, vp],
+        "pic_mcc_set_slab_density": [vp, i, vp],
         "pic_learned_reset": [vp],
         "pic_learned_weights": [vp, vp, l, vp],
         "pic_learned_set_weights": [vp, vp, l],
@@ -194,6 +196,12 @@ class World:
         self.periodic = tuple(int(p) for p in periodic)
         _check(self._L.pic_world_set_boundaries(self._h, _p(np.asarray(periodic, np.int32)),
                                                 _p(np.asarray(face_mode, np.int32)), _p(_f64(face_phi))))
+
+    def set_slabs(self, phi_lo, phi_hi):
+        """Stack independent instances along z: slab s has electrodes at phi_lo[s] (bottom plane) and
+        phi_hi[s] (top plane); pass empty sequences for a single instance."""
+        lo, hi = _f64(phi_lo), _f64(phi_hi)
+        _check(self._L.pic_world_set_slabs(self._h, len(lo), _p(lo), _p(hi)))
 
     def dirichletBoundries(self, phi=0.0):
         """All walls Dirichlet at phi (World::dirichletBoundries, World.cpp:263-274)."""
@@ -499,6 +507,11 @@ class MC_MEX_Ionization:
 
     def apply(self, dt):
         _check(self.world._L.pic_mcc_apply(self.world._h, float(dt)))
+
+    def set_slab_density(self, n_neutral):
+        """Background density of every instance slab."""
+        n = _f64(n_neutral)
+        _check(self.world._L.pic_mcc_set_slab_density(self.world._h, len(n), _p(n)))
 
     def stats(self):
         out = np.zeros(4, np.uint64)

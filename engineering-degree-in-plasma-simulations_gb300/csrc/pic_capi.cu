@@ -104,6 +104,12 @@ struct pic_world {
         double c[3], s[3], phi;
     };
     std::vector<Box> boxes;
+    // stacked independent instances along z (0: one instance): electrode potentials per slab,
+    // neutral density per slab and the candidate probabilities derived from it
+    int nslabs = 0;
+    std::vector<double> slab_lo, slab_hi, slab_n;
+    float* p_null_slab = nullptr;
+    double p_null_slab_dt = -1.0;
     // time
     double dt = 1e-4;
     int num_ts = 0;
@@ -249,9 +255,18 @@ void build_kinds(pic_world* w, std::vector<uint16_t>& kind, std::vector<double>&
                     kind[n] = kFixed;
                     continue;
                 }
+                if (w->nslabs > 0) {
+                    // instance slabs: their first and last node planes are electrodes
+                    const int P = g.nk / w->nslabs, sl = k / P, lz = k - sl * P;
+                    if (lz == 0 || lz == P - 1) {
+                        kind[n] = kFixed;
+                        phi_host[n] = lz == 0 ? w->slab_lo[sl] : w->slab_hi[sl];
+                        continue;
+                    }
+                }
                 int fixed_face = -1, wall = 0;
                 for (int d = 0; d < 3; d++) {
-                    if (w->periodic[d]) continue;
+                    if (w->periodic[d] || (d == 2 && w->nslabs > 0)) continue;
                     for (int s = 0; s < 2; s++) {
                         int f = 2 * d + s;
                         if ((s == 0 && ijk[d] == 0) || (s == 1 && ijk[d] == nn[d] - 1)) {
@@ -327,6 +342,21 @@ void fill_grid_boxes(pic_world* w) {
         g.n_boxes++;
     }
     for (int d = 0; d < 3; d++) g.periodic[d] = w->periodic[d];
+}
+
+// candidate probabilities n_s (sigma v)_max dt of the instance slabs (uploaded when dt changes)
+int slab_candidate_probabilities(pic_world* w, double dt, CollDev& c) {
+    c.p_null_slab = nullptr;
+    if (w->slab_n.empty()) return PIC_OK;
+    if (w->p_null_slab_dt != dt) {
+        std::vector<float> pn(w->slab_n.size());
+        for (size_t q = 0; q < pn.size(); q++) pn[q] = (float)(w->slab_n[q] * w->mcc_sigv * dt);
+        CU(cudaMemcpyAsync(w->p_null_slab, pn.data(), sizeof(float) * pn.size(), cudaMemcpyHostToDevice, w->stream));
+        CU(cudaStreamSynchronize(w->stream));
+        w->p_null_slab_dt = dt;
+    }
+    c.p_null_slab = w->p_null_slab;
+    return PIC_OK;
 }
 
 void free_lp(pic_world* w) {
@@ -437,9 +467,9 @@ extern "C" int pic_world_create(pic_world** out, int ni, int nj, int nk, const d
     if (!out || !x0 || !xm) return fail(PIC_ERR_ARG, "null argument");
     *out = nullptr;
     if (ni < 2 || nj < 2 || nk < 2) return fail(PIC_ERR_ARG, "need at least 2 nodes per axis");
-    // particles store their cell packed as i | j << 10 | k << 20
-    if (ni - 1 > 1024 || nj - 1 > 1024 || nk - 1 > 2047)
-        return fail(PIC_ERR_ARG, "at most 1024 x 1024 x 2047 cells");
+    // particles store their cell packed as i | j << 9 | k << 18
+    if (ni - 1 > kCellMaxIJ || nj - 1 > kCellMaxIJ || nk - 1 > kCellMaxK)
+        return fail(PIC_ERR_ARG, "at most %d x %d x %d cells", kCellMaxIJ, kCellMaxIJ, kCellMaxK);
     long long nv = (long long)ni * nj * nk;
     if (nv > (1ll << 30)) return fail(PIC_ERR_ARG, "grid too large (%lld nodes)", nv);
     for (int d = 0; d < 3; d++)
@@ -517,6 +547,7 @@ extern "C" int pic_world_destroy(pic_world* w) {
     if (w->stream) cudaStreamSynchronize(w->stream);
     free_lp(w);
     if (w->rho_prev) cudaFree(w->rho_prev);
+    if (w->p_null_slab) cudaFree(w->p_null_slab);
     if (w->bfix) cudaFree(w->bfix);
     for (auto& s : w->sp) {
         cudaFree(s.dev.pos);
@@ -596,6 +627,24 @@ extern "C" int pic_world_add_box(pic_world* w, const double* center, const doubl
     b.phi = phi;
     w->boxes.push_back(b);
     fill_grid_boxes(w);
+    return upload_kinds(w, false);
+}
+
+extern "C" int pic_world_set_slabs(pic_world* w, int nslabs, const double* phi_lo, const double* phi_hi) {
+    if (!w || nslabs < 0 || (nslabs > 0 && (!phi_lo || !phi_hi))) return fail(PIC_ERR_ARG, "bad arguments");
+    CU(cudaSetDevice(w->device));
+    GridDev& g = w->g;
+    if (nslabs > 0) {
+        if (w->periodic[2]) return fail(PIC_ERR_ARG, "instance slabs need a non-periodic z axis");
+        if (g.nk % nslabs || g.nk / nslabs < 3)
+            return fail(PIC_ERR_ARG, "%d z nodes do not split into %d slabs of at least 3 nodes", g.nk, nslabs);
+    }
+    w->nslabs = nslabs;
+    w->slab_lo.assign(phi_lo, phi_lo + nslabs);
+    w->slab_hi.assign(phi_hi, phi_hi + nslabs);
+    g.zslab = nslabs > 0 ? g.nk / nslabs : 0;
+    g.fd_zslab = make_fastdiv((unsigned)(g.zslab > 1 ? g.zslab : 2));
+    if (w->lp) free_lp(w);
     return upload_kinds(w, false);
 }
 
@@ -866,6 +915,8 @@ int push_species(pic_world* w, int sp, double dt, int deposit, bool with_mcc, bo
         a.coll = w->coll;
         a.coll.enabled = 1;
         a.coll.p_null = (float)(w->mcc_n * w->mcc_sigv * dt);
+        int prc = slab_candidate_probabilities(w, dt, a.coll);
+        if (prc) return prc;
         a.coll.step = (unsigned)w->ts;
         a.coll.ion = w->sp[w->mcc_i].dev;
     }
@@ -1592,6 +1643,17 @@ extern "C" int pic_mcc_create(pic_world* w, int electrons, int ions, double n_ne
     return PIC_OK;
 }
 
+extern "C" int pic_mcc_set_slab_density(pic_world* w, int nslabs, const double* n_neutral) {
+    if (!w || !w->mcc_on) return fail(PIC_ERR_ARG, "no collision model");
+    if (nslabs != w->nslabs || nslabs <= 0 || !n_neutral)
+        return fail(PIC_ERR_ARG, "one density per instance slab (%d slabs)", w->nslabs);
+    CU(cudaSetDevice(w->device));
+    if (!w->p_null_slab) CU(cudaMalloc(&w->p_null_slab, sizeof(float) * nslabs));
+    w->slab_n.assign(n_neutral, n_neutral + nslabs);
+    w->p_null_slab_dt = -1.0;
+    return PIC_OK;
+}
+
 extern "C" int pic_mcc_apply(pic_world* w, double dt) {
     if (!w || !w->mcc_on) return fail(PIC_ERR_ARG, "no collision model");
     CU(cudaSetDevice(w->device));
@@ -1608,6 +1670,8 @@ extern "C" int pic_mcc_apply(pic_world* w, double dt) {
     a.coll = w->coll;
     a.coll.enabled = 1;
     a.coll.p_null = (float)(w->mcc_n * w->mcc_sigv * dt);
+    int prc = slab_candidate_probabilities(w, dt, a.coll);
+    if (prc) return prc;
     a.coll.step = (unsigned)w->ts;
     a.coll.ion = w->sp[w->mcc_i].dev;
     // collisions only: dt/dx = 0 keeps every particle in place, the products are not pushed

@@ -58,7 +58,16 @@ struct GridDev {
     double x0[3], xm[3], dxd[3];
     int n_boxes;
     float box_lo[kMaxBoxes][3], box_hi[kMaxBoxes][3];  // absorbing objects, absolute coordinates
+    // independent instances stacked along z: zslab nodes per instance (0: one instance); the
+    // first and last node plane of every slab are Dirichlet electrodes, the cell between two
+    // slabs is outside every instance
+    int zslab;
+    FastDiv fd_zslab;
 };
+// z index of a node or cell inside its instance slab (the global index without slabs)
+__device__ __forceinline__ int slab_local_z(const GridDev& g, int k) {
+    return g.zslab ? k - (int)fdiv((unsigned)k, g.fd_zslab) * g.zslab : k;
+}
 
 struct SpeciesDev {
     float4* pos;
@@ -100,17 +109,22 @@ __device__ __forceinline__ void set_error(unsigned* err, unsigned bit) {
     if (err) atomicOr(err, bit);
 }
 
-// A particle's cell is stored packed, i | j << 10 | k << 20 (i, j < 1024, k < 2048): decoding
+// A particle's cell is stored packed, i | j << 9 | k << 18 (i, j < 512, k < 8192): decoding
 // needs no division, and the packed value orders cells exactly like the linear index
 // c = (k*(nj-1) + j)*(ni-1) + i of World::XtoC, which the sort and the cell lists use.
-__device__ __forceinline__ int pack_cell(int i, int j, int k) { return i | (j << 10) | (k << 20); }
+constexpr int kCellMaxIJ = 512, kCellMaxK = 8192;
+__host__ __device__ __forceinline__ int pack_cell(int i, int j, int k) { return i | (j << 9) | (k << 18); }
 __device__ __forceinline__ void cell_ijk(const GridDev&, int c, int& i, int& j, int& k) {
-    i = c & 1023;
-    j = (c >> 10) & 1023;
-    k = c >> 20;
+    i = c & 511;
+    j = (c >> 9) & 511;
+    k = c >> 18;
 }
 __device__ __forceinline__ int cell_linear(const GridDev& g, int c) {
-    return ((c >> 20) * g.cj + ((c >> 10) & 1023)) * g.ci + (c & 1023);
+    return ((c >> 18) * g.cj + ((c >> 9) & 511)) * g.ci + (c & 511);
+}
+// base node of the packed cell c
+__device__ __forceinline__ int cell_base(const GridDev& g, int c) {
+    return ((c >> 18) * g.nj + ((c >> 9) & 511)) * g.ni + (c & 511);
 }
 // linear cell index -> (i, j, k)
 __device__ __forceinline__ void linear_ijk(const GridDev& g, int c, int& i, int& j, int& k) {

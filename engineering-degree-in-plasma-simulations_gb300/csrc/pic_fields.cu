@@ -36,6 +36,9 @@ __global__ void k_finalize_rho(FinalizeArgs a) {
             if (g.periodic[d]) {
                 if (ijk[d] == nn[d] - 1) alias = true;
                 if (ijk[d] == 0) fold |= 1u << d;
+            } else if (d == 2 && g.zslab) {
+                const int lz = slab_local_z(g, ijk[2]);
+                if (lz == 0 || lz == g.zslab - 1) inv_vol *= 2.f;  // faces of the instance slab
             } else if (ijk[d] == 0 || ijk[d] == nn[d] - 1) {
                 inv_vol *= 2.f;
             }
@@ -112,7 +115,9 @@ __global__ void k_efield(GridDev g, const float2* __restrict__ phi, float4* __re
         node_ijk(g, n, ijk[0], ijk[1], ijk[2]);
         float e[3];
         for (int d = 0; d < 3; d++) {
-            const int c = ijk[d], st = stride[d], N = nn[d];
+            // along z, a stacked instance's slab is its own domain
+            const int c = d == 2 ? slab_local_z(g, ijk[2]) : ijk[d];
+            const int st = stride[d], N = (d == 2 && g.zslab) ? g.zslab : nn[d];
             float v;
             if (g.periodic[d]) {
                 int cc = (c == N - 1) ? 0 : c;

@@ -10,6 +10,7 @@ int set_last_error(int code, const char* msg);  // message for pic_last_error
 struct CollDev {
     int enabled;
     float p_null;            // n_n (sigma v)_max dt : candidate probability
+    const float* p_null_slab;  // per instance slab (stacked instances with their own n_n), or nullptr
     float sigv_max;          // (sigma v)_max [m^3/s]
     float sig_n;             // sqrt(k T_n / m_n): neutral thermal speed per axis
     float m_n, m_e;

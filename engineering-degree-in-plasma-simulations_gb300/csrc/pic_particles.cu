@@ -190,6 +190,7 @@ __device__ __forceinline__ int move_particle(const PushArgs& a, int i, int j, in
         while (k >= g.ck) k -= g.ck;
     }
     if ((unsigned)i >= (unsigned)g.ci || (unsigned)j >= (unsigned)g.cj || (unsigned)k >= (unsigned)g.ck) return -1;
+    if (g.zslab && slab_local_z(g, k) == g.zslab - 1) return -1;  // the cell between two instance slabs
     if (g.n_boxes) {
         float X = ((float)i + o.x) * g.dx[0], Y = ((float)j + o.y) * g.dx[1], Z = ((float)k + o.z) * g.dx[2];
         for (int bx = 0; bx < g.n_boxes; bx++)
@@ -429,7 +430,7 @@ __global__ void __launch_bounds__(kThreads, kMcc ? 2 : 3) k_push(PushArgs a) {
                 V[q] = pvel[x];
                 if (kMcc) ID[q] = pid[x];
                 const int c = __float_as_int(P[q].w);
-                if (c >= 0) bn[q] = ((c >> 20) * g.nj + ((c >> 10) & 1023)) * g.ni + (c & 1023);
+                if (c >= 0) bn[q] = cell_base(g, c);
             }
         }
         // ---- window: +-kHalfWin base nodes around the base node of the chunk's middle particle
@@ -437,7 +438,7 @@ __global__ void __launch_bounds__(kThreads, kMcc ? 2 : 3) k_push(PushArgs a) {
         {
             const int c = __float_as_int(ppos[nin >> 1].w);
             if (c >= 0) {
-                const int anchor = ((c >> 20) * g.nj + ((c >> 10) & 1023)) * g.ni + (c & 1023);
+                const int anchor = cell_base(g, c);
                 lo = max(0, anchor - kHalfWin);
                 hi = min(anchor + kHalfWin, max_base);
             }
@@ -490,7 +491,8 @@ __global__ void __launch_bounds__(kThreads, kMcc ? 2 : 3) k_push(PushArgs a) {
             dead_mask[q] = 0;
             if (bn[q] < 0) continue;
             int c = __float_as_int(P[q].w);
-            int i = c & 1023, j = (c >> 10) & 1023, k = c >> 20;
+            int i, j, k;
+            cell_ijk(g, c, i, j, k);
             float3 o = make_float3(P[q].x, P[q].y, P[q].z);
             float3 v = make_float3(V[q].x, V[q].y, V[q].z);
             const float w = V[q].w;
@@ -501,7 +503,9 @@ __global__ void __launch_bounds__(kThreads, kMcc ? 2 : 3) k_push(PushArgs a) {
                 const CollDev& cd = a.coll;
                 id = ID[q];
                 uint4 r0 = philox4x32_10(make_uint4((unsigned)id, (unsigned)(id >> 32), cd.step, 0u), cd.key);
-                if (u01(r0.x) < cd.p_null) {
+                const float p_null =
+                    cd.p_null_slab ? __ldg(&cd.p_null_slab[fdiv((unsigned)k, g.fd_zslab)]) : cd.p_null;
+                if (u01(r0.x) < p_null) {
                     st_cand++;
                     col = collide_candidate(cd, id, v, r0);
                     if (col.kind) {
@@ -537,7 +541,7 @@ __global__ void __launch_bounds__(kThreads, kMcc ? 2 : 3) k_push(PushArgs a) {
                             tg.dtile = nullptr;  // products go straight to HBM
                             Corners pcn;
                             corner_values(w, po, a.dep_scale, pcn, false);
-                            commit_corners(a, tg, ((pc >> 20) * g.nj + ((pc >> 10) & 1023)) * g.ni + (pc & 1023), pcn);
+                            commit_corners(a, tg, cell_base(g, pc), pcn);
                         }
                     } else {
                         st_lost++;
@@ -549,8 +553,7 @@ __global__ void __launch_bounds__(kThreads, kMcc ? 2 : 3) k_push(PushArgs a) {
             if (newc >= 0) {
                 if (a.deposit) {
                     if (newc != run_cell && run_cell >= 0)
-                        commit_corners(a, t, ((run_cell >> 20) * g.nj + ((run_cell >> 10) & 1023)) * g.ni +
-                                                 (run_cell & 1023), run);
+                        commit_corners(a, t, cell_base(g, run_cell), run);
                     corner_values(w, o, a.dep_scale, run, newc == run_cell);
                     run_cell = newc;
                 }
@@ -559,8 +562,7 @@ __global__ void __launch_bounds__(kThreads, kMcc ? 2 : 3) k_push(PushArgs a) {
             }
         }
         if (run_cell >= 0)
-            commit_corners(a, t, ((run_cell >> 20) * g.nj + ((run_cell >> 10) & 1023)) * g.ni + (run_cell & 1023),
-                           run);
+            commit_corners(a, t, cell_base(g, run_cell), run);
         // warp-aggregated record of the particles that left the domain
 #pragma unroll
         for (int q = 0; q < kPPT; q++) {

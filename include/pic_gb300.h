@@ -48,6 +48,12 @@ int pic_world_get_ts(pic_world* w, int* ts);
 int pic_world_set_boundaries(pic_world* w, const int* periodic, const int* face_mode, const double* face_phi);
 /* World::addObject<Rectangle>(pos, phi, sides) + computeObjectID     World.h:118-130, Object.cpp:231-238:
  * nodes inside the box are Dirichlet at phi; particles entering it are absorbed. */
+/* Stacked independent instances (no reference counterpart): the z nodes split into nslabs equal
+ * slabs; each slab is one instance whose first and last node planes are Dirichlet electrodes at
+ * phi_lo[s] and phi_hi[s] (the reference's cathode/anode planes), and the cell between two slabs
+ * belongs to no instance (particles entering it are absorbed).  Every kernel launch then advances
+ * all instances at once.  nslabs = 0 returns to a single instance. */
+int pic_world_set_slabs(pic_world* w, int nslabs, const double* phi_lo, const double* phi_hi);
 int pic_world_add_box(pic_world* w, const double* center, const double* sides, double phi);
 /* public fields World::phi, rho, node_vol, ef                        World.h:51-54
  * which: 0 phi, 1 rho, 2 node_vol, 3 ef (3 values per node)          */
@@ -175,6 +181,8 @@ int pic_mcc_create(pic_world* w, int electrons, int ions, double n_neutral, doub
                    const double* table_E, const double* table_s, int table_n, uint64_t seed);
 /* Interaction::apply(dt): collisions of every electron for the current step (no push). */
 int pic_mcc_apply(pic_world* w, double dt);
+/* background density per instance slab (one value per slab of pic_world_set_slabs) */
+int pic_mcc_set_slab_density(pic_world* w, int nslabs, const double* n_neutral);
 /* counters since creation: candidates, collisions, ionisations, products lost */
 int pic_mcc_stats(pic_world* w, uint64_t* out);
 
@@ -200,7 +208,7 @@ int pic_merge_stats(pic_world* w, uint64_t* out);
  * running under CUDA graph capture, plugins whose host owns all device memory, real-time
  * loops that forbid allocation): the number density of one species from particle arrays the
  * caller already holds on the current device, in the library's layout (pos4: float4 {ox, oy,
- * oz, packed cell i | j<<10 | k<<20}; vel4: float4 {vx, vy, vz, w}), written to den_out (FP32,
+ * oz, packed cell i | j<<9 | k<<18}; vel4: float4 {vx, vy, vz, w}), written to den_out (FP32,
  * one value per node, node order as above).  Same CIC weights and 64-bit fixed-point sums as
  * Species::computeNumberDensity (Species.cpp:401-416) with fixed-point scale `scale`.
  * The working accumulator is a library-owned device array of 2^20 nodes (8 MiB per GPU, held

@@ -24,7 +24,7 @@ def library_layout(pos, w, torch):
     lc = (pos - x0) / dx
     c = np.minimum(np.maximum(lc.astype(np.int64), 0), nn - 2)
     off = np.minimum((lc - c).astype(np.float32), np.float32(np.nextafter(np.float32(1), np.float32(0))))
-    cell = (c[:, 0] | (c[:, 1] << 10) | (c[:, 2] << 20)).astype(np.int32)
+    cell = (c[:, 0] | (c[:, 1] << 9) | (c[:, 2] << 18)).astype(np.int32)
     p4 = np.zeros((len(w), 4), np.float32)
     p4[:, :3] = off
     p4[:, 3] = cell.view(np.float32)
