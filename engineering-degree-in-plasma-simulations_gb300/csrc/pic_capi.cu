@@ -110,6 +110,8 @@ struct pic_world {
     std::vector<double> slab_lo, slab_hi, slab_n;
     float* p_null_slab = nullptr;
     double p_null_slab_dt = -1.0;
+    int* mcc_cand = nullptr;   // collision candidates of a step (electron capacity)
+    int* mcc_ncand = nullptr;
     // time
     double dt = 1e-4;
     int num_ts = 0;
@@ -548,6 +550,8 @@ extern "C" int pic_world_destroy(pic_world* w) {
     free_lp(w);
     if (w->rho_prev) cudaFree(w->rho_prev);
     if (w->p_null_slab) cudaFree(w->p_null_slab);
+    if (w->mcc_cand) cudaFree(w->mcc_cand);
+    if (w->mcc_ncand) cudaFree(w->mcc_ncand);
     if (w->bfix) cudaFree(w->bfix);
     for (auto& s : w->sp) {
         cudaFree(s.dev.pos);
@@ -924,9 +928,16 @@ int push_species(pic_world* w, int sp, double dt, int deposit, bool with_mcc, bo
         s.deposited = true;
         CU(cudaMemsetAsync(s.dev.acc, 0, sizeof(unsigned long long) * w->g.nv, w->stream));
     }
+    if (a.coll.enabled) {
+        // collisions first (they may deposit ejected electrons), then a collision-free push
+        Scope sc(w, "mcc", 3);
+        launch_mcc(a, w->mcc_cand, w->mcc_ncand, w->stream, w->sms);
+    }
     {
         Scope sc(w, deposit ? "push_deposit" : "push", 1);
-        launch_push(a, w->stream, a.coll.enabled ? w->grid_push_mcc : w->grid_push);
+        PushArgs ap = a;
+        ap.coll.enabled = 0;
+        launch_push(ap, w->stream, w->grid_push);
     }
     {
         Scope sc(w, "compact", a.coll.enabled ? 5 : 4);
@@ -1601,6 +1612,9 @@ extern "C" int pic_mcc_create(pic_world* w, int electrons, int ions, double n_ne
     if (w->tE) cudaFree(w->tE);
     if (w->tS) cudaFree(w->tS);
     if (!w->stats) CU(cudaMalloc((void**)&w->stats, sizeof(unsigned long long) * 4));
+    if (w->mcc_cand) cudaFree(w->mcc_cand);
+    CU(cudaMalloc((void**)&w->mcc_cand, sizeof(int) * (size_t)w->sp[electrons].capacity));
+    if (!w->mcc_ncand) CU(cudaMalloc((void**)&w->mcc_ncand, sizeof(int)));
     CU(cudaMalloc((void**)&w->tE, sizeof(float) * table_n));
     CU(cudaMalloc((void**)&w->tS, sizeof(float) * table_n));
     CU(cudaMemcpy(w->tE, Ef.data(), sizeof(float) * table_n, cudaMemcpyHostToDevice));
@@ -1676,8 +1690,8 @@ extern "C" int pic_mcc_apply(pic_world* w, double dt) {
     a.coll.ion = w->sp[w->mcc_i].dev;
     // collisions only: dt/dx = 0 keeps every particle in place, the products are not pushed
     {
-        Scope sc(w, "mcc", 3);
-        launch_push(a, w->stream, w->grid_push_mcc);
+        Scope sc(w, "mcc", 5);
+        launch_mcc(a, w->mcc_cand, w->mcc_ncand, w->stream, w->sms);
         launch_commit_appends(s.dev, w->err, w->stream);
         launch_commit_appends(w->sp[w->mcc_i].dev, w->err, w->stream);
     }

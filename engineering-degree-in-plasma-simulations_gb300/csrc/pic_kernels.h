@@ -44,6 +44,9 @@ struct PushArgs {
 
 // particles
 void launch_push(const PushArgs& a, cudaStream_t s, int grid);
+// collisions of a.coll for the electrons a.sp as two passes (candidates, their collisions); the
+// push that follows runs without collisions.  cand holds up to the species capacity.
+void launch_mcc(const PushArgs& a, int* cand, int* ncand, cudaStream_t s, int sms);
 void launch_commit_appends(SpeciesDev sp, unsigned* err, cudaStream_t s);
 void launch_compact(SpeciesDev sp, cudaStream_t s, int grid);
 void launch_sort(const GridDev& g, SpeciesDev sp, float4* pos_alt, float4* vel_alt, unsigned long long* id_alt,

@@ -597,6 +597,117 @@ __global__ void __launch_bounds__(kThreads, kMcc ? 2 : 3) k_push(PushArgs a) {
     }
 }
 
+// ------------------------------------------------------------------------------------
+// collisions as separate passes ahead of a collision-free push:
+//   candidates: one Philox draw per electron (u01(r0.x) < p_null), a list of candidates
+//   collide   : the collisions of the candidates (same draws as the fused kernel: the streams are
+//               keyed by (seed, step, id)); the ejected electron is pushed and deposited there,
+//               the ion product appended
+// The split keeps the push kernel free of the collision registers and code.
+// ------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_mcc_candidates(PushArgs a, int* cand, int* ncand) {
+    const CollDev& cd = a.coll;
+    const GridDev& g = a.g;
+    const int n = a.sp.counts[0];
+    unsigned st_cand = 0;
+    const int lane = threadIdx.x & 31;
+    for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const int p = base + threadIdx.x;
+        bool is_cand = false;
+        if (p < n) {
+            const unsigned long long id = a.sp.id[p];
+            float p_null = cd.p_null;
+            if (cd.p_null_slab) {
+                const int c = __float_as_int(a.sp.pos[p].w);
+                if (c >= 0) p_null = __ldg(&cd.p_null_slab[fdiv((unsigned)(c >> 18), g.fd_zslab)]);
+            }
+            const uint4 r0 = philox4x32_10(make_uint4((unsigned)id, (unsigned)(id >> 32), cd.step, 0u), cd.key);
+            is_cand = u01(r0.x) < p_null;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, is_cand);
+        if (m) {
+            int b0 = 0;
+            if (lane == __ffs(m) - 1) b0 = atomicAdd(ncand, __popc(m));
+            b0 = __shfl_sync(0xffffffffu, b0, __ffs(m) - 1);
+            if (is_cand) cand[b0 + __popc(m & ((1u << lane) - 1u))] = p;
+        }
+        st_cand += is_cand ? 1u : 0u;
+    }
+    const unsigned x = __reduce_add_sync(0xffffffffu, st_cand);
+    if (lane == 0 && x) atomicAdd(&cd.stats[0], (unsigned long long)x);
+}
+
+__global__ void __launch_bounds__(128) k_mcc_collide(PushArgs a, const int* cand, const int* ncand) {
+    const CollDev& cd = a.coll;
+    const GridDev& g = a.g;
+    const int n = a.sp.counts[0];
+    const int ion_n = cd.ion.counts[0];
+    const int nc = *ncand;
+    unsigned st_coll = 0, st_ion = 0, st_lost = 0;
+    Tile t;  // no staged rows: gathers and deposits go to HBM
+    t.etile = nullptr;
+    t.dtile = nullptr;
+    t.lo = 0;
+    t.span = -1;
+    t.off[0] = 0;
+    t.off[1] = g.ni;
+    t.off[2] = g.ni * g.nj;
+    t.off[3] = g.ni * g.nj + g.ni;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nc; q += gridDim.x * blockDim.x) {
+        const int p = cand[q];
+        const float4 P = a.sp.pos[p];
+        const float4 V = a.sp.vel[p];
+        const int c = __float_as_int(P.w);
+        if (c < 0) continue;
+        int i, j, k;
+        cell_ijk(g, c, i, j, k);
+        const unsigned long long id = a.sp.id[p];
+        const uint4 r0 = philox4x32_10(make_uint4((unsigned)id, (unsigned)(id >> 32), cd.step, 0u), cd.key);
+        const float w = V.w;
+        Collision col = collide_candidate(cd, id, make_float3(V.x, V.y, V.z), r0);
+        if (!col.kind) continue;
+        st_coll++;
+        a.sp.vel[p] = make_float4(col.v.x, col.v.y, col.v.z, w);
+        if (col.kind != 2) continue;
+        st_ion++;
+        // the ejected electron and the ion are created at a uniform point of the parent's cell
+        // without velocity rewind; the electron is pushed and deposited now
+        if (!append_particle(cd.ion, ion_n, make_float4(col.po.x, col.po.y, col.po.z, __int_as_float(c)),
+                             make_float4(col.nv.x, col.nv.y, col.nv.z, w), child_id(id, cd.step, 2), a.err))
+            st_lost++;
+        float3 po = col.po, pv = col.pv;
+        const float3 Ep = gather_e(a, t, cell_base(g, c), po);
+        pv.x += a.qm_dt * Ep.x;
+        pv.y += a.qm_dt * Ep.y;
+        pv.z += a.qm_dt * Ep.z;
+        const int pc = move_particle(a, i, j, k, po, pv);
+        if (pc < 0) continue;
+        if (append_particle(a.sp, n, make_float4(po.x, po.y, po.z, __int_as_float(pc)),
+                            make_float4(pv.x, pv.y, pv.z, w), child_id(id, cd.step, 1), a.err)) {
+            if (a.deposit) {
+                Corners pcn;
+                corner_values(w, po, a.dep_scale, pcn, false);
+                commit_corners(a, t, cell_base(g, pc), pcn);
+            }
+        } else {
+            st_lost++;
+        }
+    }
+    const unsigned v[3] = {st_coll, st_ion, st_lost};
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int x = 0; x < 3; x++) {
+        const unsigned s = __reduce_add_sync(0xffffffffu, v[x]);
+        if (lane == 0 && s) atomicAdd(&cd.stats[1 + x], (unsigned long long)s);
+    }
+}
+
+void launch_mcc(const PushArgs& a, int* cand, int* ncand, cudaStream_t s, int sms) {
+    cudaMemsetAsync(ncand, 0, sizeof(int), s);
+    k_mcc_candidates<<<sms * 8, 256, 0, s>>>(a, cand, ncand);
+    k_mcc_collide<<<sms * 4, 128, 0, s>>>(a, cand, ncand);
+}
+
 void launch_push(const PushArgs& a, cudaStream_t s, int grid) {
     static bool attr = false;
     if (!attr) {
