@@ -23,10 +23,8 @@ constexpr int kHalfWin = (kSeg - kMargin - 2) / 2;  // staged base nodes either 
 // shared memory of the push: the next chunk's particles (pos, vel, and ids with collisions),
 // the E rows (float4) and the fixed-point deposit tile (three 21-bit limb planes of 32-bit
 // counters), four rows of kSeg nodes each
-__host__ __device__ constexpr size_t kPbufBytes(bool mcc) { return (size_t)kChunk * (2 * sizeof(float4) + (mcc ? 8 : 0)); }
-__host__ __device__ constexpr size_t kPushSmem(bool mcc) {
-    return kPbufBytes(mcc) + 4 * kSeg * sizeof(float4) + 3 * 4 * kSeg * sizeof(unsigned);
-}
+constexpr size_t kPbufBytes = (size_t)kChunk * 2 * sizeof(float4);
+constexpr size_t kPushSmem = kPbufBytes + 4 * kSeg * sizeof(float4) + 3 * 4 * kSeg * sizeof(unsigned);
 constexpr long long kWaitLimit = 1ll << 24;  // mbarrier polls before giving up
 
 // ------------------------------------------------------------------------------------
@@ -335,7 +333,7 @@ __device__ __noinline__ Collision collide_candidate(const CollDev& cd, unsigned 
 }
 
 // ------------------------------------------------------------------------------------
-// fused collide + push + deposit
+// push + deposit (collisions run before it, k_mcc_candidates / k_mcc_collide)
 //   A CTA takes chunks of 1024 particles (4 consecutive per thread), software-pipelined: the
 //   next chunk's particle arrays are bulk-copied (TMA) into shared memory while the current
 //   chunk is processed.  For each chunk the four node rows around the base node of its middle
@@ -344,24 +342,20 @@ __device__ __noinline__ Collision collide_candidate(const CollDev& cd, unsigned 
 //   HBM with one atomic per touched node.  Particles outside the window use HBM directly.
 // ------------------------------------------------------------------------------------
 // bulk copy of one full chunk's particle arrays into the staging buffer
-template <bool kMcc>
 __device__ __forceinline__ void issue_chunk(const SpeciesDev& sp, int base, float4* ppos, float4* pvel,
-                                            unsigned long long* pid, unsigned long long* bar) {
+                                            unsigned long long* bar) {
     const unsigned b16 = kChunk * sizeof(float4);
     fence_proxy_async();
-    mbar_expect_tx(bar, 2 * b16 + (kMcc ? kChunk * 8u : 0u));
+    mbar_expect_tx(bar, 2 * b16);
     bulk_g2s(ppos, sp.pos + base, b16, bar);
     bulk_g2s(pvel, sp.vel + base, b16, bar);
-    if (kMcc) bulk_g2s(pid, sp.id + base, kChunk * 8u, bar);
 }
 
-template <bool kMcc>
-__global__ void __launch_bounds__(kThreads, kMcc ? 2 : 3) k_push(PushArgs a) {
+__global__ void __launch_bounds__(kThreads, 3) k_push(PushArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
     float4* ppos = reinterpret_cast<float4*>(smem);
     float4* pvel = ppos + kChunk;
-    unsigned long long* pid = reinterpret_cast<unsigned long long*>(pvel + kChunk);
-    float4* etile = reinterpret_cast<float4*>(smem + kPbufBytes(kMcc));
+    float4* etile = reinterpret_cast<float4*>(smem + kPbufBytes);
     unsigned* dtile = reinterpret_cast<unsigned*>(etile + 4 * kSeg);
     __shared__ __align__(8) unsigned long long bar_p, bar_e;
     __shared__ int s_fail;
@@ -369,10 +363,8 @@ __global__ void __launch_bounds__(kThreads, kMcc ? 2 : 3) k_push(PushArgs a) {
     const GridDev& g = a.g;
     const int tid = threadIdx.x, lane = tid & 31;
     const int n = a.sp.counts[0];
-    const int ion_n = kMcc ? a.coll.ion.counts[0] : 0;
     const int nchunks = (n + kChunk - 1) / kChunk;
     const int nij = g.ni * g.nj;
-    unsigned st_cand = 0, st_coll = 0, st_ion = 0, st_lost = 0;
 
     if (tid == 0) {
         mbar_init(&bar_p, 1);
@@ -392,7 +384,7 @@ __global__ void __launch_bounds__(kThreads, kMcc ? 2 : 3) k_push(PushArgs a) {
 
     int ch = blockIdx.x;
     bool pending = false;  // a particle bulk copy into the staging buffer is in flight
-    if (ch < nchunks && (ch + 1) * kChunk <= n && tid == 0) issue_chunk<kMcc>(a.sp, ch * kChunk, ppos, pvel, pid, &bar_p);
+    if (ch < nchunks && (ch + 1) * kChunk <= n && tid == 0) issue_chunk(a.sp, ch * kChunk, ppos, pvel, &bar_p);
     pending = ch < nchunks && (ch + 1) * kChunk <= n;
 
     for (; ch < nchunks; ch += gridDim.x) {
@@ -414,12 +406,10 @@ __global__ void __launch_bounds__(kThreads, kMcc ? 2 : 3) k_push(PushArgs a) {
             for (int x = tid; x < nin; x += kThreads) {
                 ppos[x] = a.sp.pos[base + x];
                 pvel[x] = a.sp.vel[base + x];
-                if (kMcc) pid[x] = a.sp.id[base + x];
             }
             __syncthreads();
         }
         float4 P[kPPT], V[kPPT];
-        unsigned long long ID[kPPT];
         int bn[kPPT];
 #pragma unroll
         for (int q = 0; q < kPPT; q++) {
@@ -428,7 +418,6 @@ __global__ void __launch_bounds__(kThreads, kMcc ? 2 : 3) k_push(PushArgs a) {
             if (x < nin) {
                 P[q] = ppos[x];
                 V[q] = pvel[x];
-                if (kMcc) ID[q] = pid[x];
                 const int c = __float_as_int(P[q].w);
                 if (c >= 0) bn[q] = cell_base(g, c);
             }
@@ -454,7 +443,7 @@ __global__ void __launch_bounds__(kThreads, kMcc ? 2 : 3) k_push(PushArgs a) {
                 for (int m = 0; m < 4; m++) bulk_g2s(etile + m * kSeg, a.ef + lo + t.off[m], bytes, &bar_e);
             }
             const int nx = ch + gridDim.x;
-            if (nx < nchunks && (nx + 1) * kChunk <= n) issue_chunk<kMcc>(a.sp, nx * kChunk, ppos, pvel, pid, &bar_p);
+            if (nx < nchunks && (nx + 1) * kChunk <= n) issue_chunk(a.sp, nx * kChunk, ppos, pvel, &bar_p);
         }
         {
             const int nx = ch + gridDim.x;
@@ -496,58 +485,12 @@ __global__ void __launch_bounds__(kThreads, kMcc ? 2 : 3) k_push(PushArgs a) {
             float3 o = make_float3(P[q].x, P[q].y, P[q].z);
             float3 v = make_float3(V[q].x, V[q].y, V[q].z);
             const float w = V[q].w;
-            Collision col;
-            col.kind = 0;
-            unsigned long long id = 0;
-            if (kMcc) {
-                const CollDev& cd = a.coll;
-                id = ID[q];
-                uint4 r0 = philox4x32_10(make_uint4((unsigned)id, (unsigned)(id >> 32), cd.step, 0u), cd.key);
-                const float p_null =
-                    cd.p_null_slab ? __ldg(&cd.p_null_slab[fdiv((unsigned)k, g.fd_zslab)]) : cd.p_null;
-                if (u01(r0.x) < p_null) {
-                    st_cand++;
-                    col = collide_candidate(cd, id, v, r0);
-                    if (col.kind) {
-                        st_coll++;
-                        v = col.v;
-                    }
-                    if (col.kind == 2) st_ion++;
-                }
-            }
             // leapfrog push (Species.cpp:369-373)
             float3 E = gather_e(a, t, bn[q], o);
             v.x += a.qm_dt * E.x;
             v.y += a.qm_dt * E.y;
             v.z += a.qm_dt * E.z;
             const int newc = move_particle(a, i, j, k, o, v);
-            if (kMcc && col.kind == 2) {
-                // the ejected electron and the ion are created at a uniform point of the parent's
-                // cell without velocity rewind; the electron is pushed and deposited now
-                if (!append_particle(a.coll.ion, ion_n, make_float4(col.po.x, col.po.y, col.po.z, __int_as_float(c)),
-                                     make_float4(col.nv.x, col.nv.y, col.nv.z, w), child_id(id, a.coll.step, 2), a.err))
-                    st_lost++;
-                float3 po = col.po, pv = col.pv;
-                float3 Ep = gather_e(a, t, bn[q], po);
-                pv.x += a.qm_dt * Ep.x;
-                pv.y += a.qm_dt * Ep.y;
-                pv.z += a.qm_dt * Ep.z;
-                int pc = move_particle(a, i, j, k, po, pv);
-                if (pc >= 0) {
-                    if (append_particle(a.sp, n, make_float4(po.x, po.y, po.z, __int_as_float(pc)),
-                                        make_float4(pv.x, pv.y, pv.z, w), child_id(id, a.coll.step, 1), a.err)) {
-                        if (a.deposit) {
-                            Tile tg = t;
-                            tg.dtile = nullptr;  // products go straight to HBM
-                            Corners pcn;
-                            corner_values(w, po, a.dep_scale, pcn, false);
-                            commit_corners(a, tg, cell_base(g, pc), pcn);
-                        }
-                    } else {
-                        st_lost++;
-                    }
-                }
-            }
             a.sp.pos[p] = make_float4(o.x, o.y, o.z, __int_as_float(newc));
             a.sp.vel[p] = make_float4(v.x, v.y, v.z, w);
             if (newc >= 0) {
@@ -586,14 +529,6 @@ __global__ void __launch_bounds__(kThreads, kMcc ? 2 : 3) k_push(PushArgs a) {
             }
         }
         __syncthreads();
-    }
-    if (kMcc) {
-        unsigned v[4] = {st_cand, st_coll, st_ion, st_lost};
-#pragma unroll
-        for (int c = 0; c < 4; c++) {
-            unsigned x = __reduce_add_sync(0xffffffffu, v[c]);
-            if (lane == 0 && x) atomicAdd(&a.coll.stats[c], (unsigned long long)x);
-        }
     }
 }
 
@@ -711,12 +646,10 @@ void launch_mcc(const PushArgs& a, int* cand, int* ncand, cudaStream_t s, int sm
 void launch_push(const PushArgs& a, cudaStream_t s, int grid) {
     static bool attr = false;
     if (!attr) {
-        cudaFuncSetAttribute(k_push<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPushSmem(true));
-        cudaFuncSetAttribute(k_push<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPushSmem(false));
+        cudaFuncSetAttribute(k_push, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPushSmem);
         attr = true;
     }
-    if (a.coll.enabled) k_push<true><<<grid, kThreads, kPushSmem(true), s>>>(a);
-    else k_push<false><<<grid, kThreads, kPushSmem(false), s>>>(a);
+    k_push<<<grid, kThreads, kPushSmem, s>>>(a);
 }
 
 // ------------------------------------------------------------------------------------
