@@ -127,6 +127,8 @@ struct pic_world {
     // (rho - rho_prev) / eps0 instead of an FP64 pass.  Cleared when phi, the boundaries or r change.
     float* rho_prev = nullptr;
     float* bfix = nullptr;  // FP32 boundary part of b per node
+    int2* aux_pairs = nullptr;  // (node, source node) of the MIRROR, then the ALIAS nodes
+    int n_mirror = 0, n_alias = 0;
     bool rhs_valid = false;
     int lp_collect = 0;     // store (first residual, total correction) of each solve as a training pair
     long lp_fallbacks = 0;  // learned solves handed to Jacobi-PCG
@@ -316,6 +318,33 @@ int upload_kinds(pic_world* w, bool reset_phi) {
     std::vector<double> ph;
     build_kinds(w, kind, ph);
     const GridDev& g = w->g;
+    {
+        // copy lists of the MIRROR nodes (clamped interior node) and the ALIAS nodes (periodic source)
+        std::vector<int2> mir, ali;
+        const int nn[3] = {g.ni, g.nj, g.nk};
+        for (int k = 0; k < g.nk; k++)
+            for (int j = 0; j < g.nj; j++)
+                for (int i = 0; i < g.ni; i++) {
+                    const int n = (k * g.nj + j) * g.ni + i, kd = kind[n] & 3;
+                    if (kd != kMirror && kd != kAlias) continue;
+                    int ijk[3] = {i, j, k};
+                    for (int d = 0; d < 3; d++) {
+                        if (kd == kMirror && !w->periodic[d])
+                            ijk[d] = ijk[d] < 1 ? 1 : (ijk[d] > nn[d] - 2 ? nn[d] - 2 : ijk[d]);
+                        if (kd == kAlias && w->periodic[d] && ijk[d] == nn[d] - 1) ijk[d] = 0;
+                    }
+                    (kd == kMirror ? mir : ali).push_back(make_int2(n, (ijk[2] * g.nj + ijk[1]) * g.ni + ijk[0]));
+                }
+        if (w->aux_pairs) cudaFree(w->aux_pairs);
+        w->aux_pairs = nullptr;
+        w->n_mirror = (int)mir.size();
+        w->n_alias = (int)ali.size();
+        mir.insert(mir.end(), ali.begin(), ali.end());
+        if (!mir.empty()) {
+            CU(cudaMalloc(&w->aux_pairs, sizeof(int2) * mir.size()));
+            CU(cudaMemcpy(w->aux_pairs, mir.data(), sizeof(int2) * mir.size(), cudaMemcpyHostToDevice));
+        }
+    }
     CU(cudaMemcpyAsync(w->kind, kind.data(), sizeof(uint16_t) * g.nv, cudaMemcpyHostToDevice, w->stream));
     std::vector<float2> cur(g.nv);
     if (reset_phi) {
@@ -501,7 +530,12 @@ extern "C" int pic_world_create(pic_world** out, int ni, int nj, int nk, const d
         g.dxd[d] = (xm[d] - x0[d]) / (nn[d] - 1);  // World::setExtents, World.cpp:72-76
         g.dx[d] = (float)g.dxd[d];
         g.inv_dx[d] = (float)(1.0 / g.dxd[d]);
+        const double c = 1.0 / (g.dxd[d] * g.dxd[d]);
+        g.c_hi[d] = (float)c;
+        g.c_lo[d] = (float)(c - (double)g.c_hi[d]);
+        g.inv2dx[d] = (float)(1.0 / (2.0 * g.dxd[d]));
     }
+    g.inv_cell_vol = (float)(1.0 / (g.dxd[0] * g.dxd[1] * g.dxd[2]));
     auto alloc = [&](void** p, size_t bytes) -> bool { return cudaMalloc(p, bytes) == cudaSuccess; };
     bool ok = cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking) == cudaSuccess;
     ok = ok && alloc((void**)&w->ef, sizeof(float4) * nv) && alloc((void**)&w->phi, sizeof(float2) * nv) &&
@@ -549,6 +583,7 @@ extern "C" int pic_world_destroy(pic_world* w) {
     if (w->stream) cudaStreamSynchronize(w->stream);
     free_lp(w);
     if (w->rho_prev) cudaFree(w->rho_prev);
+    if (w->aux_pairs) cudaFree(w->aux_pairs);
     if (w->p_null_slab) cudaFree(w->p_null_slab);
     if (w->mcc_cand) cudaFree(w->mcc_cand);
     if (w->mcc_ncand) cudaFree(w->mcc_ncand);
@@ -1347,7 +1382,7 @@ int solve_impl(pic_world* w, int* iters_out, double* rel_out) {
     }
     {
         Scope sc(w, "poisson", 2);
-        launch_fill_aux(w->g, w->phi, reinterpret_cast<const uint8_t*>(w->kind), w->stream, grid);
+        launch_fill_aux(w->aux_pairs, w->n_mirror, w->n_alias, w->phi, w->stream);
     }
     if (collect) lp_pair_end(*w->lp);
     if (iters_out) *iters_out = iters;

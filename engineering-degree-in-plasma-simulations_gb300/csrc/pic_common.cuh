@@ -55,6 +55,9 @@ struct GridDev {
     int nv, nc;           // node and cell totals
     int periodic[3];
     float dx[3], inv_dx[3];
+    float c_hi[3], c_lo[3];  // 1/dx^2 per axis as float-float (hi + lo), set on the host
+    float inv2dx[3];         // 1/(2 dx) per axis
+    float inv_cell_vol;      // 1/(dx dy dz)
     double x0[3], xm[3], dxd[3];
     int n_boxes;
     float box_lo[kMaxBoxes][3], box_hi[kMaxBoxes][3];  // absorbing objects, absolute coordinates

@@ -14,6 +14,7 @@
 //   (L x)_p = D_p x_p - sum_{q FREE or FIXED} c_q x_q,   D_p = sum_{q not MIRROR} c_q,  c = 1/dx^2.
 // kind[n] (uint16): bits 0-1 node kind, bits 2-7 "neighbour d is MIRROR", bits 8-13
 // "neighbour d is FIXED"; direction order -x +x -y +y -z +z.
+#include <algorithm>
 #include "pic_ff.cuh"
 #include "pic_stencil.cuh"
 
@@ -24,7 +25,7 @@ namespace pic {
 // ------------------------------------------------------------------------------------
 __global__ void k_finalize_rho(FinalizeArgs a) {
     const GridDev& g = a.g;
-    const float inv_base = (float)(1.0 / (g.dxd[0] * g.dxd[1] * g.dxd[2]));
+    const float inv_base = g.inv_cell_vol;
     const int nn[3] = {g.ni, g.nj, g.nk}, stride[3] = {1, g.ni, g.ni * g.nj};
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
         int ijk[3];
@@ -108,8 +109,7 @@ __device__ __forceinline__ float ffd(float2 a, float2 b) {
 }
 __global__ void k_efield(GridDev g, const float2* __restrict__ phi, float4* __restrict__ ef) {
     const int stride[3] = {1, g.ni, g.ni * g.nj}, nn[3] = {g.ni, g.nj, g.nk};
-    float inv2[3];
-    for (int d = 0; d < 3; d++) inv2[d] = (float)(1.0 / (2.0 * g.dxd[d]));
+    const float inv2[3] = {g.inv2dx[0], g.inv2dx[1], g.inv2dx[2]};
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
         int ijk[3];
         node_ijk(g, n, ijk[0], ijk[1], ijk[2]);
@@ -159,9 +159,11 @@ __global__ void __launch_bounds__(kNodeThreads) k_residual(
     const float* __restrict__ rho, const uint16_t* __restrict__ kind, float* __restrict__ r, double* gpart,
     int gstride, unsigned* ticket, double* out, int apply_e, float* __restrict__ rho_prev,
     float* __restrict__ bfix_out) {
-    FF cf[3];
-    for (int ax = 0; ax < 3; ax++) cf[ax] = ff_from_double(1.0 / (g.dxd[ax] * g.dxd[ax]));
-    const FF ie = ff_from_double(1.0 / kEps0);
+    // float-float constants from the host: no FP64 arithmetic in the kernel
+    const FF cf[3] = {FF{g.c_hi[0], g.c_lo[0]}, FF{g.c_hi[1], g.c_lo[1]}, FF{g.c_hi[2], g.c_lo[2]}};
+    constexpr float kIeHi = (float)(1.0 / kEps0);
+    constexpr float kIeLo = (float)(1.0 / kEps0 - (double)kIeHi);
+    const FF ie{kIeHi, kIeLo};
     float acc_r = 0.f, acc_b = 0.f;  // per-thread sums in FP32, block and grid sums in FP64
     const int base = blockIdx.x * kNodeTile + threadIdx.x;
 #pragma unroll
@@ -230,34 +232,53 @@ void launch_residual(const GridDev& g, SolveWork& w, int apply_e, cudaStream_t s
     }
 }
 // residual of the next solve without a full pass: r += (rho - rho_prev) / eps0 on FREE nodes
-// (r holds the residual of the current phi, rounded to FP32); |r|^2, |b|^2 into out[0..1]
-__global__ void __launch_bounds__(kNodeThreads) k_rhs_update(GridDev g, float* __restrict__ r,
-                                                             const float* __restrict__ rho,
-                                                             float* __restrict__ rho_prev,
-                                                             const float* __restrict__ bfix,
-                                                             const uint16_t* __restrict__ kind, double* gpart,
-                                                             int gstride, unsigned* ticket, double* out) {
+// (r holds the residual of the current phi, rounded to FP32); |r|^2, |b|^2 into out[0..1].
+// Four consecutive nodes per thread and iteration with 16-byte loads.
+__global__ void __launch_bounds__(256) k_rhs_update(GridDev g, float* __restrict__ r, const float* __restrict__ rho,
+                                                    float* __restrict__ rho_prev, const float* __restrict__ bfix,
+                                                    const uint16_t* __restrict__ kind, double* gpart, int gstride,
+                                                    unsigned* ticket, double* out) {
     const float inv_eps0_f = (float)(1.0 / kEps0);
     float acc_r = 0.f, acc_b = 0.f;
-    const int base = blockIdx.x * kNodeTile + threadIdx.x;
+    const int ng = g.nv >> 2;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < ng; q += gridDim.x * blockDim.x) {
+        const float4 r4 = reinterpret_cast<const float4*>(r)[q];
+        const float4 h4 = reinterpret_cast<const float4*>(rho)[q];
+        const float4 p4 = reinterpret_cast<const float4*>(rho_prev)[q];
+        const float4 f4 = reinterpret_cast<const float4*>(bfix)[q];
+        const ushort4 k4 = reinterpret_cast<const ushort4*>(kind)[q];
+        float rv[4] = {r4.x, r4.y, r4.z, r4.w}, hv[4] = {h4.x, h4.y, h4.z, h4.w};
+        const float pv[4] = {p4.x, p4.y, p4.z, p4.w}, fv[4] = {f4.x, f4.y, f4.z, f4.w};
+        const unsigned short kv[4] = {k4.x, k4.y, k4.z, k4.w};
 #pragma unroll
-    for (int q4 = 0; q4 < kNodeTile / kNodeThreads; q4++) {
-        const int n = base + q4 * kNodeThreads;
-        if (n >= g.nv) break;
-        if ((kind[n] & 3) != kFree) continue;
-        const float rh = rho[n];
-        const float rn = r[n] + (rh - rho_prev[n]) * inv_eps0_f;
-        r[n] = rn;
-        rho_prev[n] = rh;
-        const float b = rh * inv_eps0_f + bfix[n];
-        acc_r += rn * rn;
-        acc_b += b * b;
+        for (int c = 0; c < 4; c++) {
+            if ((kv[c] & 3) != kFree) continue;
+            rv[c] += (hv[c] - pv[c]) * inv_eps0_f;
+            const float b = hv[c] * inv_eps0_f + fv[c];
+            acc_r += rv[c] * rv[c];
+            acc_b += b * b;
+        }
+        reinterpret_cast<float4*>(r)[q] = make_float4(rv[0], rv[1], rv[2], rv[3]);
+        reinterpret_cast<float4*>(rho_prev)[q] = h4;
+    }
+    // the last nv % 4 nodes
+    if (blockIdx.x == 0 && threadIdx.x < (g.nv & 3)) {
+        const int n = (ng << 2) + threadIdx.x;
+        if ((kind[n] & 3) == kFree) {
+            const float rh = rho[n];
+            const float rn = r[n] + (rh - rho_prev[n]) * inv_eps0_f;
+            r[n] = rn;
+            const float b = rh * inv_eps0_f + bfix[n];
+            acc_r += rn * rn;
+            acc_b += b * b;
+        }
+        rho_prev[n] = rho[n];
     }
     const float v[2] = {acc_r, acc_b};
     grid_sum<2>(v, gpart, gstride, ticket, out);
 }
 void launch_rhs_update(const GridDev& g, SolveWork& w, float* rho_prev, const float* bfix, cudaStream_t s) {
-    k_rhs_update<<<node_blocks(g.nv), kNodeThreads, 0, s>>>(g, w.r, w.rho, rho_prev, bfix,
+    k_rhs_update<<<stream_blocks(g.nv), 256, 0, s>>>(g, w.r, w.rho, rho_prev, bfix,
                                                             reinterpret_cast<const uint16_t*>(w.kind), w.gpart,
                                                             w.gstride, w.ticket, w.scal + kS_R2);
 }
@@ -356,30 +377,38 @@ void launch_rbsor_sweeps(const GridDev& g, SolveWork& w, float omega, int sweeps
 //   K2: alpha = rz/dq ; e += alpha d' ; r -= alpha q ; z' = r/D ; partials r.z', r.z, r.r
 // scalars: scal[0..1] rz (double-buffered by iteration parity); flag[0] set when r.r <= target
 // ------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(kNodeThreads) k_pcg_init(GridDev g, const float* __restrict__ r,
-                                                           float* __restrict__ z, float* __restrict__ e,
-                                                           float* __restrict__ d, const uint16_t* __restrict__ kind,
-                                                           double* gpart, int gstride, unsigned* ticket,
-                                                           double* scal, int* flag) {
+__global__ void __launch_bounds__(256) k_pcg_init(GridDev g, const float* __restrict__ r, float* __restrict__ z,
+                                                  float* __restrict__ e, float* __restrict__ d,
+                                                  const uint16_t* __restrict__ kind, double* gpart, int gstride,
+                                                  unsigned* ticket, double* scal, int* flag) {
     if (blockIdx.x == 0 && threadIdx.x == 0) flag[0] = 0;
     const float c3[3] = {g.inv_dx[0] * g.inv_dx[0], g.inv_dx[1] * g.inv_dx[1], g.inv_dx[2] * g.inv_dx[2]};
     float acc = 0.f;
-    const int base = blockIdx.x * kNodeTile + threadIdx.x;
+    const int ng = g.nv >> 2;
+    const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < ng; q += gridDim.x * blockDim.x) {
+        const float4 r4 = reinterpret_cast<const float4*>(r)[q];
+        const ushort4 k4 = reinterpret_cast<const ushort4*>(kind)[q];
+        const float rv[4] = {r4.x, r4.y, r4.z, r4.w};
+        const unsigned short kv[4] = {k4.x, k4.y, k4.z, k4.w};
+        float zv[4];
 #pragma unroll
-    for (int q4 = 0; q4 < kNodeTile / kNodeThreads; q4++) {
-        const int n = base + q4 * kNodeThreads;
-        if (n >= g.nv) break;
+        for (int c = 0; c < 4; c++) {
+            zv[c] = (kv[c] & 3) == kFree ? rv[c] * inv_diag_of(kv[c], c3) : 0.f;
+            acc += rv[c] * zv[c];
+        }
+        reinterpret_cast<float4*>(z)[q] = make_float4(zv[0], zv[1], zv[2], zv[3]);
+        reinterpret_cast<float4*>(e)[q] = zero4;
+        reinterpret_cast<float4*>(d)[q] = zero4;
+    }
+    if (blockIdx.x == 0 && threadIdx.x < (g.nv & 3)) {
+        const int n = (ng << 2) + threadIdx.x;
         const uint16_t kd = kind[n];
+        const float zz = (kd & 3) == kFree ? r[n] * inv_diag_of(kd, c3) : 0.f;
+        z[n] = zz;
         e[n] = 0.f;
         d[n] = 0.f;
-        if ((kd & 3) != kFree) {
-            z[n] = 0.f;
-            continue;
-        }
-        const float rr = r[n];
-        const float zz = rr * inv_diag_of(kd, c3);
-        z[n] = zz;
-        acc += rr * zz;
+        acc += r[n] * zz;
     }
     const float v[1] = {acc};
     grid_sum<1>(v, gpart, gstride, ticket, scal + kS_RZN);  // r.z
@@ -438,40 +467,62 @@ __global__ void __launch_bounds__(kNodeThreads) k_pcg_k1(GridDev g, const float*
     const float v[1] = {facc};
     grid_sum<1>(v, gpart, gstride, ticket, scal + kS_DQ);
 }
-__global__ void __launch_bounds__(kNodeThreads) k_pcg_k2(GridDev g, const float* __restrict__ d,
-                                                         const float* __restrict__ q, float* __restrict__ e,
-                                                         float* __restrict__ r, float* __restrict__ z,
-                                                         const uint16_t* __restrict__ kind, double* gpart,
-                                                         int gstride, unsigned* ticket, double* scal, int* flag,
-                                                         int it) {
+__global__ void __launch_bounds__(256) k_pcg_k2(GridDev g, const float* __restrict__ d, const float* __restrict__ q,
+                                                float* __restrict__ e, float* __restrict__ r, float* __restrict__ z,
+                                                const uint16_t* __restrict__ kind, double* gpart, int gstride,
+                                                unsigned* ticket, double* scal, int* flag, int it) {
     if (flag[0]) return;
     const double dq = scal[kS_DQ];
     const double rz = scal[kS_RZ + (it & 1)];
     const float alpha = dq != 0.0 ? (float)(rz / dq) : 0.f;
     const float c3[3] = {g.inv_dx[0] * g.inv_dx[0], g.inv_dx[1] * g.inv_dx[1], g.inv_dx[2] * g.inv_dx[2]};
     float f0 = 0.f, f1 = 0.f, f2 = 0.f;
-    const int base = blockIdx.x * kNodeTile + threadIdx.x;
+    const int ng = g.nv >> 2;
+    for (int qq = blockIdx.x * blockDim.x + threadIdx.x; qq < ng; qq += gridDim.x * blockDim.x) {
+        const float4 d4 = reinterpret_cast<const float4*>(d)[qq];
+        const float4 q4 = reinterpret_cast<const float4*>(q)[qq];
+        const float4 e4 = reinterpret_cast<const float4*>(e)[qq];
+        const float4 r4 = reinterpret_cast<const float4*>(r)[qq];
+        const float4 z4 = reinterpret_cast<const float4*>(z)[qq];
+        const ushort4 k4 = reinterpret_cast<const ushort4*>(kind)[qq];
+        const float dv[4] = {d4.x, d4.y, d4.z, d4.w}, qv[4] = {q4.x, q4.y, q4.z, q4.w};
+        float ev[4] = {e4.x, e4.y, e4.z, e4.w}, rv[4] = {r4.x, r4.y, r4.z, r4.w}, zv[4] = {z4.x, z4.y, z4.z, z4.w};
+        const unsigned short kv[4] = {k4.x, k4.y, k4.z, k4.w};
 #pragma unroll
-    for (int q4 = 0; q4 < kNodeTile / kNodeThreads; q4++) {
-        const int n = base + q4 * kNodeThreads;
-        if (n >= g.nv) break;
+        for (int c = 0; c < 4; c++) {
+            if ((kv[c] & 3) != kFree) continue;
+            ev[c] += alpha * dv[c];
+            const float rn = rv[c] - alpha * qv[c];
+            const float zn = rn * inv_diag_of(kv[c], c3);
+            f0 += rn * zn;
+            f1 += rn * zv[c];
+            f2 += rn * rn;
+            rv[c] = rn;
+            zv[c] = zn;
+        }
+        reinterpret_cast<float4*>(e)[qq] = make_float4(ev[0], ev[1], ev[2], ev[3]);
+        reinterpret_cast<float4*>(r)[qq] = make_float4(rv[0], rv[1], rv[2], rv[3]);
+        reinterpret_cast<float4*>(z)[qq] = make_float4(zv[0], zv[1], zv[2], zv[3]);
+    }
+    if (blockIdx.x == 0 && threadIdx.x < (g.nv & 3)) {
+        const int n = (ng << 2) + threadIdx.x;
         const uint16_t kd = kind[n];
-        if ((kd & 3) != kFree) continue;
-        e[n] += alpha * d[n];
-        const float rn = r[n] - alpha * q[n];
-        r[n] = rn;
-        const float zo = z[n];
-        const float zn = rn * inv_diag_of(kd, c3);
-        z[n] = zn;
-        f0 += rn * zn;
-        f1 += rn * zo;
-        f2 += rn * rn;
+        if ((kd & 3) == kFree) {
+            e[n] += alpha * d[n];
+            const float rn = r[n] - alpha * q[n];
+            const float zn = rn * inv_diag_of(kd, c3);
+            f0 += rn * zn;
+            f1 += rn * z[n];
+            f2 += rn * rn;
+            r[n] = rn;
+            z[n] = zn;
+        }
     }
     const float v[3] = {f0, f1, f2};
     grid_sum<3>(v, gpart, gstride, ticket, scal + kS_RZN);  // r.z', r.z, r.r
 }
 void launch_pcg_init(const GridDev& g, SolveWork& w, cudaStream_t s) {
-    k_pcg_init<<<node_blocks(g.nv), kNodeThreads, 0, s>>>(g, w.r, w.z, w.e, w.d,
+    k_pcg_init<<<stream_blocks(g.nv), 256, 0, s>>>(g, w.r, w.z, w.e, w.d,
                                                           reinterpret_cast<const uint16_t*>(w.kind), w.gpart,
                                                           w.gstride, w.ticket, w.scal, w.flag);
 }
@@ -482,37 +533,25 @@ void launch_pcg_iter_impl(const GridDev& g, SolveWork& w, float* d_in, float* d_
     const int nb = node_blocks(g.nv);
     k_pcg_k1<<<nb, kNodeThreads, 0, s>>>(g, w.z, d_in, d_out, w.q, kd, w.gpart, w.gstride, w.ticket, w.scal, w.flag,
                                          it, target_rr);
-    k_pcg_k2<<<nb, kNodeThreads, 0, s>>>(g, d_out, w.q, w.e, w.r, w.z, kd, w.gpart, w.gstride, w.ticket, w.scal,
-                                         w.flag, it);
+    k_pcg_k2<<<stream_blocks(g.nv), 256, 0, s>>>(g, d_out, w.q, w.e, w.r, w.z, kd, w.gpart, w.gstride, w.ticket,
+                                                 w.scal, w.flag, it);
 }
 
 // ------------------------------------------------------------------------------------
 // MIRROR nodes take the clamped interior value, then ALIAS nodes their periodic source
 // ------------------------------------------------------------------------------------
-__global__ void k_fill_mirror(GridDev g, float2* phi, const uint16_t* kind) {
-    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
-        if ((kind[n] & 3) != kMirror) continue;
-        int ijk[3], nn[3] = {g.ni, g.nj, g.nk};
-        node_ijk(g, n, ijk[0], ijk[1], ijk[2]);
-        for (int d = 0; d < 3; d++)
-            if (!g.periodic[d]) ijk[d] = ijk[d] < 1 ? 1 : (ijk[d] > nn[d] - 2 ? nn[d] - 2 : ijk[d]);
-        phi[n] = phi[(ijk[2] * g.nj + ijk[1]) * g.ni + ijk[0]];
+// phi[dst] = phi[src] over a list of node pairs: the MIRROR nodes first (their clamped interior
+// node), then the ALIAS nodes (their periodic source, which may be a MIRROR node)
+__global__ void k_fill_pairs(const int2* __restrict__ pairs, int n, float2* phi) {
+    for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < n; x += gridDim.x * blockDim.x) {
+        const int2 p = pairs[x];
+        phi[p.x] = phi[p.y];
     }
 }
-__global__ void k_fill_alias(GridDev g, float2* phi, const uint16_t* kind) {
-    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
-        if ((kind[n] & 3) != kAlias) continue;
-        int ijk[3], nn[3] = {g.ni, g.nj, g.nk};
-        node_ijk(g, n, ijk[0], ijk[1], ijk[2]);
-        for (int d = 0; d < 3; d++)
-            if (g.periodic[d] && ijk[d] == nn[d] - 1) ijk[d] = 0;
-        phi[n] = phi[(ijk[2] * g.nj + ijk[1]) * g.ni + ijk[0]];
-    }
-}
-void launch_fill_aux(const GridDev& g, float2* phi, const uint8_t* kind, cudaStream_t s, int grid) {
-    const uint16_t* kd = reinterpret_cast<const uint16_t*>(kind);
-    k_fill_mirror<<<grid, 256, 0, s>>>(g, phi, kd);
-    k_fill_alias<<<grid, 256, 0, s>>>(g, phi, kd);
+void launch_fill_aux(const int2* pairs, int n_mirror, int n_alias, float2* phi, cudaStream_t s) {
+    if (n_mirror > 0) k_fill_pairs<<<std::min(1216, (n_mirror + 255) / 256), 256, 0, s>>>(pairs, n_mirror, phi);
+    if (n_alias > 0)
+        k_fill_pairs<<<std::min(1216, (n_alias + 255) / 256), 256, 0, s>>>(pairs + n_mirror, n_alias, phi);
 }
 
 }  // namespace pic

@@ -115,6 +115,12 @@ constexpr int kParts = 1024;
 constexpr int kNodeThreads = 256;
 constexpr int kNodeTile = 4 * kNodeThreads;
 inline int node_blocks(int nv) { return (nv + kNodeTile - 1) / kNodeTile; }
+// streaming node kernels (four consecutive nodes per thread and 16-byte loads, grid-stride): a
+// few CTAs per SM keep every SM busy, and the grid sum adds few partials
+inline int stream_blocks(int nv) {
+    const int want = (nv / 4 + 255) / 256;
+    return want < 1 ? 1 : (want < 1216 ? want : 1216);
+}
 // device scalar slots of the solvers
 enum : int {
     kS_RZ = 0,      // [0..1] r.z of iterations it (double-buffered by parity)
@@ -134,7 +140,8 @@ void launch_rbsor_sweeps(const GridDev& g, SolveWork& w, float omega, int sweeps
 void launch_pcg_init(const GridDev& g, SolveWork& w, cudaStream_t s);
 void launch_pcg_iter_impl(const GridDev& g, SolveWork& w, float* d_in, float* d_out, int it, double target_rr,
                           cudaStream_t s);
-void launch_fill_aux(const GridDev& g, float2* phi, const uint8_t* kind, cudaStream_t s, int grid);
+// phi[dst] = phi[src] for the MIRROR pairs (first n_mirror entries), then the ALIAS pairs
+void launch_fill_aux(const int2* pairs, int n_mirror, int n_alias, float2* phi, cudaStream_t s);
 void launch_den_avg(float* avg, const float* den, int nv, float a, float b, cudaStream_t s, int grid);
 
 }  // namespace pic

@@ -232,7 +232,7 @@ __device__ __forceinline__ float lp_stencil27(const LView& v, const float* __res
             for (int dy = 0; dy < 3; dy++) {
                 const float* row = p + dy * v.sy + dz * v.sz;
                 const float* k = S + 9 * dz + 3 * dy;
-                acc += __ldg(&k[0]) * row[0] + __ldg(&k[1]) * row[1] + __ldg(&k[2]) * row[2];
+                acc += k[0] * row[0] + k[1] * row[1] + k[2] * row[2];
             }
         return acc;
     }
@@ -249,7 +249,7 @@ __device__ __forceinline__ float lp_stencil27(const LView& v, const float* __res
 #pragma unroll
             for (int dx = -1; dx <= 1; dx++) {
                 int x = lv_nb(c[0], dx, v.n[0], v.per[0]);
-                if (x >= 0) acc += __ldg(&S[9 * (dz + 1) + 3 * (dy + 1) + dx + 1]) * row[x];
+                if (x >= 0) acc += S[9 * (dz + 1) + 3 * (dy + 1) + dx + 1] * row[x];
             }
         }
     }
@@ -275,7 +275,7 @@ __device__ float lp_net_op(const LView& v, const float* __restrict__ fold, const
                 const float* row = p + dy * v.sy + dz * v.sz;
                 const float* k = K5 + 25 * dz + 5 * dy;
 #pragma unroll
-                for (int dx = 0; dx < 5; dx++) acc += __ldg(&k[dx]) * row[dx];
+                for (int dx = 0; dx < 5; dx++) acc += k[dx] * row[dx];
             }
         return acc;
     }
@@ -292,7 +292,7 @@ __device__ float lp_net_op(const LView& v, const float* __restrict__ fold, const
 #pragma unroll
                 for (int dx = -2; dx <= 2; dx++) {
                     int x = lv_nb(c[0], dx, v.n[0], v.per[0]);
-                    if (x >= 0) acc += __ldg(&k[dx]) * row[x];
+                    if (x >= 0) acc += k[dx] * row[x];
                 }
             }
         }
@@ -308,9 +308,14 @@ __device__ float lp_net_op(const LView& v, const float* __restrict__ fold, const
 }
 
 // e_l = op_l(z_l) + P e_{l+1}; mode 1: network level (fold), 2: diagonal scaling
-__global__ void k_lp_up(LView zin, LView cin, LView out, int mode, const float* __restrict__ fold, float inv_diag,
+__global__ void k_lp_up(LView zin, LView cin, LView out, int mode, const float* __restrict__ fold_g, float inv_diag,
                         const int* flag) {
     if (flag && flag[0]) return;
+    __shared__ float fold[kLpFold];  // the level's folded stencils, read by every voxel
+    if (mode == 1) {
+        for (int x = threadIdx.x; x < kLpFold; x += blockDim.x) fold[x] = fold_g[x];
+        __syncthreads();
+    }
     for (unsigned idx = blockIdx.x * blockDim.x + threadIdx.x; idx < (unsigned)out.nvox;
          idx += gridDim.x * blockDim.x) {
         int c[3];
@@ -329,6 +334,9 @@ __global__ void __launch_bounds__(kNodeThreads) k_lp_up0(GridDev g, LView rin, L
                                                          double* gpart, int gstride, unsigned* ticket, double* out,
                                                          const int* flag) {
     if (flag && flag[0]) return;
+    __shared__ float S[27];
+    if (threadIdx.x < 27) S[threadIdx.x] = S0[threadIdx.x];
+    __syncthreads();
     float f_zr = 0.f, f_zq = 0.f;
     const int base = blockIdx.x * kNodeTile + threadIdx.x;
 #pragma unroll
@@ -341,7 +349,7 @@ __global__ void __launch_bounds__(kNodeThreads) k_lp_up0(GridDev g, LView rin, L
         }
         int c[3];
         node_ijk(g, n, c[0], c[1], c[2]);
-        float v = lp_stencil27(rin, S0, c);
+        float v = lp_stencil27(rin, S, c);
         if (cin.a) v += lp_prolong_at(cin, c);
         z[n] = v;
         f_zr += v * rin.a[n];
@@ -490,11 +498,10 @@ __global__ void __launch_bounds__(kNodeThreads) k_lpcg_k1(GridDev g, const float
     const float v[1] = {facc};
     grid_sum<1>(v, gpart, gstride, ticket, scal + kS_DQ);
 }
-__global__ void __launch_bounds__(kNodeThreads) k_lpcg_k2(GridDev g, const float* __restrict__ d,
-                                                          const float* __restrict__ q, float* __restrict__ e,
-                                                          float* __restrict__ r, const uint16_t* __restrict__ kind,
-                                                          double* gpart, int gstride, unsigned* ticket,
-                                                          double* scal, int* flag, int it) {
+__global__ void __launch_bounds__(256) k_lpcg_k2(GridDev g, const float* __restrict__ d, const float* __restrict__ q,
+                                                 float* __restrict__ e, float* __restrict__ r,
+                                                 const uint16_t* __restrict__ kind, double* gpart, int gstride,
+                                                 unsigned* ticket, double* scal, int* flag, int it) {
     if (flag[0]) return;
     const double dq = scal[kS_DQ];
     const double rz = scal[kS_RZ + (it & 1)];
@@ -502,27 +509,37 @@ __global__ void __launch_bounds__(kNodeThreads) k_lpcg_k2(GridDev g, const float
     if (blockIdx.x == 0 && threadIdx.x == 0) scal[kS_ALPHA + (it & 1)] = alpha_d;
     const float alpha = (float)alpha_d;
     float frr = 0.f;
-    const int base = blockIdx.x * kNodeTile + threadIdx.x;
+    const int ng = g.nv >> 2;
+    for (int qq = blockIdx.x * blockDim.x + threadIdx.x; qq < ng; qq += gridDim.x * blockDim.x) {
+        const float4 d4 = reinterpret_cast<const float4*>(d)[qq];
+        const float4 q4 = reinterpret_cast<const float4*>(q)[qq];
+        const float4 e4 = reinterpret_cast<const float4*>(e)[qq];
+        const float4 r4 = reinterpret_cast<const float4*>(r)[qq];
+        const ushort4 k4 = reinterpret_cast<const ushort4*>(kind)[qq];
+        const float dv[4] = {d4.x, d4.y, d4.z, d4.w}, qv[4] = {q4.x, q4.y, q4.z, q4.w};
+        float ev[4] = {e4.x, e4.y, e4.z, e4.w}, rv[4] = {r4.x, r4.y, r4.z, r4.w};
+        const unsigned short kv[4] = {k4.x, k4.y, k4.z, k4.w};
 #pragma unroll
-    for (int q4 = 0; q4 < kNodeTile / kNodeThreads; q4++) {
-        const int n = base + q4 * kNodeThreads;
-        if (n >= g.nv) break;
-        if ((kind[n] & 3) != kFree) continue;
-        e[n] += alpha * d[n];
-        const float rn = r[n] - alpha * q[n];
-        r[n] = rn;
-        frr += rn * rn;
+        for (int c = 0; c < 4; c++) {
+            if ((kv[c] & 3) != kFree) continue;
+            ev[c] += alpha * dv[c];
+            rv[c] -= alpha * qv[c];
+            frr += rv[c] * rv[c];
+        }
+        reinterpret_cast<float4*>(e)[qq] = make_float4(ev[0], ev[1], ev[2], ev[3]);
+        reinterpret_cast<float4*>(r)[qq] = make_float4(rv[0], rv[1], rv[2], rv[3]);
+    }
+    if (blockIdx.x == 0 && threadIdx.x < (g.nv & 3)) {
+        const int n = (ng << 2) + threadIdx.x;
+        if ((kind[n] & 3) == kFree) {
+            e[n] += alpha * d[n];
+            const float rn = r[n] - alpha * q[n];
+            r[n] = rn;
+            frr += rn * rn;
+        }
     }
     const float v[1] = {frr};
     grid_sum<1>(v, gpart, gstride, ticket, scal + kS_RR);
-}
-__global__ void k_lpcg_zero(float* e, float* q, float* d, int nv, int* flag) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) flag[0] = 0;
-    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nv; n += gridDim.x * blockDim.x) {
-        e[n] = 0.f;
-        q[n] = 0.f;
-        d[n] = 0.f;
-    }
 }
 // |a|^2 over n values into out[0] (deterministic: block partials, then one fixed-order sum)
 __global__ void k_lp_sq(const float* __restrict__ a, int n, double* part) {
@@ -541,7 +558,10 @@ void launch_lp_norm2(const float* a, int n, double* part, double* out, cudaStrea
 }
 
 void launch_lpcg_init(const GridDev& g, SolveWork& w, const LpState& L, cudaStream_t s, int sms) {
-    k_lpcg_zero<<<(g.nv + 255) / 256, 256, 0, s>>>(w.e, w.q, w.d, g.nv, w.flag);
+    cudaMemsetAsync(w.e, 0, sizeof(float) * g.nv, s);
+    cudaMemsetAsync(w.q, 0, sizeof(float) * g.nv, s);
+    cudaMemsetAsync(w.d, 0, sizeof(float) * g.nv, s);
+    cudaMemsetAsync(w.flag, 0, sizeof(int), s);
     launch_lp_apply(g, L, w.r, w.z, reinterpret_cast<const uint16_t*>(w.kind), w.q, &w, nullptr, s, sms);
 }
 void launch_lpcg_iter(const GridDev& g, SolveWork& w, const LpState& L, float* d_in, float* d_out, int it,
@@ -550,8 +570,8 @@ void launch_lpcg_iter(const GridDev& g, SolveWork& w, const LpState& L, float* d
     const int nb = node_blocks(g.nv);
     k_lpcg_k1<<<nb, kNodeThreads, 0, s>>>(g, w.z, d_in, d_out, w.q, kd, w.gpart, w.gstride, w.ticket, w.scal, w.flag,
                                           it, target_rr);
-    k_lpcg_k2<<<nb, kNodeThreads, 0, s>>>(g, d_out, w.q, w.e, w.r, kd, w.gpart, w.gstride, w.ticket, w.scal, w.flag,
-                                          it);
+    k_lpcg_k2<<<stream_blocks(g.nv), 256, 0, s>>>(g, d_out, w.q, w.e, w.r, kd, w.gpart, w.gstride, w.ticket, w.scal,
+                                                  w.flag, it);
     launch_lp_apply(g, L, w.r, w.z, kd, w.q, &w, w.flag, s, sms);
 }
 

@@ -10,6 +10,7 @@
 //   creation       Species::addParticle                 Species.cpp:420-434
 //   cell lists     Species::sortIndexes                 Species.cpp:905-915
 #include <climits>
+#include "pic_ff.cuh"
 #include "pic_kernels.h"
 
 namespace pic {
@@ -992,19 +993,21 @@ void launch_load_uniform(const GridDev& g, SpeciesDev sp, const LoadArgs& la, cu
 // ------------------------------------------------------------------------------------
 __global__ void k_sums(SpeciesDev sp, double* part) {
     int n = sp.counts[0];
-    double a[5] = {0, 0, 0, 0, 0};
+    // per-thread sums in float-float (exact products of the FP32 values, about 48 bits), FP64
+    // only for the per-thread totals and the block sums
+    FF a[5] = {FF{0.f, 0.f}, FF{0.f, 0.f}, FF{0.f, 0.f}, FF{0.f, 0.f}, FF{0.f, 0.f}};
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
-        float4 v = sp.vel[p];
-        double w = v.w, vx = v.x, vy = v.y, vz = v.z;
-        a[0] += w;
-        a[1] += w * vx;
-        a[2] += w * vy;
-        a[3] += w * vz;
-        a[4] += w * (vx * vx + vy * vy + vz * vz);
+        const float4 v = sp.vel[p];
+        a[0] = ff_add_f(a[0], v.w);
+        a[1] = ff_add(a[1], two_prod(v.w, v.x));
+        a[2] = ff_add(a[2], two_prod(v.w, v.y));
+        a[3] = ff_add(a[3], two_prod(v.w, v.z));
+        FF v2 = ff_add(ff_add(two_prod(v.x, v.x), two_prod(v.y, v.y)), two_prod(v.z, v.z));
+        a[4] = ff_add(a[4], ff_mul(v2, FF{v.w, 0.f}));
     }
     __shared__ double s[5][8];
     for (int c = 0; c < 5; c++) {
-        double x = a[c];
+        double x = (double)a[c].hi + (double)a[c].lo;
         for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
         if ((threadIdx.x & 31) == 0) s[c][threadIdx.x >> 5] = x;
     }
