@@ -1236,6 +1236,7 @@ int residual_update(pic_world* w, SolveWork& sw, double& r2, double& b2) {
 int ensure_lp_train(pic_world* w);
 
 constexpr int kLearnedInnerCap = 400;  // iterations of one learned inner solve before falling back
+constexpr int kWarmJacobiCap = 16;     // Jacobi iterations a warm-started learned solve tries first
 
 // FP32 flexible CG with the learned preconditioner on L e = r (w->r), e from zero, until
 // r.r <= target or cap iterations; *done = iterations, *conv = reached the target
@@ -1292,6 +1293,7 @@ int solve_impl(pic_world* w, int* iters_out, double* rel_out) {
     // an FP32 update of the last FP64 residual when phi is unchanged since; the answer is always
     // certified by an FP64 residual below
     bool estimated = w->rhs_valid;
+    const bool warm = estimated;  // phi unchanged since the last solve: a warm start
     bool use_pcg = false;  // set when the learned preconditioner stalls in this solve
     int rc = estimated ? residual_update(w, sw, r2, b2) : residual_norms(w, sw, 0, r2, b2);
     if (rc) return rc;
@@ -1330,7 +1332,7 @@ int solve_impl(pic_world* w, int* iters_out, double* rel_out) {
                 launch_rbsor_sweeps(w->g, sw, (float)w->omega, sweeps, w->stream);
             }
             iters += sweeps;
-        } else if (w->method == PIC_SOLVER_LEARNED && !use_pcg) {
+        } else if (w->method == PIC_SOLVER_LEARNED && !use_pcg && !(warm && outer == 1)) {
             // inner FP32 flexible CG with the learned multilevel preconditioner, to eta = 1e-3 of
             // the current residual (or the final target); a preconditioner that stalls hands the
             // rest of this solve to Jacobi-PCG
@@ -1354,8 +1356,10 @@ int solve_impl(pic_world* w, int* iters_out, double* rel_out) {
             float* din = w->d;
             float* dout = w->d2;
             int it = 0;
-            for (;;) {
-                int batch = std::min(16, w->max_it - iters);
+            // a warm-started refinement of the learned method tries a few Jacobi iterations first
+            const int cap = (w->method == PIC_SOLVER_LEARNED && !use_pcg) ? kWarmJacobiCap : w->max_it;
+            for (int nb = 2;; nb = std::min(16, 2 * nb)) {  // growing batches: early exits cost little
+                int batch = std::min(std::min(nb, w->max_it - iters), cap - it);
                 if (batch <= 0) break;
                 {
                     Scope sc(w, "poisson", 2 * batch);
