@@ -23,6 +23,15 @@ namespace pic {
 // ------------------------------------------------------------------------------------
 // charge density: fixed-point number density -> den_s (per species) and rho
 // ------------------------------------------------------------------------------------
+// 64-bit integer -> FP32 through 32-bit conversions and one FMA (64-bit conversions run on the
+// narrow FP64 pipe of this GPU): hi * 2^32 is exact, the FMA rounds once, the low word's own
+// rounding (at most 2^7) lies below half an ulp of the result whenever hi != 0
+__device__ __forceinline__ float u64_to_float(unsigned long long x) {
+    return __fmaf_rn(__uint2float_rn((unsigned)(x >> 32)), 4294967296.f, __uint2float_rn((unsigned)x));
+}
+__device__ __forceinline__ float i64_to_float(long long x) {
+    return __fmaf_rn(__int2float_rn((int)(x >> 32)), 4294967296.f, __uint2float_rn((unsigned)x));
+}
 __global__ void k_finalize_rho(FinalizeArgs a) {
     const GridDev& g = a.g;
     const float inv_base = g.inv_cell_vol;
@@ -61,11 +70,11 @@ __global__ void k_finalize_rho(FinalizeArgs a) {
                     tot += a.acc[s][node];
                 }
             }
-            den_out[s] = __ull2float_rn(tot) * (a.inv_scale[s] * inv_vol);
+            den_out[s] = u64_to_float(tot) * (a.inv_scale[s] * inv_vol);
             if (a.int_path) rho_fixed += (long long)a.z[s] * (long long)tot;
             else rho_f += a.charge[s] * den_out[s];
         }
-        const float rf = a.int_path ? __ll2float_rn(rho_fixed) * (a.rho_scale * inv_vol) : rho_f;
+        const float rf = a.int_path ? i64_to_float(rho_fixed) * (a.rho_scale * inv_vol) : rho_f;
 #pragma unroll
         for (int s = 0; s < kMaxSpecies; s++) {
             if (s >= a.ns) break;
@@ -418,22 +427,32 @@ __global__ void __launch_bounds__(kNodeThreads) k_pcg_k1(GridDev g, const float*
                                                          float* __restrict__ q, const uint16_t* __restrict__ kind,
                                                          double* gpart, int gstride, unsigned* ticket, double* scal,
                                                          int* flag, int it, double target_rr) {
-    // scalars of the previous iteration: r.z', r.z, r.r
-    const double rz_new = scal[kS_RZN];
-    double beta = 0.0;
-    if (it > 0) {
-        const double rzo = scal[kS_RZO], rr = scal[kS_RR];
-        if (rr <= target_rr || flag[0]) {
-            if (blockIdx.x == 0 && threadIdx.x == 0 && !flag[0]) {
-                flag[1] = it;  // iterations completed
-                flag[0] = 1;
+    // scalars of the previous iteration (r.z', r.z, r.r), evaluated once per block in FP64
+    __shared__ float s_beta;
+    __shared__ int s_stop;
+    if (threadIdx.x == 0) {
+        const double rz_new = scal[kS_RZN];
+        double beta = 0.0;
+        int stop = 0;
+        if (it > 0) {
+            const double rzo = scal[kS_RZO], rr = scal[kS_RR];
+            if (rr <= target_rr || flag[0]) {
+                stop = 1;
+                if (blockIdx.x == 0 && !flag[0]) {
+                    flag[1] = it;  // iterations completed
+                    flag[0] = 1;
+                }
+            } else {
+                beta = (rz_new - rzo) / scal[kS_RZ + ((it - 1) & 1)];
             }
-            return;
         }
-        beta = (rz_new - rzo) / scal[kS_RZ + ((it - 1) & 1)];
+        if (blockIdx.x == 0 && !stop) scal[kS_RZ + (it & 1)] = rz_new;
+        s_beta = (float)beta;
+        s_stop = stop;
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) scal[kS_RZ + (it & 1)] = rz_new;
-    const float fb = (float)beta;
+    __syncthreads();
+    if (s_stop) return;
+    const float fb = s_beta;
     float facc = 0.f;
     const int base = blockIdx.x * kNodeTile + threadIdx.x;
 #pragma unroll
@@ -472,9 +491,13 @@ __global__ void __launch_bounds__(256) k_pcg_k2(GridDev g, const float* __restri
                                                 const uint16_t* __restrict__ kind, double* gpart, int gstride,
                                                 unsigned* ticket, double* scal, int* flag, int it) {
     if (flag[0]) return;
-    const double dq = scal[kS_DQ];
-    const double rz = scal[kS_RZ + (it & 1)];
-    const float alpha = dq != 0.0 ? (float)(rz / dq) : 0.f;
+    __shared__ float s_alpha;  // alpha = rz / dq, once per block in FP64
+    if (threadIdx.x == 0) {
+        const double dq = scal[kS_DQ];
+        s_alpha = dq != 0.0 ? (float)(scal[kS_RZ + (it & 1)] / dq) : 0.f;
+    }
+    __syncthreads();
+    const float alpha = s_alpha;
     const float c3[3] = {g.inv_dx[0] * g.inv_dx[0], g.inv_dx[1] * g.inv_dx[1], g.inv_dx[2] * g.inv_dx[2]};
     float f0 = 0.f, f1 = 0.f, f2 = 0.f;
     const int ng = g.nv >> 2;

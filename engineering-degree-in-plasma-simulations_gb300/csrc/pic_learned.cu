@@ -448,24 +448,35 @@ __global__ void __launch_bounds__(kNodeThreads) k_lpcg_k1(GridDev g, const float
                                                           float* __restrict__ q, const uint16_t* __restrict__ kind,
                                                           double* gpart, int gstride, unsigned* ticket,
                                                           double* scal, int* flag, int it, double target_rr) {
-    const double rz_new = scal[kS_RZN];
-    double beta = 0.0;
-    if (it > 0) {
-        const double zq = scal[kS_RZO], rr = scal[kS_RR];
-        if (rr <= target_rr || flag[0]) {
-            if (blockIdx.x == 0 && threadIdx.x == 0 && !flag[0]) {
-                flag[1] = it;  // iterations completed
-                flag[0] = 1;
+    // scalars of the previous iteration, evaluated once per block in FP64
+    __shared__ float s_beta;
+    __shared__ int s_stop;
+    if (threadIdx.x == 0) {
+        const double rz_new = scal[kS_RZN];
+        double beta = 0.0;
+        int stop = 0;
+        if (it > 0) {
+            const double zq = scal[kS_RZO], rr = scal[kS_RR];
+            if (rr <= target_rr || flag[0]) {
+                stop = 1;
+                if (blockIdx.x == 0 && !flag[0]) {
+                    flag[1] = it;  // iterations completed
+                    flag[0] = 1;
+                }
+            } else {
+                const double rz_old = scal[kS_RZ + ((it - 1) & 1)];
+                const double alpha_old = scal[kS_ALPHA + ((it - 1) & 1)];
+                beta = rz_old != 0.0 ? -alpha_old * zq / rz_old : 0.0;
             }
-            return;
         }
-        const double rz_old = scal[kS_RZ + ((it - 1) & 1)];
-        const double alpha_old = scal[kS_ALPHA + ((it - 1) & 1)];
-        beta = rz_old != 0.0 ? -alpha_old * zq / rz_old : 0.0;
+        if (blockIdx.x == 0 && !stop) scal[kS_RZ + (it & 1)] = rz_new;
+        s_beta = (float)beta;
+        s_stop = stop;
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) scal[kS_RZ + (it & 1)] = rz_new;
+    __syncthreads();
+    if (s_stop) return;
     float facc = 0.f;
-    const float fb = (float)beta;
+    const float fb = s_beta;
     const int base = blockIdx.x * kNodeTile + threadIdx.x;
 #pragma unroll
     for (int q4 = 0; q4 < kNodeTile / kNodeThreads; q4++) {
@@ -503,11 +514,15 @@ __global__ void __launch_bounds__(256) k_lpcg_k2(GridDev g, const float* __restr
                                                  const uint16_t* __restrict__ kind, double* gpart, int gstride,
                                                  unsigned* ticket, double* scal, int* flag, int it) {
     if (flag[0]) return;
-    const double dq = scal[kS_DQ];
-    const double rz = scal[kS_RZ + (it & 1)];
-    const double alpha_d = dq != 0.0 ? rz / dq : 0.0;
-    if (blockIdx.x == 0 && threadIdx.x == 0) scal[kS_ALPHA + (it & 1)] = alpha_d;
-    const float alpha = (float)alpha_d;
+    __shared__ float s_alpha;  // alpha = rz / dq, once per block in FP64
+    if (threadIdx.x == 0) {
+        const double dq = scal[kS_DQ];
+        const double alpha_d = dq != 0.0 ? scal[kS_RZ + (it & 1)] / dq : 0.0;
+        if (blockIdx.x == 0) scal[kS_ALPHA + (it & 1)] = alpha_d;
+        s_alpha = (float)alpha_d;
+    }
+    __syncthreads();
+    const float alpha = s_alpha;
     float frr = 0.f;
     const int ng = g.nv >> 2;
     for (int qq = blockIdx.x * blockDim.x + threadIdx.x; qq < ng; qq += gridDim.x * blockDim.x) {

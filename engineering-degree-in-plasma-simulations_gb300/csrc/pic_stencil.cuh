@@ -95,11 +95,13 @@ __device__ __forceinline__ void grid_sum(const float (&v)[N], double* part, int 
     __shared__ double s[N][32];
     __shared__ unsigned s_last;
     const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    // warp sums in FP32 (FP64 would occupy the narrow FP64 pipe with every thread of the grid),
+    // block and grid sums in FP64
 #pragma unroll
     for (int c = 0; c < N; c++) {
-        double x = v[c];
+        float x = v[c];
         for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-        if (lane == 0) s[c][wp] = x;
+        if (lane == 0) s[c][wp] = (double)x;
     }
     __syncthreads();
     if (threadIdx.x < N) {
