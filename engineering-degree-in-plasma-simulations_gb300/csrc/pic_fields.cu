@@ -163,66 +163,179 @@ void launch_efield(const GridDev& g, const float2* phi, float4* ef, cudaStream_t
 // correction's part L e is FP32 (e is small against phi).  The kernel also records rho and the
 // FP32 boundary part of b, from which the next solve updates r without a full pass.
 // ------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(kNodeThreads) k_residual(
-    GridDev g, const float2* __restrict__ phi_in, float2* __restrict__ phi_out, const float* __restrict__ e,
-    const float* __restrict__ rho, const uint16_t* __restrict__ kind, float* __restrict__ r, double* gpart,
-    int gstride, unsigned* ticket, double* out, int apply_e, float* __restrict__ rho_prev,
-    float* __restrict__ bfix_out) {
+// the residual at one FREE node from its potential pp, its six face neighbours pn[d] and, with
+// apply_e, its correction ep and the neighbours' corrections en[d] (direction order -x +x -y +y
+// -z +z); a MIRROR neighbour takes the node's own values
+struct ResConst {
+    FF cf[3];
+    float c3[3];
+    FF ie;
+};
+__device__ __forceinline__ void residual_node(const ResConst& K, uint16_t kd, float2 pp, const float2 (&pn)[6], float ep,
+                                              const float (&en)[6], float rh, bool apply_e, float& rf, float& b,
+                                              float& bfix, float2& np) {
+    FF lphi{0.f, 0.f};
+    float le = 0.f;
+    bfix = 0.f;
+#pragma unroll
+    for (int ax = 0; ax < 3; ax++) {
+        const int dm = 2 * ax, dp = 2 * ax + 1;
+        const bool mm = kd & (1u << (2 + dm)), mp = kd & (1u << (2 + dp));
+        const float2 pm = mm ? pp : pn[dm];
+        const float2 pq = mp ? pp : pn[dp];
+        const FF d1 = ff_diff(pp, pm), d2 = ff_diff(pp, pq);
+        FF sd = two_sum(d1.hi, d2.hi);
+        sd.lo += d1.lo + d2.lo;
+        lphi = ff_add(lphi, ff_mul(K.cf[ax], sd));
+        if (apply_e) le += K.c3[ax] * ((2.f * ep - (mm ? ep : en[dm])) - (mp ? ep : en[dp]));
+        if (kd & (1u << (8 + dm))) bfix += K.c3[ax] * pm.x;
+        if (kd & (1u << (8 + dp))) bfix += K.c3[ax] * pq.x;
+    }
+    if (apply_e) lphi = ff_add_f(lphi, le);
+    FF src = two_prod(rh, K.ie.hi);
+    src.lo += rh * K.ie.lo;
+    const FF res = ff_add(src, ff_neg(lphi));
+    np = pp;
+    if (apply_e) {
+        const FF v = ff_add_f(FF{pp.x, pp.y}, ep);
+        np = make_float2(v.hi, v.lo);
+    }
+    rf = res.hi + res.lo;
+    b = src.hi + bfix;
+}
+
+// neighbour rows of a group of nodes in row (j, k): y and z neighbours with the periodic wrap,
+// clamped on non-periodic walls (a wall row holds no FREE node, its values go unused)
+__device__ __forceinline__ void row_neighbours(const GridDev& g, int j, int k, int& jm, int& jp, int& km, int& kp) {
+    jm = g.periodic[1] ? wrap_m(j, g.nj, 1) : max(j - 1, 0);
+    jp = g.periodic[1] ? wrap_p(j, g.nj, 1) : min(j + 1, g.nj - 1);
+    km = g.periodic[2] ? wrap_m(k, g.nk, 1) : max(k - 1, 0);
+    kp = g.periodic[2] ? wrap_p(k, g.nk, 1) : min(k + 1, g.nk - 1);
+}
+
+// Four consecutive nodes of one row per thread and iteration.  When rows are a multiple of four
+// nodes and the group does not touch the row ends, the group and its y / z neighbour rows are read
+// with 16-byte loads and the two x neighbours with scalar loads; other groups go node by node.
+__global__ void __launch_bounds__(256) k_residual(GridDev g, const float2* __restrict__ phi_in,
+                                                  float2* __restrict__ phi_out, const float* __restrict__ e,
+                                                  const float* __restrict__ rho, const uint16_t* __restrict__ kind,
+                                                  float* __restrict__ r, double* gpart, int gstride, unsigned* ticket,
+                                                  double* out, int apply_e, float* __restrict__ rho_prev,
+                                                  float* __restrict__ bfix_out) {
     // float-float constants from the host: no FP64 arithmetic in the kernel
-    const FF cf[3] = {FF{g.c_hi[0], g.c_lo[0]}, FF{g.c_hi[1], g.c_lo[1]}, FF{g.c_hi[2], g.c_lo[2]}};
     constexpr float kIeHi = (float)(1.0 / kEps0);
     constexpr float kIeLo = (float)(1.0 / kEps0 - (double)kIeHi);
-    const FF ie{kIeHi, kIeLo};
+    ResConst K;
+    for (int ax = 0; ax < 3; ax++) {
+        K.cf[ax] = FF{g.c_hi[ax], g.c_lo[ax]};
+        K.c3[ax] = g.inv_dx[ax] * g.inv_dx[ax];
+    }
+    K.ie = FF{kIeHi, kIeLo};
+    const bool ae = apply_e != 0;
+    const bool rows4 = (g.ni & 3) == 0;
+    const int nij = g.ni * g.nj;
     float acc_r = 0.f, acc_b = 0.f;  // per-thread sums in FP32, block and grid sums in FP64
-    const int base = blockIdx.x * kNodeTile + threadIdx.x;
+    const int ngroups = (g.nv + 3) >> 2;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < ngroups; q += gridDim.x * blockDim.x) {
+        const int n0 = q << 2;
+        int i0, j, k;
+        node_ijk(g, n0, i0, j, k);
+        if (rows4 && i0 >= 1 && i0 + 4 <= g.ni - 1) {
+            int jm, jp, km, kp;
+            row_neighbours(g, j, k, jm, jp, km, kp);
+            const int rowm = (k * g.nj + jm) * g.ni + i0, rowp = (k * g.nj + jp) * g.ni + i0;
+            const int plm = (km * g.nj + j) * g.ni + i0, plp = (kp * g.nj + j) * g.ni + i0;
+            const ushort4 k4 = *reinterpret_cast<const ushort4*>(kind + n0);
+            const unsigned short kv[4] = {k4.x, k4.y, k4.z, k4.w};
+            float2 P[4], Ym[4], Yp[4], Zm[4], Zp[4];
+            auto load4 = [&](const float2* src, float2 (&dst)[4]) {
+                const float4 a0 = *reinterpret_cast<const float4*>(src);
+                const float4 a1 = *reinterpret_cast<const float4*>(src + 2);
+                dst[0] = make_float2(a0.x, a0.y);
+                dst[1] = make_float2(a0.z, a0.w);
+                dst[2] = make_float2(a1.x, a1.y);
+                dst[3] = make_float2(a1.z, a1.w);
+            };
+            load4(phi_in + n0, P);
+            load4(phi_in + rowm, Ym);
+            load4(phi_in + rowp, Yp);
+            load4(phi_in + plm, Zm);
+            load4(phi_in + plp, Zp);
+            const float2 xm = phi_in[n0 - 1], xp = phi_in[n0 + 4];
+            float E[4] = {0.f, 0.f, 0.f, 0.f}, EYm[4] = {0.f, 0.f, 0.f, 0.f}, EYp[4] = {0.f, 0.f, 0.f, 0.f},
+                  EZm[4] = {0.f, 0.f, 0.f, 0.f}, EZp[4] = {0.f, 0.f, 0.f, 0.f}, exm = 0.f, exp_ = 0.f;
+            if (ae) {
+                auto ld = [&](const float* src, float (&dst)[4]) {
+                    const float4 a0 = *reinterpret_cast<const float4*>(src);
+                    dst[0] = a0.x;
+                    dst[1] = a0.y;
+                    dst[2] = a0.z;
+                    dst[3] = a0.w;
+                };
+                ld(e + n0, E);
+                ld(e + rowm, EYm);
+                ld(e + rowp, EYp);
+                ld(e + plm, EZm);
+                ld(e + plp, EZp);
+                exm = e[n0 - 1];
+                exp_ = e[n0 + 4];
+            }
+            const float4 h4 = *reinterpret_cast<const float4*>(rho + n0);
+            const float hv[4] = {h4.x, h4.y, h4.z, h4.w};
+            float rv[4], bf[4];
+            float2 pv[4];
 #pragma unroll
-    for (int q4 = 0; q4 < kNodeTile / kNodeThreads; q4++) {
-        const int n = base + q4 * kNodeThreads;
-        if (n >= g.nv) break;
-        const uint16_t kd = kind[n];
-        if ((kd & 3) != kFree) {
-            if (apply_e) phi_out[n] = phi_in[n];
-            r[n] = 0.f;
+            for (int c = 0; c < 4; c++) {
+                rv[c] = 0.f;
+                bf[c] = 0.f;
+                pv[c] = P[c];
+                if ((kv[c] & 3) != kFree) continue;
+                const float2 pn[6] = {c == 0 ? xm : P[c - 1], c == 3 ? xp : P[c + 1], Ym[c], Yp[c], Zm[c], Zp[c]};
+                const float en[6] = {c == 0 ? exm : E[c - 1], c == 3 ? exp_ : E[c + 1], EYm[c], EYp[c], EZm[c], EZp[c]};
+                float b;
+                residual_node(K, kv[c], P[c], pn, E[c], en, hv[c], ae, rv[c], b, bf[c], pv[c]);
+                acc_r += rv[c] * rv[c];
+                acc_b += b * b;
+            }
+            *reinterpret_cast<float4*>(r + n0) = make_float4(rv[0], rv[1], rv[2], rv[3]);
+            if (ae) {
+                *reinterpret_cast<float4*>(phi_out + n0) = make_float4(pv[0].x, pv[0].y, pv[1].x, pv[1].y);
+                *reinterpret_cast<float4*>(phi_out + n0 + 2) = make_float4(pv[2].x, pv[2].y, pv[3].x, pv[3].y);
+            }
+            if (rho_prev) *reinterpret_cast<float4*>(rho_prev + n0) = h4;
+            if (bfix_out) *reinterpret_cast<float4*>(bfix_out + n0) = make_float4(bf[0], bf[1], bf[2], bf[3]);
             continue;
         }
-        int i, j, k;
-        node_ijk(g, n, i, j, k);
-        Stencil s;
-        stencil(g, i, j, k, s);
-        const float2 pp = phi_in[n];
-        FF lphi{0.f, 0.f};
-        float bfix = 0.f, le = 0.f;
-        const float ep = apply_e ? e[n] : 0.f;
+        // node by node
+        for (int n = n0; n < min(n0 + 4, g.nv); n++) {
+            const uint16_t kd = kind[n];
+            if ((kd & 3) != kFree) {
+                if (ae) phi_out[n] = phi_in[n];
+                r[n] = 0.f;
+                continue;
+            }
+            int i, jj, kk;
+            node_ijk(g, n, i, jj, kk);
+            Stencil st;
+            stencil(g, i, jj, kk, st);
+            float2 pn[6];
+            float en[6];
 #pragma unroll
-        for (int ax = 0; ax < 3; ax++) {
-            const int dm = 2 * ax, dp = 2 * ax + 1;
-            const bool mm = kd & (1u << (2 + dm)), mp = kd & (1u << (2 + dp));
-            const float2 pm = mm ? pp : phi_in[s.q[dm]];
-            const float2 pq = mp ? pp : phi_in[s.q[dp]];
-            const FF d1 = ff_diff(pp, pm), d2 = ff_diff(pp, pq);
-            FF sd = two_sum(d1.hi, d2.hi);
-            sd.lo += d1.lo + d2.lo;
-            lphi = ff_add(lphi, ff_mul(cf[ax], sd));
-            if (apply_e) le += s.c[dm] * ((2.f * ep - (mm ? ep : e[s.q[dm]])) - (mp ? ep : e[s.q[dp]]));
-            if (kd & (1u << (8 + dm))) bfix += s.c[dm] * pm.x;
-            if (kd & (1u << (8 + dp))) bfix += s.c[dp] * pq.x;
+            for (int d = 0; d < 6; d++) {
+                pn[d] = phi_in[st.q[d]];
+                en[d] = ae ? e[st.q[d]] : 0.f;
+            }
+            const float rh = rho[n];
+            float rf, b, bfix;
+            float2 np;
+            residual_node(K, kd, phi_in[n], pn, ae ? e[n] : 0.f, en, rh, ae, rf, b, bfix, np);
+            r[n] = rf;
+            if (ae) phi_out[n] = np;
+            acc_r += rf * rf;
+            acc_b += b * b;
+            if (rho_prev) rho_prev[n] = rh;
+            if (bfix_out) bfix_out[n] = bfix;
         }
-        if (apply_e) lphi = ff_add_f(lphi, le);
-        const float rh = rho[n];
-        FF src = two_prod(rh, ie.hi);
-        src.lo += rh * ie.lo;
-        const FF res = ff_add(src, ff_neg(lphi));
-        if (apply_e) {
-            const FF np = ff_add_f(FF{pp.x, pp.y}, ep);
-            phi_out[n] = make_float2(np.hi, np.lo);
-        }
-        const float rf = res.hi + res.lo;
-        r[n] = rf;
-        const float b = src.hi + bfix;
-        acc_r += rf * rf;
-        acc_b += b * b;
-        if (rho_prev) rho_prev[n] = rh;
-        if (bfix_out) bfix_out[n] = bfix;
     }
     const float v[2] = {acc_r, acc_b};
     grid_sum<2>(v, gpart, gstride, ticket, out);
@@ -230,7 +343,7 @@ __global__ void __launch_bounds__(kNodeThreads) k_residual(
 void launch_residual(const GridDev& g, SolveWork& w, int apply_e, cudaStream_t s, float* rho_prev, float* bfix_out) {
     const float2* in = w.phi;
     float2* out = apply_e ? w.phi_alt : w.phi;
-    k_residual<<<node_blocks(g.nv), kNodeThreads, 0, s>>>(g, in, out, w.e, w.rho,
+    k_residual<<<stream_blocks(g.nv), 256, 0, s>>>(g, in, out, w.e, w.rho,
                                                           reinterpret_cast<const uint16_t*>(w.kind), w.r, w.gpart,
                                                           w.gstride, w.ticket, w.scal + kS_R2, apply_e, rho_prev,
                                                           bfix_out);
@@ -422,7 +535,7 @@ __global__ void __launch_bounds__(256) k_pcg_init(GridDev g, const float* __rest
     const float v[1] = {acc};
     grid_sum<1>(v, gpart, gstride, ticket, scal + kS_RZN);  // r.z
 }
-__global__ void __launch_bounds__(kNodeThreads) k_pcg_k1(GridDev g, const float* __restrict__ z,
+__global__ void __launch_bounds__(256) k_pcg_k1(GridDev g, const float* __restrict__ z,
                                                          const float* __restrict__ d_in, float* __restrict__ d_out,
                                                          float* __restrict__ q, const uint16_t* __restrict__ kind,
                                                          double* gpart, int gstride, unsigned* ticket, double* scal,
@@ -454,35 +567,9 @@ __global__ void __launch_bounds__(kNodeThreads) k_pcg_k1(GridDev g, const float*
     if (s_stop) return;
     const float fb = s_beta;
     float facc = 0.f;
-    const int base = blockIdx.x * kNodeTile + threadIdx.x;
-#pragma unroll
-    for (int q4 = 0; q4 < kNodeTile / kNodeThreads; q4++) {
-        const int n = base + q4 * kNodeThreads;
-        if (n >= g.nv) break;
-        const uint16_t kd = kind[n];
-        if ((kd & 3) != kFree) {
-            d_out[n] = 0.f;
-            q[n] = 0.f;
-            continue;
-        }
-        int i, j, k;
-        node_ijk(g, n, i, j, k);
-        Stencil s;
-        stencil(g, i, j, k, s);
-        const float dn = z[n] + fb * d_in[n];
-        float dg = 0.f, off = 0.f;
-#pragma unroll
-        for (int dd = 0; dd < 6; dd++) {
-            if (kd & (1u << (2 + dd))) continue;
-            dg += s.c[dd];
-            const int qq = s.q[dd];
-            off += s.c[dd] * (z[qq] + fb * d_in[qq]);  // zero on non-FREE neighbours
-        }
-        const float qv = dg * dn - off;
-        d_out[n] = dn;
-        q[n] = qv;
-        facc += dn * qv;
-    }
+    const int ngroups = (g.nv + 3) >> 2;
+    for (int qg = blockIdx.x * blockDim.x + threadIdx.x; qg < ngroups; qg += gridDim.x * blockDim.x)
+        spmv_group(g, qg << 2, z, d_in, d_out, q, kind, fb, facc);
     const float v[1] = {facc};
     grid_sum<1>(v, gpart, gstride, ticket, scal + kS_DQ);
 }
@@ -553,8 +640,7 @@ void launch_pcg_init(const GridDev& g, SolveWork& w, cudaStream_t s) {
 void launch_pcg_iter_impl(const GridDev& g, SolveWork& w, float* d_in, float* d_out, int it, double target_rr,
                           cudaStream_t s) {
     const uint16_t* kd = reinterpret_cast<const uint16_t*>(w.kind);
-    const int nb = node_blocks(g.nv);
-    k_pcg_k1<<<nb, kNodeThreads, 0, s>>>(g, w.z, d_in, d_out, w.q, kd, w.gpart, w.gstride, w.ticket, w.scal, w.flag,
+    k_pcg_k1<<<stream_blocks(g.nv), 256, 0, s>>>(g, w.z, d_in, d_out, w.q, kd, w.gpart, w.gstride, w.ticket, w.scal, w.flag,
                                          it, target_rr);
     k_pcg_k2<<<stream_blocks(g.nv), 256, 0, s>>>(g, d_out, w.q, w.e, w.r, w.z, kd, w.gpart, w.gstride, w.ticket,
                                                  w.scal, w.flag, it);

@@ -443,7 +443,7 @@ void launch_lp_fold(const LpState& L, cudaStream_t s) {
 //   B    : z = B r ; partials z.r, z.q            (beta = z.(r_new - r_old) / rz_prev)
 // scal[0..1] rz and scal[2..3] alpha, double-buffered by iteration parity
 // =====================================================================================
-__global__ void __launch_bounds__(kNodeThreads) k_lpcg_k1(GridDev g, const float* __restrict__ z,
+__global__ void __launch_bounds__(256) k_lpcg_k1(GridDev g, const float* __restrict__ z,
                                                           const float* __restrict__ d_in, float* __restrict__ d_out,
                                                           float* __restrict__ q, const uint16_t* __restrict__ kind,
                                                           double* gpart, int gstride, unsigned* ticket,
@@ -477,35 +477,9 @@ __global__ void __launch_bounds__(kNodeThreads) k_lpcg_k1(GridDev g, const float
     if (s_stop) return;
     float facc = 0.f;
     const float fb = s_beta;
-    const int base = blockIdx.x * kNodeTile + threadIdx.x;
-#pragma unroll
-    for (int q4 = 0; q4 < kNodeTile / kNodeThreads; q4++) {
-        const int n = base + q4 * kNodeThreads;
-        if (n >= g.nv) break;
-        const uint16_t kd = kind[n];
-        if ((kd & 3) != kFree) {
-            d_out[n] = 0.f;
-            q[n] = 0.f;
-            continue;
-        }
-        int i, j, k;
-        node_ijk(g, n, i, j, k);
-        Stencil s;
-        stencil(g, i, j, k, s);
-        const float dn = z[n] + fb * d_in[n];
-        float dg = 0.f, off = 0.f;
-#pragma unroll
-        for (int d = 0; d < 6; d++) {
-            if (kd & (1u << (2 + d))) continue;
-            dg += s.c[d];
-            const int qq = s.q[d];
-            off += s.c[d] * (z[qq] + fb * d_in[qq]);
-        }
-        const float qv = dg * dn - off;
-        d_out[n] = dn;
-        q[n] = qv;
-        facc += dn * qv;
-    }
+    const int ngroups = (g.nv + 3) >> 2;
+    for (int qg = blockIdx.x * blockDim.x + threadIdx.x; qg < ngroups; qg += gridDim.x * blockDim.x)
+        spmv_group(g, qg << 2, z, d_in, d_out, q, kind, fb, facc);
     const float v[1] = {facc};
     grid_sum<1>(v, gpart, gstride, ticket, scal + kS_DQ);
 }
@@ -582,8 +556,7 @@ void launch_lpcg_init(const GridDev& g, SolveWork& w, const LpState& L, cudaStre
 void launch_lpcg_iter(const GridDev& g, SolveWork& w, const LpState& L, float* d_in, float* d_out, int it,
                       double target_rr, cudaStream_t s, int sms) {
     const uint16_t* kd = reinterpret_cast<const uint16_t*>(w.kind);
-    const int nb = node_blocks(g.nv);
-    k_lpcg_k1<<<nb, kNodeThreads, 0, s>>>(g, w.z, d_in, d_out, w.q, kd, w.gpart, w.gstride, w.ticket, w.scal, w.flag,
+    k_lpcg_k1<<<stream_blocks(g.nv), 256, 0, s>>>(g, w.z, d_in, d_out, w.q, kd, w.gpart, w.gstride, w.ticket, w.scal, w.flag,
                                           it, target_rr);
     k_lpcg_k2<<<stream_blocks(g.nv), 256, 0, s>>>(g, d_out, w.q, w.e, w.r, kd, w.gpart, w.gstride, w.ticket, w.scal,
                                                   w.flag, it);

@@ -472,47 +472,41 @@ __global__ void __launch_bounds__(kThreads, 3) k_push(PushArgs a) {
             if (a.deposit) t.dtile = dtile;
         }
 
-        // phase 1, all kPPT particles: gather, push, move (independent chains, interleaved by the
-        // compiler); phase 2: the deposit runs over the consecutive particles
         unsigned dead_mask[kPPT];
-        float3 O[kPPT];
-        int NC[kPPT];
+        Corners run;        // deposit sums of the current cell run
+        int run_cell = -1;  // packed cell of the run, -1: none
 #pragma unroll
         for (int q = 0; q < kPPT; q++) {
             const int p = base + tid * kPPT + q;
             dead_mask[q] = 0;
-            NC[q] = -1;
             if (bn[q] < 0) continue;
-            const int c = __float_as_int(P[q].w);
+            int c = __float_as_int(P[q].w);
             int i, j, k;
             cell_ijk(g, c, i, j, k);
             float3 o = make_float3(P[q].x, P[q].y, P[q].z);
             float3 v = make_float3(V[q].x, V[q].y, V[q].z);
+            const float w = V[q].w;
             // leapfrog push (Species.cpp:369-373)
-            const float3 E = gather_e(a, t, bn[q], o);
+            float3 E = gather_e(a, t, bn[q], o);
             v.x += a.qm_dt * E.x;
             v.y += a.qm_dt * E.y;
             v.z += a.qm_dt * E.z;
             const int newc = move_particle(a, i, j, k, o, v);
             a.sp.pos[p] = make_float4(o.x, o.y, o.z, __int_as_float(newc));
-            a.sp.vel[p] = make_float4(v.x, v.y, v.z, V[q].w);
-            O[q] = o;
-            NC[q] = newc;
-            if (newc < 0) dead_mask[q] = 1;
-        }
-        if (a.deposit) {
-            Corners run;        // deposit sums of the current cell run
-            int run_cell = -1;  // packed cell of the run, -1: none
-#pragma unroll
-            for (int q = 0; q < kPPT; q++) {
-                const int newc = NC[q];
-                if (newc < 0) continue;
-                if (newc != run_cell && run_cell >= 0) commit_corners(a, t, cell_base(g, run_cell), run);
-                corner_values(V[q].w, O[q], a.dep_scale, run, newc == run_cell);
-                run_cell = newc;
+            a.sp.vel[p] = make_float4(v.x, v.y, v.z, w);
+            if (newc >= 0) {
+                if (a.deposit) {
+                    if (newc != run_cell && run_cell >= 0)
+                        commit_corners(a, t, cell_base(g, run_cell), run);
+                    corner_values(w, o, a.dep_scale, run, newc == run_cell);
+                    run_cell = newc;
+                }
+            } else {
+                dead_mask[q] = 1;
             }
-            if (run_cell >= 0) commit_corners(a, t, cell_base(g, run_cell), run);
         }
+        if (run_cell >= 0)
+            commit_corners(a, t, cell_base(g, run_cell), run);
         // warp-aggregated record of the particles that left the domain
 #pragma unroll
         for (int q = 0; q < kPPT; q++) {

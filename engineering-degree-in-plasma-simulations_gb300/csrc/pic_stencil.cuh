@@ -132,6 +132,88 @@ __device__ __forceinline__ void grid_sum(const float (&v)[N], double* part, int 
     if (threadIdx.x == 0) *ticket = 0u;
 }
 
+// d' = z + beta d_in, q = L d' over the nodes n0 .. n0+3 of one row (d'.q summed into acc).  When
+// rows are a multiple of four nodes and the group does not touch the row ends, the group and its
+// y / z neighbour rows are read with 16-byte loads; other groups go node by node.
+__device__ __forceinline__ void spmv_group(const GridDev& g, int n0, const float* __restrict__ z,
+                                           const float* __restrict__ d_in, float* __restrict__ d_out,
+                                           float* __restrict__ q, const uint16_t* __restrict__ kind, float fb,
+                                           float& acc) {
+    int i0, j, k;
+    node_ijk(g, n0, i0, j, k);
+    const float c3[3] = {g.inv_dx[0] * g.inv_dx[0], g.inv_dx[1] * g.inv_dx[1], g.inv_dx[2] * g.inv_dx[2]};
+    if ((g.ni & 3) == 0 && i0 >= 1 && i0 + 4 <= g.ni - 1) {
+        const int jm = g.periodic[1] ? wrap_m(j, g.nj, 1) : max(j - 1, 0);
+        const int jp = g.periodic[1] ? wrap_p(j, g.nj, 1) : min(j + 1, g.nj - 1);
+        const int km = g.periodic[2] ? wrap_m(k, g.nk, 1) : max(k - 1, 0);
+        const int kp = g.periodic[2] ? wrap_p(k, g.nk, 1) : min(k + 1, g.nk - 1);
+        const int off[4] = {(k * g.nj + jm) * g.ni + i0, (k * g.nj + jp) * g.ni + i0, (km * g.nj + j) * g.ni + i0,
+                            (kp * g.nj + j) * g.ni + i0};
+        // d' at the group, its x ends and its four neighbour rows
+        auto dv4 = [&](int o, float (&dst)[4]) {
+            const float4 a = *reinterpret_cast<const float4*>(z + o);
+            const float4 b = *reinterpret_cast<const float4*>(d_in + o);
+            dst[0] = a.x + fb * b.x;
+            dst[1] = a.y + fb * b.y;
+            dst[2] = a.z + fb * b.z;
+            dst[3] = a.w + fb * b.w;
+        };
+        float C[4], N[4][4];
+        dv4(n0, C);
+#pragma unroll
+        for (int m = 0; m < 4; m++) dv4(off[m], N[m]);
+        const float xm = z[n0 - 1] + fb * d_in[n0 - 1], xp = z[n0 + 4] + fb * d_in[n0 + 4];
+        const ushort4 k4 = *reinterpret_cast<const ushort4*>(kind + n0);
+        const unsigned short kv[4] = {k4.x, k4.y, k4.z, k4.w};
+        float dvo[4], qv[4];
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            dvo[c] = 0.f;
+            qv[c] = 0.f;
+            if ((kv[c] & 3) != kFree) continue;
+            const float nb[6] = {c == 0 ? xm : C[c - 1], c == 3 ? xp : C[c + 1], N[0][c], N[1][c], N[2][c], N[3][c]};
+            float dg = 0.f, o = 0.f;
+#pragma unroll
+            for (int d = 0; d < 6; d++) {
+                if (kv[c] & (1u << (2 + d))) continue;
+                dg += c3[d >> 1];
+                o += c3[d >> 1] * nb[d];  // zero on non-FREE neighbours
+            }
+            dvo[c] = C[c];
+            qv[c] = dg * C[c] - o;
+            acc += dvo[c] * qv[c];
+        }
+        *reinterpret_cast<float4*>(d_out + n0) = make_float4(dvo[0], dvo[1], dvo[2], dvo[3]);
+        *reinterpret_cast<float4*>(q + n0) = make_float4(qv[0], qv[1], qv[2], qv[3]);
+        return;
+    }
+    for (int n = n0; n < min(n0 + 4, g.nv); n++) {
+        const uint16_t kd = kind[n];
+        if ((kd & 3) != kFree) {
+            d_out[n] = 0.f;
+            q[n] = 0.f;
+            continue;
+        }
+        int i, jj, kk;
+        node_ijk(g, n, i, jj, kk);
+        Stencil st;
+        stencil(g, i, jj, kk, st);
+        const float dn = z[n] + fb * d_in[n];
+        float dg = 0.f, o = 0.f;
+#pragma unroll
+        for (int d = 0; d < 6; d++) {
+            if (kd & (1u << (2 + d))) continue;
+            dg += st.c[d];
+            const int qq = st.q[d];
+            o += st.c[d] * (z[qq] + fb * d_in[qq]);
+        }
+        const float qv = dg * dn - o;
+        d_out[n] = dn;
+        q[n] = qv;
+        acc += dn * qv;
+    }
+}
+
 // inverse diagonal of the reduced operator from the node's mirror mask
 __device__ __forceinline__ float inv_diag_of(uint16_t kd, const float c[3]) {
     float dg = 0.f;
