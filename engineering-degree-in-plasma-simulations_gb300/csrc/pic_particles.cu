@@ -206,6 +206,7 @@ __device__ __forceinline__ int move_particle(const PushArgs& a, int i, int j, in
 // whenever hi > 0.  64-bit conversions are slow on this GPU; 32-bit ones run on the integer and
 // conversion units at full rate.
 __device__ __forceinline__ unsigned long long f2u64_rn(float x) {
+    if (x < 0x1p32f) return __float2uint_rn(x);  // the common case: one 32-bit conversion
     const float hi = floorf(x * 0x1p-32f);
     const float lo = fmaf(hi, -0x1p32f, x);
     return ((unsigned long long)__float2uint_rz(hi) << 32) + __float2uint_rn(lo);
