@@ -60,6 +60,9 @@ def library():
         "pic_world_set_time": [vp, d, i],
         "pic_world_advance_time": [vp, vp],
         "pic_world_get_ts": [vp, vp],
+        "pic_world_get_time": [vp, vp],
+        "pic_world_potential_energy": [vp, vp],
+        "pic_species_sample_particles": [vp, i, l, vp, vp, vp],
         "pic_world_set_boundaries": [vp, vp, vp, vp],
         "pic_world_add_box": [vp, vp, vp, d],
         "pic_world_get_field": [vp, i, vp],
@@ -185,6 +188,18 @@ class World:
         _check(self._L.pic_world_get_ts(self._h, C.byref(t)))
         return t.value
 
+    def getTime(self):
+        """World::getTime (World.cpp:331-333): the sum of dt over the advanceTime calls."""
+        t = C.c_double()
+        _check(self._L.pic_world_get_time(self._h, C.byref(t)))
+        return t.value
+
+    def getPE(self):
+        """World::getPE (World.cpp:108-119): 0.5 eps0 sum |E|^2 node_vol, summed on the device."""
+        pe = C.c_double()
+        _check(self._L.pic_world_potential_energy(self._h, C.byref(pe)))
+        return pe.value
+
     def getDx(self):
         return self.dx.copy()
 
@@ -240,6 +255,16 @@ class World:
     @property
     def ef(self):
         return self._get(3, 3)
+
+    @property
+    def node_type(self):
+        """World::node_type (World.h:17, 57): 0 REGULAR, 1 NEUMANN, 2 DIRICHLET."""
+        return self._get(4).astype(np.int32)
+
+    @property
+    def object_id(self):
+        """World::object_id (World.h:55): 1 on nodes inside a box, else 0."""
+        return self._get(5).astype(np.int32)
 
     @ef.setter
     def ef(self, v):
@@ -338,6 +363,16 @@ class Species:
         out = np.zeros(n, PARTICLE)
         out["pos"], out["vel"], out["w"], out["id"] = pos[:n], vel[:n], w[:n], ids[:n]
         return out
+
+    def sample_particles(self, num_out):
+        """(pos [m,3], vel [m,3]) of every (n // num_out)-th particle, the particle sample of
+        Output::particlesOutput (Outputs.cpp:207-245); all particles when num_out > n."""
+        pos = np.zeros((num_out, 3))
+        vel = np.zeros((num_out, 3))
+        got = C.c_long()
+        _check(self._L.pic_species_sample_particles(self.world._h, self.id, int(num_out), _p(pos), _p(vel),
+                                                    C.byref(got)))
+        return pos[:got.value], vel[:got.value]
 
     def advance(self, dt, deposit=True):
         _check(self._L.pic_species_push(self.world._h, self.id, float(dt), int(deposit)))

@@ -15,6 +15,7 @@
 #include "pic_kernels.h"
 #include "pic_learned.h"
 #include "pic_ff.cuh"
+#include "pic_stencil.cuh"
 
 using namespace pic;
 
@@ -116,6 +117,7 @@ struct pic_world {
     double dt = 1e-4;
     int num_ts = 0;
     int ts = -1;
+    double time = 0.0;
     // solver
     int method = PIC_SOLVER_PCG;
     double tol = 1e-6;
@@ -228,6 +230,12 @@ int set_last_error(int code, const char* msg) { return fail(code, "%s", msg); }
 namespace {
 
 // node kinds and masks; Dirichlet values written into phi_host
+bool node_in_box(const pic_world::Box& b, const double x[3]) {  // Rectangle::inObject, Object.cpp:231-238
+    for (int d = 0; d < 3; d++)
+        if (std::fabs(x[d] - b.c[d]) > b.s[d] / 2) return false;
+    return true;
+}
+
 void build_kinds(pic_world* w, std::vector<uint16_t>& kind, std::vector<double>& phi_host) {
     const GridDev& g = w->g;
     int nn[3] = {g.ni, g.nj, g.nk};
@@ -246,15 +254,11 @@ void build_kinds(pic_world* w, std::vector<uint16_t>& kind, std::vector<double>&
                 }
                 double x[3] = {g.x0[0] + i * g.dxd[0], g.x0[1] + j * g.dxd[1], g.x0[2] + k * g.dxd[2]};
                 bool in_box = false;
-                for (auto& b : w->boxes) {
-                    bool in = true;
-                    for (int d = 0; d < 3; d++)
-                        if (std::fabs(x[d] - b.c[d]) > b.s[d] / 2) in = false;
-                    if (in && !in_box) {
+                for (auto& b : w->boxes)  // a later box overrides an earlier one (World.cpp:277-293)
+                    if (node_in_box(b, x)) {
                         in_box = true;
                         phi_host[n] = b.phi;
                     }
-                }
                 if (in_box) {
                     kind[n] = kFixed;
                     continue;
@@ -630,8 +634,14 @@ extern "C" int pic_world_set_time(pic_world* w, double dt, int num_ts) {
 }
 extern "C" int pic_world_advance_time(pic_world* w, int* running) {
     if (!w) return fail(PIC_ERR_ARG, "null world");
+    w->time += w->dt;
     w->ts++;
     if (running) *running = w->ts <= w->num_ts;
+    return PIC_OK;
+}
+extern "C" int pic_world_get_time(pic_world* w, double* time) {
+    if (!w || !time) return fail(PIC_ERR_ARG, "null argument");
+    *time = w->time;
     return PIC_OK;
 }
 extern "C" int pic_world_get_ts(pic_world* w, int* ts) {
@@ -702,15 +712,41 @@ extern "C" int pic_world_get_field(pic_world* w, int which, double* out) {
         CU(cudaStreamSynchronize(w->stream));
         for (int n = 0; n < g.nv; n++) out[n] = t[n];
     } else if (which == 2) {
-        int nn[3] = {g.ni, g.nj, g.nk};
+        // World::computeNodeVolumes: half a cell per non-periodic face (of each stacked instance)
+        const int nn[3] = {g.ni, g.nj, g.zslab ? g.zslab : g.nk};
         for (int k = 0; k < g.nk; k++)
             for (int j = 0; j < g.nj; j++)
                 for (int i = 0; i < g.ni; i++) {
-                    int ijk[3] = {i, j, k};
+                    int ijk[3] = {i, j, g.zslab ? k % g.zslab : k};
                     double v = g.dxd[0] * g.dxd[1] * g.dxd[2];
                     for (int d = 0; d < 3; d++)
                         if (!w->periodic[d] && (ijk[d] == 0 || ijk[d] == nn[d] - 1)) v *= 0.5;
                     out[(k * g.nj + j) * g.ni + i] = v;
+                }
+    } else if (which == 4 || which == 5) {
+        // node_type (World.h:17: REGULAR 0, NEUMANN 1, DIRICHLET 2) or object_id (1 inside an object)
+        std::vector<uint16_t> kind;
+        std::vector<double> ph;
+        build_kinds(w, kind, ph);
+        const int nn[3] = {g.ni, g.nj, g.nk};
+        for (int k = 0; k < g.nk; k++)
+            for (int j = 0; j < g.nj; j++)
+                for (int i = 0; i < g.ni; i++) {
+                    const int n = (k * g.nj + j) * g.ni + i;
+                    if (which == 4) {
+                        // the duplicate last plane of a periodic axis reports its source node
+                        int ijk[3] = {i, j, k};
+                        for (int d = 0; d < 3; d++)
+                            if (w->periodic[d] && ijk[d] == nn[d] - 1) ijk[d] = 0;
+                        const int kd = kind[(ijk[2] * g.nj + ijk[1]) * g.ni + ijk[0]] & 3;
+                        out[n] = kd == kFixed ? 2.0 : kd == kMirror ? 1.0 : 0.0;
+                        continue;
+                    }
+                    const double x[3] = {g.x0[0] + i * g.dxd[0], g.x0[1] + j * g.dxd[1], g.x0[2] + k * g.dxd[2]};
+                    double id = 0.0;
+                    for (auto& b : w->boxes)
+                        if (node_in_box(b, x)) id = 1.0;
+                    out[n] = id;
                 }
     } else if (which == 3) {
         std::vector<float4> t(g.nv);
@@ -724,6 +760,23 @@ extern "C" int pic_world_get_field(pic_world* w, int which, double* out) {
     } else {
         return fail(PIC_ERR_ARG, "unknown field %d", which);
     }
+    return check_device_error(w);
+}
+extern "C" int pic_world_potential_energy(pic_world* w, double* pe) {
+    if (!w || !pe) return fail(PIC_ERR_ARG, "null argument");
+    CU(cudaSetDevice(w->device));
+    const int grid = 512;
+    {
+        Scope sc(w, "diagnostics", 1);
+        launch_field_energy(w->g, w->ef, w->part, w->stream, grid);
+    }
+    std::vector<double> h(grid);
+    CU(cudaMemcpyAsync(h.data(), w->part, sizeof(double) * grid, cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    double t = 0;
+    for (int b = 0; b < grid; b++) t += h[b];
+    const GridDev& g = w->g;
+    *pe = 0.5 * kEps0 * g.dxd[0] * g.dxd[1] * g.dxd[2] * t;
     return check_device_error(w);
 }
 extern "C" int pic_world_set_field(pic_world* w, int which, const double* in) {
@@ -931,6 +984,35 @@ extern "C" int pic_species_get_particles(pic_world* w, int sp, double* pos, doub
     cudaFreeAsync(dv, w->stream);
     cudaFreeAsync(dw, w->stream);
     cudaFreeAsync(di, w->stream);
+    CU(cudaStreamSynchronize(w->stream));
+    return check_device_error(w);
+}
+
+extern "C" int pic_species_sample_particles(pic_world* w, int sp, long num_out, double* pos, double* vel,
+                                            long* n_out) {
+    if (!valid_sp(w, sp) || num_out <= 0 || !n_out) return fail(PIC_ERR_ARG, "bad arguments");
+    long n = 0;
+    int rc = pic_species_count(w, sp, &n);
+    if (rc) return rc;
+    // Output::particlesOutput: every (n / num_out)-th particle, all of them when there are fewer
+    long step = n / num_out, m = num_out;
+    if (num_out > n) {
+        m = n;
+        step = 1;
+    }
+    *n_out = m;
+    if (m == 0) return PIC_OK;
+    double *dp, *dv;
+    CU(cudaMallocAsync((void**)&dp, sizeof(double) * 3 * m, w->stream));
+    CU(cudaMallocAsync((void**)&dv, sizeof(double) * 3 * m, w->stream));
+    {
+        Scope sc(w, "export", 1);
+        launch_to_abs(w->g, w->sp[sp].dev, dp, dv, nullptr, nullptr, (int)m, w->stream, 0, step);
+    }
+    if (pos) CU(cudaMemcpyAsync(pos, dp, sizeof(double) * 3 * m, cudaMemcpyDeviceToHost, w->stream));
+    if (vel) CU(cudaMemcpyAsync(vel, dv, sizeof(double) * 3 * m, cudaMemcpyDeviceToHost, w->stream));
+    cudaFreeAsync(dp, w->stream);
+    cudaFreeAsync(dv, w->stream);
     CU(cudaStreamSynchronize(w->stream));
     return check_device_error(w);
 }

@@ -155,6 +155,46 @@ void launch_efield(const GridDev& g, const float2* phi, float4* ef, cudaStream_t
 }
 
 // ------------------------------------------------------------------------------------
+// field energy sum |E|^2 V_node / V_cell (World::getPE, World.cpp:108-119): node volumes halve
+// on every non-periodic face (slab faces for stacked instances); the duplicate last plane of a
+// periodic axis is skipped.  Per-thread sums in float-float, FP64 from the warp sums on; the
+// host adds the block partials and scales by eps0/2 * V_cell.
+// ------------------------------------------------------------------------------------
+__global__ void k_field_energy(GridDev g, const float4* __restrict__ ef, double* part) {
+    FF a{0.f, 0.f};
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.nv; n += gridDim.x * blockDim.x) {
+        int ijk[3];
+        node_ijk(g, n, ijk[0], ijk[1], ijk[2]);
+        const int nn[3] = {g.ni, g.nj, g.zslab ? g.zslab : g.nk};
+        ijk[2] = slab_local_z(g, ijk[2]);
+        float f = 1.f;
+        bool alias = false;
+        for (int d = 0; d < 3; d++) {
+            const bool face = ijk[d] == 0 || ijk[d] == nn[d] - 1;
+            if (g.periodic[d]) alias |= ijk[d] == nn[d] - 1;
+            else if (face) f *= 0.5f;
+        }
+        if (alias) continue;
+        const float4 e = __ldg(&ef[n]);
+        FF e2 = ff_add(ff_add(two_prod(e.x, e.x), two_prod(e.y, e.y)), two_prod(e.z, e.z));
+        a = ff_add(a, FF{e2.hi * f, e2.lo * f});  // f is a power of two: exact
+    }
+    __shared__ double s[32];
+    double x = (double)a.hi + (double)a.lo;
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = x;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += s[w];
+        part[blockIdx.x] = t;
+    }
+}
+void launch_field_energy(const GridDev& g, const float4* ef, double* part, cudaStream_t s, int grid) {
+    k_field_energy<<<grid, 256, 0, s>>>(g, ef, part);
+}
+
+// ------------------------------------------------------------------------------------
 // Residual of the reduced system in float-float, optionally after phi += e (ping-pong buffers)
 //   r = b - L phi,  b = rho/eps0 + sum_{FIXED q} c_q phi_q ; partials: |r|^2, |b|^2
 // (L phi)_p = sum_ax c_ax ((phi_p - phi_minus) + (phi_p - phi_plus)), a mirror neighbour taking

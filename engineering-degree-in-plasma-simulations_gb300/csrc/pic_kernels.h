@@ -54,8 +54,9 @@ void launch_sort(const GridDev& g, SpeciesDev sp, float4* pos_alt, float4* vel_a
 void launch_from_abs(const GridDev& g, SpeciesDev sp, const double* pos, const double* vel, const double* w,
                      const unsigned long long* id, int n, int rewind, float qm_half_dt, const float4* ef,
                      cudaStream_t s);
+// particles first + p * stride, p < n, to absolute FP64 positions (null outputs are skipped)
 void launch_to_abs(const GridDev& g, SpeciesDev sp, double* pos, double* vel, double* w, unsigned long long* id,
-                   int n, cudaStream_t s);
+                   int n, cudaStream_t s, long long first = 0, long long stride = 1);
 struct LoadArgs {
     double lo[3], hi[3];   // absolute box
     float vth;             // sqrt(kT/m) per axis (Maxwellian) or sqrt(2kT/m) (reference sampleV3th)
@@ -89,6 +90,8 @@ struct FinalizeArgs {
 };
 void launch_finalize_rho(const FinalizeArgs& a, cudaStream_t s, int grid);
 void launch_efield(const GridDev& g, const float2* phi, float4* ef, cudaStream_t s, int grid);
+// per-block partials of sum |E|^2 f over the distinct nodes, f the node's volume in cells
+void launch_field_energy(const GridDev& g, const float4* ef, double* part, cudaStream_t s, int grid);
 void launch_kinds(const GridDev& g, uint8_t* kind, cudaStream_t s);
 
 struct SolveWork {

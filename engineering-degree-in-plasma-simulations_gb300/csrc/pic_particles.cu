@@ -896,28 +896,34 @@ void launch_from_abs(const GridDev& g, SpeciesDev sp, const double* pos, const d
     launch_compact(sp, s, 256);
 }
 
+// export of particles first, first + stride, ... (n of them) to absolute FP64 positions
 __global__ void k_to_abs(GridDev g, SpeciesDev sp, double* pos, double* vel, double* w, unsigned long long* id,
-                         int n) {
+                         int n, long long first, long long stride) {
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
-        float4 ps = sp.pos[p], vs = sp.vel[p];
+        const long long q = first + (long long)p * stride;
+        float4 ps = sp.pos[q], vs = sp.vel[q];
         int i, j, k;
         cell_ijk(g, __float_as_int(ps.w), i, j, k);
-        pos[3 * p] = g.x0[0] + ((double)i + (double)ps.x) * g.dxd[0];
-        pos[3 * p + 1] = g.x0[1] + ((double)j + (double)ps.y) * g.dxd[1];
-        pos[3 * p + 2] = g.x0[2] + ((double)k + (double)ps.z) * g.dxd[2];
-        vel[3 * p] = vs.x;
-        vel[3 * p + 1] = vs.y;
-        vel[3 * p + 2] = vs.z;
-        w[p] = vs.w;
-        id[p] = sp.id[p];
+        if (pos) {
+            pos[3 * p] = g.x0[0] + ((double)i + (double)ps.x) * g.dxd[0];
+            pos[3 * p + 1] = g.x0[1] + ((double)j + (double)ps.y) * g.dxd[1];
+            pos[3 * p + 2] = g.x0[2] + ((double)k + (double)ps.z) * g.dxd[2];
+        }
+        if (vel) {
+            vel[3 * p] = vs.x;
+            vel[3 * p + 1] = vs.y;
+            vel[3 * p + 2] = vs.z;
+        }
+        if (w) w[p] = vs.w;
+        if (id) id[p] = sp.id[q];
     }
 }
 void launch_to_abs(const GridDev& g, SpeciesDev sp, double* pos, double* vel, double* w, unsigned long long* id,
-                   int n, cudaStream_t s) {
+                   int n, cudaStream_t s, long long first, long long stride) {
     int grid = (n + 255) / 256;
     if (grid > 4096) grid = 4096;
     if (grid < 1) grid = 1;
-    k_to_abs<<<grid, 256, 0, s>>>(g, sp, pos, vel, w, id, n);
+    k_to_abs<<<grid, 256, 0, s>>>(g, sp, pos, vel, w, id, n, first, stride);
 }
 
 // ------------------------------------------------------------------------------------

@@ -40,6 +40,8 @@ int pic_world_set_time(pic_world* w, double dt, int num_ts);
 int pic_world_advance_time(pic_world* w, int* running);
 /* World::getTs()                                                      World.cpp:328-330 */
 int pic_world_get_ts(pic_world* w, int* ts);
+/* World::getTime(): the sum of dt over the advanceTime calls          World.cpp:331-333, 337-341 */
+int pic_world_get_time(pic_world* w, double* time);
 /* Boundary set-up, replacing World::dirichletBoundries / addInlet / computeObjectID for the
  * domain faces (World.cpp:206-292).  periodic[3]: 1 makes an axis periodic (absent in the
  * reference).  face_mode[6] for faces -x,+x,-y,+y,-z,+z: 0 Neumann wall (reference v3 GS:
@@ -55,10 +57,15 @@ int pic_world_set_boundaries(pic_world* w, const int* periodic, const int* face_
  * all instances at once.  nslabs = 0 returns to a single instance. */
 int pic_world_set_slabs(pic_world* w, int nslabs, const double* phi_lo, const double* phi_hi);
 int pic_world_add_box(pic_world* w, const double* center, const double* sides, double phi);
-/* public fields World::phi, rho, node_vol, ef                        World.h:51-54
- * which: 0 phi, 1 rho, 2 node_vol, 3 ef (3 values per node)          */
+/* public fields World::phi, rho, node_vol, ef, node_type, object_id  World.h:51-57
+ * which: 0 phi, 1 rho, 2 node_vol, 3 ef (3 values per node), 4 node_type (World.h:17:
+ * 0 REGULAR, 1 NEUMANN, 2 DIRICHLET), 5 object_id (1 on nodes inside a box, World.cpp:277-293).
+ * Node arrays are x fastest: n = (k * nj + j) * ni + i. */
 int pic_world_get_field(pic_world* w, int which, double* out);
 int pic_world_set_field(pic_world* w, int which, const double* in); /* 0 phi, 1 rho, 3 ef */
+/* World::getPE(): 0.5 eps0 sum |E|^2 node_vol in FP64                 World.cpp:108-119
+ * (the duplicate last node plane of a periodic axis is not counted) */
+int pic_world_potential_energy(pic_world* w, double* pe);
 
 /* ---- Species (ch4/v3/src/Species.h:31-133) -------------------------------------------- */
 
@@ -89,6 +96,10 @@ int pic_species_count(pic_world* w, int sp, long* n);
 /* Species::getConstPartRef(): host copy of the particles              Species.cpp:820-822 */
 int pic_species_get_particles(pic_world* w, int sp, double* pos, double* vel, double* wgt, uint64_t* ids, long cap,
                               long* n);
+/* The particle sample of Output::particlesOutput                     Outputs.cpp:207-245
+ * particles 0, s, 2s, ... with s = n / num_out (all n when num_out > n), *n_out of them; pos and
+ * vel hold 3 * num_out values.  Particles are in device storage order (by cell after a sort). */
+int pic_species_sample_particles(pic_world* w, int sp, long num_out, double* pos, double* vel, long* n_out);
 /* Species::advanceElectrons / advanceNonElectron (dt)                 Species.cpp:258-399, 47-256
  * One leapfrog push; with deposit = 1 the weight is also scattered at the new position, which
  * is Species::computeNumberDensity (Species.cpp:401-416) fused into the push. */

@@ -9,7 +9,10 @@
 #ifndef PIC_GB300_HPP
 #define PIC_GB300_HPP
 #include <array>
+#include <chrono>
+#include <cmath>
 #include <cstdint>
+#include <iostream>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -42,8 +45,11 @@ class World {  // ch4/v3/src/World.h:15-116
 public:
     const int ni, nj, nk, nv, num_cells;
     World(int ni_, int nj_, int nk_, type_calc3 x0, type_calc3 xm, int device = 0)
-        : ni(ni_), nj(nj_), nk(nk_), nv(ni_ * nj_ * nk_), num_cells((ni_ - 1) * (nj_ - 1) * (nk_ - 1)) {
+        : ni(ni_), nj(nj_), nk(nk_), nv(ni_ * nj_ * nk_), num_cells((ni_ - 1) * (nj_ - 1) * (nk_ - 1)), x0_(x0),
+          time_start_(std::chrono::high_resolution_clock::now()) {
         check(pic_world_create(&h_, ni, nj, nk, x0.data(), xm.data(), device));
+        const int nn[3] = {ni, nj, nk};
+        for (int d = 0; d < 3; d++) dx_[d] = (xm[d] - x0[d]) / (nn[d] - 1);  // World.cpp:58-66
     }
     World(const World&) = delete;
     World& operator=(const World&) = delete;
@@ -51,6 +57,7 @@ public:
     pic_world* handle() const { return h_; }
     void setTime(type_calc dt, int num_ts) {
         dt_ = dt;
+        num_ts_ = num_ts;
         check(pic_world_set_time(h_, dt, num_ts));
     }
     type_calc getDt() const { return dt_; }
@@ -64,6 +71,30 @@ public:
         check(pic_world_get_ts(h_, &t));
         return t;
     }
+    type_calc getTime() const {  // World.cpp:331-333
+        double t = 0;
+        check(pic_world_get_time(h_, &t));
+        return t;
+    }
+    bool isLastTimeStep() const { return getTs() == num_ts_ - 1; }
+    type_calc getWallTime() const {  // seconds since construction or setTimeStart, World.cpp:342-346
+        return std::chrono::duration<double>(std::chrono::high_resolution_clock::now() - time_start_).count();
+    }
+    void setTimeStart() { time_start_ = std::chrono::high_resolution_clock::now(); }
+    type_calc3 getX0() const { return x0_; }
+    type_calc3 getDx() const { return dx_; }
+    type_calc getCellVolume() const { return dx_[0] * dx_[1] * dx_[2]; }
+    int getNumCells() const { return num_cells; }
+    type_calc getPE() const {  // World.cpp:108-119, summed on the device
+        double pe = 0;
+        check(pic_world_potential_energy(h_, &pe));
+        return pe;
+    }
+    // World.cpp:167-191: steady once the total real count, |momentum| sum and energy all change
+    // by less than 1e-3 (relative) between two calls
+    template <class V>
+    bool steadyState(V& species);
+    bool steadyState() const { return steady_state_; }
     void dirichletBoundries(type_calc phi = 0) {  // World.cpp:263-274
         int per[3] = {0, 0, 0}, mode[6] = {1, 1, 1, 1, 1, 1};
         double val[6] = {phi, phi, phi, phi, phi, phi};
@@ -79,6 +110,8 @@ public:
     std::vector<double> rho() const { return field(1, 1); }
     std::vector<double> node_vol() const { return field(2, 1); }
     std::vector<double> ef() const { return field(3, 3); }
+    std::vector<double> node_type() const { return field(4, 1); }  // World.h:17: REGULAR, NEUMANN, DIRICHLET
+    std::vector<double> object_id() const { return field(5, 1); }
     void setPhi(const std::vector<double>& v) { check(pic_world_set_field(h_, 0, v.data())); }
     void computeChargeDensity() { check(pic_charge_density(h_)); }  // World.cpp:193-200
     template <class V>
@@ -94,12 +127,20 @@ private:
     }
     pic_world* h_ = nullptr;
     type_calc dt_ = 1e-4;
+    int num_ts_ = 0;
+    type_calc3 x0_{}, dx_{};
+    std::chrono::high_resolution_clock::time_point time_start_;
+    bool steady_state_ = false;
+    type_calc last_mass_ = 0, last_mom_ = 0, last_en_ = 0;
 };
 
 class Species {  // ch4/v3/src/Species.h:31-133
 public:
     const std::string name;
     const type_calc mass, charge, mpw0;
+    // host copies of the reference's public fields, filled by the calls that compute them
+    std::vector<double> vel, T;                // computeGasProperties
+    std::vector<int32_t> macro_part_count;     // computeMacroParticlesCount
     Species(std::string name_, type_calc mass_, type_calc charge_, World& world, type_calc mpw0_,
             long capacity = 1 << 20, double weight_bound = 0)
         : name(name_), mass(mass_), charge(charge_), mpw0(mpw0_), world_(&world) {
@@ -129,16 +170,40 @@ public:
     void computeNumberDensity() { check(pic_species_number_density(world_->handle(), id_)); }
     void updateAverages() { check(pic_species_update_averages(world_->handle(), id_)); }
     void sortIndexes() { check(pic_species_sort(world_->handle(), id_, nullptr)); }
-    std::vector<int32_t> computeMacroParticlesCount() {
-        std::vector<int32_t> c((size_t)world_->num_cells);
-        check(pic_species_sort(world_->handle(), id_, c.data()));
-        return c;
+    // Species.cpp:813-819; the counts stay in macro_part_count (a cell field, x fastest)
+    const std::vector<int32_t>& computeMacroParticlesCount() {
+        macro_part_count.assign((size_t)world_->num_cells, 0);
+        check(pic_species_sort(world_->handle(), id_, macro_part_count.data()));
+        return macro_part_count;
     }
     void merge(int min_count = 10) { check(pic_species_merge(world_->handle(), id_, min_count)); }
     std::vector<double> den() const {
         std::vector<double> d((size_t)world_->nv);
         check(pic_species_get_den(world_->handle(), id_, d.data()));
         return d;
+    }
+    std::vector<double> den_avg() const {  // Species.h:50
+        std::vector<double> d((size_t)world_->nv);
+        check(pic_species_get_den_avg(world_->handle(), id_, d.data()));
+        return d;
+    }
+    void sampleMoments() { check(pic_species_sample_moments(world_->handle(), id_)); }  // Species.cpp:767-776
+    void clearSamples() { check(pic_species_clear_samples(world_->handle(), id_)); }    // Species.cpp:805-812
+    // Species.cpp:777-804: stream velocity (3 per node) into vel and temperature into T
+    void computeGasProperties() {
+        vel.assign((size_t)world_->nv * 3, 0.0);
+        T.assign((size_t)world_->nv, 0.0);
+        check(pic_species_gas_properties(world_->handle(), id_, vel.data(), T.data()));
+    }
+    // every (n / num)-th particle, the sample Output::particlesOutput writes (Outputs.cpp:207-245)
+    std::vector<Particle> sampleParticles(long num) const {
+        std::vector<double> pos((size_t)num * 3), v((size_t)num * 3);
+        long got = 0;
+        check(pic_species_sample_particles(world_->handle(), id_, num, pos.data(), v.data(), &got));
+        std::vector<Particle> out((size_t)got);
+        for (long p = 0; p < got; p++)
+            out[p] = {{pos[3 * p], pos[3 * p + 1], pos[3 * p + 2]}, {v[3 * p], v[3 * p + 1], v[3 * p + 2]}, 0.0, 0};
+        return out;
     }
     type_calc getMicroCount() const { return sums()[0]; }
     type_calc3 getMomentum() const {
@@ -168,6 +233,34 @@ private:
     World* world_;
     int id_ = -1;
 };
+
+namespace detail {
+inline Species& sp_ref(Species& s) { return s; }
+inline Species& sp_ref(Species* s) { return *s; }
+}  // namespace detail
+
+template <class V>
+bool World::steadyState(V& species) {
+    if (steady_state_) return true;
+    type_calc tot_mass = 0, tot_mom = 0, tot_en = getPE();
+    for (auto& x : species) {
+        Species& sp = detail::sp_ref(x);
+        tot_mass += sp.getMicroCount();
+        type_calc3 m = sp.getMomentum();
+        tot_mom += std::sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
+        tot_en += sp.getKE();
+    }
+    const type_calc tol = 1e-3;
+    if (std::fabs((tot_mass - last_mass_) / tot_mass) < tol && std::fabs(tot_mom - last_mom_) / tot_mom < tol &&
+        std::fabs(tot_en - last_en_) / tot_en < tol) {
+        steady_state_ = true;
+        std::cout << "\nSteady state reached at time step " << getTs() << std::endl;
+    }
+    last_mass_ = tot_mass;
+    last_mom_ = tot_mom;
+    last_en_ = tot_en;
+    return steady_state_;
+}
 
 class PotentialSolver {  // ch4/v3/src/PotentialSolver.h:26-88
 public:

@@ -8,7 +8,7 @@ import subprocess
 
 import pytest
 
-from conftest import ROOT
+from conftest import ROOT, PKG_NAME
 
 
 def header_symbols():
@@ -43,8 +43,9 @@ def test_last_error_message_is_reported(pic):
     assert b"dt" in buf.value or b"null" in buf.value
 
 
-def test_cpp_facade_compiles():
-    src = os.path.join(ROOT, "include", "pic_gb300.hpp")
-    r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-x", "c++", src, "-I", os.path.join(ROOT, "include")],
-                       capture_output=True, text=True)
+@pytest.mark.parametrize("src", ["include/pic_gb300.hpp", "include/pic_gb300_outputs.hpp",
+                                 PKG_NAME + "/examples/v3_loop.cpp"])
+def test_cpp_facade_compiles(src):
+    r = subprocess.run(["g++", "-std=c++17", "-Wall", "-Werror", "-fsyntax-only", "-x", "c++", os.path.join(ROOT, src),
+                        "-I", os.path.join(ROOT, "include")], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
