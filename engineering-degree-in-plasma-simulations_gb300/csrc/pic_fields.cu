@@ -394,14 +394,16 @@ void launch_residual(const GridDev& g, SolveWork& w, int apply_e, cudaStream_t s
     }
 }
 // residual of the next solve without a full pass: r += (rho - rho_prev) / eps0 on FREE nodes
-// (r holds the residual of the current phi, rounded to FP32); |r|^2, |b|^2 into out[0..1].
+// (r holds the residual of the current phi, rounded to FP32); |r|^2, |b|^2 and the squared norm
+// of the update t = (rho - rho_prev) / eps0 into out[0..2] (the host bounds the rounding error
+// of r from |t| and |r|).
 // Four consecutive nodes per thread and iteration with 16-byte loads.
 __global__ void __launch_bounds__(256) k_rhs_update(GridDev g, float* __restrict__ r, const float* __restrict__ rho,
                                                     float* __restrict__ rho_prev, const float* __restrict__ bfix,
                                                     const uint16_t* __restrict__ kind, double* gpart, int gstride,
                                                     unsigned* ticket, double* out) {
     const float inv_eps0_f = (float)(1.0 / kEps0);
-    float acc_r = 0.f, acc_b = 0.f;
+    float acc_r = 0.f, acc_b = 0.f, acc_t = 0.f;
     const int ng = g.nv >> 2;
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < ng; q += gridDim.x * blockDim.x) {
         const float4 r4 = reinterpret_cast<const float4*>(r)[q];
@@ -415,10 +417,12 @@ __global__ void __launch_bounds__(256) k_rhs_update(GridDev g, float* __restrict
 #pragma unroll
         for (int c = 0; c < 4; c++) {
             if ((kv[c] & 3) != kFree) continue;
-            rv[c] += (hv[c] - pv[c]) * inv_eps0_f;
+            const float t = (hv[c] - pv[c]) * inv_eps0_f;
+            rv[c] += t;
             const float b = hv[c] * inv_eps0_f + fv[c];
             acc_r += rv[c] * rv[c];
             acc_b += b * b;
+            acc_t += t * t;
         }
         reinterpret_cast<float4*>(r)[q] = make_float4(rv[0], rv[1], rv[2], rv[3]);
         reinterpret_cast<float4*>(rho_prev)[q] = h4;
@@ -428,16 +432,18 @@ __global__ void __launch_bounds__(256) k_rhs_update(GridDev g, float* __restrict
         const int n = (ng << 2) + threadIdx.x;
         if ((kind[n] & 3) == kFree) {
             const float rh = rho[n];
-            const float rn = r[n] + (rh - rho_prev[n]) * inv_eps0_f;
+            const float t = (rh - rho_prev[n]) * inv_eps0_f;
+            const float rn = r[n] + t;
             r[n] = rn;
             const float b = rh * inv_eps0_f + bfix[n];
             acc_r += rn * rn;
             acc_b += b * b;
+            acc_t += t * t;
         }
         rho_prev[n] = rho[n];
     }
-    const float v[2] = {acc_r, acc_b};
-    grid_sum<2>(v, gpart, gstride, ticket, out);
+    const float v[3] = {acc_r, acc_b, acc_t};
+    grid_sum<3>(v, gpart, gstride, ticket, out);
 }
 void launch_rhs_update(const GridDev& g, SolveWork& w, float* rho_prev, const float* bfix, cudaStream_t s) {
     k_rhs_update<<<stream_blocks(g.nv), 256, 0, s>>>(g, w.r, w.rho, rho_prev, bfix,

@@ -133,6 +133,7 @@ enum : int {
     kS_RZO = 6,     // r_new.z_old (Jacobi) / z.q (learned)
     kS_RR = 7,      // r.r
     kS_R2 = 8,      // residual |r|^2, |b|^2 at 8, 9
+    kS_T2 = 10,     // |(rho - rho_prev) / eps0|^2 of the last FP32 residual update
     kS_VAL = 12,    // validation norm
 };
 // residual (optionally after phi += e); |r|^2 and |b|^2 into scal[kS_R2..]

@@ -221,6 +221,38 @@ def test_poisson_matches_oracle(pic, port, case, method):
     assert np.max(np.abs(phi - ref)) <= 1e-6 * np.max(np.abs(ref))
 
 
+@pytest.mark.parametrize("method", ["pcg", "learned"])
+def test_warm_solves_stay_below_tolerance(pic, port, method):
+    """Warm solves for slowly changing rho: the FP32-updated residual is accepted without a full
+    pass only under its rounding-error bound, so the oracle's FP64 residual of every answer stays
+    below the tolerance, and the small updates are certified without full passes."""
+    c = POISSON_CASES["c2_periodic_xy"]
+    g = port.grid(c["nn"], c["x0"], c["xm"], periodic=c["per"], boxes=[])
+    kind = port.node_kinds(g, 1)
+    nv = int(np.prod(c["nn"]))
+    W = pic.World(*c["nn"], c["x0"], c["xm"])
+    W.set_boundaries(c["per"], c["mode"], (0, 0, 0, 0, 0.0, 50.0))
+    rng = np.random.default_rng(11)
+    rho = rng.normal(size=nv) * 1e-7 + 2e-7
+    W.rho = rho
+    solver = {"pcg": pic.SOLVER_PCG, "learned": pic.SOLVER_LEARNED}[method]
+    tol = 1e-6
+    S = pic.PotentialSolver(W, 20000, tol, solver)
+    assert S.solve(raise_on_fail=True)
+    st0 = S.stats()
+    for step in range(12):
+        # tiny drifts are certified by the bound; every fourth step a larger change needs iterations
+        scale = 1e-3 if step % 4 == 3 else 1e-12
+        rho = rho + rng.normal(size=nv) * 2e-7 * scale
+        W.rho = rho
+        assert S.solve(raise_on_fail=True)
+        assert port.rel_residual(g, kind, W.phi, W.rho) <= tol * 1.001
+    st = S.stats()
+    solves, full = st["solves"] - st0["solves"], st["refinements"] - st0["refinements"]
+    assert solves == 12
+    assert full <= 3 + 3 * 2  # the larger changes: an inner solve and its residual; the drifts: none
+
+
 def test_poisson_reference_gs_agrees_on_v3_walls(pic, port):
     """The reference GS (golden) and the device solve agree on the v3 scenario walls."""
     d = golden("poisson")
