@@ -4,6 +4,7 @@
 // model that the reference keeps in main.cpp (ch4/v3/src/main.cpp:71-139).  All device work
 // is issued on the world's own stream; only calls that hand data back to the host, and the
 // solver's convergence checks, synchronise it.
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -111,8 +112,8 @@ struct pic_world {
     // neutral density per slab and the candidate probabilities derived from it
     int nslabs = 0;
     std::vector<double> slab_lo, slab_hi, slab_n;
-    float* p_null_slab = nullptr;
-    double p_null_slab_dt = -1.0;
+    unsigned* cand_slab = nullptr;  // candidate thresholds per slab
+    double cand_slab_dt = -1.0;
     int* mcc_cand = nullptr;   // collision candidates of a step (electron capacity)
     int* mcc_ncand = nullptr;
     // time
@@ -383,18 +384,28 @@ void fill_grid_boxes(pic_world* w) {
     for (int d = 0; d < 3; d++) g.periodic[d] = w->periodic[d];
 }
 
-// candidate probabilities n_s (sigma v)_max dt of the instance slabs (uploaded when dt changes)
-int slab_candidate_probabilities(pic_world* w, double dt, CollDev& c) {
-    c.p_null_slab = nullptr;
+// candidate threshold of probability p on the 32-bit candidate draw: candidate iff draw < T,
+// probability T / 2^32 (within 2^-32 of p)
+unsigned cand_threshold(double p) {
+    if (!(p > 0.0)) return 0u;
+    if (p >= 1.0) return 0xFFFFFFFFu;
+    return (unsigned)(p * 4294967296.0);
+}
+// candidate thresholds of the collision model for a step of dt: the world's, or per instance slab
+// from n_s (sigma v)_max dt (uploaded when dt changes) with the largest as the first-pass bound
+int candidate_thresholds(pic_world* w, double dt, CollDev& c) {
+    c.cand_slab = nullptr;
+    c.cand_max = cand_threshold(w->mcc_n * w->mcc_sigv * dt);
     if (w->slab_n.empty()) return PIC_OK;
-    if (w->p_null_slab_dt != dt) {
-        std::vector<float> pn(w->slab_n.size());
-        for (size_t q = 0; q < pn.size(); q++) pn[q] = (float)(w->slab_n[q] * w->mcc_sigv * dt);
-        CU(cudaMemcpyAsync(w->p_null_slab, pn.data(), sizeof(float) * pn.size(), cudaMemcpyHostToDevice, w->stream));
+    std::vector<unsigned> th(w->slab_n.size());
+    for (size_t q = 0; q < th.size(); q++) th[q] = cand_threshold(w->slab_n[q] * w->mcc_sigv * dt);
+    if (w->cand_slab_dt != dt) {
+        CU(cudaMemcpyAsync(w->cand_slab, th.data(), sizeof(unsigned) * th.size(), cudaMemcpyHostToDevice, w->stream));
         CU(cudaStreamSynchronize(w->stream));
-        w->p_null_slab_dt = dt;
+        w->cand_slab_dt = dt;
     }
-    c.p_null_slab = w->p_null_slab;
+    c.cand_max = *std::max_element(th.begin(), th.end());
+    c.cand_slab = w->cand_slab;
     return PIC_OK;
 }
 
@@ -592,7 +603,7 @@ extern "C" int pic_world_destroy(pic_world* w) {
     free_lp(w);
     if (w->rho_prev) cudaFree(w->rho_prev);
     if (w->aux_pairs) cudaFree(w->aux_pairs);
-    if (w->p_null_slab) cudaFree(w->p_null_slab);
+    if (w->cand_slab) cudaFree(w->cand_slab);
     if (w->mcc_cand) cudaFree(w->mcc_cand);
     if (w->mcc_ncand) cudaFree(w->mcc_ncand);
     if (w->bfix) cudaFree(w->bfix);
@@ -1039,8 +1050,7 @@ int push_species(pic_world* w, int sp, double dt, int deposit, bool with_mcc, bo
     if (with_mcc && w->mcc_on && sp == w->mcc_e) {
         a.coll = w->coll;
         a.coll.enabled = 1;
-        a.coll.p_null = (float)(w->mcc_n * w->mcc_sigv * dt);
-        int prc = slab_candidate_probabilities(w, dt, a.coll);
+        int prc = candidate_thresholds(w, dt, a.coll);
         if (prc) return prc;
         a.coll.step = (unsigned)w->ts;
         a.coll.ion = w->sp[w->mcc_i].dev;
@@ -1800,9 +1810,9 @@ extern "C" int pic_mcc_set_slab_density(pic_world* w, int nslabs, const double* 
     if (nslabs != w->nslabs || nslabs <= 0 || !n_neutral)
         return fail(PIC_ERR_ARG, "one density per instance slab (%d slabs)", w->nslabs);
     CU(cudaSetDevice(w->device));
-    if (!w->p_null_slab) CU(cudaMalloc(&w->p_null_slab, sizeof(float) * nslabs));
+    if (!w->cand_slab) CU(cudaMalloc(&w->cand_slab, sizeof(unsigned) * nslabs));
     w->slab_n.assign(n_neutral, n_neutral + nslabs);
-    w->p_null_slab_dt = -1.0;
+    w->cand_slab_dt = -1.0;
     return PIC_OK;
 }
 
@@ -1821,8 +1831,7 @@ extern "C" int pic_mcc_apply(pic_world* w, double dt) {
     a.err = w->err;
     a.coll = w->coll;
     a.coll.enabled = 1;
-    a.coll.p_null = (float)(w->mcc_n * w->mcc_sigv * dt);
-    int prc = slab_candidate_probabilities(w, dt, a.coll);
+    int prc = candidate_thresholds(w, dt, a.coll);
     if (prc) return prc;
     a.coll.step = (unsigned)w->ts;
     a.coll.ion = w->sp[w->mcc_i].dev;

@@ -100,12 +100,22 @@ __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
 // uniform in (0,1): ((x >> 9) + 0.5) * 2^-23, 24 significant bits, exact in FP32
 __device__ __forceinline__ float u01(unsigned x) { return ((float)(x >> 9) + 0.5f) * (1.0f / 8388608.0f); }
 
-// splitmix64 finaliser (Steele, Lea, Flood 2014): ids of collision products
-__device__ __forceinline__ unsigned long long child_id(unsigned long long parent, unsigned step, unsigned kind) {
-    unsigned long long x = parent + 0x9E3779B97F4A7C15ull * ((((unsigned long long)step) << 2) | kind);
+// splitmix64 finaliser (Steele, Lea, Flood 2014)
+__device__ __forceinline__ unsigned long long mix64(unsigned long long x) {
     x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
     x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
     return x ^ (x >> 31);
+}
+// ids of collision products
+__device__ __forceinline__ unsigned long long child_id(unsigned long long parent, unsigned step, unsigned kind) {
+    return mix64(parent + 0x9E3779B97F4A7C15ull * ((((unsigned long long)step) << 2) | kind));
+}
+// 32-bit draw of the null-collision candidate test of particle id at a step: output step + 1 of
+// a SplitMix64 stream whose seed is the scrambled (id xor key), so the decision is keyed by
+// (seed, step, id) and independent of the particle order, for four 64-bit multiplies
+__device__ __forceinline__ unsigned cand_draw(unsigned long long id, unsigned step, uint2 key) {
+    const unsigned long long s = mix64(id ^ (((unsigned long long)key.y << 32) | key.x));
+    return (unsigned)(mix64(s + 0x9E3779B97F4A7C15ull * ((unsigned long long)step + 1ull)) >> 32);
 }
 
 __device__ __forceinline__ void set_error(unsigned* err, unsigned bit) {

@@ -6,11 +6,12 @@ namespace pic {
 
 int set_last_error(int code, const char* msg);  // message for pic_last_error
 
-// Electron-impact collisions against a uniform background gas (fused into the electron push)
+// Electron-impact collisions against a uniform background gas (candidates, then collisions)
 struct CollDev {
     int enabled;
-    float p_null;            // n_n (sigma v)_max dt : candidate probability
-    const float* p_null_slab;  // per instance slab (stacked instances with their own n_n), or nullptr
+    unsigned cand_max;       // candidate threshold 2^32 n_n (sigma v)_max dt on cand_draw (the largest
+                             // of the slabs' when cand_slab is set)
+    const unsigned* cand_slab;  // per instance slab (stacked instances with their own n_n), or nullptr
     float sigv_max;          // (sigma v)_max [m^3/s]
     float sig_n;             // sqrt(k T_n / m_n): neutral thermal speed per axis
     float m_n, m_e;

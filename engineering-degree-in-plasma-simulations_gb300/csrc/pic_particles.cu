@@ -536,31 +536,21 @@ __global__ void __launch_bounds__(kThreads, 3) k_push(PushArgs a) {
 
 // ------------------------------------------------------------------------------------
 // collisions as separate passes ahead of a collision-free push:
-//   candidates: one Philox draw per electron (u01(r0.x) < p_null), a list of candidates
-//   collide   : the collisions of the candidates (same draws as the fused kernel: the streams are
-//               keyed by (seed, step, id)); the ejected electron is pushed and deposited there,
-//               the ion product appended
-// The split keeps the push kernel free of the collision registers and code.
+//   candidates: cand_draw(id) < 2^32 P_null per electron, a list of candidates (with instance
+//               slabs the list holds the draws below the largest slab threshold; the collide pass
+//               applies the particle's own slab threshold)
+//   collide   : the collisions of the candidates (Philox draws keyed by (seed, step, id)); the
+//               ejected electron is pushed and deposited there, the ion product appended
+// The split keeps the push kernel free of the collision registers and code, and the candidate
+// pass reads only the ids.
 // ------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_mcc_candidates(PushArgs a, int* cand, int* ncand) {
     const CollDev& cd = a.coll;
-    const GridDev& g = a.g;
     const int n = a.sp.counts[0];
-    unsigned st_cand = 0;
     const int lane = threadIdx.x & 31;
     for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const int p = base + threadIdx.x;
-        bool is_cand = false;
-        if (p < n) {
-            const unsigned long long id = a.sp.id[p];
-            float p_null = cd.p_null;
-            if (cd.p_null_slab) {
-                const int c = __float_as_int(a.sp.pos[p].w);
-                if (c >= 0) p_null = __ldg(&cd.p_null_slab[fdiv((unsigned)(c >> 18), g.fd_zslab)]);
-            }
-            const uint4 r0 = philox4x32_10(make_uint4((unsigned)id, (unsigned)(id >> 32), cd.step, 0u), cd.key);
-            is_cand = u01(r0.x) < p_null;
-        }
+        const bool is_cand = p < n && cand_draw(a.sp.id[p], cd.step, cd.key) < cd.cand_max;
         const unsigned m = __ballot_sync(0xffffffffu, is_cand);
         if (m) {
             int b0 = 0;
@@ -568,10 +558,7 @@ __global__ void __launch_bounds__(256) k_mcc_candidates(PushArgs a, int* cand, i
             b0 = __shfl_sync(0xffffffffu, b0, __ffs(m) - 1);
             if (is_cand) cand[b0 + __popc(m & ((1u << lane) - 1u))] = p;
         }
-        st_cand += is_cand ? 1u : 0u;
     }
-    const unsigned x = __reduce_add_sync(0xffffffffu, st_cand);
-    if (lane == 0 && x) atomicAdd(&cd.stats[0], (unsigned long long)x);
 }
 
 __global__ void __launch_bounds__(128) k_mcc_collide(PushArgs a, const int* cand, const int* ncand) {
@@ -580,7 +567,7 @@ __global__ void __launch_bounds__(128) k_mcc_collide(PushArgs a, const int* cand
     const int n = a.sp.counts[0];
     const int ion_n = cd.ion.counts[0];
     const int nc = *ncand;
-    unsigned st_coll = 0, st_ion = 0, st_lost = 0;
+    unsigned st_cand = 0, st_coll = 0, st_ion = 0, st_lost = 0;
     Tile t;  // no staged rows: gathers and deposits go to HBM
     t.etile = nullptr;
     t.dtile = nullptr;
@@ -596,9 +583,12 @@ __global__ void __launch_bounds__(128) k_mcc_collide(PushArgs a, const int* cand
         const float4 V = a.sp.vel[p];
         const int c = __float_as_int(P.w);
         if (c < 0) continue;
+        const unsigned long long id = a.sp.id[p];
+        if (cd.cand_slab && cand_draw(id, cd.step, cd.key) >= __ldg(&cd.cand_slab[fdiv((unsigned)(c >> 18), g.fd_zslab)]))
+            continue;  // below the largest slab threshold, not below its own
+        st_cand++;
         int i, j, k;
         cell_ijk(g, c, i, j, k);
-        const unsigned long long id = a.sp.id[p];
         const uint4 r0 = philox4x32_10(make_uint4((unsigned)id, (unsigned)(id >> 32), cd.step, 0u), cd.key);
         const float w = V.w;
         Collision col = collide_candidate(cd, id, make_float3(V.x, V.y, V.z), r0);
@@ -630,12 +620,12 @@ __global__ void __launch_bounds__(128) k_mcc_collide(PushArgs a, const int* cand
             st_lost++;
         }
     }
-    const unsigned v[3] = {st_coll, st_ion, st_lost};
+    const unsigned v[4] = {st_cand, st_coll, st_ion, st_lost};
     const int lane = threadIdx.x & 31;
 #pragma unroll
-    for (int x = 0; x < 3; x++) {
+    for (int x = 0; x < 4; x++) {
         const unsigned s = __reduce_add_sync(0xffffffffu, v[x]);
-        if (lane == 0 && s) atomicAdd(&cd.stats[1 + x], (unsigned long long)s);
+        if (lane == 0 && s) atomicAdd(&cd.stats[x], (unsigned long long)s);
     }
 }
 

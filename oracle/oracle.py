@@ -101,6 +101,8 @@ class Port:
             "or_sigv_majorant": (d, [vp]),
             "or_mcc_background": (l, [vp, vp, vp, vp, vp, l, vp, vp, vp, l, d, u32, u32, u32, vp]),
             "or_child_id": (C.c_uint64, [C.c_uint64, u32, u32]),
+            "or_cand_draw": (u32, [C.c_uint64, u32, u32, u32]),
+            "or_cand_threshold": (u32, [d]),
             "or_ntc_ionize_ref": (l, [vp, vp, vp, vp, vp, l, vp, vp, l, vp, vp, l, d, vp]),
             "or_merge_ref": (l, [vp, vp, vp, l, l, vp, d, d, d, i]),
             "or_merge_gpuform": (l, [vp, vp, vp, vp, l, l, vp, d, d, d, i, u32, u32, u32]),

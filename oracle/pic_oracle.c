@@ -140,13 +140,27 @@ void or_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out
 }
 double or_u01_from_u32(uint32_t x) { return ((double)(x >> 9) + 0.5) * (1.0 / 8388608.0); }
 
-/* splitmix64 finaliser (Steele, Lea, Flood 2014) over parent id, step and product kind. */
-uint64_t or_child_id(uint64_t parent, uint32_t step, uint32_t kind) {
-    uint64_t x = parent + 0x9E3779B97F4A7C15ull * ((((uint64_t)step) << 2) | (uint64_t)kind);
+/* splitmix64 finaliser (Steele, Lea, Flood 2014) */
+static uint64_t or_mix64(uint64_t x) {
     x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
     x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
-    x ^= x >> 31;
-    return x;
+    return x ^ (x >> 31);
+}
+/* ids of collision products: the finaliser over parent id, step and product kind */
+uint64_t or_child_id(uint64_t parent, uint32_t step, uint32_t kind) {
+    return or_mix64(parent + 0x9E3779B97F4A7C15ull * ((((uint64_t)step) << 2) | (uint64_t)kind));
+}
+/* 32-bit draw of the null-collision candidate test: output step + 1 of a SplitMix64 stream
+ * seeded by the scrambled (id xor seed) */
+uint32_t or_cand_draw(uint64_t id, uint32_t step, uint32_t seed_lo, uint32_t seed_hi) {
+    uint64_t s = or_mix64(id ^ (((uint64_t)seed_hi << 32) | seed_lo));
+    return (uint32_t)(or_mix64(s + 0x9E3779B97F4A7C15ull * ((uint64_t)step + 1ull)) >> 32);
+}
+/* candidate iff draw < T, T = floor(p 2^32) clamped to [0, 2^32 - 1] */
+uint32_t or_cand_threshold(double p) {
+    if (!(p > 0.0)) return 0u;
+    if (p >= 1.0) return 0xFFFFFFFFu;
+    return (uint32_t)(p * 4294967296.0);
 }
 
 /* ------------------------------------------------------------------------------------ */
@@ -1019,8 +1033,9 @@ static double phx_draw(void* st) {
  * Equivalent in expectation to the reference NTC (Interactions.cpp:646-678) when the
  * neutral weight exceeds the electron weight: each electron is a candidate with
  * probability P_null = n_n (sigma v)_max dt and is accepted with sigma v_rel/(sigma v)_max.
- * Draw layout per electron, counter (id_lo, id_hi, step, block):
- *   block 0: a0 candidate test | a1,a2 Box-Muller (vx,vy) | a3 acceptance
+ * Candidate test: or_cand_draw(id, step, seed) < or_cand_threshold(P_null).
+ * Draw layout per candidate, counter (id_lo, id_hi, step, block):
+ *   block 0: a0 unused | a1,a2 Box-Muller (vx,vy) | a3 acceptance
  *   block 1: b0,b1 Box-Muller (vz) | b2,b3 product offset x,y
  *   blocks 2,3: the collide() draws in phx_draw order (at most six)
  *   block 4: word 0 product offset z
@@ -1033,11 +1048,12 @@ long or_mcc_background(const or_grid* g, const or_coll_params* cp, or_particle* 
     double m_n = cp->mass_neutral, m_e = cp->mass_electron;
     double m_red = m_n * m_e / (m_n + m_e);
     double E_precalc_rel_eV = 0.5 * m_red / OR_QE;
-    double p_null = cp->n_neutral * cp->sigv_max * dt;
+    uint32_t cand_max = or_cand_threshold(cp->n_neutral * cp->sigv_max * dt);
     double sig_n = sqrt(OR_KB * cp->T_neutral / m_n);
     const double TWO_PI = 6.283185307179586;
     long n0 = *n_ele, ncoll = 0, nion = 0;
     for (long p = 0; p < n0; p++) {
+        if (!(or_cand_draw(ele_id[p], step, seed_lo, seed_hi) < cand_max)) continue;
         phx_stream st;
         st.key[0] = seed_lo;
         st.key[1] = seed_hi;
@@ -1046,7 +1062,6 @@ long or_mcc_background(const or_grid* g, const or_coll_params* cp, or_particle* 
         st.ctr[2] = step;
         phx_block(&st, 0);
         uint32_t a[4] = {st.buf[0], st.buf[1], st.buf[2], st.buf[3]};
-        if (!(or_u01_from_u32(a[0]) < p_null)) continue;
         phx_block(&st, 1);
         uint32_t b[4] = {st.buf[0], st.buf[1], st.buf[2], st.buf[3]};
         double r1 = sqrt(-2 * log(or_u01_from_u32(a[1]))), t1 = TWO_PI * or_u01_from_u32(a[2]);

@@ -119,6 +119,8 @@ long or_mcc_background(const or_grid* g, const or_coll_params* cp, or_particle* 
                        long cap_ele, or_particle* ion, uint64_t* ion_id, long* n_ion, long cap_ion, double dt,
                        uint32_t seed_lo, uint32_t seed_hi, uint32_t step, long* n_ionized);
 uint64_t or_child_id(uint64_t parent, uint32_t step, uint32_t kind);
+uint32_t or_cand_draw(uint64_t id, uint32_t step, uint32_t seed_lo, uint32_t seed_hi);
+uint32_t or_cand_threshold(double p);
 
 /* Reference NTC ionisation with neutral macroparticles (Interactions.cpp:600-762), MT19937 draws.
  * wsv_max is the persistent (W*sigma*v)_max, updated in place. Returns collisions. */

@@ -43,6 +43,39 @@ def test_philox_known_answer(port):
         0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1]
 
 
+def test_candidate_draw_restatement_and_statistics(port):
+    """The null-collision candidate draw (output step + 1 of a SplitMix64 stream seeded by the
+    scrambled id ^ seed): the C restatement equals this numpy one, and the test id draw < T
+    selects a fraction T / 2^32 of the particles, independently from step to step."""
+    M = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+    def mix(x):
+        x = x.astype(np.uint64)
+        x = (x ^ (x >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        x = (x ^ (x >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        return x ^ (x >> np.uint64(31))
+
+    seed = 0x1234_5678_9ABC_DEF0
+    ids = (np.arange(200000, dtype=np.uint64) * np.uint64(7) + np.uint64(3)) & M
+    with np.errstate(over="ignore"):
+        s = mix(ids ^ np.uint64(seed))
+        draws = {st: (mix(s + np.uint64(0x9E3779B97F4A7C15) * np.uint64(st + 1)) >> np.uint64(32)).astype(np.uint32)
+                 for st in (0, 1, 2)}
+    for k in range(0, 200000, 9973):
+        for st in (0, 1, 2):
+            assert port.lib.or_cand_draw(int(ids[k]), st, seed & 0xFFFFFFFF, seed >> 32) == draws[st][k]
+    p = 0.01
+    T = port.lib.or_cand_threshold(p)
+    assert T == int(p * 2 ** 32) and port.lib.or_cand_threshold(2.0) == 2 ** 32 - 1
+    assert port.lib.or_cand_threshold(0.0) == 0
+    n = len(ids)
+    sel = [draws[st] < T for st in (0, 1, 2)]
+    for a in sel:
+        assert abs(a.sum() - n * p) <= 5 * np.sqrt(n * p)
+    both = (sel[0] & sel[1]).sum()  # independent steps: n p^2 joint selections
+    assert abs(both - n * p * p) <= 5 * np.sqrt(n * p * p) + 1
+
+
 def test_load_push_deposit_bit_exact(port):
     d = golden("push_deposit")
     g = port.grid(d["nn"], d["x0"], d["xm"])
