@@ -21,6 +21,7 @@
 using namespace pic;
 
 constexpr double kFp32Unit = 0x1p-24;  // unit roundoff of FP32 round-to-nearest
+constexpr long kUploadChunk = 1l << 22;  // particles per upload staging round (256 MB)
 
 namespace {
 
@@ -121,6 +122,8 @@ struct pic_world {
     int num_ts = 0;
     int ts = -1;
     double time = 0.0;
+    double* upload_buf = nullptr;  // particle upload staging (upload_cap particles, at most kUploadChunk)
+    long upload_cap = 0;
     // bound on the 2-norm of the rounding error of the FP32 residual r (valid with rhs_valid)
     double r_err = 0.0;
     // solver
@@ -584,7 +587,7 @@ extern "C" int pic_world_create(pic_world** out, int ni, int nj, int nk, const d
     w->gstride = std::max(kParts, node_blocks(nv));
     w->grid_nodes = (int)std::min<long long>(kParts, std::max<long long>(1, (nv + 255) / 256));
     w->grid_parts = w->sms * 8;
-    w->grid_push = w->sms * 3;
+    w->grid_push = w->sms * push_blocks_per_sm();
     w->grid_push_mcc = w->sms * 2;
     fill_grid_boxes(w);
     int rc = upload_kinds(w, true);
@@ -630,6 +633,7 @@ extern "C" int pic_world_destroy(pic_world* w) {
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (w->h_scal) cudaFreeHost(w->h_scal);
+    if (w->upload_buf) cudaFree(w->upload_buf);
     if (w->h_flag) cudaFreeHost(w->h_flag);
     for (auto& p : w->pending) {
         cudaEventDestroy(p.a);
@@ -858,6 +862,9 @@ extern "C" int pic_species_create(pic_world* w, const char* name, double mass, d
     double bound = weight_bound > 0 ? weight_bound : (double)capacity * (mpw0 > 0 ? mpw0 : 1.0) * 64.0;
     // largest power of two keeping every node sum below 2^62
     int ex = (int)std::floor(std::log2(std::ldexp(1.0, 62) / bound));
+    // a particle of the mean weight deposits at most 2^26 units (quantum 2^-26 of its weight), so
+    // the push keeps typical particles on its 32-bit run-sum path and its tile rarely carries
+    if (mpw0 > 0) ex = std::min(ex, (int)std::floor(std::log2(std::ldexp(1.0, 26) / mpw0)));
     if (ex > 60) ex = 60;
     if (ex < -60) ex = -60;
     s.scale = std::ldexp(1.0, ex);
@@ -876,28 +883,33 @@ extern "C" int pic_species_add_particles(pic_world* w, int sp, const double* pos
     if (n == 0) return PIC_OK;
     CU(cudaSetDevice(w->device));
     SpeciesHost& s = w->sp[sp];
-    std::vector<unsigned long long> idv(n);
-    for (long p = 0; p < n; p++) idv[p] = ids ? ids[p] : s.next_id + p;
-    if (!ids) s.next_id += n;
-    double *dp, *dv, *dw;
-    unsigned long long* di;
-    CU(cudaMallocAsync((void**)&dp, sizeof(double) * 3 * n, w->stream));
-    CU(cudaMallocAsync((void**)&dv, sizeof(double) * 3 * n, w->stream));
-    CU(cudaMallocAsync((void**)&dw, sizeof(double) * n, w->stream));
-    CU(cudaMallocAsync((void**)&di, sizeof(unsigned long long) * n, w->stream));
-    CU(cudaMemcpyAsync(dp, pos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, w->stream));
-    CU(cudaMemcpyAsync(dv, vel, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, w->stream));
-    CU(cudaMemcpyAsync(dw, wgt, sizeof(double) * n, cudaMemcpyHostToDevice, w->stream));
-    CU(cudaMemcpyAsync(di, idv.data(), sizeof(unsigned long long) * n, cudaMemcpyHostToDevice, w->stream));
-    {
-        Scope sc(w, "load", 5);
-        launch_from_abs(w->g, s.dev, dp, dv, dw, di, (int)n, rewind, (float)(s.charge / s.mass * 0.5 * w->dt), w->ef,
-                        w->stream);
+    // through a reusable device staging buffer, kUploadChunk particles at a time (pos, vel, w and
+    // ids in FP64 / u64); without ids the device numbers the particles from next_id on
+    const long want = std::min<long>(kUploadChunk, n);
+    if (w->upload_cap < want) {
+        if (w->upload_buf) CU(cudaFree(w->upload_buf));
+        w->upload_buf = nullptr;
+        w->upload_cap = 0;
+        CU(cudaMalloc(&w->upload_buf, (size_t)want * 8 * sizeof(double)));
+        w->upload_cap = want;
     }
-    cudaFreeAsync(dp, w->stream);
-    cudaFreeAsync(dv, w->stream);
-    cudaFreeAsync(dw, w->stream);
-    cudaFreeAsync(di, w->stream);
+    const long cap = w->upload_cap;
+    double* dp = w->upload_buf;
+    double* dv = dp + 3 * (size_t)cap;
+    double* dw = dv + 3 * (size_t)cap;
+    unsigned long long* di = reinterpret_cast<unsigned long long*>(dw + cap);
+    const unsigned long long id0 = s.next_id;
+    for (long a = 0; a < n; a += cap) {
+        const long m = std::min<long>(cap, n - a);
+        CU(cudaMemcpyAsync(dp, pos + 3 * a, sizeof(double) * 3 * m, cudaMemcpyHostToDevice, w->stream));
+        CU(cudaMemcpyAsync(dv, vel + 3 * a, sizeof(double) * 3 * m, cudaMemcpyHostToDevice, w->stream));
+        CU(cudaMemcpyAsync(dw, wgt + a, sizeof(double) * m, cudaMemcpyHostToDevice, w->stream));
+        if (ids) CU(cudaMemcpyAsync(di, ids + a, sizeof(unsigned long long) * m, cudaMemcpyHostToDevice, w->stream));
+        Scope sc(w, "load", 5);
+        launch_from_abs(w->g, s.dev, dp, dv, dw, ids ? di : nullptr, id0 + (unsigned long long)a, (int)m, rewind,
+                        (float)(s.charge / s.mass * 0.5 * w->dt), w->ef, w->stream);
+    }
+    if (!ids) s.next_id += n;
     CU(cudaStreamSynchronize(w->stream));
     return check_device_error(w);
 }

@@ -44,6 +44,7 @@ struct PushArgs {
 };
 
 // particles
+int push_blocks_per_sm();  // resident push CTAs per SM (the push grid is this times the SM count)
 void launch_push(const PushArgs& a, cudaStream_t s, int grid);
 // collisions of a.coll for the electrons a.sp as two passes (candidates, their collisions); the
 // push that follows runs without collisions.  cand holds up to the species capacity.
@@ -53,8 +54,8 @@ void launch_compact(SpeciesDev sp, cudaStream_t s, int grid);
 void launch_sort(const GridDev& g, SpeciesDev sp, float4* pos_alt, float4* vel_alt, unsigned long long* id_alt,
                  int* cell_count, int* cell_start, int* scan_aux, cudaStream_t s, int grid);
 void launch_from_abs(const GridDev& g, SpeciesDev sp, const double* pos, const double* vel, const double* w,
-                     const unsigned long long* id, int n, int rewind, float qm_half_dt, const float4* ef,
-                     cudaStream_t s);
+                     const unsigned long long* id, unsigned long long id0, int n, int rewind, float qm_half_dt,
+                     const float4* ef, cudaStream_t s);
 // particles first + p * stride, p < n, to absolute FP64 positions (null outputs are skipped)
 void launch_to_abs(const GridDev& g, SpeciesDev sp, double* pos, double* vel, double* w, unsigned long long* id,
                    int n, cudaStream_t s, long long first = 0, long long stride = 1);

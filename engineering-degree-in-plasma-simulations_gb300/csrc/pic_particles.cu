@@ -21,11 +21,12 @@ constexpr int kChunk = kThreads * kPPT;     // particles per chunk
 constexpr int kSeg = 256;                   // nodes per staged row segment
 constexpr int kMargin = 2;                  // deposit window starts this many nodes below the gather window
 constexpr int kHalfWin = (kSeg - kMargin - 2) / 2;  // staged base nodes either side of the chunk's anchor
-// shared memory of the push: the next chunk's particles (pos, vel, and ids with collisions),
-// the E rows (float4) and the fixed-point deposit tile (three 21-bit limb planes of 32-bit
-// counters), four rows of kSeg nodes each
+constexpr int kPushBlocksPerSM = 3;         // resident push CTAs per SM (80 registers, 56 KB shared)
+// shared memory of the push: the next chunk's particles (pos, vel), the E rows (float4) and the
+// fixed-point deposit tile (a low-word and a high-word plane of 32-bit counters), four rows of
+// kSeg nodes each
 constexpr size_t kPbufBytes = (size_t)kChunk * 2 * sizeof(float4);
-constexpr size_t kPushSmem = kPbufBytes + 4 * kSeg * sizeof(float4) + 3 * 4 * kSeg * sizeof(unsigned);
+constexpr size_t kPushSmem = kPbufBytes + 4 * kSeg * sizeof(float4) + 2 * 4 * kSeg * sizeof(unsigned);
 constexpr long long kWaitLimit = 1ll << 24;  // mbarrier polls before giving up
 
 // ------------------------------------------------------------------------------------
@@ -126,7 +127,7 @@ __device__ float3 new_vel_electron(const CollDev& c, float E, float3 u, float r_
 // ------------------------------------------------------------------------------------
 struct Tile {
     const float4* etile;  // staged E rows (row m at etile + m*kSeg), or nullptr
-    unsigned* dtile;      // deposit tile: limb l of row m at dtile + (l*4 + m)*kSeg, or nullptr
+    unsigned* dtile;      // deposit tile: low words of row m at dtile + m*kSeg, high words 4*kSeg on, or nullptr
     int lo;               // first base node of the staged window
     int span;             // base nodes lo .. lo + span are staged
     int off[4];           // node offsets of the four rows: 0, ni, ni*nj, ni*nj+ni
@@ -149,18 +150,16 @@ __device__ __forceinline__ float3 gather_e(const PushArgs& a, const Tile& t, int
     }
     float4 e000 = e0[0], e100 = e0[1], e010 = e0[r1], e110 = e0[r1 + 1];
     float4 e001 = e0[r2], e101 = e0[r2 + 1], e011 = e0[r3], e111 = e0[r3 + 1];
-    float wx1 = o.x, wx0 = 1.f - o.x, wy1 = o.y, wy0 = 1.f - o.y, wz1 = o.z, wz0 = 1.f - o.z;
-    float a00 = wx0 * wy0, a10 = wx1 * wy0, a01 = wx0 * wy1, a11 = wx1 * wy1;
-    float w000 = a00 * wz0, w100 = a10 * wz0, w010 = a01 * wz0, w110 = a11 * wz0;
-    float w001 = a00 * wz1, w101 = a10 * wz1, w011 = a01 * wz1, w111 = a11 * wz1;
-    float3 E;
-    E.x = e000.x * w000 + e100.x * w100 + e010.x * w010 + e110.x * w110 + e001.x * w001 + e101.x * w101 +
-          e011.x * w011 + e111.x * w111;
-    E.y = e000.y * w000 + e100.y * w100 + e010.y * w010 + e110.y * w110 + e001.y * w001 + e101.y * w101 +
-          e011.y * w011 + e111.y * w111;
-    E.z = e000.z * w000 + e100.z * w100 + e010.z * w010 + e110.z * w110 + e001.z * w001 + e101.z * w101 +
-          e011.z * w011 + e111.z * w111;
-    return E;
+    // trilinear weights as three nested linear interpolations (x, then y, then z)
+    auto lx = [&](const float4& p, const float4& q) {
+        return make_float3(fmaf(o.x, q.x - p.x, p.x), fmaf(o.x, q.y - p.y, p.y), fmaf(o.x, q.z - p.z, p.z));
+    };
+    const float3 c00 = lx(e000, e100), c10 = lx(e010, e110), c01 = lx(e001, e101), c11 = lx(e011, e111);
+    const float3 c0 = make_float3(fmaf(o.y, c10.x - c00.x, c00.x), fmaf(o.y, c10.y - c00.y, c00.y),
+                                  fmaf(o.y, c10.z - c00.z, c00.z));
+    const float3 c1 = make_float3(fmaf(o.y, c11.x - c01.x, c01.x), fmaf(o.y, c11.y - c01.y, c01.y),
+                                  fmaf(o.y, c11.z - c01.z, c01.z));
+    return make_float3(fmaf(o.z, c1.x - c0.x, c0.x), fmaf(o.z, c1.y - c0.y, c0.y), fmaf(o.z, c1.z - c0.z, c0.z));
 }
 
 // advance offsets by v dt/dx, move across cells, wrap periodic axes; returns the new packed
@@ -176,18 +175,10 @@ __device__ __forceinline__ int move_particle(const PushArgs& a, int i, int j, in
     o.x = fminf(ox - fx, kBelowOne);
     o.y = fminf(oy - fy, kBelowOne);
     o.z = fminf(oz - fz, kBelowOne);
-    if (g.periodic[0]) {
-        while (i < 0) i += g.ci;
-        while (i >= g.ci) i -= g.ci;
-    }
-    if (g.periodic[1]) {
-        while (j < 0) j += g.cj;
-        while (j >= g.cj) j -= g.cj;
-    }
-    if (g.periodic[2]) {
-        while (k < 0) k += g.ck;
-        while (k >= g.ck) k -= g.ck;
-    }
+    // periodic wrap: one unsigned compare per axis, the modulo only for a particle outside
+    if (g.periodic[0] && (unsigned)i >= (unsigned)g.ci) i = ((i % g.ci) + g.ci) % g.ci;
+    if (g.periodic[1] && (unsigned)j >= (unsigned)g.cj) j = ((j % g.cj) + g.cj) % g.cj;
+    if (g.periodic[2] && (unsigned)k >= (unsigned)g.ck) k = ((k % g.ck) + g.ck) % g.ck;
     if ((unsigned)i >= (unsigned)g.ci || (unsigned)j >= (unsigned)g.cj || (unsigned)k >= (unsigned)g.ck) return -1;
     if (g.zslab && slab_local_z(g, k) == g.zslab - 1) return -1;  // the cell between two instance slabs
     if (g.n_boxes) {
@@ -226,28 +217,65 @@ __device__ __forceinline__ void corner_values(float w, float3 o, float scale, Co
     for (int c8 = 0; c8 < 8; c8++) c.q[c8] = add ? c.q[c8] + v[c8] : v[c8];
 }
 
-// commits the corner sums of one cell (base node b): into the shared tile as 21-bit limbs with
-// native 32-bit shared atomics when the cell lies in the deposit window, else one 64-bit atomic
-// per corner in HBM.  Integer sums do not depend on the order of the additions, so rho is
-// bit-reproducible.  A tile slot receives at most one chunk's particles (1024), so a limb plane
-// cannot overflow 32 bits.
+// Deposit tile.  Each node slot keeps its 64-bit fixed-point sum as a low and a high 32-bit word
+// (native 32-bit shared atomics; 64-bit shared adds are compare-and-swap loops, four times slower
+// when measured here).  A value's low word is added with an atomic that returns the old word;
+// when the add wraps past 2^32 the carry goes to the high word together with the value's own
+// high word.  With the values light (below), the high word is touched only on a wrap, so a
+// corner costs one shared atomic.  A slot's sum over a chunk stays below 2^63 (the species'
+// fixed-point scale bounds its total weight), so the high word cannot overflow.  The tile is
+// committed to HBM with one 64-bit atomic per touched node; integer sums do not depend on the
+// order of the additions, so rho is bit-reproducible.
+__device__ __forceinline__ void tile_add(unsigned* dt, int x, unsigned long long v) {
+    const unsigned lo = (unsigned)v;
+    const unsigned old = atomicAdd(&dt[x], lo);
+    const unsigned hi = (unsigned)(v >> 32) + (old + lo < lo ? 1u : 0u);
+    if (hi) atomicAdd(&dt[4 * kSeg + x], hi);
+}
+// commits the corner sums of one cell (base node b): into the tile when the cell lies in the
+// deposit window, else one 64-bit atomic per corner in HBM
 __device__ __forceinline__ void commit_corners(const PushArgs& a, const Tile& t, int b, const Corners& c) {
     int loc = b - (t.lo - kMargin);
     if (t.dtile && loc >= 0 && loc < kSeg - 1) {
 #pragma unroll
-        for (int c8 = 0; c8 < 8; c8++) {
-            unsigned long long v = c.q[c8];
-            if (!v) continue;
-            int x = ((c8 >> 1) * kSeg) + loc + (c8 & 1);
-            atomicAdd(&t.dtile[x], (unsigned)(v & 0x1FFFFFull));
-            unsigned l1 = (unsigned)((v >> 21) & 0x1FFFFFull), l2 = (unsigned)(v >> 42);
-            if (l1) atomicAdd(&t.dtile[4 * kSeg + x], l1);
-            if (l2) atomicAdd(&t.dtile[8 * kSeg + x], l2);
-        }
+        for (int c8 = 0; c8 < 8; c8++) tile_add(t.dtile, ((c8 >> 1) * kSeg) + loc + (c8 & 1), c.q[c8]);
     } else {
 #pragma unroll
         for (int c8 = 0; c8 < 8; c8++)
             if (c.q[c8]) atomicAdd(&a.sp.acc[b + t.off[c8 >> 1] + (c8 & 1)], c.q[c8]);
+    }
+}
+// A light particle (w * scale below kLightMax, just under 2^30: the species scale puts a particle
+// of the mean weight at 2^26 at most) has corner values below 2^30, so the run of a thread's four
+// particles sums below 2^32 and the run is kept in 32-bit registers.  The values are the same
+// integers as the 64-bit path gives (both round x < 2^32 with one 32-bit conversion).
+constexpr float kLightMax = 1.07e9f;
+struct Corners32 {
+    unsigned q[8];
+};
+__device__ __forceinline__ void corner_values32(float s, float3 o, Corners32& c, bool add) {
+    float wx1 = o.x, wx0 = 1.f - o.x, wy1 = o.y, wy0 = 1.f - o.y, wz1 = o.z, wz0 = 1.f - o.z;
+    float s00 = s * wx0 * wy0, s10 = s * wx1 * wy0, s01 = s * wx0 * wy1, s11 = s * wx1 * wy1;
+    const unsigned v[8] = {__float2uint_rn(s00 * wz0), __float2uint_rn(s10 * wz0), __float2uint_rn(s01 * wz0),
+                           __float2uint_rn(s11 * wz0), __float2uint_rn(s00 * wz1), __float2uint_rn(s10 * wz1),
+                           __float2uint_rn(s01 * wz1), __float2uint_rn(s11 * wz1)};
+#pragma unroll
+    for (int c8 = 0; c8 < 8; c8++) c.q[c8] = add ? c.q[c8] + v[c8] : v[c8];
+}
+// commits a light run: the eight adds are issued before any returned word is examined
+__device__ __forceinline__ void commit_run32(const PushArgs& a, const Tile& t, int b, const Corners32& c) {
+    int loc = b - (t.lo - kMargin);
+    if (t.dtile && loc >= 0 && loc < kSeg - 1) {
+        unsigned old[8];
+#pragma unroll
+        for (int c8 = 0; c8 < 8; c8++) old[c8] = atomicAdd(&t.dtile[((c8 >> 1) * kSeg) + loc + (c8 & 1)], c.q[c8]);
+#pragma unroll
+        for (int c8 = 0; c8 < 8; c8++)
+            if (old[c8] + c.q[c8] < c.q[c8]) atomicAdd(&t.dtile[4 * kSeg + ((c8 >> 1) * kSeg) + loc + (c8 & 1)], 1u);
+    } else {
+#pragma unroll
+        for (int c8 = 0; c8 < 8; c8++)
+            if (c.q[c8]) atomicAdd(&a.sp.acc[b + t.off[c8 >> 1] + (c8 & 1)], (unsigned long long)c.q[c8]);
     }
 }
 
@@ -340,8 +368,9 @@ __device__ __noinline__ Collision collide_candidate(const CollDev& cd, unsigned 
 //   next chunk's particle arrays are bulk-copied (TMA) into shared memory while the current
 //   chunk is processed.  For each chunk the four node rows around the base node of its middle
 //   particle, [lo + off_m, lo + off_m + L), are bulk-copied into shared memory; the gather reads
-//   them there, and the deposit accumulates into a shared 64-bit fixed-point tile committed to
-//   HBM with one atomic per touched node.  Particles outside the window use HBM directly.
+//   them there, and the deposit accumulates into a shared 64-bit fixed-point tile (two 32-bit
+//   word planes) committed to HBM with one atomic per touched node.  Particles outside the window
+//   use HBM directly.
 // ------------------------------------------------------------------------------------
 // bulk copy of one full chunk's particle arrays into the staging buffer
 __device__ __forceinline__ void issue_chunk(const SpeciesDev& sp, int base, float4* ppos, float4* pvel,
@@ -353,7 +382,7 @@ __device__ __forceinline__ void issue_chunk(const SpeciesDev& sp, int base, floa
     bulk_g2s(pvel, sp.vel + base, b16, bar);
 }
 
-__global__ void __launch_bounds__(kThreads, 3) k_push(PushArgs a) {
+__global__ void __launch_bounds__(kThreads, kPushBlocksPerSM) k_push(PushArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
     float4* ppos = reinterpret_cast<float4*>(smem);
     float4* pvel = ppos + kChunk;
@@ -411,19 +440,35 @@ __global__ void __launch_bounds__(kThreads, 3) k_push(PushArgs a) {
             }
             __syncthreads();
         }
+        // A thread owns particles tid*4 .. tid*4+3.  Read in place, the eight threads of a
+        // quarter-warp would hit the same banks four times over (64-byte stride); reading them in
+        // an order rotated by (lane/2) mod 4 spreads the reads over all 32 banks, and two
+        // conditional register rotations restore the order.
         float4 P[kPPT], V[kPPT];
-        int bn[kPPT];
+        {
+            const int rot = (lane >> 1) & 3;
 #pragma unroll
-        for (int q = 0; q < kPPT; q++) {
-            const int x = tid * kPPT + q;
-            bn[q] = -1;
-            if (x < nin) {
+            for (int q = 0; q < kPPT; q++) {
+                const int x = tid * kPPT + ((q + rot) & 3);
                 P[q] = ppos[x];
                 V[q] = pvel[x];
-                const int c = __float_as_int(P[q].w);
-                if (c >= 0) bn[q] = cell_base(g, c);
+            }
+            if (rot & 1) {  // U[k] = T[k - 1]
+                const float4 p3 = P[3], v3 = V[3];
+                P[3] = P[2], P[2] = P[1], P[1] = P[0], P[0] = p3;
+                V[3] = V[2], V[2] = V[1], V[1] = V[0], V[0] = v3;
+            }
+            if (rot & 2) {  // P[k] = U[k - 2]
+                float4 t0 = P[0], t1 = P[1];
+                P[0] = P[2], P[1] = P[3], P[2] = t0, P[3] = t1;
+                t0 = V[0], t1 = V[1];
+                V[0] = V[2], V[1] = V[3], V[2] = t0, V[3] = t1;
             }
         }
+        // particles past the end of a partial chunk are marked absent
+#pragma unroll
+        for (int q = 0; q < kPPT; q++)
+            if (tid * kPPT + q >= nin) P[q].w = __int_as_float(-1);
         // ---- window: +-kHalfWin base nodes around the base node of the chunk's middle particle
         int lo = 0, hi = -1;
         {
@@ -457,7 +502,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_push(PushArgs a) {
         t.dtile = nullptr;
         if (use_tile) {
             if (a.deposit)
-                for (int x = tid; x < 12 * kSeg; x += kThreads) dtile[x] = 0u;
+                for (int x = tid; x < 8 * kSeg; x += kThreads) dtile[x] = 0u;
             if (!mbar_wait_bounded(&bar_e, phase_e)) atomicExch(&s_fail, 1);
             phase_e ^= 1u;
             __syncthreads();
@@ -474,21 +519,21 @@ __global__ void __launch_bounds__(kThreads, 3) k_push(PushArgs a) {
         }
 
         unsigned dead_mask[kPPT];
-        Corners run;        // deposit sums of the current cell run
+        Corners32 run;      // deposit sums of the current run of light particles
         int run_cell = -1;  // packed cell of the run, -1: none
 #pragma unroll
         for (int q = 0; q < kPPT; q++) {
             const int p = base + tid * kPPT + q;
             dead_mask[q] = 0;
-            if (bn[q] < 0) continue;
             int c = __float_as_int(P[q].w);
+            if (c < 0) continue;
             int i, j, k;
             cell_ijk(g, c, i, j, k);
             float3 o = make_float3(P[q].x, P[q].y, P[q].z);
             float3 v = make_float3(V[q].x, V[q].y, V[q].z);
             const float w = V[q].w;
             // leapfrog push (Species.cpp:369-373)
-            float3 E = gather_e(a, t, bn[q], o);
+            float3 E = gather_e(a, t, cell_base(g, c), o);
             v.x += a.qm_dt * E.x;
             v.y += a.qm_dt * E.y;
             v.z += a.qm_dt * E.z;
@@ -497,17 +542,24 @@ __global__ void __launch_bounds__(kThreads, 3) k_push(PushArgs a) {
             a.sp.vel[p] = make_float4(v.x, v.y, v.z, w);
             if (newc >= 0) {
                 if (a.deposit) {
-                    if (newc != run_cell && run_cell >= 0)
-                        commit_corners(a, t, cell_base(g, run_cell), run);
-                    corner_values(w, o, a.dep_scale, run, newc == run_cell);
-                    run_cell = newc;
+                    const float s = w * a.dep_scale;
+                    if (s < kLightMax) {
+                        if (newc != run_cell && run_cell >= 0)
+                            commit_run32(a, t, cell_base(g, run_cell), run);
+                        corner_values32(s, o, run, newc == run_cell);
+                        run_cell = newc;
+                    } else {
+                        Corners hc;
+                        corner_values(w, o, a.dep_scale, hc, false);
+                        commit_corners(a, t, cell_base(g, newc), hc);
+                    }
                 }
             } else {
                 dead_mask[q] = 1;
             }
         }
         if (run_cell >= 0)
-            commit_corners(a, t, cell_base(g, run_cell), run);
+            commit_run32(a, t, cell_base(g, run_cell), run);
         // warp-aggregated record of the particles that left the domain
 #pragma unroll
         for (int q = 0; q < kPPT; q++) {
@@ -525,8 +577,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_push(PushArgs a) {
             // received a deposit are nonzero, and those are nodes of the grid)
             const int wlo = lo - kMargin;
             for (int x = tid; x < 4 * kSeg; x += kThreads) {
-                unsigned long long v = (unsigned long long)dtile[x] + ((unsigned long long)dtile[4 * kSeg + x] << 21) +
-                                       ((unsigned long long)dtile[8 * kSeg + x] << 42);
+                unsigned long long v = (unsigned long long)dtile[x] + ((unsigned long long)dtile[4 * kSeg + x] << 32);
                 if (v) atomicAdd(&a.sp.acc[wlo + t.off[x / kSeg] + (x % kSeg)], v);
             }
         }
@@ -635,12 +686,18 @@ void launch_mcc(const PushArgs& a, int* cand, int* ncand, cudaStream_t s, int sm
     k_mcc_collide<<<sms * 4, 128, 0, s>>>(a, cand, ncand);
 }
 
-void launch_push(const PushArgs& a, cudaStream_t s, int grid) {
-    static bool attr = false;
-    if (!attr) {
+int push_blocks_per_sm() {
+    static int nb = 0;
+    if (!nb) {
         cudaFuncSetAttribute(k_push, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPushSmem);
-        attr = true;
+        cudaFuncSetAttribute(k_push, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_push, kThreads, kPushSmem) != cudaSuccess || nb < 1)
+            nb = 1;
     }
+    return nb;
+}
+void launch_push(const PushArgs& a, cudaStream_t s, int grid) {
+    push_blocks_per_sm();
     k_push<<<grid, kThreads, kPushSmem, s>>>(a);
 }
 
@@ -805,8 +862,10 @@ void launch_sort(const GridDev& g, SpeciesDev sp, float4* pos_alt, float4* vel_a
 // ------------------------------------------------------------------------------------
 // host <-> device conversion (Species::addParticle semantics when rewind is set)
 // ------------------------------------------------------------------------------------
+// id == nullptr: particle p gets id id0 + p
 __global__ void k_from_abs(GridDev g, SpeciesDev sp, const double* pos, const double* vel, const double* w,
-                           const unsigned long long* id, int n, int rewind, float qm_half_dt, const float4* ef) {
+                           const unsigned long long* id, unsigned long long id0, int n, int rewind, float qm_half_dt,
+                           const float4* ef) {
     int n0 = sp.counts[0];
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
         int dst = n0 + p;
@@ -863,7 +922,7 @@ __global__ void k_from_abs(GridDev g, SpeciesDev sp, const double* pos, const do
         }
         sp.pos[dst] = make_float4(o[0], o[1], o[2], __int_as_float(cell));
         sp.vel[dst] = make_float4(v.x, v.y, v.z, (float)w[p]);
-        sp.id[dst] = id[p];
+        sp.id[dst] = id ? id[p] : id0 + (unsigned long long)p;
         if (cell < 0) sp.dead[atomicAdd(&sp.counts[2], 1)] = dst;
     }
 }
@@ -876,12 +935,12 @@ __global__ void k_from_abs_count(SpeciesDev sp, int n, unsigned* err) {
     sp.counts[0] = nn;
 }
 void launch_from_abs(const GridDev& g, SpeciesDev sp, const double* pos, const double* vel, const double* w,
-                     const unsigned long long* id, int n, int rewind, float qm_half_dt, const float4* ef,
-                     cudaStream_t s) {
+                     const unsigned long long* id, unsigned long long id0, int n, int rewind, float qm_half_dt,
+                     const float4* ef, cudaStream_t s) {
     int grid = (n + 255) / 256;
     if (grid > 4096) grid = 4096;
     if (grid < 1) grid = 1;
-    k_from_abs<<<grid, 256, 0, s>>>(g, sp, pos, vel, w, id, n, rewind, qm_half_dt, ef);
+    k_from_abs<<<grid, 256, 0, s>>>(g, sp, pos, vel, w, id, id0, n, rewind, qm_half_dt, ef);
     k_from_abs_count<<<1, 1, 0, s>>>(sp, n, nullptr);
     launch_compact(sp, s, 256);
 }
