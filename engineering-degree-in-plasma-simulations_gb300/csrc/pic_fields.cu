@@ -280,7 +280,11 @@ __global__ void __launch_bounds__(256) k_residual(GridDev g, const float2* __res
         const int n0 = q << 2;
         int i0, j, k;
         node_ijk(g, n0, i0, j, k);
-        if (rows4 && i0 >= 1 && i0 + 4 <= g.ni - 1) {
+        if (rows4) {
+            // every group of a row, its ends included: see spmv_group for the x neighbours at the ends
+            const bool xend = i0 + 4 == g.ni, wrapx = g.periodic[0] != 0;
+            const int ixm = i0 > 0 ? n0 - 1 : (wrapx ? n0 + g.ni - 2 : n0);
+            const int ixp = xend ? (wrapx ? n0 - i0 : n0 + 3) : n0 + 4;
             int jm, jp, km, kp;
             row_neighbours(g, j, k, jm, jp, km, kp);
             const int rowm = (k * g.nj + jm) * g.ni + i0, rowp = (k * g.nj + jp) * g.ni + i0;
@@ -301,7 +305,7 @@ __global__ void __launch_bounds__(256) k_residual(GridDev g, const float2* __res
             load4(phi_in + rowp, Yp);
             load4(phi_in + plm, Zm);
             load4(phi_in + plp, Zp);
-            const float2 xm = phi_in[n0 - 1], xp = phi_in[n0 + 4];
+            const float2 xm = phi_in[ixm], xp = phi_in[ixp];
             float E[4] = {0.f, 0.f, 0.f, 0.f}, EYm[4] = {0.f, 0.f, 0.f, 0.f}, EYp[4] = {0.f, 0.f, 0.f, 0.f},
                   EZm[4] = {0.f, 0.f, 0.f, 0.f}, EZp[4] = {0.f, 0.f, 0.f, 0.f}, exm = 0.f, exp_ = 0.f;
             if (ae) {
@@ -317,8 +321,8 @@ __global__ void __launch_bounds__(256) k_residual(GridDev g, const float2* __res
                 ld(e + rowp, EYp);
                 ld(e + plm, EZm);
                 ld(e + plp, EZp);
-                exm = e[n0 - 1];
-                exp_ = e[n0 + 4];
+                exm = e[ixm];
+                exp_ = e[ixp];
             }
             const float4 h4 = *reinterpret_cast<const float4*>(rho + n0);
             const float hv[4] = {h4.x, h4.y, h4.z, h4.w};
@@ -330,8 +334,9 @@ __global__ void __launch_bounds__(256) k_residual(GridDev g, const float2* __res
                 bf[c] = 0.f;
                 pv[c] = P[c];
                 if ((kv[c] & 3) != kFree) continue;
-                const float2 pn[6] = {c == 0 ? xm : P[c - 1], c == 3 ? xp : P[c + 1], Ym[c], Yp[c], Zm[c], Zp[c]};
-                const float en[6] = {c == 0 ? exm : E[c - 1], c == 3 ? exp_ : E[c + 1], EYm[c], EYp[c], EZm[c], EZp[c]};
+                const bool wr = c == 3 || (c == 2 && xend && wrapx);
+                const float2 pn[6] = {c == 0 ? xm : P[c - 1], wr ? xp : P[c + 1], Ym[c], Yp[c], Zm[c], Zp[c]};
+                const float en[6] = {c == 0 ? exm : E[c - 1], wr ? exp_ : E[c + 1], EYm[c], EYp[c], EZm[c], EZp[c]};
                 float b;
                 residual_node(K, kv[c], P[c], pn, E[c], en, hv[c], ae, rv[c], b, bf[c], pv[c]);
                 acc_r += rv[c] * rv[c];

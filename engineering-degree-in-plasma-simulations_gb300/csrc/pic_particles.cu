@@ -599,15 +599,30 @@ __global__ void __launch_bounds__(256) k_mcc_candidates(PushArgs a, int* cand, i
     const CollDev& cd = a.coll;
     const int n = a.sp.counts[0];
     const int lane = threadIdx.x & 31;
-    for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
-        const int p = base + threadIdx.x;
-        const bool is_cand = p < n && cand_draw(a.sp.id[p], cd.step, cd.key) < cd.cand_max;
-        const unsigned m = __ballot_sync(0xffffffffu, is_cand);
-        if (m) {
-            int b0 = 0;
-            if (lane == __ffs(m) - 1) b0 = atomicAdd(ncand, __popc(m));
-            b0 = __shfl_sync(0xffffffffu, b0, __ffs(m) - 1);
-            if (is_cand) cand[b0 + __popc(m & ((1u << lane) - 1u))] = p;
+    const int ng = (n + 3) >> 2;  // four consecutive ids per thread, two 16-byte loads
+    for (int base = blockIdx.x * blockDim.x; base < ng; base += gridDim.x * blockDim.x) {
+        const int gq = base + threadIdx.x;
+        const int p0 = gq << 2;
+        unsigned long long id[4] = {0ull, 0ull, 0ull, 0ull};
+        if (p0 + 4 <= n) {
+            const ulonglong2 x = reinterpret_cast<const ulonglong2*>(a.sp.id)[2 * gq];
+            const ulonglong2 y = reinterpret_cast<const ulonglong2*>(a.sp.id)[2 * gq + 1];
+            id[0] = x.x, id[1] = x.y, id[2] = y.x, id[3] = y.y;
+        } else {
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                if (p0 + q < n) id[q] = a.sp.id[p0 + q];
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const bool is_cand = p0 + q < n && cand_draw(id[q], cd.step, cd.key) < cd.cand_max;
+            const unsigned m = __ballot_sync(0xffffffffu, is_cand);
+            if (m) {
+                int b0 = 0;
+                if (lane == __ffs(m) - 1) b0 = atomicAdd(ncand, __popc(m));
+                b0 = __shfl_sync(0xffffffffu, b0, __ffs(m) - 1);
+                if (is_cand) cand[b0 + __popc(m & ((1u << lane) - 1u))] = p0 + q;
+            }
         }
     }
 }

@@ -142,7 +142,10 @@ __device__ __forceinline__ void spmv_group(const GridDev& g, int n0, const float
     int i0, j, k;
     node_ijk(g, n0, i0, j, k);
     const float c3[3] = {g.inv_dx[0] * g.inv_dx[0], g.inv_dx[1] * g.inv_dx[1], g.inv_dx[2] * g.inv_dx[2]};
-    if ((g.ni & 3) == 0 && i0 >= 1 && i0 + 4 <= g.ni - 1) {
+    // rows of a multiple of four nodes: every group, the row ends included (a row-end node is
+    // never FREE except the first node of a periodic row, whose -x neighbour is node ni-2; on a
+    // periodic row node ni-2 takes node 0, not the copy plane ni-1, as its +x neighbour)
+    if ((g.ni & 3) == 0) {
         const int jm = g.periodic[1] ? wrap_m(j, g.nj, 1) : max(j - 1, 0);
         const int jp = g.periodic[1] ? wrap_p(j, g.nj, 1) : min(j + 1, g.nj - 1);
         const int km = g.periodic[2] ? wrap_m(k, g.nk, 1) : max(k - 1, 0);
@@ -162,7 +165,10 @@ __device__ __forceinline__ void spmv_group(const GridDev& g, int n0, const float
         dv4(n0, C);
 #pragma unroll
         for (int m = 0; m < 4; m++) dv4(off[m], N[m]);
-        const float xm = z[n0 - 1] + fb * d_in[n0 - 1], xp = z[n0 + 4] + fb * d_in[n0 + 4];
+        const bool xend = i0 + 4 == g.ni, wrapx = g.periodic[0] != 0;
+        const int ixm = i0 > 0 ? n0 - 1 : (wrapx ? n0 + g.ni - 2 : n0);
+        const int ixp = xend ? (wrapx ? n0 - i0 : n0 + 3) : n0 + 4;
+        const float xm = z[ixm] + fb * d_in[ixm], xp = z[ixp] + fb * d_in[ixp];
         const ushort4 k4 = *reinterpret_cast<const ushort4*>(kind + n0);
         const unsigned short kv[4] = {k4.x, k4.y, k4.z, k4.w};
         float dvo[4], qv[4];
@@ -171,7 +177,8 @@ __device__ __forceinline__ void spmv_group(const GridDev& g, int n0, const float
             dvo[c] = 0.f;
             qv[c] = 0.f;
             if ((kv[c] & 3) != kFree) continue;
-            const float nb[6] = {c == 0 ? xm : C[c - 1], c == 3 ? xp : C[c + 1], N[0][c], N[1][c], N[2][c], N[3][c]};
+            const float right = c == 3 ? xp : ((c == 2 && xend && wrapx) ? xp : C[c + 1]);
+            const float nb[6] = {c == 0 ? xm : C[c - 1], right, N[0][c], N[1][c], N[2][c], N[3][c]};
             float dg = 0.f, o = 0.f;
 #pragma unroll
             for (int d = 0; d < 6; d++) {
