@@ -22,6 +22,7 @@ using namespace pic;
 
 constexpr double kFp32Unit = 0x1p-24;  // unit roundoff of FP32 round-to-nearest
 constexpr long kUploadChunk = 1l << 22;  // particles per upload staging round (256 MB)
+constexpr long kSortMovedFraction = 50;   // re-sort a species when 2 % of it left cell order
 
 namespace {
 
@@ -1243,6 +1244,7 @@ int sort_species(pic_world* w, int sp) {
     std::swap(s.dev.pos, s.pos2);
     std::swap(s.dev.vel, s.vel2);
     std::swap(s.dev.id, s.id2);
+    CU(cudaMemsetAsync(s.dev.counts + 5, 0, sizeof(int), w->stream));  // in cell order again
     return PIC_OK;
 }
 }  // namespace
@@ -1951,8 +1953,17 @@ extern "C" int pic_step(pic_world* w) {
         rc = pic_solver_compute_ef(w);
         if (rc) return rc;
     }
-    if (w->sort_every > 0 && ts % w->sort_every == 0)
-        for (int s = 0; s < (int)w->sp.size(); s++) sort_species(w, s);
+    if (w->sort_every > 0 && ts % w->sort_every == 0) {
+        // a species is re-sorted when at least 1/kSortMovedFraction of its particles changed cell
+        // or were appended since its last sort (slow ions stay in order for many periods)
+        const int ns = (int)w->sp.size();
+        std::vector<int> cnt(8 * ns);
+        for (int s = 0; s < ns; s++)
+            CU(cudaMemcpyAsync(&cnt[8 * s], w->sp[s].dev.counts, sizeof(int) * 8, cudaMemcpyDeviceToHost, w->stream));
+        CU(cudaStreamSynchronize(w->stream));
+        for (int s = 0; s < ns; s++)
+            if ((long)cnt[8 * s + 5] * kSortMovedFraction >= (long)cnt[8 * s] && cnt[8 * s + 5] > 0) sort_species(w, s);
+    }
     CU(cudaGetLastError());
     return PIC_OK;
 }

@@ -76,7 +76,8 @@ struct SpeciesDev {
     float4* pos;
     float4* vel;
     unsigned long long* id;
-    int* counts;  // [0] n, [1] pending appends, [2] dead, [3] holes, [4] movers
+    int* counts;  // [0] n, [1] pending appends, [2] dead, [3] holes, [4] movers,
+                  // [5] particles moved to another cell or appended since the last sort
     int* dead;    // dead particle indices of the last push
     int* holes;   // compaction scratch
     unsigned long long* acc;  // fixed-point number-density accumulators, one per node

@@ -413,6 +413,7 @@ __global__ void __launch_bounds__(kThreads, kPushBlocksPerSM) k_push(PushArgs a)
     // last base node whose eight corners exist: the window must not copy past the node array
     const int max_base = g.nv - 2 - t.off[3];
 
+    int moved = 0;  // particles of this thread that changed cell or left, over all its chunks
     int ch = blockIdx.x;
     bool pending = false;  // a particle bulk copy into the staging buffer is in flight
     if (ch < nchunks && (ch + 1) * kChunk <= n && tid == 0) issue_chunk(a.sp, ch * kChunk, ppos, pvel, &bar_p);
@@ -538,6 +539,7 @@ __global__ void __launch_bounds__(kThreads, kPushBlocksPerSM) k_push(PushArgs a)
             v.y += a.qm_dt * E.y;
             v.z += a.qm_dt * E.z;
             const int newc = move_particle(a, i, j, k, o, v);
+            moved += newc != c;
             a.sp.pos[p] = make_float4(o.x, o.y, o.z, __int_as_float(newc));
             a.sp.vel[p] = make_float4(v.x, v.y, v.z, w);
             if (newc >= 0) {
@@ -583,6 +585,15 @@ __global__ void __launch_bounds__(kThreads, kPushBlocksPerSM) k_push(PushArgs a)
         }
         __syncthreads();
     }
+    // cell-order bookkeeping for the sort policy: one global atomic per CTA (a per-warp atomic on
+    // one address serialises hundreds of thousands of updates per launch)
+    __shared__ int s_moved;
+    if (tid == 0) s_moved = 0;
+    __syncthreads();
+    const int wm = __reduce_add_sync(0xffffffffu, moved);
+    if (lane == 0 && wm) atomicAdd(&s_moved, wm);
+    __syncthreads();
+    if (tid == 0 && s_moved) atomicAdd(&a.sp.counts[5], s_moved);
 }
 
 // ------------------------------------------------------------------------------------
@@ -728,6 +739,7 @@ __global__ void k_commit_appends(SpeciesDev sp, unsigned* err) {
     }
     sp.counts[0] = nn;
     sp.counts[1] = 0;
+    sp.counts[5] += nn - n;  // appended particles are out of cell order
 }
 void launch_commit_appends(SpeciesDev sp, unsigned* err, cudaStream_t s) { k_commit_appends<<<1, 1, 0, s>>>(sp, err); }
 

@@ -200,7 +200,8 @@ int pic_mcc_stats(pic_world* w, uint64_t* out);
 /* ---- the step loop (ch4/v3/src/main.cpp:177-286) -------------------------------------- */
 
 /* Loop options.  solve_each_step: Poisson + E every step (v3 comments it out, main.cpp:260-261;
- * ch2 solves every step).  sort_every: counting sort by cell every k steps.  subcycle[sp]:
+ * ch2 solves every step).  sort_every: every k steps, a counting sort by cell of each species of
+ * which at least 2 % of the particles changed cell or were appended since its last sort.  subcycle[sp]:
  * push species sp every k steps with k*dt (main.cpp:211-238); 1 = every step.
  * merge_every/merge_after/merge_min: merging (main.cpp:179: ts > 250 && ts % 50 == 0). */
 int pic_loop_configure(pic_world* w, int solve_each_step, int sort_every, const int* subcycle, int merge_every,
