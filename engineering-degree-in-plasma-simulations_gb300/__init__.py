@@ -61,6 +61,8 @@ def library():
         "pic_world_advance_time": [vp, vp],
         "pic_world_get_ts": [vp, vp],
         "pic_world_get_time": [vp, vp],
+        "pic_source_create": [vp, i, d, d, d, i, u64, vp],
+        "pic_source_sample": [vp, i],
         "pic_world_potential_energy": [vp, vp],
         "pic_species_sample_particles": [vp, i, l, vp, vp, vp],
         "pic_world_set_boundaries": [vp, vp, vp, vp],
@@ -442,6 +444,41 @@ class Species:
 
     def getKE(self):
         return self.sums()[4]
+
+
+FACES = {"x-": 0, "x+": 1, "y-": 2, "y+": 3, "z-": 4, "z+": 5,
+         "-x": 0, "+x": 1, "-y": 2, "+y": 3, "-z": 4, "+z": 5}  # inletName2Index, World.cpp:369-390
+
+
+class ColdBeamSource:
+    """ColdBeamSource(species, world, v_drift, den, inlet_face) -- ch4/v3/src/Source.h:42-52.
+
+    Each step (pic_step, or sample()) injects (int)(den v_drift A dt / mpw0 + u) particles on the
+    inlet face with velocity v_drift along the inward normal; the face becomes Dirichlet at 0 V."""
+
+    T = 0.0
+
+    def __init__(self, species, world, v_drift, den, inlet_face="-z", seed=1):
+        face = FACES.get(str(inlet_face).lower())
+        if face is None:
+            raise ValueError("Passed wrong face name.")
+        self.world = world
+        sid = C.c_int()
+        _check(world._L.pic_source_create(world._h, species.id, float(v_drift), float(den), float(self.T), face,
+                                          int(seed), C.byref(sid)))
+        self.id = sid.value
+
+    def sample(self):
+        _check(self.world._L.pic_source_sample(self.world._h, self.id))
+
+
+class WarmBeamSource(ColdBeamSource):
+    """WarmBeamSource(species, world, v_drift, den, T, inlet_face) -- ch4/v3/src/Source.h:55-66:
+    the cold beam plus a Species::sampleV3th(T) thermal velocity."""
+
+    def __init__(self, species, world, v_drift, den, T, inlet_face="-z", seed=1):
+        self.T = float(T)
+        super().__init__(species, world, v_drift, den, inlet_face, seed)
 
 
 class PotentialSolver:

@@ -110,6 +110,13 @@ struct pic_world {
         double c[3], s[3], phi;
     };
     std::vector<Box> boxes;
+    // beam sources (ColdBeamSource / WarmBeamSource, Source.h:13-68)
+    struct Source {
+        int sp, face;
+        double v_drift, den, T;
+        uint2 key;
+    };
+    std::vector<Source> sources;
     // stacked independent instances along z (0: one instance): electrode potentials per slab,
     // neutral density per slab and the candidate probabilities derived from it
     int nslabs = 0;
@@ -878,14 +885,9 @@ extern "C" int pic_species_create(pic_world* w, const char* name, double mass, d
     return PIC_OK;
 }
 
-extern "C" int pic_species_add_particles(pic_world* w, int sp, const double* pos, const double* vel,
-                                         const double* wgt, const uint64_t* ids, long n, int rewind) {
-    if (!valid_sp(w, sp) || (n > 0 && (!pos || !vel || !wgt))) return fail(PIC_ERR_ARG, "bad species or arrays");
-    if (n == 0) return PIC_OK;
-    CU(cudaSetDevice(w->device));
-    SpeciesHost& s = w->sp[sp];
-    // through a reusable device staging buffer, kUploadChunk particles at a time (pos, vel, w and
-    // ids in FP64 / u64); without ids the device numbers the particles from next_id on
+namespace {
+// the particle upload staging buffer holds at least min(n, kUploadChunk) particles
+int ensure_upload(pic_world* w, long n) {
     const long want = std::min<long>(kUploadChunk, n);
     if (w->upload_cap < want) {
         if (w->upload_buf) CU(cudaFree(w->upload_buf));
@@ -894,6 +896,20 @@ extern "C" int pic_species_add_particles(pic_world* w, int sp, const double* pos
         CU(cudaMalloc(&w->upload_buf, (size_t)want * 8 * sizeof(double)));
         w->upload_cap = want;
     }
+    return PIC_OK;
+}
+}  // namespace
+
+extern "C" int pic_species_add_particles(pic_world* w, int sp, const double* pos, const double* vel,
+                                         const double* wgt, const uint64_t* ids, long n, int rewind) {
+    if (!valid_sp(w, sp) || (n > 0 && (!pos || !vel || !wgt))) return fail(PIC_ERR_ARG, "bad species or arrays");
+    if (n == 0) return PIC_OK;
+    CU(cudaSetDevice(w->device));
+    SpeciesHost& s = w->sp[sp];
+    // through a reusable device staging buffer, kUploadChunk particles at a time (pos, vel, w and
+    // ids in FP64 / u64); without ids the device numbers the particles from next_id on
+    int urc = ensure_upload(w, n);
+    if (urc) return urc;
     const long cap = w->upload_cap;
     double* dp = w->upload_buf;
     double* dv = dp + 3 * (size_t)cap;
@@ -1758,6 +1774,79 @@ double sigv_majorant(const std::vector<double>& E, const std::vector<double>& S,
 }
 }  // namespace
 
+// =====================================================================================
+// Sources (Source.cpp)
+// =====================================================================================
+extern "C" int pic_source_create(pic_world* w, int sp, double v_drift, double den, double T, int face,
+                                 uint64_t seed, int* source_id) {
+    if (!valid_sp(w, sp) || !source_id || face < 0 || face > 5 || !(v_drift >= 0) || !(den >= 0) || !(T >= 0))
+        return fail(PIC_ERR_ARG, "bad source arguments");
+    if (w->periodic[face >> 1]) return fail(PIC_ERR_ARG, "an inlet face cannot lie on a periodic axis");
+    if (!(w->sp[sp].mpw0 > 0)) return fail(PIC_ERR_ARG, "a source needs a species with a positive mpw0");
+    CU(cudaSetDevice(w->device));
+    pic_world::Source src;
+    src.sp = sp;
+    src.face = face;
+    src.v_drift = v_drift;
+    src.den = den;
+    src.T = T;
+    src.key = make_uint2((unsigned)seed, (unsigned)(seed >> 32));
+    w->sources.push_back(src);
+    *source_id = (int)w->sources.size() - 1;
+    // World::addInlet(face) (World.cpp:206-260): the inlet face becomes Dirichlet at 0 V
+    w->face_mode[face] = 1;
+    w->face_phi[face] = 0.0;
+    fill_grid_boxes(w);
+    return upload_kinds(w, false);
+}
+
+extern "C" int pic_source_sample(pic_world* w, int source_id) {
+    if (!w || source_id < 0 || source_id >= (int)w->sources.size()) return fail(PIC_ERR_ARG, "bad source");
+    CU(cudaSetDevice(w->device));
+    const pic_world::Source& src = w->sources[source_id];
+    SpeciesHost& s = w->sp[src.sp];
+    const GridDev& g = w->g;
+    SourceArgs sa{};
+    const int nn[3] = {g.ni, g.nj, g.nk};
+    for (int d = 0; d < 3; d++) {
+        sa.x0[d] = g.x0[d];
+        sa.L[d] = g.dxd[d] * (nn[d] - 1);
+    }
+    const int ax = src.face >> 1;
+    const double A = sa.L[0] * sa.L[1] * sa.L[2] / sa.L[ax];
+    if (src.face & 1) sa.L[ax] -= g.dxd[ax];  // the + faces inject one cell in (Source.cpp:55, 74, 93)
+    sa.face = src.face;
+    sa.v_drift = src.v_drift;
+    sa.vth = src.T > 0 ? std::sqrt(2 * kKb * src.T / s.mass) : 0.0;
+    sa.mpw0 = s.mpw0;
+    sa.key = src.key;
+    sa.step = (unsigned)w->ts;
+    sa.src = (unsigned)source_id;
+    // num_macro = (int)(n v A dt / mpw0 + u) (Source.cpp:27, 41)
+    const double num_micro = src.den * src.v_drift * A * w->dt;
+    const uint4 ru = philox4x32_10(make_uint4(0xFFFFFFFFu, sa.step, 0x5C000000u + sa.src, 7u), sa.key);
+    const long n = (long)(num_micro / s.mpw0 + (double)u01(ru.x));
+    if (n <= 0) return PIC_OK;
+    int rc = ensure_upload(w, n);
+    if (rc) return rc;
+    const long cap = w->upload_cap;
+    double* dp = w->upload_buf;
+    double* dv = dp + 3 * (size_t)cap;
+    double* dw = dv + 3 * (size_t)cap;
+    for (long a = 0; a < n; a += cap) {
+        const long m = std::min<long>(cap, n - a);
+        sa.first = (int)a;
+        sa.n = (int)m;
+        Scope sc(w, "source", 6);
+        launch_source(sa, dp, dv, dw, w->stream);
+        launch_from_abs(w->g, s.dev, dp, dv, dw, nullptr, s.next_id + (unsigned long long)a, (int)m, 1,
+                        (float)(s.charge / s.mass * 0.5 * w->dt), w->ef, w->stream);
+    }
+    s.next_id += n;
+    CU(cudaGetLastError());
+    return PIC_OK;
+}
+
 extern "C" int pic_mcc_create(pic_world* w, int electrons, int ions, double n_neutral, double T_neutral,
                               double m_neutral, double E_ion_eV, double B_inc, int sigma_ion_kind,
                               const double* sigma_ion_params, const double* table_E, const double* table_s,
@@ -1932,6 +2021,10 @@ extern "C" int pic_step(pic_world* w) {
             int rc = pic_species_merge(w, s, w->merge_min);
             if (rc) return rc;
         }
+    }
+    for (int q = 0; q < (int)w->sources.size(); q++) {  // main.cpp:196-198
+        int rc = pic_source_sample(w, q);
+        if (rc) return rc;
     }
     // collisions are fused into the electron push, which runs first so that the ion products
     // are pushed in this step too (the reference applies interactions before the species loop)

@@ -87,11 +87,18 @@ struct SpeciesDev {
 // ------------------------------------------------------------------------------------
 // Philox-4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11)
 // ------------------------------------------------------------------------------------
-__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
+__host__ __device__ __forceinline__ unsigned mulhi32(unsigned a, unsigned b) {
+#ifdef __CUDA_ARCH__
+    return __umulhi(a, b);
+#else
+    return (unsigned)(((unsigned long long)a * b) >> 32);
+#endif
+}
+__host__ __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
 #pragma unroll
     for (int r = 0; r < 10; r++) {
-        unsigned hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
-        unsigned hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+        unsigned hi0 = mulhi32(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+        unsigned hi1 = mulhi32(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
         c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
         k.x += 0x9E3779B9u;
         k.y += 0xBB67AE85u;
@@ -99,7 +106,7 @@ __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
     return c;
 }
 // uniform in (0,1): ((x >> 9) + 0.5) * 2^-23, 24 significant bits, exact in FP32
-__device__ __forceinline__ float u01(unsigned x) { return ((float)(x >> 9) + 0.5f) * (1.0f / 8388608.0f); }
+__host__ __device__ __forceinline__ float u01(unsigned x) { return ((float)(x >> 9) + 0.5f) * (1.0f / 8388608.0f); }
 
 // splitmix64 finaliser (Steele, Lea, Flood 2014)
 __device__ __forceinline__ unsigned long long mix64(unsigned long long x) {

@@ -69,6 +69,20 @@ struct LoadArgs {
     int n;
 };
 void launch_load_uniform(const GridDev& g, SpeciesDev sp, const LoadArgs& la, cudaStream_t s);
+// one step of a beam source (ColdBeamSource / WarmBeamSource::sample, Source.cpp:35-192):
+// n particles on the inlet face, FP64 positions and velocities into pos / vel / w (then added
+// with Species::addParticle semantics)
+struct SourceArgs {
+    double x0[3], L[3];     // domain origin; extents of the sampled face (the + faces one cell in)
+    int face;               // 0..5: x-, x+, y-, y+, z-, z+
+    double v_drift;         // along the inward normal
+    double vth;             // sqrt(2kT/m) of Species::sampleVth, 0 for a cold beam
+    double mpw0;            // macroparticle weight
+    uint2 key;              // Philox key (seed)
+    unsigned step, src;     // counter words: the step and the source index
+    int first, n;           // particles first .. first + n - 1 of the step
+};
+void launch_source(const SourceArgs& sa, double* pos, double* vel, double* w, cudaStream_t s);
 void launch_sums(SpeciesDev sp, double* out, cudaStream_t s, int grid);
 void launch_sample_moments(const GridDev& g, SpeciesDev sp, float* mom, cudaStream_t s, int grid);
 void launch_merge(const GridDev& g, SpeciesDev sp, const float4* ef, const int* cell_start, int* list, int* nlist,

@@ -1058,6 +1058,55 @@ __global__ void k_load_uniform(GridDev g, SpeciesDev sp, LoadArgs la) {
         sp.id[dst] = id;
     }
 }
+// Beam source particles.  Particle p of a step draws Philox blocks (p, step, 0x5C000000 + src, b):
+//   b = 0: in-face coordinates a, b (u01 of words x, y); speed draws t0, t1 (z, w)
+//   b = 1: t2 .. t5;  b = 2: t6, t7, t8, theta;  b = 3: r (word x)
+// Position: the face plane (the + faces one cell in, as Source.cpp offsets L by -dx), the two
+// other coordinates uniform over the face.  Velocity: drift along the inward normal, plus for a
+// warm beam Species::sampleV3th (speed from three per-axis sums of three uniforms, isotropic
+// direction from theta = 2 pi u and r = 2u - 1), in FP64.
+__global__ void k_source(SourceArgs sa, double* pos, double* vel, double* w) {
+    const double kTwoPi = 6.283185307179586;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < sa.n; p += gridDim.x * blockDim.x) {
+        const unsigned tag = 0x5C000000u + sa.src;
+        const unsigned pp = (unsigned)(sa.first + p);
+        const uint4 r0 = philox4x32_10(make_uint4(pp, sa.step, tag, 0u), sa.key);
+        const int ax = sa.face >> 1;  // normal axis
+        const int e1 = ax == 0 ? 1 : 0, e2 = ax == 2 ? 1 : 2;
+        double x[3];
+        x[ax] = sa.x0[ax] + ((sa.face & 1) ? sa.L[ax] : 0.0);
+        x[e1] = sa.x0[e1] + (double)u01(r0.x) * sa.L[e1];
+        x[e2] = sa.x0[e2] + (double)u01(r0.y) * sa.L[e2];
+        double v[3] = {0.0, 0.0, 0.0};
+        if (sa.vth > 0.0) {
+            const uint4 r1 = philox4x32_10(make_uint4(pp, sa.step, tag, 1u), sa.key);
+            const uint4 r2 = philox4x32_10(make_uint4(pp, sa.step, tag, 2u), sa.key);
+            const uint4 r3 = philox4x32_10(make_uint4(pp, sa.step, tag, 3u), sa.key);
+            const double v1 = sa.vth * ((double)u01(r0.z) + (double)u01(r0.w) + (double)u01(r1.x) - 1.5);
+            const double v2 = sa.vth * ((double)u01(r1.y) + (double)u01(r1.z) + (double)u01(r1.w) - 1.5);
+            const double v3 = sa.vth * ((double)u01(r2.x) + (double)u01(r2.y) + (double)u01(r2.z) - 1.5);
+            const double sp_ = sqrt(v1 * v1 + v2 * v2 + v3 * v3);
+            const double th = kTwoPi * (double)u01(r2.w);
+            const double r = -1.0 + 2.0 * (double)u01(r3.x), aa = sqrt(fmax(1.0 - r * r, 0.0));
+            v[0] = sp_ * r;
+            v[1] = sp_ * (cos(th) * aa);
+            v[2] = sp_ * (sin(th) * aa);
+        }
+        v[ax] += (sa.face & 1) ? -sa.v_drift : sa.v_drift;
+        for (int d = 0; d < 3; d++) {
+            pos[3 * p + d] = x[d];
+            vel[3 * p + d] = v[d];
+        }
+        w[p] = sa.mpw0;
+    }
+}
+void launch_source(const SourceArgs& sa, double* pos, double* vel, double* w, cudaStream_t s) {
+    int grid = (sa.n + 255) / 256;
+    if (grid > 1024) grid = 1024;
+    if (grid < 1) grid = 1;
+    k_source<<<grid, 256, 0, s>>>(sa, pos, vel, w);
+}
+
 __global__ void k_load_count(SpeciesDev sp, int n) {
     int nn = sp.counts[0] + n;
     sp.counts[0] = nn > sp.capacity ? sp.capacity : nn;

@@ -128,6 +128,22 @@ int pic_species_gas_properties(pic_world* w, int sp, double* vel, double* T);
 /* World::computeChargeDensity(species): den_s and rho = sum q_s den_s  World.cpp:193-200 */
 int pic_charge_density(pic_world* w);
 
+/* ---- Sources (ch4/v3/src/Source.h:13-68, Source.cpp) ------------------------------------ */
+
+/* ColdBeamSource(species, world, v_drift, den, face) (T = 0) and
+ * WarmBeamSource(species, world, v_drift, den, T, face)               Source.cpp:3-30, 105-110
+ * face: 0..5 for x-, x+, y-, y+, z-, z+ (inletName2Index, World.cpp:369-390); the face may not lie
+ * on a periodic axis.  Like the reference constructor (World::addInlet, World.cpp:206-260) the
+ * inlet face becomes Dirichlet at 0 V.  Draws are Philox streams keyed by seed. */
+int pic_source_create(pic_world* w, int sp, double v_drift, double den, double T, int face, uint64_t seed,
+                      int* source_id);
+/* Source::sample() (Source.cpp:99-102, 186-190): (int)(den v_drift A dt / mpw0 + u) particles of
+ * weight mpw0 on the inlet face (the + faces one cell in), the two other coordinates uniform,
+ * velocity v_drift along the inward normal plus, for a warm beam, Species::sampleV3th(T); added
+ * with Species::addParticle semantics (bounds and objects checked, velocity rewound by half a
+ * step).  pic_step samples every source at the start of the step (main.cpp:196-198). */
+int pic_source_sample(pic_world* w, int source_id);
+
 /* ---- PotentialSolver (ch4/v3/src/PotentialSolver.h:26-88) ----------------------------- */
 
 #define PIC_SOLVER_RBSOR 0 /* red-black SOR, FP32 sweeps in FP64 refinement (replaces GS) */

@@ -9,6 +9,7 @@
 #ifndef PIC_GB300_HPP
 #define PIC_GB300_HPP
 #include <array>
+#include <cctype>
 #include <chrono>
 #include <cmath>
 #include <cstdint>
@@ -286,6 +287,43 @@ private:
     World* world_;
     int iters_ = 0;
     double rel_ = 0;
+};
+
+// ch4/v3/src/Source.h:13-68: inlet_face "x-" .. "z+" (or "-x" .. "+z"); the face becomes
+// Dirichlet at 0 V; sample() injects one step of particles (pic_step does it for every source)
+class Source {
+public:
+    virtual ~Source() noexcept = default;
+    virtual void sample() const noexcept { last_rc_ = pic_source_sample(world_->handle(), id_); }
+    int lastStatus() const { return last_rc_; }
+
+protected:
+    Source(Species& sp, World& world, type_calc v_drift, type_calc den, type_calc T, std::string face,
+           uint64_t seed)
+        : world_(&world) {
+        static const char* names[] = {"x-", "x+", "y-", "y+", "z-", "z+", "-x", "+x", "-y", "+y", "-z", "+z"};
+        for (auto& ch : face) ch = (char)std::tolower((unsigned char)ch);
+        int f = -1;
+        for (int k = 0; k < 12; k++)
+            if (face == names[k]) f = k % 6;
+        if (f < 0) throw std::invalid_argument("Passed wrong face name.");
+        check(pic_source_create(world.handle(), sp.id(), v_drift, den, T, f, seed, &id_));
+    }
+    World* world_;
+    int id_ = -1;
+    mutable int last_rc_ = PIC_OK;
+};
+class ColdBeamSource : public Source {
+public:
+    ColdBeamSource(Species& sp, World& world, type_calc v_drift, type_calc den, std::string inlet_face = "-z",
+                   uint64_t seed = 1)
+        : Source(sp, world, v_drift, den, 0.0, inlet_face, seed) {}
+};
+class WarmBeamSource : public Source {
+public:
+    WarmBeamSource(Species& sp, World& world, type_calc v_drift, type_calc den, type_calc T,
+                   std::string inlet_face = "-z", uint64_t seed = 1)
+        : Source(sp, world, v_drift, den, T, inlet_face, seed) {}
 };
 
 class Interaction {  // ch4/v3/src/Interactions.h:9-13
