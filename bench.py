@@ -358,6 +358,7 @@ def run_gpu(args, wl, rank, ws, local):
     W, e, i, M, S = (setup_ensemble if ensemble else setup_world)(pic, wl, seed=1 + rank)
     assert S.solve(raise_on_fail=True)  # initial vacuum + space-charge field (main.cpp:172-173)
     S.computeEF()
+    tuned = W.autotune()  # launch shapes measured on this world's data (outside the timed region)
     for _ in range(args.warmup):
         W.step()
     W.synchronize()
@@ -448,7 +449,8 @@ def run_gpu(args, wl, rank, ws, local):
                    "poisson_inner_per_step": inner / args.steps, "sort_every": 20,
                    "l2": "inputs larger than L2 (particles %.1f GB)" % (parts_per_step * 36 / 1e9),
                    "merging": "every %d steps, cells above %d particles" % (MERGE_EVERY, MERGE_MIN),
-                   "parallelism": "replicas" if ws > 1 else "1 GPU"},
+                   "parallelism": "replicas" if ws > 1 else "1 GPU",
+                   "autotuned": tuned},
         "wall_s": wall,
         "gpu_launches": launches,
         "roofline": roof,

@@ -63,6 +63,7 @@ def library():
         "pic_world_get_time": [vp, vp],
         "pic_source_create": [vp, i, d, d, d, i, u64, vp],
         "pic_source_sample": [vp, i],
+        "pic_autotune": [vp, vp, vp],
         "pic_world_potential_energy": [vp, vp],
         "pic_species_sample_particles": [vp, i, l, vp, vp, vp],
         "pic_world_set_boundaries": [vp, vp, vp, vp],
@@ -282,6 +283,12 @@ class World:
         _check(self._L.pic_loop_configure(self._h, int(solve_each_step), int(sort_every),
                                           _p(np.asarray(list(subcycle) + [1] * (4 - len(subcycle)), np.int32)),
                                           int(merge_every), int(merge_after), int(merge_min)))
+
+    def autotune(self):
+        """Measure launch shapes on this world's data and keep the fastest (pic_autotune)."""
+        a, b = C.c_int(), C.c_int()
+        _check(self._L.pic_autotune(self._h, C.byref(a), C.byref(b)))
+        return dict(push_ctas_per_sm=a.value, node_grid=b.value)
 
     def step(self):
         _check(self._L.pic_step(self._h))

@@ -2061,6 +2061,89 @@ extern "C" int pic_step(pic_world* w) {
     return PIC_OK;
 }
 
+// =====================================================================================
+// Autotuner: launch shapes measured on the world's own data
+// =====================================================================================
+namespace {
+// mean device time of f() over reps launches after one warm-up launch, in milliseconds
+template <class F>
+float time_launches(pic_world* w, int reps, F f) {
+    f();
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaEventRecord(a, w->stream);
+    for (int r = 0; r < reps; r++) f();
+    cudaEventRecord(b, w->stream);
+    cudaEventSynchronize(b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return ms / reps;
+}
+}  // namespace
+
+extern "C" int pic_autotune(pic_world* w, int* push_ctas_per_sm, int* node_grid) {
+    if (!w) return fail(PIC_ERR_ARG, "null world");
+    CU(cudaSetDevice(w->device));
+    // streaming node kernels (residual, CG, learned CG): CTA count from 2 to 16 per SM, timed on
+    // the float-float residual, which only recomputes r from phi and rho
+    {
+        SolveWork sw = solve_work(w);
+        double r2, b2;
+        int rc = residual_norms(w, sw, 0, r2, b2);  // allocates the residual's side arrays
+        if (rc) return rc;
+        const int most = std::min<long>((w->g.nv / 4 + 255) / 256, (long)w->gstride);
+        int best = 0;
+        float best_ms = 0.f;
+        for (int m : {2, 4, 8, 16}) {
+            const int cand = std::min(w->sms * m, most);
+            if (cand < 1 || cand == best) continue;
+            w->g.node_grid = cand;
+            sw = solve_work(w);
+            const float ms = time_launches(w, 5, [&] { launch_residual(w->g, sw, 0, w->stream, w->rho_prev, w->bfix); });
+            if (!best || ms < best_ms) {
+                best = cand;
+                best_ms = ms;
+            }
+        }
+        w->g.node_grid = best;
+        w->rhs_valid = false;  // r was rewritten: the next solve starts from a full residual
+    }
+    // push + deposit: CTAs per SM from 1 to the occupancy limit, timed on pushes with dt = 0
+    // (positions and velocities stay, and the deposit reproduces the density of the particles
+    // where they are, which the last step deposited)
+    {
+        long n_all = 0;
+        for (auto& s : w->sp) {
+            int n = 0;
+            CU(cudaMemcpyAsync(&n, s.dev.counts, sizeof(int), cudaMemcpyDeviceToHost, w->stream));
+            CU(cudaStreamSynchronize(w->stream));
+            n_all += n;
+        }
+        const int most = push_blocks_per_sm();
+        int best = most;
+        if (n_all > 0) {
+            float best_ms = 0.f;
+            for (int c = 1; c <= most; c++) {
+                w->grid_push = w->sms * c;
+                const float ms = time_launches(w, 3, [&] {
+                    for (int s = 0; s < (int)w->sp.size(); s++) push_species(w, s, 0.0, 1, false, true);
+                });
+                if (c == 1 || ms < best_ms) {
+                    best = c;
+                    best_ms = ms;
+                }
+            }
+        }
+        w->grid_push = w->sms * best;
+        if (push_ctas_per_sm) *push_ctas_per_sm = best;
+    }
+    if (node_grid) *node_grid = w->g.node_grid;
+    return check_device_error(w);
+}
+
 extern "C" int pic_synchronize(pic_world* w) {
     if (!w) return fail(PIC_ERR_ARG, "null world");
     CU(cudaSetDevice(w->device));

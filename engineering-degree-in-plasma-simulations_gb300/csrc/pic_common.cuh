@@ -66,6 +66,7 @@ struct GridDev {
     // slabs is outside every instance
     int zslab;
     FastDiv fd_zslab;
+    int node_grid;  // CTAs of the streaming node kernels chosen by the autotuner (0: default)
 };
 // z index of a node or cell inside its instance slab (the global index without slabs)
 __device__ __forceinline__ int slab_local_z(const GridDev& g, int k) {

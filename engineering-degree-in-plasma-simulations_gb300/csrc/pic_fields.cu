@@ -388,7 +388,7 @@ __global__ void __launch_bounds__(256) k_residual(GridDev g, const float2* __res
 void launch_residual(const GridDev& g, SolveWork& w, int apply_e, cudaStream_t s, float* rho_prev, float* bfix_out) {
     const float2* in = w.phi;
     float2* out = apply_e ? w.phi_alt : w.phi;
-    k_residual<<<stream_blocks(g.nv), 256, 0, s>>>(g, in, out, w.e, w.rho,
+    k_residual<<<stream_blocks(g), 256, 0, s>>>(g, in, out, w.e, w.rho,
                                                           reinterpret_cast<const uint16_t*>(w.kind), w.r, w.gpart,
                                                           w.gstride, w.ticket, w.scal + kS_R2, apply_e, rho_prev,
                                                           bfix_out);
@@ -451,7 +451,7 @@ __global__ void __launch_bounds__(256) k_rhs_update(GridDev g, float* __restrict
     grid_sum<3>(v, gpart, gstride, ticket, out);
 }
 void launch_rhs_update(const GridDev& g, SolveWork& w, float* rho_prev, const float* bfix, cudaStream_t s) {
-    k_rhs_update<<<stream_blocks(g.nv), 256, 0, s>>>(g, w.r, w.rho, rho_prev, bfix,
+    k_rhs_update<<<stream_blocks(g), 256, 0, s>>>(g, w.r, w.rho, rho_prev, bfix,
                                                             reinterpret_cast<const uint16_t*>(w.kind), w.gpart,
                                                             w.gstride, w.ticket, w.scal + kS_R2);
 }
@@ -683,7 +683,7 @@ __global__ void __launch_bounds__(256) k_pcg_k2(GridDev g, const float* __restri
     grid_sum<3>(v, gpart, gstride, ticket, scal + kS_RZN);  // r.z', r.z, r.r
 }
 void launch_pcg_init(const GridDev& g, SolveWork& w, cudaStream_t s) {
-    k_pcg_init<<<stream_blocks(g.nv), 256, 0, s>>>(g, w.r, w.z, w.e, w.d,
+    k_pcg_init<<<stream_blocks(g), 256, 0, s>>>(g, w.r, w.z, w.e, w.d,
                                                           reinterpret_cast<const uint16_t*>(w.kind), w.gpart,
                                                           w.gstride, w.ticket, w.scal, w.flag);
 }
@@ -691,9 +691,9 @@ void launch_pcg_init(const GridDev& g, SolveWork& w, cudaStream_t s) {
 void launch_pcg_iter_impl(const GridDev& g, SolveWork& w, float* d_in, float* d_out, int it, double target_rr,
                           cudaStream_t s) {
     const uint16_t* kd = reinterpret_cast<const uint16_t*>(w.kind);
-    k_pcg_k1<<<stream_blocks(g.nv), 256, 0, s>>>(g, w.z, d_in, d_out, w.q, kd, w.gpart, w.gstride, w.ticket, w.scal, w.flag,
+    k_pcg_k1<<<stream_blocks(g), 256, 0, s>>>(g, w.z, d_in, d_out, w.q, kd, w.gpart, w.gstride, w.ticket, w.scal, w.flag,
                                          it, target_rr);
-    k_pcg_k2<<<stream_blocks(g.nv), 256, 0, s>>>(g, d_out, w.q, w.e, w.r, w.z, kd, w.gpart, w.gstride, w.ticket,
+    k_pcg_k2<<<stream_blocks(g), 256, 0, s>>>(g, d_out, w.q, w.e, w.r, w.z, kd, w.gpart, w.gstride, w.ticket,
                                                  w.scal, w.flag, it);
 }
 

@@ -136,10 +136,11 @@ constexpr int kNodeTile = 4 * kNodeThreads;
 inline int node_blocks(int nv) { return (nv + kNodeTile - 1) / kNodeTile; }
 // streaming node kernels (four consecutive nodes per thread and 16-byte loads, grid-stride): a
 // few CTAs per SM keep every SM busy, and the grid sum adds few partials
-inline int stream_blocks(int nv) {
+inline int stream_blocks(int nv, int cap = 1216) {
     const int want = (nv / 4 + 255) / 256;
-    return want < 1 ? 1 : (want < 1216 ? want : 1216);
+    return want < 1 ? 1 : (want < cap ? want : cap);
 }
+inline int stream_blocks(const GridDev& g) { return stream_blocks(g.nv, g.node_grid > 0 ? g.node_grid : 1216); }
 // device scalar slots of the solvers
 enum : int {
     kS_RZ = 0,      // [0..1] r.z of iterations it (double-buffered by parity)

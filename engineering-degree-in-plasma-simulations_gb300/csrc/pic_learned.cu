@@ -556,9 +556,9 @@ void launch_lpcg_init(const GridDev& g, SolveWork& w, const LpState& L, cudaStre
 void launch_lpcg_iter(const GridDev& g, SolveWork& w, const LpState& L, float* d_in, float* d_out, int it,
                       double target_rr, cudaStream_t s, int sms) {
     const uint16_t* kd = reinterpret_cast<const uint16_t*>(w.kind);
-    k_lpcg_k1<<<stream_blocks(g.nv), 256, 0, s>>>(g, w.z, d_in, d_out, w.q, kd, w.gpart, w.gstride, w.ticket, w.scal, w.flag,
+    k_lpcg_k1<<<stream_blocks(g), 256, 0, s>>>(g, w.z, d_in, d_out, w.q, kd, w.gpart, w.gstride, w.ticket, w.scal, w.flag,
                                           it, target_rr);
-    k_lpcg_k2<<<stream_blocks(g.nv), 256, 0, s>>>(g, d_out, w.q, w.e, w.r, kd, w.gpart, w.gstride, w.ticket, w.scal,
+    k_lpcg_k2<<<stream_blocks(g), 256, 0, s>>>(g, d_out, w.q, w.e, w.r, kd, w.gpart, w.gstride, w.ticket, w.scal,
                                                   w.flag, it);
     launch_lp_apply(g, L, w.r, w.z, kd, w.q, &w, w.flag, s, sms);
 }

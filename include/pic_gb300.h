@@ -222,6 +222,13 @@ int pic_mcc_stats(pic_world* w, uint64_t* out);
  * merge_every/merge_after/merge_min: merging (main.cpp:179: ts > 250 && ts % 50 == 0). */
 int pic_loop_configure(pic_world* w, int solve_each_step, int sort_every, const int* subcycle, int merge_every,
                        int merge_after, int merge_min);
+/* Autotuner (no reference counterpart): measures launch shapes on the world's own data and keeps
+ * the fastest for the rest of the run: the CTA count of the streaming node kernels (residual and
+ * CG kernels; 2 to 16 per SM, timed on the float-float residual) and the push's CTAs per SM (1 to
+ * the occupancy limit, timed on pushes with dt = 0, which leave the particles and their deposit
+ * as they are).  Call it once the world holds its particles and fields; the next solve starts
+ * from a full residual.  Outputs may be NULL. */
+int pic_autotune(pic_world* w, int* push_ctas_per_sm, int* node_grid);
 /* one iteration of the time loop: advanceTime, [merge], collisions + push + deposit,
  * compaction, [averages], charge density, [solve + E], [sort] */
 int pic_step(pic_world* w);
