@@ -527,9 +527,10 @@ def poisson_bench(pic, n, seed=5, train_steps=300):
         W.phi = phi0
         S.solve()
     lp.collect(False)
-    rounds = []
-    for _ in range(max(1, train_steps // 100)):
-        loss, before, after, kept = lp.train(100)
+    cal_before, cal_after = lp.calibrate()  # level gains, judged by validation solves
+    rounds = [{"calibration": True, "val_iters_before": cal_before, "val_iters_after": cal_after, "kept": True}]
+    for k in range(max(1, train_steps // 100)):
+        loss, before, after, kept = lp.train(100, lr=1e-3 / (1 + k), pair_every=0)
         rounds.append({"loss": loss, "val_iters_before": before, "val_iters_after": after, "kept": kept})
     W.synchronize()
     train_s = time.perf_counter() - t0

@@ -116,6 +116,7 @@ def library():
         "pic_learned_loss_grad": [vp, vp, vp, vp, vp],
         "pic_learned_collect": [vp, i],
         "pic_learned_train": [vp, i, d, i, vp, vp, vp],
+        "pic_learned_calibrate": [vp, vp],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -553,7 +554,7 @@ class LearnedPreconditioner:
     def collect(self, on=True):
         _check(self.world._L.pic_learned_collect(self.world._h, int(on)))
 
-    def train(self, steps, lr=1e-4, pair_every=2):
+    def train(self, steps, lr=3e-3, pair_every=2):
         """One training round; returns (mean loss, validation iterations before, after, accepted)."""
         loss = C.c_double()
         it = np.zeros(2, np.int32)
@@ -561,6 +562,12 @@ class LearnedPreconditioner:
         _check(self.world._L.pic_learned_train(self.world._h, int(steps), float(lr), int(pair_every), C.byref(loss),
                                                _p(it), C.byref(acc)))
         return loss.value, int(it[0]), int(it[1]), bool(acc.value)
+
+    def calibrate(self):
+        """Level gains judged by validation solves (pic_learned_calibrate); returns (before, after)."""
+        it = np.zeros(2, np.int32)
+        _check(self.world._L.pic_learned_calibrate(self.world._h, _p(it)))
+        return int(it[0]), int(it[1])
 
     def apply(self, r):
         """z = B r over all nodes (r read on FREE nodes; z zero elsewhere)."""

@@ -1595,6 +1595,7 @@ extern "C" int pic_learned_set_weights(pic_world* w, const float* in, long count
     LpState& L = *w->lp;
     if (count != L.lay.total) return fail(PIC_ERR_ARG, "expected %d parameters, got %ld", L.lay.total, count);
     CU(cudaMemcpyAsync(L.W, in, sizeof(float) * count, cudaMemcpyHostToDevice, w->stream));
+    if (L.train) launch_lp_prep(L, w->stream);  // the BF16 copies of the training GEMMs
     launch_lp_fold(L, w->stream);
     CU(cudaStreamSynchronize(w->stream));
     CU(cudaGetLastError());
@@ -1740,6 +1741,94 @@ extern "C" int pic_learned_train(pic_world* w, int steps, double lr, int pair_ev
     }
     if (accepted) *accepted = keep ? 1 : 0;
     return PIC_OK;
+}
+
+// Level gains of the learned preconditioner, learned by the solver itself: each gain is kept only
+// if a validation solve (the right-hand side of the last collected solve, else a white-noise one)
+// needs fewer iterations.  The level-0 stencil is scaled first (doubling, then a half-octave
+// refinement), then each network level's lift and projection together by sqrt(g), which keeps the
+// projection the scaled adjoint of the lift (B stays symmetric).
+extern "C" int pic_learned_calibrate(pic_world* w, int* val_iters) {
+    if (!w) return fail(PIC_ERR_ARG, "null world");
+    CU(cudaSetDevice(w->device));
+    int rc = ensure_lp_train(w);
+    if (rc) return rc;
+    LpState& L = *w->lp;
+    const GridDev& g = w->g;
+    const int np = lp_npairs(L);
+    if (np > 0) {
+        CU(cudaMemcpyAsync(lp_train_val(L), lp_pair_r(L, np - 1), sizeof(float) * g.nv, cudaMemcpyDeviceToDevice,
+                           w->stream));
+    } else {
+        launch_lp_noise_pair(g, L, w->kind, w->lp_seed ^ 0x9e3779b97f4a7c15ull, w->stream, w->grid_nodes);
+        CU(cudaMemcpyAsync(lp_train_val(L), lp_train_r(L), sizeof(float) * g.nv, cudaMemcpyDeviceToDevice, w->stream));
+    }
+    std::vector<float> best(L.lay.total);
+    CU(cudaMemcpyAsync(best.data(), L.W, sizeof(float) * best.size(), cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    auto trial = [&](const std::vector<float>& wt, int* it) -> int {
+        CU(cudaMemcpyAsync(L.W, wt.data(), sizeof(float) * wt.size(), cudaMemcpyHostToDevice, w->stream));
+        launch_lp_prep(L, w->stream);
+        launch_lp_fold(L, w->stream);
+        return learned_validation_iters(w, lp_train_val(L), kLearnedInnerCap, it);
+    };
+    int before = 0;
+    rc = trial(best, &before);
+    if (rc) return rc;
+    int cur = before;
+    auto scaled = [&](const std::vector<float>& base, int off, int cnt, float f) {
+        std::vector<float> t = base;
+        for (int k = 0; k < cnt; k++) t[off + k] *= f;
+        return t;
+    };
+    // level 0: doubling while it helps, then a half octave either side of the best
+    {
+        float gbest = 1.f;
+        for (float gk = 2.f; gk <= 64.f; gk *= 2.f) {
+            int it = 0;
+            rc = trial(scaled(best, L.lay.s0, 27, gk / gbest), &it);
+            if (rc) return rc;
+            if (it < cur) {
+                best = scaled(best, L.lay.s0, 27, gk / gbest);
+                cur = it;
+                gbest = gk;
+            } else {
+                break;
+            }
+        }
+        for (float f : {1.41421356f, 0.70710678f}) {
+            int it = 0;
+            rc = trial(scaled(best, L.lay.s0, 27, f), &it);
+            if (rc) return rc;
+            if (it < cur) {
+                best = scaled(best, L.lay.s0, 27, f);
+                cur = it;
+            }
+        }
+    }
+    // network levels: gains 0.5, 0.7, 1.4, 2 on lift and projection (sqrt on each)
+    for (int l = 1; l <= kLpNetLevels && l < L.nlev; l++) {
+        const int C = lp_channels(l);
+        for (float gl : {0.5f, 0.7f, 1.4f, 2.f}) {
+            std::vector<float> t = scaled(best, L.lay.wl[l], 27 * C, std::sqrt(gl));
+            t = scaled(t, L.lay.wp[l], 27 * C, std::sqrt(gl));
+            int it = 0;
+            rc = trial(t, &it);
+            if (rc) return rc;
+            if (it < cur) {
+                best = t;
+                cur = it;
+            }
+        }
+    }
+    int after = 0;
+    rc = trial(best, &after);
+    if (rc) return rc;
+    if (val_iters) {
+        val_iters[0] = before;
+        val_iters[1] = after;
+    }
+    return check_device_error(w);
 }
 
 extern "C" int pic_solver_compute_ef(pic_world* w) {

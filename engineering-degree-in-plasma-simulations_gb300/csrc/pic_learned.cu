@@ -1169,12 +1169,53 @@ float* lp_train_grad(const LpState& L) { return L.train->grad; }
 double* lp_train_red(const LpState& L) { return L.train->red; }
 unsigned* lp_train_err(const LpState& L) { return L.train->err; }
 
+// Keeps B symmetric after every optimiser step, so that flexible CG sees a symmetric
+// preconditioner (an unconstrained step can make B indefinite, and CG then stalls): the level-0
+// stencil is made even (S0[t] = S0[26 - t]); on each network level the projection is tied to the
+// scaled adjoint of the lift, Wp[t][c] = s_l Wl[c][26 - t] with s_l = 1 / diag_l (the start weights
+// satisfy it), and the channel mix is made symmetric.  Each tied pair is replaced by its mean.
+struct LpSymScales {
+    float s[kLpNetLevels + 1];
+};
+__global__ void k_lp_symmetrize(float* W, LpLayout lay, LpSymScales sc) {
+    const int tid = threadIdx.x;
+    if (tid < 13) {
+        const float m = 0.5f * (W[lay.s0 + tid] + W[lay.s0 + 26 - tid]);
+        W[lay.s0 + tid] = m;
+        W[lay.s0 + 26 - tid] = m;
+    }
+    for (int l = 1; l <= kLpNetLevels; l++) {
+        const int C = lp_channels(l);
+        const float s = sc.s[l];
+        for (int x = tid; x < C * 27; x += blockDim.x) {
+            const int c = x / 27, t = x - c * 27;
+            float* a = W + lay.wl[l] + c * 27 + t;
+            float* p = W + lay.wp[l] + (26 - t) * C + c;
+            const float m = 0.5f * (*a + *p / s);
+            *a = m;
+            *p = s * m;
+        }
+        for (int x = tid; x < C * C; x += blockDim.x) {
+            const int i = x / C, j = x - i * C;
+            if (i >= j) continue;
+            float* u = W + lay.wm[l] + i * C + j;
+            float* v = W + lay.wm[l] + j * C + i;
+            const float m = 0.5f * (*u + *v);
+            *u = m;
+            *v = m;
+        }
+    }
+}
+
 void launch_lp_adam(LpState& L, float lr, cudaStream_t s) {
     LpTrain* T = L.train;
     T->step++;
     float bc1 = 1.f - powf(0.9f, (float)T->step), bc2 = 1.f - powf(0.999f, (float)T->step);
     k_lp_adam<<<std::max(1, std::min(1024, (L.lay.total + 255) / 256)), 256, 0, s>>>(L.W, T->grad, T->m, T->v,
                                                                                      T->pscale, L.lay.total, lr, bc1, bc2);
+    LpSymScales sc{};
+    for (int l = 1; l <= kLpNetLevels; l++) sc.s[l] = (float)(1.0 / (l < L.nlev ? L.diag[l] : 1.0));
+    k_lp_symmetrize<<<1, 256, 0, s>>>(L.W, L.lay, sc);
     launch_lp_prep(L, s);
     launch_lp_fold(L, s);
 }

@@ -194,6 +194,11 @@ int pic_learned_collect(pic_world* w, int on);
  * a round that needs more iterations is rolled back (*accepted = 0). */
 int pic_learned_train(pic_world* w, int steps, double lr, int pair_every, double* mean_loss, int* val_iters,
                       int* accepted);
+/* Level-gain calibration, learned by the solver itself: the level-0 stencil gain (doubling, then a
+ * half-octave refinement) and each network level's gain (0.5 .. 2, applied to lift and projection
+ * alike so B stays symmetric) are kept only if a validation solve (the right-hand side of the last
+ * collected solve, else white noise) needs fewer iterations.  val_iters[2]: before, after. */
+int pic_learned_calibrate(pic_world* w, int* val_iters);
 
 /* ---- Interaction: MC_MEX_Ionization (ch4/v3/src/Interactions.h:98-143) ------------------
  * Background-gas form: the neutral species is a uniform Maxwellian gas (density n_neutral,

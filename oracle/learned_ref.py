@@ -135,6 +135,20 @@ def init_weights(diags, channels=CHANNELS):
     return W
 
 
+def symmetrize(W, diags):
+    """The projection the trainer applies after every optimiser step (csrc/pic_learned.cu
+    k_lp_symmetrize): S0 even, each network level's projection the adjoint of its lift scaled by
+    1 / diag_l, its mix symmetric; every tied pair replaced by its mean.  B is then symmetric."""
+    W["S0"][:] = 0.5 * (W["S0"] + W["S0"][::-1])
+    for l, w in enumerate(W["net"], start=1):
+        sc = 1.0 / diags[l] if l < len(diags) else 1.0
+        a = 0.5 * (w["Wl"] + w["Wp"][::-1].T / sc)
+        w["Wl"][:] = a
+        w["Wp"][:] = sc * a[:, ::-1].T
+        w["Wm"][:] = 0.5 * (w["Wm"] + w["Wm"].T)
+    return W
+
+
 def stencil27(z, S, per):
     out = np.zeros_like(z)
     for t, d in enumerate(TAPS):

@@ -223,3 +223,34 @@ def test_moments_and_gas_properties_bit_exact(port):
     mom = port.sample_moments(g, p, mom)  # accumulated twice, as the golden run
     vel, T = port.gas_properties(g, mom, O.ME)
     assert np.array_equal(vel, d["gas_vel"]) and np.array_equal(T, d["gas_T"])
+
+
+def test_learned_symmetrize_makes_the_preconditioner_symmetric():
+    """The trainer's projection (learned_ref.symmetrize, as csrc/pic_learned.cu k_lp_symmetrize)
+    turns arbitrary weights into a symmetric B, and leaves the start weights as they are."""
+    import learned_ref as LR
+
+    shape, per = (17, 16, 16), (0, 1, 1)
+    mask = np.ones(shape)
+    mask[0] = mask[-1] = 0
+    c = (1e6, 1e6, 1e6)
+    nlev = len(LR.level_shapes(shape))
+    diags = LR.level_diags(c, nlev)
+    W0 = LR.init_weights(diags)
+    W1 = LR.symmetrize(LR.init_weights(diags), diags)
+    assert np.array_equal(W0["S0"], W1["S0"])
+    for a, b in zip(W0["net"], W1["net"]):
+        for k in ("Wl", "Wm", "Wp"):
+            assert np.allclose(a[k], b[k], rtol=1e-15, atol=0)
+    rng = np.random.default_rng(4)
+    W = LR.init_weights(diags)
+    W["S0"] += rng.normal(size=27) / diags[0]
+    for l, w in enumerate(W["net"], start=1):
+        for k in ("Wl", "Wm", "Wp"):
+            dl = diags[l] if l < len(diags) else 1.0
+            w[k] += rng.normal(size=w[k].shape) * (0.3 / dl if k == "Wp" else 0.3)
+    x, y = rng.normal(size=shape) * mask, rng.normal(size=shape) * mask
+    B = lambda v: LR.apply(v, mask, W, per, diags)
+    assert abs(np.vdot(x, B(y)) - np.vdot(y, B(x))) > 1e-3 * abs(np.vdot(x, B(y)))  # not symmetric yet
+    LR.symmetrize(W, diags)
+    assert abs(np.vdot(x, B(y)) - np.vdot(y, B(x))) <= 1e-10 * abs(np.vdot(x, B(y)))
