@@ -94,6 +94,9 @@ def library():
         "pic_mcc_create": [vp, i, i, d, d, d, d, d, i, vp, vp, vp, i, u64],
         "pic_mcc_apply": [vp, d],
         "pic_mcc_stats": [vp, vp],
+        "pic_dsmc_create": [vp, i, i, u64, vp],
+        "pic_dsmc_apply": [vp, i, d],
+        "pic_dsmc_stats": [vp, i, vp, vp],
         "pic_loop_configure": [vp, i, i, vp, i, i, i],
         "pic_step": [vp],
         "pic_species_merge": [vp, i, i],
@@ -603,3 +606,29 @@ class MC_MEX_Ionization:
         out = np.zeros(4, np.uint64)
         _check(self.world._L.pic_mcc_stats(self.world._h, _p(out)))
         return dict(candidates=int(out[0]), collisions=int(out[1]), ionizations=int(out[2]), lost=int(out[3]))
+
+
+class DSMC_MEX:
+    """VHS particle-particle collisions of one species with itself, DSMC_MEX(species, world), or
+    between two species of equal mpw0, DSMC_MEX(species1, species2, world)
+    (ch4/v3/src/Interactions.h:42-66).  World.step() applies it every step before the pushes."""
+
+    def __init__(self, species1, species2_or_world, world=None, seed=12345):
+        if world is None:
+            species2, world = None, species2_or_world
+        else:
+            species2 = species2_or_world
+        self.world = world
+        i = C.c_int(0)
+        _check(world._L.pic_dsmc_create(world._h, species1.id, -1 if species2 is None else species2.id, int(seed),
+                                        C.byref(i)))
+        self.id = i.value
+
+    def apply(self, dt):
+        _check(self.world._L.pic_dsmc_apply(self.world._h, self.id, float(dt)))
+
+    def stats(self):
+        out = np.zeros(2, np.uint64)
+        sv = C.c_double(0)
+        _check(self.world._L.pic_dsmc_stats(self.world._h, self.id, _p(out), C.byref(sv)))
+        return dict(collisions=int(out[0]), pairs=int(out[1]), sigma_v_rel_max=sv.value)

@@ -10,7 +10,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libpic_gb300.so")
-SOURCES = ["pic_particles.cu", "pic_fields.cu", "pic_capi.cu", "pic_noalloc.cu", "pic_learned.cu"]
+SOURCES = ["pic_particles.cu", "pic_fields.cu", "pic_capi.cu", "pic_noalloc.cu", "pic_learned.cu", "pic_dsmc.cu"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc" if os.path.exists("/usr/local/cuda/bin/nvcc") else "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]

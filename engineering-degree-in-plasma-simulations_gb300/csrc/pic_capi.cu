@@ -45,6 +45,7 @@ int fail(int code, const char* fmt, ...) {
 constexpr double kQe = 1.602176565e-19;  // ch4/v3/src/all.h:17
 constexpr double kMe = 9.10938215e-31;
 constexpr double kKb = 1.380648e-23;
+constexpr double kPiRef = 3.141592653;  // Const::pi, ch4/v3/src/all.h:20
 
 struct SpeciesHost {
     std::string name;
@@ -117,6 +118,16 @@ struct pic_world {
         uint2 key;
     };
     std::vector<Source> sources;
+    // particle-particle collisions (DSMC_MEX, Interactions.h:42-66), applied in list order
+    struct Dsmc {
+        int sp1, sp2;                  // sp2 == sp1: one species
+        DsmcArgs a;                    // constants, state pointers; species pointers set per call
+        int* start1 = nullptr;         // cell starts of the first species (two species only)
+        unsigned long long* state = nullptr;  // stats[3], then svmax and svmax_step (32 bytes)
+        double mpw0 = 0, dv = 0;
+        unsigned calls = 0;
+    };
+    std::vector<Dsmc> dsmc;
     // stacked independent instances along z (0: one instance): electrode potentials per slab,
     // neutral density per slab and the candidate probabilities derived from it
     int nslabs = 0;
@@ -618,6 +629,10 @@ extern "C" int pic_world_destroy(pic_world* w) {
     if (w->mcc_cand) cudaFree(w->mcc_cand);
     if (w->mcc_ncand) cudaFree(w->mcc_ncand);
     if (w->bfix) cudaFree(w->bfix);
+    for (auto& d : w->dsmc) {
+        if (d.start1) cudaFree(d.start1);
+        if (d.state) cudaFree(d.state);
+    }
     for (auto& s : w->sp) {
         cudaFree(s.dev.pos);
         cudaFree(s.dev.vel);
@@ -2047,6 +2062,109 @@ extern "C" int pic_mcc_stats(pic_world* w, uint64_t* out) {
 }
 
 // =====================================================================================
+// DSMC_MEX: VHS particle-particle collisions (Interactions.cpp:143-284)
+// =====================================================================================
+namespace {
+int dsmc_apply(pic_world* w, int id, double dt) {
+    pic_world::Dsmc& d = w->dsmc[id];
+    // Species::sortPointers per call (Interactions.cpp:191, 227-228): the species in cell order
+    int rc = sort_species(w, d.sp1);
+    if (rc) return rc;
+    if (!d.a.one) {
+        CU(cudaMemcpyAsync(d.start1, w->cell_start, sizeof(int) * w->g.nc, cudaMemcpyDeviceToDevice, w->stream));
+        rc = sort_species(w, d.sp2);
+        if (rc) return rc;
+    }
+    DsmcArgs a = d.a;
+    a.vel1 = w->sp[d.sp1].dev.vel;
+    a.vel2 = w->sp[d.sp2].dev.vel;
+    a.start1 = d.a.one ? w->cell_start : d.start1;
+    a.start2 = w->cell_start;
+    a.n1 = w->sp[d.sp1].dev.counts;
+    a.n2 = w->sp[d.sp2].dev.counts;
+    a.nc = w->g.nc;
+    a.half_coef = 0.5 * d.mpw0 * dt / d.dv;
+    a.call = d.calls++;
+    {
+        Scope sc(w, "dsmc", 2);
+        launch_dsmc(a, w->stream);
+    }
+    CU(cudaGetLastError());
+    return PIC_OK;
+}
+}  // namespace
+
+extern "C" int pic_dsmc_create(pic_world* w, int sp1, int sp2, uint64_t seed, int* dsmc_id) {
+    if (!valid_sp(w, sp1) || !dsmc_id) return fail(PIC_ERR_ARG, "bad species");
+    if (sp2 < 0) sp2 = sp1;
+    if (!valid_sp(w, sp2)) return fail(PIC_ERR_ARG, "bad second species");
+    if (w->dsmc.size() >= 256) return fail(PIC_ERR_ARG, "at most 256 DSMC interactions per world");
+    const SpeciesHost& s1 = w->sp[sp1];
+    const SpeciesHost& s2 = w->sp[sp2];
+    if (!(s1.mpw0 > 0)) return fail(PIC_ERR_ARG, "DSMC needs a positive macroparticle weight");
+    // the two-species constructor's check (Interactions.cpp:160-162)
+    if (s1.mpw0 != s2.mpw0)
+        return fail(PIC_ERR_ARG, "species must have the same macroparticle weight for this algorithm to work properly.");
+    CU(cudaSetDevice(w->device));
+    pic_world::Dsmc d;
+    d.sp1 = sp1;
+    d.sp2 = sp2;
+    const double m1 = s1.mass, m2 = s2.mass, m_red = m1 * m2 / (m1 + m2);
+    // Bird's VHS parameters at 273.15 K (Interactions.cpp:152-156, 173-176)
+    const double d_ref = 4.07e-10, omega = 0.77, c2 = 2 * kKb * 273.15 / m_red;
+    d.a = DsmcArgs{};
+    d.a.K = (float)(kPiRef * d_ref * d_ref * std::pow(c2, omega - 0.5) / std::tgamma(2.5 - omega));
+    d.a.ex = (float)(1.0 - omega);
+    d.a.f1 = (float)(m1 / (m1 + m2));
+    d.a.f2 = (float)(m2 / (m1 + m2));
+    d.a.one = sp1 == sp2;
+    d.a.key = make_uint2((unsigned)seed, (unsigned)(seed >> 32));
+    d.a.tag = 0xD5000000u + (unsigned)w->dsmc.size();
+    d.mpw0 = s1.mpw0;
+    d.dv = w->g.dxd[0] * w->g.dxd[1] * w->g.dxd[2];  // World::getCellVolume (World.cpp:101-103)
+    CU(cudaMalloc((void**)&d.state, 32));
+    if (!d.a.one && cudaMalloc((void**)&d.start1, sizeof(int) * (size_t)w->g.nc) != cudaSuccess) {
+        cudaFree(d.state);
+        return fail(PIC_ERR_CUDA, "out of device memory for the DSMC cell lists");
+    }
+    unsigned long long init[4] = {0, 0, 0, 0};
+    const float sv0 = 1e-14f;  // DSMC_MEX::sigma_v_rel_max initial value (Interactions.h:58)
+    std::memcpy(&init[3], &sv0, sizeof(float));
+    CU(cudaMemcpy(d.state, init, sizeof(init), cudaMemcpyHostToDevice));
+    d.a.stats = d.state;
+    d.a.svmax = reinterpret_cast<float*>(d.state + 3);
+    d.a.svmax_step = reinterpret_cast<unsigned*>(d.state + 3) + 1;
+    w->dsmc.push_back(d);
+    *dsmc_id = (int)w->dsmc.size() - 1;
+    return PIC_OK;
+}
+
+extern "C" int pic_dsmc_apply(pic_world* w, int dsmc_id, double dt) {
+    if (!w || dsmc_id < 0 || dsmc_id >= (int)w->dsmc.size()) return fail(PIC_ERR_ARG, "bad DSMC interaction");
+    if (!(dt >= 0)) return fail(PIC_ERR_ARG, "dt must be non-negative");
+    CU(cudaSetDevice(w->device));
+    return dsmc_apply(w, dsmc_id, dt);
+}
+
+extern "C" int pic_dsmc_stats(pic_world* w, int dsmc_id, uint64_t* counts, double* sigma_v_rel_max) {
+    if (!w || dsmc_id < 0 || dsmc_id >= (int)w->dsmc.size()) return fail(PIC_ERR_ARG, "bad DSMC interaction");
+    CU(cudaSetDevice(w->device));
+    unsigned long long st[4];
+    CU(cudaMemcpyAsync(st, w->dsmc[dsmc_id].state, sizeof(st), cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    if (counts) {
+        counts[0] = st[0];
+        counts[1] = st[1];
+    }
+    if (sigma_v_rel_max) {
+        float sv;
+        std::memcpy(&sv, &st[3], sizeof(float));
+        *sigma_v_rel_max = sv;
+    }
+    return PIC_OK;
+}
+
+// =====================================================================================
 // step loop (ch4/v3/src/main.cpp:177-286)
 // =====================================================================================
 extern "C" int pic_loop_configure(pic_world* w, int solve_each_step, int sort_every, const int* subcycle,
@@ -2113,6 +2231,10 @@ extern "C" int pic_step(pic_world* w) {
     }
     for (int q = 0; q < (int)w->sources.size(); q++) {  // main.cpp:196-198
         int rc = pic_source_sample(w, q);
+        if (rc) return rc;
+    }
+    for (int q = 0; q < (int)w->dsmc.size(); q++) {  // main.cpp:201-203 (MC_MEX collisions ride on the push)
+        int rc = dsmc_apply(w, q, w->dt);
         if (rc) return rc;
     }
     // collisions are fused into the electron push, which runs first so that the ion products

@@ -83,6 +83,27 @@ struct SourceArgs {
     int first, n;           // particles first .. first + n - 1 of the step
 };
 void launch_source(const SourceArgs& sa, double* pos, double* vel, double* w, cudaStream_t s);
+
+// DSMC_MEX on sorted species: cell c of species k owns particles [start_k[c], start_k[c+1])
+// (the last cell ends at the species count *n_k); vel2 == vel1 and one = 1 for one species
+struct DsmcArgs {
+    float4* vel1;
+    float4* vel2;
+    const int* start1;
+    const int* start2;
+    const int* n1;
+    const int* n2;
+    int nc, one;
+    float K, ex;                  // sigma v_rel = K (v_rel^2)^ex, ex = 1 - omega
+    float f1, f2;                 // m1 / (m1 + m2), m2 / (m1 + m2)
+    double half_coef;             // 0.5 mpw0 dt / dV
+    float* svmax;                 // (sigma v)_max read by the kernel, updated by the finishing launch
+    unsigned* svmax_step;         // largest candidate sigma v of the call (float bits, atomicMax)
+    unsigned long long* stats;    // [0] collisions, [1] candidate pairs, [2] collisions of the call
+    uint2 key;                    // Philox key (seed)
+    unsigned call, tag;           // counter words: the call number and the interaction's tag
+};
+void launch_dsmc(const DsmcArgs& a, cudaStream_t s);
 void launch_sums(SpeciesDev sp, double* out, cudaStream_t s, int grid);
 void launch_sample_moments(const GridDev& g, SpeciesDev sp, float* mom, cudaStream_t s, int grid);
 void launch_merge(const GridDev& g, SpeciesDev sp, const float4* ef, const int* cell_start, int* list, int* nlist,

@@ -218,6 +218,20 @@ int pic_mcc_set_slab_density(pic_world* w, int nslabs, const double* n_neutral);
 /* counters since creation: candidates, collisions, ionisations, products lost */
 int pic_mcc_stats(pic_world* w, uint64_t* out);
 
+/* ---- DSMC_MEX: VHS particle-particle collisions (ch4/v3/src/Interactions.h:42-66) ------ */
+/* DSMC_MEX(species, world) when sp2 < 0 or sp2 == sp1 (Interactions.cpp:143-157), else
+ * DSMC_MEX(species1, species2, world) (Interactions.cpp:158-177), which requires equal mpw0
+ * (PIC_ERR_ARG otherwise, as the reference throws).  Bird's VHS cross-section with d = 4.07e-10
+ * m, omega = 0.77 at 273.15 K; (sigma v)_max starts at 1e-14.  Pairs are drawn per cell from
+ * Philox streams keyed by (seed, cell, call).  pic_step applies every interaction each step,
+ * before the pushes, in creation order (main.cpp:201-203). */
+int pic_dsmc_create(pic_world* w, int sp1, int sp2, uint64_t seed, int* dsmc_id);
+/* DSMC_MEX::apply(dt) (Interactions.cpp:180-257): sorts the species into cell order, then
+ * collides pairs in every cell; (sigma v)_max is updated on the device (no host round trip). */
+int pic_dsmc_apply(pic_world* w, int dsmc_id, double dt);
+/* counts[0] collisions, counts[1] candidate pairs since creation; the current (sigma v)_max */
+int pic_dsmc_stats(pic_world* w, int dsmc_id, uint64_t* counts, double* sigma_v_rel_max);
+
 /* ---- the step loop (ch4/v3/src/main.cpp:177-286) -------------------------------------- */
 
 /* Loop options.  solve_each_step: Poisson + E every step (v3 comments it out, main.cpp:260-261;

@@ -358,5 +358,37 @@ private:
     int last_rc_ = PIC_OK;
 };
 
+// DSMC_MEX (Interactions.h:42-66): one species with itself, or two species of equal mpw0
+// (std::invalid_argument otherwise, as the reference's constructor throws).  A driver loop
+// calls apply(dt) with the other interactions (main.cpp:201-203); the one-call loop
+// pic_step applies every created DSMC interaction by itself.
+class DSMC_MEX : public Interaction {
+public:
+    DSMC_MEX(Species& species, World& world, uint64_t seed = 12345) : world_(&world) {
+        check(pic_dsmc_create(world.handle(), species.id(), -1, seed, &id_));
+    }
+    DSMC_MEX(Species& species1, Species& species2, World& world, uint64_t seed = 12345) : world_(&world) {
+        check(pic_dsmc_create(world.handle(), species1.id(), species2.id(), seed, &id_));
+    }
+    void apply(type_calc dt) noexcept override { last_rc_ = pic_dsmc_apply(world_->handle(), id_, dt); }
+    int lastStatus() const { return last_rc_; }
+    // collisions and candidate pairs since creation
+    std::array<uint64_t, 2> stats() const {
+        std::array<uint64_t, 2> s{};
+        check(pic_dsmc_stats(world_->handle(), id_, s.data(), nullptr));
+        return s;
+    }
+    double sigmaVRelMax() const {
+        double sv = 0;
+        check(pic_dsmc_stats(world_->handle(), id_, nullptr, &sv));
+        return sv;
+    }
+
+private:
+    World* world_;
+    int id_ = -1;
+    int last_rc_ = PIC_OK;
+};
+
 }  // namespace pic_gb300
 #endif

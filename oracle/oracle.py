@@ -65,6 +65,11 @@ class CollParams(C.Structure):
     ]
 
 
+class DsmcParams(C.Structure):
+    _fields_ = [("mass1", C.c_double), ("mass2", C.c_double), ("mpw0", C.c_double), ("dv", C.c_double),
+                ("c", C.c_double * 4)]
+
+
 class MT(C.Structure):
     _fields_ = [("mt", C.c_uint32 * 624), ("idx", C.c_int)]
 
@@ -110,6 +115,10 @@ class Port:
             "or_sums": (None, [vp, l, d, vp, vp, vp]),
             "or_sample_moments_ref": (None, [vp, vp, l, vp]),
             "or_gas_properties_ref": (None, [vp, vp, d, vp, vp]),
+            "or_dsmc_params_init": (None, [vp, vp, d, d, d]),
+            "or_dsmc_sigma": (d, [vp, d]),
+            "or_dsmc_ref": (l, [vp, vp, vp, vp, l, vp, l, d, vp, vp]),
+            "or_dsmc_gpuform": (l, [vp, vp, vp, vp, vp, l, d, d, u32, u32, u32, u32, vp, vp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -239,6 +248,28 @@ class Port:
                                         C.byref(ni_), len(ion), _p(ele), C.byref(ne), len(ele), dt, C.byref(w))
         return nc, nn.value, ni_.value, ne.value, w.value
 
+    def dsmc_params(self, g, mass1, mass2, mpw0):
+        q = DsmcParams()
+        self.lib.or_dsmc_params_init(C.byref(q), C.byref(g), mass1, mass2, mpw0)
+        return q
+
+    def dsmc_ref(self, g, q, r, p1, p2, dt, svmax):
+        """DSMC_MEX::apply on particle arrays (p2 None: one species); returns (collisions, pairs, svmax)."""
+        sv, pairs = C.c_double(svmax), C.c_long(0)
+        nc = self.lib.or_dsmc_ref(C.byref(g), C.byref(q), C.byref(r), _p(p1), len(p1), _p(p2),
+                                  0 if p2 is None else len(p2), dt, C.byref(sv), C.byref(pairs))
+        return nc, pairs.value, sv.value
+
+    def dsmc_gpuform(self, q, vel1, cnt1, vel2, cnt2, dt, svmax, seed, call, tag):
+        """The GPU form on velocities in cell order (updated in place); returns (collisions, pairs, svmax_step)."""
+        pairs, mx = C.c_long(0), C.c_double(0)
+        c1 = np.ascontiguousarray(cnt1, np.int32)
+        c2 = None if cnt2 is None else np.ascontiguousarray(cnt2, np.int32)
+        nc = self.lib.or_dsmc_gpuform(C.byref(q), _p(vel1), _p(c1), _p(vel2), _p(c2), len(c1), dt, svmax,
+                                      seed & 0xffffffff, (seed >> 32) & 0xffffffff, call, tag, C.byref(pairs),
+                                      C.byref(mx))
+        return nc, pairs.value, mx.value
+
     def merge_ref(self, g, r, parts, n, ef, charge, mass, dt, min_count=10):
         return self.lib.or_merge_ref(C.byref(g), C.byref(r), _p(parts), n, len(parts),
                                      _p(np.ascontiguousarray(ef, np.float64)), charge, mass, dt, min_count)
@@ -319,6 +350,9 @@ class Ref:
                 "ref_compute_ef": (None, [vp]),
                 "ref_mcmex_create": (i, [vp, i, i, i, cp_]),
                 "ref_mcmex_apply": (None, [vp, d]),
+                "ref_dsmc_create": (i, [vp, i, i]),
+                "ref_dsmc_apply": (None, [vp, d]),
+                "ref_dsmc_svmax": (d, [vp]),
             }
             for name, (res, args) in sig.items():
                 f = getattr(L, name)

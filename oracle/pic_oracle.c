@@ -1528,3 +1528,131 @@ void or_sums(const or_particle* p, long n, double mass, double* count, double mo
     for (int d = 0; d < 3; d++) mom[d] = m[d] * mass;
     *ke = k * mass * 0.5;
 }
+
+/* ---- DSMC_MEX (Interactions.cpp:143-284) ---- */
+void or_dsmc_params_init(or_dsmc_params* q, const or_grid* g, double mass1, double mass2, double mpw0) {
+    q->mass1 = mass1;
+    q->mass2 = mass2;
+    q->mpw0 = mpw0;
+    q->dv = g->dx[0] * g->dx[1] * g->dx[2];
+    double m_red = mass1 * mass2 / (mass1 + mass2);
+    q->c[0] = 4.07e-10; /* Bird's VHS reference diameter and viscosity index, at 273.15 K */
+    q->c[1] = 0.77;
+    q->c[2] = 2 * OR_KB * 273.15 / m_red;
+    q->c[3] = tgamma(2.5 - q->c[1]);
+}
+double or_dsmc_sigma(const or_dsmc_params* q, double v_rel) {
+    return OR_PI * q->c[0] * q->c[0] * pow(q->c[2] / (v_rel * v_rel), q->c[1] - 0.5) / q->c[3];
+}
+/* DSMC_MEX::collide (Interactions.cpp:264-284): isotropic scattering in the centre-of-mass frame */
+static void dsmc_collide_ref(const or_dsmc_params* q, or_mt* r, double v1[3], double v2[3]) {
+    double sum_mass = q->mass1 + q->mass2, inv = 1.0 / sum_mass;
+    double cm[3], vr[3];
+    for (int d = 0; d < 3; d++) cm[d] = (v1[d] * q->mass1 + v2[d] * q->mass2) * inv;
+    for (int d = 0; d < 3; d++) vr[d] = v1[d] - v2[d];
+    double mag = len3(vr);
+    double cos_ksi = 2 * or_mt_u01(r) - 1;
+    double sin_ksi = sqrt(1 - cos_ksi * cos_ksi);
+    double eps = 2 * OR_PI * or_mt_u01(r);
+    vr[0] = mag * cos_ksi;
+    vr[1] = mag * sin_ksi * cos(eps);
+    vr[2] = mag * sin_ksi * sin(eps);
+    double f2 = q->mass2 / sum_mass, f1 = q->mass1 / sum_mass;
+    for (int d = 0; d < 3; d++) {
+        v1[d] = cm[d] + vr[d] * f2;
+        v2[d] = cm[d] - vr[d] * f1;
+    }
+}
+long or_dsmc_ref(const or_grid* g, const or_dsmc_params* q, or_mt* r, or_particle* p1, long n1, or_particle* p2,
+                 long n2, double dt, double* svmax, long* pairs) {
+    int one = p2 == NULL;
+    long nc = (long)(g->ni - 1) * (g->nj - 1) * (g->nk - 1);
+    ilist* C1 = sort_indexes(g, p1, n1);
+    ilist* C2 = one ? C1 : sort_indexes(g, p2, n2);
+    or_particle* q2 = one ? p1 : p2;
+    double sv_tmp = 0;
+    long n_coll = 0, n_pairs = 0;
+    for (long c = 0; c < nc; c++) {
+        int a = (int)C1[c].n, b = (int)C2[c].n;
+        if (one ? a < 2 : (a < 1 || b < 1)) continue;
+        double frac = 0.5 * a * b * q->mpw0 * *svmax * dt / q->dv;
+        int n_groups = (int)(frac + 0.5);
+        for (int gi = 0; gi < n_groups; gi++) {
+            int i1 = (int)(or_mt_u01(r) * a);
+            int i2 = (int)(or_mt_u01(r) * b);
+            while (one && i1 == i2) i2 = (int)(or_mt_u01(r) * b);
+            double* v1 = p1[C1[c].idx[i1]].vel;
+            double* v2 = q2[C2[c].idx[i2]].vel;
+            double vr[3] = {v1[0] - v2[0], v1[1] - v2[1], v1[2] - v2[2]};
+            double v_rel = len3(vr);
+            double sv = or_dsmc_sigma(q, v_rel) * v_rel;
+            if (sv > sv_tmp) sv_tmp = sv;
+            double P = sv / *svmax;
+            n_pairs++;
+            if (P > or_mt_u01(r)) {
+                n_coll++;
+                dsmc_collide_ref(q, r, v1, v2);
+            }
+        }
+    }
+    if (n_coll) *svmax = sv_tmp;
+    if (pairs) *pairs = n_pairs;
+    free_cells(C1, nc);
+    if (!one) free_cells(C2, nc);
+    return n_coll;
+}
+long or_dsmc_gpuform(const or_dsmc_params* q, double* vel1, const int32_t* cnt1, double* vel2, const int32_t* cnt2,
+                     long nc, double dt, double svmax, uint32_t seed_lo, uint32_t seed_hi, uint32_t call,
+                     uint32_t tag, long* pairs, double* svmax_step) {
+    int one = vel2 == NULL;
+    const uint32_t key[2] = {seed_lo, seed_hi};
+    /* sigma(g) g = pi d^2 (c2/g^2)^(omega-1/2) / Gamma * g = K (g^2)^(1-omega); the kernel's
+     * constants are FP32 roundings of the FP64 parameters */
+    double K = (float)(OR_PI * q->c[0] * q->c[0] * pow(q->c[2], q->c[1] - 0.5) / q->c[3]);
+    double ex = (float)(1.0 - q->c[1]);
+    double f1 = (float)(q->mass1 / (q->mass1 + q->mass2)), f2 = (float)(q->mass2 / (q->mass1 + q->mass2));
+    double half_coef = 0.5 * q->mpw0 * dt / q->dv;
+    long s1 = 0, s2 = 0, n_coll = 0, n_pairs = 0;
+    double mx = 0;
+    for (long c = 0; c < nc; c++) {
+        int a = cnt1[c], b = one ? a : cnt2[c];
+        double* w1 = vel1 + 3 * s1;
+        double* w2 = one ? w1 : vel2 + 3 * s2;
+        s1 += a;
+        if (!one) s2 += b;
+        if (one ? a < 2 : (a < 1 || b < 1)) continue;
+        double frac = (double)a * (double)b * (half_coef * svmax);
+        int n_groups = (int)(frac + 0.5);
+        for (int gi = 0; gi < n_groups; gi++) {
+            uint32_t ctr[4] = {(uint32_t)c, call, tag, (uint32_t)gi}, rr[4];
+            or_philox4x32_10(ctr, key, rr);
+            uint32_t i1 = (uint32_t)(((uint64_t)rr[0] * (uint32_t)a) >> 32);
+            uint32_t i2 = (uint32_t)(((uint64_t)rr[1] * (uint32_t)(one ? a - 1 : b)) >> 32);
+            if (one && i2 >= i1) i2++;
+            double* v1 = w1 + 3 * i1;
+            double* v2 = w2 + 3 * i2;
+            double d[3] = {v1[0] - v2[0], v1[1] - v2[1], v1[2] - v2[2]};
+            double g2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+            double sv = K * pow(g2, ex);
+            if (sv > mx) mx = sv;
+            n_pairs++;
+            if (!(sv > or_u01_from_u32(rr[2]) * svmax)) continue;
+            n_coll++;
+            uint32_t ctr2[4] = {(uint32_t)c, call, tag | 0x00800000u, (uint32_t)gi}, qq[4];
+            or_philox4x32_10(ctr2, key, qq);
+            double ck = 2 * or_u01_from_u32(rr[3]) - 1;
+            double sk = sqrt(fmax(1 - ck * ck, 0.0));
+            double eps = 2 * 3.14159265358979323846 * or_u01_from_u32(qq[0]);
+            double gm = sqrt(g2);
+            double vr[3] = {gm * ck, gm * sk * cos(eps), gm * sk * sin(eps)};
+            for (int k = 0; k < 3; k++) {
+                double cm = f1 * v1[k] + f2 * v2[k];
+                v1[k] = cm + f2 * vr[k];
+                v2[k] = cm - f1 * vr[k];
+            }
+        }
+    }
+    if (pairs) *pairs = n_pairs;
+    if (svmax_step) *svmax_step = mx;
+    return n_coll;
+}

@@ -153,6 +153,31 @@ long or_load_box_thermal_ref(const or_grid* g, or_mt* r, or_particle* p, long ca
 void or_sample_moments_ref(const or_grid* g, const or_particle* p, long n, double* mom);
 void or_gas_properties_ref(const or_grid* g, const double* mom, double mass, double* vel, double* T);
 
+/* ---- DSMC_MEX: VHS particle-particle collisions (Interactions.cpp:143-284) ---- */
+typedef struct {
+    double mass1, mass2, mpw0, dv; /* dv: cell volume dx dy dz (World::getCellVolume, World.cpp:101) */
+    double c[4];                   /* d_ref, omega, 2 k 273.15 / m_r, Gamma(2.5 - omega) (Interactions.cpp:152-156) */
+} or_dsmc_params;
+void or_dsmc_params_init(or_dsmc_params* q, const or_grid* g, double mass1, double mass2, double mpw0);
+double or_dsmc_sigma(const or_dsmc_params* q, double v_rel); /* DSMC_MEX::evaluateSigma */
+
+/* DSMC_MEX::applyOneSpecies / applyTwoSpecies (p2 == NULL: one species), MT19937 draws in the
+ * reference's order; *svmax is the persistent (sigma v_rel)_max, updated in place.  Returns
+ * the collisions; *pairs receives the candidate pairs drawn. */
+long or_dsmc_ref(const or_grid* g, const or_dsmc_params* q, or_mt* r, or_particle* p1, long n1, or_particle* p2,
+                 long n2, double dt, double* svmax, long* pairs);
+
+/* GPU form (restated from the CUDA kernel, in FP64 on the same draws): particles of each
+ * species contiguous in cell order, cnt1/cnt2[nc] per cell (vel2/cnt2 NULL: one species);
+ * group gi of cell c draws Philox block (c, call, tag, gi) for the pair, the acceptance and
+ * cos(chi), and block (c, call, tag | 0x00800000, gi) for the azimuth of a collision;
+ * sigma v_rel is evaluated as K (v_rel^2)^(1-omega), K = pi d^2 c2^(omega-1/2) / Gamma.
+ * svmax is the FP32 majorant the kernel reads; *svmax_step receives the largest sigma v of
+ * the candidates (the next majorant when any pair collided).  Returns the collisions. */
+long or_dsmc_gpuform(const or_dsmc_params* q, double* vel1, const int32_t* cnt1, double* vel2, const int32_t* cnt2,
+                     long nc, double dt, double svmax, uint32_t seed_lo, uint32_t seed_hi, uint32_t call,
+                     uint32_t tag, long* pairs, double* svmax_step);
+
 /* conservation sums (Species.cpp:732-752) */
 void or_sums(const or_particle* p, long n, double mass, double* count, double mom[3], double* ke);
 

@@ -16,6 +16,7 @@
 //   MC_MEX_Ionization::apply                     ch4/v3/src/Interactions.cpp:567
 //   Species::merge                               ch4/v3/src/Species.cpp:1037
 //   Species::loadParticleBoxThermal              ch4/v3/src/Species.cpp:564
+//   DSMC_MEX(species[, species2], world) / apply   ch4/v3/src/Interactions.cpp:143-284
 // The global RNG `rnd` (ch4/v3/src/Rnd.cpp:18) is reseeded by assignment so
 // that runs are reproducible (the stock code seeds it from random_device).
 #include <memory>
@@ -39,6 +40,12 @@ struct RefSim {
     std::vector<Species> species;
     std::unique_ptr<PotentialSolver> solver;
     std::unique_ptr<MC_MEX_Ionization> mcmex;
+    std::unique_ptr<DSMC_MEX> dsmc;
+};
+// read access to the protected (sigma v_rel)_max, so that tests can follow its updates
+struct DsmcProbe : DSMC_MEX {
+    using DSMC_MEX::DSMC_MEX;
+    double svmax() const { return sigma_v_rel_max; }
 };
 std::ofstream g_null_sink;
 void quiet() {
@@ -216,5 +223,21 @@ int ref_mcmex_create(void* h, int neu, int ion, int ele, const char* table_path)
     return 0;
 }
 void ref_mcmex_apply(void* h, double dt) { static_cast<RefSim*>(h)->mcmex->apply(dt); }
+
+// sp2 < 0 or sp2 == sp1: the one-species constructor (Interactions.cpp:143), else the two-species one
+int ref_dsmc_create(void* h, int sp1, int sp2) {
+    RefSim* s = static_cast<RefSim*>(h);
+    try {
+        if (sp2 < 0 || sp2 == sp1)
+            s->dsmc = std::make_unique<DsmcProbe>(s->species[sp1], *s->world);
+        else
+            s->dsmc = std::make_unique<DsmcProbe>(s->species[sp1], s->species[sp2], *s->world);
+    } catch (const std::exception&) {
+        return -1;
+    }
+    return 0;
+}
+void ref_dsmc_apply(void* h, double dt) { static_cast<RefSim*>(h)->dsmc->apply(dt); }
+double ref_dsmc_svmax(void* h) { return static_cast<DsmcProbe*>(static_cast<RefSim*>(h)->dsmc.get())->svmax(); }
 
 }  // extern "C"

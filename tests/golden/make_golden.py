@@ -5,7 +5,7 @@ driven through ref_harness.cpp) on small seeded cases and stores inputs and outp
 files next to this script.  Needs the reference tree (PIC_REFERENCE_ROOT, default
 /root/reference); the fixtures themselves travel with the repository.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case ...]     (no case: all of them)
 """
 import ctypes as C
 import os
@@ -143,8 +143,46 @@ def case_merge():
     return out
 
 
+def case_dsmc():
+    """DSMC_MEX::apply (Interactions.cpp:143-284): one species three times, then two species twice.
+
+    The loads draw from the global RNG; it is reseeded (dsmc_seed) before the first apply so that a
+    restatement can start from the stored particles."""
+    nn, x0, xm = (5, 5, 5), (0.0, 0.0, 0.0), (0.004, 0.004, 0.004)
+    mpw0, dt = 3.2e10, 1e-5
+    R = O.Ref(nn, x0, xm)
+    R.seed(5)
+    a = R.species("O", 16 * O.AMU, 0.0, mpw0)
+    b = R.species("O2", 32 * O.AMU, 0.0, mpw0)
+    c, s = v3(0.002, 0.002, 0.002), v3(0.004, 0.004, 0.004)
+    R.L.ref_load_box_thermal(R.h, a, c, s, 1e21, 300.0)  # 2000 particles, ~31 per cell
+    R.L.ref_load_box_thermal(R.h, b, c, s, 1e21, 900.0)
+    out = dict(nn=np.array(nn), x0=np.array(x0), xm=np.array(xm), mpw0=np.array(mpw0), dt=np.array(dt),
+               dsmc_seed=np.array(77))
+    out.update({"a0_" + k: v for k, v in parts_arrays(R.get_particles(a)).items()})
+    out.update({"b0_" + k: v for k, v in parts_arrays(R.get_particles(b)).items()})
+    R.seed(77)
+    assert R.L.ref_dsmc_create(R.h, a, -1) == 0
+    for it in range(3):
+        R.L.ref_dsmc_apply(R.h, dt)
+        out[f"one{it + 1}_vel"] = R.get_particles(a)["vel"].copy()
+        out[f"one{it + 1}_svmax"] = np.array(R.L.ref_dsmc_svmax(R.h))
+    assert R.L.ref_dsmc_create(R.h, a, b) == 0
+    for it in range(2):
+        R.L.ref_dsmc_apply(R.h, dt)
+        out[f"two{it + 1}_vel_a"] = R.get_particles(a)["vel"].copy()
+        out[f"two{it + 1}_vel_b"] = R.get_particles(b)["vel"].copy()
+        out[f"two{it + 1}_svmax"] = np.array(R.L.ref_dsmc_svmax(R.h))
+    return out
+
+
 def main():
-    for name, fn in (("push_deposit", case_push_deposit), ("poisson", case_poisson), ("ntc", case_ntc), ("merge", case_merge)):
+    cases = (("push_deposit", case_push_deposit), ("poisson", case_poisson), ("ntc", case_ntc), ("merge", case_merge),
+             ("dsmc", case_dsmc))
+    only = set(sys.argv[1:])
+    for name, fn in cases:
+        if only and name not in only:
+            continue
         d = fn()
         path = os.path.join(HERE, name + ".npz")
         np.savez_compressed(path, **d)

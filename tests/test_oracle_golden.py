@@ -254,3 +254,28 @@ def test_learned_symmetrize_makes_the_preconditioner_symmetric():
     assert abs(np.vdot(x, B(y)) - np.vdot(y, B(x))) > 1e-3 * abs(np.vdot(x, B(y)))  # not symmetric yet
     LR.symmetrize(W, diags)
     assert abs(np.vdot(x, B(y)) - np.vdot(y, B(x))) <= 1e-10 * abs(np.vdot(x, B(y)))
+
+
+def test_dsmc_bit_exact(port):
+    """DSMC_MEX one species (three applies) and two species (two applies) against the reference."""
+    d = golden("dsmc")
+    g = port.grid(d["nn"], d["x0"], d["xm"])
+    mpw0, dt = float(d["mpw0"]), float(d["dt"])
+    a, b = to_parts(d, "a0_"), to_parts(d, "b0_")
+    mt = port.mt(int(d["dsmc_seed"]))
+    q = port.dsmc_params(g, 16 * O.AMU, 16 * O.AMU, mpw0)
+    sv = 1e-14  # DSMC_MEX::sigma_v_rel_max initial value (Interactions.h:58)
+    total = 0
+    for it in (1, 2, 3):
+        nc, pairs, sv = port.dsmc_ref(g, q, mt, a, None, dt, sv)
+        total += nc
+        assert pairs >= nc and np.array_equal(a["vel"], d[f"one{it}_vel"]), it
+        assert sv == float(d[f"one{it}_svmax"])
+    assert total > 100  # the case collides
+    q2 = port.dsmc_params(g, 16 * O.AMU, 32 * O.AMU, mpw0)
+    sv = 1e-14
+    for it in (1, 2):
+        nc, pairs, sv = port.dsmc_ref(g, q2, mt, a, b, dt, sv)
+        assert nc > 10
+        assert np.array_equal(a["vel"], d[f"two{it}_vel_a"]) and np.array_equal(b["vel"], d[f"two{it}_vel_b"]), it
+        assert sv == float(d[f"two{it}_svmax"])
