@@ -95,6 +95,8 @@ def library():
         "pic_mcc_apply": [vp, d],
         "pic_mcc_stats": [vp, vp],
         "pic_dsmc_create": [vp, i, i, u64, vp],
+        "pic_species_object_interaction": [vp, i, i, i, i, i, u64],
+        "pic_species_object_stats": [vp, i, vp],
         "pic_dsmc_apply": [vp, i, d],
         "pic_dsmc_stats": [vp, i, vp, vp],
         "pic_loop_configure": [vp, i, i, vp, i, i, i],
@@ -388,11 +390,37 @@ class Species:
         return pos[:got.value], vel[:got.value]
 
     def advance(self, dt, deposit=True):
+        """One push with the species' current object interaction (see set_object_interaction)."""
         _check(self._L.pic_species_push(self.world._h, self.id, float(dt), int(deposit)))
 
-    advanceElectrons = advance  # Species.cpp:258
+    def set_object_interaction(self, mode, neutrals=None, spherium=None, sputtering=False, seed=None):
+        """What a push does with particles that enter a box object: mode 0 removes them
+        (Species::advanceElectrons), mode 1 is Species::advanceNonElectron(neutrals, spherium):
+        neutral species bounce, ions are neutralised into `neutrals` (and sputter into
+        `spherium` when `sputtering`).  pic_step pushes with the mode set here."""
+        key = (int(mode), None if neutrals is None else neutrals.id, None if spherium is None else spherium.id,
+               bool(sputtering), seed)
+        if getattr(self, "_obj_key", None) == key:
+            return
+        seed = 0x0B1EC7 + 7919 * self.id if seed is None else int(seed)
+        _check(self._L.pic_species_object_interaction(self.world._h, self.id, int(mode), key[1] if key[1] is not None
+                                                      else -1, key[2] if key[2] is not None else -1,
+                                                      int(bool(sputtering)), seed))
+        self._obj_key = key
 
-    def advanceNonElectron(self, neutrals, spherium, dt, deposit=True):  # Species.cpp:47
+    def object_stats(self):
+        out = np.zeros(4, np.uint64)
+        _check(self._L.pic_species_object_stats(self.world._h, self.id, _p(out)))
+        return dict(impacts=int(out[0]), bounces=int(out[1]), neutrals_created=int(out[2]),
+                    sputtered_created=int(out[3]))
+
+    def advanceElectrons(self, dt, deposit=True):  # Species.cpp:258-399: objects absorb
+        self.set_object_interaction(0)
+        self.advance(dt, deposit)
+
+    def advanceNonElectron(self, neutrals, spherium, dt, deposit=True):  # Species.cpp:45-256
+        sput = Config.getInstance().getSPUTTERING()
+        self.set_object_interaction(1, neutrals, spherium, sput)
         self.advance(dt, deposit)
 
     def computeNumberDensity(self):
@@ -578,6 +606,27 @@ class LearnedPreconditioner:
         z = np.zeros_like(r)
         _check(self.world._L.pic_learned_apply(self.world._h, _p(r), _p(z)))
         return z
+
+
+class Config:
+    """The reference's Config singleton (ch4/v3/src/Config.h), for the switch the pushes read."""
+
+    _instance = None
+
+    def __init__(self):
+        self._sputtering = False
+
+    @classmethod
+    def getInstance(cls):
+        if cls._instance is None:
+            cls._instance = cls()
+        return cls._instance
+
+    def getSPUTTERING(self):
+        return self._sputtering
+
+    def setSPUTTERING(self, on):
+        self._sputtering = bool(on)
 
 
 class MC_MEX_Ionization:

@@ -62,6 +62,12 @@ struct SpeciesHost {
     double scale = 1.0;  // fixed-point scale of the density accumulator
     unsigned long long next_id = 0;
     bool deposited = false;
+    // object interaction of a push (0: absorbed, as Species::advanceElectrons; 1: the
+    // reference's advanceNonElectron(neutrals, spherium): neutrals bounce, ions are neutralised)
+    int obj_mode = 0;
+    int obj_neu = -1, obj_spu = -1, obj_sputtering = 0;
+    uint2 obj_key{0, 0};
+    unsigned long long* obj_stats = nullptr;  // hits, bounces, neutrals created, sputtered created
 };
 
 struct TimerAcc {
@@ -647,6 +653,7 @@ extern "C" int pic_world_destroy(pic_world* w) {
         cudaFree(s.den);
         cudaFree(s.den_avg);
         if (s.mom) cudaFree(s.mom);
+        if (s.obj_stats) cudaFree(s.obj_stats);
     }
     void* ptrs[] = {w->ef,   w->phi,  w->phi_alt, w->rho,        w->kind,       w->r,        w->e,
                     w->d,    w->d2,   w->q,       w->z,          w->part,       w->scal,     w->flag,
@@ -1114,10 +1121,49 @@ int push_species(pic_world* w, int sp, double dt, int deposit, bool with_mcc, bo
         ap.coll.enabled = 0;
         launch_push(ap, w->stream, w->grid_push);
     }
+    const bool objects = do_push && s.obj_mode == 1 && !w->boxes.empty();
+    if (objects) {
+        // the particles the push moved into an object (Species.cpp:211-235)
+        ObjArgs o{};
+        o.a = a;
+        o.a.coll.enabled = 0;
+        o.dt = dt;
+        o.mass = s.mass;
+        o.charged = s.charge != 0;
+        if (o.charged) {
+            const SpeciesHost& sn = w->sp[s.obj_neu];
+            o.neu = sn.dev;
+            o.neu_mpw0 = sn.mpw0;
+            o.neu_qm = sn.charge / sn.mass;
+            o.sputtering = s.obj_sputtering;
+            if (o.sputtering) {
+                const SpeciesHost& ss = w->sp[s.obj_spu];
+                o.spu = ss.dev;
+                o.spu_mpw0 = ss.mpw0;
+                o.spu_qm = ss.charge / ss.mass;
+            }
+            o.half_dt_global = 0.5 * w->dt;
+        }
+        o.n_boxes = (int)w->boxes.size();
+        for (int b = 0; b < o.n_boxes; b++)
+            for (int d = 0; d < 3; d++) {
+                o.box_c[b][d] = w->boxes[b].c[d];
+                o.box_half[b][d] = w->boxes[b].s[d] * 0.5;  // Rectangle::half_sides (Object.cpp:166-171)
+            }
+        o.key = s.obj_key;
+        o.step = (unsigned)w->ts;
+        o.stats = s.obj_stats;
+        Scope sc(w, "objects", 1);
+        launch_object_hits(o, w->stream, w->sms);
+    }
     {
-        Scope sc(w, "compact", a.coll.enabled ? 5 : 4);
+        const bool neu = objects && s.charge != 0 && s.obj_neu != sp;
+        const bool spu = objects && s.charge != 0 && s.obj_sputtering && s.obj_spu != s.obj_neu && s.obj_spu != sp;
+        Scope sc(w, "compact", (a.coll.enabled ? 5 : 4) + neu + spu);
         launch_commit_appends(s.dev, w->err, w->stream);
         if (a.coll.enabled) launch_commit_appends(w->sp[w->mcc_i].dev, w->err, w->stream);
+        if (neu) launch_commit_appends(w->sp[s.obj_neu].dev, w->err, w->stream);
+        if (spu) launch_commit_appends(w->sp[s.obj_spu].dev, w->err, w->stream);
         launch_compact(s.dev, w->stream, w->sms * 4);
     }
     return PIC_OK;
@@ -1130,6 +1176,42 @@ extern "C" int pic_species_push(pic_world* w, int sp, double dt, int deposit) {
     int rc = push_species(w, sp, dt, deposit, false, true);
     if (rc) return rc;
     CU(cudaGetLastError());
+    return PIC_OK;
+}
+
+extern "C" int pic_species_object_interaction(pic_world* w, int sp, int mode, int neutral_sp, int spherium_sp,
+                                              int sputtering, uint64_t seed) {
+    if (!valid_sp(w, sp) || (mode != 0 && mode != 1)) return fail(PIC_ERR_ARG, "bad species or mode");
+    SpeciesHost& s = w->sp[sp];
+    if (mode == 1 && s.charge != 0) {
+        if (!valid_sp(w, neutral_sp) || !(w->sp[neutral_sp].mpw0 > 0))
+            return fail(PIC_ERR_ARG, "an ion species needs a species with mpw0 > 0 to neutralise into");
+        if (sputtering && (!valid_sp(w, spherium_sp) || !(w->sp[spherium_sp].mpw0 > 0)))
+            return fail(PIC_ERR_ARG, "sputtering needs a species with mpw0 > 0 for the sputtered material");
+    }
+    CU(cudaSetDevice(w->device));
+    if (!s.obj_stats) {
+        CU(cudaMalloc((void**)&s.obj_stats, sizeof(unsigned long long) * 4));
+        CU(cudaMemsetAsync(s.obj_stats, 0, sizeof(unsigned long long) * 4, w->stream));
+    }
+    s.obj_mode = mode;
+    s.obj_neu = neutral_sp;
+    s.obj_spu = sputtering ? spherium_sp : -1;
+    s.obj_sputtering = sputtering ? 1 : 0;
+    s.obj_key = make_uint2((unsigned)seed, (unsigned)(seed >> 32));
+    return PIC_OK;
+}
+
+extern "C" int pic_species_object_stats(pic_world* w, int sp, uint64_t* out) {
+    if (!valid_sp(w, sp) || !out) return fail(PIC_ERR_ARG, "bad arguments");
+    CU(cudaSetDevice(w->device));
+    const SpeciesHost& s = w->sp[sp];
+    if (!s.obj_stats) {
+        for (int k = 0; k < 4; k++) out[k] = 0;
+        return PIC_OK;
+    }
+    CU(cudaMemcpyAsync(out, s.obj_stats, sizeof(unsigned long long) * 4, cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
     return PIC_OK;
 }
 

@@ -136,6 +136,9 @@ __device__ __forceinline__ void set_error(unsigned* err, unsigned bit) {
 // c = (k*(nj-1) + j)*(ni-1) + i of World::XtoC, which the sort and the cell lists use.
 constexpr int kCellMaxIJ = 512, kCellMaxK = 8192;
 __host__ __device__ __forceinline__ int pack_cell(int i, int j, int k) { return i | (j << 9) | (k << 18); }
+// marks the packed cell of a particle that moved into an object during a push (the value is
+// negative, so the particle is removed unless the object interaction re-creates it)
+constexpr int kHitFlag = (int)0x80000000u;
 __device__ __forceinline__ void cell_ijk(const GridDev&, int c, int& i, int& j, int& k) {
     i = c & 511;
     j = (c >> 9) & 511;

@@ -84,6 +84,28 @@ struct SourceArgs {
 };
 void launch_source(const SourceArgs& sa, double* pos, double* vel, double* w, cudaStream_t s);
 
+// Object interaction of a non-electron species (Species::advanceNoSputteringSerial and
+// advanceSputteringSerial, Species.cpp:79-256) for the particles the last push flagged with
+// kHitFlag: neutrals bounce diffusely off the object, ions are removed and leave neutrals
+// (and, with sputtering, sputtered particles) at the impact point.  FP64, one thread per hit.
+struct ObjArgs {
+    PushArgs a;                 // the pushed species, its deposit settings and the grid
+    double dt;                  // time step of that push
+    double mass;                // the pushed species' mass (Species::sampleVth)
+    int charged;                // ions are neutralised, neutrals bounce
+    SpeciesDev neu, spu;        // neutral and sputtered-material species (charged species only)
+    double neu_mpw0, spu_mpw0;  // their macroparticle weights (Species::addParticle(pos, vel))
+    double neu_qm, spu_qm;      // their charge / mass, for addParticle's half-step rewind
+    double half_dt_global;      // 0.5 World::getDt()
+    int sputtering;             // Config::SPUTTERING
+    int n_boxes;
+    double box_c[kMaxBoxes][3], box_half[kMaxBoxes][3];  // Rectangle pos and half_sides
+    uint2 key;                  // Philox key (seed)
+    unsigned step;              // counter word
+    unsigned long long* stats;  // [0] hits, [1] bounces, [2] neutrals created, [3] sputtered created
+};
+void launch_object_hits(const ObjArgs& o, cudaStream_t s, int grid);
+
 // DSMC_MEX on sorted species: cell c of species k owns particles [start_k[c], start_k[c+1])
 // (the last cell ends at the species count *n_k); vel2 == vel1 and one = 1 for one species
 struct DsmcArgs {

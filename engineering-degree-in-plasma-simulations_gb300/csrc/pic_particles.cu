@@ -163,7 +163,9 @@ __device__ __forceinline__ float3 gather_e(const PushArgs& a, const Tile& t, int
 }
 
 // advance offsets by v dt/dx, move across cells, wrap periodic axes; returns the new packed
-// cell or -1 when the particle leaves the domain or enters an absorbing object
+// cell, -1 when the particle leaves the domain, or the packed cell with kHitFlag set (also
+// negative, so the particle counts as removed) when it enters an object: k_object_hits then
+// applies the reference's object interaction to it, and without one the object absorbs it
 __device__ __forceinline__ int move_particle(const PushArgs& a, int i, int j, int k, float3& o, float3 v) {
     const GridDev& g = a.g;
     const float kBelowOne = 0x1.fffffep-1f;
@@ -186,7 +188,7 @@ __device__ __forceinline__ int move_particle(const PushArgs& a, int i, int j, in
         for (int bx = 0; bx < g.n_boxes; bx++)
             if (X >= g.box_lo[bx][0] && X <= g.box_hi[bx][0] && Y >= g.box_lo[bx][1] && Y <= g.box_hi[bx][1] &&
                 Z >= g.box_lo[bx][2] && Z <= g.box_hi[bx][2])
-                return -1;
+                return pack_cell(i, j, k) | kHitFlag;
     }
     return pack_cell(i, j, k);
 }
@@ -1106,6 +1108,273 @@ void launch_source(const SourceArgs& sa, double* pos, double* vel, double* w, cu
     if (grid < 1) grid = 1;
     k_source<<<grid, 256, 0, s>>>(sa, pos, vel, w);
 }
+
+// ------------------------------------------------------------------------------------
+// Object interaction (Species.cpp:79-256, Object.cpp:231-275, Species.cpp:835-861), FP64.
+// A particle's draws come from one Philox-4x32-10 stream keyed by (id, step, 0x0B000000 + block),
+// taken in the order of the reference's rnd() calls.
+// ------------------------------------------------------------------------------------
+namespace {
+constexpr double kKbRef = 1.380648e-23;  // Const::k, ch4/v3/src/all.h:19
+constexpr double kPiRef = 3.141592653;   // Const::pi, ch4/v3/src/all.h:20
+struct DrawStream {
+    uint4 ctr;
+    uint2 key;
+    uint4 buf;
+    int pos;
+    __device__ DrawStream(unsigned long long id, unsigned step, uint2 k)
+        : ctr(make_uint4((unsigned)id, (unsigned)(id >> 32), step, 0x0B000000u)), key(k), pos(4) {}
+    __device__ double next() {
+        if (pos == 4) {
+            buf = philox4x32_10(ctr, key);
+            ctr.w++;
+            pos = 0;
+        }
+        const unsigned x = pos == 0 ? buf.x : pos == 1 ? buf.y : pos == 2 ? buf.z : buf.w;
+        pos++;
+        return (double)u01(x);
+    }
+};
+// World::inObject over Rectangle::inObject (World.cpp:293-301, Object.cpp:231-238): object index + 1
+__device__ int in_object_d(const ObjArgs& o, const double x[3]) {
+    for (int b = 0; b < o.n_boxes; b++) {
+        bool in = true;
+        for (int d = 0; d < 3; d++)
+            if (fabs(x[d] - o.box_c[b][d]) > o.box_half[b][d]) in = false;
+        if (in) return b + 1;
+    }
+    return 0;
+}
+__device__ void add_side_normal(int side, double n[3]) {  // Rectangle::find_n (Object.cpp:277-302)
+    n[side % 3] += side < 3 ? -1.0 : 1.0;
+}
+// Rectangle::lineIntersect (Object.cpp:239-275): entry time along x1 -> x2, entry point, normal
+__device__ void line_intersect_d(const ObjArgs& o, int b, const double x1[3], const double x2[3], double& t_entry,
+                                 double xi[3], double n[3]) {
+    double tmin[3], tmax[3];
+    int ps[3] = {0, 1, 2};
+    for (int d = 0; d < 3; d++) {
+        const double A = x2[d] - x1[d];
+        tmin[d] = (o.box_c[b][d] - o.box_half[b][d] - x1[d]) / A;
+        tmax[d] = (o.box_c[b][d] + o.box_half[b][d] - x1[d]) / A;
+        if (tmin[d] > tmax[d]) {
+            const double t = tmin[d];
+            tmin[d] = tmax[d];
+            tmax[d] = t;
+            ps[d] += 3;
+        }
+    }
+    t_entry = tmin[0];
+    int j = 0, k = 0, t = 0;
+    for (int i = 0; i < 2; i++) {
+        if (t_entry < tmin[i + 1]) {
+            t_entry = tmin[i + 1];
+            j = i + 1;
+            k = 0;
+        } else if (fabs(t_entry - tmin[i + 1]) < 1e-6) {
+            k++;
+            t = i + 1;
+        }
+    }
+    n[0] = n[1] = n[2] = 0.0;
+    add_side_normal(ps[j], n);
+    if (k != 0) {  // an edge or a vertex: the sum of the faces' normals, normalised
+        if (k < 2) {
+            add_side_normal(ps[t], n);
+        } else {
+            add_side_normal(ps[2], n);
+            add_side_normal(ps[1], n);
+        }
+        const double inv = 1.0 / sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+        for (int d = 0; d < 3; d++) n[d] *= inv;
+    }
+    for (int d = 0; d < 3; d++) xi[d] = x1[d] + (x2[d] - x1[d]) * t_entry;
+}
+// Species::sampleReflectedVelocity (Species.cpp:835-853) with sampleVth(300) (855-861): full
+// thermal accommodation at 300 K, direction from the reference's diffuse vector (whose t2 term
+// carries no sin(theta) factor, kept as it is)
+__device__ void reflect_d(double mass, double v_mag1, const double n[3], DrawStream& r, double out[3]) {
+    const double v_th0 = sqrt(2 * kKbRef * 300.0 / mass);
+    double s3[3];
+    for (int d = 0; d < 3; d++) {
+        const double u1 = r.next(), u2 = r.next(), u3 = r.next();
+        s3[d] = v_th0 * (u1 + u2 + u3 - 1.5);
+    }
+    const double v_th = sqrt(s3[0] * s3[0] + s3[1] * s3[1] + s3[2] * s3[2]);
+    const double v_mag2 = v_mag1 + 1.0 * (v_th - v_mag1);
+    const double sin_theta = r.next();
+    const double cos_theta = sqrt(1 - sin_theta * sin_theta);
+    const double psi = 2 * kPiRef * r.next();
+    double t1[3];
+    if (n[0] != 0) {  // n x (1,0,0)
+        t1[0] = 0.0;
+        t1[1] = n[2];
+        t1[2] = -n[1];
+    } else {  // n x (0,1,0)
+        t1[0] = -n[2];
+        t1[1] = 0.0;
+        t1[2] = n[0];
+    }
+    const double t2[3] = {n[1] * t1[2] - n[2] * t1[1], n[2] * t1[0] - n[0] * t1[2], n[0] * t1[1] - n[1] * t1[0]};
+    const double a = sin_theta * cos(psi), b = sin(psi);
+    for (int d = 0; d < 3; d++) out[d] = (t1[d] * a + t2[d] * b + n[d] * cos_theta) * v_mag2;
+}
+__device__ bool in_bounds_d(const GridDev& g, const double x[3]) {  // World::inBounds (World.cpp:201-205)
+    for (int d = 0; d < 3; d++)
+        if (x[d] < g.x0[d] || x[d] >= g.xm[d]) return false;
+    return true;
+}
+// an absolute position as (offsets, packed cell), as the upload path converts it
+__device__ float4 to_cell(const GridDev& g, const double x[3]) {
+    const int nc3[3] = {g.ci, g.cj, g.ck};
+    int ijk[3];
+    float o[3];
+    for (int d = 0; d < 3; d++) {
+        const double lc = (x[d] - g.x0[d]) / g.dxd[d];
+        int c = (int)lc;
+        if (c >= nc3[d]) c = nc3[d] - 1;
+        ijk[d] = c;
+        o[d] = fminf((float)(lc - c), 0x1.fffffep-1f);
+    }
+    return make_float4(o[0], o[1], o[2], __int_as_float(pack_cell(ijk[0], ijk[1], ijk[2])));
+}
+// ids of the particles an impact creates: distinct from the parent's and from the merge's
+__device__ unsigned long long obj_child_id(unsigned long long parent, unsigned step, unsigned k) {
+    return mix64(child_id(parent, step, 3) + (unsigned long long)(k + 1) * 0xD1B54A32D192ED03ull);
+}
+// Field::gather of E at an absolute position in FP64 (Field.h:200-232, World::XtoL)
+__device__ void gather_e_d(const GridDev& g, const float4* ef, const double x[3], double e[3]) {
+    double f[3];
+    int c[3];
+    const int nc3[3] = {g.ci, g.cj, g.ck};
+    for (int d = 0; d < 3; d++) {
+        const double lc = (x[d] - g.x0[d]) * (1.0 / g.dxd[d]);
+        c[d] = min((int)lc, nc3[d] - 1);
+        f[d] = lc - c[d];
+    }
+    e[0] = e[1] = e[2] = 0.0;
+    for (int c8 = 0; c8 < 8; c8++) {
+        const int a = c8 & 1, b = (c8 >> 1) & 1, k = c8 >> 2;
+        const double wt = (a ? f[0] : 1 - f[0]) * (b ? f[1] : 1 - f[1]) * (k ? f[2] : 1 - f[2]);
+        const float4 E = ef[cell_base_node(g, c[0] + a, c[1] + b, c[2] + k)];
+        e[0] += wt * E.x;
+        e[1] += wt * E.y;
+        e[2] += wt * E.z;
+    }
+}
+// Species::addParticle(pos, vel) (Species.cpp:420-434): NaN, bounds and objects rejected (a
+// point on an object's surface counts as inside, Object.cpp:235), then v -= q/m E dt/2
+__device__ bool add_neutral(const ObjArgs& o, const SpeciesDev& sp, double qm, int n0, const double x[3],
+                            const double v[3], double w, unsigned long long id) {
+    for (int d = 0; d < 3; d++)
+        if (isnan(x[d]) || isnan(v[d])) return false;
+    if (!in_bounds_d(o.a.g, x) || in_object_d(o, x)) return false;
+    double vr[3] = {v[0], v[1], v[2]};
+    if (qm != 0.0) {
+        double e[3];
+        gather_e_d(o.a.g, o.a.ef, x, e);
+        for (int d = 0; d < 3; d++) vr[d] -= e[d] * qm * o.half_dt_global;
+    }
+    return append_particle(sp, n0, to_cell(o.a.g, x), make_float4((float)vr[0], (float)vr[1], (float)vr[2], (float)w),
+                           id, o.a.err);
+}
+
+__global__ void __launch_bounds__(128) k_object_hits(ObjArgs o) {
+    const GridDev& g = o.a.g;
+    const SpeciesDev& sp = o.a.sp;
+    const int nd = sp.counts[2], n_self = sp.counts[0];
+    const int n_neu = o.charged ? o.neu.counts[0] : 0, n_spu = o.charged && o.sputtering ? o.spu.counts[0] : 0;
+    unsigned long long st[4] = {0, 0, 0, 0};
+    for (int d = blockIdx.x * blockDim.x + threadIdx.x; d < nd; d += gridDim.x * blockDim.x) {
+        const int p = sp.dead[d];
+        const float4 P = sp.pos[p];
+        const int c = __float_as_int(P.w);
+        if (c >= 0 || c == -1) continue;  // alive, or left the domain
+        int ijk[3];
+        cell_ijk(g, c & ~kHitFlag, ijk[0], ijk[1], ijk[2]);
+        const float4 V = sp.vel[p];
+        const unsigned long long id = sp.id[p];
+        const double w = V.w;
+        const float off[3] = {P.x, P.y, P.z};
+        double v[3] = {V.x, V.y, V.z}, x1[3], x2[3];
+        for (int k = 0; k < 3; k++) {
+            x2[k] = g.x0[k] + ((double)ijk[k] + (double)off[k]) * g.dxd[k];
+            x1[k] = x2[k] - v[k] * o.dt;  // the start of the push's move
+        }
+        st[0]++;
+        DrawStream r(id, o.step, o.key);
+        double t_rem = 1.0;
+        int n_bounces = 1;  // the push made the first move
+        bool alive = true;
+        while (true) {
+            const int obj = in_object_d(o, x2);
+            if (!obj) break;  // FP32 said inside, FP64 says outside: the move stands
+            double tp, xi[3], nrm[3];
+            line_intersect_d(o, obj - 1, x1, x2, tp, xi, nrm);
+            const double vmag = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+            if (!o.charged) {  // neutrals bounce (Species.cpp:221-223)
+                reflect_d(o.mass, vmag, nrm, r, v);
+                st[1]++;
+                t_rem *= (1 - tp);
+                if (++n_bounces > 20) {
+                    alive = false;
+                    break;
+                }
+                for (int k = 0; k < 3; k++) {
+                    x1[k] = xi[k];
+                    x2[k] = xi[k] + v[k] * t_rem * o.dt;
+                    if (g.periodic[k]) {
+                        const double L = g.xm[k] - g.x0[k];
+                        if (x2[k] < g.x0[k]) x2[k] += L;
+                        else if (x2[k] >= g.xm[k]) x2[k] -= L;
+                    }
+                }
+                if (!in_bounds_d(g, x2)) {
+                    alive = false;
+                    break;
+                }
+                continue;
+            }
+            // ions: neutrals of the neutral species' weight at the impact point (Species.cpp:225-235)
+            const int m = (int)(w / o.neu_mpw0 + r.next());
+            for (int q = 0; q < m; q++) {
+                double vn[3];
+                reflect_d(o.mass, vmag, nrm, r, vn);
+                st[2] += add_neutral(o, o.neu, o.neu_qm, n_neu, xi, vn, o.neu_mpw0, obj_child_id(id, o.step, (unsigned)q));
+            }
+            if (o.sputtering) {  // simple yield model (Species.cpp:136-144)
+                const double yield = vmag > 5e3 ? 0.1 : 0.0;
+                const int ms = (int)(yield * w / o.spu_mpw0 + r.next());
+                for (int q = 0; q < ms; q++) {
+                    double vn[3];
+                    reflect_d(o.mass, vmag, nrm, r, vn);
+                    st[3] += add_neutral(o, o.spu, o.spu_qm, n_spu, xi, vn, o.spu_mpw0,
+                                         obj_child_id(id, o.step, 0x10000000u + (unsigned)q));
+                }
+            }
+            alive = false;
+            break;
+        }
+        if (!alive) continue;
+        // the particle lives on: re-created at its final position with its id, and deposited
+        const float4 np = to_cell(g, x2);
+        if (!append_particle(sp, n_self, np, make_float4((float)v[0], (float)v[1], (float)v[2], V.w), id, o.a.err))
+            continue;
+        if (o.a.deposit) {
+            Corners hc;
+            corner_values(V.w, make_float3(np.x, np.y, np.z), o.a.dep_scale, hc, false);
+            const int b = cell_base(g, __float_as_int(np.w));
+            const int offs[4] = {0, g.ni, g.ni * g.nj, g.ni * g.nj + g.ni};
+            for (int c8 = 0; c8 < 8; c8++)
+                if (hc.q[c8]) atomicAdd(&sp.acc[b + offs[c8 >> 1] + (c8 & 1)], hc.q[c8]);
+        }
+    }
+    for (int k = 0; k < 4; k++)
+        if (st[k]) atomicAdd(&o.stats[k], st[k]);
+}
+}  // namespace
+
+void launch_object_hits(const ObjArgs& o, cudaStream_t s, int grid) { k_object_hits<<<grid, 128, 0, s>>>(o); }
 
 __global__ void k_load_count(SpeciesDev sp, int n) {
     int nn = sp.counts[0] + n;

@@ -49,7 +49,8 @@ int pic_world_get_time(pic_world* w, double* time);
  * on every non-periodic face (World::inBounds, World.cpp:201-205). */
 int pic_world_set_boundaries(pic_world* w, const int* periodic, const int* face_mode, const double* face_phi);
 /* World::addObject<Rectangle>(pos, phi, sides) + computeObjectID     World.h:118-130, Object.cpp:231-238:
- * nodes inside the box are Dirichlet at phi; particles entering it are absorbed. */
+ * nodes inside the box are Dirichlet at phi; particles entering it are absorbed, or bounce and
+ * are neutralised as pic_species_object_interaction sets. */
 /* Stacked independent instances (no reference counterpart): the z nodes split into nslabs equal
  * slabs; each slab is one instance whose first and last node planes are Dirichlet electrodes at
  * phi_lo[s] and phi_hi[s] (the reference's cathode/anode planes), and the cell between two slabs
@@ -104,6 +105,19 @@ int pic_species_sample_particles(pic_world* w, int sp, long num_out, double* pos
  * One leapfrog push; with deposit = 1 the weight is also scattered at the new position, which
  * is Species::computeNumberDensity (Species.cpp:401-416) fused into the push. */
 int pic_species_push(pic_world* w, int sp, double dt, int deposit);
+/* What a push does with particles that enter a box object (pic_world_add_box).
+ * mode 0 (default): they are removed, as in Species::advanceElectrons (Species.cpp:369-388).
+ * mode 1: Species::advanceNonElectron(neutrals, spherium, dt) (Species.cpp:45-256): a neutral
+ * species (charge 0) bounces diffusely off the object (sampleReflectedVelocity, full
+ * accommodation at 300 K, Species.cpp:835-861), up to 20 moves per push; an ion is removed and
+ * leaves (int)(w / mpw0_n + u) particles of neutral_sp at the impact point, plus, with
+ * sputtering (Config::SPUTTERING), (int)(0.1 w / mpw0_s + u) of spherium_sp when it hit faster
+ * than 5 km/s; both are added with Species::addParticle semantics (bounds and objects checked,
+ * the target species' half-step rewind).  Draws: Philox streams keyed by (seed, particle id, step). */
+int pic_species_object_interaction(pic_world* w, int sp, int mode, int neutral_sp, int spherium_sp, int sputtering,
+                                   uint64_t seed);
+/* counters since mode 1 was set: impacts, bounces, neutrals created, sputtered particles created */
+int pic_species_object_stats(pic_world* w, int sp, uint64_t* out);
 /* Species::computeNumberDensity() alone (deposit without moving)      Species.cpp:401-416 */
 int pic_species_number_density(pic_world* w, int sp);
 /* Species::den (public field) after pic_charge_density                Species.h:49 */

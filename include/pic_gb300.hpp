@@ -166,8 +166,20 @@ public:
                      uint64_t seed) {
         check(pic_species_load_uniform(world_->handle(), id_, lo.data(), hi.data(), n, T, w_mean, w_sigma, seed));
     }
-    void advanceElectrons(type_calc dt) { check(pic_species_push(world_->handle(), id_, dt, 1)); }
-    void advanceNonElectron(Species&, Species&, type_calc dt) { check(pic_species_push(world_->handle(), id_, dt, 1)); }
+    // objects absorb electrons (Species.cpp:369-388)
+    void advanceElectrons(type_calc dt) {
+        setObjectInteraction(0, -1, -1, false);
+        check(pic_species_push(world_->handle(), id_, dt, 1));
+    }
+    // neutrals bounce off objects, ions are neutralised into `neutrals` and, with
+    // Config::SPUTTERING, sputter into `spherium` (Species.cpp:45-256)
+    void advanceNonElectron(Species& neutrals, Species& spherium, type_calc dt);
+    // counters of mode 1: impacts, bounces, neutrals created, sputtered particles created
+    std::array<uint64_t, 4> objectStats() const {
+        std::array<uint64_t, 4> s{};
+        check(pic_species_object_stats(world_->handle(), id_, s.data()));
+        return s;
+    }
     void computeNumberDensity() { check(pic_species_number_density(world_->handle(), id_)); }
     void updateAverages() { check(pic_species_update_averages(world_->handle(), id_)); }
     void sortIndexes() { check(pic_species_sort(world_->handle(), id_, nullptr)); }
@@ -231,9 +243,41 @@ private:
         check(pic_species_sums(world_->handle(), id_, s.data()));
         return s;
     }
+    void setObjectInteraction(int mode, int neu, int spu, bool sputtering) {
+        const std::array<int, 4> key{mode, neu, spu, sputtering ? 1 : 0};
+        if (key == obj_key_) return;
+        check(pic_species_object_interaction(world_->handle(), id_, mode, neu, spu, sputtering ? 1 : 0,
+                                             0x0B1EC7ull + 7919ull * (uint64_t)id_));
+        obj_key_ = key;
+    }
     World* world_;
     int id_ = -1;
+    std::array<int, 4> obj_key_{0, -1, -1, 0};
 };
+
+// the reference's configuration singleton (ch4/v3/src/Config.h:6-45), for the switch the pushes read
+class Config {
+public:
+    static Config& getInstance() {
+        static Config c;
+        return c;
+    }
+    bool setSPUTTERING(bool option) {
+        sputtering_ = option;
+        return sputtering_;
+    }
+    bool getSPUTTERING() const { return sputtering_; }
+
+private:
+    bool sputtering_ = false;
+};
+
+inline void Species::advanceNonElectron(Species& neutrals, Species& spherium, type_calc dt) {
+    const bool sput = Config::getInstance().getSPUTTERING();
+    setObjectInteraction(1, charge != 0 ? neutrals.id() : -1, charge != 0 && sput ? spherium.id() : -1,
+                         charge != 0 && sput);
+    check(pic_species_push(world_->handle(), id_, dt, 1));
+}
 
 namespace detail {
 inline Species& sp_ref(Species& s) { return s; }

@@ -70,6 +70,14 @@ class DsmcParams(C.Structure):
                 ("c", C.c_double * 4)]
 
 
+class ObjSpecies(C.Structure):
+    _fields_ = [("neu", C.c_void_p), ("neu_ids", C.c_void_p), ("n_neu", C.c_void_p), ("cap_neu", C.c_long),
+                ("neu_mpw0", C.c_double), ("spu", C.c_void_p), ("spu_ids", C.c_void_p), ("n_spu", C.c_void_p),
+                ("cap_spu", C.c_long), ("spu_mpw0", C.c_double), ("sputtering", C.c_int), ("neu_qm", C.c_double),
+                ("spu_qm", C.c_double), ("ef", C.c_void_p),
+                ("dt_global", C.c_double)]
+
+
 class MT(C.Structure):
     _fields_ = [("mt", C.c_uint32 * 624), ("idx", C.c_int)]
 
@@ -119,6 +127,8 @@ class Port:
             "or_dsmc_sigma": (d, [vp, d]),
             "or_dsmc_ref": (l, [vp, vp, vp, vp, l, vp, l, d, vp, vp]),
             "or_dsmc_gpuform": (l, [vp, vp, vp, vp, vp, l, d, d, u32, u32, u32, u32, vp, vp]),
+            "or_push_nonelectron_ref": (l, [vp, vp, vp, l, vp, d, d, d, vp, vp]),
+            "or_push_nonelectron_gpuform": (l, [vp, vp, vp, l, vp, d, d, d, vp, u32, u32, u32, vp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -270,6 +280,41 @@ class Port:
                                       C.byref(mx))
         return nc, pairs.value, mx.value
 
+    def _obj_species(self, neu, neu_mpw0, spu, spu_mpw0, sputtering, ef, dt_global, n_neu, n_spu,
+                     neu_ids=None, spu_ids=None):
+        t = ObjSpecies()
+        t.neu, t.neu_ids, t.n_neu, t.cap_neu, t.neu_mpw0 = _p(neu), _p(neu_ids), C.addressof(n_neu), len(neu), neu_mpw0
+        t.spu, t.spu_ids, t.n_spu = _p(spu), _p(spu_ids), C.addressof(n_spu)
+        t.cap_spu, t.spu_mpw0, t.sputtering = len(spu), spu_mpw0, int(sputtering)
+        t.ef, t.dt_global = _p(ef), dt_global
+        return t
+
+    def push_nonelectron_ref(self, g, r, parts, n, ef, dt, charge, mass, neu, n_neu, neu_mpw0, spu=None, n_spu=0,
+                             spu_mpw0=1.0, sputtering=False, dt_global=None):
+        """Species::advanceNonElectron on parts[:n]; neutrals (and sputtered particles) appended
+        to neu[n_neu:] (spu[n_spu:]).  Returns (n, n_neu, n_spu)."""
+        ef = np.ascontiguousarray(ef, np.float64)
+        spu = neu if spu is None else spu
+        a, b = C.c_long(n_neu), C.c_long(n_spu if spu is not neu else 0)
+        if spu is neu:
+            b = a
+        t = self._obj_species(neu, neu_mpw0, spu, spu_mpw0, sputtering, ef, dt if dt_global is None else dt_global, a, b)
+        created = (C.c_long * 2)()
+        m = self.lib.or_push_nonelectron_ref(C.byref(g), C.byref(r), _p(parts), n, _p(ef), dt, charge, mass,
+                                             C.byref(t), created)
+        return m, a.value, b.value
+
+    def push_nonelectron_gpuform(self, g, parts, ids, n, ef, dt, charge, mass, neu, neu_ids, n_neu, neu_mpw0, spu,
+                                 spu_ids, n_spu, spu_mpw0, sputtering, seed, step):
+        """GPU form; returns (n, n_neu, n_spu, stats)."""
+        ef = np.ascontiguousarray(ef, np.float64)
+        a, b = C.c_long(n_neu), C.c_long(n_spu)
+        t = self._obj_species(neu, neu_mpw0, spu, spu_mpw0, sputtering, ef, dt, a, b, neu_ids, spu_ids)
+        st = (C.c_long * 4)()
+        m = self.lib.or_push_nonelectron_gpuform(C.byref(g), _p(parts), _p(ids), n, _p(ef), dt, charge, mass,
+                                                 C.byref(t), seed & 0xffffffff, (seed >> 32) & 0xffffffff, step, st)
+        return m, a.value, b.value, list(st)
+
     def merge_ref(self, g, r, parts, n, ef, charge, mass, dt, min_count=10):
         return self.lib.or_merge_ref(C.byref(g), C.byref(r), _p(parts), n, len(parts),
                                      _p(np.ascontiguousarray(ef, np.float64)), charge, mass, dt, min_count)
@@ -353,6 +398,7 @@ class Ref:
                 "ref_dsmc_create": (i, [vp, i, i]),
                 "ref_dsmc_apply": (None, [vp, d]),
                 "ref_dsmc_svmax": (d, [vp]),
+                "ref_push_nonelectron_sput": (None, [vp, i, i, i, i, d]),
             }
             for name, (res, args) in sig.items():
                 f = getattr(L, name)

@@ -1656,3 +1656,252 @@ long or_dsmc_gpuform(const or_dsmc_params* q, double* vel1, const int32_t* cnt1,
     if (svmax_step) *svmax_step = mx;
     return n_coll;
 }
+
+/* ---- object interaction of non-electron species (Species.cpp:45-256) ---- */
+/* Rectangle::lineIntersect (Object.cpp:239-302) */
+static void box_line_intersect(const or_grid* g, int b, const double x1[3], const double x2[3], double* t_entry,
+                               double xi[3], double n[3]) {
+    double tmin[3], tmax[3], A[3];
+    int ps[3] = {0, 1, 2};
+    for (int d = 0; d < 3; d++) A[d] = x2[d] - x1[d];
+    for (int d = 0; d < 3; d++) {
+        tmin[d] = (g->box_c[b][d] - g->box_half[b][d] - x1[d]) / A[d];
+        tmax[d] = (g->box_c[b][d] + g->box_half[b][d] - x1[d]) / A[d];
+    }
+    for (int d = 0; d < 3; d++)
+        if (tmin[d] > tmax[d]) {
+            double t = tmin[d];
+            tmin[d] = tmax[d];
+            tmax[d] = t;
+            ps[d] += 3;
+        }
+    double te = tmin[0];
+    int j = 0, k = 0, t = 0;
+    for (int i = 0; i < 2; i++) {
+        if (te < tmin[i + 1]) {
+            te = tmin[i + 1];
+            j = i + 1;
+            k = 0;
+        } else if (fabs(te - tmin[i + 1]) < 1e-6) {
+            k++;
+            t = i + 1;
+        }
+    }
+    n[0] = n[1] = n[2] = 0;
+    n[ps[j] % 3] += ps[j] < 3 ? -1.0 : 1.0;
+    if (k != 0) {
+        if (k < 2) {
+            n[ps[t] % 3] += ps[t] < 3 ? -1.0 : 1.0;
+        } else {
+            n[ps[2] % 3] += ps[2] < 3 ? -1.0 : 1.0;
+            n[ps[1] % 3] += ps[1] < 3 ? -1.0 : 1.0;
+        }
+        double inv = 1.0 / sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+        for (int d = 0; d < 3; d++) n[d] *= inv;
+    }
+    for (int d = 0; d < 3; d++) xi[d] = x1[d] + (x2[d] - x1[d]) * te;
+    *t_entry = te;
+}
+typedef double (*draw_fn)(void*);
+static double draw_mt(void* r) { return or_mt_u01((or_mt*)r); }
+typedef struct {
+    uint32_t ctr[4], key[2], buf[4];
+    int pos;
+} obj_stream;
+static double draw_obj(void* s_) {
+    obj_stream* s = (obj_stream*)s_;
+    if (s->pos == 4) {
+        or_philox4x32_10(s->ctr, s->key, s->buf);
+        s->ctr[3]++;
+        s->pos = 0;
+    }
+    return or_u01_from_u32(s->buf[s->pos++]);
+}
+/* Species::sampleReflectedVelocity (Species.cpp:835-853) with sampleVth(300) (855-861) */
+static void reflect_vel(double mass, double v_mag1, const double n[3], draw_fn draw, void* r, double out[3]) {
+    double v_th0 = sqrt(2 * OR_KB * 300.0 / mass), s3[3];
+    for (int d = 0; d < 3; d++) {
+        double u1 = draw(r), u2 = draw(r), u3 = draw(r);
+        s3[d] = v_th0 * (u1 + u2 + u3 - 1.5);
+    }
+    double v_th = sqrt(s3[0] * s3[0] + s3[1] * s3[1] + s3[2] * s3[2]);
+    double v_mag2 = v_mag1 + 1.0 * (v_th - v_mag1);
+    double sin_theta = draw(r);
+    double cos_theta = sqrt(1 - sin_theta * sin_theta);
+    double psi = 2 * OR_PI * draw(r);
+    double t1[3];
+    if (n[0] * 1 + n[1] * 0 + n[2] * 0 != 0) {
+        t1[0] = n[1] * 0 - n[2] * 0;
+        t1[1] = n[2] * 1 - n[0] * 0;
+        t1[2] = n[0] * 0 - n[1] * 1;
+    } else {
+        t1[0] = n[1] * 0 - n[2] * 1;
+        t1[1] = n[2] * 0 - n[0] * 0;
+        t1[2] = n[0] * 1 - n[1] * 0;
+    }
+    double t2[3] = {n[1] * t1[2] - n[2] * t1[1], n[2] * t1[0] - n[0] * t1[2], n[0] * t1[1] - n[1] * t1[0]};
+    double a = sin_theta * cos(psi), b = sin(psi);
+    for (int d = 0; d < 3; d++) out[d] = (t1[d] * a + t2[d] * b + n[d] * cos_theta) * v_mag2;
+}
+static int in_bounds(const or_grid* g, const double x[3]) {
+    for (int d = 0; d < 3; d++)
+        if (x[d] < g->x0[d] || x[d] >= g->xm[d]) return 0;
+    return 1;
+}
+/* what an impact at xi leaves behind for an ion (Species.cpp:225-245); created ids (GPU form
+ * only) follow the device's obj_child_id */
+static uint64_t obj_child_id(uint64_t parent, uint32_t step, uint32_t k) {
+    return or_mix64(or_child_id(parent, step, 3) + (uint64_t)(k + 1) * 0xD1B54A32D192ED03ull);
+}
+static void ion_impact(const or_grid* g, const or_obj_species* t, double w, double vmag, double mass, const double xi[3],
+                       const double n[3], draw_fn draw, void* r, int with_ids, uint64_t id, uint32_t step,
+                       long* created) {
+    int m = (int)(w / t->neu_mpw0 + draw(r));
+    for (int q = 0; q < m; q++) {
+        double vn[3];
+        reflect_vel(mass, vmag, n, draw, r, vn);
+        long before = *t->n_neu;
+        add_particle(g, t->neu, t->n_neu, t->cap_neu, xi, vn, t->neu_mpw0, t->ef, t->neu_qm, 1.0, t->dt_global);
+        if (*t->n_neu > before) {
+            if (with_ids) t->neu_ids[before] = obj_child_id(id, step, (uint32_t)q);
+            created[0]++;
+        }
+    }
+    if (t->sputtering) {
+        double yield = vmag > 5e3 ? 0.1 : 0;
+        int ms = (int)(yield * w / t->spu_mpw0 + draw(r));
+        for (int q = 0; q < ms; q++) {
+            double vn[3];
+            reflect_vel(mass, vmag, n, draw, r, vn);
+            long before = *t->n_spu;
+            add_particle(g, t->spu, t->n_spu, t->cap_spu, xi, vn, t->spu_mpw0, t->ef, t->spu_qm, 1.0, t->dt_global);
+            if (*t->n_spu > before) {
+                if (with_ids) t->spu_ids[before] = obj_child_id(id, step, 0x10000000u + (uint32_t)q);
+                created[1]++;
+            }
+        }
+    }
+}
+long or_push_nonelectron_ref(const or_grid* g, or_mt* r, or_particle* p, long n, const double* ef, double dt,
+                             double charge, double mass, const or_obj_species* t, long created[2]) {
+    double factor = dt * charge / mass;
+    long np = n;
+    created[0] = created[1] = 0;
+    for (long q = 0; q < np; q++) {
+        or_particle* part = &p[q];
+        double lc[3], e[3];
+        xtol(g, part->pos, lc);
+        or_gather3_ref(g, ef, lc, e);
+        for (int d = 0; d < 3; d++) part->vel[d] += e[d] * factor;
+        double t_rem = 1;
+        int nb = 0, removed = 0;
+        while (t_rem > 0) {
+            if (++nb > 20) {
+                removed = 1;
+                break;
+            }
+            double pos_old[3] = {part->pos[0], part->pos[1], part->pos[2]};
+            for (int d = 0; d < 3; d++) part->pos[d] += part->vel[d] * t_rem * dt;
+            int obj = in_object(g, part->pos);
+            if (!in_bounds(g, part->pos)) {
+                removed = 1;
+                break;
+            } else if (obj) {
+                double tp, xi[3], nrm[3];
+                box_line_intersect(g, obj - 1, pos_old, part->pos, &tp, xi, nrm);
+                for (int d = 0; d < 3; d++) part->pos[d] = xi[d];
+                double vmag = len3(part->vel);
+                if (charge == 0) {
+                    reflect_vel(mass, len3(part->vel), nrm, draw_mt, r, part->vel);
+                } else {
+                    ion_impact(g, t, part->w, vmag, mass, xi, nrm, draw_mt, r, 0, 0, 0, created);
+                    removed = 1;
+                    break;
+                }
+                t_rem *= (1 - tp);
+                continue;
+            }
+            t_rem = 0;
+        }
+        if (removed) {
+            p[q] = p[np - 1];
+            np--;
+            q--;
+        }
+    }
+    return np;
+}
+long or_push_nonelectron_gpuform(const or_grid* g, or_particle* p, uint64_t* ids, long n, const double* ef, double dt,
+                                 double charge, double mass, const or_obj_species* t, uint32_t seed_lo,
+                                 uint32_t seed_hi, uint32_t step, long stats[4]) {
+    double factor = dt * charge / mass;
+    long np = n;
+    for (int k = 0; k < 4; k++) stats[k] = 0;
+    for (long q = 0; q < np; q++) {
+        or_particle* part = &p[q];
+        double lc[3], e[3];
+        xtol(g, part->pos, lc);
+        or_gather3_ref(g, ef, lc, e);
+        for (int d = 0; d < 3; d++) part->vel[d] += e[d] * factor;
+        double x1[3], x2[3];
+        for (int d = 0; d < 3; d++) {
+            x1[d] = part->pos[d];
+            x2[d] = part->pos[d] + part->vel[d] * dt;
+            if (g->periodic[d]) {
+                double L = g->xm[d] - g->x0[d];
+                if (x2[d] < g->x0[d]) x2[d] += L;
+                else if (x2[d] >= g->xm[d]) x2[d] -= L;
+            }
+        }
+        int removed = !in_bounds(g, x2);
+        if (!removed && in_object(g, x2)) {
+            stats[0]++;
+            obj_stream st = {{(uint32_t)ids[q], (uint32_t)(ids[q] >> 32), step, 0x0B000000u}, {seed_lo, seed_hi},
+                             {0, 0, 0, 0}, 4};
+            double t_rem = 1.0;
+            int nb = 1;
+            while (1) {
+                int obj = in_object(g, x2);
+                if (!obj) break;
+                double tp, xi[3], nrm[3];
+                box_line_intersect(g, obj - 1, x1, x2, &tp, xi, nrm);
+                double vmag = len3(part->vel);
+                if (charge == 0) {
+                    reflect_vel(mass, vmag, nrm, draw_obj, &st, part->vel);
+                    stats[1]++;
+                    t_rem *= (1 - tp);
+                    if (++nb > 20) {
+                        removed = 1;
+                        break;
+                    }
+                    for (int d = 0; d < 3; d++) {
+                        x1[d] = xi[d];
+                        x2[d] = xi[d] + part->vel[d] * t_rem * dt;
+                        if (g->periodic[d]) {
+                            double L = g->xm[d] - g->x0[d];
+                            if (x2[d] < g->x0[d]) x2[d] += L;
+                            else if (x2[d] >= g->xm[d]) x2[d] -= L;
+                        }
+                    }
+                    if (!in_bounds(g, x2)) {
+                        removed = 1;
+                        break;
+                    }
+                    continue;
+                }
+                ion_impact(g, t, part->w, vmag, mass, xi, nrm, draw_obj, &st, 1, ids[q], step, stats + 2);
+                removed = 1;
+                break;
+            }
+        }
+        if (removed) {
+            p[q] = p[np - 1];
+            ids[q] = ids[np - 1];
+            np--;
+            q--;
+        } else {
+            for (int d = 0; d < 3; d++) part->pos[d] = x2[d];
+        }
+    }
+    return np;
+}

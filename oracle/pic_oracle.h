@@ -178,6 +178,35 @@ long or_dsmc_gpuform(const or_dsmc_params* q, double* vel1, const int32_t* cnt1,
                      long nc, double dt, double svmax, uint32_t seed_lo, uint32_t seed_hi, uint32_t call,
                      uint32_t tag, long* pairs, double* svmax_step);
 
+/* ---- object interaction of non-electron species (Species.cpp:45-256) ---- */
+typedef struct {
+    or_particle* neu; /* neutral species particles are appended here (Species::addParticle) */
+    uint64_t* neu_ids; /* GPU form: ids of the created neutrals */
+    long* n_neu;
+    long cap_neu;
+    double neu_mpw0;
+    or_particle* spu; /* sputtered material (spherium) */
+    uint64_t* spu_ids;
+    long* n_spu;
+    long cap_spu;
+    double spu_mpw0;
+    int sputtering;   /* Config::SPUTTERING */
+    double neu_qm, spu_qm; /* charge / mass of the two species (addParticle's rewind) */
+    const double* ef; /* E for addParticle's rewind (no effect on neutral species) */
+    double dt_global;
+} or_obj_species;
+/* Species::advanceNoSputteringSerial / advanceSputteringSerial with Rectangle objects, MT19937
+ * draws in the reference's order; swap-with-last deletion.  Returns the new count; created[0]
+ * neutrals and created[1] sputtered particles appended. */
+long or_push_nonelectron_ref(const or_grid* g, or_mt* r, or_particle* p, long n, const double* ef, double dt,
+                             double charge, double mass, const or_obj_species* t, long created[2]);
+/* GPU form (restated from k_push + k_object_hits, FP64): periodic axes wrap; a particle that
+ * enters an object draws from Philox stream (id, step, 0x0B000000 + block) with key seed;
+ * survivors keep their ids.  stats: impacts, bounces, neutrals created, sputtered created. */
+long or_push_nonelectron_gpuform(const or_grid* g, or_particle* p, uint64_t* ids, long n, const double* ef, double dt,
+                                 double charge, double mass, const or_obj_species* t, uint32_t seed_lo,
+                                 uint32_t seed_hi, uint32_t step, long stats[4]);
+
 /* conservation sums (Species.cpp:732-752) */
 void or_sums(const or_particle* p, long n, double mass, double* count, double mom[3], double* ke);
 

@@ -140,6 +140,13 @@ void ref_push_nonelectron(void* h, int sp, int neutral_sp, double dt) {
     RefSim* s = static_cast<RefSim*>(h);
     s->species[sp].advanceNonElectron(s->species[neutral_sp], s->species[neutral_sp], dt);
 }
+// Species::advanceNonElectron(neutrals, spherium, dt) with Config::SPUTTERING set as given
+void ref_push_nonelectron_sput(void* h, int sp, int neutral_sp, int spherium_sp, int sputtering, double dt) {
+    RefSim* s = static_cast<RefSim*>(h);
+    Config::getInstance().setSPUTTERING(sputtering != 0);
+    s->species[sp].advanceNonElectron(s->species[neutral_sp], s->species[spherium_sp], dt);
+    Config::getInstance().setSPUTTERING(false);
+}
 void ref_number_density(void* h, int sp) { static_cast<RefSim*>(h)->species[sp].computeNumberDensity(); }
 void ref_charge_density(void* h) {
     RefSim* s = static_cast<RefSim*>(h);

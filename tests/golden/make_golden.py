@@ -176,9 +176,41 @@ def case_dsmc():
     return out
 
 
+def case_objects():
+    """Species::advanceNonElectron with a Rectangle (Species.cpp:45-256): neutrals bounce, ions are
+    neutralised with sputtering on.  Three steps; each pushes the neutrals, then the ions.  The
+    global RNG is reseeded (obj_seed) after the loads."""
+    nn, x0, xm = (11, 11, 11), (0.0, 0.0, 0.0), (0.01, 0.01, 0.01)
+    R = O.Ref(nn, x0, xm)
+    R.L.ref_add_rectangle(R.h, v3(0.005, 0.005, 0.005), 0.0, v3(0.004, 0.004, 0.004))
+    R.seed(13)
+    neu = R.species("O", 16 * O.AMU, 0.0, 1e9)
+    ion = R.species("O+", 16 * O.AMU, O.QE, 1e10)
+    spu = R.species("Sp", 16 * O.AMU, 0.0, 5e8)
+    c, s = v3(0.005, 0.005, 0.005), v3(0.01, 0.01, 0.01)
+    R.L.ref_load_box_thermal(R.h, neu, c, s, 2e18, 300.0)  # ~1900 outside the box
+    R.L.ref_load_box_thermal(R.h, ion, c, s, 1e19, 30000.0)
+    rng = np.random.default_rng(4)
+    ef = rng.normal(size=(R.nv, 3)) * 1e3
+    R.set_ef(ef)
+    dt_n, dt_i = 2e-6, 2e-7
+    R.L.ref_set_time(R.h, dt_i, 10)
+    out = dict(nn=np.array(nn), x0=np.array(x0), xm=np.array(xm), ef=ef, dt_n=np.array(dt_n), dt_i=np.array(dt_i),
+               box_c=np.array([0.005] * 3), box_s=np.array([0.004] * 3), obj_seed=np.array(21))
+    out.update({"neu0_" + k: v for k, v in parts_arrays(R.get_particles(neu)).items()})
+    out.update({"ion0_" + k: v for k, v in parts_arrays(R.get_particles(ion)).items()})
+    R.seed(21)
+    for it in range(3):
+        R.L.ref_push_nonelectron_sput(R.h, neu, neu, neu, 0, dt_n)
+        R.L.ref_push_nonelectron_sput(R.h, ion, neu, spu, 1, dt_i)
+        for nm, sp in (("neu", neu), ("ion", ion), ("spu", spu)):
+            out.update({f"{nm}{it + 1}_" + k: v for k, v in parts_arrays(R.get_particles(sp)).items()})
+    return out
+
+
 def main():
     cases = (("push_deposit", case_push_deposit), ("poisson", case_poisson), ("ntc", case_ntc), ("merge", case_merge),
-             ("dsmc", case_dsmc))
+             ("dsmc", case_dsmc), ("objects", case_objects))
     only = set(sys.argv[1:])
     for name, fn in cases:
         if only and name not in only:

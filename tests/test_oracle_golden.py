@@ -279,3 +279,27 @@ def test_dsmc_bit_exact(port):
         assert nc > 10
         assert np.array_equal(a["vel"], d[f"two{it}_vel_a"]) and np.array_equal(b["vel"], d[f"two{it}_vel_b"]), it
         assert sv == float(d[f"two{it}_svmax"])
+
+
+def test_object_interaction_bit_exact(port):
+    """Species::advanceNonElectron with a Rectangle: neutral bounces, ion neutralisation with
+    sputtering (Species.cpp:45-256, Object.cpp:231-302), three steps against the reference."""
+    d = golden("objects")
+    g = port.grid(d["nn"], d["x0"], d["xm"], boxes=[(tuple(d["box_c"]), tuple(d["box_s"]))])
+    mt = port.mt(int(d["obj_seed"]))
+    cap = 10000
+    neu, ion, spu = np.zeros(cap, O.PARTICLE), np.zeros(cap, O.PARTICLE), np.zeros(cap, O.PARTICLE)
+    n0, i0 = to_parts(d, "neu0_"), to_parts(d, "ion0_")
+    neu[:len(n0)], ion[:len(i0)] = n0, i0
+    nn_, ni_, ns_ = len(n0), len(i0), 0
+    m = 16 * O.AMU
+    for it in (1, 2, 3):
+        nn_, _, _ = port.push_nonelectron_ref(g, mt, neu, nn_, d["ef"], float(d["dt_n"]), 0.0, m, neu, nn_, 1e9,
+                                              dt_global=float(d["dt_i"]))
+        ni_, nn_, ns_ = port.push_nonelectron_ref(g, mt, ion, ni_, d["ef"], float(d["dt_i"]), O.QE, m, neu, nn_, 1e9,
+                                                  spu, ns_, 5e8, True)
+        for nm, arr, n in (("neu", neu, nn_), ("ion", ion, ni_), ("spu", spu, ns_)):
+            ref = to_parts(d, f"{nm}{it}_")
+            assert n == len(ref), (nm, it, n, len(ref))
+            for f in ("pos", "vel", "w"):
+                assert np.array_equal(arr[:n][f], ref[f]), (nm, it, f)
