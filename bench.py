@@ -428,7 +428,10 @@ def run_gpu(args, wl, rank, ws, local):
     e2e = None if ensemble else run_e2e(pic, wl, args, rank)
     poisson = None
     if rank == 0 and args.poisson > 0:
-        poisson = poisson_bench(pic, args.poisson)
+        poisson = poisson_bench(pic, args.poisson, methods=args.poisson_methods.split(","))
+    dsmc = None
+    if rank == 0 and args.dsmc > 0:
+        dsmc = dsmc_bench(pic, args.dsmc, cpu=not args.no_cpu)
     cpu = None
     if rank == 0 and not args.no_cpu and not ensemble:
         cpu = cpu_reference(wl, inner / max(1, args.steps), sample=args.cpu_sample, steps=1)
@@ -459,6 +462,7 @@ def run_gpu(args, wl, rank, ws, local):
         "cpu_baseline": cpu,
         "e2e": e2e,
         "poisson_time_to_1e-6": poisson,
+        "dsmc": dsmc,
         "clocks": clocks,
     }
     if rank == 0:
@@ -481,7 +485,7 @@ def blob_rho(nn, seed):
     return rho.ravel()
 
 
-def poisson_bench(pic, n, seed=5, train_steps=300):
+def poisson_bench(pic, n, seed=5, train_steps=300, methods=("rbsor", "pcg", "learned_start", "learned")):
     """Time to a 1e-6 FP64 relative residual from the Dirichlet-only start, n^3 nodes over a
     0.04 m cube, z faces at 0 V / 1000 V, periodic x, y; blob charge density.  Plain red-black
     SOR and Jacobi-PCG against the learned multilevel preconditioner, first at its starting
@@ -511,12 +515,18 @@ def poisson_bench(pic, n, seed=5, train_steps=300):
         return {"seconds": wall, "iterations": S.iters, "rel": S.rel, "converged": ok,
                 "device_seconds": dev_ms / 1e3, "launches": launches}
 
-    out["rbsor"] = timed(pic.SOLVER_RBSOR, omega)
-    out["rbsor"]["omega"] = omega
-    out["pcg"] = timed(pic.SOLVER_PCG)
+    if "rbsor" in methods:
+        out["rbsor"] = timed(pic.SOLVER_RBSOR, omega)
+        out["rbsor"]["omega"] = omega
+    if "pcg" in methods:
+        out["pcg"] = timed(pic.SOLVER_PCG)
     lp = pic.LearnedPreconditioner(W)
     lp.reset()
-    out["learned_start"] = timed(pic.SOLVER_LEARNED)
+    if "learned_start" in methods:
+        out["learned_start"] = timed(pic.SOLVER_LEARNED)
+    if "learned" not in methods:
+        W.close()
+        return out
     # online training on (rho, phi) pairs of the run's other solves
     W.synchronize()
     t0 = time.perf_counter()
@@ -537,9 +547,82 @@ def poisson_bench(pic, n, seed=5, train_steps=300):
     W.rho = rho_test
     out["learned"] = timed(pic.SOLVER_LEARNED)
     out["learned"]["training"] = {"pair_solves": 4, "steps": train_steps, "seconds": train_s, "rounds": rounds}
-    out["speedup_vs_pcg"] = out["pcg"]["seconds"] / out["learned"]["seconds"]
-    out["speedup_vs_rbsor"] = out["rbsor"]["seconds"] / out["learned"]["seconds"]
+    for m in ("pcg", "rbsor"):
+        if m in out:
+            out["speedup_vs_" + m] = out[m]["seconds"] / out["learned"]["seconds"]
     W.close()
+    return out
+
+
+def dsmc_bench(pic, ncell, ppc=16, calls=10, cpu=True):
+    """DSMC_MEX (VHS O-O collisions, Interactions.cpp:143-284) on ncell^3 cells of 1 mm^3 with ppc
+    particles per cell (n = 1e21 m^-3, 300 K, dt = 1 us): time per call (sort + collisions) after
+    three calls, candidate pairs and collisions per call, the collision kernel's roofline at 32 B per
+    particle (its velocities read and written once; pairs re-read them from L1/L2), and the
+    reference's serial algorithm (the oracle's port) on a 32^3-cell sample of the same density."""
+    L = ncell * 1e-3
+    W = pic.World(ncell + 1, ncell + 1, ncell + 1, (0.0, 0.0, 0.0), (L, L, L))
+    W.set_boundaries((1, 1, 1), (1,) * 6, (0.0,) * 6)
+    W.setTime(1e-6, 1 << 20)
+    mpw0 = 1e21 * 1e-9 / ppc
+    n = ncell ** 3 * ppc
+    a = pic.Species("O", 16 * AMU, 0.0, W, mpw0, capacity=n + 4096)
+    a.loadUniform((0, 0, 0), (L, L, L), n, 300.0, mpw0, 0.0, seed=1)
+    D = pic.DSMC_MEX(a, W, seed=3)
+    for _ in range(3):
+        D.apply(1e-6)
+    W.synchronize()
+    W.timing(True)
+    W.timing_reset()
+    s0 = D.stats()
+    t0 = time.perf_counter()
+    for _ in range(calls):
+        D.apply(1e-6)
+    W.synchronize()
+    wall = time.perf_counter() - t0
+    s1 = D.stats()
+    coll_ms, coll_l = W.timer("dsmc")
+    sort_ms, _ = W.timer("sort")
+    W.timing(False)
+    W.close()
+    pairs = (s1["pairs"] - s0["pairs"]) / calls
+    peak, peak_kind = measured_peak()
+    kernel_s = coll_ms / 1e3 / calls
+    achieved = 32.0 * n / kernel_s / 1e9
+    out = {"cells": ncell ** 3, "particles": n, "calls": calls, "ms_per_call": wall * 1e3 / calls,
+           "device_ms_per_call": (coll_ms + sort_ms) / calls, "collide_ms_per_call": coll_ms / calls,
+           "sort_ms_per_call": sort_ms / calls, "pairs_per_call": pairs,
+           "collisions_per_call": (s1["collisions"] - s0["collisions"]) / calls,
+           "pairs_per_s": pairs / (wall / calls), "sigma_v_rel_max": s1["sigma_v_rel_max"],
+           "roofline": {"bound": "hbm", "kernel": "k_dsmc", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                        "frac": achieved / peak, "peak_source": peak_kind,
+                        "algorithmic_bytes_per_launch": 32.0 * n}}
+    if cpu:
+        import oracle as O
+
+        port = O.Port()
+        nc = 32
+        g = port.grid((nc + 1,) * 3, (0, 0, 0), (nc * 1e-3,) * 3)
+        q = port.dsmc_params(g, 16 * AMU, 16 * AMU, mpw0)
+        rng = np.random.default_rng(2)
+        m = nc ** 3 * ppc
+        p = np.zeros(m, O.PARTICLE)
+        p["pos"] = rng.uniform(0, nc * 1e-3, (m, 3)) * 0.999999
+        p["vel"] = rng.normal(size=(m, 3)) * np.sqrt(KB * 300.0 / (16 * AMU))
+        p["w"] = mpw0
+        mt = port.mt(5)
+        sv = 1e-14
+        for _ in range(2):  # the majorant settles
+            _, _, sv = port.dsmc_ref(g, q, mt, p, None, 1e-6, sv)
+        t0 = time.perf_counter()
+        tot, k = 0, 0
+        while time.perf_counter() - t0 < 3.0:
+            _, pr, sv = port.dsmc_ref(g, q, mt, p, None, 1e-6, sv)
+            tot += pr
+            k += 1
+        dt_cpu = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": tot / dt_cpu, "unit": "candidate pairs/s", "cores": 1, "kind": "port",
+                               "sample": "%d^3 cells, %d particles, %d calls (sort included)" % (nc, m, k)}
     return out
 
 
@@ -617,6 +700,10 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=1_000_000)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--poisson", type=int, default=256, help="n of the n^3 Poisson time-to-1e-6 case (0: skip)")
+    ap.add_argument("--poisson-methods", default="rbsor,pcg,learned_start,learned",
+                    help="comma list of the Poisson solves to time (rbsor, pcg, learned_start, learned)")
+    ap.add_argument("--dsmc", type=int, default=128, help="n of the n^3-cell DSMC_MEX case (0: skip)")
+    ap.add_argument("--dsmc-only", action="store_true", help="run only the DSMC_MEX case and print it")
     ap.add_argument("--poisson-only", action="store_true",
                     help="run only the Poisson time-to-1e-6 comparison (the second metric) and print it")
     args = ap.parse_args()
@@ -628,7 +715,15 @@ def main():
         if rank == 0 and args.impl != "reference":
             pic = importlib.import_module(PKG)
             print(json.dumps({"metric": "Poisson time-to-1e-6 FP64 residual", "unit": "s",
-                              "poisson_time_to_1e-6": poisson_bench(pic, args.poisson or 256)}), flush=True)
+                              "poisson_time_to_1e-6": poisson_bench(pic, args.poisson or 256,
+                                                                    methods=args.poisson_methods.split(","))}),
+                  flush=True)
+        return
+    if args.dsmc_only:
+        if rank == 0 and args.impl != "reference":
+            pic = importlib.import_module(PKG)
+            print(json.dumps({"metric": "DSMC_MEX candidate pairs/s", "unit": "pairs/s",
+                              "dsmc": dsmc_bench(pic, args.dsmc or 128, cpu=not args.no_cpu)}), flush=True)
         return
     if args.impl == "reference":
         run_reference(args, wl, rank, ws)

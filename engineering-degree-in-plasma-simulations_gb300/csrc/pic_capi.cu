@@ -487,7 +487,7 @@ int ensure_lp(pic_world* w) {
     lp_galerkin_diag(c, L->nlev, L->diag);
     lp_layout(L->lay);
     CU(cudaMalloc(&L->W, sizeof(float) * L->lay.total));
-    CU(cudaMalloc(&L->fold, sizeof(float) * kLpFold * kLpNetLevels));
+    CU(cudaMalloc(&L->fold, sizeof(float) * kLpFoldStride * kLpNetLevels));
     std::vector<float> hw(L->lay.total);
     lp_init_weights(L->lay, L->diag, L->nlev, hw.data());
     CU(cudaMemcpyAsync(L->W, hw.data(), sizeof(float) * hw.size(), cudaMemcpyHostToDevice, w->stream));
@@ -592,7 +592,7 @@ extern "C" int pic_world_create(pic_world** out, int ni, int nj, int nk, const d
          alloc((void**)&w->d2, sizeof(float) * nv) && alloc((void**)&w->q, sizeof(float) * nv) &&
          alloc((void**)&w->z, sizeof(float) * nv) && alloc((void**)&w->part, sizeof(double) * kParts * 8) &&
          alloc((void**)&w->scal, sizeof(double) * 16) && alloc((void**)&w->flag, sizeof(int) * 4) &&
-         alloc((void**)&w->gpart, sizeof(double) * 8 * (size_t)std::max(kParts, node_blocks(nv))) &&
+         alloc((void**)&w->gpart, sizeof(double) * 8 * (size_t)std::max(kParts, 2 * node_blocks(nv))) &&
          alloc((void**)&w->ticket, sizeof(unsigned) * 4) &&
          alloc((void**)&w->cell_count, sizeof(int) * (g.nc + 1)) &&
          alloc((void**)&w->cell_start, sizeof(int) * (g.nc + 1)) &&
@@ -609,7 +609,7 @@ extern "C" int pic_world_create(pic_world** out, int ni, int nj, int nk, const d
     cudaMemsetAsync(w->err, 0, sizeof(unsigned), w->stream);
     cudaMemsetAsync(w->flag, 0, sizeof(int) * 4, w->stream);
     cudaMemsetAsync(w->ticket, 0, sizeof(unsigned) * 4, w->stream);
-    w->gstride = std::max(kParts, node_blocks(nv));
+    w->gstride = std::max(kParts, 2 * node_blocks(nv));
     w->grid_nodes = (int)std::min<long long>(kParts, std::max<long long>(1, (nv + 255) / 256));
     w->grid_parts = w->sms * 8;
     w->grid_push = w->sms * push_blocks_per_sm();

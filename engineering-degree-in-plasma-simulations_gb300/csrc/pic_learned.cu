@@ -9,6 +9,7 @@
 #include <cmath>
 #include <vector>
 #include <cuda_bf16.h>
+#include <cstring>
 #include "pic_learned.h"
 #include "pic_stencil.cuh"
 #include "pic_tc.cuh"
@@ -259,7 +260,8 @@ __device__ __forceinline__ float lp_stencil27(const LView& v, const float* __res
 // folded network level: away from non-periodic faces the 5x5x5 stencil K5; on a face point the
 // exact form sum_{t: c + o_t inside} sum_t' K27[t][t'] z[c + o_t + o_t'] (the network reads its
 // intermediate channels as zero outside the box)
-__device__ float lp_net_op(const LView& v, const float* __restrict__ fold, const int c[3]) {
+__device__ float lp_net_op(const LView& v, const float* __restrict__ fold, const float* __restrict__ fold_var,
+                           const int c[3]) {
     bool interior = true;
 #pragma unroll
     for (int ax = 0; ax < 3; ax++)
@@ -281,6 +283,37 @@ __device__ float lp_net_op(const LView& v, const float* __restrict__ fold, const
     }
     if (interior) {
         const float* K5 = fold + 729;
+        for (int dz = -2; dz <= 2; dz++) {
+            int z = lv_nb(c[2], dz, v.n[2], v.per[2]);
+            if (z < 0) continue;
+            for (int dy = -2; dy <= 2; dy++) {
+                int y = lv_nb(c[1], dy, v.n[1], v.per[1]);
+                if (y < 0) continue;
+                const float* row = v.a + y * v.sy + z * v.sz;
+                const float* k = K5 + 25 * (dz + 2) + 5 * (dy + 2) + 2;
+#pragma unroll
+                for (int dx = -2; dx <= 2; dx++) {
+                    int x = lv_nb(c[0], dx, v.n[0], v.per[0]);
+                    if (x >= 0) acc += k[dx] * row[x];
+                }
+            }
+        }
+        return acc;
+    }
+    // a point on a non-periodic face: the 5x5x5 variant of its face class (precomputed from K27
+    // with the first-stage taps outside the box left out), unless an axis has a single point
+    int cls = 0, mul = 1;
+    bool single = false;
+#pragma unroll
+    for (int ax = 0; ax < 3; ax++) {
+        if (!v.per[ax]) {
+            if (v.n[ax] == 1) single = true;
+            cls += mul * (c[ax] == 0 ? 1 : (c[ax] == v.n[ax] - 1 ? 2 : 0));
+        }
+        mul *= 3;
+    }
+    if (!single && fold_var) {
+        const float* K5 = fold_var + 125 * cls;
         for (int dz = -2; dz <= 2; dz++) {
             int z = lv_nb(c[2], dz, v.n[2], v.per[2]);
             if (z < 0) continue;
@@ -320,7 +353,7 @@ __global__ void k_lp_up(LView zin, LView cin, LView out, int mode, const float* 
          idx += gridDim.x * blockDim.x) {
         int c[3];
         lv_decode(out, idx, c[0], c[1], c[2]);
-        float v = mode == 1 ? lp_net_op(zin, fold, c) : inv_diag * zin.a[lv_off(zin, c[0], c[1], c[2])];
+        float v = mode == 1 ? lp_net_op(zin, fold, fold_g + kLpFold, c) : inv_diag * zin.a[lv_off(zin, c[0], c[1], c[2])];
         if (cin.a) v += lp_prolong_at(cin, c);
         out.a[lv_off(out, c[0], c[1], c[2])] = v;
     }
@@ -361,10 +394,307 @@ __global__ void __launch_bounds__(kNodeThreads) k_lp_up0(GridDev g, LView rin, L
     }
 }
 
+// The same operator as k_lp_up0 on 3-D tiles: a CTA owns 32 x 8 x 8 nodes.  It stages the residual
+// tile with its one-node halo (34 x 10 x 10 values, view neighbour rules: wrapped on periodic
+// axes, zero outside) in shared memory with all of its loads in flight at once, and issues the
+// mask, q and prolongation loads of its outputs before the barrier, so the kernel streams the
+// residual from HBM about once (the halo re-reads hit L2) instead of waiting on 27 scattered
+// loads per node.  A thread walks its column's ten tile planes, forms each plane's three 3 x 3
+// partial sums (9 shared reads, 27 FMAs) and rolls them into the outputs of planes p+1, p, p-1.
+constexpr int kUp0X = 32, kUp0Y = 8, kUp0Z = 8;
+constexpr int kUp0HX = kUp0X + 2, kUp0HY = kUp0Y + 2, kUp0HZ = kUp0Z + 2;
+__device__ __forceinline__ int lv_map(int u, int n, int per) {
+    if ((unsigned)u < (unsigned)n) return u;
+    if (!per) return -1;
+    return u < 0 ? u + n : u - n;
+}
+// Stages a halo tile of HX x R values (R rows of HX) in shared memory: element e = hx + HX row
+// reads src[mx[hx] + myz[row]] (0 when either offset is -1).  The trip count is a constant, so
+// every load of a thread is issued before its first shared store.
+template <int HX, int R, int NT>
+__device__ __forceinline__ void stage_tile(float* __restrict__ dst, const float* __restrict__ src, const int* mx,
+                                           const int* myz) {
+    constexpr int kN = HX * R, kPer = (kN + NT - 1) / NT;
+    float v[kPer];
+#pragma unroll
+    for (int k = 0; k < kPer; k++) {
+        const int e = threadIdx.x + k * NT;
+        v[k] = 0.f;
+        if (e < kN) {
+            const int ox = mx[e % HX], oyz = myz[e / HX];
+            if (ox >= 0 && oyz >= 0) v[k] = src[ox + oyz];
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < kPer; k++) {
+        const int e = threadIdx.x + k * NT;
+        if (e < kN) dst[e] = v[k];
+    }
+}
+
+// coarse tile of the prolongation for a 32 x 8 x 8 fine tile: coarse x0/2-1 .. x0/2+16 etc.
+constexpr int kPcX = kUp0X / 2 + 2, kPcY = kUp0Y / 2 + 2, kPcZ = kUp0Z / 2 + 2;
+__global__ void __launch_bounds__(kUp0X * kUp0Y) k_lp_up0_tiled(GridDev g, LView rin, LView cin, float* __restrict__ z,
+                                                                  const uint16_t* __restrict__ kind,
+                                                                  const float* __restrict__ S0,
+                                                                  const float* __restrict__ q, double* gpart,
+                                                                  int gstride, unsigned* ticket, double* out,
+                                                                  const int* flag, int bx_n, int by_n) {
+    if (flag && flag[0]) return;
+    __shared__ float S[27];
+    __shared__ float t[kUp0HZ][kUp0HY][kUp0HX];
+    __shared__ float pc[kPcZ][kPcY][kPcX];
+    __shared__ int mx[kUp0HX], myz[kUp0HY * kUp0HZ];  // halo offsets per axis (-1: outside)
+    __shared__ int cmx[kPcX], cmyz[kPcY * kPcZ];
+    const int tid = threadIdx.x;
+    const int tx = tid % kUp0X, ty = tid / kUp0X;
+    int b = blockIdx.x;
+    const int bx = b % bx_n;
+    b /= bx_n;
+    const int by = b % by_n, bz = b / by_n;
+    const int x0 = bx * kUp0X, y0 = by * kUp0Y, z0 = bz * kUp0Z;
+    if (tid < 27) S[tid] = S0[tid];
+    if (tid < kUp0HX) mx[tid] = lv_map(x0 - 1 + tid, rin.n[0], rin.per[0]);
+    if (tid < kUp0HY * kUp0HZ) {
+        const int uy = lv_map(y0 - 1 + tid % kUp0HY, rin.n[1], rin.per[1]);
+        const int uz = lv_map(z0 - 1 + tid / kUp0HY, rin.n[2], rin.per[2]);
+        myz[tid] = (uy < 0 || uz < 0) ? -1 : uy * rin.sy + uz * rin.sz;
+    }
+    if (cin.a) {
+        if (tid < kPcX) cmx[tid] = lv_map(x0 / 2 - 1 + tid, cin.n[0], cin.per[0]);
+        if (tid < kPcY * kPcZ) {
+            const int uy = lv_map(y0 / 2 - 1 + tid % kPcY, cin.n[1], cin.per[1]);
+            const int uz = lv_map(z0 / 2 - 1 + tid / kPcY, cin.n[2], cin.per[2]);
+            cmyz[tid] = (uy < 0 || uz < 0) ? -1 : uy * cin.sy + uz * cin.sz;
+        }
+    }
+    __syncthreads();
+    stage_tile<kUp0HX, kUp0HY * kUp0HZ, kUp0X * kUp0Y>(&t[0][0][0], rin.a, mx, myz);
+    if (cin.a) {
+        for (int e = tid; e < kPcX * kPcY * kPcZ; e += kUp0X * kUp0Y) {
+            const int ox = cmx[e % kPcX], oyz = cmyz[e / kPcX];
+            (&pc[0][0][0])[e] = (ox >= 0 && oyz >= 0) ? cin.a[ox + oyz] : 0.f;
+        }
+    }
+    // this thread's outputs: mask and q, in flight before the barrier
+    const int x = x0 + tx, y = y0 + ty;
+    const bool col = x < g.ni && y < g.nj;
+    float qv[kUp0Z];
+    unsigned free_mask = 0;
+#pragma unroll
+    for (int k = 0; k < kUp0Z; k++) {
+        const int zz = z0 + k;
+        qv[k] = 0.f;
+        if (col && zz < g.nk) {
+            const int n = x + y * g.ni + zz * g.ni * g.nj;
+            if ((kind[n] & 3) == kFree) {
+                free_mask |= 1u << k;
+                if (q) qv[k] = q[n];
+            }
+        }
+    }
+    __syncthreads();
+    // prolongation weights (0.75 own coarse point, 0.25 the neighbour on the parity side)
+    const int lx = (x >> 1) - (x0 / 2 - 1), ly = (y >> 1) - (y0 / 2 - 1);
+    const int sx = (x & 1) ? 1 : -1, sy = (y & 1) ? 1 : -1;
+    float P = 0.f, Q = 0.f, f_zr = 0.f, f_zq = 0.f;
+#pragma unroll
+    for (int hz = 0; hz < kUp0HZ; hz++) {
+        float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+#pragma unroll
+        for (int dy = 0; dy < 3; dy++)
+#pragma unroll
+            for (int dx = 0; dx < 3; dx++) {
+                const float r = t[hz][ty + dy][tx + dx];
+                a0 = fmaf(S[3 * dy + dx], r, a0);
+                a1 = fmaf(S[9 + 3 * dy + dx], r, a1);
+                a2 = fmaf(S[18 + 3 * dy + dx], r, a2);
+            }
+        const int k = hz - 2;  // output plane z0 + k is complete after tile plane hz = k + 2
+        if (k >= 0 && col && z0 + k < g.nk) {
+            const int n = x + y * g.ni + (z0 + k) * g.ni * g.nj;
+            if (free_mask >> k & 1u) {
+                float v = P + a2;
+                if (cin.a) {
+                    const int zf = z0 + k;
+                    const int lz = (zf >> 1) - (z0 / 2 - 1), sz = (zf & 1) ? 1 : -1;
+                    const float a00 = 0.75f * pc[lz][ly][lx] + 0.25f * pc[lz][ly][lx + sx];
+                    const float a01 = 0.75f * pc[lz][ly + sy][lx] + 0.25f * pc[lz][ly + sy][lx + sx];
+                    const float a10 = 0.75f * pc[lz + sz][ly][lx] + 0.25f * pc[lz + sz][ly][lx + sx];
+                    const float a11 = 0.75f * pc[lz + sz][ly + sy][lx] + 0.25f * pc[lz + sz][ly + sy][lx + sx];
+                    v += 0.75f * (0.75f * a00 + 0.25f * a01) + 0.25f * (0.75f * a10 + 0.25f * a11);
+                }
+                z[n] = v;
+                f_zr += v * t[k + 1][ty + 1][tx + 1];
+                f_zq += v * qv[k];
+            } else {
+                z[n] = 0.f;
+            }
+        }
+        P = Q + a1;
+        Q = a0;
+    }
+    if (out) {
+        const float vv[2] = {f_zr, f_zq};
+        grid_sum<2>(vv, gpart, gstride, ticket, out);
+    }
+}
+// A network level's operator e = op(z) + P e_coarse on 3-D tiles of 32 x 8 x 8 voxels: the z tile with
+// its two-voxel halo (36 x 12 x 12) is staged in shared memory with all loads in flight, and a
+// thread rolls the five 5 x 5 plane sums of each tile plane into its column's eight outputs.
+// Points on a non-periodic face take the exact face-class form through lp_net_op.
+constexpr int kNetX = 32, kNetY = 8, kNetZ = 8;
+constexpr int kNetHX = kNetX + 4, kNetHY = kNetY + 4, kNetHZ = kNetZ + 4;
+__device__ __noinline__ float lp_net_op_face(const LView& v, const float* __restrict__ fold, const int c[3]) {
+    return lp_net_op(v, fold, fold + kLpFold, c);
+}
+struct K5Param {
+    float k[125];
+};
+__global__ void __launch_bounds__(kNetX * kNetY, 2) k_lp_up_net_tiled(LView zin, LView cin, LView out,
+                                                                    const float* __restrict__ fold_g, const int* flag,
+                                                                    int bx_n, int by_n, K5Param K5p) {
+    if (flag && flag[0]) return;
+    const float* K5 = K5p.k;
+    __shared__ float t[kNetHZ][kNetHY][kNetHX];
+    __shared__ int mx[kNetHX], myz[kNetHY * kNetHZ];  // halo offsets per axis (-1: outside)
+    const int tx = threadIdx.x % kNetX, ty = threadIdx.x / kNetX;
+    int b = blockIdx.x;
+    const int bx = b % bx_n;
+    b /= bx_n;
+    const int by = b % by_n, bz = b / by_n;
+    const int x0 = bx * kNetX, y0 = by * kNetY, z0 = bz * kNetZ;
+    if (threadIdx.x < kNetHX) mx[threadIdx.x] = lv_map(x0 - 2 + (int)threadIdx.x, zin.n[0], zin.per[0]);
+    if (threadIdx.x < kNetHY * kNetHZ) {
+        const int uy = lv_map(y0 - 2 + (int)threadIdx.x % kNetHY, zin.n[1], zin.per[1]);
+        const int uz = lv_map(z0 - 2 + (int)threadIdx.x / kNetHY, zin.n[2], zin.per[2]);
+        myz[threadIdx.x] = (uy < 0 || uz < 0) ? -1 : uy * zin.sy + uz * zin.sz;
+    }
+    __syncthreads();
+    stage_tile<kNetHX, kNetHY * kNetHZ, kNetX * kNetY>(&t[0][0][0], zin.a, mx, myz);
+    const int x = x0 + tx, y = y0 + ty;
+    const bool col = x < out.n[0] && y < out.n[1];
+    __shared__ float pro[kNetZ][kNetX * kNetY];  // the coarse correction of every output
+#pragma unroll
+    for (int k = 0; k < kNetZ; k++) {
+        float v = 0.f;
+        if (cin.a && col && z0 + k < out.n[2]) {
+            const int c[3] = {x, y, z0 + k};
+            v = lp_prolong_at(cin, c);
+        }
+        pro[k][threadIdx.x] = v;
+    }
+    __syncthreads();
+    // rolling window: w[j] collects output plane hz - 4 + j; tile plane hz is offset dz - 2 of
+    // output plane hz - dz, i.e. w[4 - dz]
+    float w[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll 1
+    for (int hz = 0; hz < kNetHZ; hz++) {
+        float a[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int dy = 0; dy < 5; dy++)
+#pragma unroll
+            for (int dx = 0; dx < 5; dx++) {
+                const float r = t[hz][ty + dy][tx + dx];
+#pragma unroll
+                for (int dz = 0; dz < 5; dz++) a[dz] = fmaf(K5[25 * dz + 5 * dy + dx], r, a[dz]);
+            }
+#pragma unroll
+        for (int dz = 0; dz < 5; dz++) w[4 - dz] += a[dz];
+        const int k = hz - 4;  // output plane z0 + k is complete
+        if (k >= 0 && col && z0 + k < out.n[2]) {
+            const int c[3] = {x, y, z0 + k};
+            bool face = false;
+#pragma unroll
+            for (int ax = 0; ax < 3; ax++)
+                if (!zin.per[ax] && (c[ax] == 0 || c[ax] == zin.n[ax] - 1)) face = true;
+            const float v = face ? lp_net_op_face(zin, fold_g, c) : w[0];
+            out.a[lv_off(out, x, y, z0 + k)] = v + pro[k][threadIdx.x];
+        }
+#pragma unroll
+        for (int j2 = 0; j2 < 4; j2++) w[j2] = w[j2 + 1];
+        w[4] = 0.f;
+    }
+}
+
+// z_coarse = R z_fine on 3-D tiles of 16 x 8 x 4 coarse voxels: the 34 x 18 x 10 fine points they
+// read are staged in shared memory first (the same index rules as k_lp_restrict)
+constexpr int kRsX = 16, kRsY = 8, kRsZ = 4;
+constexpr int kRsHX = 2 * kRsX + 2, kRsHY = 2 * kRsY + 2, kRsHZ = 2 * kRsZ + 2;
+__device__ __forceinline__ int rs_map(int raw, const LView& f, const LView& c, int ax) {
+    if (f.per[ax]) {
+        const int nc2 = 2 * c.n[ax];
+        raw = raw < 0 ? raw + nc2 : (raw >= nc2 ? raw - nc2 : raw);
+        return raw < f.n[ax] ? raw : -1;
+    }
+    return (raw >= 0 && raw < f.n[ax]) ? raw : -1;
+}
+__global__ void __launch_bounds__(256) k_lp_restrict_tiled(LView f, LView c, const int* flag, int bx_n, int by_n) {
+    if (flag && flag[0]) return;
+    __shared__ float t[kRsHZ][kRsHY][kRsHX];
+    __shared__ int mx[kRsHX], myz[kRsHY * kRsHZ];  // fine offsets per axis (-1: outside)
+    int b = blockIdx.x;
+    const int bx = b % bx_n;
+    b /= bx_n;
+    const int by = b % by_n, bz = b / by_n;
+    const int cx0 = bx * kRsX, cy0 = by * kRsY, cz0 = bz * kRsZ;
+    const int tid = threadIdx.x;
+    if (tid < kRsHX) mx[tid] = rs_map(2 * cx0 - 1 + tid, f, c, 0);
+    if (tid < kRsHY * kRsHZ) {
+        const int uy = rs_map(2 * cy0 - 1 + tid % kRsHY, f, c, 1);
+        const int uz = rs_map(2 * cz0 - 1 + tid / kRsHY, f, c, 2);
+        myz[tid] = (uy < 0 || uz < 0) ? -1 : uy * f.sy + uz * f.sz;
+    }
+    __syncthreads();
+    stage_tile<kRsHX, kRsHY * kRsHZ, 256>(&t[0][0][0], f.a, mx, myz);
+    __syncthreads();
+    const float w4[4] = {0.25f, 0.75f, 0.75f, 0.25f};
+    for (int o = threadIdx.x; o < kRsX * kRsY * kRsZ; o += 256) {
+        const int ox = o % kRsX, oy = (o / kRsX) % kRsY, oz = o / (kRsX * kRsY);
+        const int cx = cx0 + ox, cy = cy0 + oy, cz = cz0 + oz;
+        if (cx >= c.n[0] || cy >= c.n[1] || cz >= c.n[2]) continue;
+        float acc = 0.f;
+#pragma unroll
+        for (int kz = 0; kz < 4; kz++) {
+            float az = 0.f;
+#pragma unroll
+            for (int ky = 0; ky < 4; ky++) {
+                const float* row = &t[2 * oz + kz][2 * oy + ky][2 * ox];
+                az += w4[ky] * (w4[0] * row[0] + w4[1] * row[1] + w4[2] * row[2] + w4[3] * row[3]);
+            }
+            acc += w4[kz] * az;
+        }
+        c.a[lv_off(c, cx, cy, cz)] = acc;
+    }
+}
+
+// z = B r on the finest level: the tiled kernel when its CTAs fit the reduction's partial slots
+static void launch_up0(const GridDev& g, LView r0, LView cin, float* z, const uint16_t* kind, const float* S0,
+                       const float* q, double* gpart, int gstride, unsigned* ticket, double* out, const int* flag,
+                       cudaStream_t s) {
+    const int bx_n = (g.ni + kUp0X - 1) / kUp0X, by_n = (g.nj + kUp0Y - 1) / kUp0Y;
+    const long blocks = (long)bx_n * by_n * ((g.nk + kUp0Z - 1) / kUp0Z);
+    if (!out || blocks <= gstride) {
+        k_lp_up0_tiled<<<(unsigned)blocks, kUp0X * kUp0Y, 0, s>>>(g, r0, cin, z, kind, S0, q, gpart, gstride, ticket,
+                                                                  out, flag, bx_n, by_n);
+    } else {
+        k_lp_up0<<<node_blocks(g.nv), kNodeThreads, 0, s>>>(g, r0, cin, z, kind, S0, q, gpart, gstride, ticket, out,
+                                                            flag);
+    }
+}
+
 // one thread per voxel of a level
 static int lp_blocks(int nvox, int sms) {
     (void)sms;
     return std::max(1, (nvox + 255) / 256);
+}
+static void launch_restrict(const LView& f, const LView& c, const int* flag, cudaStream_t s, int sms) {
+    const int bx_n = (c.n[0] + kRsX - 1) / kRsX, by_n = (c.n[1] + kRsY - 1) / kRsY;
+    const int blocks = bx_n * by_n * ((c.n[2] + kRsZ - 1) / kRsZ);
+    if (c.nvox >= 32 * 32 * 32)
+        k_lp_restrict_tiled<<<blocks, 256, 0, s>>>(f, c, flag, bx_n, by_n);
+    else
+        k_lp_restrict<<<lp_blocks(c.nvox, sms), 256, 0, s>>>(f, c, flag);
 }
 
 void launch_lp_apply(const GridDev& g, const LpState& L, const float* r, float* z, const uint16_t* kind,
@@ -373,23 +703,38 @@ void launch_lp_apply(const GridDev& g, const LpState& L, const float* r, float* 
     for (int l = 1; l < L.nlev; l++) {
         LView f = l == 1 ? r0 : lp_level_view(L, l - 1, L.z[l - 1]);
         LView c = lp_level_view(L, l, L.z[l]);
-        k_lp_restrict<<<lp_blocks(c.nvox, sms), 256, 0, s>>>(f, c, flag);
+        launch_restrict(f, c, flag, s, sms);
     }
     LView none{};
     none.a = nullptr;
+    if (!L.k5_valid) {
+        const int nnet = std::min(kLpNetLevels, L.nlev - 1);
+        for (int l = 1; l <= nnet; l++)
+            cudaMemcpyAsync(L.k5_host[l - 1], L.fold + (l - 1) * kLpFoldStride + 729, sizeof(float) * 125,
+                            cudaMemcpyDeviceToHost, s);
+        cudaStreamSynchronize(s);
+        L.k5_valid = true;
+    }
     for (int l = L.nlev - 1; l >= 1; l--) {
         LView zin = lp_level_view(L, l, L.z[l]);
         LView cin = l + 1 < L.nlev ? lp_level_view(L, l + 1, L.e[l + 1]) : none;
         LView out = lp_level_view(L, l, L.e[l]);
         int mode = l <= kLpNetLevels ? 1 : 2;
-        const float* fold = mode == 1 ? L.fold + (l - 1) * kLpFold : nullptr;
-        k_lp_up<<<lp_blocks(out.nvox, sms), 256, 0, s>>>(zin, cin, out, mode, fold, (float)(1.0 / L.diag[l]), flag);
+        const float* fold = mode == 1 ? L.fold + (l - 1) * kLpFoldStride : nullptr;
+        if (mode == 1 && out.nvox >= 64 * 64 * 64) {  // smaller levels: one thread per voxel has more parallelism
+            const int bx_n = (out.n[0] + kNetX - 1) / kNetX, by_n = (out.n[1] + kNetY - 1) / kNetY;
+            const int blocks = bx_n * by_n * ((out.n[2] + kNetZ - 1) / kNetZ);
+            K5Param k5;
+            std::memcpy(k5.k, L.k5_host[l - 1], sizeof(k5.k));
+            k_lp_up_net_tiled<<<blocks, kNetX * kNetY, 0, s>>>(zin, cin, out, fold, flag, bx_n, by_n, k5);
+        } else {
+            k_lp_up<<<lp_blocks(out.nvox, sms), 256, 0, s>>>(zin, cin, out, mode, fold, (float)(1.0 / L.diag[l]),
+                                                             flag);
+        }
     }
     LView cin = L.nlev > 1 ? lp_level_view(L, 1, L.e[1]) : none;
-    k_lp_up0<<<node_blocks(g.nv), kNodeThreads, 0, s>>>(g, r0, cin, z, kind, L.W + L.lay.s0, q,
-                                                        red ? red->gpart : nullptr, red ? red->gstride : 0,
-                                                        red ? red->ticket : nullptr,
-                                                        red ? red->scal + kS_RZN : nullptr, flag);
+    launch_up0(g, r0, cin, z, kind, L.W + L.lay.s0, q, red ? red->gpart : nullptr, red ? red->gstride : 0,
+               red ? red->ticket : nullptr, red ? red->scal + kS_RZN : nullptr, flag, s);
 }
 
 // folded stencils of every network level: M = Wm Wl (C x 27), K27[t][t'] = sum_c Wp[t][c] M[c][t'],
@@ -414,7 +759,7 @@ __global__ void k_lp_fold(const float* __restrict__ W, LpLayout lay, float* fold
         float a = 0.f;
         for (int c = 0; c < C; c++) a += Wp[t * C + c] * M[c * 27 + tp];
         K[x] = a;
-        fold[(l - 1) * kLpFold + x] = a;
+        fold[(l - 1) * kLpFoldStride + x] = a;
     }
     __syncthreads();
     for (int d = threadIdx.x; d < 125; d += blockDim.x) {
@@ -426,10 +771,30 @@ __global__ void k_lp_fold(const float* __restrict__ W, LpLayout lay, float* fold
             if (ux < -1 || ux > 1 || uy < -1 || uy > 1 || uz < -1 || uz > 1) continue;
             a += K[t * 27 + 9 * (uz + 1) + 3 * (uy + 1) + ux + 1];
         }
-        fold[(l - 1) * kLpFold + 729 + d] = a;
+        fold[(l - 1) * kLpFoldStride + 729 + d] = a;
+    }
+    // face-class variants: only the first-stage taps t whose point c + o_t stays inside the box
+    for (int x = threadIdx.x; x < 27 * 125; x += blockDim.x) {
+        const int cls = x / 125, d = x % 125;
+        const int cl[3] = {cls % 3, (cls / 3) % 3, cls / 9};
+        const int dd[3] = {d % 5 - 2, (d / 5) % 5 - 2, d / 25 - 2};
+        float a = 0.f;
+        for (int t = 0; t < 27; t++) {
+            const int ot[3] = {t % 3 - 1, (t / 3) % 3 - 1, t / 9 - 1};
+            bool ok = true;
+            int u[3];
+            for (int ax = 0; ax < 3; ax++) {
+                if ((cl[ax] == 1 && ot[ax] == -1) || (cl[ax] == 2 && ot[ax] == 1)) ok = false;
+                u[ax] = dd[ax] - ot[ax];
+                if (u[ax] < -1 || u[ax] > 1) ok = false;
+            }
+            if (ok) a += K[t * 27 + 9 * (u[2] + 1) + 3 * (u[1] + 1) + u[0] + 1];
+        }
+        fold[(l - 1) * kLpFoldStride + kLpFold + x] = a;
     }
 }
 void launch_lp_fold(const LpState& L, cudaStream_t s) {
+    L.k5_valid = false;
     int nnet = std::min(kLpNetLevels, L.nlev - 1);
     if (nnet > 0) k_lp_fold<<<nnet, 256, 0, s>>>(L.W, L.lay, L.fold);
 }
@@ -1096,8 +1461,7 @@ void launch_lp_loss_grad(const GridDev& g, LpState& L, const uint16_t* kind, con
         }
     }
     LView cin1 = L.nlev > 1 ? lp_level_view(L, 1, L.e[1]) : none;
-    k_lp_up0<<<node_blocks(g.nv), kNodeThreads, 0, s>>>(g, r0, cin1, T->e0, kind, L.W + L.lay.s0, nullptr, nullptr, 0,
-                                                        nullptr, nullptr, nullptr);
+    launch_up0(g, r0, cin1, T->e0, kind, L.W + L.lay.s0, nullptr, nullptr, 0, nullptr, nullptr, nullptr, s);
     // loss and its gradient with respect to e
     k_lp_loss<<<grid, 256, 0, s>>>(g, kind, T->e0, x, T->ge, T->part);
     k_lp_loss_scale<<<grid, 256, 0, s>>>(g.nv, T->ge, T->part, T->red);

@@ -35,7 +35,10 @@ struct LpLayout {
     int wm[kLpNetLevels + 1];     // mix   [C][C] (out, in)
     int wp[kLpNetLevels + 1];     // proj  [27][C]
 };
-constexpr int kLpFold = 729 + 125;  // per network level: K27 [27][27] then K5 [125]
+constexpr int kLpFold = 729 + 125;  // per network level: K27 [27][27] then K5 [125] (staged in shared memory)
+// then the 27 face-class variants of K5 [27][125] (class cx + 3 cy + 9 cz per axis: 0 away from a
+// non-periodic face, 1 on its low face, 2 on its high face; variant 0 is K5)
+constexpr int kLpFoldStride = kLpFold + 27 * 125;
 
 struct LpTrain;
 
@@ -48,8 +51,12 @@ struct LpState {
     float* e[kLpMaxLevels] = {};  // level output, levels >= 1
     LpLayout lay{};
     float* W = nullptr;     // parameters (FP32 master copy)
-    float* fold = nullptr;  // folded stencils, kLpFold per network level (index l-1)
+    float* fold = nullptr;  // folded stencils, kLpFoldStride per network level (index l-1)
     LpTrain* train = nullptr;
+    // host copy of every network level's K5, passed to the tiled level kernel as a parameter
+    // (the constant bank feeds the FMAs directly); refreshed on the first apply after a fold
+    mutable float k5_host[kLpNetLevels][125] = {};
+    mutable bool k5_valid = false;
 };
 
 LView lp_view(float* a, const int n[3], int sy, int sz, const int per[3]);
