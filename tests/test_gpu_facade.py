@@ -24,3 +24,64 @@ def test_v3_style_cpp_driver(pic, tmp_path):
     assert int(fields["ts"]) == 11
     assert int(fields["electrons"]) >= 200000 and int(fields["ions"]) >= 200000
     assert int(fields["collisions"]) > 0
+
+
+DRIVER = r"""
+#include <cstdio>
+#include <stdexcept>
+#include "pic_gb300.hpp"
+using namespace pic_gb300;
+int main() {
+    const double amu = 1.660538921e-27, q_e = 1.602176565e-19;
+    World world(17, 17, 17, {0.0, 0.0, 0.0}, {0.016, 0.016, 0.016});
+    world.setTime(1e-7, 100);
+    world.addBox({0.008, 0.008, 0.008}, 0.0, {0.004, 0.004, 0.004});
+    Species O("O", 16 * amu, 0, world, 2e10, 400000);
+    Species O2("O2", 32 * amu, 0, world, 2e10, 400000);
+    Species Op("O+", 16 * amu, q_e, world, 2e10, 100000);
+    O.loadUniform({0, 0, 0}, {0.016, 0.0058, 0.016}, 100000, 600.0, 2e10, 0.0, 1);
+    O2.loadUniform({0, 0, 0}, {0.016, 0.0058, 0.016}, 100000, 900.0, 2e10, 0.0, 2);
+    Op.loadUniform({0, 0, 0}, {0.016, 0.0058, 0.016}, 50000, 30000.0, 2e10, 0.0, 3);
+    DSMC_MEX self(O, world);          // DSMC_MEX(species, world)
+    DSMC_MEX pair(O, O2, world, 7);   // DSMC_MEX(species1, species2, world)
+    bool threw = false;
+    try {
+        Species heavy("X", 40 * amu, 0, world, 3e10, 10);
+        DSMC_MEX bad(O, heavy, world);
+    } catch (const std::invalid_argument&) {
+        threw = true;
+    }
+    Config::getInstance().setSPUTTERING(true);
+    for (int s = 0; s < 20; s++) {
+        world.advanceTime();
+        self.apply(world.getDt());
+        pair.apply(world.getDt());
+        O.advanceNonElectron(O, O, world.getDt() * 50);
+        Op.advanceNonElectron(O, O, world.getDt() * 5);
+    }
+    auto so = O.objectStats(), si = Op.objectStats();
+    auto c1 = self.stats(), c2 = pair.stats();
+    std::printf("threw=%d self=%llu pair=%llu svmax=%g o_hits=%llu o_bounces=%llu i_hits=%llu last=%d\n", threw ? 1 : 0,
+                (unsigned long long)c1[0], (unsigned long long)c2[0], self.sigmaVRelMax(), (unsigned long long)so[0],
+                (unsigned long long)so[1], (unsigned long long)si[0], self.lastStatus() | pair.lastStatus());
+    return 0;
+}
+"""
+
+
+def test_cpp_facade_dsmc_and_objects(pic, tmp_path):
+    pic.library()
+    pkg = os.path.join(ROOT, PKG_NAME)
+    src = tmp_path / "driver.cpp"
+    src.write_text(DRIVER)
+    exe = str(tmp_path / "driver")
+    r = subprocess.run(["g++", "-std=c++17", "-O2", str(src), "-I", os.path.join(ROOT, "include"), "-L",
+                        os.path.join(pkg, "lib"), "-lpic_gb300", "-Wl,-rpath," + os.path.join(pkg, "lib"), "-o", exe],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    f = dict(kv.split("=") for kv in r.stdout.strip().splitlines()[-1].split())
+    assert f["threw"] == "1" and f["last"] == "0"
+    assert int(f["self"]) > 1000 and int(f["pair"]) > 1000 and 1e-17 < float(f["svmax"]) < 1e-14
+    assert int(f["o_hits"]) > 100 and int(f["o_bounces"]) >= int(f["o_hits"]) and int(f["i_hits"]) > 100
