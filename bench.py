@@ -287,15 +287,23 @@ def cpu_reference(wl, gpu_inner_per_step, seed=3, sample=1_000_000, steps=2):
     ef = np.zeros((nv, 3))
     ne_, ni_ = n, n
     t_part = 0.0
+    t_push_mt = 0.0
     for s in range(steps):
         t0 = time.perf_counter()
         _, _, ne_, ni_ = port.mcc_background(g, cp, ele, eid, ne_, ion, iid, ni_, wl["dt"], seed, s)
+        t1 = time.perf_counter()
         ne_ = port.push(g, ele[:ne_], ef, wl["dt"], -QE, ME, ids=eid[:ne_], threads=threads)
+        t_push_mt += time.perf_counter() - t1
         ni_ = port.push(g, ion[:ni_], ef, wl["dt"], QE, 32 * AMU, ids=iid[:ni_], threads=1)
         de = port.number_density(g, ele[:ne_])
         di = port.number_density(g, ion[:ni_])
         t_part += time.perf_counter() - t0
     t_part_per_particle = t_part / steps / (ne_ + ni_)
+    # the same electron push on one thread, for the single-core figure
+    t0 = time.perf_counter()
+    port.push(g, ele[:ne_].copy(), ef, wl["dt"], -QE, ME, ids=eid[:ne_].copy(), threads=1)
+    t_push_1 = time.perf_counter() - t0
+    t_part_1 = (t_part - t_push_mt + steps * t_push_1) / steps / (ne_ + ni_)
     # field work on the full grid
     t0 = time.perf_counter()
     rho = QE * (di - de)
@@ -311,8 +319,10 @@ def cpu_reference(wl, gpu_inner_per_step, seed=3, sample=1_000_000, steps=2):
     t_ef = time.perf_counter() - t0
     n_full = 2 * wl["n_each"]
     t_step = n_full * t_part_per_particle + t_rho + gpu_inner_per_step * t_iter + t_ef
+    t_step_1 = n_full * t_part_1 + t_rho + gpu_inner_per_step * t_iter + t_ef
     return {
         "value": n_full / t_step,
+        "single_thread_value": n_full / t_step_1,
         "unit": "particle-steps/s",
         "cores": threads,
         "kind": "port",
@@ -340,7 +350,7 @@ def run_reference(args, wl, rank, ws):
         "ms_per_step": best["seconds_per_step"] * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": wl["name"]},
-        "cpu_baseline": {k: best[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "cpu_baseline": {k: best[k] for k in ("value", "unit", "cores", "kind", "sample", "single_thread_value")},
         "e2e": {"value": best["value"], "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -435,7 +445,7 @@ def run_gpu(args, wl, rank, ws, local):
     cpu = None
     if rank == 0 and not args.no_cpu and not ensemble:
         cpu = cpu_reference(wl, inner / max(1, args.steps), sample=args.cpu_sample, steps=1)
-        cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample", "single_thread_value")}
     coll = {k: coll1[k] - coll0[k] for k in coll1}
     line = {
         "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": ws,
