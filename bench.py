@@ -72,6 +72,9 @@ MERGE_EVERY = 20  # merge pass cadence in the timed loop (the reference merges e
 MERGE_MIN = 64    # a cell is merged when it holds more than this many particles of a species
 
 
+SORT_EVERY = [20]  # steps between the loop's sort checks (a species re-sorts when 2 % of it moved)
+
+
 def setup_world(pic, wl, seed=1):
     nn, L = wl["nn"], wl["L"]
     W = pic.World(*nn, (0.0, 0.0, 0.0), L)
@@ -89,7 +92,7 @@ def setup_world(pic, wl, seed=1):
     M = pic.MC_MEX_Ionization(e, i, W, wl["n_gas"], 300.0, 32 * AMU, LOTZ["I"], E, S, sigma_ion_kind=1,
                               sigma_ion_params=(LOTZ["A"], LOTZ["b"], LOTZ["c"], 0.0), seed=seed)
     S_ = pic.PotentialSolver(W, 20000, 1e-6, pic.SOLVER_LEARNED)
-    W.configure_loop(solve_each_step=True, sort_every=20, merge_every=MERGE_EVERY, merge_after=0,
+    W.configure_loop(solve_each_step=True, sort_every=SORT_EVERY[0], merge_every=MERGE_EVERY, merge_after=0,
                      merge_min=MERGE_MIN)
     return W, e, i, M, S_
 
@@ -124,7 +127,7 @@ def setup_ensemble(pic, wl, seed=1):
                               sigma_ion_params=(LOTZ["A"], LOTZ["b"], LOTZ["c"], 0.0), seed=seed)
     M.set_slab_density(dens)
     S_ = pic.PotentialSolver(W, 20000, 1e-6, pic.SOLVER_LEARNED)
-    W.configure_loop(solve_each_step=True, sort_every=20, merge_every=MERGE_EVERY, merge_after=0,
+    W.configure_loop(solve_each_step=True, sort_every=SORT_EVERY[0], merge_every=MERGE_EVERY, merge_after=0,
                      merge_min=MERGE_MIN)
     return W, e, i, M, S_
 
@@ -459,7 +462,7 @@ def run_gpu(args, wl, rank, ws, local):
                                       "float-float refinement to 1e-6 relative, warm-started",
                    "collisions_per_step": coll["collisions"] / args.steps,
                    "ionizations_per_step": coll["ionizations"] / args.steps,
-                   "poisson_inner_per_step": inner / args.steps, "sort_every": 20,
+                   "poisson_inner_per_step": inner / args.steps, "sort_every": SORT_EVERY[0],
                    "l2": "inputs larger than L2 (particles %.1f GB)" % (parts_per_step * 36 / 1e9),
                    "merging": "every %d steps, cells above %d particles" % (MERGE_EVERY, MERGE_MIN),
                    "parallelism": "replicas" if ws > 1 else "1 GPU",
@@ -469,6 +472,7 @@ def run_gpu(args, wl, rank, ws, local):
         "roofline": roof,
         "push_deposit_gbs": push_gbs,
         "kernels": kernels,
+        "groups_ms_per_step": {k: v["ms"] / args.steps for k, v in groups.items()},
         "cpu_baseline": cpu,
         "e2e": e2e,
         "poisson_time_to_1e-6": poisson,
@@ -671,7 +675,7 @@ def run_e2e(pic, wl, args, rank):
     pic.MC_MEX_Ionization(e, i, W, wl["n_gas"], 300.0, 32 * AMU, LOTZ["I"], E, S, sigma_ion_kind=1,
                           sigma_ion_params=(LOTZ["A"], LOTZ["b"], LOTZ["c"], 0.0), seed=1)
     Sv = pic.PotentialSolver(W, 20000, 1e-6, pic.SOLVER_LEARNED)
-    W.configure_loop(solve_each_step=True, sort_every=20)
+    W.configure_loop(solve_each_step=True, sort_every=SORT_EVERY[0])
     import ctypes as C
 
     L_ = W._L
@@ -712,11 +716,13 @@ def main():
     ap.add_argument("--poisson", type=int, default=256, help="n of the n^3 Poisson time-to-1e-6 case (0: skip)")
     ap.add_argument("--poisson-methods", default="rbsor,pcg,learned_start,learned",
                     help="comma list of the Poisson solves to time (rbsor, pcg, learned_start, learned)")
+    ap.add_argument("--sort-every", type=int, default=20, help="steps between the loop's sort checks")
     ap.add_argument("--dsmc", type=int, default=128, help="n of the n^3-cell DSMC_MEX case (0: skip)")
     ap.add_argument("--dsmc-only", action="store_true", help="run only the DSMC_MEX case and print it")
     ap.add_argument("--poisson-only", action="store_true",
                     help="run only the Poisson time-to-1e-6 comparison (the second metric) and print it")
     args = ap.parse_args()
+    SORT_EVERY[0] = args.sort_every
     if args.warmup < 3:
         args.warmup = 3
     wl = WORKLOADS[args.workload]
