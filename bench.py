@@ -681,14 +681,19 @@ def run_e2e(pic, wl, args, rank):
     L_ = W._L
     W.synchronize()
     t0 = time.perf_counter()
+    marks = {}
     for sp, (pos, vel, w) in ((e, he), (i, hi)):
         rc = L_.pic_species_add_particles(W.handle, sp.id, C.c_void_p(pos.data_ptr()), C.c_void_p(vel.data_ptr()),
                                           C.c_void_p(w.data_ptr()), None, n, 1)
         if rc:
             raise RuntimeError("upload failed %d" % rc)
         sp.sortIndexes()  # cell order, as after a sort step of the loop
+    W.synchronize()
+    marks["upload_and_sort"] = time.perf_counter() - t0
     Sv.solve(raise_on_fail=True)
     Sv.computeEF()
+    W.synchronize()
+    marks["initial_solve"] = time.perf_counter() - t0 - marks["upload_and_sort"]
     diag = np.zeros(5)
     for _ in range(args.steps):
         W.step()
@@ -696,12 +701,13 @@ def run_e2e(pic, wl, args, rank):
             L_.pic_species_sums(W.handle, sp.id, diag.ctypes.data_as(C.c_void_p))
     W.synchronize()
     t = time.perf_counter() - t0
+    marks["steps"] = t - marks["upload_and_sort"] - marks["initial_solve"]
     parts = e.getNumParticles() + i.getNumParticles()
     W.close()
     h2d = 2 * n * (7 * 8)  # pos, vel, w in FP64
     return {"value": parts * args.steps / t, "unit": "particle-steps/s",
             "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": 2 * 5 * 8 * 512,
-            "seconds": t}
+            "seconds": t, "seconds_by_part": marks}
 
 
 def main():

@@ -922,12 +922,49 @@ int ensure_upload(pic_world* w, long n) {
 }
 }  // namespace
 
+// a pointer the world's device can dereference: its own device memory, or pinned host memory
+// mapped into the unified address space (the kernel then reads it over the host link);
+// nullptr for pageable memory
+static const void* device_view(const pic_world* w, const void* p) {
+    if (!p) return nullptr;
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (at.type == cudaMemoryTypeHost) return at.devicePointer;
+    if ((at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) && at.device == w->device)
+        return at.devicePointer;
+    return nullptr;
+}
+
 extern "C" int pic_species_add_particles(pic_world* w, int sp, const double* pos, const double* vel,
                                          const double* wgt, const uint64_t* ids, long n, int rewind) {
     if (!valid_sp(w, sp) || (n > 0 && (!pos || !vel || !wgt))) return fail(PIC_ERR_ARG, "bad species or arrays");
     if (n == 0) return PIC_OK;
     CU(cudaSetDevice(w->device));
     SpeciesHost& s = w->sp[sp];
+    // arrays the device can read (pinned host or device memory): converted where they lie
+    {
+        const double* dp = static_cast<const double*>(device_view(w, pos));
+        const double* dv = static_cast<const double*>(device_view(w, vel));
+        const double* dw = static_cast<const double*>(device_view(w, wgt));
+        const auto* di = static_cast<const unsigned long long*>(ids ? device_view(w, ids) : nullptr);
+        if (dp && dv && dw && (!ids || di)) {
+            const unsigned long long id0 = s.next_id;
+            const long step = 1l << 30;
+            for (long a = 0; a < n; a += step) {
+                const long m = std::min<long>(step, n - a);
+                Scope sc(w, "load", 5);
+                launch_from_abs(w->g, s.dev, dp + 3 * a, dv + 3 * a, dw + a, di ? di + a : nullptr,
+                                id0 + (unsigned long long)a, (int)m, rewind, (float)(s.charge / s.mass * 0.5 * w->dt),
+                                w->ef, w->stream);
+            }
+            if (!ids) s.next_id += n;
+            CU(cudaStreamSynchronize(w->stream));
+            return check_device_error(w);
+        }
+    }
     // through a reusable device staging buffer, kUploadChunk particles at a time (pos, vel, w and
     // ids in FP64 / u64); without ids the device numbers the particles from next_id on
     int urc = ensure_upload(w, n);

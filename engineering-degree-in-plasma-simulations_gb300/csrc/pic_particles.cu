@@ -892,67 +892,87 @@ void launch_sort(const GridDev& g, SpeciesDev sp, float4* pos_alt, float4* vel_a
 // host <-> device conversion (Species::addParticle semantics when rewind is set)
 // ------------------------------------------------------------------------------------
 // id == nullptr: particle p gets id id0 + p
-__global__ void k_from_abs(GridDev g, SpeciesDev sp, const double* pos, const double* vel, const double* w,
-                           const unsigned long long* id, unsigned long long id0, int n, int rewind, float qm_half_dt,
-                           const float4* ef) {
-    int n0 = sp.counts[0];
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
-        int dst = n0 + p;
-        if (dst >= sp.capacity) continue;
-        double x[3] = {pos[3 * p], pos[3 * p + 1], pos[3 * p + 2]};
-        float3 v = make_float3((float)vel[3 * p], (float)vel[3 * p + 1], (float)vel[3 * p + 2]);
-        bool ok = !(isnan(x[0]) || isnan(x[1]) || isnan(x[2]) || isnan(v.x) || isnan(v.y) || isnan(v.z));
-        int ijk[3];
-        float o[3];
-        int nc3[3] = {g.ci, g.cj, g.ck};
-        for (int d = 0; d < 3 && ok; d++) {
-            if (g.periodic[d]) {
-                double L = g.xm[d] - g.x0[d];
-                if (x[d] < g.x0[d]) x[d] += L;
-                else if (x[d] >= g.xm[d]) x[d] -= L;
-            }
-            if (x[d] < g.x0[d] || x[d] >= g.xm[d]) ok = false;
-            double lc = (x[d] - g.x0[d]) / g.dxd[d];
-            int c = (int)lc;
-            if (c >= nc3[d]) c = nc3[d] - 1;
-            double f = lc - c;
-            ijk[d] = c;
-            o[d] = fminf((float)f, 0x1.fffffep-1f);
+// one particle of an upload: Species::addParticle semantics when rewind is set
+__device__ __forceinline__ void from_abs_one(const GridDev& g, const SpeciesDev& sp, int n0, int p, const double* xp,
+                                             const double* vp, const double* w, const unsigned long long* id,
+                                             unsigned long long id0, int rewind, float qm_half_dt, const float4* ef) {
+    int dst = n0 + p;
+    if (dst >= sp.capacity) return;
+    double x[3] = {xp[0], xp[1], xp[2]};
+    float3 v = make_float3((float)vp[0], (float)vp[1], (float)vp[2]);
+    bool ok = !(isnan(x[0]) || isnan(x[1]) || isnan(x[2]) || isnan(v.x) || isnan(v.y) || isnan(v.z));
+    int ijk[3];
+    float o[3];
+    int nc3[3] = {g.ci, g.cj, g.ck};
+    for (int d = 0; d < 3 && ok; d++) {
+        if (g.periodic[d]) {
+            double L = g.xm[d] - g.x0[d];
+            if (x[d] < g.x0[d]) x[d] += L;
+            else if (x[d] >= g.xm[d]) x[d] -= L;
         }
-        int cell = -1;
-        if (ok) {
-            cell = pack_cell(ijk[0], ijk[1], ijk[2]);
-            if (g.n_boxes) {
-                float X = ((float)ijk[0] + o[0]) * g.dx[0], Y = ((float)ijk[1] + o[1]) * g.dx[1],
-                      Z = ((float)ijk[2] + o[2]) * g.dx[2];
-                for (int b = 0; b < g.n_boxes; b++)
-                    if (X >= g.box_lo[b][0] && X <= g.box_hi[b][0] && Y >= g.box_lo[b][1] && Y <= g.box_hi[b][1] &&
-                        Z >= g.box_lo[b][2] && Z <= g.box_hi[b][2])
-                        cell = -1;
-            }
+        if (x[d] < g.x0[d] || x[d] >= g.xm[d]) ok = false;
+        double lc = (x[d] - g.x0[d]) / g.dxd[d];
+        int c = (int)lc;
+        if (c >= nc3[d]) c = nc3[d] - 1;
+        double f = lc - c;
+        ijk[d] = c;
+        o[d] = fminf((float)f, 0x1.fffffep-1f);
+    }
+    int cell = -1;
+    if (ok) {
+        cell = pack_cell(ijk[0], ijk[1], ijk[2]);
+        if (g.n_boxes) {
+            float X = ((float)ijk[0] + o[0]) * g.dx[0], Y = ((float)ijk[1] + o[1]) * g.dx[1],
+                  Z = ((float)ijk[2] + o[2]) * g.dx[2];
+            for (int b = 0; b < g.n_boxes; b++)
+                if (X >= g.box_lo[b][0] && X <= g.box_hi[b][0] && Y >= g.box_lo[b][1] && Y <= g.box_hi[b][1] &&
+                    Z >= g.box_lo[b][2] && Z <= g.box_hi[b][2])
+                    cell = -1;
         }
-        if (cell >= 0 && rewind && ef) {
-            // vel -= q/m E dt/2 (Species.cpp:431)
-            PushArgs dummy;
-            dummy.ef = ef;
-            Tile t;
-            t.etile = nullptr;
-            t.dtile = nullptr;
-            t.lo = 0;
-            t.span = -1;
-            t.off[0] = 0;
-            t.off[1] = g.ni;
-            t.off[2] = g.ni * g.nj;
-            t.off[3] = g.ni * g.nj + g.ni;
-            float3 E = gather_e(dummy, t, cell_base_node(g, ijk[0], ijk[1], ijk[2]), make_float3(o[0], o[1], o[2]));
-            v.x -= qm_half_dt * E.x;
-            v.y -= qm_half_dt * E.y;
-            v.z -= qm_half_dt * E.z;
+    }
+    if (cell >= 0 && rewind && ef) {
+        // vel -= q/m E dt/2 (Species.cpp:431)
+        PushArgs dummy;
+        dummy.ef = ef;
+        Tile t;
+        t.etile = nullptr;
+        t.dtile = nullptr;
+        t.lo = 0;
+        t.span = -1;
+        t.off[0] = 0;
+        t.off[1] = g.ni;
+        t.off[2] = g.ni * g.nj;
+        t.off[3] = g.ni * g.nj + g.ni;
+        float3 E = gather_e(dummy, t, cell_base_node(g, ijk[0], ijk[1], ijk[2]), make_float3(o[0], o[1], o[2]));
+        v.x -= qm_half_dt * E.x;
+        v.y -= qm_half_dt * E.y;
+        v.z -= qm_half_dt * E.z;
+    }
+    sp.pos[dst] = make_float4(o[0], o[1], o[2], __int_as_float(cell));
+    sp.vel[dst] = make_float4(v.x, v.y, v.z, (float)w[p]);
+    sp.id[dst] = id ? id[p] : id0 + (unsigned long long)p;
+    if (cell < 0) sp.dead[atomicAdd(&sp.counts[2], 1)] = dst;
+}
+// Block-cooperative: a block stages the FP64 positions and velocities of its 256 particles in
+// shared memory with contiguous reads (each source sector is read once, which matters when the
+// arrays are pinned host memory read over the host link), then converts one particle per thread.
+__global__ void __launch_bounds__(256) k_from_abs(GridDev g, SpeciesDev sp, const double* pos, const double* vel,
+                                                  const double* w, const unsigned long long* id,
+                                                  unsigned long long id0, int n, int rewind, float qm_half_dt,
+                                                  const float4* ef) {
+    __shared__ double s_pos[3 * 256], s_vel[3 * 256];
+    const int n0 = sp.counts[0];
+    for (long long base = (long long)blockIdx.x * 256; base < n; base += (long long)gridDim.x * 256) {
+        const int m = (int)min(256ll, n - base);
+        for (int e = threadIdx.x; e < 3 * m; e += 256) {
+            s_pos[e] = pos[3 * base + e];
+            s_vel[e] = vel[3 * base + e];
         }
-        sp.pos[dst] = make_float4(o[0], o[1], o[2], __int_as_float(cell));
-        sp.vel[dst] = make_float4(v.x, v.y, v.z, (float)w[p]);
-        sp.id[dst] = id ? id[p] : id0 + (unsigned long long)p;
-        if (cell < 0) sp.dead[atomicAdd(&sp.counts[2], 1)] = dst;
+        __syncthreads();
+        if ((int)threadIdx.x < m)
+            from_abs_one(g, sp, n0, (int)base + (int)threadIdx.x, s_pos + 3 * threadIdx.x, s_vel + 3 * threadIdx.x, w,
+                         id, id0, rewind, qm_half_dt, ef);
+        __syncthreads();
     }
 }
 __global__ void k_from_abs_count(SpeciesDev sp, int n, unsigned* err) {

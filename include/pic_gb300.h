@@ -79,7 +79,9 @@ int pic_species_create(pic_world* w, const char* name, double mass, double charg
 /* Species::addParticle(pos, vel, w) for n particles                   Species.cpp:420-434
  * rewind = 1: drop NaN / out-of-bounds / in-object particles and rewind v by q/m E dt/2 (as
  * the reference); rewind = 0: place as given (as the interactions' emplace_back).
- * ids may be NULL (sequential ids are assigned). */
+ * ids may be NULL (sequential ids are assigned).  Arrays in pinned host memory (or in the
+ * device's own memory) are read in place by the conversion kernel; pageable arrays go through
+ * a device staging buffer. */
 int pic_species_add_particles(pic_world* w, int sp, const double* pos, const double* vel, const double* wgt,
                               const uint64_t* ids, long n, int rewind);
 /* Synthetic loader (GPU form of Species::loadParticleBoxThermal, Species.cpp:564-599): n
