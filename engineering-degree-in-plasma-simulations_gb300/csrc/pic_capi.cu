@@ -1419,7 +1419,8 @@ extern "C" int pic_species_sort(pic_world* w, int sp, int32_t* cell_counts) {
 extern "C" int pic_species_sums(pic_world* w, int sp, double* out) {
     if (!valid_sp(w, sp) || !out) return fail(PIC_ERR_ARG, "bad arguments");
     CU(cudaSetDevice(w->device));
-    int grid = 512;
+    // enough CTAs to keep the particle stream in flight (5 partials per CTA fit the partial buffer)
+    const int grid = std::min(8 * w->sms, kParts * 8 / 5);
     {
         Scope sc(w, "sums", 1);
         launch_sums(w->sp[sp].dev, w->part, w->stream, grid);
