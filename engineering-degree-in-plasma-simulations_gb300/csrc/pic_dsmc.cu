@@ -5,8 +5,8 @@
 // candidate pairs; a pair collides with probability sigma(v_rel) v_rel / (sigma v)_max and is
 // scattered isotropically in its centre-of-mass frame.  Cells are independent, so the GPU form
 // gives every cell one thread that runs that cell's groups in order on the species' sorted
-// velocities (cell c owns [start[c], start[c+1])).  Draws come from Philox-4x32-10 keyed by
-// (cell, call, tag, group) instead of one global MT19937 stream, and the one-species second
+// velocities (cell c owns [start[c], start[c+1])).  Draws come from one Philox-4x32-10 block keyed
+// by (cell, call, tag, group) instead of one global MT19937 stream, and the one-species second
 // partner is drawn directly from the np-1 other particles (the reference redraws until it
 // differs: the same distribution).  (sigma v)_max follows the reference's rule: after a call
 // with at least one collision it becomes the largest sigma v of that call's candidates; the
@@ -49,16 +49,19 @@ __global__ void __launch_bounds__(128) k_dsmc(DsmcArgs a) {
             float4 v1 = v1p[i1], v2 = v2p[i2];
             const float dx = v1.x - v2.x, dy = v1.y - v2.y, dz = v1.z - v2.z;
             const float g2 = dx * dx + dy * dy + dz * dz;
-            const float sv = a.K * powf(g2, a.ex);
+            // K (g^2)^ex through the hardware base-2 logarithm and exponential (g2 = 0 gives 0)
+            const float sv = a.K * exp2f(a.ex * __log2f(g2));
             mx = fmaxf(mx, sv);
             npairs++;
             if (!(sv > u01(r.z) * svmax)) continue;
             ncoll++;
-            const uint4 q = philox4x32_10(make_uint4((unsigned)c, a.call, a.tag | 0x00800000u, (unsigned)gi), a.key);
+            // the azimuth's uniform from the nine low bits of r.x, r.y, r.z (their high 23 bits
+            // drew the pair and the acceptance), so a collision needs no second block
+            const unsigned low27 = (r.x & 511u) | ((r.y & 511u) << 9) | ((r.z & 511u) << 18);
             const float ck = 2.f * u01(r.w) - 1.f;
             const float sk = sqrtf(fmaxf(1.f - ck * ck, 0.f));
             float se, ce;
-            sincospif(2.f * u01(q.x), &se, &ce);
+            sincospif(2.f * ((float)low27 + 0.5f) * (1.0f / 134217728.0f), &se, &ce);
             const float gm = sqrtf(g2);
             const float r0 = gm * ck, r1 = gm * sk * ce, r2 = gm * sk * se;
             const float cx = a.f1 * v1.x + a.f2 * v2.x;

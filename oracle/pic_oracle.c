@@ -1638,11 +1638,10 @@ long or_dsmc_gpuform(const or_dsmc_params* q, double* vel1, const int32_t* cnt1,
             n_pairs++;
             if (!(sv > or_u01_from_u32(rr[2]) * svmax)) continue;
             n_coll++;
-            uint32_t ctr2[4] = {(uint32_t)c, call, tag | 0x00800000u, (uint32_t)gi}, qq[4];
-            or_philox4x32_10(ctr2, key, qq);
+            uint32_t low27 = (rr[0] & 511u) | ((rr[1] & 511u) << 9) | ((rr[2] & 511u) << 18);
             double ck = 2 * or_u01_from_u32(rr[3]) - 1;
             double sk = sqrt(fmax(1 - ck * ck, 0.0));
-            double eps = 2 * 3.14159265358979323846 * or_u01_from_u32(qq[0]);
+            double eps = 2 * 3.14159265358979323846 * (((double)low27 + 0.5) / 134217728.0);
             double gm = sqrt(g2);
             double vr[3] = {gm * ck, gm * sk * cos(eps), gm * sk * sin(eps)};
             for (int k = 0; k < 3; k++) {

@@ -169,8 +169,9 @@ long or_dsmc_ref(const or_grid* g, const or_dsmc_params* q, or_mt* r, or_particl
 
 /* GPU form (restated from the CUDA kernel, in FP64 on the same draws): particles of each
  * species contiguous in cell order, cnt1/cnt2[nc] per cell (vel2/cnt2 NULL: one species);
- * group gi of cell c draws Philox block (c, call, tag, gi) for the pair, the acceptance and
- * cos(chi), and block (c, call, tag | 0x00800000, gi) for the azimuth of a collision;
+ * group gi of cell c draws Philox block (c, call, tag, gi): the high 23 bits of its words for
+ * the pair, the acceptance and cos(chi), the low 9 bits of the first three words (27 bits) for
+ * the azimuth of a collision;
  * sigma v_rel is evaluated as K (v_rel^2)^(1-omega), K = pi d^2 c2^(omega-1/2) / Gamma.
  * svmax is the FP32 majorant the kernel reads; *svmax_step receives the largest sigma v of
  * the candidates (the next majorant when any pair collided).  Returns the collisions. */
