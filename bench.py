@@ -1,17 +1,22 @@
 """Benchmark of the GB300 PIC + DSMC step loop: particle-steps per second on one GB300.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload large|discharge|plain]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload large|discharge|mid|ensemble]
     python bench.py --impl reference ...   (the reference algorithm on the host cores)
 
 A step is one iteration of the ch4/v3 time loop on the workload's synthetic discharge:
-electron-impact collisions against the O2 background (fused into the electron push), leapfrog
-push with trilinear gather and fixed-point deposition for both species, charge density,
-FP64-refined Poisson solve to a 1e-6 relative residual, E = -grad(phi), and a counting sort
-by cell every 20 steps.  value = particles pushed per step / device step time (CUDA events on
-the library's stream).  Inputs (particles, fields) are resident in HBM and larger than L2.
-e2e runs the same K steps through the C ABI from pinned host buffers: the particle upload and
-a per-step read of the conservation diagnostics (Outputs.cpp:143-182) are inside its clock.
-One JSON line on stdout (rank 0).
+electron-impact collisions against the O2 background, leapfrog push with trilinear gather and
+fixed-point deposition for both species, charge density, Poisson solve warm-started from the
+last potential to ||b - L phi|| <= 1e-6 min(||b||, ||rho/eps0||) in float-float refinement (the
+residual relative to the space-charge part of b as well, so that the electrode term cannot hide
+an unresolved space-charge potential), E = -grad(phi), a counting sort by cell when 2 % of a
+species moved (checked every 20 steps) and a merge pass every 20 steps.  value = particles pushed
+per step / device step time (CUDA events on the library's stream).  Inputs (particles, fields)
+are resident in HBM and larger than L2.  e2e runs the same K steps through the C ABI from pinned
+host buffers: the particle upload and a per-step read of the conservation diagnostics
+(Outputs.cpp:143-182) are inside its clock.  Beside the headline (the large discharge) the line
+carries the electrode discharge (64x64x256), the 64-instance ensemble, and the Poisson
+time-to-tolerance comparisons at 256^3 (blob charge) and 128^3 (a charge-density snapshot of the
+discharge), each with a CPU baseline.  One JSON line on stdout (rank 0).
 """
 import argparse
 import importlib
@@ -73,6 +78,20 @@ MERGE_MIN = 64    # a cell is merged when it holds more than this many particles
 
 
 SORT_EVERY = [20]  # steps between the loop's sort checks (a species re-sorts when 2 % of it moved)
+STOP = ["charge"]  # Poisson stopping rule of the loop and of the time-to-tolerance cases
+WARM = ["extrapolate"]  # start of the loop's warm solves: "previous" phi or "extrapolate"d in time
+STOP_TEXT = {"charge": "||b - L phi|| <= 1e-6 min(||b||, ||rho/eps0||)", "rhs": "||b - L phi|| <= 1e-6 ||b||"}
+
+
+def stop_rule(pic):
+    return pic.STOP_REL_CHARGE if STOP[0] == "charge" else pic.STOP_REL_RHS
+
+
+def loop_solver(pic, W):
+    """The loop's Poisson solver: learned-preconditioned flexible CG, the stopping rule and warm start."""
+    S = pic.PotentialSolver(W, 20000, 1e-6, pic.SOLVER_LEARNED, stop=stop_rule(pic))
+    S.setWarmStart(pic.WARM_EXTRAPOLATE if WARM[0] == "extrapolate" else pic.WARM_PREVIOUS)
+    return S
 
 
 def setup_world(pic, wl, seed=1):
@@ -91,7 +110,7 @@ def setup_world(pic, wl, seed=1):
     E, S = sigma_tables()
     M = pic.MC_MEX_Ionization(e, i, W, wl["n_gas"], 300.0, 32 * AMU, LOTZ["I"], E, S, sigma_ion_kind=1,
                               sigma_ion_params=(LOTZ["A"], LOTZ["b"], LOTZ["c"], 0.0), seed=seed)
-    S_ = pic.PotentialSolver(W, 20000, 1e-6, pic.SOLVER_LEARNED)
+    S_ = loop_solver(pic, W)
     W.configure_loop(solve_each_step=True, sort_every=SORT_EVERY[0], merge_every=MERGE_EVERY, merge_after=0,
                      merge_min=MERGE_MIN)
     return W, e, i, M, S_
@@ -126,7 +145,7 @@ def setup_ensemble(pic, wl, seed=1):
     M = pic.MC_MEX_Ionization(e, i, W, float(dens[0]), 300.0, 32 * AMU, LOTZ["I"], E, S, sigma_ion_kind=1,
                               sigma_ion_params=(LOTZ["A"], LOTZ["b"], LOTZ["c"], 0.0), seed=seed)
     M.set_slab_density(dens)
-    S_ = pic.PotentialSolver(W, 20000, 1e-6, pic.SOLVER_LEARNED)
+    S_ = loop_solver(pic, W)
     W.configure_loop(solve_each_step=True, sort_every=SORT_EVERY[0], merge_every=MERGE_EVERY, merge_after=0,
                      merge_min=MERGE_MIN)
     return W, e, i, M, S_
@@ -144,6 +163,8 @@ class ClockSampler:
         self.proc = None
 
     def __enter__(self):
+        if self.index < 0:  # not sampled
+            return self
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
                                           "--format=csv,noheader,nounits", "-lms", "200"],
@@ -255,107 +276,178 @@ def aggregate(parts_per_rank, seconds_per_rank, ws):
 # ------------------------------------------------------------------------------------------
 # CPU side: the reference algorithm (oracle port of ch4/v3) on the host cores
 # ------------------------------------------------------------------------------------------
-def cpu_reference(wl, gpu_inner_per_step, seed=3, sample=1_000_000, steps=2):
-    """Times the FP64 restatement of the reference loop on a bounded sample.
+LOOP_POISSON = os.path.join(ROOT, "profiles", "loop_poisson_iterations.json")
 
-    Particle work (collisions, push, deposit) runs on `sample` electrons + `sample` ions for
-    `steps` steps and is scaled linearly to the full particle count; the field work (charge
-    density, Poisson iterations at the GPU's average count per step, E field) runs on the full
-    grid.  The electron push uses host_cores-1 threads like the reference's ThreadPool; the ion
-    push, deposit and collisions are serial as in the reference."""
-    import oracle as O
 
-    port = O.Port()
-    nn, L = wl["nn"], wl["L"]
-    g = port.grid(nn, (0, 0, 0), L, periodic=(1, 1, 0))
-    kind = port.node_kinds(g, 1)
-    nv = int(np.prod(nn))
-    threads = max(1, (os.cpu_count() or 2) - 1)
-    rng = np.random.default_rng(seed)
-    n = min(sample, wl["n_each"])
+def measured_loop_poisson(key):
+    """Poisson work per step of the GPU loop on a workload (inner FP32 iterations and FP64
+    residual passes), measured by this benchmark's GPU arm and recorded in
+    profiles/loop_poisson_iterations.json; the reference arm charges the same work."""
+    with open(LOOP_POISSON) as f:
+        rec = json.load(f)[key]
+    return rec
 
-    def make(T, mass):
-        p = np.zeros(int(n * 1.2) + 1024, O.PARTICLE)
-        p["pos"][:n] = rng.uniform((0, 0, 0.3 * L[2]), (L[0], L[1], 0.7 * L[2]), (n, 3))
-        p["vel"][:n] = rng.normal(size=(n, 3)) * np.sqrt(KB * T / mass)
-        p["w"][:n] = rng.lognormal(np.log(wl["w_mean"]) - 0.125, 0.5, n)
-        return p
 
-    ele, ion = make(2.0 * EV_K, ME), make(0.03 * EV_K, 32 * AMU)
-    eid = np.arange(len(ele), dtype=np.uint64)
-    iid = np.arange(len(ion), dtype=np.uint64) + (1 << 40)
-    E, S = sigma_tables()
-    cp = port.coll_params(E, S, 32 * AMU, LOTZ["I"], 1, (0.0, LOTZ["b"], LOTZ["c"]), sig_A=LOTZ["A"],
-                          n_neutral=wl["n_gas"], T_neutral=300.0)
-    ef = np.zeros((nv, 3))
-    ne_, ni_ = n, n
-    t_part = 0.0
-    t_push_mt = 0.0
-    for s in range(steps):
+class CpuLoop:
+    """The FP64 port of the reference loop (oracle/pic_oracle.c, a restatement of ch4/v3) on the
+    host cores, one step at a time on a bounded sample of a workload.
+
+    Particle work (collisions, push, deposit) runs on `sample` electrons + `sample` ions and is
+    scaled linearly to the workload's particle count; the electron push uses host_cores-1
+    threads like the reference's ThreadPool, the ion push, deposit and collisions are serial as
+    in the reference.  Field work runs on the full grid (one instance grid, times the instance
+    count, for the ensemble): charge density, Poisson work at a given count of Jacobi-PCG
+    iterations and FP64 residual passes (one of each timed per step and scaled), and E."""
+
+    def __init__(self, wl, sample=1_000_000, seed=3):
+        import oracle as O
+
+        self.O = O
+        self.port = O.Port()
+        self.wl = wl
+        ens = wl.get("kind") == "ensemble"
+        self.instances = wl["instances"] if ens else 1
+        nn, L = wl["nn"], wl["L"]
+        self.nn = nn
+        self.g = self.port.grid(nn, (0, 0, 0), L, periodic=(1, 1, 0))
+        self.kind = self.port.node_kinds(self.g, 1)
+        self.nv = int(np.prod(nn))
+        self.threads = max(1, (os.cpu_count() or 2) - 1)
+        rng = np.random.default_rng(seed)
+        if ens:
+            nI = wl["instances"]
+            counts = np.exp(np.random.default_rng(1).uniform(np.log(wl["n_range"][0]), np.log(wl["n_range"][1]),
+                                                             nI)).astype(np.int64)
+            self.n_full = 2 * int(counts.sum())
+            w_mean = wl["density"] * L[0] * L[1] * 0.4 * L[2] / float(np.median(counts))
+            V, n_gas = wl["V"][1], wl["n_gas"][1]
+        else:
+            self.n_full = 2 * wl["n_each"]
+            w_mean, V, n_gas = wl["w_mean"], wl["V"], wl["n_gas"]
+        self.V = V
+        n = min(sample, self.n_full // 2)
+        self.n = n
+
+        def make(T, mass):
+            p = np.zeros(int(n * 1.2) + 1024, O.PARTICLE)
+            p["pos"][:n] = rng.uniform((0, 0, 0.3 * L[2]), (L[0], L[1], 0.7 * L[2]), (n, 3))
+            p["vel"][:n] = rng.normal(size=(n, 3)) * np.sqrt(KB * T / mass)
+            p["w"][:n] = rng.lognormal(np.log(w_mean) - 0.125, 0.5, n)
+            return p
+
+        self.ele, self.ion = make(2.0 * EV_K, ME), make(0.03 * EV_K, 32 * AMU)
+        self.eid = np.arange(len(self.ele), dtype=np.uint64)
+        self.iid = np.arange(len(self.ion), dtype=np.uint64) + (1 << 40)
+        E, S = sigma_tables()
+        self.cp = self.port.coll_params(E, S, 32 * AMU, LOTZ["I"], 1, (0.0, LOTZ["b"], LOTZ["c"]), sig_A=LOTZ["A"],
+                                        n_neutral=n_gas, T_neutral=300.0)
+        self.ef = np.zeros((self.nv, 3))
+        self.ne, self.ni = n, n
+        self.s = 0
+        self.phi = np.zeros(self.nv)
+        fixed = np.nonzero(self.kind == O.FIXED)[0]
+        self.phi[fixed] = np.where(fixed // (nn[0] * nn[1]) == nn[2] - 1, V, 0.0)
+
+    def particle_step(self, electron_threads=None):
+        """Collisions, pushes and deposits of the sample; seconds, and of that the electron push."""
+        O, port, wl = self.O, self.port, self.wl
+        th = self.threads if electron_threads is None else electron_threads
         t0 = time.perf_counter()
-        _, _, ne_, ni_ = port.mcc_background(g, cp, ele, eid, ne_, ion, iid, ni_, wl["dt"], seed, s)
+        _, _, self.ne, self.ni = port.mcc_background(self.g, self.cp, self.ele, self.eid, self.ne, self.ion, self.iid,
+                                                      self.ni, wl["dt"], 1, self.s)
         t1 = time.perf_counter()
-        ne_ = port.push(g, ele[:ne_], ef, wl["dt"], -QE, ME, ids=eid[:ne_], threads=threads)
-        t_push_mt += time.perf_counter() - t1
-        ni_ = port.push(g, ion[:ni_], ef, wl["dt"], QE, 32 * AMU, ids=iid[:ni_], threads=1)
-        de = port.number_density(g, ele[:ne_])
-        di = port.number_density(g, ion[:ni_])
-        t_part += time.perf_counter() - t0
-    t_part_per_particle = t_part / steps / (ne_ + ni_)
-    # the same electron push on one thread, for the single-core figure
-    t0 = time.perf_counter()
-    port.push(g, ele[:ne_].copy(), ef, wl["dt"], -QE, ME, ids=eid[:ne_].copy(), threads=1)
-    t_push_1 = time.perf_counter() - t0
-    t_part_1 = (t_part - t_push_mt + steps * t_push_1) / steps / (ne_ + ni_)
-    # field work on the full grid
-    t0 = time.perf_counter()
-    rho = QE * (di - de)
-    t_rho = time.perf_counter() - t0
-    phi = np.zeros(nv)
-    phi[kind == O.FIXED] = np.where(np.arange(nv)[kind == O.FIXED] // (nn[0] * nn[1]) == nn[2] - 1, wl["V"], 0.0)
-    probe = 3
-    t0 = time.perf_counter()
-    port.solve_fpcg(g, kind, phi, rho, 1e-30, probe)
-    t_iter = (time.perf_counter() - t0) / probe
-    t0 = time.perf_counter()
-    port.compute_ef(g, phi)
-    t_ef = time.perf_counter() - t0
-    n_full = 2 * wl["n_each"]
-    t_step = n_full * t_part_per_particle + t_rho + gpu_inner_per_step * t_iter + t_ef
-    t_step_1 = n_full * t_part_1 + t_rho + gpu_inner_per_step * t_iter + t_ef
-    return {
-        "value": n_full / t_step,
-        "single_thread_value": n_full / t_step_1,
-        "unit": "particle-steps/s",
-        "cores": threads,
-        "kind": "port",
-        "sample": (f"{n} e- + {n} O2+ for {steps} steps on the full {nn[0]}x{nn[1]}x{nn[2]} grid "
-                   f"(collisions, push, deposit: {t_part_per_particle * 1e9:.1f} ns/particle-step, scaled to "
-                   f"{n_full} particles); charge density, {gpu_inner_per_step:.1f} PCG iterations "
-                   f"({t_iter:.3f} s each, timed on {probe}) and E field on the full grid"),
-        "seconds_per_step": t_step,
-    }
+        self.ne = port.push(self.g, self.ele[:self.ne], self.ef, wl["dt"], -QE, ME, ids=self.eid[:self.ne],
+                            threads=th)
+        t2 = time.perf_counter()
+        self.ni = port.push(self.g, self.ion[:self.ni], self.ef, wl["dt"], QE, 32 * AMU, ids=self.iid[:self.ni])
+        self.de = port.number_density(self.g, self.ele[:self.ne])
+        self.di = port.number_density(self.g, self.ion[:self.ni])
+        t3 = time.perf_counter()
+        self.s += 1
+        return t3 - t0, t2 - t1
+
+    def iteration_seconds(self, rho):
+        """Seconds of one Jacobi-PCG iteration of the port on the full grid: the difference of a
+        3-iteration and a 1-iteration solve from the same start (the set-up cancels), timed once."""
+        if getattr(self, "t_iter", None) is None:
+            ts = []
+            for its in (1, 3):
+                phi = self.phi.copy()
+                t0 = time.perf_counter()
+                self.port.solve_fpcg(self.g, self.kind, phi, rho, 1e-30, its)
+                ts.append(time.perf_counter() - t0)
+            self.t_iter = max((ts[1] - ts[0]) / 2, 1e-9)
+        return self.t_iter
+
+    def step(self, inner, refine):
+        """One sampled step; the estimated seconds of the full workload's step."""
+        O, port = self.O, self.port
+        t_part, _ = self.particle_step()
+        per_particle = t_part / (self.ne + self.ni)
+        t0 = time.perf_counter()
+        rho = QE * (self.di - self.de)
+        t_rho = time.perf_counter() - t0
+        t_iter = self.iteration_seconds(rho)
+        t0 = time.perf_counter()
+        port.residual(self.g, self.kind, self.phi, rho)  # one FP64 residual pass
+        t_res = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        self.ef = port.compute_ef(self.g, self.phi)
+        t_ef = time.perf_counter() - t0
+        field = (t_rho + inner * t_iter + refine * t_res + t_ef) * self.instances
+        return {"seconds": self.n_full * per_particle + field, "ns_per_particle": per_particle * 1e9,
+                "t_iter": t_iter, "t_res": t_res, "field": field}
+
+    def describe(self, inner, refine, steps, rec):
+        nn = self.nn
+        grid = f"{nn[0]}x{nn[1]}x{nn[2]}" + (f" (x{self.instances} instances)" if self.instances > 1 else "")
+        return (f"per step: {self.n} e- + {self.n} O2+ (collisions, push with {self.threads} threads, deposit: "
+                f"{rec['ns_per_particle']:.1f} ns/particle-step, scaled to {self.n_full} particles); charge density, "
+                f"{inner:.2f} Jacobi-PCG iterations ({rec['t_iter']:.3f} s each, timed once as the difference of 3- and "
+                f"1-iteration solves) and {refine:.2f} FP64 residual passes ({rec['t_res']:.3f} s each, timed every "
+                f"step) -- the GPU loop's measured Poisson work per step -- and E on the full {grid} grid; "
+                f"{steps} steps timed")
+
+
+def cpu_baseline(wl, inner, refine, sample=1_000_000, steps=1):
+    """The CPU port on `steps` sampled steps of the workload, and on one thread for the electron push."""
+    loop = CpuLoop(wl, sample=sample)
+    loop.particle_step()  # warm-up
+    recs = [loop.step(inner, refine) for _ in range(steps)]
+    t = sum(r["seconds"] for r in recs)
+    value = loop.n_full * steps / t
+    # the single-core figure: the electron push on one thread (the rest is serial already)
+    t_mt = loop.particle_step()[1]
+    t1 = loop.particle_step(electron_threads=1)[1]
+    extra = (t1 - t_mt) / (loop.ne + loop.ni) * loop.n_full
+    single = loop.n_full / (t / steps + extra)
+    return {"value": value, "unit": "particle-steps/s", "cores": loop.threads, "kind": "port",
+            "sample": loop.describe(inner, refine, steps, recs[-1]), "single_thread_value": single,
+            "seconds_per_step": t / steps}
 
 
 def run_reference(args, wl, rank, ws):
     if rank != 0:
         return
-    # the Poisson iteration count per step follows the plain PCG on this grid; 60 is the
-    # warm-started count measured on the GPU for this workload and is re-read when available
-    inner = float(os.environ.get("PIC_BENCH_INNER_ITERS", "60"))
-    samples = []
-    for _ in range(max(1, args.steps // 10)):
-        samples.append(cpu_reference(wl, inner, sample=args.cpu_sample, steps=1))
-    best = max(samples, key=lambda s: s["value"])
+    rec = measured_loop_poisson(args.workload)
+    inner, refine = rec["inner_per_step"], rec["refinements_per_step"]
+    loop = CpuLoop(wl, sample=args.cpu_sample)
+    for _ in range(args.warmup):
+        loop.particle_step()  # untimed warm-up steps (particle work only)
+    recs = [loop.step(inner, refine) for _ in range(args.steps)]
+    t = sum(r["seconds"] for r in recs)
+    value = loop.n_full * args.steps / t
+    cpu = {"value": value, "unit": "particle-steps/s", "cores": loop.threads, "kind": "port",
+           "sample": loop.describe(inner, refine, args.steps, recs[-1])}
     line = {
-        "metric": "particle-steps/s", "value": best["value"], "unit": "particle-steps/s", "impl": "reference",
+        "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "impl": "reference",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": best["seconds_per_step"] * 1e3, "higher_is_better": True, "scaling": "weak",
+        "ms_per_step": t / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": wl["name"]},
-        "cpu_baseline": {k: best[k] for k in ("value", "unit", "cores", "kind", "sample", "single_thread_value")},
-        "e2e": {"value": best["value"], "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
-                "d2h_bytes_per_step": 0},
+        "config": {"workload": wl["name"], "poisson_inner_per_step": inner, "poisson_refinements_per_step": refine,
+                   "poisson_work_source": rec.get("source", "")},
+        "cpu_baseline": cpu,
+        "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
@@ -363,10 +455,12 @@ def run_reference(args, wl, rank, ws):
 # ------------------------------------------------------------------------------------------
 # GPU arm
 # ------------------------------------------------------------------------------------------
-def run_gpu(args, wl, rank, ws, local):
+def measure_loop(pic, args, wl, rank, ws, local, clocks=True):
+    """K timed steps of the loop on a workload (after the initial solve, the autotuner and W
+    warm-up steps): throughput, the roofline of the dominant kernel group, the Poisson work per
+    step and the final solve's norms.  Returns (result dict, world, species) with the world open."""
     import torch
 
-    pic = importlib.import_module(PKG)
     ensemble = wl.get("kind") == "ensemble"
     W, e, i, M, S = (setup_ensemble if ensemble else setup_world)(pic, wl, seed=1 + rank)
     assert S.solve(raise_on_fail=True)  # initial vacuum + space-charge field (main.cpp:172-173)
@@ -383,7 +477,7 @@ def run_gpu(args, wl, rank, ws, local):
     coll0 = M.stats()
     barrier(ws)
     W.synchronize()
-    with ClockSampler(local) as clk:
+    with ClockSampler(local if clocks else -1) as clk:
         # the timed steps are the profiler range (cudaProfilerStart/Stop; no effect without a profiler)
         torch.cuda.profiler.start()
         t0 = time.perf_counter()
@@ -397,13 +491,13 @@ def run_gpu(args, wl, rank, ws, local):
     step_ms, _ = W.timer("step")
     st1 = S.stats()
     coll1 = M.stats()
+    norms = S.norms()
     groups = {}
-    for name in ("push_deposit", "mcc", "compact", "rho", "poisson", "efield", "sort"):
+    for name in ("push_deposit", "mcc", "compact", "rho", "poisson", "efield", "sort", "merge"):
         ms, nl = W.timer(name)
         groups[name] = dict(ms=ms, launches=nl)
     parts_per_step = 0.5 * (n0 + n1)
     value = aggregate(parts_per_step * args.steps, step_ms / 1e3, ws)
-    # roofline of the dominant kernel group
     peak, peak_kind = measured_peak()
     nv = int(W.nv)
     inner = st1["inner"] - st0["inner"]
@@ -420,11 +514,10 @@ def run_gpu(args, wl, rank, ws, local):
         "rho": (2 * 20.0 + 4.0) * nv * args.steps,
     }
     kernels = {}
-    for name, b in algo.items():
+    for name, b_ in algo.items():
         ms = groups[name]["ms"]
         if ms > 0:
-            kernels[name] = dict(share=ms / step_ms, achieved_gbs=b / (ms / 1e3) / 1e9,
-                                 ms_per_step=ms / args.steps)
+            kernels[name] = dict(share=ms / step_ms, achieved_gbs=b_ / (ms / 1e3) / 1e9, ms_per_step=ms / args.steps)
     dom = max(kernels, key=lambda k: kernels[k]["share"])
     launches_dom = max(1, groups[dom]["launches"])
     achieved = algo[dom] / (groups[dom]["ms"] / 1e3) / 1e9
@@ -433,54 +526,123 @@ def run_gpu(args, wl, rank, ws, local):
             "frac": achieved / peak, "peak_source": peak_kind,
             "traffic": traffic * algo[dom] / launches_dom if traffic else None,
             "algorithmic_bytes_per_launch": algo[dom] / launches_dom}
-    push_ms = groups["push_deposit"]["ms"]
-    push_gbs = algo["push_deposit"] / (push_ms / 1e3) / 1e9 if push_ms > 0 else None
-    clocks = clk.summary()
+    coll = {k: coll1[k] - coll0[k] for k in coll1}
+    res = {
+        "value": value, "ms_per_step": step_ms / args.steps, "wall_s": wall, "gpu_launches": launches,
+        "parts_per_step": parts_per_step, "roofline": roof, "kernels": kernels,
+        "groups_ms_per_step": {k: v["ms"] / args.steps for k, v in groups.items()},
+        "inner_per_step": inner / args.steps, "refinements_per_step": refine / args.steps,
+        "collisions_per_step": coll["collisions"] / args.steps, "ionizations_per_step": coll["ionizations"] / args.steps,
+        # how much of b the space charge carries, and the final residual against both scales
+        "poisson_norms": {"rho_over_b": norms["charge"] / norms["b"] if norms["b"] > 0 else None,
+                          "residual_rel_b": norms["r"] / norms["b"] if norms["b"] > 0 else None,
+                          "residual_rel_charge": norms["r"] / norms["charge"] if norms["charge"] > 0 else None},
+        "autotuned": tuned, "clocks": clk.summary() if clocks else None,
+    }
+    return res, W, (e, i)
+
+
+def run_gpu(args, wl, rank, ws, local):
+    pic = importlib.import_module(PKG)
+    ensemble = wl.get("kind") == "ensemble"
+    res, W, _ = measure_loop(pic, args, wl, rank, ws, local)
     W.close()
     # e2e: same loop through the C ABI from pinned host buffers (upload + per-step diagnostics)
     e2e = None if ensemble else run_e2e(pic, wl, args, rank)
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(wl, res["inner_per_step"], res["refinements_per_step"], sample=args.cpu_sample)
+        cpu.pop("seconds_per_step", None)
+    extra = {}
     poisson = None
-    if rank == 0 and args.poisson > 0:
-        poisson = poisson_bench(pic, args.poisson, methods=args.poisson_methods.split(","))
+    poisson128 = None
     dsmc = None
+    if rank == 0 and args.extra and args.workload == "large":
+        extra, snap = extra_workloads(pic, args, rank, ws, local)
+        if args.poisson > 0 and snap is not None:
+            poisson128 = poisson_bench(pic, (128, 128, 128), WORKLOADS["discharge"]["L"],
+                                       WORKLOADS["discharge"]["V"], rho=snap, cpu=not args.no_cpu,
+                                       methods=args.poisson_methods.split(","),
+                                       rho_name="charge-density snapshot of the electrode discharge after its "
+                                                "timed steps, trilinearly resampled onto 128^3 nodes")
+    if rank == 0 and args.poisson > 0:
+        n = args.poisson
+        poisson = poisson_bench(pic, (n, n, n), (0.04, 0.04, 0.04), 1000.0, cpu=not args.no_cpu,
+                                methods=args.poisson_methods.split(","))
     if rank == 0 and args.dsmc > 0:
         dsmc = dsmc_bench(pic, args.dsmc, cpu=not args.no_cpu)
-    cpu = None
-    if rank == 0 and not args.no_cpu and not ensemble:
-        cpu = cpu_reference(wl, inner / max(1, args.steps), sample=args.cpu_sample, steps=1)
-        cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample", "single_thread_value")}
-    coll = {k: coll1[k] - coll0[k] for k in coll1}
     line = {
-        "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": ws,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms / args.steps,
+        "metric": "particle-steps/s", "value": res["value"], "unit": "particle-steps/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["ms_per_step"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
         "config": {"workload": wl["name"],
                    "grid": list(wl["nn"]) + ([wl["instances"]] if ensemble else []),
-                   "particles_per_step": parts_per_step,
+                   "particles_per_step": res["parts_per_step"],
                    "poisson": "flexible CG with the learned multilevel preconditioner, FP32 iterations in "
-                                      "float-float refinement to 1e-6 relative, warm-started",
-                   "collisions_per_step": coll["collisions"] / args.steps,
-                   "ionizations_per_step": coll["ionizations"] / args.steps,
-                   "poisson_inner_per_step": inner / args.steps, "sort_every": SORT_EVERY[0],
-                   "l2": "inputs larger than L2 (particles %.1f GB)" % (parts_per_step * 36 / 1e9),
+                              "float-float refinement, warm start: " + WARM[0] + "; stop: " + STOP_TEXT[STOP[0]],
+                   "collisions_per_step": res["collisions_per_step"],
+                   "ionizations_per_step": res["ionizations_per_step"],
+                   "poisson_inner_per_step": res["inner_per_step"],
+                   "poisson_refinements_per_step": res["refinements_per_step"],
+                   "poisson_norms": res["poisson_norms"],
+                   "sort_every": SORT_EVERY[0],
+                   "l2": "inputs larger than L2 (particles %.1f GB)" % (res["parts_per_step"] * 36 / 1e9),
                    "merging": "every %d steps, cells above %d particles" % (MERGE_EVERY, MERGE_MIN),
                    "parallelism": "replicas" if ws > 1 else "1 GPU",
-                   "autotuned": tuned},
-        "wall_s": wall,
-        "gpu_launches": launches,
-        "roofline": roof,
-        "push_deposit_gbs": push_gbs,
-        "kernels": kernels,
-        "groups_ms_per_step": {k: v["ms"] / args.steps for k, v in groups.items()},
+                   "autotuned": res["autotuned"]},
+        "wall_s": res["wall_s"],
+        "gpu_launches": res["gpu_launches"],
+        "roofline": res["roofline"],
+        "push_deposit_gbs": res["kernels"].get("push_deposit", {}).get("achieved_gbs"),
+        "kernels": res["kernels"],
+        "groups_ms_per_step": res["groups_ms_per_step"],
         "cpu_baseline": cpu,
         "e2e": e2e,
+        "workloads": extra or None,
         "poisson_time_to_1e-6": poisson,
+        "poisson_128_discharge_rho": poisson128,
         "dsmc": dsmc,
-        "clocks": clocks,
+        "clocks": res["clocks"],
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def extra_workloads(pic, args, rank, ws, local):
+    """The electrode discharge and the 64-instance ensemble, each K steps after W warm-up steps
+    with its roofline and CPU baseline; returns them and the discharge's final charge density."""
+    out = {}
+    snap = None
+    for key in ("discharge", "ensemble"):
+        wl = WORKLOADS[key]
+        res, W, _ = measure_loop(pic, args, wl, rank, 1, local, clocks=False)
+        if key == "discharge":
+            snap = (W.rho.reshape(wl["nn"][2], wl["nn"][1], wl["nn"][0]), wl["nn"])
+        W.close()
+        cpu = None
+        if not args.no_cpu:
+            cpu = cpu_baseline(wl, res["inner_per_step"], res["refinements_per_step"], sample=args.cpu_sample)
+            cpu.pop("seconds_per_step", None)
+        out[key] = {"workload": wl["name"], "metric": "particle-steps/s", "value": res["value"],
+                    "unit": "particle-steps/s", "ms_per_step": res["ms_per_step"], "steps": args.steps,
+                    "particles_per_step": res["parts_per_step"], "roofline": res["roofline"],
+                    "groups_ms_per_step": res["groups_ms_per_step"],
+                    "poisson_inner_per_step": res["inner_per_step"],
+                    "poisson_refinements_per_step": res["refinements_per_step"],
+                    "poisson_norms": res["poisson_norms"], "gpu_launches": res["gpu_launches"],
+                    "cpu_baseline": cpu}
+    return out, snap
+
+
+def resample(field, nn_src, nn_dst):
+    """Trilinear resampling of a node field ([k][j][i], nn_src nodes) onto nn_dst nodes spanning
+    the same box."""
+    from scipy.ndimage import map_coordinates
+
+    axes = [np.linspace(0, nn_src[d] - 1, nn_dst[d]) for d in range(3)]
+    kk, jj, ii = np.meshgrid(axes[2], axes[1], axes[0], indexing="ij")
+    return map_coordinates(field, [kk, jj, ii], order=1, mode="nearest").ravel()
 
 
 def blob_rho(nn, seed):
@@ -499,24 +661,36 @@ def blob_rho(nn, seed):
     return rho.ravel()
 
 
-def poisson_bench(pic, n, seed=5, train_steps=300, methods=("rbsor", "pcg", "learned_start", "learned")):
-    """Time to a 1e-6 FP64 relative residual from the Dirichlet-only start, n^3 nodes over a
-    0.04 m cube, z faces at 0 V / 1000 V, periodic x, y; blob charge density.  Plain red-black
-    SOR and Jacobi-PCG against the learned multilevel preconditioner, first at its starting
-    (BPX) weights, then after online training on the pairs of four solves of other blob densities
-    plus white-noise pairs.  Training time is reported separately (it is amortised over a run)."""
-    nn = (n, n, n)
-    W = pic.World(n, n, n, (0.0, 0.0, 0.0), (0.04, 0.04, 0.04))
-    W.set_boundaries((1, 1, 0), (1,) * 6, (0, 0, 0, 0, 0.0, 1000.0))
-    rho_test = blob_rho(nn, seed)
+def poisson_bench(pic, nn, L, V, rho=None, seed=5, train_steps=300, cpu=True,
+                  methods=("rbsor", "pcg", "learned_start", "learned"), rho_name=None):
+    """Time to tolerance (the loop's stopping rule at 1e-6) from the Dirichlet-only start on nn
+    nodes over the box L, z faces at 0 V / V, periodic x, y; the charge density is a seeded sum of
+    Gaussian blobs, or a given snapshot (field [k][j][i], its node counts) resampled onto nn.
+    Plain red-black SOR and Jacobi-PCG against the learned multilevel preconditioner, first at its
+    starting (BPX) weights, then after online training on the pairs of four solves of other blob
+    densities plus white-noise pairs (training time reported separately: it is amortised over a
+    run).  The learned solve's roofline counts 56 B per node and iteration (CG 40, fine-level apply
+    14, coarse levels 2) and 24 B per node and FP64 residual pass; the CPU baseline is the port's
+    FP64 Jacobi-PCG (the reference's method) timed on a few iterations of the same system and
+    charged the GPU Jacobi-PCG's iteration count."""
+    nn = tuple(int(v) for v in nn)
+    W = pic.World(*nn, (0.0, 0.0, 0.0), L)
+    W.set_boundaries((1, 1, 0), (1,) * 6, (0, 0, 0, 0, 0.0, V))
+    if rho is None:
+        rho_test = blob_rho(nn, seed)
+        rho_name = "seeded sum of 8-64 Gaussian blobs (amplitude +-1e-3 C/m^3, widths 2-20 cells)"
+    else:
+        rho_test = resample(rho[0], rho[1], nn)
     W.rho = rho_test
     phi0 = W.phi
-    omega = 2.0 / (1.0 + np.sin(np.pi / (n - 1)))  # optimal SOR weight of the model problem
-    out = {"grid": [n, n, n], "tol": 1e-6}
+    omega = 2.0 / (1.0 + np.sin(np.pi / (max(nn) - 1)))  # optimal SOR weight of the model problem
+    out = {"grid": list(nn), "box": list(L), "anode_V": V, "rho": rho_name, "tol": 1e-6, "stop": STOP_TEXT[STOP[0]]}
+    nv = int(np.prod(nn))
 
     def timed(method, w=1.4):
         W.phi = phi0
-        S = pic.PotentialSolver(W, 200000, 1e-6, method, omega=w)
+        S = pic.PotentialSolver(W, 200000, 1e-6, method, omega=w, stop=stop_rule(pic))
+        st0 = S.stats()
         W.timing(True)
         W.timing_reset()
         W.synchronize()
@@ -526,8 +700,12 @@ def poisson_bench(pic, n, seed=5, train_steps=300, methods=("rbsor", "pcg", "lea
         wall = time.perf_counter() - t0
         dev_ms, launches = W.timer("poisson")
         W.timing(False)
+        st1 = S.stats()
+        nr = S.norms()
         return {"seconds": wall, "iterations": S.iters, "rel": S.rel, "converged": ok,
-                "device_seconds": dev_ms / 1e3, "launches": launches}
+                "device_seconds": dev_ms / 1e3, "launches": launches,
+                "refinements": st1["refinements"] - st0["refinements"],
+                "rho_over_b": nr["charge"] / nr["b"] if nr["b"] > 0 else None}
 
     if "rbsor" in methods:
         out["rbsor"] = timed(pic.SOLVER_RBSOR, omega)
@@ -538,32 +716,54 @@ def poisson_bench(pic, n, seed=5, train_steps=300, methods=("rbsor", "pcg", "lea
     lp.reset()
     if "learned_start" in methods:
         out["learned_start"] = timed(pic.SOLVER_LEARNED)
-    if "learned" not in methods:
-        W.close()
-        return out
-    # online training on (rho, phi) pairs of the run's other solves
-    W.synchronize()
-    t0 = time.perf_counter()
-    lp.collect(True)
-    S = pic.PotentialSolver(W, 200000, 1e-6, pic.SOLVER_LEARNED)
-    for k in range(4):
-        W.rho = blob_rho(nn, seed + 101 + k)
-        W.phi = phi0
-        S.solve()
-    lp.collect(False)
-    cal_before, cal_after = lp.calibrate()  # level gains, judged by validation solves
-    rounds = [{"calibration": True, "val_iters_before": cal_before, "val_iters_after": cal_after, "kept": True}]
-    for k in range(max(1, train_steps // 100)):
-        loss, before, after, kept = lp.train(100, lr=1e-3 / (1 + k), pair_every=0)
-        rounds.append({"loss": loss, "val_iters_before": before, "val_iters_after": after, "kept": kept})
-    W.synchronize()
-    train_s = time.perf_counter() - t0
-    W.rho = rho_test
-    out["learned"] = timed(pic.SOLVER_LEARNED)
-    out["learned"]["training"] = {"pair_solves": 4, "steps": train_steps, "seconds": train_s, "rounds": rounds}
-    for m in ("pcg", "rbsor"):
-        if m in out:
-            out["speedup_vs_" + m] = out[m]["seconds"] / out["learned"]["seconds"]
+    if "learned" in methods:
+        # online training on (rho, phi) pairs of the run's other solves
+        W.synchronize()
+        t0 = time.perf_counter()
+        lp.collect(True)
+        S = pic.PotentialSolver(W, 200000, 1e-6, pic.SOLVER_LEARNED, stop=stop_rule(pic))
+        for k in range(4):
+            W.rho = blob_rho(nn, seed + 101 + k)
+            W.phi = phi0
+            S.solve()
+        lp.collect(False)
+        cal_before, cal_after = lp.calibrate()  # level gains, judged by validation solves
+        rounds = [{"calibration": True, "val_iters_before": cal_before, "val_iters_after": cal_after, "kept": True}]
+        for k in range(max(1, train_steps // 100)):
+            loss, before, after, kept = lp.train(100, lr=1e-3 / (1 + k), pair_every=0)
+            rounds.append({"loss": loss, "val_iters_before": before, "val_iters_after": after, "kept": kept})
+        W.synchronize()
+        train_s = time.perf_counter() - t0
+        W.rho = rho_test
+        out["learned"] = timed(pic.SOLVER_LEARNED)
+        out["learned"]["training"] = {"pair_solves": 4, "steps": train_steps, "seconds": train_s, "rounds": rounds}
+        r = out["learned"]
+        peak, peak_kind = measured_peak()
+        achieved = (56.0 * nv * r["iterations"] + 24.0 * nv * r["refinements"]) / r["device_seconds"] / 1e9
+        out["learned"]["roofline"] = {"bound": "hbm", "kernel": "learned CG iteration", "achieved": achieved,
+                                      "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind}
+        for m in ("pcg", "rbsor"):
+            if m in out:
+                out["speedup_vs_" + m] = out[m]["seconds"] / out["learned"]["seconds"]
+    if cpu and "pcg" in out:
+        import oracle as O
+
+        port = O.Port()
+        g = port.grid(nn, (0, 0, 0), L, periodic=(1, 1, 0))
+        kind = port.node_kinds(g, 1)
+        phi = np.zeros(nv)
+        fixed = np.nonzero(kind == O.FIXED)[0]
+        phi[fixed] = np.where(fixed // (nn[0] * nn[1]) == nn[2] - 1, V, 0.0)
+        probe = 3
+        t0 = time.perf_counter()
+        port.solve_fpcg(g, kind, phi, rho_test, 1e-30, probe)
+        t_iter = (time.perf_counter() - t0) / probe
+        its = out["pcg"]["iterations"]
+        out["cpu_baseline"] = {"value": its * t_iter, "unit": "s", "cores": 1, "kind": "port",
+                               "sample": "FP64 Jacobi-PCG of the port, %d iterations timed on the same system "
+                                         "(%.3f s each), charged the GPU Jacobi-PCG's %d iterations" % (probe, t_iter, its)}
+        if "learned" in out:
+            out["speedup_vs_cpu_pcg"] = out["cpu_baseline"]["value"] / out["learned"]["seconds"]
     W.close()
     return out
 
@@ -674,8 +874,9 @@ def run_e2e(pic, wl, args, rank):
     E, S = sigma_tables()
     pic.MC_MEX_Ionization(e, i, W, wl["n_gas"], 300.0, 32 * AMU, LOTZ["I"], E, S, sigma_ion_kind=1,
                           sigma_ion_params=(LOTZ["A"], LOTZ["b"], LOTZ["c"], 0.0), seed=1)
-    Sv = pic.PotentialSolver(W, 20000, 1e-6, pic.SOLVER_LEARNED)
-    W.configure_loop(solve_each_step=True, sort_every=SORT_EVERY[0])
+    Sv = loop_solver(pic, W)
+    W.configure_loop(solve_each_step=True, sort_every=SORT_EVERY[0], merge_every=MERGE_EVERY, merge_after=0,
+                     merge_min=MERGE_MIN)
     import ctypes as C
 
     L_ = W._L
@@ -723,12 +924,20 @@ def main():
     ap.add_argument("--poisson-methods", default="rbsor,pcg,learned_start,learned",
                     help="comma list of the Poisson solves to time (rbsor, pcg, learned_start, learned)")
     ap.add_argument("--sort-every", type=int, default=20, help="steps between the loop's sort checks")
+    ap.add_argument("--stop", default="charge", choices=sorted(STOP_TEXT),
+                    help="Poisson stopping rule: charge (relative to min(||b||, ||rho/eps0||)) or rhs (to ||b||)")
+    ap.add_argument("--warm", default="extrapolate", choices=["extrapolate", "previous"],
+                    help="start of the loop's warm Poisson solves: the last phi, or extrapolated in time")
+    ap.add_argument("--no-extra", dest="extra", action="store_false",
+                    help="skip the discharge, ensemble and 128^3 snapshot cases beside the headline")
     ap.add_argument("--dsmc", type=int, default=128, help="n of the n^3-cell DSMC_MEX case (0: skip)")
     ap.add_argument("--dsmc-only", action="store_true", help="run only the DSMC_MEX case and print it")
     ap.add_argument("--poisson-only", action="store_true",
                     help="run only the Poisson time-to-1e-6 comparison (the second metric) and print it")
     args = ap.parse_args()
     SORT_EVERY[0] = args.sort_every
+    STOP[0] = args.stop
+    WARM[0] = args.warm
     if args.warmup < 3:
         args.warmup = 3
     wl = WORKLOADS[args.workload]
@@ -736,8 +945,10 @@ def main():
     if args.poisson_only:
         if rank == 0 and args.impl != "reference":
             pic = importlib.import_module(PKG)
+            n = args.poisson or 256
             print(json.dumps({"metric": "Poisson time-to-1e-6 FP64 residual", "unit": "s",
-                              "poisson_time_to_1e-6": poisson_bench(pic, args.poisson or 256,
+                              "poisson_time_to_1e-6": poisson_bench(pic, (n, n, n), (0.04, 0.04, 0.04), 1000.0,
+                                                                    cpu=not args.no_cpu,
                                                                     methods=args.poisson_methods.split(","))}),
                   flush=True)
         return

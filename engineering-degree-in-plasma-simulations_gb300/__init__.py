@@ -16,6 +16,8 @@ LIB_PATH = os.path.join(_HERE, "lib", "libpic_gb300.so")
 
 PIC_OK, PIC_ERR_ARG, PIC_ERR_CUDA, PIC_ERR_NOT_CONVERGED, PIC_ERR_CAPACITY, PIC_ERR_DEVICE = range(6)
 SOLVER_RBSOR, SOLVER_PCG, SOLVER_LEARNED = 0, 1, 2
+STOP_REL_RHS, STOP_ABS_RMS, STOP_REL_CHARGE = 0, 1, 2  # Poisson stopping rules (pic_solver_set_stop)
+WARM_PREVIOUS, WARM_EXTRAPOLATE = 0, 1  # start of a warm solve (pic_solver_set_warm_start)
 GS, PCG = SOLVER_RBSOR, SOLVER_PCG  # reference SolverType names (PotentialSolver.h:24)
 
 # ch4/v3/src/all.h:16-25
@@ -91,6 +93,9 @@ def library():
         "pic_solver_solve": [vp, vp, vp],
         "pic_solver_compute_ef": [vp],
         "pic_solver_stats": [vp, vp, vp, vp],
+        "pic_solver_set_stop": [vp, i, d],
+        "pic_solver_set_warm_start": [vp, i],
+        "pic_solver_last_norms": [vp, vp],
         "pic_mcc_create": [vp, i, i, d, d, d, d, d, i, vp, vp, vp, i, u64],
         "pic_mcc_apply": [vp, d],
         "pic_mcc_stats": [vp, vp],
@@ -104,6 +109,7 @@ def library():
         "pic_species_merge": [vp, i, i],
         "pic_merge_stats": [vp, vp],
         "pic_synchronize": [vp],
+        "pic_debug_set_wait_polls": [vp, C.c_longlong],
         "pic_last_error": [C.c_char_p, i],
         "pic_timing_enable": [vp, i],
         "pic_timing_read": [vp, C.c_char_p, vp, vp],
@@ -523,13 +529,27 @@ class WarmBeamSource(ColdBeamSource):
 class PotentialSolver:
     """PotentialSolver(world, max_it, tol, type) -- ch4/v3/src/PotentialSolver.h:26-88.
 
-    tol is the FP64 relative residual ||b - L phi|| / ||b|| of the reduced system."""
+    tol is the FP64 relative residual ||b - L phi|| / ||b|| of the reduced system, unless `stop`
+    chooses another rule: STOP_ABS_RMS (the reference's sqrt(||r||^2 / nv) <= tol) or
+    STOP_REL_CHARGE (relative to min(||b||, ||rho/eps0||))."""
 
-    def __init__(self, world, max_solver_it, tolerance, solver_type=SOLVER_PCG, omega=1.4):
+    def __init__(self, world, max_solver_it, tolerance, solver_type=SOLVER_PCG, omega=1.4, stop=None):
         self.world = world
         _check(world._L.pic_solver_configure(world._h, int(solver_type), float(tolerance), int(max_solver_it),
                                              float(omega)))
+        _check(world._L.pic_solver_set_stop(world._h, int(STOP_REL_RHS if stop is None else stop),
+                                            float(tolerance)))
         self.iters, self.rel = 0, float("nan")
+
+    def setWarmStart(self, mode):
+        """WARM_PREVIOUS (the last potential) or WARM_EXTRAPOLATE (plus the last step's change)."""
+        _check(self.world._L.pic_solver_set_warm_start(self.world._h, int(mode)))
+
+    def norms(self):
+        """(||b - L phi||, ||b||, ||rho/eps0||) of the last solve's final residual (FREE nodes)."""
+        out = np.zeros(3)
+        _check(self.world._L.pic_solver_last_norms(self.world._h, _p(out)))
+        return dict(r=out[0], b=out[1], charge=out[2])
 
     def solve(self, raise_on_fail=False):
         it, rel = C.c_int(), C.c_double()

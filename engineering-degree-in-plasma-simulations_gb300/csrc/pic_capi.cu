@@ -154,6 +154,12 @@ struct pic_world {
     // solver
     int method = PIC_SOLVER_PCG;
     double tol = 1e-6;
+    int stop_rule = PIC_STOP_REL_RHS;
+    int warm_mode = PIC_WARM_PREVIOUS;  // start of a warm solve (PIC_WARM_*)
+    float* dphi = nullptr;  // the last solve's total change of phi (FP32), for PIC_WARM_EXTRAPOLATE
+    bool dphi_valid = false;  // dphi holds the change of one warm solve
+    int jacobi_skip = 0;  // warm solves left that skip the Jacobi attempt (its last one failed)
+    double last_norms[3] = {0, 0, 0};  // |r|, |b|, |rho/eps0| of the last solve's final residual
     int max_it = 10000;
     double omega = 1.4;
     long n_solves = 0, n_refine = 0, n_inner = 0;
@@ -188,6 +194,7 @@ struct pic_world {
     long launches = 0;
     int grid_nodes = 1024;
     int grid_push_mcc = 304, grid_push = 456, grid_parts = 1216;
+    long long wait_polls_arg = 0;  // PushArgs::wait_polls of this world's pushes (0: the default)
 };
 
 namespace {
@@ -630,6 +637,7 @@ extern "C" int pic_world_destroy(pic_world* w) {
     if (w->stream) cudaStreamSynchronize(w->stream);
     free_lp(w);
     if (w->rho_prev) cudaFree(w->rho_prev);
+    if (w->dphi) cudaFree(w->dphi);
     if (w->aux_pairs) cudaFree(w->aux_pairs);
     if (w->cand_slab) cudaFree(w->cand_slab);
     if (w->mcc_cand) cudaFree(w->mcc_cand);
@@ -1134,6 +1142,7 @@ int push_species(pic_world* w, int sp, double dt, int deposit, bool with_mcc, bo
     a.dep_scale = (float)s.scale;
     a.staged = 1;
     a.err = w->err;
+    a.wait_polls = w->wait_polls_arg;
     a.coll.enabled = 0;
     if (with_mcc && w->mcc_on && sp == w->mcc_e) {
         a.coll = w->coll;
@@ -1459,9 +1468,42 @@ extern "C" int pic_solver_configure(pic_world* w, int method, double tol_rel, in
     return PIC_OK;
 }
 
+extern "C" int pic_solver_set_stop(pic_world* w, int rule, double tol) {
+    if (!w || (rule != PIC_STOP_REL_RHS && rule != PIC_STOP_ABS_RMS && rule != PIC_STOP_REL_CHARGE) || !(tol > 0))
+        return fail(PIC_ERR_ARG, "bad stopping rule");
+    w->stop_rule = rule;
+    w->tol = tol;
+    return PIC_OK;
+}
+
+extern "C" int pic_solver_set_warm_start(pic_world* w, int mode) {
+    if (!w || (mode != PIC_WARM_PREVIOUS && mode != PIC_WARM_EXTRAPOLATE)) return fail(PIC_ERR_ARG, "bad warm-start mode");
+    w->warm_mode = mode;
+    w->dphi_valid = false;
+    return PIC_OK;
+}
+
+extern "C" int pic_solver_last_norms(pic_world* w, double* out) {
+    if (!w || !out) return fail(PIC_ERR_ARG, "null argument");
+    for (int c = 0; c < 3; c++) out[c] = w->last_norms[c];
+    return PIC_OK;
+}
+
 namespace {
-// FP64 residual (optionally after phi += e), returns |r|^2 and |b|^2 on the host
-int residual_norms(pic_world* w, SolveWork& sw, int apply_e, double& r2, double& b2) {
+// the quantity the residual norm is compared with: tol * stop_scale(...) (PIC_STOP_* rules)
+double stop_scale(const pic_world* w, double b2, double s2) {
+    const double bn = b2 > 0 ? std::sqrt(b2) : 1.0;
+    switch (w->stop_rule) {
+        case PIC_STOP_ABS_RMS:  // sqrt(|r|^2 / nv) <= tol (PotentialSolver.cpp:150-158)
+            return std::sqrt((double)w->g.nv);
+        case PIC_STOP_REL_CHARGE:  // relative to the smaller of |b| and its space-charge part
+            return s2 > 0 ? std::min(bn, std::sqrt(s2)) : bn;
+        default:
+            return bn;
+    }
+}
+// FP64 residual (optionally after phi += e), returns |r|^2, |b|^2 and |rho/eps0|^2 on the host
+int residual_norms(pic_world* w, SolveWork& sw, int apply_e, double& r2, double& b2, double& s2) {
     if (!w->rho_prev) {
         CU(cudaMalloc(&w->rho_prev, sizeof(float) * w->g.nv));
         CU(cudaMalloc(&w->bfix, sizeof(float) * w->g.nv));
@@ -1474,10 +1516,11 @@ int residual_norms(pic_world* w, SolveWork& sw, int apply_e, double& r2, double&
     w->phi = sw.phi;
     w->phi_alt = sw.phi_alt;
     w->n_refine++;
-    CU(cudaMemcpyAsync(w->h_scal, w->scal + 8, sizeof(double) * 2, cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaMemcpyAsync(w->h_scal, w->scal + kS_R2, sizeof(double) * 4, cudaMemcpyDeviceToHost, w->stream));
     CU(cudaStreamSynchronize(w->stream));
     r2 = w->h_scal[0];
     b2 = w->h_scal[1];
+    s2 = w->h_scal[3];
     w->rhs_valid = true;
     // r holds the float-float residual rounded to FP32: at most half an ulp per node, plus the
     // float-float evaluation error (about 2^-44 of the terms, bounded generously)
@@ -1485,15 +1528,16 @@ int residual_norms(pic_world* w, SolveWork& sw, int apply_e, double& r2, double&
     return PIC_OK;
 }
 // the residual of the current phi for the new rho from the last FP64 residual (FP32 update)
-int residual_update(pic_world* w, SolveWork& sw, double& r2, double& b2) {
+int residual_update(pic_world* w, SolveWork& sw, double& r2, double& b2, double& s2) {
     {
         Scope sc(w, "poisson", 1);
         launch_rhs_update(w->g, sw, w->rho_prev, w->bfix, w->stream);
     }
-    CU(cudaMemcpyAsync(w->h_scal, w->scal + 8, sizeof(double) * 3, cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaMemcpyAsync(w->h_scal, w->scal + kS_R2, sizeof(double) * 4, cudaMemcpyDeviceToHost, w->stream));
     CU(cudaStreamSynchronize(w->stream));
     r2 = w->h_scal[0];
     b2 = w->h_scal[1];
+    s2 = w->h_scal[3];
     // per FREE node the update t = fl(fl(rho - rho_prev) * fl(1/eps0)) is within 3.01 u |t| of
     // (rho - rho_prev) / eps0 and the sum r + t rounds by at most u |r_new|; by the triangle
     // inequality the 2-norm of the error of r grows by at most 3.01 u |t| + u |r_new|
@@ -1502,14 +1546,18 @@ int residual_update(pic_world* w, SolveWork& sw, double& r2, double& b2) {
 }
 // the FP32-updated residual is certified without a full pass when its norm plus the bound on its
 // error stays below the tolerance (the FP32-summed norms carry a relative error below 1e-5)
-bool estimate_certified(const pic_world* w, double r2, double b2) {
-    return std::sqrt(r2) * (1.0 + 1e-5) + w->r_err <= w->tol * std::sqrt(b2) * (1.0 - 1e-5);
+bool estimate_certified(const pic_world* w, double r2, double scale) {
+    return std::sqrt(r2) * (1.0 + 1e-5) + w->r_err <= w->tol * scale * (1.0 - 1e-5);
 }
 
 int ensure_lp_train(pic_world* w);
 
 constexpr int kLearnedInnerCap = 400;  // iterations of one learned inner solve before falling back
 constexpr int kWarmJacobiCap = 16;     // Jacobi iterations a warm-started learned solve tries first
+constexpr int kJacobiRetry = 8;        // warm solves that skip the Jacobi attempt after it failed
+// the last inner solve stops at sqrt(kInnerTarget) of the tolerance: below it with a margin for the
+// FP32 recurrence of the inner residual, which the following float-float residual then certifies
+constexpr double kInnerTarget = 0.25;
 
 // FP32 flexible CG with the learned preconditioner on L e = r (w->r), e from zero, until
 // r.r <= target or cap iterations; *done = iterations, *conv = reached the target
@@ -1562,32 +1610,52 @@ int learned_validation_iters(pic_world* w, const float* r, int cap, int* iters) 
 
 int solve_impl(pic_world* w, int* iters_out, double* rel_out) {
     SolveWork sw = solve_work(w);
-    double r2, b2;
+    double r2, b2, s2 = 0;
     // an FP32 update of the last full residual when phi is unchanged since; the answer is always
     // certified, by a full float-float residual pass or, without one, when the FP32 estimate plus
     // the bound on its accumulated rounding error is below the tolerance
     bool estimated = w->rhs_valid;
     const bool warm = estimated;  // phi unchanged since the last solve: a warm start
     bool use_pcg = false;  // set when the learned preconditioner stalls in this solve
-    int rc = estimated ? residual_update(w, sw, r2, b2) : residual_norms(w, sw, 0, r2, b2);
+    // extrapolated warm start: phi += (phi_n-1 - phi_n-2), the last warm solve's whole change,
+    // then a full float-float residual of the extrapolated potential
+    const bool extrapolate = warm && w->warm_mode == PIC_WARM_EXTRAPOLATE && w->dphi_valid;
+    const bool track = w->warm_mode == PIC_WARM_EXTRAPOLATE;
+    if (track && !w->dphi) CU(cudaMalloc((void**)&w->dphi, sizeof(float) * w->g.nv));
+    int rc;
+    if (extrapolate) {
+        SolveWork sx = sw;
+        sx.e = w->dphi;  // dphi stays as the first part of this solve's change
+        rc = residual_norms(w, sx, 1, r2, b2, s2);
+        sw = solve_work(w);  // phi and phi_alt were swapped
+        estimated = false;
+    } else {
+        if (track) CU(cudaMemsetAsync(w->dphi, 0, sizeof(float) * w->g.nv, w->stream));
+        rc = estimated ? residual_update(w, sw, r2, b2, s2) : residual_norms(w, sw, 0, r2, b2, s2);
+    }
     if (rc) return rc;
+    // a warm solve of the learned method first tries a few Jacobi iterations, unless the last
+    // attempt failed (then it retries after kJacobiRetry warm solves)
+    bool jacobi_first = warm && w->method == PIC_SOLVER_LEARNED && w->jacobi_skip == 0;
+    if (warm && w->jacobi_skip > 0) w->jacobi_skip--;
     const bool collect = w->lp_collect && w->method != PIC_SOLVER_RBSOR;
     if (collect) {
         rc = ensure_lp_train(w);
         if (rc) return rc;
         if (lp_pair_begin(*w->lp, w->r, w->g.nv, w->stream)) return fail(PIC_ERR_CUDA, "training pair allocation");
     }
-    double bn = b2 > 0 ? std::sqrt(b2) : 1.0;
+    // rel: the residual norm over the stopping rule's scale (PIC_STOP_*); converged when <= tol
+    double bn = stop_scale(w, b2, s2);
     double rel = std::sqrt(r2) / bn;
     int iters = 0, outer = 0;
     const int grid = w->grid_nodes;
     for (;;) {
         if (rel <= w->tol) {
-            if (!estimated || estimate_certified(w, r2, b2)) break;
+            if (!estimated || estimate_certified(w, r2, bn)) break;
             estimated = false;  // certify the FP32 estimate by a full residual pass
-            rc = residual_norms(w, sw, 0, r2, b2);
+            rc = residual_norms(w, sw, 0, r2, b2, s2);
             if (rc) return rc;
-            bn = b2 > 0 ? std::sqrt(b2) : 1.0;
+            bn = stop_scale(w, b2, s2);
             rel = std::sqrt(r2) / bn;
             continue;
         }
@@ -1606,11 +1674,11 @@ int solve_impl(pic_world* w, int* iters_out, double* rel_out) {
                 launch_rbsor_sweeps(w->g, sw, (float)w->omega, sweeps, w->stream);
             }
             iters += sweeps;
-        } else if (w->method == PIC_SOLVER_LEARNED && !use_pcg && !(warm && outer == 1)) {
+        } else if (w->method == PIC_SOLVER_LEARNED && !use_pcg && !(jacobi_first && outer == 1)) {
             // inner FP32 flexible CG with the learned multilevel preconditioner, to eta = 1e-3 of
             // the current residual (or the final target); a preconditioner that stalls hands the
             // rest of this solve to Jacobi-PCG
-            double target = std::max(1e-6 * r2, 0.09 * w->tol * w->tol * b2);
+            double target = std::max(1e-6 * r2, kInnerTarget * w->tol * w->tol * bn * bn);
             int done = 0;
             bool conv = false;
             rc = learned_inner(w, sw, target, std::min(kLearnedInnerCap, w->max_it - iters), &done, &conv);
@@ -1622,7 +1690,7 @@ int solve_impl(pic_world* w, int* iters_out, double* rel_out) {
             }
         } else {
             // inner FP32 flexible PCG to eta = 1e-3 of the current residual (or the final target)
-            double target = std::max(1e-6 * r2, 0.09 * w->tol * w->tol * b2);
+            double target = std::max(1e-6 * r2, kInnerTarget * w->tol * w->tol * bn * bn);
             {
                 Scope sc(w, "poisson", 1);
                 launch_pcg_init(w->g, sw, w->stream);
@@ -1651,10 +1719,16 @@ int solve_impl(pic_world* w, int* iters_out, double* rel_out) {
                 }
                 iters += batch;
             }
+            if (cap == kWarmJacobiCap && !w->h_flag[0]) w->jacobi_skip = kJacobiRetry;
         }
         if (collect) lp_pair_add(*w->lp, w->e, w->g.nv, w->stream, grid);
-        rc = residual_norms(w, sw, 1, r2, b2);
+        if (track) {
+            Scope sc(w, "poisson", 1);
+            launch_add(w->dphi, w->e, w->g.nv, w->stream, grid);  // dphi += e
+        }
+        rc = residual_norms(w, sw, 1, r2, b2, s2);
         if (rc) return rc;
+        bn = stop_scale(w, b2, s2);
         rel = std::sqrt(r2) / bn;
         if (!(rel == rel)) break;  // NaN: diverged
     }
@@ -1663,6 +1737,10 @@ int solve_impl(pic_world* w, int* iters_out, double* rel_out) {
         launch_fill_aux(w->aux_pairs, w->n_mirror, w->n_alias, w->phi, w->stream);
     }
     if (collect) lp_pair_end(*w->lp);
+    w->dphi_valid = track && warm;  // the change of a warm solve: one step's change
+    w->last_norms[0] = std::sqrt(r2);
+    w->last_norms[1] = std::sqrt(b2);
+    w->last_norms[2] = std::sqrt(s2);
     if (iters_out) *iters_out = iters;
     if (rel_out) *rel_out = rel;
     w->n_solves++;
@@ -2422,8 +2500,8 @@ extern "C" int pic_autotune(pic_world* w, int* push_ctas_per_sm, int* node_grid)
     // the float-float residual, which only recomputes r from phi and rho
     {
         SolveWork sw = solve_work(w);
-        double r2, b2;
-        int rc = residual_norms(w, sw, 0, r2, b2);  // allocates the residual's side arrays
+        double r2, b2, s2;
+        int rc = residual_norms(w, sw, 0, r2, b2, s2);  // allocates the residual's side arrays
         if (rc) return rc;
         const int most = std::min<long>((w->g.nv / 4 + 255) / 256, (long)w->gstride);
         int best = 0;
@@ -2473,6 +2551,15 @@ extern "C" int pic_autotune(pic_world* w, int* push_ctas_per_sm, int* node_grid)
     }
     if (node_grid) *node_grid = w->g.node_grid;
     return check_device_error(w);
+}
+
+extern "C" int pic_debug_set_wait_polls(pic_world* w, long long polls) {
+    if (!w) return fail(PIC_ERR_ARG, "null world");
+    CU(cudaSetDevice(w->device));
+    const long long arg = polls < 0 ? 0 : (polls == 0 ? -1 : polls);
+    w->wait_polls_arg = arg;
+    if (lp_set_tc_wait_polls(arg)) return fail(PIC_ERR_CUDA, "setting the tensor-core wait limit failed");
+    return PIC_OK;
 }
 
 extern "C" int pic_synchronize(pic_world* w) {

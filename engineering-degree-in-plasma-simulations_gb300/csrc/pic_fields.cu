@@ -29,8 +29,12 @@ namespace pic {
 __device__ __forceinline__ float u64_to_float(unsigned long long x) {
     return __fmaf_rn(__uint2float_rn((unsigned)(x >> 32)), 4294967296.f, __uint2float_rn((unsigned)x));
 }
+// signed: through the magnitude.  (Splitting a negative value directly gives hi = -1 and a low
+// word near 2^32, whose rounding, up to 2^7, is then not small against a small result.)
 __device__ __forceinline__ float i64_to_float(long long x) {
-    return __fmaf_rn(__int2float_rn((int)(x >> 32)), 4294967296.f, __uint2float_rn((unsigned)x));
+    const unsigned long long m = x < 0 ? 0ull - (unsigned long long)x : (unsigned long long)x;
+    const float f = u64_to_float(m);
+    return x < 0 ? -f : f;
 }
 __global__ void k_finalize_rho(FinalizeArgs a) {
     const GridDev& g = a.g;
@@ -98,6 +102,24 @@ __global__ void k_finalize_rho(FinalizeArgs a) {
     }
 }
 void launch_finalize_rho(const FinalizeArgs& a, cudaStream_t s, int grid) { k_finalize_rho<<<grid, 256, 0, s>>>(a); }
+
+// dst += src over n floats, four per thread with 16-byte accesses where n allows
+__global__ void k_add_f32(float* __restrict__ dst, const float* __restrict__ src, int n) {
+    const int n4 = n >> 2;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n4; q += gridDim.x * blockDim.x) {
+        float4 a = reinterpret_cast<float4*>(dst)[q];
+        const float4 b = reinterpret_cast<const float4*>(src)[q];
+        a.x += b.x;
+        a.y += b.y;
+        a.z += b.z;
+        a.w += b.w;
+        reinterpret_cast<float4*>(dst)[q] = a;
+    }
+    if (blockIdx.x == 0 && threadIdx.x < (n & 3)) dst[(n4 << 2) + threadIdx.x] += src[(n4 << 2) + threadIdx.x];
+}
+void launch_add(float* dst, const float* src, int n, cudaStream_t s, int grid) {
+    k_add_f32<<<grid, 256, 0, s>>>(dst, src, n);
+}
 
 // avg = a*avg + b*den  (Field::updateMovingAverage with the sample count handled on the host)
 __global__ void k_den_avg(float* avg, const float* den, int nv, float a, float b) {
@@ -274,7 +296,8 @@ __global__ void __launch_bounds__(256) k_residual(GridDev g, const float2* __res
     const bool ae = apply_e != 0;
     const bool rows4 = (g.ni & 3) == 0;
     const int nij = g.ni * g.nj;
-    float acc_r = 0.f, acc_b = 0.f;  // per-thread sums in FP32, block and grid sums in FP64
+    const float ie_f = kIeHi;
+    float acc_r = 0.f, acc_b = 0.f, acc_s = 0.f;  // per-thread sums in FP32, block and grid sums in FP64
     const int ngroups = (g.nv + 3) >> 2;
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < ngroups; q += gridDim.x * blockDim.x) {
         const int n0 = q << 2;
@@ -341,6 +364,8 @@ __global__ void __launch_bounds__(256) k_residual(GridDev g, const float2* __res
                 residual_node(K, kv[c], P[c], pn, E[c], en, hv[c], ae, rv[c], b, bf[c], pv[c]);
                 acc_r += rv[c] * rv[c];
                 acc_b += b * b;
+                const float sc = hv[c] * ie_f;
+                acc_s += sc * sc;
             }
             *reinterpret_cast<float4*>(r + n0) = make_float4(rv[0], rv[1], rv[2], rv[3]);
             if (ae) {
@@ -378,12 +403,14 @@ __global__ void __launch_bounds__(256) k_residual(GridDev g, const float2* __res
             if (ae) phi_out[n] = np;
             acc_r += rf * rf;
             acc_b += b * b;
+            const float sc = rh * ie_f;
+            acc_s += sc * sc;
             if (rho_prev) rho_prev[n] = rh;
             if (bfix_out) bfix_out[n] = bfix;
         }
     }
-    const float v[2] = {acc_r, acc_b};
-    grid_sum<2>(v, gpart, gstride, ticket, out);
+    const float v[4] = {acc_r, acc_b, 0.f, acc_s};
+    grid_sum<4>(v, gpart, gstride, ticket, out);
 }
 void launch_residual(const GridDev& g, SolveWork& w, int apply_e, cudaStream_t s, float* rho_prev, float* bfix_out) {
     const float2* in = w.phi;
@@ -399,16 +426,16 @@ void launch_residual(const GridDev& g, SolveWork& w, int apply_e, cudaStream_t s
     }
 }
 // residual of the next solve without a full pass: r += (rho - rho_prev) / eps0 on FREE nodes
-// (r holds the residual of the current phi, rounded to FP32); |r|^2, |b|^2 and the squared norm
-// of the update t = (rho - rho_prev) / eps0 into out[0..2] (the host bounds the rounding error
-// of r from |t| and |r|).
+// (r holds the residual of the current phi, rounded to FP32); |r|^2, |b|^2, the squared norm
+// of the update t = (rho - rho_prev) / eps0 and |rho / eps0|^2 into out[0..3] (the host bounds
+// the rounding error of r from |t| and |r|).
 // Four consecutive nodes per thread and iteration with 16-byte loads.
 __global__ void __launch_bounds__(256) k_rhs_update(GridDev g, float* __restrict__ r, const float* __restrict__ rho,
                                                     float* __restrict__ rho_prev, const float* __restrict__ bfix,
                                                     const uint16_t* __restrict__ kind, double* gpart, int gstride,
                                                     unsigned* ticket, double* out) {
     const float inv_eps0_f = (float)(1.0 / kEps0);
-    float acc_r = 0.f, acc_b = 0.f, acc_t = 0.f;
+    float acc_r = 0.f, acc_b = 0.f, acc_t = 0.f, acc_s = 0.f;
     const int ng = g.nv >> 2;
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < ng; q += gridDim.x * blockDim.x) {
         const float4 r4 = reinterpret_cast<const float4*>(r)[q];
@@ -424,10 +451,12 @@ __global__ void __launch_bounds__(256) k_rhs_update(GridDev g, float* __restrict
             if ((kv[c] & 3) != kFree) continue;
             const float t = (hv[c] - pv[c]) * inv_eps0_f;
             rv[c] += t;
-            const float b = hv[c] * inv_eps0_f + fv[c];
+            const float sc = hv[c] * inv_eps0_f;
+            const float b = sc + fv[c];
             acc_r += rv[c] * rv[c];
             acc_b += b * b;
             acc_t += t * t;
+            acc_s += sc * sc;
         }
         reinterpret_cast<float4*>(r)[q] = make_float4(rv[0], rv[1], rv[2], rv[3]);
         reinterpret_cast<float4*>(rho_prev)[q] = h4;
@@ -440,15 +469,17 @@ __global__ void __launch_bounds__(256) k_rhs_update(GridDev g, float* __restrict
             const float t = (rh - rho_prev[n]) * inv_eps0_f;
             const float rn = r[n] + t;
             r[n] = rn;
-            const float b = rh * inv_eps0_f + bfix[n];
+            const float sc = rh * inv_eps0_f;
+            const float b = sc + bfix[n];
             acc_r += rn * rn;
             acc_b += b * b;
             acc_t += t * t;
+            acc_s += sc * sc;
         }
         rho_prev[n] = rho[n];
     }
-    const float v[3] = {acc_r, acc_b, acc_t};
-    grid_sum<3>(v, gpart, gstride, ticket, out);
+    const float v[4] = {acc_r, acc_b, acc_t, acc_s};
+    grid_sum<4>(v, gpart, gstride, ticket, out);
 }
 void launch_rhs_update(const GridDev& g, SolveWork& w, float* rho_prev, const float* bfix, cudaStream_t s) {
     k_rhs_update<<<stream_blocks(g), 256, 0, s>>>(g, w.r, w.rho, rho_prev, bfix,

@@ -41,7 +41,15 @@ struct PushArgs {
     int staged;      // allow TMA-staged E tiles
     unsigned* err;
     CollDev coll;
+    // mbarrier polls of a wait for a bulk copy before it gives up: 0 (the zero-initialised
+    // value) kMbarWaitPolls, > 0 that many, < 0 none (a test makes the wait run out).  The drain
+    // of the copies in flight after a timeout always allows kMbarWaitPolls.
+    long long wait_polls;
 };
+__host__ __device__ inline long long wait_poll_limit(long long arg, long long dflt) {
+    return arg == 0 ? dflt : (arg < 0 ? 0 : arg);
+}
+constexpr long long kMbarWaitPolls = 1ll << 24;
 
 // particles
 int push_blocks_per_sm();  // resident push CTAs per SM (the push grid is this times the SM count)
@@ -194,9 +202,11 @@ enum : int {
     kS_RR = 7,      // r.r
     kS_R2 = 8,      // residual |r|^2, |b|^2 at 8, 9
     kS_T2 = 10,     // |(rho - rho_prev) / eps0|^2 of the last FP32 residual update
+    kS_S2 = 11,     // |rho / eps0|^2 over the FREE nodes (the space-charge part of b)
     kS_VAL = 12,    // validation norm
 };
-// residual (optionally after phi += e); |r|^2 and |b|^2 into scal[kS_R2..]
+// residual (optionally after phi += e); |r|^2, |b|^2 and |rho/eps0|^2 into scal[kS_R2], [kS_R2 + 1],
+// [kS_S2] (scal[kS_T2] is set to 0)
 void launch_residual(const GridDev& g, SolveWork& w, int apply_e, cudaStream_t s, float* rho_prev, float* bfix_out);
 void launch_rhs_update(const GridDev& g, SolveWork& w, float* rho_prev, const float* bfix, cudaStream_t s);
 void launch_reduce_partials(const double* part, int nslots, int nblocks, double* out, cudaStream_t s);
@@ -207,5 +217,7 @@ void launch_pcg_iter_impl(const GridDev& g, SolveWork& w, float* d_in, float* d_
 // phi[dst] = phi[src] for the MIRROR pairs (first n_mirror entries), then the ALIAS pairs
 void launch_fill_aux(const int2* pairs, int n_mirror, int n_alias, float2* phi, cudaStream_t s);
 void launch_den_avg(float* avg, const float* den, int nv, float a, float b, cudaStream_t s, int grid);
+// dst += src (n floats; both 16-byte aligned)
+void launch_add(float* dst, const float* src, int n, cudaStream_t s, int grid);
 
 }  // namespace pic

@@ -16,7 +16,10 @@
 
 namespace pic {
 
-constexpr long long kTcWaitLimit = 1ll << 24;
+constexpr long long kTcWaitLimit = kMbarWaitPolls;
+// polls of a first wait for MMA completion, as PushArgs::wait_polls (0: kTcWaitLimit); the wait
+// for the MMAs in flight after a timeout always allows kTcWaitLimit before TMEM is freed
+static __device__ long long g_tc_wait_arg = 0;
 
 // D (128 x N, FP32, row-major) = A (128 x K, bf16, row-major) * B^T (B: N x K, bf16, row-major)
 // 128 threads; K a multiple of 16, N in {16, 32, 64, 128}
@@ -56,7 +59,7 @@ __global__ void __launch_bounds__(128) k_tc_gemm_tile(const __nv_bfloat16* __res
                         s > 0 ? 1u : 0u);
         tc_commit(&bar);
     }
-    bool ok = tc_mbar_wait(&bar, 0, kTcWaitLimit);
+    bool ok = tc_mbar_wait(&bar, 0, wait_poll_limit(g_tc_wait_arg, kTcWaitLimit));
     if (!ok) {
         if (tid == 0) set_error(err, kErrBarrierTimeout);
         tc_mbar_wait(&bar, 0, kTcWaitLimit);  // bounded wait for the MMAs in flight before freeing TMEM
@@ -1032,7 +1035,7 @@ __global__ void __launch_bounds__(128) k_tc_act(LView src, const __nv_bfloat16* 
                             idesc, sl > 0 ? 1u : 0u);
             tc_commit(&bar);
         }
-        if (!tc_mbar_wait(&bar, phase, kTcWaitLimit)) atomicExch(&s_fail, 1);
+        if (!tc_mbar_wait(&bar, phase, wait_poll_limit(g_tc_wait_arg, kTcWaitLimit))) atomicExch(&s_fail, 1);
         phase ^= 1u;
         __syncthreads();
         if (s_fail) {
@@ -1119,7 +1122,7 @@ __global__ void __launch_bounds__(128) k_tc_wgrad(LView src, const __nv_bfloat16
             tc_commit(&bar);
         }
         first = false;
-        if (!tc_mbar_wait(&bar, phase, kTcWaitLimit)) atomicExch(&s_fail, 1);
+        if (!tc_mbar_wait(&bar, phase, wait_poll_limit(g_tc_wait_arg, kTcWaitLimit))) atomicExch(&s_fail, 1);
         phase ^= 1u;
         __syncthreads();
         if (s_fail) {
@@ -1665,6 +1668,11 @@ void lp_galerkin_diag(const double c[3], int nlev, double* diag) {
         }
         diag[l] = (c[0] + c[1] + c[2]) * tf[nc / 2] * mf[nc / 2] * mf[nc / 2];
     }
+}
+
+// the first-wait poll count of the tensor-core kernels on the current device (test hook)
+int lp_set_tc_wait_polls(long long arg) {
+    return cudaMemcpyToSymbol(g_tc_wait_arg, &arg, sizeof(arg)) == cudaSuccess ? 0 : -1;
 }
 
 }  // namespace pic

@@ -84,6 +84,8 @@ void lp_pair_end(LpState& L);
 const float* lp_pair_r(const LpState& L, int k);
 const float* lp_pair_x(const LpState& L, int k);
 int lp_npairs(const LpState& L);
+// first-wait poll count of the tensor-core kernels (PushArgs::wait_polls convention; test hook)
+int lp_set_tc_wait_polls(long long arg);
 float* lp_train_x(const LpState& L);
 float* lp_train_val(const LpState& L);
 float* lp_train_wprev(const LpState& L);

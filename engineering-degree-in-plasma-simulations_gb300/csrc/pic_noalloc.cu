@@ -1,12 +1,13 @@
 // Number density of one species without any device allocation.
 //
-// Some callers cannot allocate device memory: code that runs while a CUDA graph is being
-// captured, plugins whose host application owns all device memory through its own allocator,
-// and real-time loops that forbid allocation after start-up.  They still own the particle
-// arrays and the output field, and pass them in.  The only working memory this entry point
-// needs -- the 64-bit fixed-point accumulator of one node field -- lives in the file-scope
-// device array below, sized for kNoAllocMaxNodes nodes.  Every GPU that loads the library
-// holds it (8 MiB) until the process exits.
+// Some callers cannot allocate device memory: plugins whose host application owns all device
+// memory through its own allocator (a cudaMalloc of theirs would bypass that allocator's
+// accounting and limits), and real-time loops that forbid allocation after start-up because an
+// allocation can block for an unbounded time.  They still own the particle arrays and the
+// output field, and pass them in.  The only working memory this entry point needs -- the 64-bit
+// fixed-point accumulator of one node field -- lives in the file-scope device array below, sized
+// for kNoAllocMaxNodes nodes.  Every GPU that loads the library holds it (8 MiB) until the
+// process exits.
 //
 // The array name is only a host-side stand-in for a device address; the real address is
 // looked up with cudaGetSymbolAddress once per device, with that device current, on the first
@@ -111,8 +112,9 @@ extern "C" int pic_number_density_noalloc(int ni, int nj, int nk, const double* 
     long long nv = (long long)ni * nj * nk;
     if (!x0 || !xm || (n > 0 && (!pos4 || !vel4)) || !den_out || n < 0 || !(scale > 0))
         return set_last_error(PIC_ERR_ARG, "pic_number_density_noalloc: null array, negative count or scale <= 0");
-    if (ni < 2 || nj < 2 || nk < 2 || ni - 1 > 1024 || nj - 1 > 1024 || nk - 1 > 2047)
-        return set_last_error(PIC_ERR_ARG, "pic_number_density_noalloc: grid must have 2..1025 x 2..1025 x 2..2048 nodes");
+    // the packed particle cell keeps 9 bits for i and j and 13 for k (pic_world_create's limits)
+    if (ni < 2 || nj < 2 || nk < 2 || ni - 1 > kCellMaxIJ || nj - 1 > kCellMaxIJ || nk - 1 > kCellMaxK)
+        return set_last_error(PIC_ERR_ARG, "pic_number_density_noalloc: grid must have 2..513 x 2..513 x 2..8193 nodes");
     if (nv > kNoAllocMaxNodes) {
         char msg[160];
         snprintf(msg, sizeof(msg), "pic_number_density_noalloc: %lld nodes exceed the %d-node accumulator", nv,
@@ -121,6 +123,16 @@ extern "C" int pic_number_density_noalloc(int ni, int nj, int nk, const double* 
     }
     for (int d = 0; d < 3; d++)
         if (!(xm[d] > x0[d])) return set_last_error(PIC_ERR_ARG, "pic_number_density_noalloc: xm must exceed x0");
+    {
+        const int nn3[3] = {ni, nj, nk};
+        for (int d = 0; d < 3; d++)  // as pic_world_set_boundaries
+            if (periodic && periodic[d] && nn3[d] < 4)
+                return set_last_error(PIC_ERR_ARG, "pic_number_density_noalloc: periodic axis needs at least 4 nodes");
+    }
+    // the deposit scales in FP32; the finalize divides by the same FP32 value
+    const float fscale = (float)scale;
+    if (!(fscale > 0.f) || !(fscale < 3.0e38f))
+        return set_last_error(PIC_ERR_ARG, "pic_number_density_noalloc: scale is not a finite FP32 value");
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices)
         return set_last_error(PIC_ERR_CUDA, "pic_number_density_noalloc: no current CUDA device");
@@ -157,16 +169,25 @@ extern "C" int pic_number_density_noalloc(int ni, int nj, int nk, const double* 
     cudaStream_t s = (cudaStream_t)stream;
     if (cudaMemsetAsync(acc, 0, sizeof(unsigned long long) * nv, s) != cudaSuccess)
         return set_last_error(PIC_ERR_CUDA, "pic_number_density_noalloc: clearing the accumulator failed");
+    // launched through cudaLaunchKernel, whose return value is this launch's own status: an error
+    // the caller left pending before this call is neither reported nor cleared here
+    unsigned long long* accp = (unsigned long long*)acc;
     if (n > 0) {
         long blocks = (n + 255) / 256;
         if (blocks > 4096) blocks = 4096;
-        k_noalloc_deposit<<<(int)blocks, 256, 0, s>>>(g, (const float4*)pos4, (const float4*)vel4, n, (float)scale,
-                                                      (unsigned long long*)acc);
+        const float4* p4 = (const float4*)pos4;
+        const float4* v4 = (const float4*)vel4;
+        void* args[] = {&g, &p4, &v4, &n, (void*)&fscale, &accp};
+        if (cudaLaunchKernel((const void*)k_noalloc_deposit, dim3((unsigned)blocks), dim3(256), args, 0, s) !=
+            cudaSuccess)
+            return set_last_error(PIC_ERR_CUDA, "pic_number_density_noalloc: deposit launch failed");
     }
     int fb = (int)((nv + 255) / 256);
     if (fb > 4096) fb = 4096;
-    k_noalloc_finalize<<<fb, 256, 0, s>>>(g, (const unsigned long long*)acc, 1.0 / scale, den_out);
-    if (cudaGetLastError() != cudaSuccess)
-        return set_last_error(PIC_ERR_CUDA, "pic_number_density_noalloc: kernel launch failed");
+    const unsigned long long* caccp = accp;
+    double inv_scale = 1.0 / (double)fscale;
+    void* fargs[] = {&g, &caccp, &inv_scale, &den_out};
+    if (cudaLaunchKernel((const void*)k_noalloc_finalize, dim3((unsigned)fb), dim3(256), fargs, 0, s) != cudaSuccess)
+        return set_last_error(PIC_ERR_CUDA, "pic_number_density_noalloc: finalize launch failed");
     return PIC_OK;
 }

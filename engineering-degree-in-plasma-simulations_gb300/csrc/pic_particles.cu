@@ -27,7 +27,7 @@ constexpr int kPushBlocksPerSM = 3;         // resident push CTAs per SM (80 reg
 // kSeg nodes each
 constexpr size_t kPbufBytes = (size_t)kChunk * 2 * sizeof(float4);
 constexpr size_t kPushSmem = kPbufBytes + 4 * kSeg * sizeof(float4) + 2 * 4 * kSeg * sizeof(unsigned);
-constexpr long long kWaitLimit = 1ll << 24;  // mbarrier polls before giving up
+constexpr long long kWaitLimit = kMbarWaitPolls;  // mbarrier polls of a drain before giving up
 
 // ------------------------------------------------------------------------------------
 // mbarrier + bulk-copy (TMA) helpers
@@ -58,9 +58,10 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned by
         "l"(src), "r"(bytes), "r"(smem_u32(bar))
         : "memory");
 }
-// bounded wait: returns false if the copies did not land within kWaitLimit polls
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity) {
-    for (long long it = 0; it < kWaitLimit; it++)
+// bounded wait: returns false if the copies did not land within `limit` polls
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity,
+                                                  long long limit = kWaitLimit) {
+    for (long long it = 0; it < limit; it++)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
@@ -407,6 +408,7 @@ __global__ void __launch_bounds__(kThreads, kPushBlocksPerSM) k_push(PushArgs a)
     }
     __syncthreads();
     unsigned phase_p = 0, phase_e = 0;
+    const long long wait_lim = wait_poll_limit(a.wait_polls, kWaitLimit);
     Tile t;
     t.off[0] = 0;
     t.off[1] = g.ni;
@@ -427,7 +429,7 @@ __global__ void __launch_bounds__(kThreads, kPushBlocksPerSM) k_push(PushArgs a)
         // ---- this chunk's particles into registers (staged by TMA, or loaded here for the last,
         // partial chunk)
         if (pending) {
-            if (!mbar_wait_bounded(&bar_p, phase_p)) atomicExch(&s_fail, 1);
+            if (!mbar_wait_bounded(&bar_p, phase_p, wait_lim)) atomicExch(&s_fail, 1);
             phase_p ^= 1u;
             pending = false;
             __syncthreads();
@@ -506,7 +508,7 @@ __global__ void __launch_bounds__(kThreads, kPushBlocksPerSM) k_push(PushArgs a)
         if (use_tile) {
             if (a.deposit)
                 for (int x = tid; x < 8 * kSeg; x += kThreads) dtile[x] = 0u;
-            if (!mbar_wait_bounded(&bar_e, phase_e)) atomicExch(&s_fail, 1);
+            if (!mbar_wait_bounded(&bar_e, phase_e, wait_lim)) atomicExch(&s_fail, 1);
             phase_e ^= 1u;
             __syncthreads();
             if (s_fail) {

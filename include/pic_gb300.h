@@ -167,8 +167,9 @@ int pic_source_sample(pic_world* w, int source_id);
 #define PIC_SOLVER_LEARNED 2 /* flexible CG with the learned multilevel preconditioner, FP32 iterations in
                               * FP64 refinement (no reference counterpart) */
 /* PotentialSolver(world, max_it, tolerance, SolverType)               PotentialSolver.cpp:44-52
- * Stopping rule: FP64 ||b - L phi||_2 / ||b||_2 <= tol_rel (the reference stops on an absolute
- * RMS residual).  omega is the SOR weight (reference 1.4). */
+ * Stopping rule: FP64 ||b - L phi||_2 / ||b||_2 <= tol_rel unless pic_solver_set_stop chose
+ * another (the reference stops on an absolute RMS residual).  omega is the SOR weight
+ * (reference 1.4). */
 int pic_solver_configure(pic_world* w, int method, double tol_rel, int max_it, double omega);
 /* PotentialSolver::solve()                                            PotentialSolver.cpp:55-67
  * iters: inner sweeps / iterations; rel: final FP64 relative residual.
@@ -176,6 +177,33 @@ int pic_solver_configure(pic_world* w, int method, double tol_rel, int max_it, d
 int pic_solver_solve(pic_world* w, int* iters, double* rel);
 /* PotentialSolver::computeEF()                                        PotentialSolver.cpp:354-408 */
 int pic_solver_compute_ef(pic_world* w);
+/* Stopping rule of pic_solver_solve (the tolerance set here replaces pic_solver_configure's):
+ *   PIC_STOP_REL_RHS     ||b - L phi||_2 <= tol ||b||_2 (the default)
+ *   PIC_STOP_ABS_RMS     sqrt(||b - L phi||_2^2 / nv) <= tol, the reference's own rule: the GS
+ *                        check (PotentialSolver.cpp:150-158) and vec::norm of PCG
+ *                        (PotentialSolver.cpp:36-38, 300) divide the squared residual by the
+ *                        node count
+ *   PIC_STOP_REL_CHARGE  ||b - L phi||_2 <= tol min(||b||_2, ||rho/eps0||_2): relative to the
+ *                        space-charge part of b as well, so that a large Dirichlet (electrode)
+ *                        term in b cannot hide an unresolved space-charge potential
+ * (no reference counterpart for the relative rules).  rel of pic_solver_solve is the residual
+ * norm over the rule's scale. */
+#define PIC_STOP_REL_RHS 0
+#define PIC_STOP_ABS_RMS 1
+#define PIC_STOP_REL_CHARGE 2
+int pic_solver_set_stop(pic_world* w, int rule, double tol);
+/* Start of a warm solve (phi unchanged since the last solve), no reference counterpart:
+ *   PIC_WARM_PREVIOUS     the last potential, as the reference's solvers continue from world.phi
+ *   PIC_WARM_EXTRAPOLATE  the last potential plus the last warm solve's whole change (linear
+ *                         extrapolation in time: ballistic particles change rho almost linearly
+ *                         from step to step); one float-float residual pass evaluates it
+ * Either way the solve ends at the same certified residual. */
+#define PIC_WARM_PREVIOUS 0
+#define PIC_WARM_EXTRAPOLATE 1
+int pic_solver_set_warm_start(pic_world* w, int mode);
+/* ||b - L phi||_2, ||b||_2 and ||rho/eps0||_2 (FREE nodes) of the last solve's final residual
+ * (no reference counterpart) */
+int pic_solver_last_norms(pic_world* w, double* out3);
 /* cumulative solver work since creation: solves, FP64 refinements (residual evaluations) and
  * inner FP32 sweeps / iterations (no reference counterpart; the reference prints progress) */
 int pic_solver_stats(pic_world* w, long* solves, long* refinements, long* inner_iterations);
@@ -274,24 +302,35 @@ int pic_species_merge(pic_world* w, int sp, int min_count);
 int pic_merge_stats(pic_world* w, uint64_t* out);
 
 /* ---- number density without device allocation -------------------------------------
- * No counterpart in the reference.  For callers that cannot allocate device memory (code
- * running under CUDA graph capture, plugins whose host owns all device memory, real-time
- * loops that forbid allocation): the number density of one species from particle arrays the
- * caller already holds on the current device, in the library's layout (pos4: float4 {ox, oy,
- * oz, packed cell i | j<<9 | k<<18}; vel4: float4 {vx, vy, vz, w}), written to den_out (FP32,
- * one value per node, node order as above).  Same CIC weights and 64-bit fixed-point sums as
- * Species::computeNumberDensity (Species.cpp:401-416) with fixed-point scale `scale`.
+ * No counterpart in the reference.  For callers that cannot allocate device memory: plugins
+ * whose host application owns all device memory through its own allocator, and real-time loops
+ * that forbid allocation after start-up.  It computes the number density of one species from
+ * particle arrays the caller already holds on the current device, in the library's layout
+ * (pos4: float4 {ox, oy, oz, packed cell i | j<<9 | k<<18}; vel4: float4 {vx, vy, vz, w}), and
+ * writes it to den_out (FP32, one value per node, node order as above).  The deposit uses the
+ * same CIC weights and 64-bit fixed-point rounding as this library's fused push deposit, with
+ * fixed-point scale `scale` (rounded to FP32); scale times the weight summed at any one node
+ * must stay below 2^63.  Grids are limited to 513 x 513 x 8193 nodes, as pic_world_create, and
+ * a periodic axis needs at least 4 nodes.
  * The working accumulator is a library-owned device array of 2^20 nodes (8 MiB per GPU, held
  * until exit); larger grids are rejected with PIC_ERR_ARG.  No allocation is made.  The first
  * call on a device looks up that array's address and should come before any stream capture.
- * All calls share the array: calls that overlap on the GPU race.  Work is queued on `stream`
- * (a cudaStream_t, NULL for the default stream) and not waited for. */
+ * All calls share the array, which keeps the last call's contents (each call clears it first):
+ * calls that overlap on the GPU race.  Work is queued on `stream` (a cudaStream_t, NULL for the
+ * default stream) and not waited for; an error the caller left pending is not cleared. */
 int pic_number_density_noalloc(int ni, int nj, int nk, const double* x0, const double* xm, const int* periodic,
                                const void* pos4, const void* vel4, long n, double scale, float* den_out,
                                void* stream);
 
 /* ---- runtime ------------------------------------------------------------------------- */
 int pic_synchronize(pic_world* w);
+/* Test hook, no reference counterpart: how many times a kernel's first wait for a bulk copy
+ * (the push) or for tensor-core MMAs (training) polls its mbarrier before it gives up, records
+ * the fault and returns (pic_synchronize then returns PIC_ERR_DEVICE).  polls < 0 restores the
+ * default 2^24; 0 makes every such wait give up at once.  The wait for the copies or MMAs still
+ * in flight after a timeout always keeps the full limit, so no copy outlives its block.  The
+ * tensor-core setting applies to the current device. */
+int pic_debug_set_wait_polls(pic_world* w, long long polls);
 /* message of the last failing call on this thread (empty if none) */
 int pic_last_error(char* buf, int len);
 /* per-kernel CUDA-event timing: enable, then read accumulated milliseconds and launch counts

@@ -326,6 +326,13 @@ public:
     }
     int iterations() const { return iters_; }
     double relativeResidual() const { return rel_; }
+    // stopping rule PIC_STOP_*; PIC_STOP_ABS_RMS is the reference's own absolute RMS residual
+    // (PotentialSolver.cpp:150-158), the relative rules have no reference counterpart
+    void setStopRule(int rule, type_calc tolerance) { check(pic_solver_set_stop(world_->handle(), rule, tolerance)); }
+    // start of warm solves: PIC_WARM_PREVIOUS (the reference's) or PIC_WARM_EXTRAPOLATE
+    void setWarmStart(int mode) { check(pic_solver_set_warm_start(world_->handle(), mode)); }
+    // ||b - L phi||_2, ||b||_2 and ||rho/eps0||_2 of the last solve's final residual
+    void lastNorms(double out[3]) const { check(pic_solver_last_norms(world_->handle(), out)); }
 
 private:
     World* world_;

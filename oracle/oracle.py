@@ -14,7 +14,19 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "libpicoracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libpicref.so")
-REF_ROOT = os.environ.get("PIC_REFERENCE_ROOT", "/root/reference")
+
+
+def reference_root():
+    """Location of the reference tree: PIC_REFERENCE_ROOT, else the build recipe's default."""
+    root = os.environ.get("PIC_REFERENCE_ROOT")
+    if root:
+        return root
+    try:
+        out = subprocess.run(["make", "-s", "print-ref"], cwd=HERE, check=True, capture_output=True, text=True)
+        return out.stdout.strip()
+    except (OSError, subprocess.CalledProcessError):
+        return ""
+
 
 # physical constants of ch4/v3/src/all.h:16-25
 EPS0 = 8.85418782e-12
@@ -35,14 +47,39 @@ def build_port():
 
 def build_ref():
     """Compile the reference sources (needs the reference tree; absent on GPU hosts)."""
-    if not os.path.isdir(os.path.join(REF_ROOT, "ch4", "v3", "src")):
+    root = reference_root()
+    if not root or not os.path.isdir(os.path.join(root, "ch4", "v3", "src")):
         return False
-    subprocess.run(["make", "-s", "-j8", "ref", "REF=" + REF_ROOT], cwd=HERE, check=True)
+    subprocess.run(["make", "-s", "-j8", "ref", "REF=" + root], cwd=HERE, check=True)
     return True
 
 
 def _p(a):
     return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+def moving_average_update(avg, samples, den):
+    """Field::updateMovingAverage (Field.h:245-261) as Species::updateAverages calls it
+    (Species.cpp:764-766): the sample counter restarts after 20 samples (the field is cleared),
+    then avg = (den + avg (samples - 1)) / samples.  Updates avg in place; returns the counter."""
+    samples += 1
+    if samples > 20:
+        avg[:] = 0.0
+        samples = 1
+    avg[:] = (den + avg * (samples - 1.0)) / samples
+    return samples
+
+
+def macro_particle_count(g, parts):
+    """Species::computeMacroParticlesCount (Species.cpp:813-819): particles per cell, the cell
+    from World::XtoIJK (World.cpp:120-133), int((x - x0) * inv_dx) per axis.  Counts in the
+    linear cell order c = (k (nj-1) + j) (ni-1) + i of World::XtoC (World.cpp:134-137)."""
+    x0 = np.array(g.x0[:])
+    inv = np.array(g.inv_dx[:])
+    ijk = ((parts["pos"] - x0) * inv).astype(np.int64)
+    ci, cj, ck = g.ni - 1, g.nj - 1, g.nk - 1
+    c = (ijk[:, 2] * cj + ijk[:, 1]) * ci + ijk[:, 0]
+    return np.bincount(c, minlength=ci * cj * ck)
 
 
 class Grid(C.Structure):
@@ -388,6 +425,9 @@ class Ref:
                 "ref_get_field": (None, [vp, i, vp]),
                 "ref_set_field": (None, [vp, i, vp]),
                 "ref_get_den": (None, [vp, i, vp]),
+                "ref_update_averages": (None, [vp, i]),
+                "ref_get_den_avg": (None, [vp, i, vp]),
+                "ref_macro_count": (None, [vp, i, vp]),
                 "ref_get_ef": (None, [vp, vp]),
                 "ref_set_ef": (None, [vp, vp]),
                 "ref_solver_create": (None, [vp, C.c_uint, d, i]),

@@ -11,6 +11,8 @@
 //   Species(name,mass,charge,world,mpw0[,E_ion]) ch4/v3/src/Species.h:56-57
 //   Species::advanceElectrons / advanceNonElectron ch4/v3/src/Species.cpp:258, 47
 //   Species::computeNumberDensity                ch4/v3/src/Species.cpp:401
+//   Species::updateAverages / den_avg            ch4/v3/src/Species.cpp:764
+//   Species::computeMacroParticlesCount          ch4/v3/src/Species.cpp:813
 //   World::computeChargeDensity                  ch4/v3/src/World.cpp:193
 //   PotentialSolver::solve / computeEF           ch4/v3/src/PotentialSolver.cpp:55, 354
 //   MC_MEX_Ionization::apply                     ch4/v3/src/Interactions.cpp:567
@@ -195,6 +197,16 @@ void ref_set_field(void* h, int which, const double* in) {
     else if (which == 1) set_scalar(w.rho, in);
 }
 void ref_get_den(void* h, int sp, double* out) { get_scalar(static_cast<RefSim*>(h)->species[sp].den, out); }
+// Species::updateAverages (Species.cpp:764-766) and its public den_avg field
+void ref_update_averages(void* h, int sp) { static_cast<RefSim*>(h)->species[sp].updateAverages(); }
+void ref_get_den_avg(void* h, int sp, double* out) { get_scalar(static_cast<RefSim*>(h)->species[sp].den_avg, out); }
+// Species::computeMacroParticlesCount (Species.cpp:813-819); the public macro_part_count field
+// is cell-sized (Species.cpp:32), so out holds (ni-1)(nj-1)(nk-1) values in linear cell order
+void ref_macro_count(void* h, int sp, double* out) {
+    Species& s = static_cast<RefSim*>(h)->species[sp];
+    s.computeMacroParticlesCount();
+    get_scalar(s.macro_part_count, out);
+}
 void ref_get_ef(void* h, double* out) {
     World& w = *static_cast<RefSim*>(h)->world;
     for (int k = 0; k < w.nk; k++)

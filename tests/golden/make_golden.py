@@ -2,8 +2,8 @@
 
 Runs oracle/_ref/libpicref.so (the reference sources compiled unmodified by oracle/Makefile,
 driven through ref_harness.cpp) on small seeded cases and stores inputs and outputs as .npz
-files next to this script.  Needs the reference tree (PIC_REFERENCE_ROOT, default
-/root/reference); the fixtures themselves travel with the repository.
+files next to this script.  Needs the reference tree (PIC_REFERENCE_ROOT, else the default of
+oracle/Makefile); the fixtures themselves travel with the repository.
 
     python tests/golden/make_golden.py [case ...]     (no case: all of them)
 """
@@ -208,9 +208,39 @@ def case_objects():
     return out
 
 
+def case_averages():
+    """Species::updateAverages (the Field.h:245-261 moving average, which restarts after 20
+    samples) over 45 number densities of changing particle sets, and
+    Species::computeMacroParticlesCount (Species.cpp:813-819) of the last set."""
+    nn, x0, xm = (6, 5, 7), (0.0, 0.0, 0.0), (0.005, 0.004, 0.006)
+    R = O.Ref(nn, x0, xm)
+    ele = R.species("e-", O.ME, -O.QE, 10.0)
+    rng = np.random.default_rng(3)
+    dens, avgs = [], []
+    for it in range(45):
+        n = 500 + 20 * it
+        p = np.zeros(n, O.PARTICLE)
+        p["pos"] = rng.uniform(0, 1, (n, 3)) * np.array(xm) * 0.999999
+        p["vel"] = rng.normal(size=(n, 3)) * 1e5
+        p["w"] = rng.lognormal(np.log(10.0), 0.5, n)
+        R.set_particles(ele, p)
+        R.L.ref_number_density(R.h, ele)
+        R.L.ref_update_averages(R.h, ele)
+        den = np.zeros(R.nv)
+        avg = np.zeros(R.nv)
+        R.L.ref_get_den(R.h, ele, den.ctypes.data_as(C.c_void_p))
+        R.L.ref_get_den_avg(R.h, ele, avg.ctypes.data_as(C.c_void_p))
+        dens.append(den)
+        avgs.append(avg)
+    cnt = np.zeros((nn[0] - 1) * (nn[1] - 1) * (nn[2] - 1))  # a cell-sized field (Species.cpp:32)
+    R.L.ref_macro_count(R.h, ele, cnt.ctypes.data_as(C.c_void_p))
+    return dict(nn=np.array(nn), x0=np.array(x0), xm=np.array(xm), den=np.array(dens), den_avg=np.array(avgs),
+                last_pos=p["pos"].copy(), macro_count=cnt)
+
+
 def main():
     cases = (("push_deposit", case_push_deposit), ("poisson", case_poisson), ("ntc", case_ntc), ("merge", case_merge),
-             ("dsmc", case_dsmc), ("objects", case_objects))
+             ("dsmc", case_dsmc), ("objects", case_objects), ("averages", case_averages))
     only = set(sys.argv[1:])
     for name, fn in cases:
         if only and name not in only:

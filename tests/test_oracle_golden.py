@@ -303,3 +303,25 @@ def test_object_interaction_bit_exact(port):
             assert n == len(ref), (nm, it, n, len(ref))
             for f in ("pos", "vel", "w"):
                 assert np.array_equal(arr[:n][f], ref[f]), (nm, it, f)
+
+
+def test_moving_average_bit_exact():
+    """oracle.moving_average_update against Species::updateAverages of the reference, over 45
+    samples (two restarts of the 20-sample average)."""
+    d = golden("averages")
+    avg = np.zeros(d["den"].shape[1])
+    samples = 0
+    for it in range(len(d["den"])):
+        samples = O.moving_average_update(avg, samples, d["den"][it])
+        assert np.array_equal(avg, d["den_avg"][it]), it
+
+
+def test_macro_particle_count_matches_reference(port):
+    d = golden("averages")
+    nn = tuple(int(v) for v in d["nn"])
+    g = port.grid(nn, d["x0"], d["xm"])
+    p = np.zeros(len(d["last_pos"]), O.PARTICLE)
+    p["pos"] = d["last_pos"]
+    got = O.macro_particle_count(g, p)
+    assert got.sum() == len(p)
+    assert np.array_equal(got, d["macro_count"])

@@ -1,8 +1,9 @@
 """pic_number_density_noalloc: the number density for callers that cannot allocate device memory.
 
-Those callers (code under CUDA graph capture, plugins whose host application owns all device
-memory, allocation-free real-time loops) pass particle arrays and the output field they
-already hold; the entry point works in a library-owned device array instead of allocating.
+Those callers (plugins whose host application owns all device memory through its own
+allocator, real-time loops that forbid allocation after start-up) pass particle arrays and the
+output field they already hold; the entry point works in a library-owned device array instead
+of allocating.
 It is checked through the C ABI against the existing path (pic_species_number_density +
 pic_charge_density) on two calls in a row, within the deposit tolerance of the other tests.
 This file is collected last on purpose.
@@ -54,12 +55,16 @@ def test_noalloc_density_matches_existing_entry_point(pic):
         ref = s.den
         # the no-allocation entry point on the same particles
         p4, v4 = library_layout(pos, w, torch)
+        torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info()[0]
         rc = L.pic_number_density_noalloc(NN[0], NN[1], NN[2], x0.ctypes.data_as(C.c_void_p),
                                           xm.ctypes.data_as(C.c_void_p), per.ctypes.data_as(C.c_void_p),
                                           C.c_void_p(p4.data_ptr()), C.c_void_p(v4.data_ptr()), n, 2.0 ** 30,
                                           C.c_void_p(out.data_ptr()), None)
         assert rc == pic.PIC_OK
         torch.cuda.synchronize()
+        if call > 0:  # the first call on a device may load the library's module (its device array)
+            assert torch.cuda.mem_get_info()[0] == free0, "device memory changed during the call"
         got = out.cpu().numpy().astype(np.float64)
         assert np.max(np.abs(got - ref)) <= 1e-6 * np.max(ref), call
 
@@ -74,3 +79,17 @@ def test_noalloc_rejects_grids_beyond_its_accumulator(pic):
     buf = C.create_string_buffer(256)
     L.pic_last_error(buf, 256)
     assert b"exceed" in buf.value
+
+
+@pytest.mark.parametrize("nn,per", [((514, 4, 4), None), ((4, 514, 4), None), ((3, 8, 8), (1, 0, 0))])
+def test_noalloc_rejects_grids_the_world_rejects(pic, nn, per):
+    """A 513-cell axis does not fit the packed particle cell, and a periodic axis needs 4 nodes."""
+    L = pic.library()
+    x0 = np.zeros(3)
+    xm = np.ones(3)
+    p = np.array(per, np.int32) if per else None
+    rc = L.pic_number_density_noalloc(nn[0], nn[1], nn[2], x0.ctypes.data_as(C.c_void_p),
+                                      xm.ctypes.data_as(C.c_void_p),
+                                      p.ctypes.data_as(C.c_void_p) if p is not None else None, None, None, 0, 1.0,
+                                      C.c_void_p(1), None)
+    assert rc == pic.PIC_ERR_ARG
