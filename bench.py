@@ -80,6 +80,7 @@ MERGE_MIN = 64    # a cell is merged when it holds more than this many particles
 SORT_EVERY = [20]  # steps between the loop's sort checks (a species re-sorts when 2 % of it moved)
 STOP = ["charge"]  # Poisson stopping rule of the loop and of the time-to-tolerance cases
 WARM = ["extrapolate"]  # start of the loop's warm solves: "previous" phi or "extrapolate"d in time
+WARM_JACOBI = [0]  # Jacobi-PCG iterations a warm learned solve runs first (measured best with training)
 STOP_TEXT = {"charge": "||b - L phi|| <= 1e-6 min(||b||, ||rho/eps0||)", "rhs": "||b - L phi|| <= 1e-6 ||b||"}
 
 
@@ -91,6 +92,7 @@ def loop_solver(pic, W):
     """The loop's Poisson solver: learned-preconditioned flexible CG, the stopping rule and warm start."""
     S = pic.PotentialSolver(W, 20000, 1e-6, pic.SOLVER_LEARNED, stop=stop_rule(pic))
     S.setWarmStart(pic.WARM_EXTRAPOLATE if WARM[0] == "extrapolate" else pic.WARM_PREVIOUS)
+    S.setWarmJacobi(WARM_JACOBI[0])
     return S
 
 
@@ -466,8 +468,29 @@ def measure_loop(pic, args, wl, rank, ws, local, clocks=True):
     assert S.solve(raise_on_fail=True)  # initial vacuum + space-charge field (main.cpp:172-173)
     S.computeEF()
     tuned = W.autotune()  # launch shapes measured on this world's data (outside the timed region)
+    lp = pic.LearnedPreconditioner(W)
+    training = None
+    if args.train:
+        # online training on the run's own (residual, correction) pairs: the warm-up steps' solves
+        # are collected, then the level gains are calibrated and gradient rounds run on those
+        # pairs, each round kept only if the validation solve (the latest pair's residual) needs
+        # fewer iterations; outside the timed region, its time reported
+        lp.collect(True)
     for _ in range(args.warmup):
         W.step()
+    if args.train:
+        lp.collect(False)
+        W.synchronize()
+        t0 = time.perf_counter()
+        cal_before, cal_after = lp.calibrate()
+        rounds = [{"calibration": True, "val_iters_before": cal_before, "val_iters_after": cal_after, "kept": True}]
+        for k in range(args.train_rounds):
+            loss, before, after, kept = lp.train(100, lr=1e-3 / (1 + k), pair_every=1)
+            rounds.append({"loss": loss, "val_iters_before": before, "val_iters_after": after, "kept": kept})
+        W.synchronize()
+        training = {"pairs_from_steps": args.warmup, "seconds": time.perf_counter() - t0, "rounds": rounds}
+        for _ in range(2):  # the loop's warm start settles on the trained preconditioner
+            W.step()
     W.synchronize()
     W.timing(True)
     W.timing_reset()
@@ -537,7 +560,7 @@ def measure_loop(pic, args, wl, rank, ws, local, clocks=True):
         "poisson_norms": {"rho_over_b": norms["charge"] / norms["b"] if norms["b"] > 0 else None,
                           "residual_rel_b": norms["r"] / norms["b"] if norms["b"] > 0 else None,
                           "residual_rel_charge": norms["r"] / norms["charge"] if norms["charge"] > 0 else None},
-        "autotuned": tuned, "clocks": clk.summary() if clocks else None,
+        "autotuned": tuned, "clocks": clk.summary() if clocks else None, "training": training,
     }
     return res, W, (e, i)
 
@@ -586,6 +609,7 @@ def run_gpu(args, wl, rank, ws, local):
                    "poisson_inner_per_step": res["inner_per_step"],
                    "poisson_refinements_per_step": res["refinements_per_step"],
                    "poisson_norms": res["poisson_norms"],
+                   "poisson_training": res["training"],
                    "sort_every": SORT_EVERY[0],
                    "l2": "inputs larger than L2 (particles %.1f GB)" % (res["parts_per_step"] * 36 / 1e9),
                    "merging": "every %d steps, cells above %d particles" % (MERGE_EVERY, MERGE_MIN),
@@ -630,7 +654,8 @@ def extra_workloads(pic, args, rank, ws, local):
                     "groups_ms_per_step": res["groups_ms_per_step"],
                     "poisson_inner_per_step": res["inner_per_step"],
                     "poisson_refinements_per_step": res["refinements_per_step"],
-                    "poisson_norms": res["poisson_norms"], "gpu_launches": res["gpu_launches"],
+                    "poisson_norms": res["poisson_norms"], "poisson_training": res["training"],
+                    "gpu_launches": res["gpu_launches"],
                     "cpu_baseline": cpu}
     return out, snap
 
@@ -928,6 +953,11 @@ def main():
                     help="Poisson stopping rule: charge (relative to min(||b||, ||rho/eps0||)) or rhs (to ||b||)")
     ap.add_argument("--warm", default="extrapolate", choices=["extrapolate", "previous"],
                     help="start of the loop's warm Poisson solves: the last phi, or extrapolated in time")
+    ap.add_argument("--warm-jacobi", type=int, default=0,
+                    help="Jacobi-PCG iterations a warm learned solve runs before the learned preconditioner")
+    ap.add_argument("--no-train", dest="train", action="store_false",
+                    help="run the loop with the learned preconditioner's starting (BPX) weights")
+    ap.add_argument("--train-rounds", type=int, default=3, help="gradient rounds after the level-gain calibration")
     ap.add_argument("--no-extra", dest="extra", action="store_false",
                     help="skip the discharge, ensemble and 128^3 snapshot cases beside the headline")
     ap.add_argument("--dsmc", type=int, default=128, help="n of the n^3-cell DSMC_MEX case (0: skip)")
@@ -938,6 +968,7 @@ def main():
     SORT_EVERY[0] = args.sort_every
     STOP[0] = args.stop
     WARM[0] = args.warm
+    WARM_JACOBI[0] = args.warm_jacobi
     if args.warmup < 3:
         args.warmup = 3
     wl = WORKLOADS[args.workload]

@@ -95,6 +95,7 @@ def library():
         "pic_solver_stats": [vp, vp, vp, vp],
         "pic_solver_set_stop": [vp, i, d],
         "pic_solver_set_warm_start": [vp, i],
+        "pic_solver_set_warm_jacobi": [vp, i],
         "pic_solver_last_norms": [vp, vp],
         "pic_mcc_create": [vp, i, i, d, d, d, d, d, i, vp, vp, vp, i, u64],
         "pic_mcc_apply": [vp, d],
@@ -544,6 +545,10 @@ class PotentialSolver:
     def setWarmStart(self, mode):
         """WARM_PREVIOUS (the last potential) or WARM_EXTRAPOLATE (plus the last step's change)."""
         _check(self.world._L.pic_solver_set_warm_start(self.world._h, int(mode)))
+
+    def setWarmJacobi(self, iterations):
+        """Jacobi-PCG iterations a warm learned solve runs before the learned preconditioner."""
+        _check(self.world._L.pic_solver_set_warm_jacobi(self.world._h, int(iterations)))
 
     def norms(self):
         """(||b - L phi||, ||b||, ||rho/eps0||) of the last solve's final residual (FREE nodes)."""

@@ -156,9 +156,9 @@ struct pic_world {
     double tol = 1e-6;
     int stop_rule = PIC_STOP_REL_RHS;
     int warm_mode = PIC_WARM_PREVIOUS;  // start of a warm solve (PIC_WARM_*)
+    int warm_jacobi = 16;  // Jacobi-PCG iterations a warm solve of the learned method runs first
     float* dphi = nullptr;  // the last solve's total change of phi (FP32), for PIC_WARM_EXTRAPOLATE
     bool dphi_valid = false;  // dphi holds the change of one warm solve
-    int jacobi_skip = 0;  // warm solves left that skip the Jacobi attempt (its last one failed)
     double last_norms[3] = {0, 0, 0};  // |r|, |b|, |rho/eps0| of the last solve's final residual
     int max_it = 10000;
     double omega = 1.4;
@@ -1483,6 +1483,12 @@ extern "C" int pic_solver_set_warm_start(pic_world* w, int mode) {
     return PIC_OK;
 }
 
+extern "C" int pic_solver_set_warm_jacobi(pic_world* w, int iterations) {
+    if (!w || iterations < 0 || iterations > 1000) return fail(PIC_ERR_ARG, "bad Jacobi iteration count");
+    w->warm_jacobi = iterations;
+    return PIC_OK;
+}
+
 extern "C" int pic_solver_last_norms(pic_world* w, double* out) {
     if (!w || !out) return fail(PIC_ERR_ARG, "null argument");
     for (int c = 0; c < 3; c++) out[c] = w->last_norms[c];
@@ -1553,8 +1559,6 @@ bool estimate_certified(const pic_world* w, double r2, double scale) {
 int ensure_lp_train(pic_world* w);
 
 constexpr int kLearnedInnerCap = 400;  // iterations of one learned inner solve before falling back
-constexpr int kWarmJacobiCap = 16;     // Jacobi iterations a warm-started learned solve tries first
-constexpr int kJacobiRetry = 8;        // warm solves that skip the Jacobi attempt after it failed
 // the last inner solve stops at sqrt(kInnerTarget) of the tolerance: below it with a margin for the
 // FP32 recurrence of the inner residual, which the following float-float residual then certifies
 constexpr double kInnerTarget = 0.25;
@@ -1634,10 +1638,10 @@ int solve_impl(pic_world* w, int* iters_out, double* rel_out) {
         rc = estimated ? residual_update(w, sw, r2, b2, s2) : residual_norms(w, sw, 0, r2, b2, s2);
     }
     if (rc) return rc;
-    // a warm solve of the learned method first tries a few Jacobi iterations, unless the last
-    // attempt failed (then it retries after kJacobiRetry warm solves)
-    bool jacobi_first = warm && w->method == PIC_SOLVER_LEARNED && w->jacobi_skip == 0;
-    if (warm && w->jacobi_skip > 0) w->jacobi_skip--;
+    // a warm solve of the learned method first runs a few Jacobi iterations: even when they do
+    // not reach the target they remove the high-frequency part of a warm residual (the particle
+    // noise of the step's charge change) at a quarter of the cost of a learned iteration
+    const bool jacobi_first = warm && w->method == PIC_SOLVER_LEARNED && w->warm_jacobi > 0;
     const bool collect = w->lp_collect && w->method != PIC_SOLVER_RBSOR;
     if (collect) {
         rc = ensure_lp_train(w);
@@ -1699,7 +1703,7 @@ int solve_impl(pic_world* w, int* iters_out, double* rel_out) {
             float* dout = w->d2;
             int it = 0;
             // a warm-started refinement of the learned method tries a few Jacobi iterations first
-            const int cap = (w->method == PIC_SOLVER_LEARNED && !use_pcg) ? kWarmJacobiCap : w->max_it;
+            const int cap = (w->method == PIC_SOLVER_LEARNED && !use_pcg) ? w->warm_jacobi : w->max_it;
             for (int nb = 2;; nb = std::min(16, 2 * nb)) {  // growing batches: early exits cost little
                 int batch = std::min(std::min(nb, w->max_it - iters), cap - it);
                 if (batch <= 0) break;
@@ -1719,7 +1723,6 @@ int solve_impl(pic_world* w, int* iters_out, double* rel_out) {
                 }
                 iters += batch;
             }
-            if (cap == kWarmJacobiCap && !w->h_flag[0]) w->jacobi_skip = kJacobiRetry;
         }
         if (collect) lp_pair_add(*w->lp, w->e, w->g.nv, w->stream, grid);
         if (track) {
