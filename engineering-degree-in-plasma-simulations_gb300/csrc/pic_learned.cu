@@ -397,13 +397,6 @@ __global__ void __launch_bounds__(kNodeThreads) k_lp_up0(GridDev g, LView rin, L
     }
 }
 
-// The same operator as k_lp_up0 on 3-D tiles: a CTA owns 32 x 8 x 8 nodes.  It stages the residual
-// tile with its one-node halo (34 x 10 x 10 values, view neighbour rules: wrapped on periodic
-// axes, zero outside) in shared memory with all of its loads in flight at once, and issues the
-// mask, q and prolongation loads of its outputs before the barrier, so the kernel streams the
-// residual from HBM about once (the halo re-reads hit L2) instead of waiting on 27 scattered
-// loads per node.  A thread walks its column's ten tile planes, forms each plane's three 3 x 3
-// partial sums (9 shared reads, 27 FMAs) and rolls them into the outputs of planes p+1, p, p-1.
 constexpr int kUp0X = 32, kUp0Y = 8, kUp0Z = 8;
 constexpr int kUp0HX = kUp0X + 2, kUp0HY = kUp0Y + 2, kUp0HZ = kUp0Z + 2;
 __device__ __forceinline__ int lv_map(int u, int n, int per) {
@@ -437,105 +430,154 @@ __device__ __forceinline__ void stage_tile(float* __restrict__ dst, const float*
 
 // coarse tile of the prolongation for a 32 x 8 x 8 fine tile: coarse x0/2-1 .. x0/2+16 etc.
 constexpr int kPcX = kUp0X / 2 + 2, kPcY = kUp0Y / 2 + 2, kPcZ = kUp0Z / 2 + 2;
-__global__ void __launch_bounds__(kUp0X * kUp0Y) k_lp_up0_tiled(GridDev g, LView rin, LView cin, float* __restrict__ z,
-                                                                  const uint16_t* __restrict__ kind,
-                                                                  const float* __restrict__ S0,
-                                                                  const float* __restrict__ q, double* gpart,
-                                                                  int gstride, unsigned* ticket, double* out,
-                                                                  const int* flag, int bx_n, int by_n) {
+constexpr int kUp0Tile = kUp0HX * kUp0HY * kUp0HZ, kPcTile = kPcX * kPcY * kPcZ;
+constexpr int kUp0CtasPerSM = 4;
+
+// asynchronous 4-byte global -> shared copy (cp.async); with ok false nothing is read and the
+// shared word is zero-filled (src-size 0; src is then any valid address)
+__device__ __forceinline__ void cp_async_f32(float* dst, const float* src, bool ok) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(tc_smem_u32(dst)), "l"(src), "r"(ok ? 4 : 0)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// The fine level z = mask (S0 * r + P e_1), z.r and z.q, on 32 x 8 x 8 tiles of nodes by
+// persistent CTAs that pipeline the tiles: while a CTA computes one tile from shared memory, the
+// residual tile of its next tile (34 x 10 x 10 with the one-node halo, view neighbour rules:
+// wrapped on periodic axes, zero outside) and the coarse tile of the prolongation (18 x 6 x 6) are
+// already on their way into the other buffer through cp.async, which needs no registers.  A
+// thread walks its column's ten tile planes, forms each plane's three 3 x 3 partial sums (9 shared
+// reads, 27 FMAs) and rolls them into the outputs of planes p+1, p, p-1.
+__global__ void __launch_bounds__(kUp0X * kUp0Y, kUp0CtasPerSM)
+    k_lp_up0_pipe(GridDev g, LView rin, LView cin, float* __restrict__ z, const uint16_t* __restrict__ kind,
+                  const float* __restrict__ S0, const float* __restrict__ q, double* gpart, int gstride,
+                  unsigned* ticket, double* out, const int* flag, int bx_n, int by_n, int ntiles) {
     if (flag && flag[0]) return;
     __shared__ float S[27];
-    __shared__ float t[kUp0HZ][kUp0HY][kUp0HX];
-    __shared__ float pc[kPcZ][kPcY][kPcX];
+    __shared__ __align__(16) float t[2][kUp0Tile];
+    __shared__ __align__(16) float pc[2][kPcTile];
     __shared__ int mx[kUp0HX], myz[kUp0HY * kUp0HZ];  // halo offsets per axis (-1: outside)
     __shared__ int cmx[kPcX], cmyz[kPcY * kPcZ];
     const int tid = threadIdx.x;
     const int tx = tid % kUp0X, ty = tid / kUp0X;
-    int b = blockIdx.x;
-    const int bx = b % bx_n;
-    b /= bx_n;
-    const int by = b % by_n, bz = b / by_n;
-    const int x0 = bx * kUp0X, y0 = by * kUp0Y, z0 = bz * kUp0Z;
     if (tid < 27) S[tid] = S0[tid];
-    if (tid < kUp0HX) mx[tid] = lv_map(x0 - 1 + tid, rin.n[0], rin.per[0]);
-    if (tid < kUp0HY * kUp0HZ) {
-        const int uy = lv_map(y0 - 1 + tid % kUp0HY, rin.n[1], rin.per[1]);
-        const int uz = lv_map(z0 - 1 + tid / kUp0HY, rin.n[2], rin.per[2]);
-        myz[tid] = (uy < 0 || uz < 0) ? -1 : uy * rin.sy + uz * rin.sz;
-    }
-    if (cin.a) {
-        if (tid < kPcX) cmx[tid] = lv_map(x0 / 2 - 1 + tid, cin.n[0], cin.per[0]);
-        if (tid < kPcY * kPcZ) {
-            const int uy = lv_map(y0 / 2 - 1 + tid % kPcY, cin.n[1], cin.per[1]);
-            const int uz = lv_map(z0 / 2 - 1 + tid / kPcY, cin.n[2], cin.per[2]);
-            cmyz[tid] = (uy < 0 || uz < 0) ? -1 : uy * cin.sy + uz * cin.sz;
+    // the halo maps of a tile, a barrier, then its copies into buffer b as one commit group
+    auto issue = [&](int tile, int b) {
+        int bb = tile;
+        const int bx = bb % bx_n;
+        bb /= bx_n;
+        const int by = bb % by_n, bz = bb / by_n;
+        const int x0 = bx * kUp0X, y0 = by * kUp0Y, z0 = bz * kUp0Z;
+        if (tid < kUp0HX) mx[tid] = lv_map(x0 - 1 + tid, rin.n[0], rin.per[0]);
+        if (tid < kUp0HY * kUp0HZ) {
+            const int uy = lv_map(y0 - 1 + tid % kUp0HY, rin.n[1], rin.per[1]);
+            const int uz = lv_map(z0 - 1 + tid / kUp0HY, rin.n[2], rin.per[2]);
+            myz[tid] = (uy < 0 || uz < 0) ? -1 : uy * rin.sy + uz * rin.sz;
         }
-    }
-    __syncthreads();
-    stage_tile<kUp0HX, kUp0HY * kUp0HZ, kUp0X * kUp0Y>(&t[0][0][0], rin.a, mx, myz);
-    if (cin.a) {
-        for (int e = tid; e < kPcX * kPcY * kPcZ; e += kUp0X * kUp0Y) {
-            const int ox = cmx[e % kPcX], oyz = cmyz[e / kPcX];
-            (&pc[0][0][0])[e] = (ox >= 0 && oyz >= 0) ? cin.a[ox + oyz] : 0.f;
-        }
-    }
-    // this thread's outputs: mask and q, in flight before the barrier
-    const int x = x0 + tx, y = y0 + ty;
-    const bool col = x < g.ni && y < g.nj;
-    float qv[kUp0Z];
-    unsigned free_mask = 0;
-#pragma unroll
-    for (int k = 0; k < kUp0Z; k++) {
-        const int zz = z0 + k;
-        qv[k] = 0.f;
-        if (col && zz < g.nk) {
-            const int n = x + y * g.ni + zz * g.ni * g.nj;
-            if ((kind[n] & 3) == kFree) {
-                free_mask |= 1u << k;
-                if (q) qv[k] = q[n];
+        if (cin.a) {
+            if (tid < kPcX) cmx[tid] = lv_map(x0 / 2 - 1 + tid, cin.n[0], cin.per[0]);
+            if (tid < kPcY * kPcZ) {
+                const int uy = lv_map(y0 / 2 - 1 + tid % kPcY, cin.n[1], cin.per[1]);
+                const int uz = lv_map(z0 / 2 - 1 + tid / kPcY, cin.n[2], cin.per[2]);
+                cmyz[tid] = (uy < 0 || uz < 0) ? -1 : uy * cin.sy + uz * cin.sz;
             }
         }
-    }
-    __syncthreads();
-    // prolongation weights (0.75 own coarse point, 0.25 the neighbour on the parity side)
-    const int lx = (x >> 1) - (x0 / 2 - 1), ly = (y >> 1) - (y0 / 2 - 1);
-    const int sx = (x & 1) ? 1 : -1, sy = (y & 1) ? 1 : -1;
-    float P = 0.f, Q = 0.f, f_zr = 0.f, f_zq = 0.f;
-#pragma unroll
-    for (int hz = 0; hz < kUp0HZ; hz++) {
-        float a0 = 0.f, a1 = 0.f, a2 = 0.f;
-#pragma unroll
-        for (int dy = 0; dy < 3; dy++)
-#pragma unroll
-            for (int dx = 0; dx < 3; dx++) {
-                const float r = t[hz][ty + dy][tx + dx];
-                a0 = fmaf(S[3 * dy + dx], r, a0);
-                a1 = fmaf(S[9 + 3 * dy + dx], r, a1);
-                a2 = fmaf(S[18 + 3 * dy + dx], r, a2);
+        __syncthreads();
+        for (int e = tid; e < kUp0Tile; e += kUp0X * kUp0Y) {
+            const int ox = mx[e % kUp0HX], oyz = myz[e / kUp0HX];
+            const bool ok = ox >= 0 && oyz >= 0;
+            cp_async_f32(&t[b][e], ok ? rin.a + ox + oyz : rin.a, ok);
+        }
+        if (cin.a) {
+            for (int e = tid; e < kPcTile; e += kUp0X * kUp0Y) {
+                const int ox = cmx[e % kPcX], oyz = cmyz[e / kPcX];
+                const bool ok = ox >= 0 && oyz >= 0;
+                cp_async_f32(&pc[b][e], ok ? cin.a + ox + oyz : cin.a, ok);
             }
-        const int k = hz - 2;  // output plane z0 + k is complete after tile plane hz = k + 2
-        if (k >= 0 && col && z0 + k < g.nk) {
-            const int n = x + y * g.ni + (z0 + k) * g.ni * g.nj;
-            if (free_mask >> k & 1u) {
-                float v = P + a2;
-                if (cin.a) {
-                    const int zf = z0 + k;
-                    const int lz = (zf >> 1) - (z0 / 2 - 1), sz = (zf & 1) ? 1 : -1;
-                    const float a00 = 0.75f * pc[lz][ly][lx] + 0.25f * pc[lz][ly][lx + sx];
-                    const float a01 = 0.75f * pc[lz][ly + sy][lx] + 0.25f * pc[lz][ly + sy][lx + sx];
-                    const float a10 = 0.75f * pc[lz + sz][ly][lx] + 0.25f * pc[lz + sz][ly][lx + sx];
-                    const float a11 = 0.75f * pc[lz + sz][ly + sy][lx] + 0.25f * pc[lz + sz][ly + sy][lx + sx];
-                    v += 0.75f * (0.75f * a00 + 0.25f * a01) + 0.25f * (0.75f * a10 + 0.25f * a11);
+        }
+        cp_async_commit();
+    };
+    int tile = blockIdx.x;
+    if (tile < ntiles) issue(tile, 0);
+    float f_zr = 0.f, f_zq = 0.f;
+    for (int b = 0; tile < ntiles; tile += gridDim.x, b ^= 1) {
+        const int next = tile + gridDim.x;
+        __syncthreads();  // every thread is done with the other buffer and with the maps
+        if (next < ntiles) issue(next, b ^ 1);
+        int bb = tile;
+        const int bx = bb % bx_n;
+        bb /= bx_n;
+        const int by = bb % by_n, bz = bb / by_n;
+        const int x0 = bx * kUp0X, y0 = by * kUp0Y, z0 = bz * kUp0Z;
+        // this thread's outputs: mask and q, in flight during the wait
+        const int x = x0 + tx, y = y0 + ty;
+        const bool col = x < g.ni && y < g.nj;
+        float qv[kUp0Z];
+        unsigned free_mask = 0;
+#pragma unroll
+        for (int k = 0; k < kUp0Z; k++) {
+            const int zz = z0 + k;
+            qv[k] = 0.f;
+            if (col && zz < g.nk) {
+                const int n = x + y * g.ni + zz * g.ni * g.nj;
+                if ((kind[n] & 3) == kFree) {
+                    free_mask |= 1u << k;
+                    if (q) qv[k] = q[n];
                 }
-                z[n] = v;
-                f_zr += v * t[k + 1][ty + 1][tx + 1];
-                f_zq += v * qv[k];
-            } else {
-                z[n] = 0.f;
             }
         }
-        P = Q + a1;
-        Q = a0;
+        if (next < ntiles)
+            cp_async_wait<1>();
+        else
+            cp_async_wait<0>();
+        __syncthreads();  // this tile's copies of every thread have landed
+        const float* T = t[b];
+        const float* PC = pc[b];
+        // prolongation weights (0.75 own coarse point, 0.25 the neighbour on the parity side)
+        const int lx = (x >> 1) - (x0 / 2 - 1), ly = (y >> 1) - (y0 / 2 - 1);
+        const int sx = (x & 1) ? 1 : -1, sy = (y & 1) ? 1 : -1;
+        float P = 0.f, Q = 0.f;
+#pragma unroll
+        for (int hz = 0; hz < kUp0HZ; hz++) {
+            float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+#pragma unroll
+            for (int dy = 0; dy < 3; dy++)
+#pragma unroll
+                for (int dx = 0; dx < 3; dx++) {
+                    const float r = T[(hz * kUp0HY + ty + dy) * kUp0HX + tx + dx];
+                    a0 = fmaf(S[3 * dy + dx], r, a0);
+                    a1 = fmaf(S[9 + 3 * dy + dx], r, a1);
+                    a2 = fmaf(S[18 + 3 * dy + dx], r, a2);
+                }
+            const int k = hz - 2;  // output plane z0 + k is complete after tile plane hz = k + 2
+            if (k >= 0 && col && z0 + k < g.nk) {
+                const int n = x + y * g.ni + (z0 + k) * g.ni * g.nj;
+                if (free_mask >> k & 1u) {
+                    float v = P + a2;
+                    if (cin.a) {
+                        const int zf = z0 + k;
+                        const int lz = (zf >> 1) - (z0 / 2 - 1), sz = (zf & 1) ? 1 : -1;
+                        auto C = [&](int cz, int cy, int cx) { return PC[(cz * kPcY + cy) * kPcX + cx]; };
+                        const float a00 = 0.75f * C(lz, ly, lx) + 0.25f * C(lz, ly, lx + sx);
+                        const float a01 = 0.75f * C(lz, ly + sy, lx) + 0.25f * C(lz, ly + sy, lx + sx);
+                        const float a10 = 0.75f * C(lz + sz, ly, lx) + 0.25f * C(lz + sz, ly, lx + sx);
+                        const float a11 = 0.75f * C(lz + sz, ly + sy, lx) + 0.25f * C(lz + sz, ly + sy, lx + sx);
+                        v += 0.75f * (0.75f * a00 + 0.25f * a01) + 0.25f * (0.75f * a10 + 0.25f * a11);
+                    }
+                    z[n] = v;
+                    f_zr += v * T[((k + 1) * kUp0HY + ty + 1) * kUp0HX + tx + 1];
+                    f_zq += v * qv[k];
+                } else {
+                    z[n] = 0.f;
+                }
+            }
+            P = Q + a1;
+            Q = a0;
+        }
     }
     if (out) {
         const float vv[2] = {f_zr, f_zq};
@@ -674,12 +716,13 @@ __global__ void __launch_bounds__(256) k_lp_restrict_tiled(LView f, LView c, con
 // z = B r on the finest level: the tiled kernel when its CTAs fit the reduction's partial slots
 static void launch_up0(const GridDev& g, LView r0, LView cin, float* z, const uint16_t* kind, const float* S0,
                        const float* q, double* gpart, int gstride, unsigned* ticket, double* out, const int* flag,
-                       cudaStream_t s) {
+                       cudaStream_t s, int sms) {
     const int bx_n = (g.ni + kUp0X - 1) / kUp0X, by_n = (g.nj + kUp0Y - 1) / kUp0Y;
-    const long blocks = (long)bx_n * by_n * ((g.nk + kUp0Z - 1) / kUp0Z);
-    if (!out || blocks <= gstride) {
-        k_lp_up0_tiled<<<(unsigned)blocks, kUp0X * kUp0Y, 0, s>>>(g, r0, cin, z, kind, S0, q, gpart, gstride, ticket,
-                                                                  out, flag, bx_n, by_n);
+    const long tiles = (long)bx_n * by_n * ((g.nk + kUp0Z - 1) / kUp0Z);
+    const long ctas = std::min(tiles, (long)std::max(1, sms) * kUp0CtasPerSM);
+    if (!out || ctas <= gstride) {
+        k_lp_up0_pipe<<<(unsigned)ctas, kUp0X * kUp0Y, 0, s>>>(g, r0, cin, z, kind, S0, q, gpart, gstride, ticket, out,
+                                                                flag, bx_n, by_n, (int)tiles);
     } else {
         k_lp_up0<<<node_blocks(g.nv), kNodeThreads, 0, s>>>(g, r0, cin, z, kind, S0, q, gpart, gstride, ticket, out,
                                                             flag);
@@ -737,7 +780,7 @@ void launch_lp_apply(const GridDev& g, const LpState& L, const float* r, float* 
     }
     LView cin = L.nlev > 1 ? lp_level_view(L, 1, L.e[1]) : none;
     launch_up0(g, r0, cin, z, kind, L.W + L.lay.s0, q, red ? red->gpart : nullptr, red ? red->gstride : 0,
-               red ? red->ticket : nullptr, red ? red->scal + kS_RZN : nullptr, flag, s);
+               red ? red->ticket : nullptr, red ? red->scal + kS_RZN : nullptr, flag, s, sms);
 }
 
 // folded stencils of every network level: M = Wm Wl (C x 27), K27[t][t'] = sum_c Wp[t][c] M[c][t'],
@@ -1464,7 +1507,7 @@ void launch_lp_loss_grad(const GridDev& g, LpState& L, const uint16_t* kind, con
         }
     }
     LView cin1 = L.nlev > 1 ? lp_level_view(L, 1, L.e[1]) : none;
-    launch_up0(g, r0, cin1, T->e0, kind, L.W + L.lay.s0, nullptr, nullptr, 0, nullptr, nullptr, nullptr, s);
+    launch_up0(g, r0, cin1, T->e0, kind, L.W + L.lay.s0, nullptr, nullptr, 0, nullptr, nullptr, nullptr, s, sms);
     // loss and its gradient with respect to e
     k_lp_loss<<<grid, 256, 0, s>>>(g, kind, T->e0, x, T->ge, T->part);
     k_lp_loss_scale<<<grid, 256, 0, s>>>(g.nv, T->ge, T->part, T->red);
