@@ -118,10 +118,9 @@ __device__ __forceinline__ int lv_nb(int c, int d, int n, int per) {
     return (u < 0 || u >= n) ? -1 : u;
 }
 
-// z_coarse = R z_fine
-__global__ void k_lp_restrict(LView f, LView c, const int* flag) {
-    if (flag && flag[0]) return;
-    for (unsigned idx = blockIdx.x * blockDim.x + threadIdx.x; idx < (unsigned)c.nvox; idx += gridDim.x * blockDim.x) {
+// z_coarse = R z_fine at coarse voxel idx
+__device__ __forceinline__ void lp_restrict_at(const LView& f, const LView& c, unsigned idx) {
+    {
         int cc[3];
         lv_decode(c, idx, cc[0], cc[1], cc[2]);
         const float w4[4] = {0.25f, 0.75f, 0.75f, 0.25f};
@@ -141,7 +140,7 @@ __global__ void k_lp_restrict(LView f, LView c, const int* flag) {
                 acc += w4[kz] * az;
             }
             c.a[lv_off(c, cc[0], cc[1], cc[2])] = acc;
-            continue;
+            return;
         }
         int fi[3][4];
 #pragma unroll
@@ -177,6 +176,11 @@ __global__ void k_lp_restrict(LView f, LView c, const int* flag) {
         }
         c.a[lv_off(c, cc[0], cc[1], cc[2])] = acc;
     }
+}
+__global__ void k_lp_restrict(LView f, LView c, const int* flag) {
+    if (flag && flag[0]) return;
+    for (unsigned idx = blockIdx.x * blockDim.x + threadIdx.x; idx < (unsigned)c.nvox; idx += gridDim.x * blockDim.x)
+        lp_restrict_at(f, c, idx);
 }
 
 // sum_c P(f, c) e_coarse[c] at fine point f
@@ -343,6 +347,18 @@ __device__ float lp_net_op(const LView& v, const float* __restrict__ fold, const
     return acc;
 }
 
+// e_l = op_l(z_l) + P e_{l+1} at voxel idx of level l; mode 1: network level (fold: its folded
+// stencils in shared memory, fold_g the same in global memory with the face variants after them),
+// 2: diagonal scaling
+__device__ __forceinline__ void lp_up_at(const LView& zin, const LView& cin, const LView& out, int mode,
+                                         const float* fold, const float* __restrict__ fold_g, float inv_diag,
+                                         unsigned idx) {
+    int c[3];
+    lv_decode(out, idx, c[0], c[1], c[2]);
+    float v = mode == 1 ? lp_net_op(zin, fold, fold_g + kLpFold, c) : inv_diag * zin.a[lv_off(zin, c[0], c[1], c[2])];
+    if (cin.a) v += lp_prolong_at(cin, c);
+    out.a[lv_off(out, c[0], c[1], c[2])] = v;
+}
 // e_l = op_l(z_l) + P e_{l+1}; mode 1: network level (fold), 2: diagonal scaling
 __global__ void k_lp_up(LView zin, LView cin, LView out, int mode, const float* __restrict__ fold_g, float inv_diag,
                         const int* flag) {
@@ -353,12 +369,45 @@ __global__ void k_lp_up(LView zin, LView cin, LView out, int mode, const float* 
         __syncthreads();
     }
     for (unsigned idx = blockIdx.x * blockDim.x + threadIdx.x; idx < (unsigned)out.nvox;
-         idx += gridDim.x * blockDim.x) {
-        int c[3];
-        lv_decode(out, idx, c[0], c[1], c[2]);
-        float v = mode == 1 ? lp_net_op(zin, fold, fold_g + kLpFold, c) : inv_diag * zin.a[lv_off(zin, c[0], c[1], c[2])];
-        if (cin.a) v += lp_prolong_at(cin, c);
-        out.a[lv_off(out, c[0], c[1], c[2])] = v;
+         idx += gridDim.x * blockDim.x)
+        lp_up_at(zin, cin, out, mode, fold, fold_g, inv_diag, idx);
+}
+
+// The coarse end of the hierarchy in one CTA: the restrictions from level l0 - 1 down to the
+// last level, then the level operators from the last level back up to l0, with a block barrier
+// between levels.  These levels hold a few thousand voxels or fewer, so one kernel instead of a
+// launch per level and direction removes a chain of latency-bound launches; every voxel is
+// computed by the same device functions as k_lp_restrict and k_lp_up.
+struct LpCoarseArgs {
+    int l0, nlev;
+    LView f0;                        // level l0 - 1 (its restricted input; the residual if l0 == 1)
+    LView z[kLpMaxLevels], e[kLpMaxLevels];
+    int mode[kLpMaxLevels];          // 1: network level (folded stencils), 2: diagonal scaling
+    const float* fold[kLpMaxLevels];
+    float inv_diag[kLpMaxLevels];
+};
+constexpr int kLpCoarseThreads = 512;
+constexpr int kLpCoarseMaxVox = 8192;    // diagonal levels up to this size join the fused chain
+constexpr int kLpCoarseMaxNetVox = 1024;  // network levels up to this size
+__global__ void __launch_bounds__(kLpCoarseThreads) k_lp_coarse(LpCoarseArgs a, const int* flag) {
+    if (flag && flag[0]) return;
+    __shared__ float fold[kLpFold];
+    for (int l = a.l0; l < a.nlev; l++) {
+        const LView& f = l == a.l0 ? a.f0 : a.z[l - 1];
+        for (unsigned idx = threadIdx.x; idx < (unsigned)a.z[l].nvox; idx += blockDim.x) lp_restrict_at(f, a.z[l], idx);
+        __syncthreads();
+    }
+    LView none{};
+    none.a = nullptr;
+    for (int l = a.nlev - 1; l >= a.l0; l--) {
+        if (a.mode[l] == 1) {
+            for (int x = threadIdx.x; x < kLpFold; x += blockDim.x) fold[x] = a.fold[l][x];
+            __syncthreads();
+        }
+        const LView& cin = l + 1 < a.nlev ? a.e[l + 1] : none;
+        for (unsigned idx = threadIdx.x; idx < (unsigned)a.e[l].nvox; idx += blockDim.x)
+            lp_up_at(a.z[l], cin, a.e[l], a.mode[l], fold, a.fold[l], a.inv_diag[l], idx);
+        __syncthreads();
     }
 }
 
@@ -746,10 +795,32 @@ static void launch_restrict(const LView& f, const LView& c, const int* flag, cud
 void launch_lp_apply(const GridDev& g, const LpState& L, const float* r, float* z, const uint16_t* kind,
                      const float* q, const SolveWork* red, const int* flag, cudaStream_t s, int sms) {
     LView r0 = lp_node_view(g, L, const_cast<float*>(r));
-    for (int l = 1; l < L.nlev; l++) {
+    // the first level of the fused coarse chain: every level from it down is small, and a network
+    // level only when it is tiny (one CTA is too little parallelism for the folded stencil above)
+    int l0 = L.nlev;
+    while (l0 > 1) {
+        const long nv_l = (long)L.dims[l0 - 1][0] * L.dims[l0 - 1][1] * L.dims[l0 - 1][2];
+        if (nv_l > kLpCoarseMaxVox || (l0 - 1 <= kLpNetLevels && nv_l > kLpCoarseMaxNetVox)) break;
+        l0--;
+    }
+    for (int l = 1; l < l0; l++) {
         LView f = l == 1 ? r0 : lp_level_view(L, l - 1, L.z[l - 1]);
         LView c = lp_level_view(L, l, L.z[l]);
         launch_restrict(f, c, flag, s, sms);
+    }
+    if (l0 < L.nlev) {
+        LpCoarseArgs ca{};
+        ca.l0 = l0;
+        ca.nlev = L.nlev;
+        ca.f0 = l0 == 1 ? r0 : lp_level_view(L, l0 - 1, L.z[l0 - 1]);
+        for (int l = l0; l < L.nlev; l++) {
+            ca.z[l] = lp_level_view(L, l, L.z[l]);
+            ca.e[l] = lp_level_view(L, l, L.e[l]);
+            ca.mode[l] = l <= kLpNetLevels ? 1 : 2;
+            ca.fold[l] = ca.mode[l] == 1 ? L.fold + (l - 1) * kLpFoldStride : nullptr;
+            ca.inv_diag[l] = (float)(1.0 / L.diag[l]);
+        }
+        k_lp_coarse<<<1, kLpCoarseThreads, 0, s>>>(ca, flag);
     }
     LView none{};
     none.a = nullptr;
@@ -761,7 +832,7 @@ void launch_lp_apply(const GridDev& g, const LpState& L, const float* r, float* 
         cudaStreamSynchronize(s);
         L.k5_valid = true;
     }
-    for (int l = L.nlev - 1; l >= 1; l--) {
+    for (int l = l0 - 1; l >= 1; l--) {
         LView zin = lp_level_view(L, l, L.z[l]);
         LView cin = l + 1 < L.nlev ? lp_level_view(L, l + 1, L.e[l + 1]) : none;
         LView out = lp_level_view(L, l, L.e[l]);
