@@ -485,10 +485,10 @@ def measure_loop(pic, args, wl, rank, ws, local, clocks=True):
         cal_before, cal_after = lp.calibrate()
         rounds = [{"calibration": True, "val_iters_before": cal_before, "val_iters_after": cal_after, "kept": True}]
         for k in range(args.train_rounds):
-            loss, before, after, kept = lp.train(100, lr=1e-3 / (1 + k), pair_every=1)
+            loss, before, after, kept = lp.train(100, lr=args.train_lr / (1 + k), pair_every=1)
             rounds.append({"loss": loss, "val_iters_before": before, "val_iters_after": after, "kept": kept})
         W.synchronize()
-        training = {"pairs_from_steps": args.warmup, "seconds": time.perf_counter() - t0, "rounds": rounds}
+        training = {"pairs_from_steps": args.warmup, "lr": args.train_lr, "seconds": time.perf_counter() - t0, "rounds": rounds}
         for _ in range(2):  # the loop's warm start settles on the trained preconditioner
             W.step()
     W.synchronize()
@@ -958,6 +958,7 @@ def main():
     ap.add_argument("--no-train", dest="train", action="store_false",
                     help="run the loop with the learned preconditioner's starting (BPX) weights")
     ap.add_argument("--train-rounds", type=int, default=3, help="gradient rounds after the level-gain calibration")
+    ap.add_argument("--train-lr", type=float, default=1e-4, help="Adam step of the first gradient round")
     ap.add_argument("--no-extra", dest="extra", action="store_false",
                     help="skip the discharge, ensemble and 128^3 snapshot cases beside the headline")
     ap.add_argument("--dsmc", type=int, default=128, help="n of the n^3-cell DSMC_MEX case (0: skip)")

@@ -536,16 +536,28 @@ __global__ void __launch_bounds__(kUp0X * kUp0Y, kUp0CtasPerSM)
             }
         }
         __syncthreads();
-        for (int e = tid; e < kUp0Tile; e += kUp0X * kUp0Y) {
-            const int ox = mx[e % kUp0HX], oyz = myz[e / kUp0HX];
-            const bool ok = ox >= 0 && oyz >= 0;
-            cp_async_f32(&t[b][e], ok ? rin.a + ox + oyz : rin.a, ok);
+        // a warp copies whole rows: lane l the row's point l (lanes 0, 1 also 32, 33), so the
+        // x offsets stay in registers and each row costs one shared read of its y/z offset
+        const int lane = tid & 31, wp = tid >> 5;
+        const int ox0 = mx[lane], ox1 = lane < kUp0HX - 32 ? mx[32 + lane] : -1;
+        for (int row = wp; row < kUp0HY * kUp0HZ; row += kUp0X * kUp0Y / 32) {
+            const int oyz = myz[row];
+            float* dst = &t[b][row * kUp0HX];
+            const bool ok0 = ox0 >= 0 && oyz >= 0;
+            cp_async_f32(dst + lane, ok0 ? rin.a + ox0 + oyz : rin.a, ok0);
+            if (lane < kUp0HX - 32) {
+                const bool ok1 = ox1 >= 0 && oyz >= 0;
+                cp_async_f32(dst + 32 + lane, ok1 ? rin.a + ox1 + oyz : rin.a, ok1);
+            }
         }
         if (cin.a) {
-            for (int e = tid; e < kPcTile; e += kUp0X * kUp0Y) {
-                const int ox = cmx[e % kPcX], oyz = cmyz[e / kPcX];
-                const bool ok = ox >= 0 && oyz >= 0;
-                cp_async_f32(&pc[b][e], ok ? cin.a + ox + oyz : cin.a, ok);
+            const int cox = lane < kPcX ? cmx[lane] : -1;
+            for (int row = wp; row < kPcY * kPcZ; row += kUp0X * kUp0Y / 32) {
+                const int oyz = cmyz[row];
+                if (lane < kPcX) {
+                    const bool ok = cox >= 0 && oyz >= 0;
+                    cp_async_f32(&pc[b][row * kPcX + lane], ok ? cin.a + cox + oyz : cin.a, ok);
+                }
             }
         }
         cp_async_commit();
@@ -586,9 +598,21 @@ __global__ void __launch_bounds__(kUp0X * kUp0Y, kUp0CtasPerSM)
         __syncthreads();  // this tile's copies of every thread have landed
         const float* T = t[b];
         const float* PC = pc[b];
-        // prolongation weights (0.75 own coarse point, 0.25 the neighbour on the parity side)
-        const int lx = (x >> 1) - (x0 / 2 - 1), ly = (y >> 1) - (y0 / 2 - 1);
-        const int sx = (x & 1) ? 1 : -1, sy = (y & 1) ? 1 : -1;
+        // prolongation weights (0.75 own coarse point, 0.25 the neighbour on the parity side):
+        // the x-y interpolation of this column's six coarse planes, then per output plane the two
+        // planes on its parity side
+        float pxy[kPcZ];
+        if (cin.a) {
+            const int lx = (x >> 1) - (x0 / 2 - 1), ly = (y >> 1) - (y0 / 2 - 1);
+            const int sx = (x & 1) ? 1 : -1, sy = (y & 1) ? 1 : -1;
+#pragma unroll
+            for (int cz = 0; cz < kPcZ; cz++) {
+                auto C = [&](int cy, int cx) { return PC[(cz * kPcY + cy) * kPcX + cx]; };
+                const float a0 = 0.75f * C(ly, lx) + 0.25f * C(ly, lx + sx);
+                const float a1 = 0.75f * C(ly + sy, lx) + 0.25f * C(ly + sy, lx + sx);
+                pxy[cz] = 0.75f * a0 + 0.25f * a1;
+            }
+        }
         float P = 0.f, Q = 0.f;
 #pragma unroll
         for (int hz = 0; hz < kUp0HZ; hz++) {
@@ -608,14 +632,9 @@ __global__ void __launch_bounds__(kUp0X * kUp0Y, kUp0CtasPerSM)
                 if (free_mask >> k & 1u) {
                     float v = P + a2;
                     if (cin.a) {
-                        const int zf = z0 + k;
-                        const int lz = (zf >> 1) - (z0 / 2 - 1), sz = (zf & 1) ? 1 : -1;
-                        auto C = [&](int cz, int cy, int cx) { return PC[(cz * kPcY + cy) * kPcX + cx]; };
-                        const float a00 = 0.75f * C(lz, ly, lx) + 0.25f * C(lz, ly, lx + sx);
-                        const float a01 = 0.75f * C(lz, ly + sy, lx) + 0.25f * C(lz, ly + sy, lx + sx);
-                        const float a10 = 0.75f * C(lz + sz, ly, lx) + 0.25f * C(lz + sz, ly, lx + sx);
-                        const float a11 = 0.75f * C(lz + sz, ly + sy, lx) + 0.25f * C(lz + sz, ly + sy, lx + sx);
-                        v += 0.75f * (0.75f * a00 + 0.25f * a01) + 0.25f * (0.75f * a10 + 0.25f * a11);
+                        // z0 is even: output plane k sits over coarse plane 1 + k/2, parity side k & 1
+                        const int lz = 1 + (k >> 1), sz = (k & 1) ? 1 : -1;
+                        v += 0.75f * pxy[lz] + 0.25f * pxy[lz + sz];
                     }
                     z[n] = v;
                     f_zr += v * T[((k + 1) * kUp0HY + ty + 1) * kUp0HX + tx + 1];
@@ -639,7 +658,8 @@ __global__ void __launch_bounds__(kUp0X * kUp0Y, kUp0CtasPerSM)
 // Points on a non-periodic face take the exact face-class form through lp_net_op.
 constexpr int kNetX = 32, kNetY = 8, kNetZ = 8;
 constexpr int kNetHX = kNetX + 4, kNetHY = kNetY + 4, kNetHZ = kNetZ + 4;
-__device__ __noinline__ float lp_net_op_face(const LView& v, const float* __restrict__ fold, const int c[3]) {
+__device__ __noinline__ float lp_net_op_face(LView v, const float* __restrict__ fold, int x, int y, int z) {
+    const int c[3] = {x, y, z};
     return lp_net_op(v, fold, fold + kLpFold, c);
 }
 struct K5Param {
@@ -649,7 +669,8 @@ __global__ void __launch_bounds__(kNetX * kNetY, 2) k_lp_up_net_tiled(LView zin,
                                                                     const float* __restrict__ fold_g, const int* flag,
                                                                     int bx_n, int by_n, K5Param K5p) {
     if (flag && flag[0]) return;
-    const float* K5 = K5p.k;
+    // K5p.k is indexed with compile-time offsets only, so every coefficient is an FMA operand from
+    // the constant bank (a pointer into the parameter would copy it to local memory)
     __shared__ float t[kNetHZ][kNetHY][kNetHX];
     __shared__ int mx[kNetHX], myz[kNetHY * kNetHZ];  // halo offsets per axis (-1: outside)
     const int tx = threadIdx.x % kNetX, ty = threadIdx.x / kNetX;
@@ -685,14 +706,15 @@ __global__ void __launch_bounds__(kNetX * kNetY, 2) k_lp_up_net_tiled(LView zin,
 #pragma unroll 1
     for (int hz = 0; hz < kNetHZ; hz++) {
         float a[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+        float win[25];  // the plane's 5 x 5 window, loaded once
 #pragma unroll
         for (int dy = 0; dy < 5; dy++)
 #pragma unroll
-            for (int dx = 0; dx < 5; dx++) {
-                const float r = t[hz][ty + dy][tx + dx];
+            for (int dx = 0; dx < 5; dx++) win[5 * dy + dx] = t[hz][ty + dy][tx + dx];
 #pragma unroll
-                for (int dz = 0; dz < 5; dz++) a[dz] = fmaf(K5[25 * dz + 5 * dy + dx], r, a[dz]);
-            }
+        for (int m = 0; m < 25; m++)
+#pragma unroll
+            for (int dz = 0; dz < 5; dz++) a[dz] = fmaf(K5p.k[25 * dz + m], win[m], a[dz]);
 #pragma unroll
         for (int dz = 0; dz < 5; dz++) w[4 - dz] += a[dz];
         const int k = hz - 4;  // output plane z0 + k is complete
@@ -702,7 +724,7 @@ __global__ void __launch_bounds__(kNetX * kNetY, 2) k_lp_up_net_tiled(LView zin,
 #pragma unroll
             for (int ax = 0; ax < 3; ax++)
                 if (!zin.per[ax] && (c[ax] == 0 || c[ax] == zin.n[ax] - 1)) face = true;
-            const float v = face ? lp_net_op_face(zin, fold_g, c) : w[0];
+            const float v = face ? lp_net_op_face(zin, fold_g, c[0], c[1], c[2]) : w[0];
             out.a[lv_off(out, x, y, z0 + k)] = v + pro[k][threadIdx.x];
         }
 #pragma unroll
