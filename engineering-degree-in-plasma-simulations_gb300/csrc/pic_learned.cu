@@ -658,10 +658,6 @@ __global__ void __launch_bounds__(kUp0X * kUp0Y, kUp0CtasPerSM)
 // Points on a non-periodic face take the exact face-class form through lp_net_op.
 constexpr int kNetX = 32, kNetY = 8, kNetZ = 8;
 constexpr int kNetHX = kNetX + 4, kNetHY = kNetY + 4, kNetHZ = kNetZ + 4;
-__device__ __noinline__ float lp_net_op_face(LView v, const float* __restrict__ fold, int x, int y, int z) {
-    const int c[3] = {x, y, z};
-    return lp_net_op(v, fold, fold + kLpFold, c);
-}
 struct K5Param {
     float k[125];
 };
@@ -720,11 +716,23 @@ __global__ void __launch_bounds__(kNetX * kNetY, 2) k_lp_up_net_tiled(LView zin,
         const int k = hz - 4;  // output plane z0 + k is complete
         if (k >= 0 && col && z0 + k < out.n[2]) {
             const int c[3] = {x, y, z0 + k};
-            bool face = false;
+            // a point on a non-periodic face takes the 5 x 5 x 5 variant of its face class (the
+            // network's first-stage taps outside the box left out), applied to the same staged
+            // window: the tile holds zero outside the box and the wrap on periodic axes
+            int cls = 0, mul = 1;
 #pragma unroll
-            for (int ax = 0; ax < 3; ax++)
-                if (!zin.per[ax] && (c[ax] == 0 || c[ax] == zin.n[ax] - 1)) face = true;
-            const float v = face ? lp_net_op_face(zin, fold_g, c[0], c[1], c[2]) : w[0];
+            for (int ax = 0; ax < 3; ax++) {
+                if (!zin.per[ax]) cls += mul * (c[ax] == 0 ? 1 : (c[ax] == zin.n[ax] - 1 ? 2 : 0));
+                mul *= 3;
+            }
+            float v = w[0];
+            if (cls) {
+                const float* __restrict__ K5v = fold_g + kLpFold + 125 * cls;
+                v = 0.f;
+                for (int dz = 0; dz < 5; dz++)
+#pragma unroll
+                    for (int m = 0; m < 25; m++) v = fmaf(K5v[25 * dz + m], t[k + dz][ty + m / 5][tx + m % 5], v);
+            }
             out.a[lv_off(out, x, y, z0 + k)] = v + pro[k][threadIdx.x];
         }
 #pragma unroll
@@ -860,7 +868,9 @@ void launch_lp_apply(const GridDev& g, const LpState& L, const float* r, float* 
         LView out = lp_level_view(L, l, L.e[l]);
         int mode = l <= kLpNetLevels ? 1 : 2;
         const float* fold = mode == 1 ? L.fold + (l - 1) * kLpFoldStride : nullptr;
-        if (mode == 1 && out.nvox >= 64 * 64 * 64) {  // smaller levels: one thread per voxel has more parallelism
+        // the tiled kernel once every axis has at least 8 points (its halo wraps at most once);
+        // below that one thread per voxel
+        if (mode == 1 && out.n[0] >= 8 && out.n[1] >= 8 && out.n[2] >= 8) {
             const int bx_n = (out.n[0] + kNetX - 1) / kNetX, by_n = (out.n[1] + kNetY - 1) / kNetY;
             const int blocks = bx_n * by_n * ((out.n[2] + kNetZ - 1) / kNetZ);
             K5Param k5;
