@@ -1561,7 +1561,7 @@ int ensure_lp_train(pic_world* w);
 constexpr int kLearnedInnerCap = 400;  // iterations of one learned inner solve before falling back
 // the last inner solve stops at sqrt(kInnerTarget) of the tolerance: below it with a margin for the
 // FP32 recurrence of the inner residual, which the following float-float residual then certifies
-constexpr double kInnerTarget = 0.25;
+constexpr double kInnerTarget = 0.64;
 
 // FP32 flexible CG with the learned preconditioner on L e = r (w->r), e from zero, until
 // r.r <= target or cap iterations; *done = iterations, *conv = reached the target
