@@ -681,21 +681,42 @@ __global__ void __launch_bounds__(kNetX * kNetY, 2) k_lp_up_net_tiled(LView zin,
         const int uz = lv_map(z0 - 2 + (int)threadIdx.x / kNetHY, zin.n[2], zin.per[2]);
         myz[threadIdx.x] = (uy < 0 || uz < 0) ? -1 : uy * zin.sy + uz * zin.sz;
     }
-    __syncthreads();
-    stage_tile<kNetHX, kNetHY * kNetHZ, kNetX * kNetY>(&t[0][0][0], zin.a, mx, myz);
-    const int x = x0 + tx, y = y0 + ty;
-    const bool col = x < out.n[0] && y < out.n[1];
-    __shared__ float pro[kNetZ][kNetX * kNetY];  // the coarse correction of every output
-#pragma unroll
-    for (int k = 0; k < kNetZ; k++) {
-        float v = 0.f;
-        if (cin.a && col && z0 + k < out.n[2]) {
-            const int c[3] = {x, y, z0 + k};
-            v = lp_prolong_at(cin, c);
+    // the coarse tile of the prolongation (the fine level's tile rules: wrapped or zero outside)
+    __shared__ float pc[kPcZ][kPcY][kPcX];
+    __shared__ int cmx[kPcX], cmyz[kPcY * kPcZ];
+    if (cin.a) {
+        if (threadIdx.x < kPcX) cmx[threadIdx.x] = lv_map(x0 / 2 - 1 + (int)threadIdx.x, cin.n[0], cin.per[0]);
+        if (threadIdx.x < kPcY * kPcZ) {
+            const int uy = lv_map(y0 / 2 - 1 + (int)threadIdx.x % kPcY, cin.n[1], cin.per[1]);
+            const int uz = lv_map(z0 / 2 - 1 + (int)threadIdx.x / kPcY, cin.n[2], cin.per[2]);
+            cmyz[threadIdx.x] = (uy < 0 || uz < 0) ? -1 : uy * cin.sy + uz * cin.sz;
         }
-        pro[k][threadIdx.x] = v;
     }
     __syncthreads();
+    stage_tile<kNetHX, kNetHY * kNetHZ, kNetX * kNetY>(&t[0][0][0], zin.a, mx, myz);
+    if (cin.a) stage_tile<kPcX, kPcY * kPcZ, kNetX * kNetY>(&pc[0][0][0], cin.a, cmx, cmyz);
+    const int x = x0 + tx, y = y0 + ty;
+    const bool col = x < out.n[0] && y < out.n[1];
+    __syncthreads();
+    // prolongation: the x-y interpolation of this column's six coarse planes (kept in shared
+    // memory, one slot per thread, as the plane loop below indexes it at run time), then per output
+    // plane the two planes on its parity side (z0 is even)
+    static_assert(kNetX == kUp0X && kNetY == kUp0Y && kNetZ == kUp0Z, "the coarse tile follows the fine tile");
+    __shared__ float pxy[kPcZ][kNetX * kNetY];
+    {
+        const int lx = (x >> 1) - (x0 / 2 - 1), ly = (y >> 1) - (y0 / 2 - 1);
+        const int sx = (x & 1) ? 1 : -1, sy = (y & 1) ? 1 : -1;
+#pragma unroll
+        for (int cz = 0; cz < kPcZ; cz++) {
+            float v = 0.f;
+            if (cin.a) {
+                const float a0 = 0.75f * pc[cz][ly][lx] + 0.25f * pc[cz][ly][lx + sx];
+                const float a1 = 0.75f * pc[cz][ly + sy][lx] + 0.25f * pc[cz][ly + sy][lx + sx];
+                v = 0.75f * a0 + 0.25f * a1;
+            }
+            pxy[cz][threadIdx.x] = v;
+        }
+    }
     // rolling window: w[j] collects output plane hz - 4 + j; tile plane hz is offset dz - 2 of
     // output plane hz - dz, i.e. w[4 - dz]
     float w[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
@@ -733,7 +754,9 @@ __global__ void __launch_bounds__(kNetX * kNetY, 2) k_lp_up_net_tiled(LView zin,
 #pragma unroll
                     for (int m = 0; m < 25; m++) v = fmaf(K5v[25 * dz + m], t[k + dz][ty + m / 5][tx + m % 5], v);
             }
-            out.a[lv_off(out, x, y, z0 + k)] = v + pro[k][threadIdx.x];
+            // z0 is even: output plane k sits over coarse plane 1 + k/2, parity side k & 1
+            const int lz = 1 + (k >> 1), sz = (k & 1) ? 1 : -1;
+            out.a[lv_off(out, x, y, z0 + k)] = v + (0.75f * pxy[lz][threadIdx.x] + 0.25f * pxy[lz + sz][threadIdx.x]);
         }
 #pragma unroll
         for (int j2 = 0; j2 < 4; j2++) w[j2] = w[j2 + 1];
