@@ -92,6 +92,7 @@ struct pic_world {
     float2* phi_alt = nullptr;
     float* rho = nullptr;
     uint16_t* kind = nullptr;
+    unsigned* free_bits = nullptr;  // FREE nodes, one bit each (GridDev::free_bits)
     float *r = nullptr, *e = nullptr, *d = nullptr, *d2 = nullptr, *q = nullptr, *z = nullptr;
     double* part = nullptr;
     double* gpart = nullptr;     // block partials of the node-kernel reductions [8][gstride]
@@ -390,6 +391,18 @@ int upload_kinds(pic_world* w, bool reset_phi) {
         }
     }
     CU(cudaMemcpyAsync(w->kind, kind.data(), sizeof(uint16_t) * g.nv, cudaMemcpyHostToDevice, w->stream));
+    {
+        // the FREE nodes as a bit mask, rows padded to whole 32-bit words
+        const int wpr = (g.ni + 31) / 32;
+        std::vector<unsigned> bits((size_t)wpr * g.nj * g.nk, 0u);
+        for (int r = 0; r < g.nj * g.nk; r++)
+            for (int i = 0; i < g.ni; i++)
+                if ((kind[(size_t)r * g.ni + i] & 3) == kFree) bits[(size_t)r * wpr + (i >> 5)] |= 1u << (i & 31);
+        if (!w->free_bits) CU(cudaMalloc((void**)&w->free_bits, sizeof(unsigned) * bits.size()));
+        CU(cudaMemcpy(w->free_bits, bits.data(), sizeof(unsigned) * bits.size(), cudaMemcpyHostToDevice));
+        w->g.free_bits = w->free_bits;
+        w->g.free_wpr = wpr;
+    }
     std::vector<float2> cur(g.nv);
     if (reset_phi) {
         for (int n = 0; n < g.nv; n++) cur[n] = ff_pack(ph[n]);
@@ -638,6 +651,7 @@ extern "C" int pic_world_destroy(pic_world* w) {
     free_lp(w);
     if (w->rho_prev) cudaFree(w->rho_prev);
     if (w->dphi) cudaFree(w->dphi);
+    if (w->free_bits) cudaFree(w->free_bits);
     if (w->aux_pairs) cudaFree(w->aux_pairs);
     if (w->cand_slab) cudaFree(w->cand_slab);
     if (w->mcc_cand) cudaFree(w->mcc_cand);

@@ -67,6 +67,9 @@ struct GridDev {
     int zslab;
     FastDiv fd_zslab;
     int node_grid;  // CTAs of the streaming node kernels chosen by the autotuner (0: default)
+    // one bit per node, set on FREE nodes: row (j, k) of x bits starts at word (k nj + j) free_wpr
+    const unsigned* free_bits;
+    int free_wpr;
 };
 // z index of a node or cell inside its instance slab (the global index without slabs)
 __device__ __forceinline__ int slab_local_z(const GridDev& g, int k) {

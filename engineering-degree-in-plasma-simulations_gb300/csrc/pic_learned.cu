@@ -481,6 +481,7 @@ __device__ __forceinline__ void stage_tile(float* __restrict__ dst, const float*
 constexpr int kPcX = kUp0X / 2 + 2, kPcY = kUp0Y / 2 + 2, kPcZ = kUp0Z / 2 + 2;
 constexpr int kUp0Tile = kUp0HX * kUp0HY * kUp0HZ, kPcTile = kPcX * kPcY * kPcZ;
 constexpr int kUp0CtasPerSM = 4;
+constexpr int kUp0DynSmem = 4 * 2 * (kUp0Tile + kPcTile + kUp0Z * kUp0X * kUp0Y + kUp0Z * kUp0Y);
 
 // asynchronous 4-byte global -> shared copy (cp.async); with ok false nothing is read and the
 // shared word is zero-filled (src-size 0; src is then any valid address)
@@ -507,10 +508,16 @@ __global__ void __launch_bounds__(kUp0X * kUp0Y, kUp0CtasPerSM)
                   unsigned* ticket, double* out, const int* flag, int bx_n, int by_n, int ntiles) {
     if (flag && flag[0]) return;
     __shared__ float S[27];
-    __shared__ __align__(16) float t[2][kUp0Tile];
-    __shared__ __align__(16) float pc[2][kPcTile];
     __shared__ int mx[kUp0HX], myz[kUp0HY * kUp0HZ];  // halo offsets per axis (-1: outside)
     __shared__ int cmx[kPcX], cmyz[kPcY * kPcZ];
+    // double buffers in dynamic shared memory (kUp0DynSmem bytes): residual tile, coarse tile,
+    // q at the tile's outputs, FREE bits of the tile's output rows (x0 is a multiple of 32)
+    extern __shared__ __align__(16) float up0_dyn[];
+    float(*t)[kUp0Tile] = reinterpret_cast<float(*)[kUp0Tile]>(up0_dyn);
+    float(*pc)[kPcTile] = reinterpret_cast<float(*)[kPcTile]>(up0_dyn + 2 * kUp0Tile);
+    float(*qs)[kUp0Z][kUp0X * kUp0Y] = reinterpret_cast<float(*)[kUp0Z][kUp0X * kUp0Y]>(up0_dyn + 2 * (kUp0Tile + kPcTile));
+    unsigned(*fm)[kUp0Z * kUp0Y] =
+        reinterpret_cast<unsigned(*)[kUp0Z * kUp0Y]>(up0_dyn + 2 * (kUp0Tile + kPcTile + kUp0Z * kUp0X * kUp0Y));
     const int tid = threadIdx.x;
     const int tx = tid % kUp0X, ty = tid / kUp0X;
     if (tid < 27) S[tid] = S0[tid];
@@ -560,6 +567,25 @@ __global__ void __launch_bounds__(kUp0X * kUp0Y, kUp0CtasPerSM)
                 }
             }
         }
+        {
+            // this thread's outputs: q, and the FREE word of each output row (zero outside the grid)
+            const int x = x0 + tx, y = y0 + ty;
+            const bool col = x < g.ni && y < g.nj;
+#pragma unroll
+            for (int k = 0; k < kUp0Z; k++) {
+                const int zz = z0 + k;
+                const bool ok = q && col && zz < g.nk;
+                cp_async_f32(&qs[b][k][tid], ok ? q + (x + y * g.ni + zz * g.ni * g.nj) : rin.a, ok);
+            }
+            if (tid < kUp0Z * kUp0Y) {
+                const int k = tid / kUp0Y, yy = y0 + tid % kUp0Y, zz = z0 + k;
+                const bool ok = yy < g.nj && zz < g.nk;
+                cp_async_f32(reinterpret_cast<float*>(&fm[b][tid]),
+                             ok ? reinterpret_cast<const float*>(g.free_bits + ((zz * g.nj + yy) * g.free_wpr + (x0 >> 5)))
+                                : rin.a,
+                             ok);
+            }
+        }
         cp_async_commit();
     };
     int tile = blockIdx.x;
@@ -574,23 +600,8 @@ __global__ void __launch_bounds__(kUp0X * kUp0Y, kUp0CtasPerSM)
         bb /= bx_n;
         const int by = bb % by_n, bz = bb / by_n;
         const int x0 = bx * kUp0X, y0 = by * kUp0Y, z0 = bz * kUp0Z;
-        // this thread's outputs: mask and q, in flight during the wait
         const int x = x0 + tx, y = y0 + ty;
         const bool col = x < g.ni && y < g.nj;
-        float qv[kUp0Z];
-        unsigned free_mask = 0;
-#pragma unroll
-        for (int k = 0; k < kUp0Z; k++) {
-            const int zz = z0 + k;
-            qv[k] = 0.f;
-            if (col && zz < g.nk) {
-                const int n = x + y * g.ni + zz * g.ni * g.nj;
-                if ((kind[n] & 3) == kFree) {
-                    free_mask |= 1u << k;
-                    if (q) qv[k] = q[n];
-                }
-            }
-        }
         if (next < ntiles)
             cp_async_wait<1>();
         else
@@ -629,7 +640,7 @@ __global__ void __launch_bounds__(kUp0X * kUp0Y, kUp0CtasPerSM)
             const int k = hz - 2;  // output plane z0 + k is complete after tile plane hz = k + 2
             if (k >= 0 && col && z0 + k < g.nk) {
                 const int n = x + y * g.ni + (z0 + k) * g.ni * g.nj;
-                if (free_mask >> k & 1u) {
+                if (fm[b][k * kUp0Y + ty] >> tx & 1u) {
                     float v = P + a2;
                     if (cin.a) {
                         // z0 is even: output plane k sits over coarse plane 1 + k/2, parity side k & 1
@@ -638,7 +649,7 @@ __global__ void __launch_bounds__(kUp0X * kUp0Y, kUp0CtasPerSM)
                     }
                     z[n] = v;
                     f_zr += v * T[((k + 1) * kUp0HY + ty + 1) * kUp0HX + tx + 1];
-                    f_zq += v * qv[k];
+                    f_zq += v * qs[b][k][tid];
                 } else {
                     z[n] = 0.f;
                 }
@@ -823,8 +834,15 @@ static void launch_up0(const GridDev& g, LView r0, LView cin, float* z, const ui
     const long tiles = (long)bx_n * by_n * ((g.nk + kUp0Z - 1) / kUp0Z);
     const long ctas = std::min(tiles, (long)std::max(1, sms) * kUp0CtasPerSM);
     if (!out || ctas <= gstride) {
-        k_lp_up0_pipe<<<(unsigned)ctas, kUp0X * kUp0Y, 0, s>>>(g, r0, cin, z, kind, S0, q, gpart, gstride, ticket, out,
-                                                                flag, bx_n, by_n, (int)tiles);
+        static int dyn_set = -1;  // the device whose attribute is set (one device per process here)
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (dyn_set != dev) {
+            cudaFuncSetAttribute(k_lp_up0_pipe, cudaFuncAttributeMaxDynamicSharedMemorySize, kUp0DynSmem);
+            dyn_set = dev;
+        }
+        k_lp_up0_pipe<<<(unsigned)ctas, kUp0X * kUp0Y, kUp0DynSmem, s>>>(g, r0, cin, z, kind, S0, q, gpart, gstride,
+                                                                          ticket, out, flag, bx_n, by_n, (int)tiles);
     } else {
         k_lp_up0<<<node_blocks(g.nv), kNodeThreads, 0, s>>>(g, r0, cin, z, kind, S0, q, gpart, gstride, ticket, out,
                                                             flag);
