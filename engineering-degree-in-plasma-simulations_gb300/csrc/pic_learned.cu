@@ -1059,13 +1059,12 @@ __global__ void __launch_bounds__(256) k_lpcg_k2(GridDev g, const float* __restr
         const float4 q4 = reinterpret_cast<const float4*>(q)[qq];
         const float4 e4 = reinterpret_cast<const float4*>(e)[qq];
         const float4 r4 = reinterpret_cast<const float4*>(r)[qq];
-        const ushort4 k4 = reinterpret_cast<const ushort4*>(kind)[qq];
         const float dv[4] = {d4.x, d4.y, d4.z, d4.w}, qv[4] = {q4.x, q4.y, q4.z, q4.w};
         float ev[4] = {e4.x, e4.y, e4.z, e4.w}, rv[4] = {r4.x, r4.y, r4.z, r4.w};
-        const unsigned short kv[4] = {k4.x, k4.y, k4.z, k4.w};
+        // no kind read: d and q are zero on non-FREE nodes (k_lpcg_k1 writes them so) and so is r,
+        // which leaves e and r unchanged there
 #pragma unroll
         for (int c = 0; c < 4; c++) {
-            if ((kv[c] & 3) != kFree) continue;
             ev[c] += alpha * dv[c];
             rv[c] -= alpha * qv[c];
             frr += rv[c] * rv[c];
@@ -1075,12 +1074,10 @@ __global__ void __launch_bounds__(256) k_lpcg_k2(GridDev g, const float* __restr
     }
     if (blockIdx.x == 0 && threadIdx.x < (g.nv & 3)) {
         const int n = (ng << 2) + threadIdx.x;
-        if ((kind[n] & 3) == kFree) {
-            e[n] += alpha * d[n];
-            const float rn = r[n] - alpha * q[n];
-            r[n] = rn;
-            frr += rn * rn;
-        }
+        e[n] += alpha * d[n];
+        const float rn = r[n] - alpha * q[n];
+        r[n] = rn;
+        frr += rn * rn;
     }
     const float v[1] = {frr};
     grid_sum<1>(v, gpart, gstride, ticket, scal + kS_RR);
