@@ -531,8 +531,10 @@ def measure_loop(pic, args, wl, rank, ws, local, clocks=True):
         "push_deposit": (60.0 * parts_per_step + 2 * 20.0 * nv) * args.steps,
         # collision candidates: the 8 B id of every electron (the collisions themselves are rare)
         "mcc": 8.0 * n_e_avg * args.steps,
-        # 40 B per node per inner PCG iteration, 24 B per node per FP64 refinement
-        "poisson": 40.0 * nv * inner + 24.0 * nv * refine,
+        # per inner iteration 56 B per node for the learned-preconditioned CG (CG 40, fine level 14,
+        # coarse levels 2) -- the loop's warm solves run no Jacobi iterations first unless asked,
+        # which count 40 B -- and 24 B per node per FP64 refinement
+        "poisson": (56.0 if WARM_JACOBI[0] == 0 else 40.0) * nv * inner + 24.0 * nv * refine,
         "efield": 24.0 * nv * args.steps,
         "rho": (2 * 20.0 + 4.0) * nv * args.steps,
     }
