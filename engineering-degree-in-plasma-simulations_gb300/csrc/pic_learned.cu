@@ -451,7 +451,10 @@ constexpr int kUp0HX = kUp0X + 2, kUp0HY = kUp0Y + 2, kUp0HZ = kUp0Z + 2;
 __device__ __forceinline__ int lv_map(int u, int n, int per) {
     if ((unsigned)u < (unsigned)n) return u;
     if (!per) return -1;
-    return u < 0 ? u + n : u - n;
+    // a tile past the end of a short periodic axis can reach beyond one period: reduce fully so
+    // that every staged read stays on the grid
+    const int m = u % n;
+    return m < 0 ? m + n : m;
 }
 // Stages a halo tile of HX x R values (R rows of HX) in shared memory: element e = hx + HX row
 // reads src[mx[hx] + myz[row]] (0 when either offset is -1).  The trip count is a constant, so
