@@ -491,6 +491,7 @@ def measure_loop(pic, args, wl, rank, ws, local, clocks=True):
         training = {"pairs_from_steps": args.warmup, "lr": args.train_lr, "seconds": time.perf_counter() - t0, "rounds": rounds}
         for _ in range(2):  # the loop's warm start settles on the trained preconditioner
             W.step()
+    trained_weights = lp.weights() if args.train else None
     W.synchronize()
     W.timing(True)
     W.timing_reset()
@@ -563,6 +564,7 @@ def measure_loop(pic, args, wl, rank, ws, local, clocks=True):
                           "residual_rel_b": norms["r"] / norms["b"] if norms["b"] > 0 else None,
                           "residual_rel_charge": norms["r"] / norms["charge"] if norms["charge"] > 0 else None},
         "autotuned": tuned, "clocks": clk.summary() if clocks else None, "training": training,
+        "trained_weights": trained_weights,
     }
     return res, W, (e, i)
 
@@ -573,7 +575,8 @@ def run_gpu(args, wl, rank, ws, local):
     res, W, _ = measure_loop(pic, args, wl, rank, ws, local)
     W.close()
     # e2e: same loop through the C ABI from pinned host buffers (upload + per-step diagnostics)
-    e2e = None if ensemble else run_e2e(pic, wl, args, rank)
+    e2e = None if ensemble else run_e2e(pic, wl, args, rank, weights=res.pop("trained_weights"),
+                                        shapes=res["autotuned"])
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(wl, res["inner_per_step"], res["refinements_per_step"], sample=args.cpu_sample)
@@ -867,9 +870,12 @@ def dsmc_bench(pic, ncell, ppc=16, calls=10, cpu=True):
     return out
 
 
-def run_e2e(pic, wl, args, rank):
+def run_e2e(pic, wl, args, rank, weights=None, shapes=None):
     """Host-facing run: particles uploaded from pinned FP64 host buffers through the C ABI,
-    K steps, and the conservation diagnostics read back every step."""
+    K steps, and the conservation diagnostics read back every step.  The preconditioner starts
+    from `weights` and the launch shapes are `shapes` when given: the ones the device arm trained
+    and tuned on this workload, loaded before the clock as a user loads a previous run's trained
+    weights and tuned shapes (the training and tuning themselves are reported with the device arm)."""
     import torch
 
     n = wl["n_each"]
@@ -904,6 +910,10 @@ def run_e2e(pic, wl, args, rank):
     Sv = loop_solver(pic, W)
     W.configure_loop(solve_each_step=True, sort_every=SORT_EVERY[0], merge_every=MERGE_EVERY, merge_after=0,
                      merge_min=MERGE_MIN)
+    if weights is not None:
+        pic.LearnedPreconditioner(W).set_weights(weights)
+    if shapes is not None:
+        W.set_launch_shapes(**shapes)
     import ctypes as C
 
     L_ = W._L
@@ -911,17 +921,25 @@ def run_e2e(pic, wl, args, rank):
     t0 = time.perf_counter()
     marks = {}
     for sp, (pos, vel, w) in ((e, he), (i, hi)):
+        t1 = time.perf_counter()
         rc = L_.pic_species_add_particles(W.handle, sp.id, C.c_void_p(pos.data_ptr()), C.c_void_p(vel.data_ptr()),
                                           C.c_void_p(w.data_ptr()), None, n, 1)
         if rc:
             raise RuntimeError("upload failed %d" % rc)
+        t2 = time.perf_counter()
         sp.sortIndexes()  # cell order, as after a sort step of the loop
+        W.synchronize()
+        marks["upload_" + sp.name] = t2 - t1
+        marks["sort_" + sp.name] = time.perf_counter() - t2
     W.synchronize()
     marks["upload_and_sort"] = time.perf_counter() - t0
     Sv.solve(raise_on_fail=True)
     Sv.computeEF()
     W.synchronize()
     marks["initial_solve"] = time.perf_counter() - t0 - marks["upload_and_sort"]
+    W.timing(True)
+    W.timing_reset()
+    st0 = Sv.stats()
     diag = np.zeros(5)
     for _ in range(args.steps):
         W.step()
@@ -931,11 +949,16 @@ def run_e2e(pic, wl, args, rank):
     t = time.perf_counter() - t0
     marks["steps"] = t - marks["upload_and_sort"] - marks["initial_solve"]
     parts = e.getNumParticles() + i.getNumParticles()
+    groups = {name: W.timer(name)[0] / args.steps for name in ("step", "push_deposit", "poisson", "sums", "sort", "merge")}
+    inner = (Sv.stats()["inner"] - st0["inner"]) / args.steps
+    W_shapes = W.launch_shapes()
     W.close()
     h2d = 2 * n * (7 * 8)  # pos, vel, w in FP64
     return {"value": parts * args.steps / t, "unit": "particle-steps/s",
             "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": 2 * 5 * 8 * 512,
-            "seconds": t, "seconds_by_part": marks}
+            "seconds": t, "seconds_by_part": marks, "groups_ms_per_step": groups, "poisson_inner_per_step": inner,
+            "preconditioner": "trained weights of the device arm" if weights is not None else "starting weights",
+            "launch_shapes": W_shapes}
 
 
 def main():

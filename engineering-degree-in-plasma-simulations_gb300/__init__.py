@@ -66,6 +66,8 @@ def library():
         "pic_source_create": [vp, i, d, d, d, i, u64, vp],
         "pic_source_sample": [vp, i],
         "pic_autotune": [vp, vp, vp],
+        "pic_launch_shapes": [vp, vp, vp, vp],
+        "pic_set_launch_shapes": [vp, i, i, i],
         "pic_world_potential_energy": [vp, vp],
         "pic_species_sample_particles": [vp, i, l, vp, vp, vp],
         "pic_world_set_boundaries": [vp, vp, vp, vp],
@@ -301,7 +303,17 @@ class World:
         """Measure launch shapes on this world's data and keep the fastest (pic_autotune)."""
         a, b = C.c_int(), C.c_int()
         _check(self._L.pic_autotune(self._h, C.byref(a), C.byref(b)))
-        return dict(push_ctas_per_sm=a.value, node_grid=b.value)
+        return self.launch_shapes()
+
+    def launch_shapes(self):
+        """Launch shapes in use: push CTAs per SM, CTAs of the streaming and of the CG stencil kernels."""
+        a, b, c = C.c_int(), C.c_int(), C.c_int()
+        _check(self._L.pic_launch_shapes(self._h, C.byref(a), C.byref(b), C.byref(c)))
+        return dict(push_ctas_per_sm=a.value, node_grid=b.value, cg_grid=c.value)
+
+    def set_launch_shapes(self, push_ctas_per_sm=0, node_grid=0, cg_grid=0):
+        """Use launch shapes tuned on an earlier world of the same size (0: built-in default)."""
+        _check(self._L.pic_set_launch_shapes(self._h, int(push_ctas_per_sm), int(node_grid), int(cg_grid)))
 
     def step(self):
         _check(self._L.pic_step(self._h))

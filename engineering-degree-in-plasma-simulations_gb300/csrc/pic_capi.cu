@@ -2537,6 +2537,26 @@ extern "C" int pic_autotune(pic_world* w, int* push_ctas_per_sm, int* node_grid)
         w->g.node_grid = best;
         w->rhs_valid = false;  // r was rewritten: the next solve starts from a full residual
     }
+    // CG stencil kernels (d = z + beta d, q = L d): timed on the learned-CG one at iteration 0, which
+    // writes only the solver's scratch arrays (d2, q and the dot-product slot; every solve starts
+    // them afresh)
+    {
+        SolveWork sw = solve_work(w);
+        const int most = std::min<long>((w->g.nv / 4 + 255) / 256, (long)w->gstride);
+        int best = 0;
+        float best_ms = 0.f;
+        for (int m : {2, 4, 8, 16}) {
+            const int cand = std::min(w->sms * m, most);
+            if (cand < 1 || cand == best) continue;
+            w->g.cg_grid = cand;
+            const float ms = time_launches(w, 5, [&] { launch_lpcg_k1_probe(w->g, sw, w->d, w->d2, w->stream); });
+            if (!best || ms < best_ms) {
+                best = cand;
+                best_ms = ms;
+            }
+        }
+        w->g.cg_grid = best;
+    }
     // push + deposit: CTAs per SM from 1 to the occupancy limit, timed on pushes with dt = 0
     // (positions and velocities stay, and the deposit reproduces the density of the particles
     // where they are, which the last step deposited)
@@ -2568,6 +2588,30 @@ extern "C" int pic_autotune(pic_world* w, int* push_ctas_per_sm, int* node_grid)
     }
     if (node_grid) *node_grid = w->g.node_grid;
     return check_device_error(w);
+}
+
+extern "C" int pic_launch_shapes(pic_world* w, int* push_ctas_per_sm, int* node_grid, int* cg_grid) {
+    if (!w) return fail(PIC_ERR_ARG, "null world");
+    if (push_ctas_per_sm) *push_ctas_per_sm = w->sms > 0 ? w->grid_push / w->sms : 0;
+    if (node_grid) *node_grid = w->g.node_grid;
+    if (cg_grid) *cg_grid = w->g.cg_grid;
+    return PIC_OK;
+}
+
+extern "C" int pic_set_launch_shapes(pic_world* w, int push_ctas_per_sm, int node_grid, int cg_grid) {
+    if (!w) return fail(PIC_ERR_ARG, "null world");
+    CU(cudaSetDevice(w->device));
+    const int push_most = push_blocks_per_sm();
+    if (push_ctas_per_sm < 0 || push_ctas_per_sm > push_most)
+        return fail(PIC_ERR_ARG, "push CTAs per SM %d outside 0..%d", push_ctas_per_sm, push_most);
+    // any positive count is safe: a launch never takes more than one CTA per 1024 nodes, which the
+    // block-partial buffer holds
+    for (int v : {node_grid, cg_grid})
+        if (v < 0) return fail(PIC_ERR_ARG, "negative node-kernel grid %d", v);
+    w->grid_push = w->sms * (push_ctas_per_sm > 0 ? push_ctas_per_sm : push_most);
+    w->g.node_grid = node_grid;
+    w->g.cg_grid = cg_grid;
+    return PIC_OK;
 }
 
 extern "C" int pic_debug_set_wait_polls(pic_world* w, long long polls) {

@@ -67,6 +67,7 @@ struct GridDev {
     int zslab;
     FastDiv fd_zslab;
     int node_grid;  // CTAs of the streaming node kernels chosen by the autotuner (0: default)
+    int cg_grid;    // CTAs of the CG stencil kernels (d = z + beta d, q = L d) chosen likewise (0: node_grid)
     // one bit per node, set on FREE nodes: row (j, k) of x bits starts at word (k nj + j) free_wpr
     const unsigned* free_bits;
     int free_wpr;

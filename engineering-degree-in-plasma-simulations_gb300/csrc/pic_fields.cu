@@ -722,7 +722,7 @@ void launch_pcg_init(const GridDev& g, SolveWork& w, cudaStream_t s) {
 void launch_pcg_iter_impl(const GridDev& g, SolveWork& w, float* d_in, float* d_out, int it, double target_rr,
                           cudaStream_t s) {
     const uint16_t* kd = reinterpret_cast<const uint16_t*>(w.kind);
-    k_pcg_k1<<<stream_blocks(g), 256, 0, s>>>(g, w.z, d_in, d_out, w.q, kd, w.gpart, w.gstride, w.ticket, w.scal, w.flag,
+    k_pcg_k1<<<cg_blocks(g), 256, 0, s>>>(g, w.z, d_in, d_out, w.q, kd, w.gpart, w.gstride, w.ticket, w.scal, w.flag,
                                          it, target_rr);
     k_pcg_k2<<<stream_blocks(g), 256, 0, s>>>(g, d_out, w.q, w.e, w.r, w.z, kd, w.gpart, w.gstride, w.ticket,
                                                  w.scal, w.flag, it);

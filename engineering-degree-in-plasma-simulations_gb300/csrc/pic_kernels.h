@@ -192,6 +192,9 @@ inline int stream_blocks(int nv, int cap = 1216) {
     return want < 1 ? 1 : (want < cap ? want : cap);
 }
 inline int stream_blocks(const GridDev& g) { return stream_blocks(g.nv, g.node_grid > 0 ? g.node_grid : 1216); }
+// the CG stencil kernels wait on five neighbour rows per group of four nodes: they want more warps
+// in flight than the streaming kernels, so their CTA count is tuned on its own
+inline int cg_blocks(const GridDev& g) { return g.cg_grid > 0 ? stream_blocks(g.nv, g.cg_grid) : stream_blocks(g); }
 // device scalar slots of the solvers
 enum : int {
     kS_RZ = 0,      // [0..1] r.z of iterations it (double-buffered by parity)

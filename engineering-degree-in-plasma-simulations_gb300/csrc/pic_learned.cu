@@ -1111,11 +1111,18 @@ void launch_lpcg_init(const GridDev& g, SolveWork& w, const LpState& L, cudaStre
 void launch_lpcg_iter(const GridDev& g, SolveWork& w, const LpState& L, float* d_in, float* d_out, int it,
                       double target_rr, cudaStream_t s, int sms) {
     const uint16_t* kd = reinterpret_cast<const uint16_t*>(w.kind);
-    k_lpcg_k1<<<stream_blocks(g), 256, 0, s>>>(g, w.z, d_in, d_out, w.q, kd, w.gpart, w.gstride, w.ticket, w.scal, w.flag,
-                                          it, target_rr);
+    k_lpcg_k1<<<cg_blocks(g), 256, 0, s>>>(g, w.z, d_in, d_out, w.q, kd, w.gpart, w.gstride, w.ticket, w.scal, w.flag,
+                                           it, target_rr);
     k_lpcg_k2<<<stream_blocks(g), 256, 0, s>>>(g, d_out, w.q, w.e, w.r, kd, w.gpart, w.gstride, w.ticket, w.scal,
                                                   w.flag, it);
     launch_lp_apply(g, L, w.r, w.z, kd, w.q, &w, w.flag, s, sms);
+}
+// the first kernel of an iteration alone, at iteration 0 (beta = 0: d = z, q = L z on the scratch
+// arrays): what the launch-shape tuner times
+void launch_lpcg_k1_probe(const GridDev& g, SolveWork& w, float* d_in, float* d_out, cudaStream_t s) {
+    const uint16_t* kd = reinterpret_cast<const uint16_t*>(w.kind);
+    k_lpcg_k1<<<cg_blocks(g), 256, 0, s>>>(g, w.z, d_in, d_out, w.q, kd, w.gpart, w.gstride, w.ticket, w.scal, w.flag,
+                                           0, 0.0);
 }
 
 // =====================================================================================

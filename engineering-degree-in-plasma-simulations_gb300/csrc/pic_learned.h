@@ -103,5 +103,6 @@ void launch_lp_norm2(const float* a, int n, double* part, double* out, cudaStrea
 void launch_lpcg_init(const GridDev& g, SolveWork& w, const LpState& L, cudaStream_t s, int sms);
 void launch_lpcg_iter(const GridDev& g, SolveWork& w, const LpState& L, float* d_in, float* d_out, int it,
                       double target_rr, cudaStream_t s, int sms);
+void launch_lpcg_k1_probe(const GridDev& g, SolveWork& w, float* d_in, float* d_out, cudaStream_t s);
 
 }  // namespace pic

@@ -290,12 +290,21 @@ int pic_dsmc_stats(pic_world* w, int dsmc_id, uint64_t* counts, double* sigma_v_
 int pic_loop_configure(pic_world* w, int solve_each_step, int sort_every, const int* subcycle, int merge_every,
                        int merge_after, int merge_min);
 /* Autotuner (no reference counterpart): measures launch shapes on the world's own data and keeps
- * the fastest for the rest of the run: the CTA count of the streaming node kernels (residual and
- * CG kernels; 2 to 16 per SM, timed on the float-float residual) and the push's CTAs per SM (1 to
- * the occupancy limit, timed on pushes with dt = 0, which leave the particles and their deposit
- * as they are).  Call it once the world holds its particles and fields; the next solve starts
- * from a full residual.  Outputs may be NULL. */
+ * the fastest for the rest of the run: the CTA count of the streaming node kernels (2 to 16 per
+ * SM, timed on the float-float residual), that of the CG stencil kernels (d = z + beta d, q = L d;
+ * same range, timed on the learned-CG one) and the push's CTAs per SM (1 to the occupancy limit,
+ * timed on pushes with dt = 0, which leave the particles and their deposit as they are).  Call it
+ * once the world holds its particles and fields; the next solve starts from a full residual.
+ * Outputs may be NULL. */
 int pic_autotune(pic_world* w, int* push_ctas_per_sm, int* node_grid);
+/* The launch shapes in use (no reference counterpart): push CTAs per SM, CTAs of the streaming
+ * node kernels and of the CG stencil kernels (0: the built-in default).  Outputs may be NULL. */
+int pic_launch_shapes(pic_world* w, int* push_ctas_per_sm, int* node_grid, int* cg_grid);
+/* Sets the launch shapes, e.g. the ones pic_launch_shapes reported after pic_autotune on an earlier
+ * world of the same size (no reference counterpart).  push_ctas_per_sm: 1 to the push's occupancy
+ * limit; node_grid, cg_grid: CTA counts (a launch takes at most one CTA per 1024 nodes); 0 keeps
+ * the built-in default for that shape.  PIC_ERR_ARG for a negative value or too many push CTAs. */
+int pic_set_launch_shapes(pic_world* w, int push_ctas_per_sm, int node_grid, int cg_grid);
 /* one iteration of the time loop: advanceTime, [merge], collisions + push + deposit,
  * compaction, [averages], charge density, [solve + E], [sort] */
 int pic_step(pic_world* w);
