@@ -778,10 +778,8 @@ __global__ void __launch_bounds__(kNetX * kNetY, 2) k_lp_up_net_tiled(LView zin,
     }
 }
 
-// z_coarse = R z_fine on 3-D tiles of 16 x 8 x 4 coarse voxels: the 34 x 18 x 10 fine points they
-// read are staged in shared memory first (the same index rules as k_lp_restrict)
-constexpr int kRsX = 16, kRsY = 8, kRsZ = 4;
-constexpr int kRsHX = 2 * kRsX + 2, kRsHY = 2 * kRsY + 2, kRsHZ = 2 * kRsZ + 2;
+// index rule of the restriction along one axis (k_lp_restrict): fine point raw of coarse level c,
+// wrapped once by the coarse period on a periodic axis; -1 outside the fine box
 __device__ __forceinline__ int rs_map(int raw, const LView& f, const LView& c, int ax) {
     if (f.per[ax]) {
         const int nc2 = 2 * c.n[ax];
@@ -790,43 +788,110 @@ __device__ __forceinline__ int rs_map(int raw, const LView& f, const LView& c, i
     }
     return (raw >= 0 && raw < f.n[ax]) ? raw : -1;
 }
-__global__ void __launch_bounds__(256) k_lp_restrict_tiled(LView f, LView c, const int* flag, int bx_n, int by_n) {
+// z_coarse = R z_fine, one warp per column of 32 x 4 x 4 coarse voxels, all in registers.  Lane l
+// owns coarse x = cx0 + l.  The warp marches through the column's ten fine planes; in each it
+// reads the ten fine rows of the column, lane l taking fine x 2cx and 2cx + 1 as one float2 (a
+// warp reads 64 consecutive fine points) and fine x 2cx - 1 and 2cx + 2 from its neighbour lanes
+// (x pass), combines four rows per coarse y (y pass) and adds the plane into the two coarse planes
+// it is a tap of (z pass).  The two halo points of a row (fine x 2 cx0 - 1 and 2 cx0 + 64, read by
+// lanes 0 and 31) follow the index rules of k_lp_restrict (outside the box or wrapped); a column
+// whose 64 body points leave the box or wrap, or a level whose rows are not 8-byte aligned, reads
+// four mapped points per lane instead.
+constexpr int kRmX = 32, kRmY = 4, kRmZ = 4;
+constexpr int kRmHY = 2 * kRmY + 2, kRmHZ = 2 * kRmZ + 2;
+constexpr int kRmWarps = 4;  // warps per CTA
+__global__ void __launch_bounds__(32 * kRmWarps, 4) k_lp_restrict_march(LView f, LView c, const int* flag, int bx_n,
+                                                                      int by_n, int nwarps) {
     if (flag && flag[0]) return;
-    __shared__ float t[kRsHZ][kRsHY][kRsHX];
-    __shared__ int mx[kRsHX], myz[kRsHY * kRsHZ];  // fine offsets per axis (-1: outside)
-    int b = blockIdx.x;
+    const int gw = (int)blockIdx.x * kRmWarps + (int)(threadIdx.x >> 5);
+    if (gw >= nwarps) return;  // whole warps
+    const int lane = threadIdx.x & 31;
+    int b = gw;
     const int bx = b % bx_n;
     b /= bx_n;
     const int by = b % by_n, bz = b / by_n;
-    const int cx0 = bx * kRsX, cy0 = by * kRsY, cz0 = bz * kRsZ;
-    const int tid = threadIdx.x;
-    if (tid < kRsHX) mx[tid] = rs_map(2 * cx0 - 1 + tid, f, c, 0);
-    if (tid < kRsHY * kRsHZ) {
-        const int uy = rs_map(2 * cy0 - 1 + tid % kRsHY, f, c, 1);
-        const int uz = rs_map(2 * cz0 - 1 + tid / kRsHY, f, c, 2);
-        myz[tid] = (uy < 0 || uz < 0) ? -1 : uy * f.sy + uz * f.sz;
+    const int cx0 = bx * kRmX, cy0 = by * kRmY, cz0 = bz * kRmZ;
+    const int fx = 2 * (cx0 + lane);  // this lane's even fine x
+    const int body_end = 2 * cx0 + 2 * kRmX;
+    const bool fast = body_end <= f.n[0] && (!f.per[0] || body_end <= 2 * c.n[0]) && ((f.sy | f.sz) & 1) == 0 &&
+                      (reinterpret_cast<uintptr_t>(f.a) & 7) == 0;
+    // fast: xo[0] is the halo of lane 0 or 31 (-1: none); otherwise the four mapped fine x
+    int xo[4];
+    if (fast) {
+        xo[0] = lane == 0 ? rs_map(2 * cx0 - 1, f, c, 0) : (lane == 31 ? rs_map(body_end, f, c, 0) : -1);
+        xo[1] = xo[2] = xo[3] = -1;
+    } else {
+#pragma unroll
+        for (int k = 0; k < 4; k++) xo[k] = rs_map(fx - 1 + k, f, c, 0);
     }
-    __syncthreads();
-    stage_tile<kRsHX, kRsHY * kRsHZ, 256>(&t[0][0][0], f.a, mx, myz);
-    __syncthreads();
+    // fine row offsets of the column's y range; a row outside the box reads row 0 and is dropped
+    int oy[kRmHY];
+    bool my[kRmHY];
+#pragma unroll
+    for (int r = 0; r < kRmHY; r++) {
+        const int u = rs_map(2 * cy0 - 1 + r, f, c, 1);
+        oy[r] = u < 0 ? 0 : u * f.sy;
+        my[r] = u >= 0;
+    }
     const float w4[4] = {0.25f, 0.75f, 0.75f, 0.25f};
-    for (int o = threadIdx.x; o < kRsX * kRsY * kRsZ; o += 256) {
-        const int ox = o % kRsX, oy = (o / kRsX) % kRsY, oz = o / (kRsX * kRsY);
-        const int cx = cx0 + ox, cy = cy0 + oy, cz = cz0 + oz;
-        if (cx >= c.n[0] || cy >= c.n[1] || cz >= c.n[2]) continue;
-        float acc = 0.f;
+    float acc[kRmZ][kRmY];
 #pragma unroll
-        for (int kz = 0; kz < 4; kz++) {
-            float az = 0.f;
+    for (int cz = 0; cz < kRmZ; cz++)
 #pragma unroll
-            for (int ky = 0; ky < 4; ky++) {
-                const float* row = &t[2 * oz + kz][2 * oy + ky][2 * ox];
-                az += w4[ky] * (w4[0] * row[0] + w4[1] * row[1] + w4[2] * row[2] + w4[3] * row[3]);
+        for (int cy = 0; cy < kRmY; cy++) acc[cz][cy] = 0.f;
+    // straight-line over the planes (no branch between the loads of consecutive planes), so that
+    // the next planes' rows are in flight while one is combined
+#pragma unroll
+    for (int pz = 0; pz < kRmHZ; pz++) {
+        const int uz = rs_map(2 * cz0 - 1 + pz, f, c, 2);
+        const float* plane = f.a + (size_t)(uz < 0 ? 0 : uz) * f.sz;
+        const bool mz = uz >= 0;
+        float xv[kRmHY];
+        if (fast) {
+            float2 pv[kRmHY];
+            float ph[kRmHY];
+#pragma unroll
+            for (int r = 0; r < kRmHY; r++) {
+                pv[r] = *reinterpret_cast<const float2*>(plane + oy[r] + fx);
+                ph[r] = xo[0] >= 0 ? plane[oy[r] + xo[0]] : 0.f;
             }
-            acc += w4[kz] * az;
+#pragma unroll
+            for (int r = 0; r < kRmHY; r++) {
+                float left = __shfl_up_sync(0xffffffffu, pv[r].y, 1);
+                float right = __shfl_down_sync(0xffffffffu, pv[r].x, 1);
+                if (lane == 0) left = ph[r];
+                if (lane == 31) right = ph[r];
+                xv[r] = my[r] && mz ? w4[0] * left + w4[1] * pv[r].x + w4[2] * pv[r].y + w4[3] * right : 0.f;
+            }
+        } else {
+#pragma unroll
+            for (int r = 0; r < kRmHY; r++) {
+                float a[4];
+#pragma unroll
+                for (int k = 0; k < 4; k++) a[k] = xo[k] >= 0 ? plane[oy[r] + xo[k]] : 0.f;
+                xv[r] = my[r] && mz ? w4[0] * a[0] + w4[1] * a[1] + w4[2] * a[2] + w4[3] * a[3] : 0.f;
+            }
         }
-        c.a[lv_off(c, cx, cy, cz)] = acc;
+        // fine plane pz is tap pz - 2 cz of coarse plane cz
+#pragma unroll
+        for (int cz = 0; cz < kRmZ; cz++) {
+            const int k = pz - 2 * cz;
+            if (k < 0 || k > 3) continue;
+#pragma unroll
+            for (int cy = 0; cy < kRmY; cy++) {
+                const float yv = w4[0] * xv[2 * cy] + w4[1] * xv[2 * cy + 1] + w4[2] * xv[2 * cy + 2] +
+                                 w4[3] * xv[2 * cy + 3];
+                acc[cz][cy] += w4[k] * yv;
+            }
+        }
     }
+    const int cx = cx0 + lane;
+    if (cx >= c.n[0]) return;
+#pragma unroll
+    for (int cz = 0; cz < kRmZ; cz++)
+#pragma unroll
+        for (int cy = 0; cy < kRmY; cy++)
+            if (cy0 + cy < c.n[1] && cz0 + cz < c.n[2]) c.a[lv_off(c, cx, cy0 + cy, cz0 + cz)] = acc[cz][cy];
 }
 
 // z = B r on the finest level: the tiled kernel when its CTAs fit the reduction's partial slots
@@ -858,12 +923,10 @@ static int lp_blocks(int nvox, int sms) {
     return std::max(1, (nvox + 255) / 256);
 }
 static void launch_restrict(const LView& f, const LView& c, const int* flag, cudaStream_t s, int sms) {
-    const int bx_n = (c.n[0] + kRsX - 1) / kRsX, by_n = (c.n[1] + kRsY - 1) / kRsY;
-    const int blocks = bx_n * by_n * ((c.n[2] + kRsZ - 1) / kRsZ);
-    if (c.nvox >= 32 * 32 * 32)
-        k_lp_restrict_tiled<<<blocks, 256, 0, s>>>(f, c, flag, bx_n, by_n);
-    else
-        k_lp_restrict<<<lp_blocks(c.nvox, sms), 256, 0, s>>>(f, c, flag);
+    (void)sms;
+    const int bx_n = (c.n[0] + kRmX - 1) / kRmX, by_n = (c.n[1] + kRmY - 1) / kRmY;
+    const int nwarps = bx_n * by_n * ((c.n[2] + kRmZ - 1) / kRmZ);
+    k_lp_restrict_march<<<(nwarps + kRmWarps - 1) / kRmWarps, 32 * kRmWarps, 0, s>>>(f, c, flag, bx_n, by_n, nwarps);
 }
 
 void launch_lp_apply(const GridDev& g, const LpState& L, const float* r, float* z, const uint16_t* kind,
