@@ -502,10 +502,13 @@ __device__ __forceinline__ void cp_async_wait() {
 // persistent CTAs that pipeline the tiles: while a CTA computes one tile from shared memory, the
 // residual tile of its next tile (34 x 10 x 10 with the one-node halo, view neighbour rules:
 // wrapped on periodic axes, zero outside) and the coarse tile of the prolongation (18 x 6 x 6) are
-// already on their way into the other buffer through cp.async, which needs no registers.  A
-// thread walks its column's ten tile planes, forms each plane's three 3 x 3 partial sums (9 shared
-// reads, 27 FMAs) and rolls them into the outputs of planes p+1, p, p-1.
-__global__ void __launch_bounds__(kUp0X * kUp0Y, kUp0CtasPerSM)
+// already on their way into the other buffer through cp.async, which needs no registers.  A thread
+// owns the columns of two adjacent output rows (2p and 2p + 1 of the tile): it walks the ten tile
+// planes, reads the plane's four rows around them once (12 shared reads), forms each row's three
+// 3 x 3 partial sums with the 27 weights held in registers (54 FMAs) and rolls them into the
+// outputs of planes p+1, p, p-1.
+constexpr int kUp0Threads = kUp0X * kUp0Y / 2;
+__global__ void __launch_bounds__(kUp0Threads, kUp0CtasPerSM)
     k_lp_up0_pipe(GridDev g, LView rin, LView cin, float* __restrict__ z, const uint16_t* __restrict__ kind,
                   const float* __restrict__ S0, const float* __restrict__ q, double* gpart, int gstride,
                   unsigned* ticket, double* out, const int* flag, int bx_n, int by_n, int ntiles) {
@@ -522,7 +525,8 @@ __global__ void __launch_bounds__(kUp0X * kUp0Y, kUp0CtasPerSM)
     unsigned(*fm)[kUp0Z * kUp0Y] =
         reinterpret_cast<unsigned(*)[kUp0Z * kUp0Y]>(up0_dyn + 2 * (kUp0Tile + kPcTile + kUp0Z * kUp0X * kUp0Y));
     const int tid = threadIdx.x;
-    const int tx = tid % kUp0X, ty = tid / kUp0X;
+    const int tx = tid % kUp0X, ty0 = 2 * (tid / kUp0X);  // rows ty0 and ty0 + 1 of the tile
+    constexpr int kWarps = kUp0Threads / 32;
     if (tid < 27) S[tid] = S0[tid];
     // the halo maps of a tile, a barrier, then its copies into buffer b as one commit group
     auto issue = [&](int tile, int b) {
@@ -550,7 +554,7 @@ __global__ void __launch_bounds__(kUp0X * kUp0Y, kUp0CtasPerSM)
         // x offsets stay in registers and each row costs one shared read of its y/z offset
         const int lane = tid & 31, wp = tid >> 5;
         const int ox0 = mx[lane], ox1 = lane < kUp0HX - 32 ? mx[32 + lane] : -1;
-        for (int row = wp; row < kUp0HY * kUp0HZ; row += kUp0X * kUp0Y / 32) {
+        for (int row = wp; row < kUp0HY * kUp0HZ; row += kWarps) {
             const int oyz = myz[row];
             float* dst = &t[b][row * kUp0HX];
             const bool ok0 = ox0 >= 0 && oyz >= 0;
@@ -562,7 +566,7 @@ __global__ void __launch_bounds__(kUp0X * kUp0Y, kUp0CtasPerSM)
         }
         if (cin.a) {
             const int cox = lane < kPcX ? cmx[lane] : -1;
-            for (int row = wp; row < kPcY * kPcZ; row += kUp0X * kUp0Y / 32) {
+            for (int row = wp; row < kPcY * kPcZ; row += kWarps) {
                 const int oyz = cmyz[row];
                 if (lane < kPcX) {
                     const bool ok = cox >= 0 && oyz >= 0;
@@ -572,13 +576,17 @@ __global__ void __launch_bounds__(kUp0X * kUp0Y, kUp0CtasPerSM)
         }
         {
             // this thread's outputs: q, and the FREE word of each output row (zero outside the grid)
-            const int x = x0 + tx, y = y0 + ty;
-            const bool col = x < g.ni && y < g.nj;
+            const int x = x0 + tx;
 #pragma unroll
-            for (int k = 0; k < kUp0Z; k++) {
-                const int zz = z0 + k;
-                const bool ok = q && col && zz < g.nk;
-                cp_async_f32(&qs[b][k][tid], ok ? q + (x + y * g.ni + zz * g.ni * g.nj) : rin.a, ok);
+            for (int h = 0; h < 2; h++) {
+                const int ty = ty0 + h, y = y0 + ty;
+                const bool col = x < g.ni && y < g.nj;
+#pragma unroll
+                for (int k = 0; k < kUp0Z; k++) {
+                    const int zz = z0 + k;
+                    const bool ok = q && col && zz < g.nk;
+                    cp_async_f32(&qs[b][k][ty * kUp0X + tx], ok ? q + (x + y * g.ni + zz * g.ni * g.nj) : rin.a, ok);
+                }
             }
             if (tid < kUp0Z * kUp0Y) {
                 const int k = tid / kUp0Y, yy = y0 + tid % kUp0Y, zz = z0 + k;
@@ -592,7 +600,10 @@ __global__ void __launch_bounds__(kUp0X * kUp0Y, kUp0CtasPerSM)
         cp_async_commit();
     };
     int tile = blockIdx.x;
-    if (tile < ntiles) issue(tile, 0);
+    if (tile < ntiles) issue(tile, 0);  // its barrier also publishes S
+    float w[27];
+#pragma unroll
+    for (int m = 0; m < 27; m++) w[m] = S[m];
     float f_zr = 0.f, f_zq = 0.f;
     for (int b = 0; tile < ntiles; tile += gridDim.x, b ^= 1) {
         const int next = tile + gridDim.x;
@@ -603,8 +614,8 @@ __global__ void __launch_bounds__(kUp0X * kUp0Y, kUp0CtasPerSM)
         bb /= bx_n;
         const int by = bb % by_n, bz = bb / by_n;
         const int x0 = bx * kUp0X, y0 = by * kUp0Y, z0 = bz * kUp0Z;
-        const int x = x0 + tx, y = y0 + ty;
-        const bool col = x < g.ni && y < g.nj;
+        const int x = x0 + tx;
+        const bool colA = x < g.ni && y0 + ty0 < g.nj, colB = x < g.ni && y0 + ty0 + 1 < g.nj;
         if (next < ntiles)
             cp_async_wait<1>();
         else
@@ -612,53 +623,72 @@ __global__ void __launch_bounds__(kUp0X * kUp0Y, kUp0CtasPerSM)
         __syncthreads();  // this tile's copies of every thread have landed
         const float* T = t[b];
         const float* PC = pc[b];
-        // prolongation weights (0.75 own coarse point, 0.25 the neighbour on the parity side):
-        // the x-y interpolation of this column's six coarse planes, then per output plane the two
-        // planes on its parity side
-        float pxy[kPcZ];
+        // prolongation weights (0.75 own coarse point, 0.25 the neighbour on the parity side): the
+        // x-y interpolation of the six coarse planes for both rows (even row: the coarse row
+        // below, odd row: the one above; both over the same coarse row ly), then per output plane
+        // the two planes on its parity side
+        float pxA[kPcZ], pxB[kPcZ];
         if (cin.a) {
-            const int lx = (x >> 1) - (x0 / 2 - 1), ly = (y >> 1) - (y0 / 2 - 1);
-            const int sx = (x & 1) ? 1 : -1, sy = (y & 1) ? 1 : -1;
+            const int lx = (x >> 1) - (x0 / 2 - 1), ly = ty0 / 2 + 1;
+            const int sx = (x & 1) ? 1 : -1;
 #pragma unroll
             for (int cz = 0; cz < kPcZ; cz++) {
                 auto C = [&](int cy, int cx) { return PC[(cz * kPcY + cy) * kPcX + cx]; };
                 const float a0 = 0.75f * C(ly, lx) + 0.25f * C(ly, lx + sx);
-                const float a1 = 0.75f * C(ly + sy, lx) + 0.25f * C(ly + sy, lx + sx);
-                pxy[cz] = 0.75f * a0 + 0.25f * a1;
+                const float am = 0.75f * C(ly - 1, lx) + 0.25f * C(ly - 1, lx + sx);
+                const float ap = 0.75f * C(ly + 1, lx) + 0.25f * C(ly + 1, lx + sx);
+                pxA[cz] = 0.75f * a0 + 0.25f * am;
+                pxB[cz] = 0.75f * a0 + 0.25f * ap;
             }
         }
-        float P = 0.f, Q = 0.f;
+        float PA = 0.f, QA = 0.f, PB = 0.f, QB = 0.f;
 #pragma unroll
         for (int hz = 0; hz < kUp0HZ; hz++) {
-            float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+            float rr[4][3];
+#pragma unroll
+            for (int dy = 0; dy < 4; dy++)
+#pragma unroll
+                for (int dx = 0; dx < 3; dx++) rr[dy][dx] = T[(hz * kUp0HY + ty0 + dy) * kUp0HX + tx + dx];
+            float a0A = 0.f, a1A = 0.f, a2A = 0.f, a0B = 0.f, a1B = 0.f, a2B = 0.f;
 #pragma unroll
             for (int dy = 0; dy < 3; dy++)
 #pragma unroll
                 for (int dx = 0; dx < 3; dx++) {
-                    const float r = T[(hz * kUp0HY + ty + dy) * kUp0HX + tx + dx];
-                    a0 = fmaf(S[3 * dy + dx], r, a0);
-                    a1 = fmaf(S[9 + 3 * dy + dx], r, a1);
-                    a2 = fmaf(S[18 + 3 * dy + dx], r, a2);
+                    const int m = 3 * dy + dx;
+                    a0A = fmaf(w[m], rr[dy][dx], a0A);
+                    a1A = fmaf(w[9 + m], rr[dy][dx], a1A);
+                    a2A = fmaf(w[18 + m], rr[dy][dx], a2A);
+                    a0B = fmaf(w[m], rr[dy + 1][dx], a0B);
+                    a1B = fmaf(w[9 + m], rr[dy + 1][dx], a1B);
+                    a2B = fmaf(w[18 + m], rr[dy + 1][dx], a2B);
                 }
             const int k = hz - 2;  // output plane z0 + k is complete after tile plane hz = k + 2
-            if (k >= 0 && col && z0 + k < g.nk) {
-                const int n = x + y * g.ni + (z0 + k) * g.ni * g.nj;
-                if (fm[b][k * kUp0Y + ty] >> tx & 1u) {
-                    float v = P + a2;
-                    if (cin.a) {
-                        // z0 is even: output plane k sits over coarse plane 1 + k/2, parity side k & 1
-                        const int lz = 1 + (k >> 1), sz = (k & 1) ? 1 : -1;
-                        v += 0.75f * pxy[lz] + 0.25f * pxy[lz + sz];
+            if (k >= 0 && z0 + k < g.nk) {
+                // z0 is even: output plane k sits over coarse plane 1 + k/2, parity side k & 1
+                const int lz = 1 + (k >> 1), sz = (k & 1) ? 1 : -1;
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const int ty = ty0 + h;
+                    if (!(h ? colB : colA)) continue;
+                    const int n = x + (y0 + ty) * g.ni + (z0 + k) * g.ni * g.nj;
+                    if (fm[b][k * kUp0Y + ty] >> tx & 1u) {
+                        float v = h ? PB + a2B : PA + a2A;
+                        if (cin.a) {
+                            const float* px = h ? pxB : pxA;
+                            v += 0.75f * px[lz] + 0.25f * px[lz + sz];
+                        }
+                        z[n] = v;
+                        f_zr += v * T[((k + 1) * kUp0HY + ty + 1) * kUp0HX + tx + 1];
+                        f_zq += v * qs[b][k][ty * kUp0X + tx];
+                    } else {
+                        z[n] = 0.f;
                     }
-                    z[n] = v;
-                    f_zr += v * T[((k + 1) * kUp0HY + ty + 1) * kUp0HX + tx + 1];
-                    f_zq += v * qs[b][k][tid];
-                } else {
-                    z[n] = 0.f;
                 }
             }
-            P = Q + a1;
-            Q = a0;
+            PA = QA + a1A;
+            QA = a0A;
+            PB = QB + a1B;
+            QB = a0B;
         }
     }
     if (out) {
@@ -909,7 +939,7 @@ static void launch_up0(const GridDev& g, LView r0, LView cin, float* z, const ui
             cudaFuncSetAttribute(k_lp_up0_pipe, cudaFuncAttributeMaxDynamicSharedMemorySize, kUp0DynSmem);
             dyn_set = dev;
         }
-        k_lp_up0_pipe<<<(unsigned)ctas, kUp0X * kUp0Y, kUp0DynSmem, s>>>(g, r0, cin, z, kind, S0, q, gpart, gstride,
+        k_lp_up0_pipe<<<(unsigned)ctas, kUp0Threads, kUp0DynSmem, s>>>(g, r0, cin, z, kind, S0, q, gpart, gstride,
                                                                           ticket, out, flag, bx_n, by_n, (int)tiles);
     } else {
         k_lp_up0<<<node_blocks(g.nv), kNodeThreads, 0, s>>>(g, r0, cin, z, kind, S0, q, gpart, gstride, ticket, out,
