@@ -1414,23 +1414,33 @@ void launch_load_uniform(const GridDev& g, SpeciesDev sp, const LoadArgs& la, cu
 // FP64 conservation sums (Species::getMicroCount / getMomentum / getKE, Species.cpp:732-752)
 // out[0] sum w, out[1..3] sum w v, out[4] sum w v.v   (per-block partials reduced on host side)
 // ------------------------------------------------------------------------------------
+// compensated FP32 accumulation: hi += x by TwoSum, its rounding error and the exact error ex of
+// the term collected in lo
+__device__ __forceinline__ void comp_add(float& hi, float& lo, float x, float ex) {
+    const FF s = two_sum(hi, x);
+    hi = s.hi;
+    lo += s.lo + ex;
+}
 __global__ void k_sums(SpeciesDev sp, double* part) {
     int n = sp.counts[0];
-    // per-thread sums in float-float (exact products of the FP32 values, about 48 bits), FP64
-    // only for the per-thread totals and the block sums
-    FF a[5] = {FF{0.f, 0.f}, FF{0.f, 0.f}, FF{0.f, 0.f}, FF{0.f, 0.f}, FF{0.f, 0.f}};
+    // per-thread compensated sums of w, w v (exact products) and w |v|^2 (|v|^2 rounded once, as
+    // the FP32 velocities it comes from; the exact product with w), FP64 only for the per-thread
+    // totals and the block sums: the totals do not depend on the particle order beyond ~1e-14
+    float h[5] = {0.f, 0.f, 0.f, 0.f, 0.f}, l[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll 4
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
         const float4 v = sp.vel[p];
-        a[0] = ff_add_f(a[0], v.w);
-        a[1] = ff_add(a[1], two_prod(v.w, v.x));
-        a[2] = ff_add(a[2], two_prod(v.w, v.y));
-        a[3] = ff_add(a[3], two_prod(v.w, v.z));
-        FF v2 = ff_add(ff_add(two_prod(v.x, v.x), two_prod(v.y, v.y)), two_prod(v.z, v.z));
-        a[4] = ff_add(a[4], ff_mul(v2, FF{v.w, 0.f}));
+        comp_add(h[0], l[0], v.w, 0.f);
+        const FF px = two_prod(v.w, v.x), py = two_prod(v.w, v.y), pz = two_prod(v.w, v.z);
+        comp_add(h[1], l[1], px.hi, px.lo);
+        comp_add(h[2], l[2], py.hi, py.lo);
+        comp_add(h[3], l[3], pz.hi, pz.lo);
+        const FF ke = two_prod(v.w, fmaf(v.z, v.z, fmaf(v.y, v.y, v.x * v.x)));
+        comp_add(h[4], l[4], ke.hi, ke.lo);
     }
     __shared__ double s[5][8];
     for (int c = 0; c < 5; c++) {
-        double x = (double)a[c].hi + (double)a[c].lo;
+        double x = (double)h[c] + (double)l[c];
         for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
         if ((threadIdx.x & 31) == 0) s[c][threadIdx.x >> 5] = x;
     }
