@@ -482,7 +482,10 @@ __device__ __forceinline__ void stage_tile(float* __restrict__ dst, const float*
 
 // coarse tile of the prolongation for a 32 x 8 x 8 fine tile: coarse x0/2-1 .. x0/2+16 etc.
 constexpr int kPcX = kUp0X / 2 + 2, kPcY = kUp0Y / 2 + 2, kPcZ = kUp0Z / 2 + 2;
-constexpr int kUp0Tile = kUp0HX * kUp0HY * kUp0HZ, kPcTile = kPcX * kPcY * kPcZ;
+// a staged residual row: slot 3 holds x0 - 1, slots 4 .. 35 x0 .. x0 + 31 (16-byte aligned), slot 36
+// x0 + 32; the row pitch keeps every row's body 16-byte aligned
+constexpr int kUp0P = 40, kUp0O = 3;
+constexpr int kUp0Tile = kUp0P * kUp0HY * kUp0HZ, kPcTile = kPcX * kPcY * kPcZ;
 constexpr int kUp0CtasPerSM = 4;
 constexpr int kUp0DynSmem = 4 * 2 * (kUp0Tile + kPcTile + kUp0Z * kUp0X * kUp0Y + kUp0Z * kUp0Y);
 
@@ -490,6 +493,11 @@ constexpr int kUp0DynSmem = 4 * 2 * (kUp0Tile + kPcTile + kUp0Z * kUp0X * kUp0Y 
 // shared word is zero-filled (src-size 0; src is then any valid address)
 __device__ __forceinline__ void cp_async_f32(float* dst, const float* src, bool ok) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(tc_smem_u32(dst)), "l"(src), "r"(ok ? 4 : 0)
+                 : "memory");
+}
+// the same for 16 bytes (both addresses 16-byte aligned)
+__device__ __forceinline__ void cp_async_16(float* dst, const float* src, bool ok) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(tc_smem_u32(dst)), "l"(src), "r"(ok ? 16 : 0)
                  : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
@@ -500,7 +508,8 @@ __device__ __forceinline__ void cp_async_wait() {
 
 // The fine level z = mask (S0 * r + P e_1), z.r and z.q, on 32 x 8 x 8 tiles of nodes by
 // persistent CTAs that pipeline the tiles: while a CTA computes one tile from shared memory, the
-// residual tile of its next tile (34 x 10 x 10 with the one-node halo, view neighbour rules:
+// residual tile of its next tile (34 x 10 x 10 with the one-node halo, rows at a 40-float pitch
+// with 16-byte aligned bodies, view neighbour rules:
 // wrapped on periodic axes, zero outside) and the coarse tile of the prolongation (18 x 6 x 6) are
 // already on their way into the other buffer through cp.async, which needs no registers.  A thread
 // owns the columns of two adjacent output rows (2p and 2p + 1 of the tile): it walks the ten tile
@@ -550,18 +559,40 @@ __global__ void __launch_bounds__(kUp0Threads, kUp0CtasPerSM)
             }
         }
         __syncthreads();
-        // a warp copies whole rows: lane l the row's point l (lanes 0, 1 also 32, 33), so the
-        // x offsets stay in registers and each row costs one shared read of its y/z offset
         const int lane = tid & 31, wp = tid >> 5;
-        const int ox0 = mx[lane], ox1 = lane < kUp0HX - 32 ? mx[32 + lane] : -1;
-        for (int row = wp; row < kUp0HY * kUp0HZ; row += kWarps) {
-            const int oyz = myz[row];
-            float* dst = &t[b][row * kUp0HX];
-            const bool ok0 = ox0 >= 0 && oyz >= 0;
-            cp_async_f32(dst + lane, ok0 ? rin.a + ox0 + oyz : rin.a, ok0);
-            if (lane < kUp0HX - 32) {
-                const bool ok1 = ox1 >= 0 && oyz >= 0;
-                cp_async_f32(dst + 32 + lane, ok1 ? rin.a + ox1 + oyz : rin.a, ok1);
+        // rows whose 32 body points are inside the box on aligned offsets go as eight 16-byte
+        // copies and two halo words, three rows per warp step (lanes 10 s .. 10 s + 9 row s: slots
+        // 0-7 the body chunks, 8 the left and 9 the right halo); other tiles point by point
+        if (x0 + kUp0X <= rin.n[0] && ((rin.sy | rin.sz) & 3) == 0 &&
+            (reinterpret_cast<uintptr_t>(rin.a) & 15) == 0) {
+            const int u = lane % 10, sub = lane / 10;
+            const int hxo = u == 8 ? mx[0] : (u == 9 ? mx[kUp0HX - 1] : -1);
+            for (int row0 = 3 * wp; row0 < kUp0HY * kUp0HZ; row0 += 3 * kWarps) {
+                const int row = row0 + sub;
+                if (sub < 3 && row < kUp0HY * kUp0HZ) {
+                    const int oyz = myz[row];
+                    float* dst = &t[b][row * kUp0P];
+                    if (u < 8) {
+                        cp_async_16(dst + kUp0O + 1 + 4 * u, oyz >= 0 ? rin.a + oyz + x0 + 4 * u : rin.a, oyz >= 0);
+                    } else {
+                        const bool ok = hxo >= 0 && oyz >= 0;
+                        cp_async_f32(dst + (u == 8 ? kUp0O : kUp0O + kUp0HX - 1), ok ? rin.a + hxo + oyz : rin.a, ok);
+                    }
+                }
+            }
+        } else {
+            // lane l the row's point l (lanes 0, 1 also 32, 33): the x offsets stay in registers and
+            // each row costs one shared read of its y/z offset
+            const int ox0 = mx[lane], ox1 = lane < kUp0HX - 32 ? mx[32 + lane] : -1;
+            for (int row = wp; row < kUp0HY * kUp0HZ; row += kWarps) {
+                const int oyz = myz[row];
+                float* dst = &t[b][row * kUp0P + kUp0O];
+                const bool ok0 = ox0 >= 0 && oyz >= 0;
+                cp_async_f32(dst + lane, ok0 ? rin.a + ox0 + oyz : rin.a, ok0);
+                if (lane < kUp0HX - 32) {
+                    const bool ok1 = ox1 >= 0 && oyz >= 0;
+                    cp_async_f32(dst + 32 + lane, ok1 ? rin.a + ox1 + oyz : rin.a, ok1);
+                }
             }
         }
         if (cin.a) {
@@ -575,17 +606,28 @@ __global__ void __launch_bounds__(kUp0Threads, kUp0CtasPerSM)
             }
         }
         {
-            // this thread's outputs: q, and the FREE word of each output row (zero outside the grid)
-            const int x = x0 + tx;
+            // q at the tile's outputs (16-byte copies of whole 32-point row segments when aligned),
+            // and the FREE word of each output row (zero outside the grid)
+            if (q && x0 + kUp0X <= g.ni && (g.ni & 3) == 0 && (reinterpret_cast<uintptr_t>(q) & 15) == 0) {
 #pragma unroll
-            for (int h = 0; h < 2; h++) {
-                const int ty = ty0 + h, y = y0 + ty;
-                const bool col = x < g.ni && y < g.nj;
+                for (int j = 0; j < kUp0Z * kUp0Y * kUp0X / 4 / kUp0Threads; j++) {
+                    const int c = tid + j * kUp0Threads, seg = c / (kUp0X / 4), u = c % (kUp0X / 4);
+                    const int k = seg / kUp0Y, ty = seg % kUp0Y, y = y0 + ty, zz = z0 + k;
+                    const bool ok = y < g.nj && zz < g.nk;
+                    cp_async_16(&qs[b][k][ty * kUp0X + 4 * u], ok ? q + (x0 + 4 * u + y * g.ni + zz * g.ni * g.nj) : q, ok);
+                }
+            } else {
+                const int x = x0 + tx;
 #pragma unroll
-                for (int k = 0; k < kUp0Z; k++) {
-                    const int zz = z0 + k;
-                    const bool ok = q && col && zz < g.nk;
-                    cp_async_f32(&qs[b][k][ty * kUp0X + tx], ok ? q + (x + y * g.ni + zz * g.ni * g.nj) : rin.a, ok);
+                for (int h = 0; h < 2; h++) {
+                    const int ty = ty0 + h, y = y0 + ty;
+                    const bool col = x < g.ni && y < g.nj;
+#pragma unroll
+                    for (int k = 0; k < kUp0Z; k++) {
+                        const int zz = z0 + k;
+                        const bool ok = q && col && zz < g.nk;
+                        cp_async_f32(&qs[b][k][ty * kUp0X + tx], ok ? q + (x + y * g.ni + zz * g.ni * g.nj) : rin.a, ok);
+                    }
                 }
             }
             if (tid < kUp0Z * kUp0Y) {
@@ -648,7 +690,7 @@ __global__ void __launch_bounds__(kUp0Threads, kUp0CtasPerSM)
 #pragma unroll
             for (int dy = 0; dy < 4; dy++)
 #pragma unroll
-                for (int dx = 0; dx < 3; dx++) rr[dy][dx] = T[(hz * kUp0HY + ty0 + dy) * kUp0HX + tx + dx];
+                for (int dx = 0; dx < 3; dx++) rr[dy][dx] = T[(hz * kUp0HY + ty0 + dy) * kUp0P + kUp0O + tx + dx];
             float a0A = 0.f, a1A = 0.f, a2A = 0.f, a0B = 0.f, a1B = 0.f, a2B = 0.f;
 #pragma unroll
             for (int dy = 0; dy < 3; dy++)
@@ -678,7 +720,7 @@ __global__ void __launch_bounds__(kUp0Threads, kUp0CtasPerSM)
                             v += 0.75f * px[lz] + 0.25f * px[lz + sz];
                         }
                         z[n] = v;
-                        f_zr += v * T[((k + 1) * kUp0HY + ty + 1) * kUp0HX + tx + 1];
+                        f_zr += v * T[((k + 1) * kUp0HY + ty + 1) * kUp0P + kUp0O + tx + 1];
                         f_zq += v * qs[b][k][ty * kUp0X + tx];
                     } else {
                         z[n] = 0.f;
