@@ -7,6 +7,7 @@
 // the level's own extent), other axes read zero outside the box.
 #include <algorithm>
 #include <cmath>
+#include <type_traits>
 #include <vector>
 #include <cuda_bf16.h>
 #include <cstring>
@@ -804,10 +805,12 @@ __global__ void __launch_bounds__(kNetX * kNetY, 2) k_lp_up_net_tiled(LView zin,
         }
     }
     // rolling window: w[j] collects output plane hz - 4 + j; tile plane hz is offset dz - 2 of
-    // output plane hz - dz, i.e. w[4 - dz]
+    // output plane hz - dz, i.e. w[4 - dz].  Only the taps whose output plane lies in the tile are
+    // formed: dz from max(0, hz - 7) to min(4, hz) (40 of the 60 plane-tap pairs), with the ranges
+    // of the four first and four last planes fixed at compile time
     float w[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
-#pragma unroll 1
-    for (int hz = 0; hz < kNetHZ; hz++) {
+    auto plane = [&](auto d0c, auto d1c, int hz) {
+        constexpr int d0 = decltype(d0c)::value, d1 = decltype(d1c)::value;
         float a[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
         float win[25];  // the plane's 5 x 5 window, loaded once
 #pragma unroll
@@ -817,9 +820,9 @@ __global__ void __launch_bounds__(kNetX * kNetY, 2) k_lp_up_net_tiled(LView zin,
 #pragma unroll
         for (int m = 0; m < 25; m++)
 #pragma unroll
-            for (int dz = 0; dz < 5; dz++) a[dz] = fmaf(K5p.k[25 * dz + m], win[m], a[dz]);
+            for (int dz = d0; dz <= d1; dz++) a[dz] = fmaf(K5p.k[25 * dz + m], win[m], a[dz]);
 #pragma unroll
-        for (int dz = 0; dz < 5; dz++) w[4 - dz] += a[dz];
+        for (int dz = d0; dz <= d1; dz++) w[4 - dz] += a[dz];
         const int k = hz - 4;  // output plane z0 + k is complete
         if (k >= 0 && col && z0 + k < out.n[2]) {
             const int c[3] = {x, y, z0 + k};
@@ -847,7 +850,20 @@ __global__ void __launch_bounds__(kNetX * kNetY, 2) k_lp_up_net_tiled(LView zin,
 #pragma unroll
         for (int j2 = 0; j2 < 4; j2++) w[j2] = w[j2 + 1];
         w[4] = 0.f;
-    }
+    };
+    using I0 = std::integral_constant<int, 0>;
+    using I4 = std::integral_constant<int, 4>;
+    static_assert(kNetHZ == 12 && kNetZ == 8, "the tap ranges below follow the 8-plane tile");
+    plane(I0{}, I0{}, 0);
+    plane(I0{}, std::integral_constant<int, 1>{}, 1);
+    plane(I0{}, std::integral_constant<int, 2>{}, 2);
+    plane(I0{}, std::integral_constant<int, 3>{}, 3);
+#pragma unroll 1
+    for (int hz = 4; hz < 8; hz++) plane(I0{}, I4{}, hz);
+    plane(std::integral_constant<int, 1>{}, I4{}, 8);
+    plane(std::integral_constant<int, 2>{}, I4{}, 9);
+    plane(std::integral_constant<int, 3>{}, I4{}, 10);
+    plane(I4{}, I4{}, 11);
 }
 
 // index rule of the restriction along one axis (k_lp_restrict): fine point raw of coarse level c,
