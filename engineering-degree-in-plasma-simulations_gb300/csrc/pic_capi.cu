@@ -158,6 +158,7 @@ struct pic_world {
     int stop_rule = PIC_STOP_REL_RHS;
     int warm_mode = PIC_WARM_PREVIOUS;  // start of a warm solve (PIC_WARM_*)
     int warm_jacobi = 16;  // Jacobi-PCG iterations a warm solve of the learned method runs first
+    int lp_hint = 0;       // iterations of the last converged first learned inner solve (0: none)
     float* dphi = nullptr;  // the last solve's total change of phi (FP32), for PIC_WARM_EXTRAPOLATE
     bool dphi_valid = false;  // dphi holds the change of one warm solve
     double last_norms[3] = {0, 0, 0};  // |r|, |b|, |rho/eps0| of the last solve's final residual
@@ -1578,8 +1579,10 @@ constexpr int kLearnedInnerCap = 400;  // iterations of one learned inner solve 
 constexpr double kInnerTarget = 0.64;
 
 // FP32 flexible CG with the learned preconditioner on L e = r (w->r), e from zero, until
-// r.r <= target or cap iterations; *done = iterations, *conv = reached the target
-int learned_inner(pic_world* w, SolveWork& sw, double target, int cap, int* done, bool* conv) {
+// r.r <= target or cap iterations; *done = iterations, *conv = reached the target.  Iterations go
+// out in batches between which the host reads the stop flag (the iterations of a batch after the
+// stop return at once): first_batch, then 2, 4, 8, 8, ...
+int learned_inner(pic_world* w, SolveWork& sw, double target, int cap, int first_batch, int* done, bool* conv) {
     {
         Scope sc(w, "poisson", 4 + 2 * w->lp->nlev);
         launch_lpcg_init(w->g, sw, *w->lp, w->stream, w->sms);
@@ -1589,8 +1592,8 @@ int learned_inner(pic_world* w, SolveWork& sw, double target, int cap, int* done
     int it = 0;
     *done = 0;
     *conv = false;
-    while (it < cap) {
-        int batch = std::min(4, cap - it);
+    for (int nb = 0; it < cap; nb++) {
+        int batch = std::min(nb == 0 ? std::max(1, first_batch) : std::min(8, 1 << nb), cap - it);
         {
             Scope sc(w, "poisson", (1 + 2 * w->lp->nlev) * batch);
             for (int b = 0; b < batch; b++) {
@@ -1621,7 +1624,7 @@ int learned_validation_iters(pic_world* w, const float* r, int cap, int* iters) 
     CU(cudaStreamSynchronize(w->stream));
     SolveWork sw = solve_work(w);
     bool conv = false;
-    int rc = learned_inner(w, sw, 1e-12 * w->h_scal[0], cap, iters, &conv);
+    int rc = learned_inner(w, sw, 1e-12 * w->h_scal[0], cap, 4, iters, &conv);
     if (!conv) *iters = cap;
     return rc;
 }
@@ -1635,6 +1638,7 @@ int solve_impl(pic_world* w, int* iters_out, double* rel_out) {
     bool estimated = w->rhs_valid;
     const bool warm = estimated;  // phi unchanged since the last solve: a warm start
     bool use_pcg = false;  // set when the learned preconditioner stalls in this solve
+    bool first_learned = true;  // no learned inner solve in this solve yet
     // extrapolated warm start: phi += (phi_n-1 - phi_n-2), the last warm solve's whole change,
     // then a full float-float residual of the extrapolated potential
     const bool extrapolate = warm && w->warm_mode == PIC_WARM_EXTRAPOLATE && w->dphi_valid;
@@ -1699,8 +1703,14 @@ int solve_impl(pic_world* w, int* iters_out, double* rel_out) {
             double target = std::max(1e-6 * r2, kInnerTarget * w->tol * w->tol * bn * bn);
             int done = 0;
             bool conv = false;
-            rc = learned_inner(w, sw, target, std::min(kLearnedInnerCap, w->max_it - iters), &done, &conv);
+            // the first inner solve of a solve sized from the last one: consecutive warm solves of a
+            // run need about the same count N, and iteration N is the one that finds the first N
+            // converged, so the first batch runs N + 1 iterations
+            const int first_batch = first_learned && w->lp_hint > 0 ? w->lp_hint + 1 : 4;
+            rc = learned_inner(w, sw, target, std::min(kLearnedInnerCap, w->max_it - iters), first_batch, &done, &conv);
             if (rc) return rc;
+            if (first_learned && conv) w->lp_hint = done;
+            first_learned = false;
             iters += done;
             if (!conv) {
                 use_pcg = true;
