@@ -278,7 +278,9 @@ __device__ __forceinline__ void row_neighbours(const GridDev& g, int j, int k, i
 // Four consecutive nodes of one row per thread and iteration.  When rows are a multiple of four
 // nodes and the group does not touch the row ends, the group and its y / z neighbour rows are read
 // with 16-byte loads and the two x neighbours with scalar loads; other groups go node by node.
-__global__ void __launch_bounds__(256) k_residual(GridDev g, const float2* __restrict__ phi_in,
+// Capped at 80 registers (three CTAs per SM; a few bytes spill): measured faster than two CTAs at
+// 116 registers or four at 64.
+__global__ void __launch_bounds__(256, 3) k_residual(GridDev g, const float2* __restrict__ phi_in,
                                                   float2* __restrict__ phi_out, const float* __restrict__ e,
                                                   const float* __restrict__ rho, const uint16_t* __restrict__ kind,
                                                   float* __restrict__ r, double* gpart, int gstride, unsigned* ticket,
