@@ -982,6 +982,51 @@ __global__ void __launch_bounds__(32 * kRmWarps, 4) k_lp_restrict_march(LView f,
             if (cy0 + cy < c.n[1] && cz0 + cz < c.n[2]) c.a[lv_off(c, cx, cy0 + cy, cz0 + cz)] = acc[cz][cy];
 }
 
+// z_coarse = R z_fine on 3-D tiles of 16 x 8 x 4 coarse voxels: the 34 x 18 x 10 fine points they
+// read are staged in shared memory first (the same index rules as k_lp_restrict).  For the mid-size
+// levels: with fewer than ~10^6 coarse voxels the marching kernel has too few warps for its chains
+// of planes.
+constexpr int kRsX = 16, kRsY = 8, kRsZ = 4;
+constexpr int kRsHX = 2 * kRsX + 2, kRsHY = 2 * kRsY + 2, kRsHZ = 2 * kRsZ + 2;
+__global__ void __launch_bounds__(256) k_lp_restrict_tiled(LView f, LView c, const int* flag, int bx_n, int by_n) {
+    if (flag && flag[0]) return;
+    __shared__ float t[kRsHZ][kRsHY][kRsHX];
+    __shared__ int mx[kRsHX], myz[kRsHY * kRsHZ];  // fine offsets per axis (-1: outside)
+    int b = blockIdx.x;
+    const int bx = b % bx_n;
+    b /= bx_n;
+    const int by = b % by_n, bz = b / by_n;
+    const int cx0 = bx * kRsX, cy0 = by * kRsY, cz0 = bz * kRsZ;
+    const int tid = threadIdx.x;
+    if (tid < kRsHX) mx[tid] = rs_map(2 * cx0 - 1 + tid, f, c, 0);
+    if (tid < kRsHY * kRsHZ) {
+        const int uy = rs_map(2 * cy0 - 1 + tid % kRsHY, f, c, 1);
+        const int uz = rs_map(2 * cz0 - 1 + tid / kRsHY, f, c, 2);
+        myz[tid] = (uy < 0 || uz < 0) ? -1 : uy * f.sy + uz * f.sz;
+    }
+    __syncthreads();
+    stage_tile<kRsHX, kRsHY * kRsHZ, 256>(&t[0][0][0], f.a, mx, myz);
+    __syncthreads();
+    const float w4[4] = {0.25f, 0.75f, 0.75f, 0.25f};
+    for (int o = threadIdx.x; o < kRsX * kRsY * kRsZ; o += 256) {
+        const int ox = o % kRsX, oy = (o / kRsX) % kRsY, oz = o / (kRsX * kRsY);
+        const int cx = cx0 + ox, cy = cy0 + oy, cz = cz0 + oz;
+        if (cx >= c.n[0] || cy >= c.n[1] || cz >= c.n[2]) continue;
+        float acc = 0.f;
+#pragma unroll
+        for (int kz = 0; kz < 4; kz++) {
+            float az = 0.f;
+#pragma unroll
+            for (int ky = 0; ky < 4; ky++) {
+                const float* row = &t[2 * oz + kz][2 * oy + ky][2 * ox];
+                az += w4[ky] * (w4[0] * row[0] + w4[1] * row[1] + w4[2] * row[2] + w4[3] * row[3]);
+            }
+            acc += w4[kz] * az;
+        }
+        c.a[lv_off(c, cx, cy, cz)] = acc;
+    }
+}
+
 // z = B r on the finest level: the tiled kernel when its CTAs fit the reduction's partial slots
 static void launch_up0(const GridDev& g, LView r0, LView cin, float* z, const uint16_t* kind, const float* S0,
                        const float* q, double* gpart, int gstride, unsigned* ticket, double* out, const int* flag,
@@ -1010,11 +1055,22 @@ static int lp_blocks(int nvox, int sms) {
     (void)sms;
     return std::max(1, (nvox + 255) / 256);
 }
+// per level the fastest of three forms (ncu launch lists of the large discharge): the marching
+// kernel from 2^20 coarse voxels (level 1: 45 against 62 us for the tiled one), the tiled kernel
+// from 32^3 (levels 2-3: 12 and 5 us against 14-15 us marching), one thread per voxel below
 static void launch_restrict(const LView& f, const LView& c, const int* flag, cudaStream_t s, int sms) {
-    (void)sms;
-    const int bx_n = (c.n[0] + kRmX - 1) / kRmX, by_n = (c.n[1] + kRmY - 1) / kRmY;
-    const int nwarps = bx_n * by_n * ((c.n[2] + kRmZ - 1) / kRmZ);
-    k_lp_restrict_march<<<(nwarps + kRmWarps - 1) / kRmWarps, 32 * kRmWarps, 0, s>>>(f, c, flag, bx_n, by_n, nwarps);
+    if (c.nvox >= (1 << 20)) {
+        const int bx_n = (c.n[0] + kRmX - 1) / kRmX, by_n = (c.n[1] + kRmY - 1) / kRmY;
+        const int nwarps = bx_n * by_n * ((c.n[2] + kRmZ - 1) / kRmZ);
+        k_lp_restrict_march<<<(nwarps + kRmWarps - 1) / kRmWarps, 32 * kRmWarps, 0, s>>>(f, c, flag, bx_n, by_n,
+                                                                                         nwarps);
+    } else if (c.nvox >= 32 * 32 * 32) {
+        const int bx_n = (c.n[0] + kRsX - 1) / kRsX, by_n = (c.n[1] + kRsY - 1) / kRsY;
+        const int blocks = bx_n * by_n * ((c.n[2] + kRsZ - 1) / kRsZ);
+        k_lp_restrict_tiled<<<blocks, 256, 0, s>>>(f, c, flag, bx_n, by_n);
+    } else {
+        k_lp_restrict<<<lp_blocks(c.nvox, sms), 256, 0, s>>>(f, c, flag);
+    }
 }
 
 void launch_lp_apply(const GridDev& g, const LpState& L, const float* r, float* z, const uint16_t* kind,
