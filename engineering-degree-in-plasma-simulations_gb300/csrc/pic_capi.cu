@@ -1581,7 +1581,7 @@ constexpr double kInnerTarget = 0.64;
 // FP32 flexible CG with the learned preconditioner on L e = r (w->r), e from zero, until
 // r.r <= target or cap iterations; *done = iterations, *conv = reached the target.  Iterations go
 // out in batches between which the host reads the stop flag (the iterations of a batch after the
-// stop return at once): first_batch, then 2, 4, 8, 8, ...
+// stop return at once, about 30 us each at 256^3): first_batch, then 2, 4, 4, ...
 int learned_inner(pic_world* w, SolveWork& sw, double target, int cap, int first_batch, int* done, bool* conv) {
     {
         Scope sc(w, "poisson", 4 + 2 * w->lp->nlev);
@@ -1593,7 +1593,7 @@ int learned_inner(pic_world* w, SolveWork& sw, double target, int cap, int first
     *done = 0;
     *conv = false;
     for (int nb = 0; it < cap; nb++) {
-        int batch = std::min(nb == 0 ? std::max(1, first_batch) : std::min(8, 1 << nb), cap - it);
+        int batch = std::min(nb == 0 ? std::max(1, first_batch) : std::min(4, 1 << nb), cap - it);
         {
             Scope sc(w, "poisson", (1 + 2 * w->lp->nlev) * batch);
             for (int b = 0; b < batch; b++) {

@@ -513,12 +513,14 @@ __device__ __forceinline__ void cp_async_wait() {
 // with 16-byte aligned bodies, view neighbour rules:
 // wrapped on periodic axes, zero outside) and the coarse tile of the prolongation (18 x 6 x 6) are
 // already on their way into the other buffer through cp.async, which needs no registers.  A thread
-// owns the columns of two adjacent output rows (2p and 2p + 1 of the tile): it walks the ten tile
-// planes, reads the plane's four rows around them once (12 shared reads), forms each row's three
-// 3 x 3 partial sums with the 27 weights held in registers (54 FMAs) and rolls them into the
-// outputs of planes p+1, p, p-1.
-constexpr int kUp0Threads = kUp0X * kUp0Y / 2;
-__global__ void __launch_bounds__(kUp0Threads, kUp0CtasPerSM)
+// owns the columns of R adjacent output rows (R p .. R p + R - 1 of the tile): it walks the ten tile
+// planes, reads the plane's R + 2 rows around them once, forms each row's three 3 x 3 partial sums
+// and rolls them into the outputs of planes p+1, p, p-1.  R = 2 (128 threads, the 27 weights in
+// registers: 12 shared reads per plane for two rows instead of 18) for grids with at least four
+// tiles per persistent CTA; R = 1 (256 threads, weights read from shared memory within 64
+// registers) below that, where eight warps per tile hide more of a tile's latency.
+template <int R>
+__global__ void __launch_bounds__(kUp0X * kUp0Y / R, kUp0CtasPerSM)
     k_lp_up0_pipe(GridDev g, LView rin, LView cin, float* __restrict__ z, const uint16_t* __restrict__ kind,
                   const float* __restrict__ S0, const float* __restrict__ q, double* gpart, int gstride,
                   unsigned* ticket, double* out, const int* flag, int bx_n, int by_n, int ntiles) {
@@ -534,9 +536,10 @@ __global__ void __launch_bounds__(kUp0Threads, kUp0CtasPerSM)
     float(*qs)[kUp0Z][kUp0X * kUp0Y] = reinterpret_cast<float(*)[kUp0Z][kUp0X * kUp0Y]>(up0_dyn + 2 * (kUp0Tile + kPcTile));
     unsigned(*fm)[kUp0Z * kUp0Y] =
         reinterpret_cast<unsigned(*)[kUp0Z * kUp0Y]>(up0_dyn + 2 * (kUp0Tile + kPcTile + kUp0Z * kUp0X * kUp0Y));
+    constexpr int kThr = kUp0X * kUp0Y / R;
     const int tid = threadIdx.x;
-    const int tx = tid % kUp0X, ty0 = 2 * (tid / kUp0X);  // rows ty0 and ty0 + 1 of the tile
-    constexpr int kWarps = kUp0Threads / 32;
+    const int tx = tid % kUp0X, ty0 = R * (tid / kUp0X);  // rows ty0 .. ty0 + R - 1 of the tile
+    constexpr int kWarps = kThr / 32;
     if (tid < 27) S[tid] = S0[tid];
     // the halo maps of a tile, a barrier, then its copies into buffer b as one commit group
     auto issue = [&](int tile, int b) {
@@ -611,8 +614,8 @@ __global__ void __launch_bounds__(kUp0Threads, kUp0CtasPerSM)
             // and the FREE word of each output row (zero outside the grid)
             if (q && x0 + kUp0X <= g.ni && (g.ni & 3) == 0 && (reinterpret_cast<uintptr_t>(q) & 15) == 0) {
 #pragma unroll
-                for (int j = 0; j < kUp0Z * kUp0Y * kUp0X / 4 / kUp0Threads; j++) {
-                    const int c = tid + j * kUp0Threads, seg = c / (kUp0X / 4), u = c % (kUp0X / 4);
+                for (int j = 0; j < kUp0Z * kUp0Y * kUp0X / 4 / kThr; j++) {
+                    const int c = tid + j * kThr, seg = c / (kUp0X / 4), u = c % (kUp0X / 4);
                     const int k = seg / kUp0Y, ty = seg % kUp0Y, y = y0 + ty, zz = z0 + k;
                     const bool ok = y < g.nj && zz < g.nk;
                     cp_async_16(&qs[b][k][ty * kUp0X + 4 * u], ok ? q + (x0 + 4 * u + y * g.ni + zz * g.ni * g.nj) : q, ok);
@@ -620,7 +623,7 @@ __global__ void __launch_bounds__(kUp0Threads, kUp0CtasPerSM)
             } else {
                 const int x = x0 + tx;
 #pragma unroll
-                for (int h = 0; h < 2; h++) {
+                for (int h = 0; h < R; h++) {
                     const int ty = ty0 + h, y = y0 + ty;
                     const bool col = x < g.ni && y < g.nj;
 #pragma unroll
@@ -644,7 +647,7 @@ __global__ void __launch_bounds__(kUp0Threads, kUp0CtasPerSM)
     };
     int tile = blockIdx.x;
     if (tile < ntiles) issue(tile, 0);  // its barrier also publishes S
-    float w[27];
+    float w[27];  // R = 2 only (unused and removed for R = 1)
 #pragma unroll
     for (int m = 0; m < 27; m++) w[m] = S[m];
     float f_zr = 0.f, f_zq = 0.f;
@@ -658,7 +661,9 @@ __global__ void __launch_bounds__(kUp0Threads, kUp0CtasPerSM)
         const int by = bb % by_n, bz = bb / by_n;
         const int x0 = bx * kUp0X, y0 = by * kUp0Y, z0 = bz * kUp0Z;
         const int x = x0 + tx;
-        const bool colA = x < g.ni && y0 + ty0 < g.nj, colB = x < g.ni && y0 + ty0 + 1 < g.nj;
+        bool colr[R];
+#pragma unroll
+        for (int h = 0; h < R; h++) colr[h] = x < g.ni && y0 + ty0 + h < g.nj;
         if (next < ntiles)
             cp_async_wait<1>();
         else
@@ -667,59 +672,65 @@ __global__ void __launch_bounds__(kUp0Threads, kUp0CtasPerSM)
         const float* T = t[b];
         const float* PC = pc[b];
         // prolongation weights (0.75 own coarse point, 0.25 the neighbour on the parity side): the
-        // x-y interpolation of the six coarse planes for both rows (even row: the coarse row
-        // below, odd row: the one above; both over the same coarse row ly), then per output plane
-        // the two planes on its parity side
-        float pxA[kPcZ], pxB[kPcZ];
+        // x-y interpolation of the six coarse planes for each row (an even row takes the coarse
+        // row below, an odd row the one above), then per output plane the two planes on its parity
+        // side
+        float px[R][kPcZ];
         if (cin.a) {
-            const int lx = (x >> 1) - (x0 / 2 - 1), ly = ty0 / 2 + 1;
+            const int lx = (x >> 1) - (x0 / 2 - 1);
             const int sx = (x & 1) ? 1 : -1;
 #pragma unroll
-            for (int cz = 0; cz < kPcZ; cz++) {
-                auto C = [&](int cy, int cx) { return PC[(cz * kPcY + cy) * kPcX + cx]; };
-                const float a0 = 0.75f * C(ly, lx) + 0.25f * C(ly, lx + sx);
-                const float am = 0.75f * C(ly - 1, lx) + 0.25f * C(ly - 1, lx + sx);
-                const float ap = 0.75f * C(ly + 1, lx) + 0.25f * C(ly + 1, lx + sx);
-                pxA[cz] = 0.75f * a0 + 0.25f * am;
-                pxB[cz] = 0.75f * a0 + 0.25f * ap;
+            for (int h = 0; h < R; h++) {
+                const int ty = ty0 + h, ly = ty / 2 + 1, sy = (ty & 1) ? 1 : -1;  // y0 is even
+#pragma unroll
+                for (int cz = 0; cz < kPcZ; cz++) {
+                    auto C = [&](int cy, int cx) { return PC[(cz * kPcY + cy) * kPcX + cx]; };
+                    const float a0 = 0.75f * C(ly, lx) + 0.25f * C(ly, lx + sx);
+                    const float a1 = 0.75f * C(ly + sy, lx) + 0.25f * C(ly + sy, lx + sx);
+                    px[h][cz] = 0.75f * a0 + 0.25f * a1;
+                }
             }
         }
-        float PA = 0.f, QA = 0.f, PB = 0.f, QB = 0.f;
+        float Pr[R], Qr[R];
+#pragma unroll
+        for (int h = 0; h < R; h++) Pr[h] = Qr[h] = 0.f;
 #pragma unroll
         for (int hz = 0; hz < kUp0HZ; hz++) {
-            float rr[4][3];
+            float rr[R + 2][3];
 #pragma unroll
-            for (int dy = 0; dy < 4; dy++)
+            for (int dy = 0; dy < R + 2; dy++)
 #pragma unroll
                 for (int dx = 0; dx < 3; dx++) rr[dy][dx] = T[(hz * kUp0HY + ty0 + dy) * kUp0P + kUp0O + tx + dx];
-            float a0A = 0.f, a1A = 0.f, a2A = 0.f, a0B = 0.f, a1B = 0.f, a2B = 0.f;
+            float a0[R], a1[R], a2[R];
+#pragma unroll
+            for (int h = 0; h < R; h++) a0[h] = a1[h] = a2[h] = 0.f;
 #pragma unroll
             for (int dy = 0; dy < 3; dy++)
 #pragma unroll
                 for (int dx = 0; dx < 3; dx++) {
                     const int m = 3 * dy + dx;
-                    a0A = fmaf(w[m], rr[dy][dx], a0A);
-                    a1A = fmaf(w[9 + m], rr[dy][dx], a1A);
-                    a2A = fmaf(w[18 + m], rr[dy][dx], a2A);
-                    a0B = fmaf(w[m], rr[dy + 1][dx], a0B);
-                    a1B = fmaf(w[9 + m], rr[dy + 1][dx], a1B);
-                    a2B = fmaf(w[18 + m], rr[dy + 1][dx], a2B);
+                    // R = 2: weights in registers; R = 1: from shared memory (64 registers)
+                    const float w0 = R == 2 ? w[m] : S[m], w1 = R == 2 ? w[9 + m] : S[9 + m],
+                                w2 = R == 2 ? w[18 + m] : S[18 + m];
+#pragma unroll
+                    for (int h = 0; h < R; h++) {
+                        a0[h] = fmaf(w0, rr[dy + h][dx], a0[h]);
+                        a1[h] = fmaf(w1, rr[dy + h][dx], a1[h]);
+                        a2[h] = fmaf(w2, rr[dy + h][dx], a2[h]);
+                    }
                 }
             const int k = hz - 2;  // output plane z0 + k is complete after tile plane hz = k + 2
             if (k >= 0 && z0 + k < g.nk) {
                 // z0 is even: output plane k sits over coarse plane 1 + k/2, parity side k & 1
                 const int lz = 1 + (k >> 1), sz = (k & 1) ? 1 : -1;
 #pragma unroll
-                for (int h = 0; h < 2; h++) {
+                for (int h = 0; h < R; h++) {
                     const int ty = ty0 + h;
-                    if (!(h ? colB : colA)) continue;
+                    if (!colr[h]) continue;
                     const int n = x + (y0 + ty) * g.ni + (z0 + k) * g.ni * g.nj;
                     if (fm[b][k * kUp0Y + ty] >> tx & 1u) {
-                        float v = h ? PB + a2B : PA + a2A;
-                        if (cin.a) {
-                            const float* px = h ? pxB : pxA;
-                            v += 0.75f * px[lz] + 0.25f * px[lz + sz];
-                        }
+                        float v = Pr[h] + a2[h];
+                        if (cin.a) v += 0.75f * px[h][lz] + 0.25f * px[h][lz + sz];
                         z[n] = v;
                         f_zr += v * T[((k + 1) * kUp0HY + ty + 1) * kUp0P + kUp0O + tx + 1];
                         f_zq += v * qs[b][k][ty * kUp0X + tx];
@@ -728,10 +739,11 @@ __global__ void __launch_bounds__(kUp0Threads, kUp0CtasPerSM)
                     }
                 }
             }
-            PA = QA + a1A;
-            QA = a0A;
-            PB = QB + a1B;
-            QB = a0B;
+#pragma unroll
+            for (int h = 0; h < R; h++) {
+                Pr[h] = Qr[h] + a1[h];
+                Qr[h] = a0[h];
+            }
         }
     }
     if (out) {
@@ -1035,15 +1047,20 @@ static void launch_up0(const GridDev& g, LView r0, LView cin, float* z, const ui
     const long tiles = (long)bx_n * by_n * ((g.nk + kUp0Z - 1) / kUp0Z);
     const long ctas = std::min(tiles, (long)std::max(1, sms) * kUp0CtasPerSM);
     if (!out || ctas <= gstride) {
-        static int dyn_set = -1;  // the device whose attribute is set (one device per process here)
+        static int dyn_set = -1;  // the device whose attributes are set (one device per process here)
         int dev = 0;
         cudaGetDevice(&dev);
         if (dyn_set != dev) {
-            cudaFuncSetAttribute(k_lp_up0_pipe, cudaFuncAttributeMaxDynamicSharedMemorySize, kUp0DynSmem);
+            cudaFuncSetAttribute(k_lp_up0_pipe<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUp0DynSmem);
+            cudaFuncSetAttribute(k_lp_up0_pipe<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUp0DynSmem);
             dyn_set = dev;
         }
-        k_lp_up0_pipe<<<(unsigned)ctas, kUp0Threads, kUp0DynSmem, s>>>(g, r0, cin, z, kind, S0, q, gpart, gstride,
-                                                                          ticket, out, flag, bx_n, by_n, (int)tiles);
+        if (tiles >= 4 * (long)std::max(1, sms) * kUp0CtasPerSM)
+            k_lp_up0_pipe<2><<<(unsigned)ctas, kUp0X * kUp0Y / 2, kUp0DynSmem, s>>>(
+                g, r0, cin, z, kind, S0, q, gpart, gstride, ticket, out, flag, bx_n, by_n, (int)tiles);
+        else
+            k_lp_up0_pipe<1><<<(unsigned)ctas, kUp0X * kUp0Y, kUp0DynSmem, s>>>(
+                g, r0, cin, z, kind, S0, q, gpart, gstride, ticket, out, flag, bx_n, by_n, (int)tiles);
     } else {
         k_lp_up0<<<node_blocks(g.nv), kNodeThreads, 0, s>>>(g, r0, cin, z, kind, S0, q, gpart, gstride, ticket, out,
                                                             flag);
