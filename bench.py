@@ -923,17 +923,9 @@ def run_e2e(pic, wl, args, rank, weights=None, shapes=None):
         W.synchronize()
         t0 = time.perf_counter()
         marks = {}
-        for sp, (pos, vel, w) in ((e, he), (i, hi)):
-            t1 = time.perf_counter()
-            rc = L_.pic_species_add_particles(W.handle, sp.id, C.c_void_p(pos.data_ptr()), C.c_void_p(vel.data_ptr()),
-                                              C.c_void_p(w.data_ptr()), None, n, 1)
-            if rc:
-                raise RuntimeError("upload failed %d" % rc)
-            t2 = time.perf_counter()
-            sp.sortIndexes()  # cell order, as after a sort step of the loop
-            W.synchronize()
-            marks["upload_" + sp.name] = t2 - t1
-            marks["sort_" + sp.name] = time.perf_counter() - t2
+        # both species through the batch upload: read in place from the pinned arrays, each sorted
+        # into cell order (as after a sort step of the loop) while the next one uploads
+        W.add_particles_batch([e, i], [he[0], hi[0]], [he[1], hi[1]], [he[2], hi[2]], rewind=True, sort=True)
         W.synchronize()
         marks["upload_and_sort"] = time.perf_counter() - t0
         Sv.solve(raise_on_fail=True)

@@ -76,6 +76,7 @@ def library():
         "pic_world_set_field": [vp, i, vp],
         "pic_species_create": [vp, C.c_char_p, d, d, d, l, d, vp],
         "pic_species_add_particles": [vp, i, vp, vp, vp, vp, l, i],
+        "pic_species_add_particles_batch": [vp, i, vp, vp, vp, vp, vp, vp, i, i],
         "pic_species_load_uniform": [vp, i, vp, vp, l, d, d, d, u64],
         "pic_species_count": [vp, i, vp],
         "pic_species_load_box_thermal": [vp, i, vp, vp, d, d, u64],
@@ -310,6 +311,33 @@ class World:
         a, b, c = C.c_int(), C.c_int(), C.c_int()
         _check(self._L.pic_launch_shapes(self._h, C.byref(a), C.byref(b), C.byref(c)))
         return dict(push_ctas_per_sm=a.value, node_grid=b.value, cg_grid=c.value)
+
+    def add_particles_batch(self, species, pos, vel, w, ids=None, rewind=True, sort=True):
+        """Several species at once (pic_species_add_particles_batch): per species its (n, 3) positions
+        and velocities and (n,) weights in FP64, as numpy arrays or as tensors in pinned host or
+        device memory (objects with data_ptr(), read in place); with sort, each species leaves in
+        cell order, its sort overlapping the next species' upload."""
+        keep = []
+
+        def addr(a, shape, dtype=np.float64):
+            if a is None:
+                return None
+            if hasattr(a, "data_ptr"):
+                keep.append(a)
+                return a.data_ptr()
+            a = np.ascontiguousarray(a, dtype=dtype)
+            if shape is not None:
+                a = a.reshape(shape)
+            keep.append(a)
+            return a.ctypes.data
+
+        k = len(species)
+        sp = np.asarray([s.id for s in species], np.int32)
+        ns = np.asarray([len(x) for x in w], np.int64)
+        arr = lambda xs, shape: (C.c_void_p * k)(*[addr(x, shape) for x in xs])
+        idp = None if ids is None else (C.c_void_p * k)(*[addr(x, None, np.uint64) for x in ids])
+        _check(self._L.pic_species_add_particles_batch(self._h, k, _p(sp), arr(pos, (-1, 3)), arr(vel, (-1, 3)),
+                                                       arr(w, (-1,)), idp, _p(ns), int(rewind), int(sort)))
 
     def set_launch_shapes(self, push_ctas_per_sm=0, node_grid=0, cg_grid=0):
         """Use launch shapes tuned on an earlier world of the same size (0: built-in default)."""

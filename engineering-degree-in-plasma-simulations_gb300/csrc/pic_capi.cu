@@ -85,6 +85,7 @@ struct pic_world {
     int device = 0;
     int sms = 152;
     cudaStream_t stream = nullptr;
+    cudaStream_t upload_stream = nullptr;  // uploads of a batch (pic_species_add_particles_batch)
     GridDev g{};
     // node fields
     float4* ef = nullptr;
@@ -694,6 +695,7 @@ extern "C" int pic_world_destroy(pic_world* w) {
     }
     for (auto e : w->event_pool) cudaEventDestroy(e);
     if (w->stream) cudaStreamDestroy(w->stream);
+    if (w->upload_stream) cudaStreamDestroy(w->upload_stream);
     delete w;
     return PIC_OK;
 }
@@ -1016,6 +1018,69 @@ extern "C" int pic_species_add_particles(pic_world* w, int sp, const double* pos
 namespace {
 int sort_species(pic_world* w, int sp);
 }  // namespace
+
+// Several species at once: every upload runs on a side stream, and a species is sorted on the
+// world's stream as soon as its upload is done, so a species' sort (HBM) overlaps the next
+// species' upload (host link).  Arrays that the device cannot read in place (pageable memory)
+// take the one-species path in turn.
+extern "C" int pic_species_add_particles_batch(pic_world* w, int count, const int* sps, const double* const* pos,
+                                               const double* const* vel, const double* const* wgt,
+                                               const uint64_t* const* ids, const long* n, int rewind, int sort) {
+    if (!w || count < 0 || (count > 0 && (!sps || !pos || !vel || !wgt || !n)))
+        return fail(PIC_ERR_ARG, "bad arguments");
+    CU(cudaSetDevice(w->device));
+    bool inplace = true;
+    for (int k = 0; k < count; k++) {
+        if (!valid_sp(w, sps[k]) || n[k] < 0 || (n[k] > 0 && (!pos[k] || !vel[k] || !wgt[k])))
+            return fail(PIC_ERR_ARG, "bad species or arrays at batch entry %d", k);
+        for (int j = 0; j < k; j++)
+            if (sps[j] == sps[k]) return fail(PIC_ERR_ARG, "species %d appears twice in the batch", sps[k]);
+        const uint64_t* idk = ids ? ids[k] : nullptr;
+        if (n[k] > 0 && (!device_view(w, pos[k]) || !device_view(w, vel[k]) || !device_view(w, wgt[k]) ||
+                         (idk && !device_view(w, idk))))
+            inplace = false;
+    }
+    if (!inplace) {
+        for (int k = 0; k < count; k++) {
+            int rc = pic_species_add_particles(w, sps[k], pos[k], vel[k], wgt[k], ids ? ids[k] : nullptr, n[k], rewind);
+            if (rc) return rc;
+            if (sort) sort_species(w, sps[k]);
+        }
+        CU(cudaStreamSynchronize(w->stream));
+        return check_device_error(w);
+    }
+    if (!w->upload_stream) CU(cudaStreamCreateWithFlags(&w->upload_stream, cudaStreamNonBlocking));
+    std::vector<cudaEvent_t> ev(count + 1, nullptr);
+    for (auto& e : ev) CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    // the uploads start after the world's pending work
+    CU(cudaEventRecord(ev[count], w->stream));
+    CU(cudaStreamWaitEvent(w->upload_stream, ev[count], 0));
+    for (int k = 0; k < count; k++) {
+        SpeciesHost& s = w->sp[sps[k]];
+        const double* dp = static_cast<const double*>(device_view(w, pos[k]));
+        const double* dv = static_cast<const double*>(device_view(w, vel[k]));
+        const double* dw = static_cast<const double*>(device_view(w, wgt[k]));
+        const uint64_t* idk = ids ? ids[k] : nullptr;
+        const auto* di = static_cast<const unsigned long long*>(idk ? device_view(w, idk) : nullptr);
+        const unsigned long long id0 = s.next_id;
+        const long step = 1l << 30;
+        for (long a = 0; a < n[k]; a += step) {
+            const long m = std::min<long>(step, n[k] - a);
+            // two CTAs per SM keep the host link busy and leave the SMs to the previous species' sort
+            launch_from_abs(w->g, s.dev, dp + 3 * a, dv + 3 * a, dw + a, di ? di + a : nullptr,
+                            id0 + (unsigned long long)a, (int)m, rewind, (float)(s.charge / s.mass * 0.5 * w->dt),
+                            w->ef, w->upload_stream, 2 * w->sms);
+        }
+        if (!idk) s.next_id += n[k];
+        CU(cudaEventRecord(ev[k], w->upload_stream));
+        CU(cudaStreamWaitEvent(w->stream, ev[k], 0));
+        if (sort) sort_species(w, sps[k]);  // on the world's stream, beside the next upload
+    }
+    CU(cudaStreamSynchronize(w->stream));  // it waited for every upload
+    for (auto e : ev) cudaEventDestroy(e);
+    CU(cudaGetLastError());
+    return check_device_error(w);
+}
 
 extern "C" int pic_species_load_uniform(pic_world* w, int sp, const double* lo, const double* hi, long n, double T,
                                         double w_mean, double w_sigma, uint64_t seed) {

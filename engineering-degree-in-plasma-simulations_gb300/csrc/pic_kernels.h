@@ -63,7 +63,8 @@ void launch_sort(const GridDev& g, SpeciesDev sp, float4* pos_alt, float4* vel_a
                  int* cell_count, int* cell_start, int* scan_aux, cudaStream_t s, int grid);
 void launch_from_abs(const GridDev& g, SpeciesDev sp, const double* pos, const double* vel, const double* w,
                      const unsigned long long* id, unsigned long long id0, int n, int rewind, float qm_half_dt,
-                     const float4* ef, cudaStream_t s);
+                     const float4* ef, cudaStream_t s,
+                     int max_grid = 4096);
 // particles first + p * stride, p < n, to absolute FP64 positions (null outputs are skipped)
 void launch_to_abs(const GridDev& g, SpeciesDev sp, double* pos, double* vel, double* w, unsigned long long* id,
                    int n, cudaStream_t s, long long first = 0, long long stride = 1);

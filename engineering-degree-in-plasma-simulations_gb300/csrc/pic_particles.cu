@@ -987,9 +987,9 @@ __global__ void k_from_abs_count(SpeciesDev sp, int n, unsigned* err) {
 }
 void launch_from_abs(const GridDev& g, SpeciesDev sp, const double* pos, const double* vel, const double* w,
                      const unsigned long long* id, unsigned long long id0, int n, int rewind, float qm_half_dt,
-                     const float4* ef, cudaStream_t s) {
+                     const float4* ef, cudaStream_t s, int max_grid) {
     int grid = (n + 255) / 256;
-    if (grid > 4096) grid = 4096;
+    if (grid > max_grid) grid = max_grid;
     if (grid < 1) grid = 1;
     k_from_abs<<<grid, 256, 0, s>>>(g, sp, pos, vel, w, id, id0, n, rewind, qm_half_dt, ef);
     k_from_abs_count<<<1, 1, 0, s>>>(sp, n, nullptr);

@@ -84,6 +84,15 @@ int pic_species_create(pic_world* w, const char* name, double mass, double charg
  * a device staging buffer. */
 int pic_species_add_particles(pic_world* w, int sp, const double* pos, const double* vel, const double* wgt,
                               const uint64_t* ids, long n, int rewind);
+/* Several species at once (no reference counterpart; the reference adds particles species by
+ * species): entry k adds n[k] particles to species sps[k] as pic_species_add_particles does
+ * (ids may be NULL, or hold NULL entries), and with sort = 1 sorts each species into cell order
+ * (pic_species_sort) as soon as its upload is done.  When every array is device-readable in place
+ * (pinned host or device memory), the uploads run on a side stream, so one species' sort overlaps
+ * the next species' upload.  A species may appear once. */
+int pic_species_add_particles_batch(pic_world* w, int count, const int* sps, const double* const* pos,
+                                    const double* const* vel, const double* const* wgt, const uint64_t* const* ids,
+                                    const long* n, int rewind, int sort);
 /* Synthetic loader (GPU form of Species::loadParticleBoxThermal, Species.cpp:564-599): n
  * particles uniform in [lo, hi), Maxwellian at T [K], lognormal weights of mean w_mean and
  * log-sigma w_sigma (0: all w_mean), Philox stream keyed by seed. */
