@@ -159,7 +159,7 @@ struct pic_world {
     int stop_rule = PIC_STOP_REL_RHS;
     int warm_mode = PIC_WARM_PREVIOUS;  // start of a warm solve (PIC_WARM_*)
     int warm_jacobi = 16;  // Jacobi-PCG iterations a warm solve of the learned method runs first
-    int lp_hint = 0;       // iterations of the last converged first learned inner solve (0: none)
+    int lp_hint = 0;       // iterations of the last warm solve's converged first learned inner solve (0: none)
     float* dphi = nullptr;  // the last solve's total change of phi (FP32), for PIC_WARM_EXTRAPOLATE
     bool dphi_valid = false;  // dphi holds the change of one warm solve
     double last_norms[3] = {0, 0, 0};  // |r|, |b|, |rho/eps0| of the last solve's final residual
@@ -1768,13 +1768,14 @@ int solve_impl(pic_world* w, int* iters_out, double* rel_out) {
             double target = std::max(1e-6 * r2, kInnerTarget * w->tol * w->tol * bn * bn);
             int done = 0;
             bool conv = false;
-            // the first inner solve of a solve sized from the last one: consecutive warm solves of a
-            // run need about the same count N, and iteration N is the one that finds the first N
-            // converged, so the first batch runs N + 1 iterations
-            const int first_batch = first_learned && w->lp_hint > 0 ? w->lp_hint + 1 : 4;
+            // the first inner solve of a warm solve sized from the last warm one: consecutive warm
+            // solves of a run need about the same count N, and iteration N is the one that finds the
+            // first N converged, so the first batch runs N + 1 iterations (a cold solve, which needs
+            // several times more, neither uses nor sets the count)
+            const int first_batch = warm && first_learned && w->lp_hint > 0 ? w->lp_hint + 1 : 4;
             rc = learned_inner(w, sw, target, std::min(kLearnedInnerCap, w->max_it - iters), first_batch, &done, &conv);
             if (rc) return rc;
-            if (first_learned && conv) w->lp_hint = done;
+            if (warm && first_learned && conv) w->lp_hint = done;
             first_learned = false;
             iters += done;
             if (!conv) {
