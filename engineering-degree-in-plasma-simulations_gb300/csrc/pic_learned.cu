@@ -913,8 +913,13 @@ __global__ void __launch_bounds__(32 * kRmWarps, 4) k_lp_restrict_march(LView f,
     const int cx0 = bx * kRmX, cy0 = by * kRmY, cz0 = bz * kRmZ;
     const int fx = 2 * (cx0 + lane);  // this lane's even fine x
     const int body_end = 2 * cx0 + 2 * kRmX;
-    const bool fast = body_end <= f.n[0] && (!f.per[0] || body_end <= 2 * c.n[0]) && ((f.sy | f.sz) & 1) == 0 &&
+    // the body may reach one point past the view when the row's storage holds it (a periodic node
+    // array keeps its alias node there); the index rules give that point zero (no wrap below the
+    // coarse period 2 c.n), so its value is read and replaced by zero
+    const bool fast = (body_end <= f.n[0] || (body_end == f.n[0] + 1 && f.sy >= body_end)) &&
+                      (!f.per[0] || body_end <= 2 * c.n[0]) && ((f.sy | f.sz) & 1) == 0 &&
                       (reinterpret_cast<uintptr_t>(f.a) & 7) == 0;
+    const bool hi_out = fx + 1 >= f.n[0];  // fast path: this lane's odd point is past the view
     // fast: xo[0] is the halo of lane 0 or 31 (-1: none); otherwise the four mapped fine x
     int xo[4];
     if (fast) {
@@ -953,6 +958,7 @@ __global__ void __launch_bounds__(32 * kRmWarps, 4) k_lp_restrict_march(LView f,
 #pragma unroll
             for (int r = 0; r < kRmHY; r++) {
                 pv[r] = *reinterpret_cast<const float2*>(plane + oy[r] + fx);
+                if (hi_out) pv[r].y = 0.f;
                 ph[r] = xo[0] >= 0 ? plane[oy[r] + xo[0]] : 0.f;
             }
 #pragma unroll
