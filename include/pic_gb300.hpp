@@ -114,6 +114,16 @@ public:
     std::vector<double> node_type() const { return field(4, 1); }  // World.h:17: REGULAR, NEUMANN, DIRICHLET
     std::vector<double> object_id() const { return field(5, 1); }
     void setPhi(const std::vector<double>& v) { check(pic_world_set_field(h_, 0, v.data())); }
+    // launch shapes (no reference counterpart): measured on this world's data (pic_autotune), read,
+    // or carried over from an earlier world of the same size; {push CTAs per SM, node-kernel CTAs,
+    // CG-stencil CTAs}, 0 = built-in default
+    void autotune() { check(pic_autotune(h_, nullptr, nullptr)); }
+    std::array<int, 3> launchShapes() const {
+        std::array<int, 3> s{};
+        check(pic_launch_shapes(h_, &s[0], &s[1], &s[2]));
+        return s;
+    }
+    void setLaunchShapes(const std::array<int, 3>& s) { check(pic_set_launch_shapes(h_, s[0], s[1], s[2])); }
     void computeChargeDensity() { check(pic_charge_density(h_)); }  // World.cpp:193-200
     template <class V>
     void computeChargeDensity(V&) {
@@ -283,6 +293,33 @@ namespace detail {
 inline Species& sp_ref(Species& s) { return s; }
 inline Species& sp_ref(Species* s) { return *s; }
 }  // namespace detail
+
+// One species' particles for addParticlesBatch: n positions and velocities (x, y, z each) and
+// weights in FP64; pinned host or device memory is read in place.
+struct ParticleArrays {
+    const double* pos;
+    const double* vel;
+    const double* w;
+    long n;
+};
+// Several species at once, each sorted into cell order as soon as its upload is done, its sort
+// beside the next species' upload (no reference counterpart: pic_species_add_particles_batch)
+inline void addParticlesBatch(World& world, const std::vector<Species*>& species,
+                              const std::vector<ParticleArrays>& arrays, bool rewind = true, bool sort = true) {
+    if (species.size() != arrays.size()) throw std::invalid_argument("addParticlesBatch: one array set per species");
+    std::vector<int> ids;
+    std::vector<const double*> pos, vel, w;
+    std::vector<long> n;
+    for (size_t k = 0; k < species.size(); k++) {
+        ids.push_back(species[k]->id());
+        pos.push_back(arrays[k].pos);
+        vel.push_back(arrays[k].vel);
+        w.push_back(arrays[k].w);
+        n.push_back(arrays[k].n);
+    }
+    check(pic_species_add_particles_batch(world.handle(), (int)ids.size(), ids.data(), pos.data(), vel.data(),
+                                          w.data(), nullptr, n.data(), rewind ? 1 : 0, sort ? 1 : 0));
+}
 
 template <class V>
 bool World::steadyState(V& species) {

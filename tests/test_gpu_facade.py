@@ -85,3 +85,50 @@ def test_cpp_facade_dsmc_and_objects(pic, tmp_path):
     assert f["threw"] == "1" and f["last"] == "0"
     assert int(f["self"]) > 1000 and int(f["pair"]) > 1000 and 1e-17 < float(f["svmax"]) < 1e-14
     assert int(f["o_hits"]) > 100 and int(f["o_bounces"]) >= int(f["o_hits"]) and int(f["i_hits"]) > 100
+
+
+BATCH = r"""
+#include <cstdio>
+#include <vector>
+#include "pic_gb300.hpp"
+using namespace pic_gb300;
+int main() {
+    const double m_e = 9.10938215e-31, q_e = 1.602176565e-19;
+    World world(17, 17, 17, {0.0, 0.0, 0.0}, {0.01, 0.01, 0.01});
+    world.setTime(1e-11, 10);
+    Species a("a", m_e, -q_e, world, 1.0, 20000), b("b", 40 * m_e, -q_e, world, 1.0, 20000);
+    std::vector<double> pa, va, wa, pb, vb, wb;
+    for (int k = 0; k < 9000; k++) {
+        const double u = (k % 97) / 97.0, v = (k % 89) / 89.0, s = (k % 83) / 83.0;
+        for (double x : {0.01 * u * 0.999, 0.01 * v * 0.999, 0.01 * s * 0.999}) pa.push_back(x);
+        for (double x : {1e5 * (u - 0.5), 1e5 * (v - 0.5), 1e5 * (s - 0.5)}) va.push_back(x);
+        wa.push_back(1.0 + u);
+        if (k < 5000) {
+            for (double x : {0.01 * s * 0.999, 0.01 * u * 0.999, 0.01 * v * 0.999}) pb.push_back(x);
+            for (double x : {1e4 * (s - 0.5), 1e4 * (u - 0.5), 1e4 * (v - 0.5)}) vb.push_back(x);
+            wb.push_back(2.0 - v);
+        }
+    }
+    addParticlesBatch(world, {&a, &b}, {{pa.data(), va.data(), wa.data(), (long)wa.size()},
+                                        {pb.data(), vb.data(), wb.data(), (long)wb.size()}});
+    world.setLaunchShapes({2, 456, 608});
+    const auto s = world.launchShapes();
+    std::printf("a=%zu b=%zu shapes=%d,%d,%d\n", a.getNumParticles(), b.getNumParticles(), s[0], s[1], s[2]);
+    return 0;
+}
+"""
+
+
+def test_cpp_facade_batch_upload_and_launch_shapes(pic, tmp_path):
+    pic.library()
+    pkg = os.path.join(ROOT, PKG_NAME)
+    src = tmp_path / "batch.cpp"
+    src.write_text(BATCH)
+    exe = str(tmp_path / "batch")
+    r = subprocess.run(["g++", "-std=c++17", "-O2", str(src), "-I", os.path.join(ROOT, "include"), "-L",
+                        os.path.join(pkg, "lib"), "-lpic_gb300", "-Wl,-rpath," + os.path.join(pkg, "lib"), "-o", exe],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.strip() == "a=9000 b=5000 shapes=2,456,608"
