@@ -1231,6 +1231,95 @@ void launch_lp_fold(const LpState& L, cudaStream_t s) {
 //   B    : z = B r ; partials z.r, z.q            (beta = z.(r_new - r_old) / rz_prev)
 // scal[0..1] rz and scal[2..3] alpha, double-buffered by iteration parity
 // =====================================================================================
+// d' = z + beta d and q = L d' for the four nodes n0 .. n0 + 3 of a row, from d' at the row (C), at
+// its neighbour rows (N: -y, +y, -z, +z), at its x ends (xm, xp) and the node kinds: writes d' and
+// q there and adds d'.q to acc (the rules of spmv_group: non-FREE nodes give zero, a flagged
+// neighbour is left out of the stencil, on a periodic row node ni-2 takes node 0 as +x neighbour)
+__device__ __forceinline__ void cg_row4(const float (&c3)[3], int n0, bool xend, bool wrapx, const float (&C)[4],
+                                        const float (&N)[4][4], float xm, float xp, ushort4 k4,
+                                        float* __restrict__ d_out, float* __restrict__ q, float& acc) {
+    const unsigned short kv[4] = {k4.x, k4.y, k4.z, k4.w};
+    float dvo[4], qv[4];
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        dvo[c] = 0.f;
+        qv[c] = 0.f;
+        if ((kv[c] & 3) != kFree) continue;
+        const float right = c == 3 ? xp : ((c == 2 && xend && wrapx) ? xp : C[c + 1]);
+        const float nb[6] = {c == 0 ? xm : C[c - 1], right, N[0][c], N[1][c], N[2][c], N[3][c]};
+        float dg = 0.f, o = 0.f;
+#pragma unroll
+        for (int d = 0; d < 6; d++) {
+            if (kv[c] & (1u << (2 + d))) continue;
+            dg += c3[d >> 1];
+            o += c3[d >> 1] * nb[d];
+        }
+        dvo[c] = C[c];
+        qv[c] = dg * C[c] - o;
+        acc += dvo[c] * qv[c];
+    }
+    *reinterpret_cast<float4*>(d_out + n0) = make_float4(dvo[0], dvo[1], dvo[2], dvo[3]);
+    *reinterpret_cast<float4*>(q + n0) = make_float4(qv[0], qv[1], qv[2], qv[3]);
+}
+// The same for rows j0 and j0 + 1 of a plane at once (rows a multiple of four nodes, the two rows
+// adjacent without a periodic seam between them): the centre rows are each other's y neighbours,
+// so the pair reads eight rows of z and d instead of ten, all issued before any is used.
+__device__ __forceinline__ void cg_pair(const GridDev& g, int i0, int j0, int k, const float* __restrict__ z,
+                                        const float* __restrict__ d_in, float* __restrict__ d_out,
+                                        float* __restrict__ q, const uint16_t* __restrict__ kind, float fb,
+                                        float& acc) {
+    const float c3[3] = {g.inv_dx[0] * g.inv_dx[0], g.inv_dx[1] * g.inv_dx[1], g.inv_dx[2] * g.inv_dx[2]};
+    const int j1 = j0 + 1;
+    const int jm = g.periodic[1] ? wrap_m(j0, g.nj, 1) : max(j0 - 1, 0);
+    const int jq = g.periodic[1] ? wrap_p(j1, g.nj, 1) : min(j1 + 1, g.nj - 1);
+    const int km = g.periodic[2] ? wrap_m(k, g.nk, 1) : max(k - 1, 0);
+    const int kp = g.periodic[2] ? wrap_p(k, g.nk, 1) : min(k + 1, g.nk - 1);
+    const int na = (k * g.nj + j0) * g.ni + i0, nb = na + g.ni;
+    const int off[8] = {(k * g.nj + jm) * g.ni + i0, na, nb, (k * g.nj + jq) * g.ni + i0,
+                        (km * g.nj + j0) * g.ni + i0, (kp * g.nj + j0) * g.ni + i0,
+                        (km * g.nj + j1) * g.ni + i0, (kp * g.nj + j1) * g.ni + i0};
+    float4 zr[8], dr[8];
+#pragma unroll
+    for (int m = 0; m < 8; m++) {
+        zr[m] = *reinterpret_cast<const float4*>(z + off[m]);
+        dr[m] = *reinterpret_cast<const float4*>(d_in + off[m]);
+    }
+    const bool xend = i0 + 4 == g.ni, wrapx = g.periodic[0] != 0;
+    float xe[4];  // x ends: row a -x, +x, row b -x, +x
+#pragma unroll
+    for (int r = 0; r < 2; r++) {
+        const int n0 = r ? nb : na;
+        const int ixm = i0 > 0 ? n0 - 1 : (wrapx ? n0 + g.ni - 2 : n0);
+        const int ixp = xend ? (wrapx ? n0 - i0 : n0 + 3) : n0 + 4;
+        xe[2 * r] = z[ixm] + fb * d_in[ixm];
+        xe[2 * r + 1] = z[ixp] + fb * d_in[ixp];
+    }
+    const ushort4 ka = *reinterpret_cast<const ushort4*>(kind + na);
+    const ushort4 kb = *reinterpret_cast<const ushort4*>(kind + nb);
+    float v[8][4];
+#pragma unroll
+    for (int m = 0; m < 8; m++) {
+        v[m][0] = zr[m].x + fb * dr[m].x;
+        v[m][1] = zr[m].y + fb * dr[m].y;
+        v[m][2] = zr[m].z + fb * dr[m].z;
+        v[m][3] = zr[m].w + fb * dr[m].w;
+    }
+    float Na[4][4], Nb[4][4];
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        Na[0][c] = v[0][c];  // row a: -y jm, +y row b, -z, +z
+        Na[1][c] = v[2][c];
+        Na[2][c] = v[4][c];
+        Na[3][c] = v[5][c];
+        Nb[0][c] = v[1][c];  // row b: -y row a, +y jq, -z, +z
+        Nb[1][c] = v[3][c];
+        Nb[2][c] = v[6][c];
+        Nb[3][c] = v[7][c];
+    }
+    cg_row4(c3, na, xend, wrapx, v[1], Na, xe[0], xe[1], ka, d_out, q, acc);
+    cg_row4(c3, nb, xend, wrapx, v[2], Nb, xe[2], xe[3], kb, d_out, q, acc);
+}
+
 __global__ void __launch_bounds__(256) k_lpcg_k1(GridDev g, const float* __restrict__ z,
                                                           const float* __restrict__ d_in, float* __restrict__ d_out,
                                                           float* __restrict__ q, const uint16_t* __restrict__ kind,
@@ -1265,9 +1354,29 @@ __global__ void __launch_bounds__(256) k_lpcg_k1(GridDev g, const float* __restr
     if (s_stop) return;
     float facc = 0.f;
     const float fb = s_beta;
-    const int ngroups = (g.nv + 3) >> 2;
-    for (int qg = blockIdx.x * blockDim.x + threadIdx.x; qg < ngroups; qg += gridDim.x * blockDim.x)
-        spmv_group(g, qg << 2, z, d_in, d_out, q, kind, fb, facc);
+    if ((g.ni & 3) == 0) {
+        // pairs of rows (j0 even, j0 + 1) of a plane; an odd last row, or a pair across the seam
+        // of a periodic y axis (the +y neighbour of j0 is not j0 + 1), goes row by row
+        const int gpr = g.ni >> 2, npair = (g.nj + 1) >> 1;
+        const int total = gpr * npair * g.nk;
+        for (int pg = blockIdx.x * blockDim.x + threadIdx.x; pg < total; pg += gridDim.x * blockDim.x) {
+            const int gx = pg % gpr, t = pg / gpr;
+            const int j0 = 2 * (t % npair), k = t / npair;
+            const int i0 = 4 * gx;
+            const int n0 = (k * g.nj + j0) * g.ni + i0;
+            const bool pair = j0 + 1 < g.nj && (g.periodic[1] ? wrap_p(j0, g.nj, 1) : j0 + 1) == j0 + 1;
+            if (pair) {
+                cg_pair(g, i0, j0, k, z, d_in, d_out, q, kind, fb, facc);
+            } else {
+                spmv_group(g, n0, z, d_in, d_out, q, kind, fb, facc);
+                if (j0 + 1 < g.nj) spmv_group(g, n0 + g.ni, z, d_in, d_out, q, kind, fb, facc);
+            }
+        }
+    } else {
+        const int ngroups = (g.nv + 3) >> 2;
+        for (int qg = blockIdx.x * blockDim.x + threadIdx.x; qg < ngroups; qg += gridDim.x * blockDim.x)
+            spmv_group(g, qg << 2, z, d_in, d_out, q, kind, fb, facc);
+    }
     const float v[1] = {facc};
     grid_sum<1>(v, gpart, gstride, ticket, scal + kS_DQ);
 }
